@@ -1,0 +1,377 @@
+#!/usr/bin/env python
+"""Irving-Kirkwood stress-field throughput on GB300 (frames/s).
+
+Workload (default ``ik2d_n64k_g256_gauss``): 64 seeded 2D polydisperse12 frames,
+N = 64,000 particles (L = 253), a 256 x 256 lattice grid, Gaussian coarse-graining
+kernel of width 2 truncated at 3 widths, Gauss-Legendre-5 bond integrals, virial +
+kinetic stress.  One step = one pass of the tuned FP32 path over the 64 frames.
+
+  value        frames/s with the frames resident in HBM (cycled: 64 x 4 MB of
+               inputs > L2), CUDA events on the engine's stream, max over ranks;
+  e2e          frames/s through the C ABI with host buffers: pinned host->device
+               upload of every frame and device->host read of both fields each step;
+  plain_fp64   frames/s of the plain FP64 GPU kernels (same workload), and the
+               tuned path's relative L2 error against them;
+  roofline     the FP32 gather kernel: algorithmic FLOPs (66 per active (grid, i, j)
+               triple, the GL-5-equivalent bond integral + 2D stress accumulation)
+               per launch / its CUDA-event duration, against the FP32 FMA peak
+               measured live on this GPU;
+  cpu_baseline the FP64 oracle (restatement of IrvingKirkwood::compute) on the host
+               cores on a bounded sample of frame 0.
+
+``--impl reference`` times that CPU restatement of the reference's path alone.
+``--gpus N`` under torchrun runs N independent replicas (the path is not sharded).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "IK stress frames/s, 2D N=64k 256² grid: tuned vs plain FP64 GPU @≤1e-5 rel"
+
+WORKLOADS = {
+    "ik2d_n64k_g256_gauss": dict(N=64000, dim=2, nmax=256, frames=64, cg=dict(kind="gaussian", rcut=6.0, width=2.0),
+                                 desc="Gaussian w=2 cut at 3w (R=6), GL-5"),
+    "ik2d_n2k_g64_octic": dict(N=2000, dim=2, nmax=64, frames=64, cg=dict(kind="octic", rcut=2.0, width=0.0),
+                               desc="octic R=2, GL-5"),
+    "ik3d_n32k_g64_octic": dict(N=32000, dim=3, nmax=64, frames=16, cg=dict(kind="octic", rcut=2.0, width=0.0),
+                                desc="octic R=2, GL-5"),
+}
+FLOP_PER_TRIPLE = {2: 66, 3: 82}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="ik2d_n64k_g256_gauss", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def make_frames(wl, rank):
+    from pyglasstools_gb300 import synth
+    frames = [synth.make_frame(wl["N"], dim=wl["dim"], seed=10007 * rank + k) for k in range(wl["frames"])]
+    grid = synth.lattice_grid(frames[0].L, wl["nmax"], wl["dim"])
+    return frames, grid
+
+
+def config_of(name, wl, world):
+    return {"workload": name, "N": wl["N"], "dim": wl["dim"],
+            "grid": "x".join([str(wl["nmax"])] * wl["dim"]), "cgfunc": wl["desc"],
+            "potential": "polydisperse12 v0=1 eps=0.2 rcut=1.25", "frames_per_step": wl["frames"],
+            "l2": "inputs larger than L2: %d resident frames cycled each step" % wl["frames"],
+            "parallelism": "replicas x%d (no sharding)" % world}
+
+
+# ---------------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append((time.perf_counter(), parts))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self, t0, t1):
+        sel = [p for (t, p) in self.samples if t0 <= t <= t1] or [p for (_, p) in self.samples]
+        if not sel:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(p[1]) for p in sel if num(p[1]) is not None]
+        mx = [num(p[2]) for p in sel if num(p[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for p in sel for k in range(4) if p[5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sel)}
+
+
+# ---------------------------------------------------------------------------- dist helpers
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------- CPU baseline
+def cpu_sample(wl, frames, grid, g1, nthreads):
+    from oracle import oracle as O
+    f = frames[0]
+    box = O.make_box(wl["dim"], [f.L, f.L, f.L if wl["dim"] == 3 else 1.0])
+    pot = O.make_poly12()
+    cg = O.make_cg(wl["cg"]["kind"], rcut=wl["cg"]["rcut"], mode="fixedpoint", order=5, width=wl["cg"]["width"])
+    t = time.perf_counter()
+    O.compute(box, f.pos, f.diam, pot, cg, grid, vel=f.vel, mass=f.mass, g0=0, g1=g1, nthreads=nthreads)
+    return time.perf_counter() - t
+
+
+def reference_arm(args, wl, name):
+    world, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    frames, grid = make_frames(dict(wl, frames=1), 0)
+    cores = os.cpu_count() or 1
+    G = len(grid)
+    g1 = max(256, G // 32)  # a bounded slice of frame 0's grid per step
+    for _ in range(args.warmup):
+        cpu_sample(wl, frames, grid, g1, cores)
+    t = 0.0
+    for _ in range(args.steps):
+        t += cpu_sample(wl, frames, grid, g1, cores)
+    frac = g1 / G
+    value = frac * args.steps / t
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_of(name, wl, world),
+            "cpu_baseline": {"value": value, "unit": "frames/s", "cores": cores, "kind": "port",
+                             "sample": f"grid points [0, {g1}) of frame 0 ({frac:.4f} of a frame) per step, "
+                                       f"FP64 oracle restating IrvingKirkwood::compute, OpenMP {cores} threads"},
+            "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------- our arm
+def ours(args, wl, name):
+    import torch
+    from pyglasstools_gb300 import ikabi
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    frames, grid = make_frames(wl, rank)
+    F, D = wl["frames"], wl["dim"]
+    NC = 3 if D == 2 else 6
+    L = frames[0].L
+    ctx = ikabi.IKContext(local)
+    ctx.set_box(D, [L, L, L if D == 3 else 1.0])
+    ctx.set_poly12()
+    ctx.set_cgfunc(wl["cg"]["kind"], wl["cg"]["rcut"], order=5, width=wl["cg"]["width"])
+    ctx.set_grid(grid)
+    ctx.reserve_slots(F)
+    for k, f in enumerate(frames):
+        ctx.upload_frame(k, f.pos, f.diam, f.vel, f.mass)
+        ctx.synchronize()
+    stream = torch.cuda.ExternalStream(ctx.stream())
+
+    def step(prec="fp32", nfr=F):
+        for k in range(nfr):
+            ctx.compute_slot(k, prec)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    # ---- warm-up (also a soak so that the clock sampler sees the GPU under load)
+    t_soak = time.perf_counter()
+    for _ in range(max(args.warmup, 3)):
+        step()
+    ctx.synchronize()
+    while time.perf_counter() - t_soak < 1.5:
+        step()
+        ctx.synchronize()
+    # ---- timed region (device-resident inputs)
+    barrier(world)
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    launches0 = ctx.launch_count()
+    t_host0 = time.perf_counter()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    t_host1 = time.perf_counter()
+    launches = ctx.launch_count() - launches0
+    ms = ev0.elapsed_time(ev1)
+    barrier(world)
+    ms_max = max_over_ranks(ms, world)
+    value = world * F * args.steps / (ms_max * 1e-3)
+
+    # ---- end to end through the C ABI with host buffers
+    pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    hpos = [pin((wl["N"], 3)) for _ in range(F)]
+    hvel = [pin((wl["N"], 3)) for _ in range(F)]
+    hmass = [pin((wl["N"],)) for _ in range(F)]
+    hdiam = [pin((wl["N"],)) for _ in range(F)]
+    for k, f in enumerate(frames):
+        hpos[k][:] = f.pos
+        hvel[k][:] = f.vel
+        hmass[k][:] = f.mass
+        hdiam[k][:] = f.diam
+    hvir = [pin((len(grid), NC)) for _ in range(F)]
+    hkin = [pin((len(grid), NC)) for _ in range(F)]
+
+    def e2e_step():
+        for k in range(F):
+            ctx.upload_frame(k, hpos[k], hdiam[k], hvel[k], hmass[k])
+            ctx.compute_slot(k, "fp32")
+            ctx.download_field_async(hvir[k], ikabi.FIELD_VIRIAL, k)
+            ctx.download_field_async(hkin[k], ikabi.FIELD_KINETIC, k)
+        ctx.synchronize()
+
+    e2e_step()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    t1 = time.perf_counter()
+    e2e_s = max_over_ranks(t1 - t0, world)
+    e2e_value = world * F * args.steps / e2e_s
+    h2d = F * wl["N"] * (3 + 3 + 1 + 1) * 8
+    d2h = F * len(grid) * NC * 2 * 8
+    clocks.stop()
+
+    # ---- plain FP64 GPU path on the same frames + error of the tuned path vs it
+    nplain = min(F, 4)
+    step("fp64", nplain)  # warm
+    ctx.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    step("fp64", nplain)
+    e1.record(stream)
+    ctx.synchronize()
+    plain_value = nplain / (e0.elapsed_time(e1) * 1e-3)
+    v64 = ctx.get_field(ikabi.FIELD_VIRIAL, slot=0)
+    k64 = ctx.get_field(ikabi.FIELD_KINETIC, slot=0)
+    ctx.compute_slot(0, "fp32")
+    ctx.synchronize()
+    v32 = ctx.get_field(ikabi.FIELD_VIRIAL, slot=0)
+    k32 = ctx.get_field(ikabi.FIELD_KINETIC, slot=0)
+
+    def relerr(a, b):
+        iu = [(0, 0), (1, 1), (0, 1)] if D == 2 else [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]
+        return [float(np.linalg.norm(a[:, i, j] - b[:, i, j]) / np.linalg.norm(b[:, i, j])) for i, j in iu]
+
+    err_v, err_k = relerr(v32, v64), relerr(k32, k64)
+
+    # ---- roofline of the gather kernel (per-launch CUDA events around it)
+    ctx.set_flags(ikabi.FLAG_TIMING)
+    gms, trip = [], []
+    for k in range(F):
+        ctx.compute_slot(k, "fp32")
+        ctx.synchronize()
+        gms.append(ctx.timing()[2])
+        trip.append(ctx.counters(k)[2])
+    ctx.set_flags(0)
+    g_ms = float(np.mean(gms))
+    A = float(np.mean(trip))
+    flop = FLOP_PER_TRIPLE[D] * A
+    achieved = flop / (g_ms * 1e-3) / 1e12
+    peak = ikabi.measure_fp32_peak(local)
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
+    if os.path.exists(tf):
+        for ln in open(tf):
+            parts = ln.split()
+            if len(parts) >= 3 and parts[0] == "k_gather32" and parts[1] == name:
+                traffic = float(parts[2])
+
+    out = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, shapes of the named config)",
+           "config": config_of(name, wl, world),
+           "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+           "gpu_launches": int(launches),
+           "clocks": clocks.summary(t_soak, t_host1),
+           "roofline": {"bound": "fp32", "kernel": "k_gather32", "achieved": achieved, "peak": peak,
+                        "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+                        "flop_per_launch": flop, "active_triples_per_launch": A, "launch_ms": g_ms,
+                        "peak_source": "measured live: FFMA throughput probe (ik_measure_fp32_peak)"},
+           "plain_fp64": {"value": plain_value, "unit": "frames/s", "frames_timed": nplain},
+           "tuned_over_plain": value / plain_value,
+           "rel_err_vs_fp64": {"virial": err_v, "kinetic": err_k},
+           "interactions_per_s": A * value}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        G = len(grid)
+        g1 = max(256, G // 8)
+        t = cpu_sample(wl, frames, grid, g1, cores)
+        out["cpu_baseline"] = {"value": (g1 / G) / t, "unit": "frames/s", "cores": cores, "kind": "port",
+                               "sample": f"grid points [0, {g1}) of frame 0 ({g1 / G:.4f} of a frame), FP64 oracle "
+                                         f"restating IrvingKirkwood::compute, OpenMP {cores} threads, {t:.2f} s"}
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        reference_arm(args, wl, args.workload)
+    else:
+        ours(args, wl, args.workload)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,160 @@
+/*
+ * ik_gb300.h -- C ABI of the GB300 (sm_103a) Irving-Kirkwood stress-field engine.
+ *
+ * One context = one GPU stream, one box, one pair potential, one coarse-graining
+ * function, one grid and any number of resident frame slots.  All pointers are
+ * HOST pointers unless the name says _device.  Every call returns an int status
+ * (IK_OK = 0, negative on error); ik_last_error() gives the message of the last
+ * failing call on the calling thread.  No call aborts the process and no kernel
+ * traps: device-side failures are reported through status words.
+ *
+ * Each entry point cites the reference interface it replaces (paths relative to
+ * the pyglasstools repository).
+ */
+#ifndef IK_GB300_H
+#define IK_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------- */
+#define IK_OK             0
+#define IK_ERR_ARG       -1  /* bad argument (size mismatch, NaN, unknown enum) */
+#define IK_ERR_CUDA      -2  /* a CUDA runtime call failed */
+#define IK_ERR_STATE     -3  /* call out of order (e.g. compute before set_grid) */
+#define IK_ERR_BOX       -4  /* a cut-off is >= half the periodic box */
+#define IK_ERR_CAPACITY  -5  /* a fixed-capacity buffer overflowed and could not grow */
+#define IK_ERR_TIMEOUT   -6  /* a bounded device-side wait gave up */
+#define IK_ERR_NOMEM     -7  /* device allocation failed */
+#define IK_ERR_UNSUPPORTED -8
+
+/* ---- enums ------------------------------------------------------------------ */
+enum ik_cg_kind { IK_CG_OCTIC = 0, IK_CG_GAUSSIAN = 1, IK_CG_RECT = 2, IK_CG_MOLLIFIER = 3 };
+enum ik_quad_mode { IK_QUAD_FIXEDPOINT = 0, IK_QUAD_ADAPTIVE = 1, IK_QUAD_EXACT = 2,
+                    IK_QUAD_MLP = 3 };
+enum ik_precision { IK_PREC_FP64 = 0,   /* plain path: FP64 throughout */
+                    IK_PREC_FP32 = 1 }; /* tuned path: FP32 pair arithmetic, compensated
+                                           accumulation, FP64 min-image/selection/final */
+enum ik_field { IK_FIELD_VIRIAL = 1, IK_FIELD_KINETIC = 2 };
+
+typedef struct ik_ctx ik_ctx;
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* ik_last_error(void);
+/* ABI version (major * 10000 + minor * 100 + patch). */
+int ik_version(void);
+
+/* Create / destroy a context on CUDA device `device`.
+ * Replaces: construction of IrvingKirkwood (irvingkirkwood/IrvingKirkwood.h:12-18)
+ * and the MPI Communicator it holds (MPIInterface.h:58). */
+int ik_create(ik_ctx** out, int device);
+int ik_destroy(ik_ctx* ctx);
+
+/* Box: SimBox(boxsize, origin, dim) semantics -- bounds [-L/2 - origin, L/2 - origin],
+ * periodic in x, y and (3D only) z.  Replaces SimBox::SimBox (SimBox.cc:25-45). */
+int ik_set_box(ik_ctx* ctx, int dim, const double boxsize[3], const double origin[3]);
+
+/* Pair potential PairPotentialPoly12(scaled_rcut, {v0, eps, c0, c1, c2}).
+ * Replaces ShortRangePairPotential<Polydisperse12> (potential/PairPotential.h:83-104,
+ * potential/Polydisperse12.h:38-55). */
+int ik_set_potential_poly12(ik_ctx* ctx, double scaled_rcut, const double params[5]);
+
+/* Coarse-graining function.  rcut = support radius R (Gaussian: cut * width);
+ * width = Gaussian standard deviation (Mollifier: the radius its normalisation was
+ * built with); order = Gauss-Legendre points for IK_QUAD_FIXEDPOINT.
+ * Replaces FixedPointCGFunc<...>(order, rcut) / AdaptiveCGFunc<...>(neval, relerr,
+ * abserr, rcut) (irvingkirkwood/cgfunc/CoarseGrainFunction.h:56-134). */
+int ik_set_cgfunc(ik_ctx* ctx, int kind, int mode, int order, double rcut, double width);
+/* Adaptive-mode tolerances (AdaptiveCGFunc(neval, relerr, abserr, rcut)). */
+int ik_set_adaptive(ik_ctx* ctx, int neval, double relerr, double abserr);
+
+/* Neighbour cut-off max_rcut; frozen like Calculator::max_rcut (Calculator.h:41-45).
+ * If never set, the first uploaded frame fixes it to max(scaled_rcut*dmax, dmax). */
+int ik_set_max_rcut(ik_ctx* ctx, double max_rcut);
+int ik_get_max_rcut(ik_ctx* ctx, double* out);
+
+/* Grid points (g x 3, FP64).  Replaces the gridpoints argument of
+ * IrvingKirkwood::compute (IrvingKirkwood.h:21,74) and
+ * CoarseGrainedField::addGridpoints (CoarseGrainedField.h:18-21). */
+int ik_set_grid(ik_ctx* ctx, int64_t g, const double* xyz);
+
+/* Frame slots.  pos/vel: n x 3 FP64 (vel may be NULL -> 0), mass: n (NULL -> 1),
+ * diam: n.  Replaces ParticleSystem(simbox, N, d, m, pos, vel)
+ * (ParticleSystem.cc:3-30) and IrvingKirkwood::setSystemData (Calculator.h:50-53).
+ * Slot 0 is the default frame.  The copy is asynchronous on the context stream
+ * from pinned host memory and synchronous otherwise. */
+int ik_reserve_slots(ik_ctx* ctx, int nslots);
+int ik_upload_frame(ik_ctx* ctx, int slot, int64_t n, const double* pos, const double* vel,
+                    const double* mass, const double* diam);
+int ik_set_frame(ik_ctx* ctx, int64_t n, const double* pos, const double* vel,
+                 const double* mass, const double* diam); /* = upload to slot 0 */
+
+/* Enqueue the IK computation of a slot (cell list, bonds, gather) on the context
+ * stream; results stay in HBM in the slot's field buffers.  fields: IK_FIELD_* mask.
+ * Replaces IrvingKirkwood::compute (IrvingKirkwood.h:74-110). */
+int ik_compute_slot(ik_ctx* ctx, int slot, int precision, int fields);
+/* Wait for the stream; reports device-side status words. */
+int ik_synchronize(ik_ctx* ctx);
+/* ik_compute_slot(0) + ik_synchronize. */
+int ik_compute(ik_ctx* ctx, int precision, int fields);
+
+/* Field download: out = g x dim x dim FP64, column-major per grid point
+ * (element (a,b) at g*dim*dim + a + dim*b), matching the Eigen::Tensor<double,2>
+ * storage behind CoarseGrainedField::gettostring (CoarseGrainedField.h:160-183). */
+int ik_get_field(ik_ctx* ctx, int slot, int field, double* out, int64_t count);
+
+/* Candidate neighbour list within `radius` (FP64 minimum image, |r_ij|^2 < radius^2,
+ * j != i, j ascending): CSR offs[n+1], idx[nnz].  Call with idx == NULL to get nnz.
+ * Replaces ParticleSystem::getNeighborsDistance / the Aboria euclidean_search
+ * around particles (ParticleSystem.cc:183-195, IrvingKirkwood.h:93-95). */
+int ik_get_neighbors(ik_ctx* ctx, int slot, double radius, int64_t* offs, int32_t* idx,
+                     int64_t idx_capacity, int64_t* nnz);
+/* Particles within `radius` of a point, ascending ids.
+ * Replaces ParticleSystem::getNeighbors (ParticleSystem.cc:171-181). */
+int ik_get_neighbors_point(ik_ctx* ctx, int slot, const double point[3], double radius,
+                           int32_t* ids, int64_t capacity, int64_t* count);
+
+/* Per-pair scalar kernels on the device for API parity with
+ * PairPotential::getPairForceDivR / getPairEnergy and
+ * CoarseGrainFunction::getDeltaFunc / getBondFunc (PairPotential.h:98-113,
+ * CoarseGrainFunction.h:78-88).  Arrays of m queries; rij/x/ri: m x 3. */
+int ik_eval_pair(ik_ctx* ctx, int64_t m, const double* rij, const double* di,
+                 const double* dj, double* force_divr, double* energy);
+int ik_eval_bond(ik_ctx* ctx, int64_t m, const double* x, const double* ri,
+                 const double* rij, double* bond, double* delta);
+
+/* Timing of the last ik_compute_slot on the stream (ms per stage, CUDA events):
+ * [0] cells, [1] bonds, [2] gather, [3] total.  Needs IK_TIMING in ik_set_flags. */
+#define IK_FLAG_TIMING 1
+/* FP32 path: plain FP32 per-lane sums instead of Kahan-compensated ones. */
+#define IK_FLAG_NO_KAHAN 2
+int ik_set_flags(ik_ctx* ctx, int flags);
+int ik_get_timing(ik_ctx* ctx, float* ms4);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that time or order
+ * work against it (e.g. CUDA events recorded on this stream). */
+int ik_get_stream(ik_ctx* ctx, void** stream);
+
+/* Asynchronous download of a slot's field in compact form: g x NC FP64 with
+ * NC = 3 (xx, yy, xy) in 2D or 6 (xx, yy, zz, xy, xz, yz) in 3D.  host_out should be
+ * pinned for the copy to overlap; it is complete after ik_synchronize. */
+int ik_download_field_async(ik_ctx* ctx, int slot, int field, double* host_out, int64_t count);
+
+/* Measured FP32 FMA throughput of `device` (TFLOP/s, 2 FLOP per FMA) from a
+ * dependent-chain-free FFMA loop over all SMs; the roofline denominator of the
+ * FP32 gather.  Diagnostic: no reference counterpart. */
+int ik_measure_fp32_peak(int device, double* tflops);
+
+/* Number of kernels this context has launched since it was created. */
+int ik_get_launch_count(ik_ctx* ctx, int64_t* out);
+
+/* Counters of the last computation: [0] force-active directed bonds,
+ * [1] accepted (grid, particle) pairs, [2] active (grid, i, j) triples (FP32 path). */
+int ik_get_counters(ik_ctx* ctx, int slot, int64_t* out3);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IK_GB300_H */

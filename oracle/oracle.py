@@ -1,0 +1,244 @@
+"""ctypes front-end of the FP64 CPU oracle (oracle/ik_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()`` and the
+CPU-baseline legs of ``bench.py``.  The product (``pyglasstools_gb300``) never
+imports this module.
+
+Parity: the reference's IK field cannot be produced here (its loop needs Aboria,
+Eigen, GSL and MPI), so field parity is *unpinned by the reference*; the force
+and kernel formulas are pinned bit-for-bit against the reference headers built
+by ``oracle/build_ref.sh`` (tests/test_oracle_pins.py).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+CG_KIND = {"octic": 0, "gaussian": 1, "rect": 2, "mollifier": 3}
+QUAD_MODE = {"fixedpoint": 0, "adaptive": 1, "exact": 2}
+
+
+class Box(C.Structure):
+    _fields_ = [("dim", C.c_int), ("L", C.c_double * 3), ("lo", C.c_double * 3),
+                ("periodic", C.c_int * 3)]
+
+
+class Poly12(C.Structure):
+    _fields_ = [("scaled_rcut", C.c_double), ("v0", C.c_double), ("eps", C.c_double),
+                ("c0", C.c_double), ("c1", C.c_double), ("c2", C.c_double)]
+
+
+class CG(C.Structure):
+    _fields_ = [("kind", C.c_int), ("mode", C.c_int), ("order", C.c_int),
+                ("rcut", C.c_double), ("width", C.c_double), ("epsabs", C.c_double),
+                ("epsrel", C.c_double), ("limit", C.c_int)]
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build()
+        L = C.CDLL(path)
+        dp = C.POINTER(C.c_double)
+        L.ikor_gl_rule.argtypes = [C.c_int, dp, dp]
+        L.ikor_gk15_rule.argtypes = [dp, dp, dp]
+        for f in ("ikor_force_divr", "ikor_pair_energy", "ikor_bond_stiffness"):
+            getattr(L, f).argtypes = [C.POINTER(Poly12), C.c_double, C.c_double, C.c_double]
+            getattr(L, f).restype = C.c_double
+        L.ikor_delta.argtypes = [C.POINTER(CG), C.c_int, C.c_double]
+        L.ikor_delta.restype = C.c_double
+        L.ikor_bond.argtypes = [C.POINTER(CG), C.c_int, dp, dp, dp]
+        L.ikor_bond.restype = C.c_double
+        L.ikor_max_rcut.argtypes = [C.c_double, C.c_int64, dp]
+        L.ikor_max_rcut.restype = C.c_double
+        L.ikor_neighbors.argtypes = [C.POINTER(Box), C.c_int64, dp, C.c_double,
+                                     C.POINTER(C.c_int64), C.POINTER(C.c_int32)]
+        L.ikor_neighbors.restype = C.c_int64
+        L.ikor_compute_range.argtypes = [C.POINTER(Box), C.c_int64, dp, dp, dp, dp,
+                                         C.POINTER(Poly12), C.POINTER(CG), C.c_double,
+                                         C.c_int64, C.c_int64, dp, dp, dp, C.c_int]
+        L.ikor_compute_range.restype = C.c_int
+        L.ikor_global_virial.argtypes = [C.POINTER(Box), C.c_int64, dp, dp, C.POINTER(Poly12),
+                                         C.c_double, dp]
+        _LIB = L
+    return _LIB
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def make_box(dim, L, origin=(0.0, 0.0, 0.0)):
+    """SimBox(boxsize, origin, dim) bounds: lo = -L/2 - origin (SimBox.cc:48-52);
+    z non-periodic in 2D (SimBox.cc:34-40)."""
+    L = np.broadcast_to(np.asarray(L, dtype=np.float64), (3,)).copy()
+    if dim == 2:
+        L[2] = 1.0 if L[2] == 0 else L[2]
+    b = Box()
+    b.dim = dim
+    for c in range(3):
+        b.L[c] = float(L[c])
+        b.lo[c] = -0.5 * float(L[c]) - float(origin[c])
+        b.periodic[c] = 1 if (c < dim) else 0
+    return b
+
+
+def make_poly12(v0=1.0, eps=0.2, rcut=1.25):
+    """pyglasstools.potential.polydisperse12 coefficients (potential/__init__.py:81-86)."""
+    p = Poly12()
+    p.scaled_rcut = rcut
+    p.v0 = v0
+    p.eps = eps
+    p.c0 = -28.0 * v0 / rcut ** 12
+    p.c1 = 48.0 * v0 / rcut ** 14
+    p.c2 = -21.0 * v0 / rcut ** 16
+    return p
+
+
+def make_cg(kind="octic", rcut=2.0, mode="fixedpoint", order=5, width=0.0,
+            epsabs=1e-10, epsrel=1e-10, limit=1000):
+    c = CG()
+    c.kind = CG_KIND[kind]
+    c.mode = QUAD_MODE[mode]
+    c.order = order
+    c.rcut = rcut
+    c.width = width
+    c.epsabs = epsabs
+    c.epsrel = epsrel
+    c.limit = limit
+    return c
+
+
+def gl_rule(n):
+    x = np.zeros(n)
+    w = np.zeros(n)
+    lib().ikor_gl_rule(n, _dp(x), _dp(w))
+    return x, w
+
+
+def gk15_rule():
+    x = np.zeros(8)
+    wk = np.zeros(8)
+    wg = np.zeros(4)
+    lib().ikor_gk15_rule(_dp(x), _dp(wk), _dp(wg))
+    return x, wk, wg
+
+
+def force_divr(pot, rsq, di, dj):
+    return lib().ikor_force_divr(C.byref(pot), rsq, di, dj)
+
+
+def pair_energy(pot, rsq, di, dj):
+    return lib().ikor_pair_energy(C.byref(pot), rsq, di, dj)
+
+
+def bond_stiffness(pot, rsq, di, dj):
+    return lib().ikor_bond_stiffness(C.byref(pot), rsq, di, dj)
+
+
+def delta(cg, dim, dr_sq):
+    return lib().ikor_delta(C.byref(cg), dim, dr_sq)
+
+
+def bond(cg, dim, x, ri, rij):
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    ri = np.ascontiguousarray(ri, dtype=np.float64)
+    rij = np.ascontiguousarray(rij, dtype=np.float64)
+    return lib().ikor_bond(C.byref(cg), dim, _dp(x), _dp(ri), _dp(rij))
+
+
+def max_rcut(scaled_rcut, diam):
+    diam = np.ascontiguousarray(diam, dtype=np.float64)
+    return lib().ikor_max_rcut(scaled_rcut, len(diam), _dp(diam))
+
+
+def neighbors(box, pos, radius):
+    """Candidate CSR (offs, idx) with j ascending; pos is n x 3."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    n = len(pos)
+    offs = np.zeros(n + 1, dtype=np.int64)
+    L = lib()
+    nnz = L.ikor_neighbors(C.byref(box), n, _dp(pos), radius,
+                           offs.ctypes.data_as(C.POINTER(C.c_int64)), None)
+    idx = np.zeros(max(nnz, 1), dtype=np.int32)
+    L.ikor_neighbors(C.byref(box), n, _dp(pos), radius,
+                     offs.ctypes.data_as(C.POINTER(C.c_int64)),
+                     idx.ctypes.data_as(C.POINTER(C.c_int32)))
+    return offs, idx[:nnz]
+
+
+def compute(box, pos, diam, pot, cg, grid, vel=None, mass=None, max_rc=None,
+            g0=0, g1=None, nthreads=0):
+    """Run the IK gather over grid points [g0, g1).  Returns (virial, kinetic), each
+    (g1-g0) x dim x dim with [g, a, b] = T_ab (symmetric)."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    diam = np.ascontiguousarray(diam, dtype=np.float64)
+    grid = np.ascontiguousarray(grid, dtype=np.float64)
+    n = len(pos)
+    if g1 is None:
+        g1 = len(grid)
+    if max_rc is None:
+        max_rc = max_rcut(pot.scaled_rcut, diam)
+    D = box.dim
+    vir = np.zeros((g1 - g0) * D * D)
+    kin = np.zeros((g1 - g0) * D * D)
+    if vel is not None and mass is not None:
+        vel = np.ascontiguousarray(vel, dtype=np.float64)
+        mass = np.ascontiguousarray(mass, dtype=np.float64)
+        vp, mp = _dp(vel), _dp(mass)
+    else:
+        vp = mp = None
+    rc = lib().ikor_compute_range(C.byref(box), n, _dp(pos), vp, mp, _dp(diam), C.byref(pot),
+                                  C.byref(cg), max_rc, g0, g1, _dp(grid), _dp(vir), _dp(kin),
+                                  nthreads)
+    if rc != 0:
+        raise ValueError(f"oracle compute failed ({rc}): box too small for the cut-offs")
+    # column-major per grid point: index a + D*b -> [g, b, a]; symmetric so same
+    vir = vir.reshape(g1 - g0, D, D).transpose(0, 2, 1).copy()
+    kin = kin.reshape(g1 - g0, D, D).transpose(0, 2, 1).copy()
+    return vir, kin
+
+
+def global_virial(box, pos, diam, pot, max_rc=None):
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    diam = np.ascontiguousarray(diam, dtype=np.float64)
+    if max_rc is None:
+        max_rc = max_rcut(pot.scaled_rcut, diam)
+    D = box.dim
+    out = np.zeros(D * D)
+    lib().ikor_global_virial(C.byref(box), len(pos), _dp(pos), _dp(diam), C.byref(pot),
+                             max_rc, _dp(out))
+    return out.reshape(D, D).T.copy()
+
+
+# ---- reference kernels compiled from the reference tree (oracle/_ref) --------
+def ref_lib():
+    """The reference's own Polydisperse12/Octic/Rect/Mollifier, or None when
+    oracle/_ref was not built (no reference tree on this machine)."""
+    path = os.path.join(_HERE, "_ref", "libref_kernels.so")
+    if not os.path.exists(path):
+        return None
+    try:
+        L = C.CDLL(path)
+    except OSError:
+        return None
+    dp = C.POINTER(C.c_double)
+    for f in ("ref_poly12_force_divr", "ref_poly12_energy", "ref_poly12_stiffness"):
+        getattr(L, f).argtypes = [C.c_double, C.c_double, dp, C.c_double, C.c_double]
+        getattr(L, f).restype = C.c_double
+    for f in ("ref_octic", "ref_rect", "ref_mollifier"):
+        getattr(L, f).argtypes = [C.c_double, C.c_double]
+        getattr(L, f).restype = C.c_double
+    return L

@@ -1,0 +1,631 @@
+// bindings.cpp -- pybind11 modules with the reference's class and method names
+// (_pyglasstools, _potential, _cgfunc, _irvingkirkwood), thin over the C ABI of
+// libik_gb300.so (include/ik_gb300.h).  Every numeric evaluation goes to the GPU.
+//
+// Mirrors: module-pyglasstools.cpp, ParticleSystem.cc:199-221, SimBox.cc:55-69,
+// potential/PairPotential.h:125-152, irvingkirkwood/cgfunc/CoarseGrainFunction.h:136-167,
+// irvingkirkwood/IrvingKirkwood.h:113-122, irvingkirkwood/CoarseGrainedField.h:342-358.
+#include <pybind11/numpy.h>
+#include <pybind11/pybind11.h>
+#include <pybind11/stl.h>
+
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "ik_gb300.h"
+
+namespace py = pybind11;
+using Vec3 = std::array<double, 3>;
+using DArr = py::array_t<double, py::array::c_style | py::array::forcecast>;
+
+static void check(int rc)
+{
+    if (rc != IK_OK) {
+        std::string msg = ik_last_error();
+        if (rc == IK_ERR_ARG || rc == IK_ERR_BOX) throw std::invalid_argument("[ERROR]: " + msg);
+        throw std::runtime_error("[ERROR]: " + msg);
+    }
+}
+
+// One shared context for scalar evaluations (getPairForceDivR, getBondFunc, ...).
+static ik_ctx* util_ctx()
+{
+    static ik_ctx* c = nullptr;
+    static std::mutex m;
+    std::lock_guard<std::mutex> lk(m);
+    if (!c) check(ik_create(&c, 0));
+    return c;
+}
+
+static std::vector<double> to_xyz(py::handle obj, size_t expect_rows, const char* what)
+{
+    DArr a = DArr::ensure(obj);
+    if (!a) throw std::invalid_argument(std::string("[ERROR]: ") + what + " must be array-like");
+    auto b = a.request();
+    std::vector<double> out;
+    size_t rows = b.ndim >= 1 ? (size_t)b.shape[0] : 0;
+    size_t cols = b.ndim == 2 ? (size_t)b.shape[1] : (b.ndim == 1 ? 1 : 0);
+    if (b.ndim == 1 && expect_rows == 1) { rows = 1; cols = (size_t)b.shape[0]; }
+    if (b.ndim > 2 || cols < 2 || cols > 3)
+        throw std::invalid_argument(std::string("[ERROR]: ") + what + " must be (n, 2) or (n, 3)");
+    if (expect_rows != (size_t)-1 && rows != expect_rows)
+        throw std::invalid_argument(std::string("[ERROR]: Size of ") + what + " array mismatch with # of particles!");
+    out.assign(rows * 3, 0.0);
+    const double* p = static_cast<const double*>(b.ptr);
+    for (size_t i = 0; i < rows; ++i)
+        for (size_t c = 0; c < cols; ++c) out[3 * i + c] = p[i * cols + c];
+    return out;
+}
+
+static std::vector<double> to_vec(py::handle obj, const char* what)
+{
+    DArr a = DArr::ensure(obj);
+    if (!a) throw std::invalid_argument(std::string("[ERROR]: ") + what + " must be array-like");
+    auto b = a.request();
+    const double* p = static_cast<const double*>(b.ptr);
+    return std::vector<double>(p, p + b.size);
+}
+
+static Vec3 to3(py::handle obj)
+{
+    std::vector<double> v = to_vec(obj, "vector");
+    Vec3 r = {0, 0, 0};
+    for (size_t k = 0; k < v.size() && k < 3; ++k) r[k] = v[k];
+    return r;
+}
+
+// ---------------------------------------------------------------- _pyglasstools
+struct SimBox {
+    int dim = 3;
+    Vec3 origin{}, boxsize{}, lowerbound{}, upperbound{}, periodic{};
+    double vol = 0.0;
+    SimBox(Vec3 L, Vec3 o, int d) { init(L, o, d); }
+    void init(Vec3 L, Vec3 o, int d)
+    {
+        // SimBox.cc:25-52 (bounds set before the 2D z overrides, as in the reference)
+        dim = d;
+        origin = o;
+        boxsize = L;
+        for (int a = 0; a < 3; ++a) {
+            upperbound[a] = 0.5 * boxsize[a] - origin[a];
+            lowerbound[a] = -upperbound[a] - 2.0 * origin[a];
+            periodic[a] = 1;
+        }
+        if (dim == 2) {
+            boxsize[2] = 1.0;
+            periodic[2] = 0;
+            origin[2] = 0.0;
+            vol = boxsize[0] * boxsize[1];
+        } else {
+            vol = boxsize[0] * boxsize[1] * boxsize[2];
+        }
+    }
+    Vec3 minImage(Vec3 v) const
+    {
+        Vec3 w = v;
+        for (int a = 2; a >= 0; --a)
+            if (periodic[a]) w[a] -= boxsize[a] * (double)rintf((float)(w[a] / boxsize[a]));
+        return w;
+    }
+};
+
+struct ParticleSystem {
+    std::shared_ptr<SimBox> simbox;
+    unsigned int N = 0;
+    std::vector<double> diameter, mass, pos, vel, disp;
+    uint64_t version = 0;
+    ik_ctx* qctx = nullptr;      // lazily created context for neighbour queries
+    uint64_t qversion = (uint64_t)-1;
+
+    ParticleSystem(std::shared_ptr<SimBox> box, unsigned int n, py::handle d, py::handle m, py::handle p,
+                   py::handle v)
+        : simbox(std::move(box))
+    {
+        set(n, d, m, p, v);
+    }
+    ~ParticleSystem() { if (qctx) ik_destroy(qctx); }
+    void set(unsigned int n, py::handle d, py::handle m, py::handle p, py::handle v)
+    {
+        N = n;
+        diameter = to_vec(d, "diameter");
+        mass = to_vec(m, "mass");
+        if (diameter.size() != n) throw std::invalid_argument("[ERROR]: Size of diameter array mismatch with # of particles!");
+        if (mass.size() != n) throw std::invalid_argument("[ERROR]: Size of mass array mismatch with # of particles!");
+        pos = to_xyz(p, n, "position");
+        vel = to_xyz(v, n, "velocity");
+        disp.assign(3 * (size_t)n, 0.0);
+        ++version;
+    }
+    ik_ctx* query_ctx()
+    {
+        if (!qctx) check(ik_create(&qctx, 0));
+        if (qversion != version) {
+            double L[3] = {simbox->boxsize[0], simbox->boxsize[1], simbox->boxsize[2]};
+            double o[3] = {simbox->origin[0], simbox->origin[1], simbox->origin[2]};
+            check(ik_set_box(qctx, simbox->dim, L, o));
+            check(ik_set_frame(qctx, N, pos.data(), vel.data(), mass.data(), diameter.data()));
+            check(ik_synchronize(qctx));
+            qversion = version;
+        }
+        return qctx;
+    }
+    std::vector<unsigned int> getNeighbors(py::handle point, double radius)
+    {
+        Vec3 q = to3(point);
+        ik_ctx* c = query_ctx();
+        int64_t cnt = 0;
+        check(ik_get_neighbors_point(c, 0, q.data(), radius, nullptr, 0, &cnt));
+        std::vector<int32_t> ids((size_t)std::max<int64_t>(cnt, 1));
+        check(ik_get_neighbors_point(c, 0, q.data(), radius, ids.data(), cnt, &cnt));
+        return std::vector<unsigned int>(ids.begin(), ids.begin() + cnt);
+    }
+    py::array_t<double> getNeighborsDistance(int tag, double radius)
+    {
+        if (tag < 0 || (unsigned)tag >= N) throw std::invalid_argument("[ERROR]: particle tag out of range");
+        ik_ctx* c = query_ctx();
+        std::vector<int64_t> offs(N + 1);
+        int64_t nnz = 0;
+        check(ik_get_neighbors(c, 0, radius, offs.data(), nullptr, 0, &nnz));
+        std::vector<int32_t> idx((size_t)std::max<int64_t>(nnz, 1));
+        check(ik_get_neighbors(c, 0, radius, offs.data(), idx.data(), nnz, &nnz));
+        int64_t s = offs[(size_t)tag], e = offs[(size_t)tag + 1];
+        py::array_t<double> out({(py::ssize_t)(e - s), (py::ssize_t)3});
+        auto o = out.mutable_unchecked<2>();
+        for (int64_t k = s; k < e; ++k) {
+            int j = idx[(size_t)k];
+            for (int a = 0; a < 3; ++a) {
+                double d = pos[3 * (size_t)j + a] - pos[3 * (size_t)tag + a];
+                if (simbox->periodic[a]) d = d - simbox->boxsize[a] * std::nearbyint(d / simbox->boxsize[a]);
+                o(k - s, a) = d;
+            }
+        }
+        return out;
+    }
+    py::tuple neighborList(double radius)
+    {
+        ik_ctx* c = query_ctx();
+        py::array_t<int64_t> offs((py::ssize_t)N + 1);
+        int64_t nnz = 0;
+        check(ik_get_neighbors(c, 0, radius, offs.mutable_data(), nullptr, 0, &nnz));
+        py::array_t<int32_t> idx((py::ssize_t)nnz);
+        check(ik_get_neighbors(c, 0, radius, offs.mutable_data(), idx.mutable_data(), nnz, &nnz));
+        return py::make_tuple(offs, idx);
+    }
+    static py::array_t<double> as_nx3(const std::vector<double>& v)
+    {
+        py::array_t<double> a({(py::ssize_t)(v.size() / 3), (py::ssize_t)3});
+        std::copy(v.begin(), v.end(), a.mutable_data());
+        return a;
+    }
+};
+
+// Single-rank communicator with the methods the Python layer uses (MPIInterface.h:58-441).
+struct Communicator {
+    int getRank() const { return 0; }
+    int getSizeGlobal() const { return 1; }
+    void barrier() const {}
+    void abort(int code) const { std::fflush(nullptr); std::_Exit(code); }
+    py::object bcast(py::object v, int) const { return v; }
+    py::object scatter_v(py::list parts, int) const { return parts.size() ? parts[0] : py::object(py::none()); }
+    py::object gather_v(py::object v, int) const { py::list l; l.append(v); return std::move(l); }
+    py::object all_gather_v(py::object v) const { py::list l; l.append(v); return std::move(l); }
+    void send(py::object, int, int) const {}
+    py::object recv(int, int) const { return py::bool_(true); }
+};
+
+// Buffered stand-in of MPI::LogFile (MPIFile.h:23-56): write_shared appends.
+struct MPILogFile {
+    std::ofstream f;
+    MPILogFile(std::shared_ptr<Communicator>, const std::string& name) : f(name, std::ios::out | std::ios::app)
+    {
+        if (!f) throw std::runtime_error("[ERROR]: cannot open " + name);
+    }
+    void write_shared(const std::string& s) { f << s; }
+    void flush() { f.flush(); }
+    void close() { f.close(); }
+};
+
+struct Manager {
+    int notice_level = 2;
+};
+
+// ---------------------------------------------------------------- _potential
+struct PairPotential {
+    double scaled_rcut = 0.0;
+    std::vector<double> params;
+    PairPotential(std::vector<double> p) : params(std::move(p)) {}
+    PairPotential(double rc, std::vector<double> p) : scaled_rcut(rc), params(std::move(p)) {}
+    virtual ~PairPotential() = default;
+    virtual int model() const { return -1; }
+    virtual double getRcut(py::handle, double, double) { return 0.0; }
+    virtual double getPairForceDivR(py::handle, double, double) { return 0.0; }
+    virtual double getPairEnergy(py::handle, double, double) { return 0.0; }
+    void setParams(double v, int k)
+    {
+        if (k < 0 || (size_t)k >= params.size()) throw std::invalid_argument("[ERROR]: parameter index out of range");
+        params[(size_t)k] = v;
+    }
+    std::vector<double> getParams() const { return params; }
+};
+
+struct PairPotentialPoly12 : PairPotential {
+    using PairPotential::PairPotential;
+    int model() const override { return 12; }
+    void validate() const
+    {
+        if (params.size() < 5) throw std::invalid_argument("[ERROR]: Poly12 needs [v0, eps, c0, c1, c2]");
+    }
+    double sigma(double di, double dj) const { return 0.5 * (di + dj) * (1 - params[1] * std::fabs(di - dj)); }
+    double getRcut(py::handle, double di, double dj) override
+    {
+        validate();
+        double s = sigma(di, dj);
+        return scaled_rcut * scaled_rcut * s * s; // computeRcut (Polydisperse12.h:75-79)
+    }
+    std::pair<double, double> eval(py::handle rij, double di, double dj)
+    {
+        validate();
+        Vec3 r = to3(rij);
+        ik_ctx* c = util_ctx();
+        check(ik_set_potential_poly12(c, scaled_rcut, params.data()));
+        double f = 0, e = 0;
+        check(ik_eval_pair(c, 1, r.data(), &di, &dj, &f, &e));
+        return {f, e};
+    }
+    double getPairForceDivR(py::handle rij, double di, double dj) override { return eval(rij, di, dj).first; }
+    double getPairEnergy(py::handle rij, double di, double dj) override { return eval(rij, di, dj).second; }
+};
+
+// ---------------------------------------------------------------- _cgfunc
+struct CoarseGrainFunction {
+    int kind = 0, mode = IK_QUAD_FIXEDPOINT, order = 1, neval = 1000;
+    double cg_rcut = 0.0, width = 0.0, relerr = 1e-9, abserr = 1e-9;
+    CoarseGrainFunction(double rc) : cg_rcut(rc) {}
+    virtual ~CoarseGrainFunction() = default;
+    void setRcut(double rc) { cg_rcut = rc; }
+    double getRcut() const { return cg_rcut; }
+    void apply(ik_ctx* c) const
+    {
+        check(ik_set_cgfunc(c, kind, mode, order, cg_rcut, width));
+        if (mode == IK_QUAD_ADAPTIVE) check(ik_set_adaptive(c, neval, relerr, abserr));
+    }
+    std::pair<double, double> eval(py::handle x, py::handle ri, py::handle rij) const
+    {
+        Vec3 a = to3(x), b = to3(ri), r = to3(rij);
+        ik_ctx* c = util_ctx();
+        apply(c);
+        double bond = 0, delta = 0;
+        check(ik_eval_bond(c, 1, a.data(), b.data(), r.data(), &bond, &delta));
+        return {bond, delta};
+    }
+    double getDeltaFunc(py::handle x, py::handle ri) const
+    {
+        return eval(x, ri, py::cast(std::vector<double>{0.0, 0.0, 0.0})).second;
+    }
+    double getObjFunc(double s, py::handle x, py::handle ri, py::handle rij) const
+    {
+        Vec3 b = to3(ri), r = to3(rij);
+        std::vector<double> p = {b[0] + s * r[0], b[1] + s * r[1], b[2] + s * r[2]};
+        return getDeltaFunc(x, py::cast(p));
+    }
+    double getBondFunc(py::handle x, py::handle ri, py::handle rij) const { return eval(x, ri, rij).first; }
+};
+
+template <int KIND>
+struct CGFixed : CoarseGrainFunction {
+    CGFixed(int ord, double rc) : CoarseGrainFunction(rc)
+    {
+        kind = KIND;
+        mode = IK_QUAD_FIXEDPOINT;
+        order = ord;
+        if (KIND == IK_CG_MOLLIFIER) width = rc; // normalisation radius frozen at construction
+    }
+};
+template <int KIND>
+struct CGAdaptive : CoarseGrainFunction {
+    CGAdaptive(int nev, double rel, double abs_, double rc) : CoarseGrainFunction(rc)
+    {
+        kind = KIND;
+        mode = IK_QUAD_ADAPTIVE;
+        neval = nev;
+        relerr = rel;
+        abserr = abs_;
+        if (KIND == IK_CG_MOLLIFIER) width = rc;
+    }
+};
+// Gaussian: support R = cut * width (new kernel, not in the reference)
+struct CGGaussianFixed : CoarseGrainFunction {
+    CGGaussianFixed(int ord, double w, double cut) : CoarseGrainFunction(cut * w)
+    {
+        kind = IK_CG_GAUSSIAN;
+        mode = IK_QUAD_FIXEDPOINT;
+        order = ord;
+        width = w;
+    }
+};
+
+// ---------------------------------------------------------------- _irvingkirkwood
+struct CoarseGrainedField {
+    std::string name, type;
+    bool islocal = false;
+    int dim = 2;
+    int field = IK_FIELD_VIRIAL;
+    std::vector<double> val; // gridsize x dim x dim, column-major per grid point
+    py::object gridpoints = py::none();
+    CoarseGrainedField(std::string n, std::string t, bool local, int gridsize, int d, int f)
+        : name(std::move(n)), type(std::move(t)), islocal(local), dim(d), field(f)
+    {
+        if (gridsize < 0) throw std::invalid_argument("[ERROR]: gridsize must be >= 0");
+        val.assign((size_t)gridsize * d * d, 0.0);
+    }
+    virtual ~CoarseGrainedField() = default;
+    void addGridpoints(py::object g) { gridpoints = std::move(g); }
+    std::string gettostring(int index, int grid_id) const
+    {
+        // CoarseGrainedField.h:284-307: default ostream formatting (6 significant digits) + " "
+        size_t DD = (size_t)dim * dim;
+        if (grid_id < 0 || (size_t)grid_id * DD >= val.size() || index < 0 || (size_t)index >= DD)
+            throw std::out_of_range("[ERROR]: grid/component index out of range");
+        std::ostringstream os;
+        os << val[(size_t)grid_id * DD + (size_t)index] << " ";
+        return os.str();
+    }
+    void save(MPILogFile& f, int index, int grid_id) { f.write_shared(gettostring(index, grid_id)); }
+    void clear(int grid_id)
+    {
+        size_t DD = (size_t)dim * dim;
+        if (grid_id < 0 || (size_t)grid_id * DD >= val.size()) throw std::out_of_range("[ERROR]: grid index out of range");
+        std::fill(val.begin() + (long)grid_id * DD, val.begin() + (long)(grid_id + 1) * DD, 0.0);
+    }
+    py::array_t<double> values() const
+    {
+        size_t G = val.size() / ((size_t)dim * dim);
+        py::array_t<double> a({(py::ssize_t)G, (py::ssize_t)dim, (py::ssize_t)dim});
+        auto m = a.mutable_unchecked<3>();
+        for (size_t g = 0; g < G; ++g)
+            for (int i = 0; i < dim; ++i)
+                for (int j = 0; j < dim; ++j) m(g, i, j) = val[g * dim * dim + i + dim * j];
+        return a;
+    }
+};
+
+template <int D, int FIELD>
+struct FieldT : CoarseGrainedField {
+    FieldT(std::string n, std::string t, bool local, int gridsize)
+        : CoarseGrainedField(std::move(n), std::move(t), local, gridsize, D, FIELD)
+    {
+    }
+};
+
+struct IrvingKirkwood {
+    std::shared_ptr<ParticleSystem> sys;
+    std::shared_ptr<PairPotential> pot;
+    std::shared_ptr<CoarseGrainFunction> cg;
+    std::shared_ptr<Communicator> comm;
+    std::map<std::string, std::shared_ptr<CoarseGrainedField>> obs;
+    ik_ctx* ctx = nullptr;
+    double max_rcut = 0.0;
+    int precision = IK_PREC_FP32;
+    uint64_t uploaded = (uint64_t)-1;
+    const ParticleSystem* uploaded_sys = nullptr;
+    std::vector<double> last_grid;
+
+    IrvingKirkwood(std::shared_ptr<ParticleSystem> s, std::shared_ptr<PairPotential> p,
+                   std::shared_ptr<CoarseGrainFunction> c, std::shared_ptr<Communicator> cm)
+        : sys(std::move(s)), pot(std::move(p)), cg(std::move(c)), comm(std::move(cm))
+    {
+        if (!sys || !pot || !cg) throw std::invalid_argument("[ERROR]: IrvingKirkwood needs sysdata, potential, cgfunc");
+        // Calculator.h:41-45: frozen at construction
+        double dmax = 0.0;
+        for (double d : sys->diameter) dmax = std::max(dmax, d);
+        max_rcut = std::max(pot->scaled_rcut * dmax, dmax);
+        check(ik_create(&ctx, 0));
+    }
+    ~IrvingKirkwood() { if (ctx) ik_destroy(ctx); }
+    void setSystemData(std::shared_ptr<ParticleSystem> s) { sys = std::move(s); }
+    void addObservable(std::shared_ptr<CoarseGrainedField> f) { obs[f->name] = std::move(f); }
+    void printDisplacement()
+    {
+        for (unsigned i = 0; i < sys->N; ++i) py::print(sys->disp[3 * i], sys->disp[3 * i + 1], i);
+    }
+    void setPrecision(const std::string& p)
+    {
+        if (p == "fp64") precision = IK_PREC_FP64;
+        else if (p == "fp32") precision = IK_PREC_FP32;
+        else throw std::invalid_argument("[ERROR]: precision must be 'fp64' or 'fp32'");
+    }
+    std::string getPrecision() const { return precision == IK_PREC_FP64 ? "fp64" : "fp32"; }
+    void compute(py::handle gridpoints)
+    {
+        std::vector<double> grid = to_xyz(gridpoints, (size_t)-1, "gridpoints");
+        int64_t G = (int64_t)grid.size() / 3;
+        auto pp = std::dynamic_pointer_cast<PairPotentialPoly12>(pot);
+        if (!pp) throw std::invalid_argument("[ERROR]: only the polydisperse12 potential is on the GPU path");
+        pp->validate();
+        const SimBox& b = *sys->simbox;
+        double L[3] = {b.boxsize[0], b.boxsize[1], b.boxsize[2]};
+        double o[3] = {b.origin[0], b.origin[1], b.origin[2]};
+        int fields = 0;
+        for (auto& kv : obs) {
+            if (kv.second->dim != b.dim) throw std::invalid_argument("[ERROR]: observable dimension != box dimension");
+            if ((int64_t)kv.second->val.size() != G * b.dim * b.dim)
+                throw std::invalid_argument("[ERROR]: observable gridsize != number of grid points");
+            fields |= kv.second->field;
+        }
+        if (!fields) return;
+        {
+            py::gil_scoped_release nogil;
+            check(ik_set_box(ctx, b.dim, L, o));
+            check(ik_set_potential_poly12(ctx, pot->scaled_rcut, pot->params.data()));
+            cg->apply(ctx);
+            check(ik_set_max_rcut(ctx, max_rcut));
+            if (grid != last_grid) {
+                check(ik_set_grid(ctx, G, grid.data()));
+                last_grid = grid;
+            }
+            if (uploaded != sys->version || uploaded_sys != sys.get()) {
+                check(ik_set_frame(ctx, sys->N, sys->pos.data(), sys->vel.data(), sys->mass.data(),
+                                   sys->diameter.data()));
+                uploaded = sys->version;
+                uploaded_sys = sys.get();
+            }
+            check(ik_compute(ctx, precision, fields));
+            for (auto& kv : obs)
+                check(ik_get_field(ctx, 0, kv.second->field, kv.second->val.data(), (int64_t)kv.second->val.size()));
+        }
+    }
+    std::vector<int64_t> counters()
+    {
+        std::vector<int64_t> c(3, 0);
+        check(ik_get_counters(ctx, 0, c.data()));
+        return c;
+    }
+};
+
+// ---------------------------------------------------------------- module
+PYBIND11_MODULE(_core, m)
+{
+    m.doc() = "GB300 Irving-Kirkwood engine: pybind11 mirror of pyglasstools' native modules";
+    m.def("abi_version", &ik_version);
+
+    py::module pg = m.def_submodule("_pyglasstools");
+    py::class_<SimBox, std::shared_ptr<SimBox>>(pg, "SimBox")
+        .def(py::init([](double L, py::handle o, int d) { return std::make_shared<SimBox>(Vec3{L, L, L}, to3(o), d); }))
+        .def(py::init([](py::handle L, py::handle o, int d) { return std::make_shared<SimBox>(to3(L), to3(o), d); }))
+        .def("minImage", &SimBox::minImage)
+        .def_readwrite("dim", &SimBox::dim)
+        .def_readwrite("origin", &SimBox::origin)
+        .def_readwrite("boxsize", &SimBox::boxsize)
+        .def_readwrite("upperbound", &SimBox::upperbound)
+        .def_readwrite("lowerbound", &SimBox::lowerbound)
+        .def_readwrite("periodic", &SimBox::periodic)
+        .def_readwrite("vol", &SimBox::vol);
+    py::class_<ParticleSystem, std::shared_ptr<ParticleSystem>>(pg, "ParticleSystem")
+        .def(py::init<std::shared_ptr<SimBox>, unsigned int, py::handle, py::handle, py::handle, py::handle>())
+        .def("getMass", [](ParticleSystem& s) { return s.mass; })
+        .def("setMass", [](ParticleSystem& s, py::handle m) {
+            auto v = to_vec(m, "mass");
+            if (v.size() != s.N) throw std::invalid_argument("[ERROR]: Size of mass array mismatch with # of particles!");
+            s.mass = v; ++s.version; })
+        .def("getDiameter", [](ParticleSystem& s) { return s.diameter; })
+        .def("setDiameter", [](ParticleSystem& s, py::handle d) {
+            auto v = to_vec(d, "diameter");
+            if (v.size() != s.N) throw std::invalid_argument("[ERROR]: Size of diameter array mismatch with # of particles!");
+            s.diameter = v; ++s.version; })
+        .def("getDisplacement", [](ParticleSystem& s) { return ParticleSystem::as_nx3(s.disp); })
+        .def("setDisplacement", [](ParticleSystem& s, py::handle d) { s.disp = to_xyz(d, s.N, "displacement"); })
+        .def("setAtomPosition", [](ParticleSystem& s, py::handle p) { s.pos = to_xyz(p, s.N, "position"); ++s.version; })
+        .def("setAtomVelocity", [](ParticleSystem& s, py::handle v) { s.vel = to_xyz(v, s.N, "velocity"); ++s.version; })
+        .def("getAtomPosition", [](ParticleSystem& s) { return ParticleSystem::as_nx3(s.pos); })
+        .def("getAtomVelocity", [](ParticleSystem& s) { return ParticleSystem::as_nx3(s.vel); })
+        .def("moveParticles", [](ParticleSystem& s, py::handle p) {
+            auto d = to_xyz(p, s.N, "position");
+            for (size_t k = 0; k < d.size(); ++k) s.pos[k] += d[k];
+            ++s.version; })
+        .def("moveParticles", [](ParticleSystem& s) {
+            for (size_t k = 0; k < s.pos.size(); ++k) s.pos[k] += s.disp[k];
+            ++s.version; })
+        .def("getNeighbors", &ParticleSystem::getNeighbors)
+        .def("getNeighborsDistance", &ParticleSystem::getNeighborsDistance)
+        .def("neighborList", &ParticleSystem::neighborList)
+        .def("update", [](ParticleSystem& s, unsigned int n, py::handle d, py::handle m, py::handle p, py::handle v) {
+            s.set(n, d, m, p, v); })
+        .def_readonly("N", &ParticleSystem::N)
+        .def_readonly("simbox", &ParticleSystem::simbox);
+    py::class_<Communicator, std::shared_ptr<Communicator>>(pg, "Communicator")
+        .def(py::init<>())
+        .def("getRank", &Communicator::getRank)
+        .def("getSizeGlobal", &Communicator::getSizeGlobal)
+        .def("barrier", &Communicator::barrier)
+        .def("abort", &Communicator::abort)
+        .def("bcast", &Communicator::bcast)
+        .def("scatter_v", &Communicator::scatter_v)
+        .def("gather_v", &Communicator::gather_v)
+        .def("all_gather_v", &Communicator::all_gather_v)
+        .def("send", &Communicator::send)
+        .def("recv", &Communicator::recv);
+    py::class_<MPILogFile, std::shared_ptr<MPILogFile>>(pg, "MPILogFile")
+        .def(py::init<std::shared_ptr<Communicator>, const std::string&>())
+        .def("write_shared", &MPILogFile::write_shared)
+        .def("flush", &MPILogFile::flush)
+        .def("close", &MPILogFile::close);
+    py::class_<Manager, std::shared_ptr<Manager>>(pg, "Manager")
+        .def(py::init<>())
+        .def_readwrite("notice_level", &Manager::notice_level);
+
+    py::module pm = m.def_submodule("_potential");
+    py::class_<PairPotential, std::shared_ptr<PairPotential>>(pm, "PairPotential")
+        .def(py::init<std::vector<double>>())
+        .def(py::init<double, std::vector<double>>())
+        .def("getRcut", &PairPotential::getRcut)
+        .def("getPairForceDivR", &PairPotential::getPairForceDivR)
+        .def("getPairEnergy", &PairPotential::getPairEnergy)
+        .def("getParams", &PairPotential::getParams)
+        .def("setParams", &PairPotential::setParams)
+        .def_readwrite("scaled_rcut", &PairPotential::scaled_rcut);
+    py::class_<PairPotentialPoly12, PairPotential, std::shared_ptr<PairPotentialPoly12>>(pm, "PairPotentialPoly12")
+        .def(py::init<std::vector<double>>())
+        .def(py::init<double, std::vector<double>>());
+
+    py::module cm = m.def_submodule("_cgfunc");
+    py::class_<CoarseGrainFunction, std::shared_ptr<CoarseGrainFunction>>(cm, "CoarseGrainFunction")
+        .def(py::init<double>())
+        .def("getRcut", &CoarseGrainFunction::getRcut)
+        .def("setRcut", &CoarseGrainFunction::setRcut)
+        .def("getDeltaFunc", &CoarseGrainFunction::getDeltaFunc)
+        .def("getObjFunc", &CoarseGrainFunction::getObjFunc)
+        .def("getBondFunc", &CoarseGrainFunction::getBondFunc);
+#define FIXED(T, NAME) py::class_<T, CoarseGrainFunction, std::shared_ptr<T>>(cm, NAME).def(py::init<int, double>())
+#define ADAPT(T, NAME) \
+    py::class_<T, CoarseGrainFunction, std::shared_ptr<T>>(cm, NAME).def(py::init<int, double, double, double>())
+    FIXED(CGFixed<IK_CG_OCTIC>, "CGFuncOcticFixedPoint");
+    ADAPT(CGAdaptive<IK_CG_OCTIC>, "CGFuncOcticAdaptive");
+    FIXED(CGFixed<IK_CG_RECT>, "CGFuncRectFixedPoint");
+    ADAPT(CGAdaptive<IK_CG_RECT>, "CGFuncRectAdaptive");
+    FIXED(CGFixed<IK_CG_MOLLIFIER>, "CGFuncMollifierFixedPoint");
+    ADAPT(CGAdaptive<IK_CG_MOLLIFIER>, "CGFuncMollifierAdaptive");
+#undef FIXED
+#undef ADAPT
+    py::class_<CGGaussianFixed, CoarseGrainFunction, std::shared_ptr<CGGaussianFixed>>(cm, "CGFuncGaussianFixedPoint")
+        .def(py::init<int, double, double>(), py::arg("order"), py::arg("width"), py::arg("cut") = 3.0);
+
+    py::module im = m.def_submodule("_irvingkirkwood");
+    py::class_<IrvingKirkwood, std::shared_ptr<IrvingKirkwood>>(im, "IrvingKirkwood")
+        .def(py::init<std::shared_ptr<ParticleSystem>, std::shared_ptr<PairPotential>,
+                      std::shared_ptr<CoarseGrainFunction>, std::shared_ptr<Communicator>>())
+        .def("compute", &IrvingKirkwood::compute)
+        .def("setSystemData", &IrvingKirkwood::setSystemData)
+        .def("addObservable", &IrvingKirkwood::addObservable)
+        .def("printDisplacement", &IrvingKirkwood::printDisplacement)
+        .def("setPrecision", &IrvingKirkwood::setPrecision)
+        .def("getPrecision", &IrvingKirkwood::getPrecision)
+        .def("counters", &IrvingKirkwood::counters)
+        .def_readonly("max_rcut", &IrvingKirkwood::max_rcut);
+    py::class_<CoarseGrainedField, std::shared_ptr<CoarseGrainedField>>(im, "CoarseGrainedField")
+        .def("addGridpoints", &CoarseGrainedField::addGridpoints)
+        .def("gettostring", &CoarseGrainedField::gettostring)
+        .def("save", &CoarseGrainedField::save)
+        .def("clear", &CoarseGrainedField::clear)
+        .def("values", &CoarseGrainedField::values)
+        .def_readonly("name", &CoarseGrainedField::name)
+        .def_readonly("type", &CoarseGrainedField::type)
+        .def_readonly("islocal", &CoarseGrainedField::islocal)
+        .def_readonly("dim", &CoarseGrainedField::dim);
+#define FIELD(D, F, NAME)                                                                    \
+    py::class_<FieldT<D, F>, CoarseGrainedField, std::shared_ptr<FieldT<D, F>>>(im, NAME) \
+        .def(py::init<std::string, std::string, bool, int>())
+    FIELD(2, IK_FIELD_VIRIAL, "VirialStressField2D");
+    FIELD(3, IK_FIELD_VIRIAL, "VirialStressField3D");
+    FIELD(2, IK_FIELD_KINETIC, "KineticStressField2D");
+    FIELD(3, IK_FIELD_KINETIC, "KineticStressField3D");
+#undef FIELD
+}

@@ -1,0 +1,1050 @@
+// ik_api.cu -- C ABI of the GB300 Irving-Kirkwood engine (declared in include/ik_gb300.h):
+// context, device buffers, geometry/bin set-up and the per-frame launch sequence.
+#include "ik_kernels.h"
+#include "../../include/ik_gb300.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return fail(e_ == cudaErrorMemoryAllocation ? IK_ERR_NOMEM : IK_ERR_CUDA,     \
+                        "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                        __LINE__);                                                        \
+    } while (0)
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    ~DevBuf() { if (p) cudaFree(p); }
+    int ensure(size_t need)
+    {
+        if (need <= bytes && p) return IK_OK;
+        if (p) { cudaFree(p); p = nullptr; bytes = 0; }
+        size_t b = std::max<size_t>(need, 256);
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return fail(IK_ERR_NOMEM, "cudaMalloc(%zu) failed: %s", b, cudaGetErrorString(e));
+        }
+        bytes = b;
+        return IK_OK;
+    }
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+#define ENS(buf, n) do { int r_ = (buf).ensure(n); if (r_) return r_; } while (0)
+
+struct Slot {
+    int64_t n = 0;
+    bool has_vel = false, has_mass = false;
+    double dmax = 0.0;
+    DevBuf pos, vel, mass, diam;
+    DevBuf vir, kin;
+    int last_prec = -1, last_fields = 0;
+    DevBuf counters; // 4 x u64: bonds, pairs, triples, spare
+};
+
+struct PendingOp { int slot, prec, fields; };
+
+} // namespace
+
+struct ik_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+    int flags = 0;
+    // configuration
+    int dim = 0;
+    double boxsize[3] = {0, 0, 0}, origin[3] = {0, 0, 0};
+    bool box_set = false;
+    IkPoly12 pot{};
+    bool pot_set = false;
+    IkCG cg{};
+    bool cg_set = false;
+    IkGL gl{};
+    double cg_width_param = 0.0;
+    double max_rcut = 0.0;
+    bool max_rcut_set = false;
+    // grid
+    std::vector<double> grid_h;
+    int64_t G = 0;
+    DevBuf grid_d;
+    // geometry + binning cache
+    IkGeom geom{};
+    bool geom_valid = false;
+    int bw[3] = {1, 1, 1}, reach[3] = {0, 0, 0};
+    int nitems = 0;
+    DevBuf gpts_d, items_d;
+    // work buffers
+    DevBuf cell_of, rank, cell_count, cell_start, sorted, prec, kin, diam32;
+    DevBuf bonds32, nb32, bonds64, nb64;
+    DevBuf status, maxnb, work_counter;
+    int maxb = 0, halo_cap = 0;
+    // neighbour-query scratch
+    DevBuf q_cell_of, q_rank, q_count, q_start, q_sorted, q_cnt, q_offs, q_idx, q_flag;
+    std::vector<Slot> slots;
+    std::vector<PendingOp> pending;
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    int64_t launches = 0;
+    float timing[4] = {0, 0, 0, 0};
+};
+
+// ---------------------------------------------------------------------------
+namespace {
+
+void gl_rule(int n, double* x, double* w)
+{
+    // Newton iteration on the Legendre three-term recurrence.
+    for (int k = 0; k < n; ++k) {
+        long double z = cosl(3.14159265358979323846264338327950288L * (k + 0.75L) / (n + 0.5L));
+        long double pp = 1.0L;
+        for (int it = 0; it < 100; ++it) {
+            long double p0 = 1.0L, p1 = z;
+            for (int j = 2; j <= n; ++j) {
+                long double p2 = ((2.0L * j - 1.0L) * z * p1 - (j - 1.0L) * p0) / j;
+                p0 = p1; p1 = p2;
+            }
+            if (n == 1) { p1 = z; p0 = 1.0L; }
+            pp = n * (z * p1 - p0) / (z * z - 1.0L);
+            long double dz = p1 / pp;
+            z -= dz;
+            if (fabsl(dz) < 1e-19L) break;
+        }
+        long double p0 = 1.0L, p1 = z;
+        for (int j = 2; j <= n; ++j) {
+            long double p2 = ((2.0L * j - 1.0L) * z * p1 - (j - 1.0L) * p0) / j;
+            p0 = p1; p1 = p2;
+        }
+        if (n == 1) { p1 = z; p0 = 1.0L; }
+        pp = n * (z * p1 - p0) / (z * z - 1.0L);
+        x[n - 1 - k] = (double)z;
+        w[n - 1 - k] = (double)(2.0L / ((1.0L - z * z) * pp * pp));
+    }
+    if (n % 2 == 1) x[n / 2] = 0.0;
+}
+
+int check_ctx(ik_ctx* c)
+{
+    if (!c) return fail(IK_ERR_ARG, "null context");
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return fail(IK_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+    return IK_OK;
+}
+
+int nc_of(int dim, int c) { return c < dim ? 1 : 0; }
+
+// (Re)build the cell geometry and the grid binning for the current box, cut-offs and grid.
+int ensure_geometry(ik_ctx* c)
+{
+    if (c->geom_valid) return IK_OK;
+    IkGeom g{};
+    g.dim = c->dim;
+    const double R = c->cg.rcut;
+    for (int a = 0; a < 3; ++a) {
+        g.L[a] = c->boxsize[a];
+        g.lo[a] = -0.5 * c->boxsize[a] - c->origin[a];
+        g.periodic[a] = nc_of(c->dim, a);
+        int nc = 1;
+        if (g.periodic[a]) {
+            if (!(2.0 * c->max_rcut < g.L[a]) || !(2.0 * R < g.L[a]))
+                return fail(IK_ERR_BOX,
+                            "cut-off too large for the periodic box: max_rcut=%g, R_cg=%g, L[%d]=%g "
+                            "(need 2*cutoff < L)", c->max_rcut, R, a, g.L[a]);
+            nc = (int)std::floor(g.L[a] / c->max_rcut);
+            if (nc < 1) nc = 1;
+            if (nc > (1 << 20)) nc = 1 << 20;
+        }
+        g.nc[a] = nc;
+        g.cw[a] = g.L[a] / nc;
+        g.reach_bond[a] = 1;
+        g.all_bond[a] = (nc < 3) ? 1 : 0;
+    }
+    if (c->dim == 2) { g.lo[2] = -0.5 * c->boxsize[2] - c->origin[2]; g.cw[2] = g.L[2]; }
+    long long ncell = (long long)g.nc[0] * g.nc[1] * g.nc[2];
+    if (ncell > (1LL << 30)) return fail(IK_ERR_UNSUPPORTED, "too many cells (%lld)", ncell);
+    g.ncell = (int)ncell;
+
+    // halo reach and bin width for the FP32 gather
+    double cellvol = 1.0, boxvol = 1.0;
+    for (int a = 0; a < c->dim; ++a) { cellvol *= g.cw[a]; boxvol *= g.L[a]; }
+    double pts_per_cell = c->G > 0 ? (double)c->G * cellvol / boxvol : 1.0;
+    double target = c->dim == 2 ? 20.0 : 24.0;
+    int bwv = (int)std::lround(std::pow(std::max(target / std::max(pts_per_cell, 1e-9), 1.0), 1.0 / c->dim));
+    bwv = std::max(1, std::min(bwv, 8));
+    for (int a = 0; a < 3; ++a) {
+        if (a < c->dim) {
+            c->reach[a] = (int)std::ceil(R / g.cw[a]);
+            if (c->reach[a] < 1) c->reach[a] = 1;
+            c->bw[a] = std::min(bwv, g.nc[a]);
+        } else {
+            c->reach[a] = 0;
+            c->bw[a] = 1;
+        }
+    }
+    c->geom = g;
+
+    // ---- bin the grid points (host, once per box/grid)
+    const int D = c->dim;
+    int nb[3] = {1, 1, 1};
+    for (int a = 0; a < D; ++a) nb[a] = (g.nc[a] + c->bw[a] - 1) / c->bw[a];
+    const double spacing = std::pow(boxvol / std::max<int64_t>(c->G, 1), 1.0 / D);
+    struct Key { int64_t bin; uint64_t morton; int64_t idx; double w[3]; int cell0[3]; };
+    std::vector<Key> keys((size_t)c->G);
+    for (int64_t i = 0; i < c->G; ++i) {
+        Key k{};
+        k.idx = i;
+        int bcoord[3] = {0, 0, 0};
+        uint32_t qv[3] = {0, 0, 0};
+        for (int a = 0; a < 3; ++a) {
+            double x = c->grid_h[3 * i + a];
+            if (a < D) {
+                double t = (x - g.lo[a]) / g.L[a];
+                t -= std::floor(t);
+                double xw = g.lo[a] + t * g.L[a];
+                int cell = (int)(t * g.nc[a]);
+                cell = std::max(0, std::min(cell, g.nc[a] - 1));
+                bcoord[a] = cell / c->bw[a];
+                k.cell0[a] = bcoord[a] * c->bw[a];
+                k.w[a] = xw - (g.lo[a] + k.cell0[a] * g.cw[a]);
+                double qq = std::floor(k.w[a] / spacing);
+                qv[a] = (uint32_t)std::max(0.0, std::min(qq, 1023.0));
+            } else {
+                k.cell0[a] = 0;
+                k.w[a] = x; // non-periodic axis: absolute (2D z is 0)
+            }
+        }
+        k.bin = ((int64_t)bcoord[2] * nb[1] + bcoord[1]) * nb[0] + bcoord[0];
+        uint64_t m = 0;
+        for (int b = 0; b < 10; ++b)
+            for (int a = 0; a < D; ++a) m |= (uint64_t)((qv[a] >> b) & 1u) << (b * D + a);
+        k.morton = m;
+        keys[(size_t)i] = k;
+    }
+    std::sort(keys.begin(), keys.end(), [](const Key& x, const Key& y) {
+        if (x.bin != y.bin) return x.bin < y.bin;
+        if (x.morton != y.morton) return x.morton < y.morton;
+        return x.idx < y.idx;
+    });
+    const float kappa = c->cg.kappa;
+    std::vector<float4> gpts((size_t)std::max<int64_t>(c->G, 1));
+    for (int64_t k = 0; k < c->G; ++k) {
+        const Key& kk = keys[(size_t)k];
+        float4 v;
+        v.x = (float)(kappa * kk.w[0]);
+        v.y = (float)(kappa * kk.w[1]);
+        v.z = D == 3 ? (float)(kappa * kk.w[2]) : 0.f;
+        int gi = (int)kk.idx;
+        std::memcpy(&v.w, &gi, 4);
+        gpts[(size_t)k] = v;
+    }
+    // work items: ranges of groups inside a bin, sized for >= ~4 items per warp slot
+    int64_t nbins_used = 0;
+    for (int64_t k = 0; k < c->G; ++k) if (k == 0 || keys[(size_t)k].bin != keys[(size_t)k - 1].bin) ++nbins_used;
+    int64_t total_groups = 0;
+    {
+        int64_t s = 0;
+        for (int64_t k = 1; k <= c->G; ++k)
+            if (k == c->G || keys[(size_t)k].bin != keys[(size_t)k - 1].bin) { total_groups += (k - s + IK_P - 1) / IK_P; s = k; }
+    }
+    int64_t warps = (int64_t)c->sm_count * 16;
+    int64_t want_items = std::max<int64_t>(4 * warps, nbins_used);
+    int gi_max = (int)std::max<int64_t>(1, (total_groups + want_items - 1) / want_items);
+    std::vector<int4> items;
+    {
+        int64_t s = 0;
+        for (int64_t k = 1; k <= c->G; ++k) {
+            if (k == c->G || keys[(size_t)k].bin != keys[(size_t)k - 1].bin) {
+                const Key& kk = keys[(size_t)s];
+                for (int64_t t = s; t < k; t += (int64_t)gi_max * IK_P)
+                    items.push_back(make_int4(kk.cell0[0], kk.cell0[1], kk.cell0[2], (int)t));
+                s = k;
+            }
+        }
+        items.push_back(make_int4(0, 0, 0, (int)c->G));
+    }
+    c->nitems = (int)items.size() - 1;
+    ENS(c->gpts_d, gpts.size() * sizeof(float4));
+    ENS(c->items_d, items.size() * sizeof(int4));
+    CK(cudaMemcpy(c->gpts_d.p, gpts.data(), gpts.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->items_d.p, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    c->geom_valid = true;
+    return IK_OK;
+}
+
+int ensure_ready(ik_ctx* c)
+{
+    if (!c->box_set) return fail(IK_ERR_STATE, "box not set (ik_set_box)");
+    if (!c->pot_set) return fail(IK_ERR_STATE, "pair potential not set");
+    if (!c->cg_set) return fail(IK_ERR_STATE, "coarse-graining function not set");
+    if (c->G <= 0) return fail(IK_ERR_STATE, "grid not set (ik_set_grid)");
+    if (!c->max_rcut_set) return fail(IK_ERR_STATE, "max_rcut unknown: upload a frame or call ik_set_max_rcut");
+    return IK_OK;
+}
+
+// Cell list for a slot into (cell_of, rank, count, start, sorted) buffers.
+int build_cells(ik_ctx* c, Slot& s, const IkGeom& g, DevBuf& cell_of, DevBuf& rank, DevBuf& count,
+                DevBuf& start, DevBuf& sorted)
+{
+    int n = (int)s.n;
+    ENS(cell_of, sizeof(int) * std::max(n, 1));
+    ENS(rank, sizeof(int) * std::max(n, 1));
+    ENS(count, sizeof(int) * (g.ncell + 1));
+    ENS(start, sizeof(int) * (g.ncell + 1));
+    ENS(sorted, sizeof(int) * std::max(n, 1));
+    CK(cudaMemsetAsync(count.p, 0, sizeof(int) * (g.ncell + 1), c->stream));
+    if (n > 0) {
+        k_bin<<<(n + 255) / 256, 256, 0, c->stream>>>(s.pos.as<double>(), n, g, cell_of.as<int>(),
+                                                      rank.as<int>(), count.as<int>(), c->status.as<int>());
+        CK(cudaGetLastError());
+    }
+    k_scan<<<1, 1024, 0, c->stream>>>(count.as<int>(), g.ncell, start.as<int>());
+    CK(cudaGetLastError());
+    if (n > 0) {
+        k_scatter<<<(n + 255) / 256, 256, 0, c->stream>>>(cell_of.as<int>(), rank.as<int>(), start.as<int>(), n,
+                                                          sorted.as<int>());
+        CK(cudaGetLastError());
+    }
+    return IK_OK;
+}
+
+int slot_ok(ik_ctx* c, int slot)
+{
+    if (slot < 0 || slot >= (int)c->slots.size()) return fail(IK_ERR_ARG, "slot %d out of range", slot);
+    return IK_OK;
+}
+
+int enqueue(ik_ctx* c, int slot, int prec, int fields)
+{
+    Slot& s = c->slots[(size_t)slot];
+    const IkGeom& g = c->geom;
+    const int D = c->dim, NC = D == 2 ? 3 : 6;
+    const int n = (int)s.n;
+    bool timing = (c->flags & IK_FLAG_TIMING) != 0;
+    if (timing) CK(cudaEventRecord(c->ev[0], c->stream));
+    ENS(s.vir, sizeof(double) * NC * c->G);
+    ENS(s.kin, sizeof(double) * NC * c->G);
+    ENS(s.counters, sizeof(unsigned long long) * 4);
+    CK(cudaMemsetAsync(s.counters.p, 0, sizeof(unsigned long long) * 4, c->stream));
+    if (!(fields & IK_FIELD_KINETIC)) CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->G, c->stream));
+    if (!(fields & IK_FIELD_VIRIAL)) CK(cudaMemsetAsync(s.vir.p, 0, sizeof(double) * NC * c->G, c->stream));
+    int r = build_cells(c, s, g, c->cell_of, c->rank, c->cell_count, c->cell_start, c->sorted);
+    if (r) return r;
+    c->launches += (n > 0 ? 3 : 1) + (g.ncell > 0 ? 1 : 0) + (n > 0 ? 1 : 0) + 1; // cells, bonds, gather
+    ENS(c->prec, sizeof(IkPRec) * std::max(n, 1));
+    ENS(c->kin, sizeof(float4) * 2 * std::max(n, 1));
+    ENS(c->diam32, sizeof(float) * std::max(n, 1));
+    if (g.ncell > 0) {
+        k_cell_sort_pack<<<(g.ncell + 127) / 128, 128, 0, c->stream>>>(
+            g, c->cell_start.as<int>(), c->sorted.as<int>(), s.pos.as<double>(),
+            s.has_vel ? s.vel.as<double>() : nullptr, s.has_mass ? s.mass.as<double>() : nullptr,
+            s.diam.as<double>(), c->prec.as<IkPRec>(), c->kin.as<float4>(), c->diam32.as<float>(),
+            prec == IK_PREC_FP32 ? 1 : 0);
+        CK(cudaGetLastError());
+    }
+    if (timing) CK(cudaEventRecord(c->ev[1], c->stream));
+    unsigned long long* cnt = s.counters.as<unsigned long long>();
+    if (prec == IK_PREC_FP32) {
+        const int NV = D == 2 ? 2 : 3;
+        ENS(c->bonds32, sizeof(float4) * NV * (size_t)c->maxb * std::max(n, 1));
+        ENS(c->nb32, sizeof(int) * std::max(n, 1));
+        CK(launch_bonds32(D, g, c->pot, c->cg.kappa, n, c->prec.as<IkPRec>(), c->diam32.as<float>(),
+                          c->cell_start.as<int>(), c->bonds32.as<float4>(), c->maxb, c->nb32.as<int>(),
+                          c->status.as<int>(), c->maxnb.as<int>(), cnt, c->stream));
+        if (timing) CK(cudaEventRecord(c->ev[2], c->stream));
+        GatherArgs32 a{};
+        a.g = g;
+        for (int k = 0; k < 3; ++k) {
+            a.cws[k] = (float)(c->cg.kappa * g.cw[k]);
+            a.bw[k] = c->bw[k];
+            a.reach[k] = c->reach[k];
+        }
+        a.kappa = c->cg.kappa;
+        a.R2s = c->cg.R2s;
+        a.margin = 1e-4f * c->cg.R2s;
+        a.R2 = c->cg.rcutsq;
+        a.npairs = c->gl.npairs;
+        a.w0 = c->gl.w0;
+        for (int k = 0; k < 32; ++k) { a.xi[k] = c->gl.t[k]; a.w[k] = c->gl.wt[k]; }
+        a.prec = c->prec.as<IkPRec>();
+        a.cell_start = c->cell_start.as<int>();
+        a.nb = c->nb32.as<int>();
+        a.bonds = c->bonds32.as<float4>();
+        a.maxb = c->maxb;
+        a.kin = c->kin.as<float4>();
+        a.sorted = c->sorted.as<int>();
+        a.pos = s.pos.as<double>();
+        a.gpts = c->gpts_d.as<float4>();
+        a.grid = c->grid_d.as<double>();
+        a.items = c->items_d.as<int4>();
+        a.nitems = c->nitems;
+        a.halo_cap = c->halo_cap;
+        a.qcap = 32 * (c->maxb + 1);
+        double norm = c->cg.kind == IK_CG_MOLLIFIER ? c->cg.mollifier_norm : c->cg.norm;
+        a.vir_scale = 0.5 * norm;
+        a.kin_scale = norm;
+        a.out_vir = s.vir.as<double>();
+        a.out_kin = s.kin.as<double>();
+        a.fields = fields & (s.has_vel ? 3 : 1);
+        if ((fields & IK_FIELD_KINETIC) && !s.has_vel)
+            CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->G, c->stream));
+        a.work_counter = c->work_counter.as<int>();
+        a.status = c->status.as<int>();
+        a.cnt_pairs = cnt + 1;
+        a.cnt_triples = cnt + 2;
+        CK(cudaMemsetAsync(c->work_counter.p, 0, sizeof(int), c->stream));
+        size_t smem = (size_t)IK_WARPS_GATHER * ((size_t)c->halo_cap * 16 + (size_t)a.qcap * 4);
+        int blocks = std::min(c->nitems, c->sm_count * 2);
+        if (blocks > 0) CK(launch_gather32(a, c->cg.kind, (c->flags & IK_FLAG_NO_KAHAN) == 0, blocks, 32 * IK_WARPS_GATHER, smem, c->stream));
+    } else {
+        ENS(c->bonds64, sizeof(IkB64) * (size_t)c->maxb * std::max(n, 1));
+        ENS(c->nb64, sizeof(int) * std::max(n, 1));
+        if (n > 0) {
+            k_bonds64<<<(n + 127) / 128, 128, 0, c->stream>>>(
+                g, c->pot, n, c->sorted.as<int>(), c->cell_of.as<int>(), s.pos.as<double>(), s.diam.as<double>(),
+                c->cell_start.as<int>(), c->bonds64.as<IkB64>(), c->maxb, c->nb64.as<int>(), c->status.as<int>(),
+                c->maxnb.as<int>());
+            CK(cudaGetLastError());
+        }
+        if (timing) CK(cudaEventRecord(c->ev[2], c->stream));
+        GatherArgs64 a{};
+        a.g = g;
+        a.cg = c->cg;
+        for (int k = 0; k < 3; ++k) {
+            a.reach[k] = c->reach[k];
+            a.all[k] = (k < D && 2 * c->reach[k] + 1 >= g.nc[k]) ? 1 : 0;
+        }
+        a.nq = c->gl.n;
+        for (int k = 0; k < c->gl.n; ++k) { a.xs[k] = 0.5 + 0.5 * c->gl.x[k]; a.ws[k] = c->gl.w[k]; }
+        a.sorted = c->sorted.as<int>();
+        a.cell_start = c->cell_start.as<int>();
+        a.pos = s.pos.as<double>();
+        a.vel = s.has_vel ? s.vel.as<double>() : nullptr;
+        a.mass = s.has_mass ? s.mass.as<double>() : nullptr;
+        a.nb = c->nb64.as<int>();
+        a.bonds = c->bonds64.as<IkB64>();
+        a.maxb = c->maxb;
+        a.grid = c->grid_d.as<double>();
+        a.ngrid = c->G;
+        a.out_vir = s.vir.as<double>();
+        a.out_kin = s.kin.as<double>();
+        a.fields = fields;
+        if ((fields & IK_FIELD_KINETIC) && !s.has_vel)
+            CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->G, c->stream));
+        CK(launch_gather64(a, c->stream));
+    }
+    if (timing) CK(cudaEventRecord(c->ev[3], c->stream));
+    s.last_prec = prec;
+    s.last_fields = fields;
+    return IK_OK;
+}
+
+} // namespace
+
+// ===========================================================================
+extern "C" {
+
+const char* ik_last_error(void) { return g_err.c_str(); }
+int ik_version(void) { return 100; }
+
+int ik_create(ik_ctx** out, int device)
+{
+    if (!out) return fail(IK_ERR_ARG, "null output pointer");
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(IK_ERR_CUDA, "no CUDA device available (%s)", cudaGetErrorString(e));
+    if (device < 0 || device >= ndev) return fail(IK_ERR_ARG, "device %d out of range (%d devices)", device, ndev);
+    ik_ctx* c = new ik_ctx();
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess) { delete c; return fail(IK_ERR_CUDA, "cudaSetDevice failed"); }
+    cudaDeviceProp prop;
+    cudaGetDeviceProperties(&prop, device);
+    c->sm_count = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return fail(IK_ERR_CUDA, "cudaStreamCreate failed");
+    }
+    for (auto& ev : c->ev) cudaEventCreate(&ev);
+    c->slots.resize(1);
+    int r;
+    if ((r = c->status.ensure(sizeof(int))) || (r = c->maxnb.ensure(sizeof(int))) ||
+        (r = c->work_counter.ensure(sizeof(int)))) {
+        ik_destroy(c);
+        return r;
+    }
+    cudaMemset(c->status.p, 0, sizeof(int));
+    cudaMemset(c->maxnb.p, 0, sizeof(int));
+    *out = c;
+    return IK_OK;
+}
+
+int ik_destroy(ik_ctx* c)
+{
+    if (!c) return IK_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& ev : c->ev) if (ev) cudaEventDestroy(ev);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return IK_OK;
+}
+
+int ik_set_box(ik_ctx* c, int dim, const double boxsize[3], const double origin[3])
+{
+    if (int r = check_ctx(c)) return r;
+    if (dim != 2 && dim != 3) return fail(IK_ERR_ARG, "dim must be 2 or 3 (got %d)", dim);
+    if (!boxsize) return fail(IK_ERR_ARG, "null boxsize");
+    double b[3] = {boxsize[0], boxsize[1], boxsize[2]};
+    double o[3] = {origin ? origin[0] : 0.0, origin ? origin[1] : 0.0, origin ? origin[2] : 0.0};
+    if (dim == 2) { b[2] = 1.0; o[2] = 0.0; } // SimBox.cc:34-40
+    for (int a = 0; a < dim; ++a)
+        if (!(b[a] > 0.0) || !std::isfinite(b[a])) return fail(IK_ERR_ARG, "box edge %d must be > 0 (got %g)", a, b[a]);
+    bool same = c->box_set && c->dim == dim;
+    for (int a = 0; a < 3 && same; ++a) same = (c->boxsize[a] == b[a] && c->origin[a] == o[a]);
+    if (!same) {
+        c->dim = dim;
+        for (int a = 0; a < 3; ++a) { c->boxsize[a] = b[a]; c->origin[a] = o[a]; }
+        c->geom_valid = false;
+        c->box_set = true;
+        if (c->cg_set) { // the Gaussian normalisation depends on dim
+            int r = ik_set_cgfunc(c, c->cg.kind, c->cg.mode, c->cg.order, c->cg.rcut, c->cg_width_param);
+            if (r) return r;
+        }
+    }
+    return IK_OK;
+}
+
+int ik_set_potential_poly12(ik_ctx* c, double scaled_rcut, const double params[5])
+{
+    if (int r = check_ctx(c)) return r;
+    if (!params) return fail(IK_ERR_ARG, "null params");
+    if (!(scaled_rcut > 0.0)) return fail(IK_ERR_ARG, "scaled_rcut must be > 0");
+    c->pot.rcutsq = scaled_rcut * scaled_rcut;
+    c->pot.v0 = params[0];
+    c->pot.eps = params[1];
+    c->pot.c0 = params[2];
+    c->pot.c1 = params[3];
+    c->pot.c2 = params[4];
+    c->pot.max_rcut_sq = c->max_rcut * c->max_rcut;
+    c->pot_set = true;
+    return IK_OK;
+}
+
+int ik_set_cgfunc(ik_ctx* c, int kind, int mode, int order, double rcut, double width)
+{
+    if (int r = check_ctx(c)) return r;
+    if (kind < 0 || kind > 3) return fail(IK_ERR_ARG, "unknown coarse-graining kind %d", kind);
+    if (mode < 0 || mode > 3) return fail(IK_ERR_ARG, "unknown quadrature mode %d", mode);
+    if (!(rcut > 0.0) || !std::isfinite(rcut)) return fail(IK_ERR_ARG, "rcut must be > 0");
+    if (mode == IK_QUAD_FIXEDPOINT && (order < 1 || order > 64))
+        return fail(IK_ERR_ARG, "Gauss-Legendre order must be in [1, 64] (got %d)", order);
+    if (kind == IK_CG_GAUSSIAN && !(width > 0.0)) return fail(IK_ERR_ARG, "Gaussian width must be > 0");
+    const double PI = 3.14159265358979323846;
+    int dim = c->dim ? c->dim : 2;
+    IkCG& cg = c->cg;
+    int old_kind = cg.kind;
+    double old_rcut = cg.rcut;
+    cg.kind = kind;
+    cg.mode = mode;
+    cg.order = order;
+    cg.rcut = rcut;
+    cg.rcutsq = rcut * rcut;
+    cg.width = kind == IK_CG_GAUSSIAN ? width : 0.0;
+    c->cg_width_param = width;
+    switch (kind) {
+    case IK_CG_OCTIC: cg.norm = 15.0 / (8 * PI * cg.rcutsq); break;
+    case IK_CG_GAUSSIAN: {
+        double w2 = width * width;
+        cg.norm = dim == 3 ? 1.0 / ((2.0 * PI * w2) * std::sqrt(2.0 * PI * w2)) : 1.0 / (2.0 * PI * w2);
+        break;
+    }
+    case IK_CG_RECT: cg.norm = 1 / (PI * cg.rcutsq); break;
+    default: {
+        double rn = width > 0.0 ? width : rcut; // Mollifier keeps its construction radius
+        cg.mollifier_norm = 13.46842098743079272180855772032086697297031125109170011102 / (2.0 * PI * rn * rn);
+        cg.norm = cg.mollifier_norm;
+    }
+    }
+    if (kind == IK_CG_GAUSSIAN) {
+        cg.kappa = (float)std::sqrt(1.4426950408889634 / (2.0 * width * width));
+        cg.R2s = (float)((double)cg.kappa * cg.kappa * cg.rcutsq);
+    } else {
+        cg.kappa = (float)(1.0 / rcut);
+        cg.R2s = 1.0f;
+    }
+    if (mode == IK_QUAD_FIXEDPOINT) {
+        IkGL& gl = c->gl;
+        gl.n = order;
+        gl_rule(order, gl.x, gl.w);
+        gl.npairs = order / 2;
+        gl.w0 = (order % 2) ? (float)gl.w[order / 2] : 0.f;
+        for (int k = 0; k < 32; ++k) { gl.t[k] = 0.f; gl.wt[k] = 0.f; }
+        for (int k = 0; k < gl.npairs; ++k) {
+            gl.t[k] = (float)gl.x[order - 1 - k];
+            gl.wt[k] = (float)gl.w[order - 1 - k];
+        }
+    }
+    if (!c->cg_set || old_kind != kind || old_rcut != rcut) c->geom_valid = false;
+    if (kind == IK_CG_GAUSSIAN) c->geom_valid = false; // kappa changes gpts
+    c->cg_set = true;
+    return IK_OK;
+}
+
+int ik_set_adaptive(ik_ctx* c, int neval, double relerr, double abserr)
+{
+    if (int r = check_ctx(c)) return r;
+    c->cg.neval = neval;
+    c->cg.relerr = relerr;
+    c->cg.abserr = abserr;
+    return IK_OK;
+}
+
+int ik_set_max_rcut(ik_ctx* c, double max_rcut)
+{
+    if (int r = check_ctx(c)) return r;
+    if (!(max_rcut > 0.0) || !std::isfinite(max_rcut)) return fail(IK_ERR_ARG, "max_rcut must be > 0");
+    if (!c->max_rcut_set || c->max_rcut != max_rcut) c->geom_valid = false;
+    c->max_rcut = max_rcut;
+    c->max_rcut_set = true;
+    c->pot.max_rcut_sq = max_rcut * max_rcut;
+    return IK_OK;
+}
+
+int ik_get_max_rcut(ik_ctx* c, double* out)
+{
+    if (int r = check_ctx(c)) return r;
+    if (!out) return fail(IK_ERR_ARG, "null output");
+    if (!c->max_rcut_set) return fail(IK_ERR_STATE, "max_rcut not set yet");
+    *out = c->max_rcut;
+    return IK_OK;
+}
+
+int ik_set_grid(ik_ctx* c, int64_t g, const double* xyz)
+{
+    if (int r = check_ctx(c)) return r;
+    if (g < 0 || (g > 0 && !xyz)) return fail(IK_ERR_ARG, "bad grid arguments");
+    if (g > (int64_t)1 << 30) return fail(IK_ERR_UNSUPPORTED, "grid too large");
+    for (int64_t i = 0; i < 3 * g; ++i)
+        if (!std::isfinite(xyz[i])) return fail(IK_ERR_ARG, "grid coordinate %lld is not finite", (long long)i);
+    c->grid_h.assign(xyz, xyz + 3 * g);
+    c->G = g;
+    ENS(c->grid_d, sizeof(double) * 3 * std::max<int64_t>(g, 1));
+    if (g > 0) CK(cudaMemcpy(c->grid_d.p, xyz, sizeof(double) * 3 * g, cudaMemcpyHostToDevice));
+    c->geom_valid = false;
+    return IK_OK;
+}
+
+int ik_reserve_slots(ik_ctx* c, int nslots)
+{
+    if (int r = check_ctx(c)) return r;
+    if (nslots < 1 || nslots > 65536) return fail(IK_ERR_ARG, "nslots out of range");
+    CK(cudaStreamSynchronize(c->stream));
+    if ((int)c->slots.size() < nslots) {
+        std::vector<Slot> ns(nslots);
+        // move existing DevBufs
+        for (size_t k = 0; k < c->slots.size(); ++k) {
+            std::swap(ns[k].pos, c->slots[k].pos); std::swap(ns[k].vel, c->slots[k].vel);
+            std::swap(ns[k].mass, c->slots[k].mass); std::swap(ns[k].diam, c->slots[k].diam);
+            std::swap(ns[k].vir, c->slots[k].vir); std::swap(ns[k].kin, c->slots[k].kin);
+            std::swap(ns[k].counters, c->slots[k].counters);
+            ns[k].n = c->slots[k].n; ns[k].has_vel = c->slots[k].has_vel; ns[k].has_mass = c->slots[k].has_mass;
+            ns[k].dmax = c->slots[k].dmax; ns[k].last_prec = c->slots[k].last_prec;
+            ns[k].last_fields = c->slots[k].last_fields;
+        }
+        c->slots.swap(ns);
+    }
+    return IK_OK;
+}
+
+int ik_upload_frame(ik_ctx* c, int slot, int64_t n, const double* pos, const double* vel, const double* mass,
+                    const double* diam)
+{
+    if (int r = check_ctx(c)) return r;
+    if (int r = slot_ok(c, slot)) return r;
+    if (n < 0 || n > (1 << 26)) return fail(IK_ERR_ARG, "particle count %lld out of range", (long long)n);
+    if (n > 0 && (!pos || !diam)) return fail(IK_ERR_ARG, "positions and diameters are required");
+    if (!c->box_set) return fail(IK_ERR_STATE, "box not set (ik_set_box)");
+    double dmax = 0.0;
+    if (!c->max_rcut_set) // Calculator.h:41-45 freezes max_rcut from the first frame
+        for (int64_t i = 0; i < n; ++i) dmax = std::max(dmax, diam[i]);
+    Slot& s = c->slots[(size_t)slot];
+    ENS(s.pos, sizeof(double) * 3 * std::max<int64_t>(n, 1));
+    ENS(s.diam, sizeof(double) * std::max<int64_t>(n, 1));
+    if (n > 0) {
+        CK(cudaMemcpyAsync(s.pos.p, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(s.diam.p, diam, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    }
+    s.has_vel = vel != nullptr;
+    s.has_mass = mass != nullptr;
+    if (vel) {
+        ENS(s.vel, sizeof(double) * 3 * std::max<int64_t>(n, 1));
+        if (n > 0) CK(cudaMemcpyAsync(s.vel.p, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c->stream));
+    }
+    if (mass) {
+        ENS(s.mass, sizeof(double) * std::max<int64_t>(n, 1));
+        if (n > 0) CK(cudaMemcpyAsync(s.mass.p, mass, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    }
+    if (n > 0) { // device-side validation; reported by ik_synchronize
+        k_validate<<<(int)((n + 255) / 256), 256, 0, c->stream>>>(s.pos.as<double>(), s.diam.as<double>(), (int)n,
+                                                                  c->dim, c->status.as<int>());
+        CK(cudaGetLastError());
+    }
+    s.n = n;
+    s.dmax = dmax;
+    if (!c->max_rcut_set && n > 0 && c->pot_set) {
+        double sr = std::sqrt(c->pot.rcutsq);
+        double m = sr * dmax;
+        ik_set_max_rcut(c, m > dmax ? m : dmax); // Calculator.h:41-45
+    }
+    return IK_OK;
+}
+
+int ik_set_frame(ik_ctx* c, int64_t n, const double* pos, const double* vel, const double* mass,
+                 const double* diam)
+{
+    return ik_upload_frame(c, 0, n, pos, vel, mass, diam);
+}
+
+int ik_compute_slot(ik_ctx* c, int slot, int precision, int fields)
+{
+    if (int r = check_ctx(c)) return r;
+    if (int r = slot_ok(c, slot)) return r;
+    if (precision != IK_PREC_FP64 && precision != IK_PREC_FP32) return fail(IK_ERR_ARG, "unknown precision %d", precision);
+    if (fields < 1 || fields > 3) return fail(IK_ERR_ARG, "fields mask must be 1, 2 or 3");
+    if (int r = ensure_ready(c)) return r;
+    if (c->cg.mode != IK_QUAD_FIXEDPOINT)
+        return fail(IK_ERR_UNSUPPORTED, "quadrature mode %d is not available on the GPU path yet", c->cg.mode);
+    if (int r = ensure_geometry(c)) return r;
+    if (c->maxb == 0) c->maxb = c->dim == 2 ? IK_MAXB_2D : IK_MAXB_3D;
+    if (c->halo_cap == 0) c->halo_cap = c->dim == 2 ? 512 : 768;
+    c->pending.push_back({slot, precision, fields});
+    return enqueue(c, slot, precision, fields);
+}
+
+int ik_synchronize(ik_ctx* c)
+{
+    if (int r = check_ctx(c)) return r;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        CK(cudaStreamSynchronize(c->stream));
+        int st = 0, mx = 0;
+        CK(cudaMemcpy(&st, c->status.p, sizeof(int), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(&mx, c->maxnb.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (st == 0) { c->pending.clear(); return IK_OK; }
+        CK(cudaMemset(c->status.p, 0, sizeof(int)));
+        if (st & IK_ST_BAD_INPUT) {
+            c->pending.clear();
+            return fail(IK_ERR_ARG, "invalid frame: a position is not finite, a diameter is not > 0, or a 2D "
+                                    "frame has z != 0");
+        }
+        bool grow = false;
+        if (st & IK_ST_BOND_OVERFLOW) {
+            int nm = std::max(mx, c->maxb + 1);
+            if (nm > 63) { c->pending.clear(); return fail(IK_ERR_CAPACITY, "a particle has %d force-active bonds (max 63)", mx); }
+            c->maxb = nm;
+            grow = true;
+        }
+        if (st & IK_ST_HALO_OVERFLOW) {
+            if (c->halo_cap >= 8192) { c->pending.clear(); return fail(IK_ERR_CAPACITY, "a cell holds more particles than the halo buffer"); }
+            c->halo_cap *= 2;
+            grow = true;
+        }
+        if (!grow) { c->pending.clear(); return fail(IK_ERR_CUDA, "device status 0x%x", st); }
+        std::vector<PendingOp> ops = c->pending;
+        for (const PendingOp& op : ops)
+            if (int r = enqueue(c, op.slot, op.prec, op.fields)) { c->pending.clear(); return r; }
+    }
+    c->pending.clear();
+    return fail(IK_ERR_CAPACITY, "capacity growth did not converge");
+}
+
+int ik_compute(ik_ctx* c, int precision, int fields)
+{
+    if (int r = ik_compute_slot(c, 0, precision, fields)) return r;
+    return ik_synchronize(c);
+}
+
+int ik_get_field(ik_ctx* c, int slot, int field, double* out, int64_t count)
+{
+    if (int r = check_ctx(c)) return r;
+    if (int r = slot_ok(c, slot)) return r;
+    if (field != IK_FIELD_VIRIAL && field != IK_FIELD_KINETIC) return fail(IK_ERR_ARG, "unknown field %d", field);
+    if (int r = ik_synchronize(c)) return r;
+    Slot& s = c->slots[(size_t)slot];
+    if (s.last_prec < 0) return fail(IK_ERR_STATE, "slot %d has not been computed", slot);
+    const int D = c->dim, NC = D == 2 ? 3 : 6;
+    if (count != c->G * D * D) return fail(IK_ERR_ARG, "output needs %lld doubles (got %lld)", (long long)(c->G * D * D), (long long)count);
+    std::vector<double> tmp((size_t)(NC * c->G));
+    const DevBuf& src = field == IK_FIELD_VIRIAL ? s.vir : s.kin;
+    if (c->G > 0) CK(cudaMemcpy(tmp.data(), src.p, sizeof(double) * NC * c->G, cudaMemcpyDeviceToHost));
+    static const int map2[3][2] = {{0, 0}, {1, 1}, {0, 1}};
+    static const int map3[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+    for (int64_t g = 0; g < c->G; ++g) {
+        double* o = out + g * D * D;
+        for (int k = 0; k < NC; ++k) {
+            int a = D == 2 ? map2[k][0] : map3[k][0], b = D == 2 ? map2[k][1] : map3[k][1];
+            double v = tmp[(size_t)(g * NC + k)];
+            o[a + D * b] = v;
+            o[b + D * a] = v;
+        }
+    }
+    return IK_OK;
+}
+
+int ik_get_neighbors(ik_ctx* c, int slot, double radius, int64_t* offs, int32_t* idx, int64_t idx_capacity,
+                     int64_t* nnz)
+{
+    if (int r = check_ctx(c)) return r;
+    if (int r = slot_ok(c, slot)) return r;
+    if (!c->box_set) return fail(IK_ERR_STATE, "box not set");
+    if (!(radius > 0.0)) return fail(IK_ERR_ARG, "radius must be > 0");
+    if (!offs || !nnz) return fail(IK_ERR_ARG, "null output");
+    Slot& s = c->slots[(size_t)slot];
+    int n = (int)s.n;
+    IkGeom g{};
+    g.dim = c->dim;
+    for (int a = 0; a < 3; ++a) {
+        g.L[a] = c->boxsize[a];
+        g.lo[a] = -0.5 * c->boxsize[a] - c->origin[a];
+        g.periodic[a] = nc_of(c->dim, a);
+        int nc = 1;
+        if (g.periodic[a]) {
+            if (!(2.0 * radius < g.L[a])) return fail(IK_ERR_BOX, "radius %g >= half the box edge %g", radius, g.L[a]);
+            nc = std::max(1, (int)std::floor(g.L[a] / radius));
+        }
+        g.nc[a] = nc;
+        g.cw[a] = g.L[a] / nc;
+        g.reach_bond[a] = 1;
+        g.all_bond[a] = nc < 3 ? 1 : 0;
+    }
+    g.ncell = g.nc[0] * g.nc[1] * g.nc[2];
+    if (int r = build_cells(c, s, g, c->q_cell_of, c->q_rank, c->q_count, c->q_start, c->q_sorted)) return r;
+    if (g.ncell > 0)
+        k_cell_sort_pack<<<(g.ncell + 127) / 128, 128, 0, c->stream>>>(g, c->q_start.as<int>(), c->q_sorted.as<int>(),
+                                                                       nullptr, nullptr, nullptr, nullptr, nullptr,
+                                                                       nullptr, nullptr, 0);
+    ENS(c->q_cnt, sizeof(int) * (n + 1));
+    ENS(c->q_offs, sizeof(int) * (n + 1));
+    double r2 = radius * radius;
+    CK(launch_neigh(false, g, n, r2, c->q_sorted.as<int>(), c->q_cell_of.as<int>(), s.pos.as<double>(),
+                    c->q_start.as<int>(), c->q_cnt.as<int>(), nullptr, nullptr, c->stream));
+    k_scan<<<1, 1024, 0, c->stream>>>(c->q_cnt.as<int>(), n, c->q_offs.as<int>());
+    std::vector<int> ho((size_t)n + 1);
+    CK(cudaMemcpyAsync(ho.data(), c->q_offs.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    int64_t total = ho[(size_t)n];
+    *nnz = total;
+    for (int i = 0; i <= n; ++i) offs[i] = ho[(size_t)i];
+    if (!idx) return IK_OK;
+    if (idx_capacity < total) return fail(IK_ERR_ARG, "idx capacity %lld < %lld", (long long)idx_capacity, (long long)total);
+    ENS(c->q_idx, sizeof(int) * std::max<int64_t>(total, 1));
+    CK(launch_neigh(true, g, n, r2, c->q_sorted.as<int>(), c->q_cell_of.as<int>(), s.pos.as<double>(),
+                    c->q_start.as<int>(), nullptr, c->q_offs.as<int>(), c->q_idx.as<int>(), c->stream));
+    if (total > 0) CK(cudaMemcpyAsync(idx, c->q_idx.p, sizeof(int) * total, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return IK_OK;
+}
+
+int ik_get_neighbors_point(ik_ctx* c, int slot, const double point[3], double radius, int32_t* ids,
+                           int64_t capacity, int64_t* count)
+{
+    if (int r = check_ctx(c)) return r;
+    if (int r = slot_ok(c, slot)) return r;
+    if (!c->box_set) return fail(IK_ERR_STATE, "box not set");
+    if (!point || !count) return fail(IK_ERR_ARG, "null argument");
+    Slot& s = c->slots[(size_t)slot];
+    int n = (int)s.n;
+    IkGeom g{};
+    g.dim = c->dim;
+    for (int a = 0; a < 3; ++a) {
+        g.L[a] = c->boxsize[a];
+        g.lo[a] = -0.5 * c->boxsize[a] - c->origin[a];
+        g.periodic[a] = nc_of(c->dim, a);
+    }
+    ENS(c->q_flag, std::max(n, 1));
+    if (n > 0) {
+        k_point_query<<<(n + 255) / 256, 256, 0, c->stream>>>(g, n, s.pos.as<double>(), point[0], point[1], point[2],
+                                                             radius * radius, c->q_flag.as<unsigned char>());
+        CK(cudaGetLastError());
+    }
+    std::vector<unsigned char> f((size_t)std::max(n, 1));
+    if (n > 0) CK(cudaMemcpyAsync(f.data(), c->q_flag.p, n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    int64_t k = 0;
+    for (int i = 0; i < n; ++i)
+        if (f[(size_t)i]) {
+            if (ids && k < capacity) ids[k] = i;
+            ++k;
+        }
+    *count = k;
+    if (ids && k > capacity) return fail(IK_ERR_ARG, "capacity %lld < %lld", (long long)capacity, (long long)k);
+    return IK_OK;
+}
+
+int ik_eval_pair(ik_ctx* c, int64_t m, const double* rij, const double* di, const double* dj, double* force_divr,
+                 double* energy)
+{
+    if (int r = check_ctx(c)) return r;
+    if (!c->pot_set) return fail(IK_ERR_STATE, "pair potential not set");
+    if (m < 0 || (m > 0 && (!rij || !di || !dj || !force_divr || !energy))) return fail(IK_ERR_ARG, "bad arguments");
+    if (m == 0) return IK_OK;
+    DevBuf b;
+    ENS(b, sizeof(double) * 7 * m);
+    double* d = b.as<double>();
+    CK(cudaMemcpyAsync(d, rij, sizeof(double) * 3 * m, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(d + 3 * m, di, sizeof(double) * m, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(d + 4 * m, dj, sizeof(double) * m, cudaMemcpyHostToDevice, c->stream));
+    k_eval_pair<<<(int)((m + 127) / 128), 128, 0, c->stream>>>(c->pot, (int)m, d, d + 3 * m, d + 4 * m, d + 5 * m,
+                                                                d + 6 * m);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(force_divr, d + 5 * m, sizeof(double) * m, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(energy, d + 6 * m, sizeof(double) * m, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return IK_OK;
+}
+
+int ik_eval_bond(ik_ctx* c, int64_t m, const double* x, const double* ri, const double* rij, double* bond,
+                 double* delta)
+{
+    if (int r = check_ctx(c)) return r;
+    if (!c->cg_set) return fail(IK_ERR_STATE, "coarse-graining function not set");
+    if (c->cg.mode != IK_QUAD_FIXEDPOINT)
+        return fail(IK_ERR_UNSUPPORTED, "quadrature mode %d is not available on the GPU path yet", c->cg.mode);
+    if (m < 0 || (m > 0 && (!x || !ri || !rij || !bond || !delta))) return fail(IK_ERR_ARG, "bad arguments");
+    if (m == 0) return IK_OK;
+    DevBuf b;
+    ENS(b, sizeof(double) * 11 * m);
+    double* d = b.as<double>();
+    CK(cudaMemcpyAsync(d, x, sizeof(double) * 3 * m, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(d + 3 * m, ri, sizeof(double) * 3 * m, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(d + 6 * m, rij, sizeof(double) * 3 * m, cudaMemcpyHostToDevice, c->stream));
+    double xs[64], ws[64];
+    for (int k = 0; k < c->gl.n; ++k) { xs[k] = 0.5 + 0.5 * c->gl.x[k]; ws[k] = c->gl.w[k]; }
+    CK(launch_eval_bond(c->cg, c->dim ? c->dim : 2, xs, ws, c->gl.n, (int)m, d, d + 3 * m, d + 6 * m, d + 9 * m,
+                        d + 10 * m, c->stream));
+    CK(cudaMemcpyAsync(bond, d + 9 * m, sizeof(double) * m, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(delta, d + 10 * m, sizeof(double) * m, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return IK_OK;
+}
+
+int ik_set_flags(ik_ctx* c, int flags)
+{
+    if (int r = check_ctx(c)) return r;
+    c->flags = flags;
+    return IK_OK;
+}
+
+int ik_get_timing(ik_ctx* c, float* ms4)
+{
+    if (int r = check_ctx(c)) return r;
+    if (!ms4) return fail(IK_ERR_ARG, "null output");
+    if (!(c->flags & IK_FLAG_TIMING)) return fail(IK_ERR_STATE, "timing flag not set");
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaEventElapsedTime(&ms4[0], c->ev[0], c->ev[1]));
+    CK(cudaEventElapsedTime(&ms4[1], c->ev[1], c->ev[2]));
+    CK(cudaEventElapsedTime(&ms4[2], c->ev[2], c->ev[3]));
+    CK(cudaEventElapsedTime(&ms4[3], c->ev[0], c->ev[3]));
+    return IK_OK;
+}
+
+int ik_get_launch_count(ik_ctx* c, int64_t* out)
+{
+    if (int r = check_ctx(c)) return r;
+    if (!out) return fail(IK_ERR_ARG, "null output");
+    *out = c->launches;
+    return IK_OK;
+}
+
+int ik_get_stream(ik_ctx* c, void** stream)
+{
+    if (int r = check_ctx(c)) return r;
+    if (!stream) return fail(IK_ERR_ARG, "null output");
+    *stream = (void*)c->stream;
+    return IK_OK;
+}
+
+int ik_download_field_async(ik_ctx* c, int slot, int field, double* host_out, int64_t count)
+{
+    if (int r = check_ctx(c)) return r;
+    if (int r = slot_ok(c, slot)) return r;
+    if (field != IK_FIELD_VIRIAL && field != IK_FIELD_KINETIC) return fail(IK_ERR_ARG, "unknown field %d", field);
+    const int NC = c->dim == 2 ? 3 : 6;
+    if (!host_out || count != c->G * NC) return fail(IK_ERR_ARG, "output needs %lld doubles", (long long)(c->G * NC));
+    Slot& s = c->slots[(size_t)slot];
+    const DevBuf& src = field == IK_FIELD_VIRIAL ? s.vir : s.kin;
+    if (!src.p) return fail(IK_ERR_STATE, "slot %d has not been computed", slot);
+    if (c->G > 0) CK(cudaMemcpyAsync(host_out, src.p, sizeof(double) * NC * c->G, cudaMemcpyDeviceToHost, c->stream));
+    return IK_OK;
+}
+
+int ik_measure_fp32_peak(int device, double* tflops)
+{
+    if (!tflops) return fail(IK_ERR_ARG, "null output");
+    CK(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    CK(cudaGetDeviceProperties(&prop, device));
+    int blocks = prop.multiProcessorCount * 8, threads = 256, iters = 4096;
+    float* out = nullptr;
+    CK(cudaMalloc(&out, sizeof(float) * blocks * threads));
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    float best = 1e30f;
+    for (int rep = 0; rep < 5; ++rep) {
+        cudaEventRecord(a);
+        cudaError_t e = launch_fma_probe(blocks, threads, iters, out);
+        cudaEventRecord(b);
+        cudaEventSynchronize(b);
+        if (e != cudaSuccess) { cudaFree(out); return fail(IK_ERR_CUDA, "probe launch: %s", cudaGetErrorString(e)); }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        if (rep > 0 && ms < best) best = ms; // first launch is warm-up
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(out);
+    double flop = 2.0 * IK_FMA_PROBE_CHAINS * (double)iters * blocks * threads;
+    *tflops = flop / (best * 1e-3) / 1e12;
+    return IK_OK;
+}
+
+int ik_get_counters(ik_ctx* c, int slot, int64_t* out3)
+{
+    if (int r = check_ctx(c)) return r;
+    if (int r = slot_ok(c, slot)) return r;
+    if (!out3) return fail(IK_ERR_ARG, "null output");
+    if (int r = ik_synchronize(c)) return r;
+    Slot& s = c->slots[(size_t)slot];
+    unsigned long long h[4] = {0, 0, 0, 0};
+    if (s.counters.p) CK(cudaMemcpy(h, s.counters.p, sizeof h, cudaMemcpyDeviceToHost));
+    out3[0] = (int64_t)h[0];
+    out3[1] = (int64_t)h[1];
+    out3[2] = (int64_t)h[2];
+    return IK_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,396 @@
+// ik_cells.cu -- cell list (counting sort), FP32/FP64 force-active bond lists and the
+// bit-exact FP64 candidate neighbour list.
+//
+// Replaces the Aboria cell list and its two radius searches in
+// IrvingKirkwood::compute (irvingkirkwood/IrvingKirkwood.h:80-95) and
+// ParticleSystem::init_neighbour_search (ParticleSystem.cc:13).
+#include "ik_common.cuh"
+#include "ik_kernels.h"
+
+// ---------------------------------------------------------------------------
+// 1. cell id + rank within the cell (atomic, order fixed later by k_cell_sort)
+__global__ void k_bin(const double* __restrict__ pos, int n, IkGeom g, int* __restrict__ cell_of,
+                      int* __restrict__ rank, int* __restrict__ cell_count, int* __restrict__ status)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+    if (!(isfinite(x) && isfinite(y) && isfinite(z))) atomicOr(status, IK_ST_BAD_INPUT);
+    int cx = ik_cell_coord(g, 0, x);
+    int cy = ik_cell_coord(g, 1, y);
+    int cz = g.dim == 3 ? ik_cell_coord(g, 2, z) : 0;
+    int c = (cz * g.nc[1] + cy) * g.nc[0] + cx;
+    cell_of[i] = c;
+    rank[i] = atomicAdd(&cell_count[c], 1);
+}
+
+// 2. exclusive scan of n ints into out[0..n] (single CTA of 1024 threads; tiles of
+//    4096 with a running carry).  Used for cell starts and neighbour offsets.
+__global__ void __launch_bounds__(1024) k_scan(const int* __restrict__ in, int n, int* __restrict__ out)
+{
+    __shared__ int wsum[32];
+    __shared__ int carry_s;
+    int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) carry_s = 0;
+    __syncthreads();
+    for (int base = 0; base < n; base += 4096) {
+        int v[4], s = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            int idx = base + tid * 4 + k;
+            v[k] = idx < n ? in[idx] : 0;
+            s += v[k];
+        }
+        int incl = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) wsum[wid] = incl;
+        __syncthreads();
+        if (wid == 0) {
+            int w = wsum[lane];
+            int wi = w;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int t = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= o) wi += t;
+            }
+            wsum[lane] = wi - w; // exclusive warp offsets
+        }
+        __syncthreads();
+        int run = carry_s + wsum[wid] + incl - s;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            int idx = base + tid * 4 + k;
+            if (idx < n) out[idx] = run;
+            run += v[k];
+        }
+        __syncthreads();
+        if (tid == 1023) carry_s = run;
+        __syncthreads();
+    }
+    if (tid == 0) out[n] = carry_s;
+}
+
+// 3. scatter particle ids into cell order
+__global__ void k_scatter(const int* __restrict__ cell_of, const int* __restrict__ rank,
+                          const int* __restrict__ cell_start, int n, int* __restrict__ sorted)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    sorted[cell_start[cell_of[i]] + rank[i]] = i;
+}
+
+// 4. per cell: sort ids ascending (deterministic order), then write the FP32
+//    particle records, kinetic coefficients and FP32 diameters in sorted order.
+__global__ void k_cell_sort_pack(IkGeom g, const int* __restrict__ cell_start, int* __restrict__ sorted,
+                                 const double* __restrict__ pos, const double* __restrict__ vel,
+                                 const double* __restrict__ mass, const double* __restrict__ diam,
+                                 IkPRec* __restrict__ prec, float4* __restrict__ kin,
+                                 float* __restrict__ diam32, int want_pack)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.ncell) return;
+    int s = cell_start[c], e = cell_start[c + 1];
+    for (int a = s + 1; a < e; ++a) { // insertion sort (cells hold a handful of particles)
+        int v = sorted[a], b = a - 1;
+        while (b >= s && sorted[b] > v) { sorted[b + 1] = sorted[b]; --b; }
+        sorted[b + 1] = v;
+    }
+    if (!want_pack) return;
+    int cx = c % g.nc[0], cy = (c / g.nc[0]) % g.nc[1], cz = c / (g.nc[0] * g.nc[1]);
+    double ox = g.lo[0] + cx * g.cw[0], oy = g.lo[1] + cy * g.cw[1], oz = g.lo[2] + cz * g.cw[2];
+    for (int p = s; p < e; ++p) {
+        int i = sorted[p];
+        double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+        x -= g.L[0] * floor((x - g.lo[0]) / g.L[0]);
+        y -= g.L[1] * floor((y - g.lo[1]) / g.L[1]);
+        if (g.dim == 3) z -= g.L[2] * floor((z - g.lo[2]) / g.L[2]);
+        IkPRec r;
+        r.x = (float)(x - ox);
+        r.y = (float)(y - oy);
+        r.z = g.dim == 3 ? (float)(z - oz) : 0.0f;
+        r.cell = c;
+        prec[p] = r;
+        double m = mass ? mass[i] : 1.0;
+        double vx = vel ? vel[3 * i] : 0.0, vy = vel ? vel[3 * i + 1] : 0.0, vz = vel ? vel[3 * i + 2] : 0.0;
+        if (g.dim == 2) {
+            kin[p] = make_float4((float)(m * vx * vx), (float)(m * vy * vy), (float)(m * vx * vy), 0.f);
+        } else {
+            kin[2 * p] = make_float4((float)(m * vx * vx), (float)(m * vy * vy), (float)(m * vz * vz),
+                                     (float)(m * vx * vy));
+            kin[2 * p + 1] = make_float4((float)(m * vx * vz), (float)(m * vy * vz), 0.f, 0.f);
+        }
+        diam32[p] = (float)diam[i];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Stencil enumeration shared by the bond builders.  For axis c: if all_bond[c]
+// the axis is scanned once over all its cells (offset computed per pair by the
+// minimum image), else offsets -reach..+reach around the home cell.
+struct StencilAxis { int lo, hi, all; };
+__device__ __forceinline__ StencilAxis ik_axis(const IkGeom& g, int c, int home)
+{
+    StencilAxis a;
+    if (g.nc[c] == 1) { a.lo = 0; a.hi = 0; a.all = 1; return a; }
+    if (g.all_bond[c]) { a.lo = 0; a.hi = g.nc[c] - 1; a.all = 1; return a; }
+    a.lo = home - g.reach_bond[c]; a.hi = home + g.reach_bond[c]; a.all = 0;
+    return a;
+}
+
+// 5a. FP32 force-active bond records (tuned path).  One thread per sorted particle.
+//     Record (float4 x NV): 2D {hbx,hby,hh,cxx} {cyy,cxy,-,-}; 3D {hbx,hby,hbz,hh}
+//     {cxx,cyy,czz,cxy} {cxz,cyz,-,-}; hb = kappa*r_ij/2 (scaled half bond),
+//     hh = |hb|^2, c = 0.5*forceDivR*r_ij(x)r_ij (unscaled), r_ij = r_j - r_i.
+template <int DIM>
+__global__ void k_bonds32(IkGeom g, IkPoly12 pot, float kappa, int n,
+                          const IkPRec* __restrict__ prec, const float* __restrict__ diam32,
+                          const int* __restrict__ cell_start, float4* __restrict__ bonds, int maxb,
+                          int* __restrict__ nb, int* __restrict__ status, int* __restrict__ maxnb,
+                          unsigned long long* __restrict__ nbond_total)
+{
+    constexpr int NV = DIM == 2 ? 2 : 3;
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = p < n;
+    int cnt = 0;
+    if (valid) {
+    IkPRec me = prec[p];
+    int c = me.cell;
+    int cx = c % g.nc[0], cy = (c / g.nc[0]) % g.nc[1], cz = c / (g.nc[0] * g.nc[1]);
+    float di = diam32[p];
+    float cw0 = (float)g.cw[0], cw1 = (float)g.cw[1], cw2 = (float)g.cw[2];
+    float L0 = (float)g.L[0], L1 = (float)g.L[1], L2 = (float)g.L[2];
+    float rc2 = (float)pot.rcutsq, mr2 = (float)pot.max_rcut_sq;
+    float eps = (float)pot.eps, v12 = (float)(12.0 * pot.v0), c1x2 = (float)(2.0 * pot.c1),
+          c2x4 = (float)(4.0 * pot.c2);
+    StencilAxis az = ik_axis(g, 2, cz), ay = ik_axis(g, 1, cy), ax = ik_axis(g, 0, cx);
+    for (int zz = az.lo; zz <= az.hi; ++zz) {
+        int wz = DIM == 3 ? ik_wrap(zz, g.nc[2]) : 0;
+        for (int yy = ay.lo; yy <= ay.hi; ++yy) {
+            int wy = ik_wrap(yy, g.nc[1]);
+            for (int xx = ax.lo; xx <= ax.hi; ++xx) {
+                int wx = ik_wrap(xx, g.nc[0]);
+                int cell = (wz * g.nc[1] + wy) * g.nc[0] + wx;
+                float ox = (xx - cx) * cw0, oy = (yy - cy) * cw1, oz = (zz - cz) * cw2;
+                int e = cell_start[cell + 1];
+                for (int q = cell_start[cell]; q < e; ++q) {
+                    if (q == p) continue;
+                    IkPRec o = prec[q];
+                    float bx = ox + (o.x - me.x), by = oy + (o.y - me.y), bz = DIM == 3 ? oz + (o.z - me.z) : 0.f;
+                    if (ax.all) bx -= L0 * rintf(bx / L0);
+                    if (ay.all) by -= L1 * rintf(by / L1);
+                    if (DIM == 3 && az.all) bz -= L2 * rintf(bz / L2);
+                    float r2 = bx * bx + by * by + bz * bz;
+                    if (!(r2 < mr2)) continue;
+                    float dj = diam32[q];
+                    float sig = 0.5f * (di + dj) * (1.f - eps * fabsf(di - dj));
+                    float s2 = sig * sig;
+                    if (!(r2 < rc2 * s2)) continue;
+                    float r2inv = s2 / r2;
+                    float r6 = r2inv * r2inv * r2inv;
+                    float f = (v12 * r2inv * r6 * r6 - c1x2 - c2x4 * (r2 / s2)) / s2;
+                    if (cnt < maxb) {
+                        float4* rec = bonds + ((size_t)p * maxb + cnt) * NV;
+                        float hf = 0.5f * f;
+                        float hx = 0.5f * kappa * bx, hy = 0.5f * kappa * by, hz = 0.5f * kappa * bz;
+                        if (DIM == 2) {
+                            rec[0] = make_float4(hx, hy, hx * hx + hy * hy, hf * bx * bx);
+                            rec[1] = make_float4(hf * by * by, hf * bx * by, 0.f, 0.f);
+                        } else {
+                            rec[0] = make_float4(hx, hy, hz, hx * hx + hy * hy + hz * hz);
+                            rec[1] = make_float4(hf * bx * bx, hf * by * by, hf * bz * bz, hf * bx * by);
+                            rec[2] = make_float4(hf * bx * bz, hf * by * bz, 0.f, 0.f);
+                        }
+                    }
+                    ++cnt;
+                }
+            }
+        }
+    }
+    nb[p] = cnt < maxb ? cnt : maxb;
+    if (cnt > maxb) atomicOr(status, IK_ST_BOND_OVERFLOW);
+    atomicMax(maxnb, cnt);
+    } // valid
+    // warp-aggregated count of force-active directed bonds
+    unsigned v = __reduce_add_sync(0xffffffffu, (unsigned)cnt);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(nbond_total, (unsigned long long)v);
+}
+cudaError_t launch_bonds32(int dim, IkGeom g, IkPoly12 pot, float kappa, int n, const IkPRec* prec,
+                          const float* diam32, const int* cell_start, float4* bonds, int maxb, int* nb,
+                          int* status, int* maxnb, unsigned long long* nbond_total, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    int blocks = (n + 127) / 128;
+    if (dim == 2)
+        k_bonds32<2><<<blocks, 128, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, bonds, maxb, nb, status,
+                                              maxnb, nbond_total);
+    else
+        k_bonds32<3><<<blocks, 128, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, bonds, maxb, nb, status,
+                                              maxnb, nbond_total);
+    return cudaGetLastError();
+}
+
+// 5b. FP64 force-active bond records (plain path): {rij.x, rij.y, rij.z, forceDivR}
+//     in sorted-particle order, bit-identical selection to the oracle.
+__global__ void k_bonds64(IkGeom g, IkPoly12 pot, int n, const int* __restrict__ sorted,
+                          const int* __restrict__ cell_of, const double* __restrict__ pos,
+                          const double* __restrict__ diam, const int* __restrict__ cell_start,
+                          IkB64* __restrict__ bonds, int maxb, int* __restrict__ nb,
+                          int* __restrict__ status, int* __restrict__ maxnb)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    int i = sorted[p];
+    int c = cell_of[i];
+    int cx = c % g.nc[0], cy = (c / g.nc[0]) % g.nc[1], cz = c / (g.nc[0] * g.nc[1]);
+    double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2], di = diam[i];
+    int cnt = 0;
+    StencilAxis az = ik_axis(g, 2, cz), ay = ik_axis(g, 1, cy), ax = ik_axis(g, 0, cx);
+    for (int zz = az.lo; zz <= az.hi; ++zz) {
+        int wz = g.dim == 3 ? ik_wrap(zz, g.nc[2]) : 0;
+        for (int yy = ay.lo; yy <= ay.hi; ++yy) {
+            int wy = ik_wrap(yy, g.nc[1]);
+            for (int xx = ax.lo; xx <= ax.hi; ++xx) {
+                int wx = ik_wrap(xx, g.nc[0]);
+                int cell = (wz * g.nc[1] + wy) * g.nc[0] + wx;
+                int e = cell_start[cell + 1];
+                for (int q = cell_start[cell]; q < e; ++q) {
+                    int j = sorted[q];
+                    if (j == i) continue;
+                    double dx = ik_minimg(__dsub_rn(pos[3 * j], xi), g.L[0], g.periodic[0]);
+                    double dy = ik_minimg(__dsub_rn(pos[3 * j + 1], yi), g.L[1], g.periodic[1]);
+                    double dz = ik_minimg(__dsub_rn(pos[3 * j + 2], zi), g.L[2], g.periodic[2]);
+                    double rsq = ik_dot3(dx, dy, dz);
+                    if (!(rsq < pot.max_rcut_sq)) continue;
+                    double sig = ik_sigma64(pot, di, diam[j]);
+                    if (!ik_active64(pot, rsq, sig)) continue;
+                    double f = ik_force64(pot, rsq, sig);
+                    if (cnt < maxb) bonds[(size_t)p * maxb + cnt] = make_ikb64(dx, dy, dz, f);
+                    ++cnt;
+                }
+            }
+        }
+    }
+    nb[p] = cnt < maxb ? cnt : maxb;
+    if (cnt > maxb) atomicOr(status, IK_ST_BOND_OVERFLOW);
+    atomicMax(maxnb, cnt);
+}
+
+// ---------------------------------------------------------------------------
+// 6. Candidate neighbour list (FP64, |r_ij|^2 < radius^2, j != i), CSR by
+//    original particle id; count pass, scan, fill pass, per-row sort.
+template <bool FILL>
+__global__ void k_neigh(IkGeom g, int n, double r2cut, const int* __restrict__ sorted,
+                        const int* __restrict__ cell_of, const double* __restrict__ pos,
+                        const int* __restrict__ cell_start, int* __restrict__ count,
+                        const int* __restrict__ offs, int* __restrict__ idx)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int c = cell_of[i];
+    int cx = c % g.nc[0], cy = (c / g.nc[0]) % g.nc[1], cz = c / (g.nc[0] * g.nc[1]);
+    double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
+    int cnt = 0, base = FILL ? offs[i] : 0;
+    StencilAxis az = ik_axis(g, 2, cz), ay = ik_axis(g, 1, cy), ax = ik_axis(g, 0, cx);
+    for (int zz = az.lo; zz <= az.hi; ++zz) {
+        int wz = g.dim == 3 ? ik_wrap(zz, g.nc[2]) : 0;
+        for (int yy = ay.lo; yy <= ay.hi; ++yy) {
+            int wy = ik_wrap(yy, g.nc[1]);
+            for (int xx = ax.lo; xx <= ax.hi; ++xx) {
+                int wx = ik_wrap(xx, g.nc[0]);
+                int cell = (wz * g.nc[1] + wy) * g.nc[0] + wx;
+                int e = cell_start[cell + 1];
+                for (int q = cell_start[cell]; q < e; ++q) {
+                    int j = sorted[q];
+                    if (j == i) continue;
+                    double dx = ik_minimg(__dsub_rn(pos[3 * j], xi), g.L[0], g.periodic[0]);
+                    double dy = ik_minimg(__dsub_rn(pos[3 * j + 1], yi), g.L[1], g.periodic[1]);
+                    double dz = ik_minimg(__dsub_rn(pos[3 * j + 2], zi), g.L[2], g.periodic[2]);
+                    if (ik_dot3(dx, dy, dz) < r2cut) {
+                        if (FILL) idx[base + cnt] = j;
+                        ++cnt;
+                    }
+                }
+            }
+        }
+    }
+    if (!FILL) { count[i] = cnt; return; }
+    int* row = idx + base;
+    for (int a = 1; a < cnt; ++a) {
+        int v = row[a], b = a - 1;
+        while (b >= 0 && row[b] > v) { row[b + 1] = row[b]; --b; }
+        row[b + 1] = v;
+    }
+}
+cudaError_t launch_neigh(bool fill, IkGeom g, int n, double r2cut, const int* sorted, const int* cell_of,
+                         const double* pos, const int* cell_start, int* count, const int* offs, int* idx,
+                         cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    int blocks = (n + 127) / 128;
+    if (fill) k_neigh<true><<<blocks, 128, 0, st>>>(g, n, r2cut, sorted, cell_of, pos, cell_start, count, offs, idx);
+    else k_neigh<false><<<blocks, 128, 0, st>>>(g, n, r2cut, sorted, cell_of, pos, cell_start, count, offs, idx);
+    return cudaGetLastError();
+}
+
+// 7. particles within radius of a point (flag per particle, FP64 min-image)
+__global__ void k_point_query(IkGeom g, int n, const double* __restrict__ pos, double px, double py,
+                              double pz, double r2cut, unsigned char* __restrict__ flag)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double dx = ik_minimg(__dsub_rn(px, pos[3 * i]), g.L[0], g.periodic[0]);
+    double dy = ik_minimg(__dsub_rn(py, pos[3 * i + 1]), g.L[1], g.periodic[1]);
+    double dz = ik_minimg(__dsub_rn(pz, pos[3 * i + 2]), g.L[2], g.periodic[2]);
+    flag[i] = ik_dot3(dx, dy, dz) < r2cut ? 1 : 0;
+}
+
+// 8. scalar evaluations for the Python-facing getPairForceDivR / getBondFunc
+__global__ void k_eval_pair(IkPoly12 pot, int m, const double* __restrict__ rij, const double* __restrict__ di,
+                            const double* __restrict__ dj, double* __restrict__ f, double* __restrict__ en)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m) return;
+    double rsq = ik_dot3(rij[3 * k], rij[3 * k + 1], rij[3 * k + 2]);
+    double sig = ik_sigma64(pot, di[k], dj[k]);
+    bool act = ik_active64(pot, rsq, sig);
+    f[k] = act ? ik_force64(pot, rsq, sig) : 0.0;
+    en[k] = act ? ik_energy64(pot, rsq, sig) : 0.0;
+}
+
+// 9. FP32 FMA throughput probe: IK_FMA_PROBE_CHAINS independent FFMA chains per thread.
+__global__ void __launch_bounds__(256) k_fma_probe(int iters, float* out)
+{
+    float a[IK_FMA_PROBE_CHAINS];
+    float m = 1.0f + 1e-7f * threadIdx.x, c = 1e-7f;
+#pragma unroll
+    for (int k = 0; k < IK_FMA_PROBE_CHAINS; ++k) a[k] = (float)k * 1e-3f;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int k = 0; k < IK_FMA_PROBE_CHAINS; ++k) a[k] = fmaf(a[k], m, c);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < IK_FMA_PROBE_CHAINS; ++k) s += a[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+cudaError_t launch_fma_probe(int blocks, int threads, int iters, float* out)
+{
+    k_fma_probe<<<blocks, threads>>>(iters, out);
+    return cudaGetLastError();
+}
+
+// 10. frame validation at upload: finite positions, diameters > 0, z == 0 in 2D
+__global__ void k_validate(const double* __restrict__ pos, const double* __restrict__ diam, int n, int dim,
+                           int* __restrict__ status)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2], d = diam[i];
+    bool ok = isfinite(x) && isfinite(y) && isfinite(z) && isfinite(d) && d > 0.0 && (dim == 3 || z == 0.0);
+    if (!ok) atomicOr(status, IK_ST_BAD_INPUT);
+}

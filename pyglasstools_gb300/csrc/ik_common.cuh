@@ -1,0 +1,170 @@
+// ik_common.cuh -- shared device/host definitions of the GB300 Irving-Kirkwood engine.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define IK_MAXB_2D 16   // default force-active bonds per particle (grows on overflow)
+#define IK_MAXB_3D 32
+#define IK_WARPS_GATHER 8
+#define IK_P 4          // grid points per warp group in the FP32 gather
+
+// device status word bits (ctx->d_status)
+#define IK_ST_BOND_OVERFLOW 1
+#define IK_ST_HALO_OVERFLOW 2
+#define IK_ST_BAD_INPUT     4
+#define IK_ST_NEIGH_OVERFLOW 8
+
+// Box + cell grid.  Cells tile [lo, lo+L) per axis; nc[c] = 1 on non-periodic axes.
+struct IkGeom {
+    int dim;
+    int nc[3];
+    int ncell;
+    int reach_bond[3];   // stencil half-width for the bond search (cells)
+    int all_bond[3];     // 1: stencil covers the whole axis once
+    double L[3], lo[3], cw[3];
+    int periodic[3];
+};
+
+struct IkPoly12 {
+    double rcutsq;       // scaled_rcut^2
+    double v0, eps, c0, c1, c2;
+    double max_rcut_sq;
+};
+
+// Coarse-graining function, in the two forms the kernels use.
+struct IkCG {
+    int kind;            // IK_CG_*
+    int mode;            // IK_QUAD_*
+    int order;           // GL points
+    double rcut, rcutsq, width;
+    double norm;         // prefactor of Delta (Gaussian: (2 pi w^2)^(-d/2), octic 15/(8 pi R^2), ...)
+    // FP32 tuned path works in scaled coordinates u = kappa * x:
+    //   Gaussian: kappa = sqrt(log2(e) / (2 w^2)), Delta = norm * 2^(-|u|^2), cut |u|^2 < R2s
+    //   others:   kappa = 1/R, q = |u|^2 in [0,1)
+    float kappa;
+    float R2s;           // scaled squared support radius
+    double mollifier_norm;
+    // adaptive
+    int neval;
+    double relerr, abserr;
+};
+
+// GL nodes on [-1,1] (ascending) and weights, FP64 + FP32 copies (max 64 points).
+struct IkGL {
+    int n;
+    double x[64], w[64];
+    float t[32], wt[32];   // symmetric form: t_k = x_k/2 for the positive half, weights
+    float w0;              // centre weight (odd n), else 0
+    int npairs;
+};
+
+// ---------------------------------------------------------------------------
+// FP64 helpers with explicit rounding (no contraction) so the neighbour and
+// selection tests are bit-identical to the CPU oracle (compiled with
+// -ffp-contract=off).
+__device__ __forceinline__ double ik_minimg(double d, double L, int periodic)
+{
+    if (periodic) {
+        double k = rint(__ddiv_rn(d, L));
+        d = __dsub_rn(d, __dmul_rn(L, k));
+    }
+    return d;
+}
+
+__device__ __forceinline__ double ik_dot2(double a, double b)
+{
+    return __dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b));
+}
+__device__ __forceinline__ double ik_dot3(double a, double b, double c)
+{
+    return __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c));
+}
+
+// Polydisperse12::computeForceDivR in FP64, evaluation order of the reference
+// (potential/Polydisperse12.h:38-55), explicit rounding.
+__device__ __forceinline__ double ik_sigma64(const IkPoly12& p, double di, double dj)
+{
+    return __dmul_rn(__dmul_rn(0.5, __dadd_rn(di, dj)),
+                     __dsub_rn(1.0, __dmul_rn(p.eps, fabs(__dsub_rn(di, dj)))));
+}
+__device__ __forceinline__ bool ik_active64(const IkPoly12& p, double rsq, double sigma)
+{
+    double actual = __dmul_rn(__dmul_rn(p.rcutsq, sigma), sigma);
+    return rsq < actual;
+}
+__device__ __forceinline__ double ik_force64(const IkPoly12& p, double rsq, double sigma)
+{
+    double s2 = __dmul_rn(sigma, sigma);
+    double r2inv = __dmul_rn(__ddiv_rn(1.0, rsq), s2);
+    double rs = __ddiv_rn(rsq, s2);
+    double r6inv = __dmul_rn(__dmul_rn(r2inv, r2inv), r2inv);
+    double t = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(12.0, p.v0), r2inv), r6inv), r6inv);
+    t = __dsub_rn(t, __dmul_rn(2.0, p.c1));
+    t = __dsub_rn(t, __dmul_rn(__dmul_rn(4.0, p.c2), rs));
+    return __ddiv_rn(t, s2);
+}
+__device__ __forceinline__ double ik_energy64(const IkPoly12& p, double rsq, double sigma)
+{
+    double s2 = __dmul_rn(sigma, sigma);
+    double r2inv = __dmul_rn(__ddiv_rn(1.0, rsq), s2);
+    double rs = __ddiv_rn(rsq, s2);
+    double r6inv = __dmul_rn(__dmul_rn(r2inv, r2inv), r2inv);
+    double t = __dmul_rn(__dmul_rn(p.v0, r6inv), r6inv);
+    t = __dadd_rn(t, p.c0);
+    t = __dadd_rn(t, __dmul_rn(p.c1, rs));
+    t = __dadd_rn(t, __dmul_rn(__dmul_rn(p.c2, rs), rs));
+    return t;
+}
+
+// Coarse-graining kernels in FP64 (CGFuncOctic.h:16-29, CGFuncRect.h,
+// CGFuncMollifier.h; Gaussian added).  Returns Delta(dr_sq).
+__device__ __forceinline__ double ik_delta64(const IkCG& cg, double dr_sq)
+{
+    if (!(dr_sq < cg.rcutsq)) return 0.0;
+    switch (cg.kind) {
+    case 0: { // octic
+        double r4 = dr_sq * dr_sq / (cg.rcutsq * cg.rcutsq);
+        double r8 = r4 * r4;
+        return cg.norm * (1 - 2 * r4 + r8);
+    }
+    case 1: // gaussian
+        return cg.norm * exp(-dr_sq / (2.0 * cg.width * cg.width));
+    case 2: // rect
+        return cg.norm;
+    default: { // mollifier
+        double r2 = dr_sq / cg.rcutsq;
+        return cg.mollifier_norm * exp(-1.0 / (1 - r2));
+    }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// cell coordinate of a position along axis c (wrapped into [0, nc))
+__device__ __forceinline__ int ik_cell_coord(const IkGeom& g, int c, double x)
+{
+    if (g.nc[c] == 1) return 0;
+    double t = (x - g.lo[c]) / g.L[c];
+    t -= floor(t);
+    int k = (int)(t * g.nc[c]);
+    return k < 0 ? 0 : (k >= g.nc[c] ? g.nc[c] - 1 : k);
+}
+
+__device__ __forceinline__ int ik_wrap(int k, int n)
+{
+    k %= n;
+    return k < 0 ? k + n : k;
+}
+
+// Particle record of the FP32 path, in cell-sorted order (16 bytes): position
+// relative to the lower corner of its cell (unscaled), and the linear cell index.
+struct __align__(16) IkPRec {
+    float x, y, z;
+    int cell;
+};
+
+// FP64 bond record of the plain path: r_ij and forceDivR.
+struct __align__(16) IkB64 { double x, y, z, w; };
+__host__ __device__ __forceinline__ IkB64 make_ikb64(double x, double y, double z, double w)
+{
+    IkB64 b; b.x = x; b.y = y; b.z = z; b.w = w; return b;
+}

@@ -1,0 +1,150 @@
+// ik_gather64.cu -- the plain FP64 Irving-Kirkwood gather (one thread per grid
+// point) and scalar bond-integral evaluation.
+//
+// Straight FP64 restatement of IrvingKirkwood::compute
+// (irvingkirkwood/IrvingKirkwood.h:74-110): per grid point, particles i with
+// |x - r_i| < R (minimum image, ri = x - dx), kinetic term m v(x)v Delta(x - ri),
+// and for each force-active bond (i, j) the Gauss-Legendre bond integral of
+// FixedPointCGFunc::getBondFunc (cgfunc/CoarseGrainFunction.h:85-88) times
+// 0.5 * forceDivR * r_ij (x) r_ij (ListofCommonObservables.h:57-81).
+#include "ik_kernels.h"
+
+__device__ __forceinline__ double ik_bond64(const IkCG& cg, const double* xs, const double* ws, int nq,
+                                            const double x[3], const double ri[3], const double rij[3])
+{
+    double acc = 0.0;
+    for (int k = 0; k < nq; ++k) {
+        double s = xs[k];
+        double p0 = ri[0] + s * rij[0], p1 = ri[1] + s * rij[1], p2 = ri[2] + s * rij[2];
+        double d0 = x[0] - p0, d1 = x[1] - p1, d2 = x[2] - p2;
+        acc += ws[k] * ik_delta64(cg, d0 * d0 + d1 * d1 + d2 * d2);
+    }
+    return 0.5 * acc;
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(128) k_gather64(const GatherArgs64 a)
+{
+    constexpr int NC = DIM == 2 ? 3 : 6;
+    int64_t gidx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gidx >= a.ngrid) return;
+    const IkGeom& g = a.g;
+    double x[3] = {a.grid[3 * gidx], a.grid[3 * gidx + 1], a.grid[3 * gidx + 2]};
+    double vir[NC], kin[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) { vir[c] = 0.0; kin[c] = 0.0; }
+    const double R2 = a.cg.rcutsq;
+    int home[3], lo[3], hi[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if (c >= DIM || g.nc[c] == 1) { lo[c] = hi[c] = 0; home[c] = 0; continue; }
+        home[c] = ik_cell_coord(g, c, x[c]);
+        if (a.all[c]) { lo[c] = 0; hi[c] = g.nc[c] - 1; }
+        else { lo[c] = home[c] - a.reach[c]; hi[c] = home[c] + a.reach[c]; }
+    }
+    const bool want_kin = (a.fields & 2) && a.vel;
+    for (int zz = lo[2]; zz <= hi[2]; ++zz) {
+        int wz = DIM == 3 ? ik_wrap(zz, g.nc[2]) : 0;
+        for (int yy = lo[1]; yy <= hi[1]; ++yy) {
+            int wy = ik_wrap(yy, g.nc[1]);
+            for (int xx = lo[0]; xx <= hi[0]; ++xx) {
+                int wx = ik_wrap(xx, g.nc[0]);
+                int cell = (wz * g.nc[1] + wy) * g.nc[0] + wx;
+                int e = a.cell_start[cell + 1];
+                for (int q = a.cell_start[cell]; q < e; ++q) {
+                    int i = a.sorted[q];
+                    const double* pi = a.pos + 3 * (size_t)i;
+                    double d0 = ik_minimg(__dsub_rn(x[0], pi[0]), g.L[0], g.periodic[0]);
+                    double d1 = ik_minimg(__dsub_rn(x[1], pi[1]), g.L[1], g.periodic[1]);
+                    double d2 = ik_minimg(__dsub_rn(x[2], pi[2]), g.L[2], g.periodic[2]);
+                    if (!(ik_dot3(d0, d1, d2) < R2)) continue;
+                    double ri[3] = {x[0] - d0, x[1] - d1, x[2] - d2};
+                    if (want_kin) {
+                        double e0 = x[0] - ri[0], e1 = x[1] - ri[1], e2 = x[2] - ri[2];
+                        double cgval = ik_delta64(a.cg, e0 * e0 + e1 * e1 + e2 * e2);
+                        double m = a.mass ? a.mass[i] : 1.0;
+                        const double* v = a.vel + 3 * (size_t)i;
+                        kin[0] += (m * v[0] * v[0]) * cgval;
+                        kin[1] += (m * v[1] * v[1]) * cgval;
+                        if (DIM == 2) {
+                            kin[2] += (m * v[0] * v[1]) * cgval;
+                        } else {
+                            kin[2] += (m * v[2] * v[2]) * cgval;
+                            kin[3] += (m * v[0] * v[1]) * cgval;
+                            kin[4 % NC] += (m * v[0] * v[2]) * cgval;
+                            kin[5 % NC] += (m * v[1] * v[2]) * cgval;
+                        }
+                    }
+                    int nbq = a.nb[q];
+                    const IkB64* bq = a.bonds + (size_t)q * a.maxb;
+                    for (int k = 0; k < nbq; ++k) {
+                        IkB64 b = bq[k];
+                        double rij[3] = {b.x, b.y, b.z};
+                        double bond = ik_bond64(a.cg, a.xs, a.ws, a.nq, x, ri, rij);
+                        double hb = 0.5 * bond, f = b.w;
+                        vir[0] += hb * ((f * rij[0]) * rij[0]);
+                        vir[1] += hb * ((f * rij[1]) * rij[1]);
+                        if (DIM == 2) {
+                            vir[2] += hb * ((f * rij[0]) * rij[1]);
+                        } else {
+                            vir[2] += hb * ((f * rij[2]) * rij[2]);
+                            vir[3] += hb * ((f * rij[0]) * rij[1]);
+                            vir[4 % NC] += hb * ((f * rij[0]) * rij[2]);
+                            vir[5 % NC] += hb * ((f * rij[1]) * rij[2]);
+                        }
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        if (a.fields & 1) a.out_vir[gidx * NC + c] = vir[c];
+        if (a.fields & 2) a.out_kin[gidx * NC + c] = kin[c];
+    }
+}
+
+cudaError_t launch_gather64(const GatherArgs64& a, cudaStream_t st)
+{
+    int threads = 128;
+    int blocks = (int)((a.ngrid + threads - 1) / threads);
+    if (blocks == 0) return cudaSuccess;
+    if (a.g.dim == 2) k_gather64<2><<<blocks, threads, 0, st>>>(a);
+    else k_gather64<3><<<blocks, threads, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+struct EvalBondArgs {
+    IkCG cg;
+    int nq;
+    double xs[64], ws[64];
+};
+
+__global__ void k_eval_bond(const EvalBondArgs a, int m, const double* __restrict__ x,
+                            const double* __restrict__ ri, const double* __restrict__ rij,
+                            double* __restrict__ bond, double* __restrict__ delta)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m) return;
+    double xx[3] = {x[3 * k], x[3 * k + 1], x[3 * k + 2]};
+    double rr[3] = {ri[3 * k], ri[3 * k + 1], ri[3 * k + 2]};
+    double bb[3] = {rij[3 * k], rij[3 * k + 1], rij[3 * k + 2]};
+    bond[k] = ik_bond64(a.cg, a.xs, a.ws, a.nq, xx, rr, bb);
+    double e0 = xx[0] - rr[0], e1 = xx[1] - rr[1], e2 = xx[2] - rr[2];
+    delta[k] = ik_delta64(a.cg, e0 * e0 + e1 * e1 + e2 * e2);
+}
+
+cudaError_t launch_eval_bond(const IkCG& cg, int dim, const double* xs, const double* ws, int nq, int m,
+                             const double* x, const double* ri, const double* rij, double* bond,
+                             double* delta, cudaStream_t st)
+{
+    (void)dim;
+    EvalBondArgs a;
+    a.cg = cg;
+    a.nq = nq;
+    for (int k = 0; k < nq && k < 64; ++k) { a.xs[k] = xs[k]; a.ws[k] = ws[k]; }
+    int threads = 128, blocks = (m + threads - 1) / threads;
+    if (blocks == 0) return cudaSuccess;
+    k_eval_bond<<<blocks, threads, 0, st>>>(a, m, x, ri, rij, bond, delta);
+    return cudaGetLastError();
+}

@@ -1,0 +1,99 @@
+// ik_kernels.h -- kernel argument blocks and launcher prototypes shared by the
+// .cu translation units of the GB300 Irving-Kirkwood engine.
+#pragma once
+#include "ik_common.cuh"
+
+// ---- cells / bonds (ik_cells.cu) -------------------------------------------
+__global__ void k_bin(const double* pos, int n, IkGeom g, int* cell_of, int* rank, int* cell_count,
+                      int* status);
+__global__ void k_scan(const int* in, int n, int* out);
+__global__ void k_scatter(const int* cell_of, const int* rank, const int* cell_start, int n, int* sorted);
+__global__ void k_cell_sort_pack(IkGeom g, const int* cell_start, int* sorted, const double* pos,
+                                 const double* vel, const double* mass, const double* diam,
+                                 IkPRec* prec, float4* kin, float* diam32, int want_pack);
+cudaError_t launch_bonds32(int dim, IkGeom g, IkPoly12 pot, float kappa, int n, const IkPRec* prec,
+                          const float* diam32, const int* cell_start, float4* bonds, int maxb, int* nb,
+                          int* status, int* maxnb, unsigned long long* nbond_total, cudaStream_t st);
+__global__ void k_bonds64(IkGeom g, IkPoly12 pot, int n, const int* sorted, const int* cell_of,
+                          const double* pos, const double* diam, const int* cell_start, IkB64* bonds,
+                          int maxb, int* nb, int* status, int* maxnb);
+cudaError_t launch_neigh(bool fill, IkGeom g, int n, double r2cut, const int* sorted, const int* cell_of,
+                         const double* pos, const int* cell_start, int* count, const int* offs, int* idx,
+                         cudaStream_t st);
+__global__ void k_point_query(IkGeom g, int n, const double* pos, double px, double py, double pz,
+                              double r2cut, unsigned char* flag);
+__global__ void k_validate(const double* pos, const double* diam, int n, int dim, int* status);
+__global__ void k_eval_pair(IkPoly12 pot, int m, const double* rij, const double* di, const double* dj,
+                            double* f, double* en);
+
+// ---- FP32 tuned gather (ik_gather32.cu) ------------------------------------
+struct GatherArgs32 {
+    IkGeom g;
+    float cws[3];          // kappa * cell width
+    int bw[3];             // bin width (cells) per axis
+    int reach[3];          // halo reach (cells) per axis; 0 on non-periodic axes
+    float kappa, R2s, margin;
+    double R2;             // FP64 R^2 for the boundary re-check
+    // Gauss-Legendre in symmetric form: xi_k > 0 (k < npairs) with weights w_k, centre w0
+    int npairs;
+    float w0, xi[32], w[32];
+    // particle data (sorted order)
+    const IkPRec* prec;
+    const int* cell_start;
+    const int* nb;
+    const float4* bonds;
+    int maxb;
+    const float4* kin;
+    const int* sorted;
+    const double* pos;
+    // grid
+    const float4* gpts;    // bin-ordered {ux,uy,uz, bits(grid index)}
+    const double* grid;    // original FP64 grid (g x 3)
+    const int4* items;     // {cx0, cy0, cz0, gstart}; items[nitems].w = end
+    int nitems;
+    int halo_cap, qcap;
+    double vir_scale, kin_scale;
+    double* out_vir;
+    double* out_kin;
+    int fields;
+    int* work_counter;
+    int* status;
+    unsigned long long* cnt_pairs;
+    unsigned long long* cnt_triples;
+};
+cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, int blocks, int threads,
+                            size_t smem, cudaStream_t st);
+int gather32_regs(int dim, int kind, bool kahan);
+
+// ---- FP64 plain gather (ik_gather64.cu) ------------------------------------
+struct GatherArgs64 {
+    IkGeom g;
+    IkCG cg;
+    int reach[3];
+    int all[3];
+    int nq;
+    double xs[64], ws[64];  // GL nodes mapped to [0,1] (s) and their [-1,1] weights
+    const int* sorted;
+    const int* cell_start;
+    const double* pos;
+    const double* vel;
+    const double* mass;
+    const int* nb;
+    const IkB64* bonds;
+    int maxb;
+    const double* grid;
+    int64_t ngrid;
+    double* out_vir;
+    double* out_kin;
+    int fields;
+};
+cudaError_t launch_gather64(const GatherArgs64& a, cudaStream_t st);
+
+// ---- scalar bond evaluations (ik_gather64.cu) ------------------------------
+cudaError_t launch_eval_bond(const IkCG& cg, int dim, const double* xs, const double* ws, int nq,
+                             int m, const double* x, const double* ri, const double* rij, double* bond,
+                             double* delta, cudaStream_t st);
+
+// ---- FP32 FMA throughput probe (ik_cells.cu) --------------------------------
+#define IK_FMA_PROBE_CHAINS 8
+cudaError_t launch_fma_probe(int blocks, int threads, int iters, float* out);

@@ -1,0 +1,256 @@
+"""ctypes binding of the C ABI in include/ik_gb300.h (libik_gb300.so).
+
+This is the low-level route a host program takes without the pybind11 layer:
+plain pointers and sizes, one status code per call, ``ik_last_error()`` text on
+failure (raised here as ``IKError``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libik_gb300.so")
+
+IK_OK = 0
+ERR = {-1: "IK_ERR_ARG", -2: "IK_ERR_CUDA", -3: "IK_ERR_STATE", -4: "IK_ERR_BOX",
+       -5: "IK_ERR_CAPACITY", -6: "IK_ERR_TIMEOUT", -7: "IK_ERR_NOMEM", -8: "IK_ERR_UNSUPPORTED"}
+CG = {"octic": 0, "gaussian": 1, "rect": 2, "mollifier": 3}
+QUAD = {"fixedpoint": 0, "adaptive": 1, "exact": 2, "mlp": 3}
+PREC = {"fp64": 0, "fp32": 1}
+FIELD_VIRIAL, FIELD_KINETIC = 1, 2
+FLAG_TIMING, FLAG_NO_KAHAN = 1, 2
+
+_lib = None
+
+
+class IKError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERR.get(code, code)}: {msg}")
+        self.code = code
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is not built (python -m pyglasstools_gb300._build)")
+        L = C.CDLL(LIB_PATH)
+        vp, dp, i64, i32 = C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.c_int
+        sig = {
+            "ik_last_error": ([], C.c_char_p),
+            "ik_version": ([], i32),
+            "ik_create": ([C.POINTER(vp), i32], i32),
+            "ik_destroy": ([vp], i32),
+            "ik_set_box": ([vp, i32, dp, dp], i32),
+            "ik_set_potential_poly12": ([vp, C.c_double, dp], i32),
+            "ik_set_cgfunc": ([vp, i32, i32, i32, C.c_double, C.c_double], i32),
+            "ik_set_adaptive": ([vp, i32, C.c_double, C.c_double], i32),
+            "ik_set_max_rcut": ([vp, C.c_double], i32),
+            "ik_get_max_rcut": ([vp, dp], i32),
+            "ik_set_grid": ([vp, i64, dp], i32),
+            "ik_reserve_slots": ([vp, i32], i32),
+            "ik_upload_frame": ([vp, i32, i64, dp, dp, dp, dp], i32),
+            "ik_set_frame": ([vp, i64, dp, dp, dp, dp], i32),
+            "ik_compute_slot": ([vp, i32, i32, i32], i32),
+            "ik_synchronize": ([vp], i32),
+            "ik_compute": ([vp, i32, i32], i32),
+            "ik_get_field": ([vp, i32, i32, dp, i64], i32),
+            "ik_get_neighbors": ([vp, i32, C.c_double, C.POINTER(C.c_int64), C.POINTER(C.c_int32), i64,
+                                  C.POINTER(C.c_int64)], i32),
+            "ik_get_neighbors_point": ([vp, i32, dp, C.c_double, C.POINTER(C.c_int32), i64,
+                                        C.POINTER(C.c_int64)], i32),
+            "ik_eval_pair": ([vp, i64, dp, dp, dp, dp, dp], i32),
+            "ik_eval_bond": ([vp, i64, dp, dp, dp, dp, dp], i32),
+            "ik_set_flags": ([vp, i32], i32),
+            "ik_get_timing": ([vp, C.POINTER(C.c_float)], i32),
+            "ik_get_counters": ([vp, i32, C.POINTER(C.c_int64)], i32),
+            "ik_get_stream": ([vp, C.POINTER(vp)], i32),
+            "ik_download_field_async": ([vp, i32, i32, dp, i64], i32),
+            "ik_measure_fp32_peak": ([i32, dp], i32),
+            "ik_get_launch_count": ([vp, C.POINTER(C.c_int64)], i32),
+        }
+        for name, (args, res) in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _c64(a, shape=None):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a if shape is None else a.reshape(shape)
+
+
+def check(rc):
+    if rc != IK_OK:
+        raise IKError(rc, lib().ik_last_error().decode(errors="replace"))
+
+
+class IKContext:
+    """One engine context (one CUDA stream) -- see include/ik_gb300.h."""
+
+    def __init__(self, device=0):
+        self._h = C.c_void_p()
+        check(lib().ik_create(C.byref(self._h), device))
+        self.dim = None
+        self.G = 0
+
+    def close(self):
+        if self._h:
+            lib().ik_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # configuration ---------------------------------------------------------
+    def set_box(self, dim, boxsize, origin=(0.0, 0.0, 0.0)):
+        b = np.broadcast_to(np.asarray(boxsize, np.float64), (3,)).copy()
+        o = np.asarray(origin, np.float64).copy()
+        check(lib().ik_set_box(self._h, dim, _dp(b), _dp(o)))
+        self.dim = dim
+
+    def set_poly12(self, v0=1.0, eps=0.2, rcut=1.25):
+        p = np.array([v0, eps, -28.0 * v0 / rcut ** 12, 48.0 * v0 / rcut ** 14, -21.0 * v0 / rcut ** 16])
+        check(lib().ik_set_potential_poly12(self._h, rcut, _dp(p)))
+
+    def set_cgfunc(self, kind, rcut, mode="fixedpoint", order=5, width=0.0):
+        check(lib().ik_set_cgfunc(self._h, CG[kind], QUAD[mode], order, rcut, width))
+
+    def set_max_rcut(self, r):
+        check(lib().ik_set_max_rcut(self._h, r))
+
+    def get_max_rcut(self):
+        v = C.c_double()
+        check(lib().ik_get_max_rcut(self._h, C.byref(v)))
+        return v.value
+
+    def set_grid(self, grid):
+        g = _c64(grid, (-1, 3))
+        check(lib().ik_set_grid(self._h, len(g), _dp(g)))
+        self.G = len(g)
+
+    def set_flags(self, flags):
+        check(lib().ik_set_flags(self._h, flags))
+
+    # frames ----------------------------------------------------------------
+    def reserve_slots(self, n):
+        check(lib().ik_reserve_slots(self._h, n))
+
+    def upload_frame(self, slot, pos, diam, vel=None, mass=None):
+        pos = _c64(pos, (-1, 3))
+        diam = _c64(diam)
+        vel = _c64(vel, (-1, 3))
+        mass = _c64(mass)
+        self._keep = (pos, diam, vel, mass)  # alive until the async copy completes
+        check(lib().ik_upload_frame(self._h, slot, len(diam), _dp(pos), _dp(vel), _dp(mass), _dp(diam)))
+
+    def set_frame(self, pos, diam, vel=None, mass=None):
+        self.upload_frame(0, pos, diam, vel, mass)
+        self.synchronize()
+
+    def compute_slot(self, slot, precision="fp32", fields=FIELD_VIRIAL | FIELD_KINETIC):
+        check(lib().ik_compute_slot(self._h, slot, PREC[precision], fields))
+
+    def synchronize(self):
+        check(lib().ik_synchronize(self._h))
+
+    def compute(self, precision="fp32", fields=FIELD_VIRIAL | FIELD_KINETIC):
+        check(lib().ik_compute(self._h, PREC[precision], fields))
+
+    def get_field(self, field=FIELD_VIRIAL, slot=0):
+        D = self.dim
+        out = np.zeros((self.G, D, D))
+        check(lib().ik_get_field(self._h, slot, field, _dp(out), out.size))
+        # column-major per grid point -> [g, a, b] = T_ab (symmetric)
+        return out.transpose(0, 2, 1).copy()
+
+    # queries ---------------------------------------------------------------
+    def neighbors(self, radius, slot=0, n=None):
+        if n is None:
+            raise ValueError("pass n = number of particles of the slot")
+        offs = np.zeros(n + 1, np.int64)
+        nnz = C.c_int64()
+        check(lib().ik_get_neighbors(self._h, slot, radius, offs.ctypes.data_as(C.POINTER(C.c_int64)), None, 0,
+                                     C.byref(nnz)))
+        idx = np.zeros(max(nnz.value, 1), np.int32)
+        check(lib().ik_get_neighbors(self._h, slot, radius, offs.ctypes.data_as(C.POINTER(C.c_int64)),
+                                     idx.ctypes.data_as(C.POINTER(C.c_int32)), nnz.value, C.byref(nnz)))
+        return offs, idx[:nnz.value]
+
+    def neighbors_point(self, point, radius, slot=0):
+        p = np.asarray(point, np.float64).copy()
+        cnt = C.c_int64()
+        check(lib().ik_get_neighbors_point(self._h, slot, _dp(p), radius, None, 0, C.byref(cnt)))
+        ids = np.zeros(max(cnt.value, 1), np.int32)
+        check(lib().ik_get_neighbors_point(self._h, slot, _dp(p), radius, ids.ctypes.data_as(C.POINTER(C.c_int32)),
+                                           cnt.value, C.byref(cnt)))
+        return ids[:cnt.value]
+
+    def eval_pair(self, rij, di, dj):
+        rij = _c64(rij, (-1, 3))
+        di = _c64(di)
+        dj = _c64(dj)
+        f = np.zeros(len(di))
+        e = np.zeros(len(di))
+        check(lib().ik_eval_pair(self._h, len(di), _dp(rij), _dp(di), _dp(dj), _dp(f), _dp(e)))
+        return f, e
+
+    def eval_bond(self, x, ri, rij):
+        x = _c64(x, (-1, 3))
+        ri = _c64(ri, (-1, 3))
+        rij = _c64(rij, (-1, 3))
+        b = np.zeros(len(x))
+        d = np.zeros(len(x))
+        check(lib().ik_eval_bond(self._h, len(x), _dp(x), _dp(ri), _dp(rij), _dp(b), _dp(d)))
+        return b, d
+
+    def timing(self):
+        t = (C.c_float * 4)()
+        check(lib().ik_get_timing(self._h, t))
+        return list(t)
+
+    def stream(self):
+        v = C.c_void_p()
+        check(lib().ik_get_stream(self._h, C.byref(v)))
+        return v.value
+
+    def download_field_async(self, out, field=FIELD_VIRIAL, slot=0):
+        """out: C-contiguous float64 (G, NC) host array (pinned for overlap)."""
+        assert out.dtype == np.float64 and out.flags.c_contiguous
+        check(lib().ik_download_field_async(self._h, slot, field, _dp(out), out.size))
+
+    def launch_count(self):
+        v = C.c_int64()
+        check(lib().ik_get_launch_count(self._h, C.byref(v)))
+        return v.value
+
+    def counters(self, slot=0):
+        c = (C.c_int64 * 3)()
+        check(lib().ik_get_counters(self._h, slot, c))
+        return list(c)
+
+
+def measure_fp32_peak(device=0):
+    v = C.c_double()
+    check(lib().ik_measure_fp32_peak(device, C.byref(v)))
+    return v.value

@@ -1,0 +1,251 @@
+"""CPU tests pinning the FP64 oracle: against the reference's own kernel headers
+(compiled by oracle/build_ref.sh, or their committed golden values), against
+exactness properties of the quadrature rules and against closed forms."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+
+def test_gl_rule_exact_on_polynomials(oracle):
+    for n in (1, 2, 3, 5, 8, 15, 32, 64):
+        x, w = oracle.gl_rule(n)
+        assert np.all(np.diff(x) > 0)
+        for k in range(2 * n):
+            exact = 2.0 / (k + 1) if k % 2 == 0 else 0.0
+            assert abs(np.sum(w * x ** k) - exact) < 5e-14 * max(1, n), (n, k)
+
+
+def test_gk15_rule_degree_22(oracle):
+    x, wk, wg = oracle.gk15_rule()
+    xs = np.concatenate([-x[:0:-1], x])
+    ws = np.concatenate([wk[:0:-1], wk])
+    for k in range(23):
+        exact = 2.0 / (k + 1) if k % 2 == 0 else 0.0
+        assert abs(np.sum(ws * xs ** k) - exact) < 1e-14
+    # the embedded Gauss-7 nodes are the 7-point Legendre roots
+    gx, gw = oracle.gl_rule(7)
+    np.testing.assert_allclose(x[[0, 2, 4, 6]], gx[3:], atol=1e-15)
+    np.testing.assert_allclose(wg, gw[3:], atol=1e-15)
+
+
+def test_force_matches_reference_header_golden(oracle, golden):
+    """Polydisperse12 force/energy/stiffness: bit-identical to the reference's own
+    Polydisperse12.h (values generated by compiling it; tests/golden/make_golden.py)."""
+    g = golden("ref_kernels.npz")
+    pot = oracle.make_poly12()
+    f = np.array([oracle.force_divr(pot, a, b, c) for a, b, c in zip(g["rsq"], g["di"], g["dj"])])
+    e = np.array([oracle.pair_energy(pot, a, b, c) for a, b, c in zip(g["rsq"], g["di"], g["dj"])])
+    s = np.array([oracle.bond_stiffness(pot, a, b, c) for a, b, c in zip(g["rsq"], g["di"], g["dj"])])
+    assert np.array_equal(f, g["force"])
+    assert np.array_equal(e, g["energy"])
+    assert np.array_equal(s, g["stiffness"])
+    assert np.count_nonzero(f) > 100 and np.count_nonzero(f == 0) > 100  # both branches exercised
+
+
+def test_cg_kernels_match_reference_headers_golden(oracle, golden):
+    g = golden("ref_kernels.npz")
+    rc = float(g["rc"])
+    for kind in ("octic", "rect", "mollifier"):
+        cg = oracle.make_cg(kind, rcut=rc)
+        v = np.array([oracle.delta(cg, 2, x) for x in g["dr"]])
+        assert np.array_equal(v, g[kind]), kind
+
+
+def test_live_reference_build_if_present(oracle):
+    """When the reference tree is on this machine, recompile its headers and compare live."""
+    import ctypes as C
+    R = oracle.ref_lib()
+    if R is None:
+        pytest.skip("oracle/_ref not built (no reference tree here)")
+    rng = np.random.default_rng(7)
+    pot = oracle.make_poly12(v0=1.3, eps=0.15, rcut=1.4)
+    prm = (C.c_double * 5)(pot.v0, pot.eps, pot.c0, pot.c1, pot.c2)
+    for _ in range(3000):
+        rsq, di, dj = rng.uniform(0.05, 5.0), rng.uniform(0.6, 1.8), rng.uniform(0.6, 1.8)
+        assert oracle.force_divr(pot, rsq, di, dj) == R.ref_poly12_force_divr(rsq, pot.scaled_rcut, prm, di, dj)
+        assert oracle.pair_energy(pot, rsq, di, dj) == R.ref_poly12_energy(rsq, pot.scaled_rcut, prm, di, dj)
+
+
+def test_octic_bond_closed_form(oracle):
+    """Segment inside the support: the octic bond integral is a degree-8 polynomial in s;
+    GL-5 integrates it exactly, and the exact mode agrees."""
+    rng = np.random.default_rng(3)
+    R = 2.0
+    fixed = oracle.make_cg("octic", rcut=R, mode="fixedpoint", order=5)
+    exact = oracle.make_cg("octic", rcut=R, mode="exact")
+    for _ in range(200):
+        ri = np.r_[rng.uniform(-0.6, 0.6, 2), 0.0]
+        rij = np.r_[rng.uniform(-0.6, 0.6, 2), 0.0]
+        x = np.zeros(3)
+        # dense reference by Simpson on 20001 points
+        s = np.linspace(0, 1, 20001)
+        d = x[None, :] - (ri[None, :] + s[:, None] * rij[None, :])
+        q = (d ** 2).sum(1) / R ** 2
+        f = 15 / (8 * np.pi * R * R) * (1 - 2 * q ** 2 + q ** 4)
+        h = s[1] - s[0]
+        simpson = h / 3 * (f[0] + f[-1] + 4 * f[1:-1:2].sum() + 2 * f[2:-1:2].sum())
+        a = oracle.bond(fixed, 2, x, ri, rij)
+        b = oracle.bond(exact, 2, x, ri, rij)
+        assert abs(a - simpson) < 1e-12 * abs(simpson)
+        assert abs(b - simpson) < 1e-12 * abs(simpson)
+
+
+def test_gaussian_exact_vs_clipped_adaptive(oracle):
+    """Truncated Gaussian: erf closed form == adaptive GK15 on the clipped interval."""
+    from scipy.integrate import quad
+    rng = np.random.default_rng(5)
+    w, R = 2.0, 6.0
+    exact = oracle.make_cg("gaussian", rcut=R, mode="exact", width=w)
+    norm = 1 / (2 * np.pi * w * w)
+    for _ in range(300):
+        ri = np.r_[rng.uniform(-6.5, 6.5, 2), 0.0]
+        rij = np.r_[rng.uniform(-2, 2, 2), 0.0]
+        x = np.zeros(3)
+        f = lambda s: norm * np.exp(-np.sum((x - ri - s * rij) ** 2) / (2 * w * w)) \
+            if np.sum((x - ri - s * rij) ** 2) < R * R else 0.0
+        # split at the truncation crossings for the scipy reference
+        u = x - ri
+        bb, ub, uu = rij @ rij, u @ rij, u @ u
+        disc = ub * ub - bb * (uu - R * R)
+        pts = []
+        if disc > 0:
+            for r in ((ub - np.sqrt(disc)) / bb, (ub + np.sqrt(disc)) / bb):
+                if 0 < r < 1:
+                    pts.append(r)
+        ref = quad(f, 0, 1, points=pts or None, epsabs=1e-15, epsrel=1e-13, limit=200)[0]
+        assert abs(oracle.bond(exact, 2, x, ri, rij) - ref) < 1e-12 + 1e-10 * abs(ref)
+
+
+def test_two_particle_hand_computed_field(oracle):
+    """Two particles on the x axis, octic R = 2, one grid point: the virial field is
+    0.5 * f(r) r^2 * [B(x; r1, r12) + B(x; r2, r21)] in xx only."""
+    L = 20.0
+    box = oracle.make_box(2, [L, L, 1.0])
+    pos = np.array([[-0.5, 0.0, 0.0], [0.5, 0.0, 0.0]])
+    diam = np.array([1.0, 1.0])
+    pot = oracle.make_poly12()
+    cg = oracle.make_cg("octic", rcut=2.0, mode="fixedpoint", order=5)
+    grid = np.array([[0.3, 0.2, 0.0]])
+    vir, kin = oracle.compute(box, pos, diam, pot, cg, grid)
+    f = oracle.force_divr(pot, 1.0, 1.0, 1.0)
+    x = grid[0]
+    b12 = oracle.bond(cg, 2, x, pos[0], pos[1] - pos[0])
+    b21 = oracle.bond(cg, 2, x, pos[1], pos[0] - pos[1])
+    expect = 0.5 * f * 1.0 * (b12 + b21)
+    assert abs(vir[0, 0, 0] - expect) < 1e-14 * abs(expect)
+    assert vir[0, 1, 1] == 0.0 and vir[0, 0, 1] == 0.0
+    assert np.all(kin == 0.0)
+
+
+def test_selection_rule_half_weight(oracle):
+    """A bond with only one end inside the support enters once (ordered pair (i,j) with
+    i inside), a bond with both ends outside not at all (IrvingKirkwood.h:80-105)."""
+    L = 30.0
+    box = oracle.make_box(2, [L, L, 1.0])
+    pot = oracle.make_poly12()
+    cg = oracle.make_cg("octic", rcut=2.0, mode="fixedpoint", order=5)
+    diam = np.array([1.0, 1.0])
+    grid = np.array([[0.0, 0.0, 0.0]])
+    pos = np.array([[1.5, 0.0, 0.0], [2.4, 0.0, 0.0]])  # i inside, j outside
+    vir, _ = oracle.compute(box, pos, diam, pot, cg, grid)
+    f = oracle.force_divr(pot, 0.81, 1.0, 1.0)
+    b = oracle.bond(cg, 2, grid[0], pos[0], pos[1] - pos[0])
+    assert abs(vir[0, 0, 0] - 0.5 * f * 0.81 * b) < 1e-15
+    pos = np.array([[2.1, 0.5, 0.0], [2.1, -0.5, 0.0]])  # both outside, segment crosses support
+    vir, _ = oracle.compute(box, pos, diam, pot, cg, grid)
+    assert np.all(vir == 0.0)
+
+
+def test_periodic_wrap_and_translation(oracle):
+    """Translating the frame and the grid by a lattice vector, or wrapping particles
+    into the box, leaves the field unchanged (min-image convention)."""
+    from pyglasstools_gb300 import synth
+    f = synth.make_frame(600, dim=2, seed=11)
+    grid = synth.lattice_grid(f.L, 24, 2)
+    box = oracle.make_box(2, [f.L, f.L, 1.0])
+    pot = oracle.make_poly12()
+    cg = oracle.make_cg("octic", rcut=2.0, mode="fixedpoint", order=5)
+    v0, k0 = oracle.compute(box, f.pos, f.diam, pot, cg, grid, vel=f.vel, mass=f.mass)
+    shifted = f.pos.copy()
+    shifted[:, 0] += f.L  # an image of every particle
+    v1, k1 = oracle.compute(box, shifted, f.diam, pot, cg, grid, vel=f.vel, mass=f.mass)
+    assert np.max(np.abs(v1 - v0)) <= 1e-9 * np.max(np.abs(v0))
+    assert np.max(np.abs(k1 - k0)) <= 1e-9 * np.max(np.abs(k0))
+
+
+def test_xy_swap_symmetry(oracle):
+    from pyglasstools_gb300 import synth
+    f = synth.make_frame(500, dim=2, seed=12)
+    n = 20
+    grid = synth.lattice_grid(f.L, n, 2)
+    box = oracle.make_box(2, [f.L, f.L, 1.0])
+    pot = oracle.make_poly12()
+    cg = oracle.make_cg("octic", rcut=2.0, mode="fixedpoint", order=5)
+    v, _ = oracle.compute(box, f.pos, f.diam, pot, cg, grid)
+    sw = f.pos[:, [1, 0, 2]]
+    vs, _ = oracle.compute(box, sw, f.diam, pot, cg, grid)
+    # grid point (i, j) of the swapped frame is (j, i) of the original
+    v = v.reshape(n, n, 2, 2)
+    vs = vs.reshape(n, n, 2, 2)
+    np.testing.assert_allclose(vs[:, :, 0, 0], v.transpose(1, 0, 2, 3)[:, :, 1, 1], rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(vs[:, :, 0, 1], v.transpose(1, 0, 2, 3)[:, :, 0, 1], rtol=1e-10, atol=1e-12)
+
+
+def test_sum_rule_against_global_virial(oracle):
+    """Integrating the IK virial field over the box recovers the global virial
+    sum_{i<j} F_ij (x) r_ij (ThermoCalculator.h:68-90) up to the i-in-support
+    selection rule, whose deficit shrinks as R grows relative to the bond length:
+    the ratio approaches 1 from below, monotonically in R."""
+    from pyglasstools_gb300 import synth
+    f = synth.make_frame(400, dim=2, seed=4, jitter=0.02)
+    n = 80
+    grid = synth.lattice_grid(f.L, n + 1, 2)
+    box = oracle.make_box(2, [f.L, f.L, 1.0])
+    pot = oracle.make_poly12()
+    glob = oracle.global_virial(box, f.pos, f.diam, pot)
+    ratios = []
+    for R in (2.0, 4.0, 6.0):
+        cg = oracle.make_cg("octic", rcut=R, mode="fixedpoint", order=5)
+        v, _ = oracle.compute(box, f.pos, f.diam, pot, cg, grid)
+        v = v.reshape(n + 1, n + 1, 2, 2)[:n, :n]  # drop the periodic duplicate row/column
+        integral = v.sum(axis=(0, 1)) * (f.L / n) ** 2
+        ratios.append([integral[0, 0] / glob[0, 0], integral[1, 1] / glob[1, 1]])
+    ratios = np.array(ratios)
+    assert np.all(ratios < 1.0)
+    assert np.all(np.diff(ratios, axis=0) > 0)
+    assert np.all(ratios[-1] > 0.99)
+
+
+def test_neighbors_definition(oracle):
+    from pyglasstools_gb300 import synth
+    f = synth.make_frame(300, dim=2, seed=9)
+    box = oracle.make_box(2, [f.L, f.L, 1.0])
+    offs, idx = oracle.neighbors(box, f.pos, 2.0)
+    # brute force with the same FP64 min-image rule
+    d = f.pos[None, :, :] - f.pos[:, None, :]
+    d[..., :2] -= f.L * np.rint(d[..., :2] / f.L)
+    r2 = (d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1]) + d[..., 2] * d[..., 2]
+    for i in range(len(f.pos)):
+        want = np.nonzero((r2[i] < 4.0) & (np.arange(len(f.pos)) != i))[0]
+        assert np.array_equal(idx[offs[i]:offs[i + 1]], want)
+
+
+def test_golden_fixture_field_regenerates(oracle, golden):
+    """The committed oracle field on fixture frame 180 is what the oracle computes now."""
+    fr = golden("fixture_frames.npz")
+    gold = golden("oracle_fixture180.npz")
+    pos = fr["pos180"].astype(np.float64)
+    diam = fr["diam180"].astype(np.float64)
+    L = float(fr["box180"][0])
+    assert int(gold["nmax"]) == int(L / 0.25) == 127
+    pts = np.linspace(-L / 2, L / 2, int(gold["nmax"]))
+    gx, gy = np.meshgrid(pts, pts, indexing="ij")
+    grid = np.stack([gx.ravel(), gy.ravel(), np.zeros(gx.size)], axis=1)
+    sel = slice(0, None, 37)  # every 37th grid point keeps this test fast
+    box = oracle.make_box(2, [L, L, 1.0])
+    pot = oracle.make_poly12()
+    cg = oracle.make_cg("octic", rcut=2.0, mode="fixedpoint", order=5)
+    v, _ = oracle.compute(box, pos, diam, pot, cg, grid[sel], max_rc=float(gold["max_rcut"]))
+    u = np.stack([v[:, 0, 0], v[:, 1, 1], v[:, 0, 1]], axis=1)
+    assert np.max(rel_l2(u, gold["virial"][sel])) < 1e-13
