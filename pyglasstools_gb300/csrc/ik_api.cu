@@ -685,7 +685,7 @@ int ik_upload_frame(ik_ctx* c, int slot, int64_t n, const double* pos, const dou
 {
     if (int r = check_ctx(c)) return r;
     if (int r = slot_ok(c, slot)) return r;
-    if (n < 0 || n > (1 << 26)) return fail(IK_ERR_ARG, "particle count %lld out of range", (long long)n);
+    if (n < 0 || n >= (1 << 25)) return fail(IK_ERR_ARG, "particle count %lld out of range (max 2^25 - 1)", (long long)n);
     if (n > 0 && (!pos || !diam)) return fail(IK_ERR_ARG, "positions and diameters are required");
     if (!c->box_set) return fail(IK_ERR_STATE, "box not set (ik_set_box)");
     double dmax = 0.0;
