@@ -56,6 +56,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ik2d_n64k_g256_gauss", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--frames", type=int, default=0, help="override the frames per step (profiling)")
+    ap.add_argument("--profile", action="store_true",
+                    help="only warm-up + timed steps (for ncu launch lists); prints a short JSON line")
     return ap.parse_args()
 
 
@@ -222,6 +225,20 @@ def ours(args, wl, name):
         for k in range(nfr):
             ctx.compute_slot(k, prec)
 
+    if args.profile:
+        for _ in range(args.warmup):
+            step()
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step()
+        ctx.synchronize()
+        dt = time.perf_counter() - t0
+        print(json.dumps({"profile": name, "frames": F, "steps": args.steps, "host_s": dt,
+                          "frames_per_s_host": F * args.steps / dt, "counters_slot0": ctx.counters(0)}))
+        ctx.close()
+        return
+
     clocks = ClockSampler(local)
     clocks.start()
     # ---- warm-up (also a soak so that the clock sampler sees the GPU under load)
@@ -366,7 +383,9 @@ def ours(args, wl, name):
 
 def main():
     args = parse()
-    wl = WORKLOADS[args.workload]
+    wl = dict(WORKLOADS[args.workload])
+    if args.frames > 0:
+        wl["frames"] = args.frames
     if args.impl == "reference":
         reference_arm(args, wl, args.workload)
     else:

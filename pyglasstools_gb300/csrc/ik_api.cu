@@ -371,7 +371,8 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         ENS(c->bonds32, sizeof(float4) * NV * (size_t)c->maxb * std::max(n, 1));
         ENS(c->nb32, sizeof(int) * std::max(n, 1));
         CK(launch_bonds32(D, g, c->pot, c->cg.kappa, n, c->prec.as<IkPRec>(), c->diam32.as<float>(),
-                          c->cell_start.as<int>(), c->bonds32.as<float4>(), c->maxb, c->nb32.as<int>(),
+                          c->cell_start.as<int>(), c->sorted.as<int>(), s.pos.as<double>(),
+                          c->bonds32.as<float4>(), c->maxb, c->nb32.as<int>(),
                           c->status.as<int>(), c->maxnb.as<int>(), cnt, c->stream));
         if (timing) CK(cudaEventRecord(c->ev[2], c->stream));
         GatherArgs32 a{};

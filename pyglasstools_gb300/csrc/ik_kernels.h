@@ -12,8 +12,9 @@ __global__ void k_cell_sort_pack(IkGeom g, const int* cell_start, int* sorted, c
                                  const double* vel, const double* mass, const double* diam,
                                  IkPRec* prec, float4* kin, float* diam32, int want_pack);
 cudaError_t launch_bonds32(int dim, IkGeom g, IkPoly12 pot, float kappa, int n, const IkPRec* prec,
-                          const float* diam32, const int* cell_start, float4* bonds, int maxb, int* nb,
-                          int* status, int* maxnb, unsigned long long* nbond_total, cudaStream_t st);
+                          const float* diam32, const int* cell_start, const int* sorted, const double* pos,
+                          float4* bonds, int maxb, int* nb, int* status, int* maxnb,
+                          unsigned long long* nbond_total, cudaStream_t st);
 __global__ void k_bonds64(IkGeom g, IkPoly12 pot, int n, const int* sorted, const int* cell_of,
                           const double* pos, const double* diam, const int* cell_start, IkB64* bonds,
                           int maxb, int* nb, int* status, int* maxnb);
