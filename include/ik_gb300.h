@@ -147,6 +147,30 @@ int ik_download_field_async(ik_ctx* ctx, int slot, int field, double* host_out, 
  * FP32 gather.  Diagnostic: no reference counterpart. */
 int ik_measure_fp32_peak(int device, double* tflops);
 
+/* No-allocation variant of the plain FP64 computation (ik_compute with IK_PREC_FP64),
+ * for callers that cannot call cudaMalloc: code running where the allocator may not
+ * be entered (host callbacks, real-time loops), or in processes whose device memory
+ * belongs to another framework's pool or a budget fixed at start-up.  No counterpart
+ * in the reference.  Allocates nothing: the caller passes DEVICE pointers for inputs
+ * (d_pos n x 3, d_diam n, optional d_vel n x 3 and d_mass n, d_grid g x 3) and outputs
+ * (d_virial and optional d_kinetic, each g x NC FP64 with NC = 3 in 2D (xx, yy, xy)
+ * or 6 in 3D (xx, yy, zz, xy, xz, yz)); all scratch is a static device array of about
+ * 4.3 MB that every GPU loading the library holds until exit.  Limits: n <= 4096
+ * particles (larger n is rejected with IK_ERR_CAPACITY), at most 32 force-active
+ * bonds per particle.  Runs on `stream` (a cudaStream_t; NULL = default stream) and
+ * returns after that stream has finished.  The first call on each device sets up
+ * the scratch address; make it before any stream capture.  Calls share the scratch
+ * array: calls that overlap on the GPU race and must be serialised by the caller.
+ * Box, potential and coarse-graining arguments mean what they mean in ik_set_box,
+ * ik_set_potential_poly12, ik_set_max_rcut and ik_set_cgfunc (fixed-point mode). */
+int ik_compute_fp64_noalloc(int dim, const double boxsize[3], const double origin[3],
+                            double scaled_rcut, const double params[5], double max_rcut,
+                            int cg_kind, int gl_order, double cg_rcut, double cg_width,
+                            int64_t n, const double* d_pos, const double* d_diam,
+                            const double* d_vel, const double* d_mass, int64_t g,
+                            const double* d_grid, double* d_virial, double* d_kinetic,
+                            void* stream);
+
 /* Number of kernels this context has launched since it was created. */
 int ik_get_launch_count(ik_ctx* ctx, int64_t* out);
 

@@ -464,6 +464,9 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
 
 } // namespace
 
+// Lets entry points defined in other translation units report through ik_last_error().
+void ik_internal_set_error(const char* msg) { g_err = msg; }
+
 // ===========================================================================
 extern "C" {
 

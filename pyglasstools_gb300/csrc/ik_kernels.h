@@ -98,3 +98,6 @@ cudaError_t launch_eval_bond(const IkCG& cg, int dim, const double* xs, const do
 // ---- FP32 FMA throughput probe (ik_cells.cu) --------------------------------
 #define IK_FMA_PROBE_CHAINS 8
 cudaError_t launch_fma_probe(int blocks, int threads, int iters, float* out);
+
+// ---- error text shared by the C-ABI translation units (ik_api.cu) ------------
+void ik_internal_set_error(const char* msg);
