@@ -128,8 +128,9 @@ int ik_eval_bond(ik_ctx* ctx, int64_t m, const double* x, const double* ri,
 /* Timing of the last ik_compute_slot on the stream (ms per stage, CUDA events):
  * [0] cells, [1] bonds, [2] gather, [3] total.  Needs IK_TIMING in ik_set_flags. */
 #define IK_FLAG_TIMING 1
-/* FP32 path: plain FP32 per-lane sums instead of Kahan-compensated ones. */
-#define IK_FLAG_NO_KAHAN 2
+/* FP32 path: Kahan-compensated per-lane sums (the combination of the lane partials
+ * of every grid point is always compensated; per-lane sums are plain by default). */
+#define IK_FLAG_LANE_KAHAN 2
 int ik_set_flags(ik_ctx* ctx, int flags);
 int ik_get_timing(ik_ctx* ctx, float* ms4);
 

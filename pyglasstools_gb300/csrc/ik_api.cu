@@ -100,7 +100,7 @@ struct ik_ctx {
     DevBuf gpts_d, items_d;
     // work buffers
     DevBuf cell_of, rank, cell_count, cell_start, sorted, prec, kin, diam32;
-    DevBuf bonds32, nb32, bonds64, nb64;
+    DevBuf bonds32, nb32, bonds64, nb64, pos64, bonds_tmp, boff, bsum;
     DevBuf status, maxnb, work_counter;
     int maxb = 0, halo_cap = 0;
     // neighbour-query scratch
@@ -179,6 +179,7 @@ int ensure_geometry(ik_ctx* c)
         }
         g.nc[a] = nc;
         g.cw[a] = g.L[a] / nc;
+        g.invL[a] = 1.0 / g.L[a];
         g.reach_bond[a] = 1;
         g.all_bond[a] = (nc < 3) ? 1 : 0;
     }
@@ -352,28 +353,36 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
     if (!(fields & IK_FIELD_VIRIAL)) CK(cudaMemsetAsync(s.vir.p, 0, sizeof(double) * NC * c->G, c->stream));
     int r = build_cells(c, s, g, c->cell_of, c->rank, c->cell_count, c->cell_start, c->sorted);
     if (r) return r;
-    c->launches += (n > 0 ? 3 : 1) + (g.ncell > 0 ? 1 : 0) + (n > 0 ? 1 : 0) + 1; // cells, bonds, gather
+    c->launches += (n > 0 ? 3 : 1) + (g.ncell > 0 ? 1 : 0) + (n > 0 ? 1 : 0) + 1; // cells, sort, bonds|pack, gather
     ENS(c->prec, sizeof(IkPRec) * std::max(n, 1));
     ENS(c->kin, sizeof(float4) * 2 * std::max(n, 1));
     ENS(c->diam32, sizeof(float) * std::max(n, 1));
-    if (g.ncell > 0) {
+    if (g.ncell > 0) { // sort ids inside each cell: deterministic order
         k_cell_sort_pack<<<(g.ncell + 127) / 128, 128, 0, c->stream>>>(
-            g, c->cell_start.as<int>(), c->sorted.as<int>(), s.pos.as<double>(),
-            s.has_vel ? s.vel.as<double>() : nullptr, s.has_mass ? s.mass.as<double>() : nullptr,
-            s.diam.as<double>(), c->prec.as<IkPRec>(), c->kin.as<float4>(), c->diam32.as<float>(),
-            prec == IK_PREC_FP32 ? 1 : 0);
+            g, c->cell_start.as<int>(), c->sorted.as<int>(), nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+            nullptr, 0);
         CK(cudaGetLastError());
     }
-    if (timing) CK(cudaEventRecord(c->ev[1], c->stream));
     unsigned long long* cnt = s.counters.as<unsigned long long>();
     if (prec == IK_PREC_FP32) {
-        const int NV = D == 2 ? 2 : 3;
-        ENS(c->bonds32, sizeof(float4) * NV * (size_t)c->maxb * std::max(n, 1));
-        ENS(c->nb32, sizeof(int) * std::max(n, 1));
-        CK(launch_bonds32(D, g, c->pot, c->cg.kappa, n, c->prec.as<IkPRec>(), c->diam32.as<float>(),
-                          c->cell_start.as<int>(), c->sorted.as<int>(), s.pos.as<double>(),
-                          c->bonds32.as<float4>(), c->maxb, c->nb32.as<int>(),
-                          c->status.as<int>(), c->maxnb.as<int>(), cnt, c->stream));
+        ENS(c->pos64, sizeof(IkB64) * std::max(n, 1));
+        CK(launch_pack32(g, n, c->sorted.as<int>(), c->cell_of.as<int>(), s.pos.as<double>(),
+                         s.has_vel ? s.vel.as<double>() : nullptr, s.has_mass ? s.mass.as<double>() : nullptr,
+                         s.diam.as<double>(), c->prec.as<IkPRec>(), c->pos64.as<IkB64>(), c->kin.as<float4>(),
+                         c->diam32.as<float>(), c->stream));
+        if (timing) CK(cudaEventRecord(c->ev[1], c->stream));
+        ENS(c->bonds_tmp, sizeof(float4) * (size_t)c->maxb * std::max(n, 1));
+        ENS(c->bonds32, sizeof(float4) * (size_t)c->maxb * std::max(n, 1));
+        ENS(c->nb32, sizeof(int) * (std::max(n, 1) + 1));
+        ENS(c->boff, sizeof(int) * (std::max(n, 1) + 1));
+        ENS(c->bsum, sizeof(int) * ((std::max(n, 1) + 4095) / 4096 + 1));
+        CK(launch_bonds32w(D, g, c->pot, c->cg.kappa, n, c->prec.as<IkPRec>(), c->diam32.as<float>(),
+                           c->cell_start.as<int>(), c->pos64.as<IkB64>(), c->bonds_tmp.as<float4>(), c->maxb,
+                           c->nb32.as<int>(), c->status.as<int>(), c->maxnb.as<int>(), cnt, c->stream));
+        CK(launch_scan(c->nb32.as<int>(), n, c->boff.as<int>(), c->bsum.as<int>(), c->stream));
+        CK(launch_bond_compact(n, c->maxb, c->nb32.as<int>(), c->boff.as<int>(), c->bonds_tmp.as<float4>(),
+                               c->bonds32.as<float4>(), c->stream));
+        c->launches += 5;
         if (timing) CK(cudaEventRecord(c->ev[2], c->stream));
         GatherArgs32 a{};
         a.g = g;
@@ -388,15 +397,18 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         a.R2 = c->cg.rcutsq;
         a.npairs = c->gl.npairs;
         a.w0 = c->gl.w0;
-        for (int k = 0; k < 32; ++k) { a.xi[k] = c->gl.t[k]; a.w[k] = c->gl.wt[k]; }
+        for (int k = 0; k < 32; ++k) {
+            a.xi2[k] = c->gl.t[k] * c->gl.t[k];
+            a.m2xi[k] = -2.0f * c->gl.t[k];
+            a.w[k] = c->gl.wt[k];
+        }
         a.prec = c->prec.as<IkPRec>();
+        a.pos64 = c->pos64.as<IkB64>();
         a.cell_start = c->cell_start.as<int>();
-        a.nb = c->nb32.as<int>();
+        a.boff = c->boff.as<int>();
         a.bonds = c->bonds32.as<float4>();
         a.maxb = c->maxb;
         a.kin = c->kin.as<float4>();
-        a.sorted = c->sorted.as<int>();
-        a.pos = s.pos.as<double>();
         a.gpts = c->gpts_d.as<float4>();
         a.grid = c->grid_d.as<double>();
         a.items = c->items_d.as<int4>();
@@ -418,8 +430,11 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         CK(cudaMemsetAsync(c->work_counter.p, 0, sizeof(int), c->stream));
         size_t smem = (size_t)IK_WARPS_GATHER * ((size_t)c->halo_cap * 16 + (size_t)a.qcap * 4);
         int blocks = std::min(c->nitems, c->sm_count * 2);
-        if (blocks > 0) CK(launch_gather32(a, c->cg.kind, (c->flags & IK_FLAG_NO_KAHAN) == 0, blocks, 32 * IK_WARPS_GATHER, smem, c->stream));
+        if (blocks > 0)
+            CK(launch_gather32(a, c->cg.kind, (c->flags & IK_FLAG_LANE_KAHAN) != 0, blocks, 32 * IK_WARPS_GATHER,
+                               smem, c->stream));
     } else {
+        if (timing) CK(cudaEventRecord(c->ev[1], c->stream));
         ENS(c->bonds64, sizeof(IkB64) * (size_t)c->maxb * std::max(n, 1));
         ENS(c->nb64, sizeof(int) * std::max(n, 1));
         if (n > 0) {

@@ -1,0 +1,318 @@
+// ik_bonds.cu -- per-frame preparation of the tuned FP32 path: particle packing in
+// cell order, the force-active bond list (one warp per particle) and its compaction
+// into a CSR layout, and a multi-block exclusive scan.
+//
+// Replaces, for the tuned path, the Aboria neighbour search around each particle and
+// the per-(grid point, pair) force evaluation of IrvingKirkwood::compute
+// (irvingkirkwood/IrvingKirkwood.h:93-105 with potential/Polydisperse12.h:38-55): here
+// the force of every directed bond is evaluated once per frame.
+#include "ik_kernels.h"
+
+#define FULL 0xffffffffu
+
+// ---------------------------------------------------------------------------
+// Pack the particles in cell order: FP32 position relative to the cell corner
+// (wrapped in FP64), the raw FP64 position, kinetic coefficients m v(x)v, FP32
+// diameter.  One thread per sorted particle.
+__global__ void k_pack32(IkGeom g, int n, const int* __restrict__ sorted, const int* __restrict__ cell_of,
+                         const double* __restrict__ pos, const double* __restrict__ vel,
+                         const double* __restrict__ mass, const double* __restrict__ diam,
+                         IkPRec* __restrict__ prec, IkB64* __restrict__ pos64, float4* __restrict__ kin,
+                         float* __restrict__ diam32)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    int i = sorted[p];
+    int c = cell_of[i];
+    int cx = c % g.nc[0], cy = (c / g.nc[0]) % g.nc[1], cz = c / (g.nc[0] * g.nc[1]);
+    double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+    pos64[p] = make_ikb64(x, y, z, 0.0);
+    // the fractional box coordinate exactly as k_bin computed it (ik_cell_coord), so
+    // that the offset inside the cell is consistent with the cell index
+    double tx = (x - g.lo[0]) / g.L[0], ty = (y - g.lo[1]) / g.L[1];
+    tx -= floor(tx);
+    ty -= floor(ty);
+    IkPRec r;
+    r.x = (float)(tx * g.L[0] - cx * g.cw[0]);
+    r.y = (float)(ty * g.L[1] - cy * g.cw[1]);
+    if (g.dim == 3) {
+        double tz = (z - g.lo[2]) / g.L[2];
+        tz -= floor(tz);
+        r.z = (float)(tz * g.L[2] - cz * g.cw[2]);
+    } else {
+        r.z = 0.0f;
+    }
+    r.cell = c;
+    prec[p] = r;
+    double m = mass ? mass[i] : 1.0;
+    double vx = vel ? vel[3 * i] : 0.0, vy = vel ? vel[3 * i + 1] : 0.0, vz = vel ? vel[3 * i + 2] : 0.0;
+    if (g.dim == 2) {
+        kin[p] = make_float4((float)(m * vx * vx), (float)(m * vy * vy), (float)(m * vx * vy), 0.f);
+    } else {
+        kin[2 * p] = make_float4((float)(m * vx * vx), (float)(m * vy * vy), (float)(m * vz * vz), (float)(m * vx * vy));
+        kin[2 * p + 1] = make_float4((float)(m * vx * vz), (float)(m * vy * vz), 0.f, 0.f);
+    }
+    diam32[p] = (float)diam[i];
+}
+
+// ---------------------------------------------------------------------------
+// Force-active bonds of one particle per warp.  The 3^d stencil cells are set up by
+// lanes 0..S-1; their candidates are walked 32 at a time (a lane finds its cell by
+// binary search over the stencil prefix sums).  Each candidate is screened in FP32
+// from the cell-relative positions; survivors are re-measured from the FP64
+// positions (minimum image in FP64), so that r_ij carries only its final FP32
+// rounding -- the r^-14 force amplifies position rounding for overlapping pairs.
+// Output record (16 B): {hb_x, hb_y, hb_z, f'} with hb = kappa * r_ij / 2 (scaled half
+// bond, r_ij = r_j - r_i) and f' = 2 forceDivR / kappa^2, so that
+// f' * hb (x) hb = 0.5 * forceDivR * r_ij (x) r_ij.  Written at a fixed stride of
+// `maxb` records per particle in candidate order (stencil cell, then ascending
+// sorted index): deterministic.
+template <int DIM>
+__global__ void __launch_bounds__(256) k_bonds32w(IkGeom g, IkPoly12 pot, float kappa, int n,
+                                                  const IkPRec* __restrict__ prec,
+                                                  const float* __restrict__ diam32,
+                                                  const int* __restrict__ cell_start,
+                                                  const IkB64* __restrict__ pos64, float4* __restrict__ tmp,
+                                                  int maxb, int* __restrict__ nb, int* __restrict__ status,
+                                                  int* __restrict__ maxnb,
+                                                  unsigned long long* __restrict__ nbond_total)
+{
+    const int lane = threadIdx.x & 31;
+    const int p = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    if (p >= n) return; // warp-uniform
+    const IkPRec me = prec[p];
+    const int c = me.cell;
+    const int home[3] = {c % g.nc[0], (c / g.nc[0]) % g.nc[1], c / (g.nc[0] * g.nc[1])};
+    // stencil extent per axis
+    int lo[3], len[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (a >= DIM || g.nc[a] == 1) { lo[a] = 0; len[a] = 1; }
+        else if (g.all_bond[a]) { lo[a] = 0; len[a] = g.nc[a]; }
+        else { lo[a] = home[a] - 1; len[a] = 3; }
+    }
+    const int S = len[0] * len[1] * len[2]; // <= 27
+    int sstart = 0, scnt = 0;
+    float sox = 0.f, soy = 0.f, soz = 0.f;
+    if (lane < S) {
+        int ix = lane % len[0], iy = (lane / len[0]) % len[1], iz = lane / (len[0] * len[1]);
+        int ux = lo[0] + ix, uy = lo[1] + iy, uz = lo[2] + iz;
+        int wx = ik_wrap(ux, g.nc[0]), wy = ik_wrap(uy, g.nc[1]), wz = DIM == 3 ? ik_wrap(uz, g.nc[2]) : 0;
+        int cell = (wz * g.nc[1] + wy) * g.nc[0] + wx;
+        sstart = cell_start[cell];
+        scnt = cell_start[cell + 1] - sstart;
+        sox = (float)((ux - home[0]) * g.cw[0]);
+        soy = (float)((uy - home[1]) * g.cw[1]);
+        soz = DIM == 3 ? (float)((uz - home[2]) * g.cw[2]) : 0.f;
+    }
+    int incl = scnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const int excl = incl - scnt;
+    const int total = __shfl_sync(FULL, incl, 31);
+    const bool allx = len[0] > 3 || (g.all_bond[0] && g.nc[0] > 1);
+    const bool ally = len[1] > 3 || (g.all_bond[1] && g.nc[1] > 1);
+    const bool allz = DIM == 3 && (len[2] > 3 || (g.all_bond[2] && g.nc[2] > 1));
+    const float L0 = (float)g.L[0], L1 = (float)g.L[1], L2 = (float)g.L[2];
+    const float rc2 = (float)pot.rcutsq, mr2 = (float)pot.max_rcut_sq;
+    const float eps = (float)pot.eps, v12 = (float)(12.0 * pot.v0), c1x2 = (float)(2.0 * pot.c1),
+                c2x4 = (float)(4.0 * pot.c2);
+    const float screen = 1.0f + 1e-4f;
+    const float di = diam32[p];
+    const IkB64 pi = pos64[p];
+    const float hk = 0.5f * kappa, fk = 2.0f / (kappa * kappa);
+    int cnt = 0;
+    for (int base = 0; base < total; base += 32) {
+        const int v = base + lane;
+        // stencil slot of candidate v: largest s with excl_s <= v (binary search)
+        int s = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            int t = s + step;
+            int et = __shfl_sync(FULL, excl, t & 31);
+            if (t < S && et <= v) s = t;
+        }
+        const int qs = __shfl_sync(FULL, sstart, s), qe = __shfl_sync(FULL, excl, s);
+        const float ox = __shfl_sync(FULL, sox, s), oy = __shfl_sync(FULL, soy, s), oz = __shfl_sync(FULL, soz, s);
+        bool act = false;
+        float4 rec = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (v < total) {
+            const int q = qs + (v - qe);
+            if (q != p) {
+                const IkPRec o = prec[q];
+                float bx = ox + (o.x - me.x), by = oy + (o.y - me.y), bz = DIM == 3 ? oz + (o.z - me.z) : 0.f;
+                if (allx) bx -= L0 * rintf(bx / L0);
+                if (ally) by -= L1 * rintf(by / L1);
+                if (allz) bz -= L2 * rintf(bz / L2);
+                float r2 = bx * bx + by * by + bz * bz;
+                const float dj = diam32[q];
+                const float sig = 0.5f * (di + dj) * (1.f - eps * fabsf(di - dj));
+                const float s2 = sig * sig;
+                if (r2 < mr2 * screen && r2 < rc2 * s2 * screen) {
+                    const IkB64 pj = pos64[q];
+                    double dx = pj.x - pi.x, dy = pj.y - pi.y;
+                    dx = fma(-g.L[0], rint(dx * g.invL[0]), dx);
+                    dy = fma(-g.L[1], rint(dy * g.invL[1]), dy);
+                    bx = (float)dx;
+                    by = (float)dy;
+                    if (DIM == 3) {
+                        double dz = pj.z - pi.z;
+                        dz = fma(-g.L[2], rint(dz * g.invL[2]), dz);
+                        bz = (float)dz;
+                    }
+                    r2 = bx * bx + by * by + bz * bz;
+                    if (r2 < mr2 && r2 < rc2 * s2) {
+                        const float r2inv = s2 / r2;
+                        const float r6 = r2inv * r2inv * r2inv;
+                        const float f = (v12 * r2inv * r6 * r6 - c1x2 - c2x4 * (r2 / s2)) / s2;
+                        rec = make_float4(hk * bx, hk * by, hk * bz, fk * f);
+                        act = true;
+                    }
+                }
+            }
+        }
+        const unsigned bal = __ballot_sync(FULL, act);
+        const int rank = __popc(bal & ((1u << lane) - 1u));
+        if (act && cnt + rank < maxb) tmp[(size_t)p * maxb + cnt + rank] = rec;
+        cnt += __popc(bal);
+    }
+    if (lane == 0) {
+        nb[p] = cnt < maxb ? cnt : maxb;
+        if (cnt > maxb) atomicOr(status, IK_ST_BOND_OVERFLOW);
+        atomicMax(maxnb, cnt);
+        atomicAdd(nbond_total, (unsigned long long)cnt);
+    }
+}
+
+// Compact the fixed-stride records into CSR order (boff = exclusive scan of nb).
+__global__ void k_bond_compact(int n, int maxb, const int* __restrict__ nb, const int* __restrict__ boff,
+                               const float4* __restrict__ tmp, float4* __restrict__ bonds)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int p = t / maxb, k = t - p * maxb;
+    if (p >= n) return;
+    if (k < nb[p]) bonds[boff[p] + k] = tmp[(size_t)p * maxb + k];
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan of n ints (any n < 2^31): per-block sums, then each block adds the
+// sum of the blocks before it and scans its own tile.  Tiles of 4096 (1024 x 4).
+__device__ __forceinline__ int ik_block_excl_scan(int v, int* wsum)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) wsum[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        int w = lane < (int)(blockDim.x >> 5) ? wsum[lane] : 0;
+        int wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(FULL, wi, o);
+            if (lane >= o) wi += t;
+        }
+        wsum[lane] = wi - w;
+    }
+    __syncthreads();
+    int r = wsum[wid] + incl - v;
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_sums(const int* __restrict__ in, int n, int* __restrict__ bsum)
+{
+    __shared__ int red[32];
+    int base = blockIdx.x * 4096 + threadIdx.x * 4, s = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) s += (base + k < n) ? in[base + k] : 0;
+    s = __reduce_add_sync(FULL, s);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int t = red[threadIdx.x];
+        t = __reduce_add_sync(FULL, t);
+        if (threadIdx.x == 0) bsum[blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_apply(const int* __restrict__ in, int n, const int* __restrict__ bsum,
+                                                     int* __restrict__ out)
+{
+    __shared__ int wsum[32];
+    __shared__ int prefix_s;
+    // sum of the blocks before this one
+    int pre = 0;
+    for (int b = threadIdx.x; b < (int)blockIdx.x; b += blockDim.x) pre += bsum[b];
+    pre = __reduce_add_sync(FULL, pre);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = pre;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int t = wsum[threadIdx.x];
+        t = __reduce_add_sync(FULL, t);
+        if (threadIdx.x == 0) prefix_s = t;
+    }
+    __syncthreads();
+    const int prefix = prefix_s;
+    int base = blockIdx.x * 4096 + threadIdx.x * 4;
+    int v[4], s = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { v[k] = (base + k < n) ? in[base + k] : 0; s += v[k]; }
+    int run = prefix + ik_block_excl_scan(s, wsum);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (base + k < n) out[base + k] = run;
+        run += v[k];
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) out[n] = run;
+}
+
+cudaError_t launch_scan(const int* in, int n, int* out, int* bsum, cudaStream_t st)
+{
+    int blocks = (n + 4095) / 4096;
+    if (blocks < 1) blocks = 1;
+    k_scan_sums<<<blocks, 1024, 0, st>>>(in, n, bsum);
+    k_scan_apply<<<blocks, 1024, 0, st>>>(in, n, bsum, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack32(IkGeom g, int n, const int* sorted, const int* cell_of, const double* pos,
+                          const double* vel, const double* mass, const double* diam, IkPRec* prec, IkB64* pos64,
+                          float4* kin, float* diam32, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    k_pack32<<<(n + 255) / 256, 256, 0, st>>>(g, n, sorted, cell_of, pos, vel, mass, diam, prec, pos64, kin, diam32);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bonds32w(int dim, IkGeom g, IkPoly12 pot, float kappa, int n, const IkPRec* prec,
+                            const float* diam32, const int* cell_start, const IkB64* pos64, float4* tmp, int maxb,
+                            int* nb, int* status, int* maxnb, unsigned long long* nbond_total, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    const int wpb = 8;
+    int blocks = (n + wpb - 1) / wpb;
+    if (dim == 2)
+        k_bonds32w<2><<<blocks, 32 * wpb, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, pos64, tmp, maxb, nb,
+                                                   status, maxnb, nbond_total);
+    else
+        k_bonds32w<3><<<blocks, 32 * wpb, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, pos64, tmp, maxb, nb,
+                                                   status, maxnb, nbond_total);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bond_compact(int n, int maxb, const int* nb, const int* boff, const float4* tmp, float4* bonds,
+                                cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    long long t = (long long)n * maxb;
+    k_bond_compact<<<(int)((t + 255) / 256), 256, 0, st>>>(n, maxb, nb, boff, tmp, bonds);
+    return cudaGetLastError();
+}

@@ -141,124 +141,6 @@ __device__ __forceinline__ StencilAxis ik_axis(const IkGeom& g, int c, int home)
     return a;
 }
 
-// 5a. FP32 force-active bond records (tuned path).  One thread per sorted particle.
-//     Record (float4 x NV): 2D {hbx,hby,hh,cxx} {cyy,cxy,-,-}; 3D {hbx,hby,hbz,hh}
-//     {cxx,cyy,czz,cxy} {cxz,cyz,-,-}; hb = kappa*r_ij/2 (scaled half bond),
-//     hh = |hb|^2, c = 0.5*forceDivR*r_ij(x)r_ij (unscaled), r_ij = r_j - r_i.
-//     Candidates are screened in FP32 from the cell-relative positions; every pair
-//     that may be force-active is then re-measured from the FP64 positions (minimum
-//     image in FP64) so that r_ij carries only its final FP32 rounding -- this keeps
-//     the force accurate for strongly overlapping pairs (r << sigma), where the
-//     FP32 rounding of positions would be amplified by the r^-14 force.
-template <int DIM>
-__global__ void k_bonds32(IkGeom g, IkPoly12 pot, float kappa, int n,
-                          const IkPRec* __restrict__ prec, const float* __restrict__ diam32,
-                          const int* __restrict__ cell_start, const int* __restrict__ sorted,
-                          const double* __restrict__ pos, float4* __restrict__ bonds, int maxb,
-                          int* __restrict__ nb, int* __restrict__ status, int* __restrict__ maxnb,
-                          unsigned long long* __restrict__ nbond_total)
-{
-    constexpr int NV = DIM == 2 ? 2 : 3;
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = p < n;
-    int cnt = 0;
-    if (valid) {
-    IkPRec me = prec[p];
-    int c = me.cell;
-    int cx = c % g.nc[0], cy = (c / g.nc[0]) % g.nc[1], cz = c / (g.nc[0] * g.nc[1]);
-    float di = diam32[p];
-    float cw0 = (float)g.cw[0], cw1 = (float)g.cw[1], cw2 = (float)g.cw[2];
-    float L0 = (float)g.L[0], L1 = (float)g.L[1], L2 = (float)g.L[2];
-    float rc2 = (float)pot.rcutsq, mr2 = (float)pot.max_rcut_sq;
-    float eps = (float)pot.eps, v12 = (float)(12.0 * pot.v0), c1x2 = (float)(2.0 * pot.c1),
-          c2x4 = (float)(4.0 * pot.c2);
-    const float screen = 1.0f + 1e-4f; // FP32 screening margin on r^2
-    const int ip = sorted[p];
-    const double xi = pos[3 * ip], yi = pos[3 * ip + 1], zi = pos[3 * ip + 2];
-    const double iL0 = 1.0 / g.L[0], iL1 = 1.0 / g.L[1], iL2 = 1.0 / g.L[2];
-    StencilAxis az = ik_axis(g, 2, cz), ay = ik_axis(g, 1, cy), ax = ik_axis(g, 0, cx);
-    for (int zz = az.lo; zz <= az.hi; ++zz) {
-        int wz = DIM == 3 ? ik_wrap(zz, g.nc[2]) : 0;
-        for (int yy = ay.lo; yy <= ay.hi; ++yy) {
-            int wy = ik_wrap(yy, g.nc[1]);
-            for (int xx = ax.lo; xx <= ax.hi; ++xx) {
-                int wx = ik_wrap(xx, g.nc[0]);
-                int cell = (wz * g.nc[1] + wy) * g.nc[0] + wx;
-                float ox = (xx - cx) * cw0, oy = (yy - cy) * cw1, oz = (zz - cz) * cw2;
-                int e = cell_start[cell + 1];
-                for (int q = cell_start[cell]; q < e; ++q) {
-                    if (q == p) continue;
-                    IkPRec o = prec[q];
-                    float bx = ox + (o.x - me.x), by = oy + (o.y - me.y), bz = DIM == 3 ? oz + (o.z - me.z) : 0.f;
-                    if (ax.all) bx -= L0 * rintf(bx / L0);
-                    if (ay.all) by -= L1 * rintf(by / L1);
-                    if (DIM == 3 && az.all) bz -= L2 * rintf(bz / L2);
-                    float r2 = bx * bx + by * by + bz * bz;
-                    if (!(r2 < mr2 * screen)) continue;
-                    float dj = diam32[q];
-                    float sig = 0.5f * (di + dj) * (1.f - eps * fabsf(di - dj));
-                    float s2 = sig * sig;
-                    if (!(r2 < rc2 * s2 * screen)) continue;
-                    {   // FP64 re-measure of r_ij = minimg(r_j - r_i)
-                        const int jp = sorted[q];
-                        double dx = pos[3 * jp] - xi, dy = pos[3 * jp + 1] - yi;
-                        dx = fma(-g.L[0], rint(dx * iL0), dx);
-                        dy = fma(-g.L[1], rint(dy * iL1), dy);
-                        bx = (float)dx;
-                        by = (float)dy;
-                        if (DIM == 3) {
-                            double dz = pos[3 * jp + 2] - zi;
-                            dz = fma(-g.L[2], rint(dz * iL2), dz);
-                            bz = (float)dz;
-                        }
-                        r2 = bx * bx + by * by + bz * bz;
-                        if (!(r2 < mr2) || !(r2 < rc2 * s2)) continue;
-                    }
-                    float r2inv = s2 / r2;
-                    float r6 = r2inv * r2inv * r2inv;
-                    float f = (v12 * r2inv * r6 * r6 - c1x2 - c2x4 * (r2 / s2)) / s2;
-                    if (cnt < maxb) {
-                        float4* rec = bonds + ((size_t)p * maxb + cnt) * NV;
-                        float hf = 0.5f * f;
-                        float hx = 0.5f * kappa * bx, hy = 0.5f * kappa * by, hz = 0.5f * kappa * bz;
-                        if (DIM == 2) {
-                            rec[0] = make_float4(hx, hy, hx * hx + hy * hy, hf * bx * bx);
-                            rec[1] = make_float4(hf * by * by, hf * bx * by, 0.f, 0.f);
-                        } else {
-                            rec[0] = make_float4(hx, hy, hz, hx * hx + hy * hy + hz * hz);
-                            rec[1] = make_float4(hf * bx * bx, hf * by * by, hf * bz * bz, hf * bx * by);
-                            rec[2] = make_float4(hf * bx * bz, hf * by * bz, 0.f, 0.f);
-                        }
-                    }
-                    ++cnt;
-                }
-            }
-        }
-    }
-    nb[p] = cnt < maxb ? cnt : maxb;
-    if (cnt > maxb) atomicOr(status, IK_ST_BOND_OVERFLOW);
-    atomicMax(maxnb, cnt);
-    } // valid
-    // warp-aggregated count of force-active directed bonds
-    unsigned v = __reduce_add_sync(0xffffffffu, (unsigned)cnt);
-    if ((threadIdx.x & 31) == 0 && v) atomicAdd(nbond_total, (unsigned long long)v);
-}
-cudaError_t launch_bonds32(int dim, IkGeom g, IkPoly12 pot, float kappa, int n, const IkPRec* prec,
-                          const float* diam32, const int* cell_start, const int* sorted, const double* pos,
-                          float4* bonds, int maxb, int* nb, int* status, int* maxnb,
-                          unsigned long long* nbond_total, cudaStream_t st)
-{
-    if (n <= 0) return cudaSuccess;
-    int blocks = (n + 127) / 128;
-    if (dim == 2)
-        k_bonds32<2><<<blocks, 128, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, sorted, pos, bonds, maxb,
-                                              nb, status, maxnb, nbond_total);
-    else
-        k_bonds32<3><<<blocks, 128, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, sorted, pos, bonds, maxb,
-                                              nb, status, maxnb, nbond_total);
-    return cudaGetLastError();
-}
-
 // 5b. FP64 force-active bond records (plain path): {rij.x, rij.y, rij.z, forceDivR}
 //     in sorted-particle order, bit-identical selection to the oracle.
 __global__ void k_bonds64(IkGeom g, IkPoly12 pot, int n, const int* __restrict__ sorted,

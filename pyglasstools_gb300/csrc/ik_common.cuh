@@ -22,6 +22,7 @@ struct IkGeom {
     int reach_bond[3];   // stencil half-width for the bond search (cells)
     int all_bond[3];     // 1: stencil covers the whole axis once
     double L[3], lo[3], cw[3];
+    double invL[3];      // 1 / L (used for minimum-image rounding only)
     int periodic[3];
 };
 

@@ -3,23 +3,26 @@
 // Computes, for every grid point x_g,
 //   T(x_g) = sum_{i: |x_g - r_i| < R} sum_{j in bonds(i)} c_ij * int_0^1 Delta(x_g - r_i - s r_ij) ds
 //          + sum_{i: |x_g - r_i| < R} m_i v_i (x) v_i Delta(x_g - r_i)
-// the loop of IrvingKirkwood::compute (irvingkirkwood/IrvingKirkwood.h:74-110) with
+// i.e. the loop of IrvingKirkwood::compute (irvingkirkwood/IrvingKirkwood.h:74-110) with
 // VirialStress::compute_cg (ListofCommonObservables.h:72-82) and the intended
 // KineticStress (ListofCommonObservables.h:131-148), c_ij = 0.5 * forceDivR * r_ij (x) r_ij.
 //
 // Organisation (one warp = one worker, persistent, dynamic work queue):
-//   * a work item is a range of grid-point groups inside one spatial bin of
-//     bw^dim cells; the warp stages the bin's halo (particles of the cells within
-//     R) into its private shared memory as scaled, bin-relative FP32 positions;
-//   * a group is IK_P grid points; lanes test 32 staged particles at a time
-//     against the group (FP32, with an FP64 re-check inside a thin band around R
-//     so the selection equals the FP64 rule), accumulate the kinetic term, and
-//     push (particle, bond, grid mask) slots of accepted particles into a
-//     per-warp queue; every full batch of 32 slots is processed with all lanes
-//     busy: per slot, the bond integral by symmetric Gauss-Legendre for each grid
-//     point of the group, accumulated in FP32 (optionally Kahan-compensated);
-//   * the group's partial sums are combined across lanes with a transposing
-//     butterfly (each shuffle level halves the values per lane) and written in FP64.
+//   * a work item is a range of grid-point groups inside one spatial bin of bw^dim
+//     cells; the warp stages the bin's halo (particles of the cells within R) into its
+//     private shared memory as scaled, bin-relative FP32 positions;
+//   * a group is IK_P grid points; lanes test 32 staged particles at a time against
+//     the group (FP32, with an FP64 re-check inside a thin band around R so that the
+//     selection equals the FP64 rule), accumulate the kinetic term, and push
+//     (particle, bond, grid mask) slots of accepted particles into a per-warp queue;
+//     every full batch of 32 slots is processed with all lanes busy: per slot, the
+//     bond integral by symmetric Gauss-Legendre for each grid point of the group;
+//   * accumulation: every lane sums its slots of a group in FP32 (optionally with
+//     Kahan compensation); the 32 lane partials are combined with error-free
+//     transformations (TwoSum) in a transposing butterfly -- each shuffle level halves
+//     the values a lane holds -- and the compensated result is written in FP64.
+// Bond records (CSR, 16 B): {hb = kappa r_ij / 2, f' = 2 forceDivR / kappa^2}; the
+// stress coefficient is f' hb (x) hb.
 #include "ik_kernels.h"
 
 #define FULL 0xffffffffu
@@ -52,38 +55,65 @@ __device__ __forceinline__ float ik_kern(float q, float R2s)
         return q < 1.0f ? ik_ex2(-1.4426950408889634f * ik_rcp(1.0f - q)) : 0.0f;
     }
 }
-
-template <int DIM>
-struct Vec { float v[3]; };
-
-// Transposing butterfly: each lane holds V values (V power of two >= 32 is not
-// required); after the call lane l holds the warp total of value indices
-// idx(l, k), k < max(V/32, 1), where idx is given by ik_red_index.
-template <int V>
-__device__ __forceinline__ void ik_warp_transpose_reduce(float (&val)[V], int lane)
+// Kernel value of a particle already selected by the (FP64) support rule.
+template <int KIND>
+__device__ __forceinline__ float ik_kern_in(float q)
 {
-    int cur = V;
+    if (KIND == 1) return ik_ex2(-q);
+    if (KIND == 0) { float u = fmaxf(fmaf(-q, q, 1.0f), 0.0f); return u * u; }
+    if (KIND == 2) return 1.0f;
+    return q < 1.0f ? ik_ex2(-1.4426950408889634f * ik_rcp(1.0f - q)) : 0.0f;
+}
+
+// TwoSum (Knuth): s + e == a + b exactly.
+__device__ __forceinline__ void ik_two_sum(float a, float b, float& s, float& e)
+{
+    s = a + b;
+    float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+__host__ __device__ constexpr int ik_pow2_ceil(int x) { int p = 1; while (p < x) p <<= 1; return p; }
+
+// Compensated transposing butterfly over a warp: on entry each lane holds V values
+// (hi[k], lo[k] = 0); after the call lane l holds, for k < max(V/32, 1), the warp sum
+// of value ik_red_index<V>(l, k) as hi[k] + lo[k] (hi + lo exact to ~2 ulp of the
+// sum, i.e. the accumulation of the 32 partials is compensated).
+template <int V>
+__device__ __forceinline__ void ik_warp_reduce_cmp(float (&hi)[V], float (&lo)[V], int lane)
+{
 #pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) {
+    for (int lev = 0; lev < 5; ++lev) {
+        const int o = 16 >> lev;
+        const int cur = (V >> lev) > 1 ? (V >> lev) : 1;
         if (cur > 1) {
-            int half = cur >> 1;
-            bool up = (lane & o) != 0;
+            const int half = cur >> 1;
+            const bool up = (lane & o) != 0;
 #pragma unroll
             for (int k = 0; k < V / 2; ++k) {
                 if (k < half) {
-                    float send = up ? val[k] : val[k + half];
-                    float keep = up ? val[k + half] : val[k];
-                    float recv = __shfl_xor_sync(FULL, send, o);
-                    val[k] = keep + recv;
+                    float sh = up ? hi[k] : hi[k + half];
+                    float sl = up ? lo[k] : lo[k + half];
+                    float kh = up ? hi[k + half] : hi[k];
+                    float kl = up ? lo[k + half] : lo[k];
+                    float rh = __shfl_xor_sync(FULL, sh, o);
+                    float rl = __shfl_xor_sync(FULL, sl, o);
+                    float s, e;
+                    ik_two_sum(kh, rh, s, e);
+                    hi[k] = s;
+                    lo[k] = e + (kl + rl);
                 }
             }
-            cur = half;
         } else {
-            val[0] += __shfl_xor_sync(FULL, val[0], o);
+            float rh = __shfl_xor_sync(FULL, hi[0], o);
+            float rl = __shfl_xor_sync(FULL, lo[0], o);
+            float s, e;
+            ik_two_sum(hi[0], rh, s, e);
+            hi[0] = s;
+            lo[0] = e + (lo[0] + rl);
         }
     }
 }
-// value index held in slot k of lane `lane` after ik_warp_transpose_reduce<V>
 template <int V>
 __device__ __forceinline__ int ik_red_index(int lane, int k)
 {
@@ -99,15 +129,12 @@ __device__ __forceinline__ int ik_red_index(int lane, int k)
     return idx + k;
 }
 
-__host__ __device__ constexpr int ik_pow2_ceil(int x) { int p = 1; while (p < x) p <<= 1; return p; }
-
-template <int DIM, int KIND, bool KAHAN>
+// NP: number of symmetric Gauss-Legendre node pairs (compile-time when > 0; 0 = runtime).
+template <int DIM, int KIND, bool KAHAN, int NP>
 __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
 {
     constexpr int NC = DIM == 2 ? 3 : 6;       // unique tensor components
-    constexpr int NV = DIM == 2 ? 2 : 3;       // float4 per bond record
     constexpr int P = IK_P;
-    constexpr int VR = ik_pow2_ceil(2 * P * NC); // reduction width (virial + kinetic)
 
     extern __shared__ float4 smem[];
     const int lane = threadIdx.x & 31;
@@ -117,6 +144,7 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
 
     const float R2s = a.R2s, margin = a.margin, kappa = a.kappa;
     const bool want_kin = (a.fields & 2) != 0;
+    const int npairs = NP > 0 ? NP : a.npairs;
     unsigned long long my_pairs = 0, my_triples = 0;
 
     for (;;) {
@@ -165,9 +193,7 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                     if (lane >= o) incl += t;
                 }
                 unsigned fit = __ballot_sync(FULL, cid < nh && nst + incl <= a.halo_cap);
-                // cells fit as a prefix; count leading ones
-                int k = __popc(fit & ~(fit + 1u)) ; // length of the run of ones from bit 0
-                if ((fit & 1u) == 0) k = 0;
+                int k = __popc(fit & ~(fit + 1u)); // length of the run of ones from bit 0
                 if (k == 0) {
                     if (nst == 0 && hc < nh) {
                         // a single cell exceeds the halo buffer: report and skip it
@@ -182,12 +208,11 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                     for (int t = 0; t < ccnt; ++t) {
                         int q = cstart + t;
                         IkPRec r = a.prec[q];
-                        int nbq = a.nb[q];
                         float4 s;
                         s.x = fmaf(kappa, r.x, ox);
                         s.y = fmaf(kappa, r.y, oy);
                         s.z = DIM == 3 ? fmaf(kappa, r.z, oz) : 0.f;
-                        s.w = __int_as_float((q << 6) | nbq);
+                        s.w = __int_as_float(q);
                         stage[dst + t] = s;
                     }
                 }
@@ -218,52 +243,69 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
 #pragma unroll
                     for (int c = 0; c < NC; ++c) { acc[p][c] = 0.f; cmp[p][c] = 0.f; kac[p][c] = 0.f; }
 
-                // one 32-slot batch of (staged particle, bond, mask)
+                // one slot: staged particle s, its bond k, grid mask m
                 auto process_slot = [&](int e) {
-                    int s = e >> 10, k = (e >> 4) & 63, m = e & 15;
-                    float4 sp = stage[s];
-                    int q = __float_as_int(sp.w) >> 6;
-                    const float4* rec = a.bonds + ((size_t)q * a.maxb + k) * NV;
-                    float4 r0 = __ldg(rec), r1 = __ldg(rec + 1);
-                    float4 r2v = NV == 3 ? __ldg(rec + 2) : make_float4(0.f, 0.f, 0.f, 0.f);
-                    float hbx, hby, hbz, hh, cf[NC];
+                    const int s = e >> 10, m = e & 15;
+                    const float4 sp = stage[s];
+                    const int q = __float_as_int(sp.w);
+                    const float4 b = __ldg(a.bonds + a.boff[q] + ((e >> 4) & 63));
+                    const float hbx = b.x, hby = b.y, hbz = b.z;
+                    const float hh = DIM == 3 ? fmaf(hbz, hbz, fmaf(hby, hby, hbx * hbx)) : fmaf(hby, hby, hbx * hbx);
+                    const float fx = b.w * hbx, fy = b.w * hby;
+                    float cf[NC];
+                    cf[0] = fx * hbx;
+                    cf[1] = fy * hby;
                     if (DIM == 2) {
-                        hbx = r0.x; hby = r0.y; hbz = 0.f; hh = r0.z;
-                        cf[0] = r0.w; cf[1] = r1.x; cf[2] = r1.y;
+                        cf[2] = fx * hby;
                     } else {
-                        hbx = r0.x; hby = r0.y; hbz = r0.z; hh = r0.w;
-                        cf[0] = r1.x; cf[1] = r1.y; cf[2] = r1.z; cf[3] = r1.w;
-                        cf[4] = r2v.x; cf[5] = r2v.y;
+                        const float fz = b.w * hbz;
+                        cf[2] = fz * hbz;
+                        cf[3 % NC] = fx * hby;
+                        cf[4 % NC] = fx * hbz;
+                        cf[5 % NC] = fy * hbz;
                     }
-                    float mx0 = sp.x + hbx, my0 = sp.y + hby, mz0 = sp.z + hbz; // bond midpoint
+                    float cq[NP > 0 ? NP : 1];
+                    if constexpr (NP > 0) {
+#pragma unroll
+                        for (int t = 0; t < NP; ++t) cq[t] = a.xi2[t] * hh;
+                    }
+                    const float mx0 = sp.x + hbx, my0 = sp.y + hby, mz0 = sp.z + hbz; // bond midpoint
 #pragma unroll
                     for (int p = 0; p < P; ++p) {
-                        float mx = gu[p][0] - mx0, my = gu[p][1] - my0;
+                        const float mx = gu[p][0] - mx0, my = gu[p][1] - my0;
                         float M = mx * mx, mb = mx * hbx;
                         M = fmaf(my, my, M);
                         mb = fmaf(my, hby, mb);
                         if (DIM == 3) {
-                            float mz = gu[p][2] - mz0;
+                            const float mz = gu[p][2] - mz0;
                             M = fmaf(mz, mz, M);
                             mb = fmaf(mz, hbz, mb);
                         }
-                        // r^2(xi) = M - 2 xi mb + xi^2 hh  at the GL nodes
-                        float B = a.w0 != 0.f ? a.w0 * ik_kern<KIND>(M, R2s) : 0.f;
-#pragma unroll 4
-                        for (int t = 0; t < a.npairs; ++t) {
-                            float xi = a.xi[t];
-                            float base = fmaf(xi * xi, hh, M);
-                            float d = 2.f * xi * mb;
-                            float kp = ik_kern<KIND>(base - d, R2s);
-                            float km = ik_kern<KIND>(base + d, R2s);
-                            B = fmaf(a.w[t], kp + km, B);
+                        // r^2(xi) = M - 2 xi mb + xi^2 hh at the symmetric nodes +-xi
+                        float B = a.w0 * ik_kern<KIND>(M, R2s);
+                        if constexpr (NP > 0) {
+#pragma unroll
+                            for (int t = 0; t < NP; ++t) {
+                                const float base = M + cq[t];
+                                const float kp = ik_kern<KIND>(fmaf(a.m2xi[t], mb, base), R2s);
+                                const float km = ik_kern<KIND>(fmaf(-a.m2xi[t], mb, base), R2s);
+                                B = fmaf(a.w[t], kp + km, B);
+                            }
+                        } else {
+#pragma unroll 1
+                            for (int t = 0; t < npairs; ++t) {
+                                const float base = fmaf(a.xi2[t], hh, M);
+                                const float kp = ik_kern<KIND>(fmaf(a.m2xi[t], mb, base), R2s);
+                                const float km = ik_kern<KIND>(fmaf(-a.m2xi[t], mb, base), R2s);
+                                B = fmaf(a.w[t], kp + km, B);
+                            }
                         }
-                        B = ((m >> p) & 1) ? B : 0.f;
+                        B = (m & (1 << p)) ? B : 0.f;
 #pragma unroll
                         for (int c = 0; c < NC; ++c) {
                             if (KAHAN) {
-                                float y = fmaf(B, cf[c], -cmp[p][c]);
-                                float t2 = acc[p][c] + y;
+                                const float y = fmaf(B, cf[c], -cmp[p][c]);
+                                const float t2 = acc[p][c] + y;
                                 cmp[p][c] = (t2 - acc[p][c]) - y;
                                 acc[p][c] = t2;
                             } else {
@@ -276,50 +318,51 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
 
                 int qn = 0;
                 for (int base = 0; base < nst; base += 32) {
-                    int s = base + lane;
+                    const int s = base + lane;
                     int mask = 0, cnt = 0;
                     if (s < nst) {
-                        float4 sp = stage[s];
-                        int wq = __float_as_int(sp.w);
-                        int q = wq >> 6;
+                        const float4 sp = stage[s];
+                        const int q = __float_as_int(sp.w);
+                        float r2v[P];
 #pragma unroll
                         for (int p = 0; p < P; ++p) {
-                            float dx = gu[p][0] - sp.x, dy = gu[p][1] - sp.y;
+                            const float dx = gu[p][0] - sp.x, dy = gu[p][1] - sp.y;
                             float r2 = fmaf(dy, dy, dx * dx);
-                            if (DIM == 3) { float dz = gu[p][2] - sp.z; r2 = fmaf(dz, dz, r2); }
+                            if (DIM == 3) { const float dz = gu[p][2] - sp.z; r2 = fmaf(dz, dz, r2); }
                             bool in = r2 < R2s;
                             if (fabsf(r2 - R2s) < margin && gi[p] >= 0) {
                                 // boundary band: decide with the FP64 rule of the reference
-                                int i = a.sorted[q];
+                                const IkB64 pq = a.pos64[q];
                                 const double* xg = a.grid + 3 * (size_t)gi[p];
-                                double ddx = ik_minimg(__dsub_rn(xg[0], a.pos[3 * i]), a.g.L[0], a.g.periodic[0]);
-                                double ddy = ik_minimg(__dsub_rn(xg[1], a.pos[3 * i + 1]), a.g.L[1], a.g.periodic[1]);
-                                double ddz = ik_minimg(__dsub_rn(xg[2], a.pos[3 * i + 2]), a.g.L[2], a.g.periodic[2]);
+                                const double ddx = ik_minimg(__dsub_rn(xg[0], pq.x), a.g.L[0], a.g.periodic[0]);
+                                const double ddy = ik_minimg(__dsub_rn(xg[1], pq.y), a.g.L[1], a.g.periodic[1]);
+                                const double ddz = ik_minimg(__dsub_rn(xg[2], pq.z), a.g.L[2], a.g.periodic[2]);
                                 in = ik_dot3(ddx, ddy, ddz) < a.R2;
                             }
-                            if (in) {
-                                mask |= 1 << p;
-                                if (want_kin) {
-                                    float kv = ik_kern<KIND>(KIND == 1 ? r2 : r2, R2s);
-                                    if (DIM == 2) {
-                                        float4 kc = __ldg(a.kin + q);
-                                        kac[p][0] = fmaf(kv, kc.x, kac[p][0]);
-                                        kac[p][1] = fmaf(kv, kc.y, kac[p][1]);
-                                        kac[p][2] = fmaf(kv, kc.z, kac[p][2]);
-                                    } else {
-                                        float4 k0 = __ldg(a.kin + 2 * q), k1 = __ldg(a.kin + 2 * q + 1);
-                                        kac[p][0] = fmaf(kv, k0.x, kac[p][0]);
-                                        kac[p][1] = fmaf(kv, k0.y, kac[p][1]);
-                                        kac[p][2] = fmaf(kv, k0.z, kac[p][2]);
-                                        kac[p][NC > 3 ? 3 : 0] = fmaf(kv, k0.w, kac[p][NC > 3 ? 3 : 0]);
-                                        kac[p][NC > 4 ? 4 : 0] = fmaf(kv, k1.x, kac[p][NC > 4 ? 4 : 0]);
-                                        kac[p][NC > 5 ? 5 : 0] = fmaf(kv, k1.y, kac[p][NC > 5 ? 5 : 0]);
+                            r2v[p] = r2;
+                            if (in) mask |= 1 << p;
+                        }
+                        if (mask) {
+                            const int nbq = a.boff[q + 1] - a.boff[q];
+                            cnt = nbq;
+                            if (want_kin) {
+                                float4 k0 = __ldg(a.kin + (DIM == 2 ? q : 2 * q));
+                                float4 k1 = DIM == 3 ? __ldg(a.kin + 2 * q + 1) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                                for (int p = 0; p < P; ++p) {
+                                    const float kv = (mask & (1 << p)) ? ik_kern_in<KIND>(r2v[p]) : 0.f;
+                                    kac[p][0] = fmaf(kv, k0.x, kac[p][0]);
+                                    kac[p][1] = fmaf(kv, k0.y, kac[p][1]);
+                                    kac[p][2] = fmaf(kv, k0.z, kac[p][2]);
+                                    if (DIM == 3) {
+                                        kac[p][3 % NC] = fmaf(kv, k0.w, kac[p][3 % NC]);
+                                        kac[p][4 % NC] = fmaf(kv, k1.x, kac[p][4 % NC]);
+                                        kac[p][5 % NC] = fmaf(kv, k1.y, kac[p][5 % NC]);
                                     }
                                 }
                             }
+                            my_pairs += __popc(mask);
                         }
-                        cnt = mask ? (wq & 63) : 0;
-                        my_pairs += __popc(mask);
                     }
                     int incl = cnt;
 #pragma unroll
@@ -327,9 +370,9 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                         int t = __shfl_up_sync(FULL, incl, o);
                         if (lane >= o) incl += t;
                     }
-                    int tot = __shfl_sync(FULL, incl, 31);
-                    int off = qn + incl - cnt;
-                    int entry = (s << 10) | mask;
+                    const int tot = __shfl_sync(FULL, incl, 31);
+                    const int off = qn + incl - cnt;
+                    const int entry = (s << 10) | mask;
                     for (int k = 0; k < cnt; ++k) queue[off + k] = entry | (k << 4);
                     qn += tot;
                     __syncwarp();
@@ -342,35 +385,40 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                 if (lane < qn) process_slot(queue[lane]);
                 __syncwarp();
 
-                // ---- combine lanes and write the group's results (FP64)
-                float red[VR];
+                // ---- combine lanes (compensated) and write the group's results (FP64):
+                //      virial first, then kinetic, each a transposing butterfly of VH values
+                constexpr int VH = ik_pow2_ceil(P * NC);
+                constexpr int PER = VH >= 32 ? VH / 32 : 1;
 #pragma unroll
-                for (int p = 0; p < P; ++p)
+                for (int kinf = 0; kinf < 2; ++kinf) {
+                    if (kinf ? !want_kin : !(a.fields & 1)) continue; // warp-uniform
+                    float hi[VH], lo[VH];
 #pragma unroll
-                    for (int c = 0; c < NC; ++c) {
-                        red[p * NC + c] = KAHAN ? acc[p][c] - cmp[p][c] : acc[p][c];
-                        red[P * NC + p * NC + c] = kac[p][c];
-                    }
+                    for (int p = 0; p < P; ++p)
 #pragma unroll
-                for (int k = 2 * P * NC; k < VR; ++k) red[k] = 0.f;
-                ik_warp_transpose_reduce<VR>(red, lane);
-                constexpr int PER = VR >= 32 ? VR / 32 : 1;
+                        for (int c = 0; c < NC; ++c) {
+                            hi[p * NC + c] = kinf ? kac[p][c] : acc[p][c];
+                            lo[p * NC + c] = (!kinf && KAHAN) ? -cmp[p][c] : 0.f;
+                        }
 #pragma unroll
-                for (int k = 0; k < PER; ++k) {
-                    int idx = ik_red_index<VR>(lane, k);
-                    bool dup = VR < 32 && (lane & ((32 / VR) - 1)) != 0; // duplicated copies
-                    if (idx < 2 * P * NC && !dup) {
-                        int kinf = idx >= P * NC;
-                        int r = kinf ? idx - P * NC : idx;
-                        int p = r / NC, c = r - p * NC;
-                        int g = -1;
+                    for (int k = P * NC; k < VH; ++k) { hi[k] = 0.f; lo[k] = 0.f; }
+                    ik_warp_reduce_cmp<VH>(hi, lo, lane);
 #pragma unroll
-                        for (int pp = 0; pp < P; ++pp) if (pp == p) g = gi[pp];
-                        if (g >= 0 && (kinf ? want_kin : (a.fields & 1))) {
-                            double* out = kinf ? a.out_kin : a.out_vir;
-                            double v = (double)red[k] * (kinf ? a.kin_scale : a.vir_scale);
-                            size_t o = (size_t)g * NC + c;
-                            out[o] = first ? v : out[o] + v;
+                    for (int k = 0; k < PER; ++k) {
+                        const int idx = ik_red_index<VH>(lane, k);
+                        // with VH < 32 every value is held by 32/VH lanes: the lowest writes
+                        const bool owner = VH >= 32 || (lane & (32 / VH - 1)) == 0;
+                        if (idx < P * NC && owner) {
+                            const int p = idx / NC, c = idx - p * NC;
+                            int g = -1;
+#pragma unroll
+                            for (int pp = 0; pp < P; ++pp) if (pp == p) g = gi[pp];
+                            if (g >= 0) {
+                                double* out = kinf ? a.out_kin : a.out_vir;
+                                const double v = ((double)hi[k] + (double)lo[k]) * (kinf ? a.kin_scale : a.vir_scale);
+                                const size_t o = (size_t)g * NC + c;
+                                out[o] = first ? v : out[o] + v;
+                            }
                         }
                     }
                 }
@@ -390,45 +438,40 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
     }
 }
 
-template <int DIM, int KIND, bool KAHAN>
+template <int DIM, int KIND, bool KAHAN, int NP>
 static cudaError_t launch_one(const GatherArgs32& a, int blocks, int threads, size_t smem, cudaStream_t st)
 {
-    auto kfn = k_gather32<DIM, KIND, KAHAN>;
+    auto kfn = k_gather32<DIM, KIND, KAHAN, NP>;
     cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kfn<<<blocks, threads, smem, st>>>(a);
     return cudaGetLastError();
 }
 
-template <int DIM, bool KAHAN>
+template <int DIM, bool KAHAN, int NP>
 static cudaError_t launch_kind(const GatherArgs32& a, int kind, int blocks, int threads, size_t smem,
                                cudaStream_t st)
 {
     switch (kind) {
-    case 0: return launch_one<DIM, 0, KAHAN>(a, blocks, threads, smem, st);
-    case 1: return launch_one<DIM, 1, KAHAN>(a, blocks, threads, smem, st);
-    case 2: return launch_one<DIM, 2, KAHAN>(a, blocks, threads, smem, st);
-    default: return launch_one<DIM, 3, KAHAN>(a, blocks, threads, smem, st);
+    case 0: return launch_one<DIM, 0, KAHAN, NP>(a, blocks, threads, smem, st);
+    case 1: return launch_one<DIM, 1, KAHAN, NP>(a, blocks, threads, smem, st);
+    case 2: return launch_one<DIM, 2, KAHAN, NP>(a, blocks, threads, smem, st);
+    default: return launch_one<DIM, 3, KAHAN, NP>(a, blocks, threads, smem, st);
     }
+}
+
+template <int DIM, bool KAHAN>
+static cudaError_t launch_np(const GatherArgs32& a, int kind, int blocks, int threads, size_t smem, cudaStream_t st)
+{
+    if (a.npairs == 2) return launch_kind<DIM, KAHAN, 2>(a, kind, blocks, threads, smem, st);
+    return launch_kind<DIM, KAHAN, 0>(a, kind, blocks, threads, smem, st);
 }
 
 cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, int blocks, int threads,
                             size_t smem, cudaStream_t st)
 {
-    if (a.g.dim == 2) return kahan ? launch_kind<2, true>(a, kind, blocks, threads, smem, st)
-                                   : launch_kind<2, false>(a, kind, blocks, threads, smem, st);
-    return kahan ? launch_kind<3, true>(a, kind, blocks, threads, smem, st)
-                 : launch_kind<3, false>(a, kind, blocks, threads, smem, st);
-}
-
-int gather32_regs(int dim, int kind, bool kahan)
-{
-    cudaFuncAttributes fa;
-    cudaError_t e;
-    if (dim == 2) e = kahan ? cudaFuncGetAttributes(&fa, k_gather32<2, 1, true>)
-                            : cudaFuncGetAttributes(&fa, k_gather32<2, 1, false>);
-    else e = kahan ? cudaFuncGetAttributes(&fa, k_gather32<3, 1, true>)
-                   : cudaFuncGetAttributes(&fa, k_gather32<3, 1, false>);
-    (void)kind;
-    return e == cudaSuccess ? fa.numRegs : -1;
+    if (a.g.dim == 2) return kahan ? launch_np<2, true>(a, kind, blocks, threads, smem, st)
+                                   : launch_np<2, false>(a, kind, blocks, threads, smem, st);
+    return kahan ? launch_np<3, true>(a, kind, blocks, threads, smem, st)
+                 : launch_np<3, false>(a, kind, blocks, threads, smem, st);
 }

@@ -11,10 +11,17 @@ __global__ void k_scatter(const int* cell_of, const int* rank, const int* cell_s
 __global__ void k_cell_sort_pack(IkGeom g, const int* cell_start, int* sorted, const double* pos,
                                  const double* vel, const double* mass, const double* diam,
                                  IkPRec* prec, float4* kin, float* diam32, int want_pack);
-cudaError_t launch_bonds32(int dim, IkGeom g, IkPoly12 pot, float kappa, int n, const IkPRec* prec,
-                          const float* diam32, const int* cell_start, const int* sorted, const double* pos,
-                          float4* bonds, int maxb, int* nb, int* status, int* maxnb,
-                          unsigned long long* nbond_total, cudaStream_t st);
+// ---- tuned-path preparation (ik_bonds.cu) ---------------------------------
+cudaError_t launch_pack32(IkGeom g, int n, const int* sorted, const int* cell_of, const double* pos,
+                          const double* vel, const double* mass, const double* diam, IkPRec* prec, IkB64* pos64,
+                          float4* kin, float* diam32, cudaStream_t st);
+cudaError_t launch_bonds32w(int dim, IkGeom g, IkPoly12 pot, float kappa, int n, const IkPRec* prec,
+                            const float* diam32, const int* cell_start, const IkB64* pos64, float4* tmp, int maxb,
+                            int* nb, int* status, int* maxnb, unsigned long long* nbond_total, cudaStream_t st);
+cudaError_t launch_bond_compact(int n, int maxb, const int* nb, const int* boff, const float4* tmp, float4* bonds,
+                                cudaStream_t st);
+// exclusive scan of n ints into out[0..n]; bsum needs ceil(n / 4096) ints
+cudaError_t launch_scan(const int* in, int n, int* out, int* bsum, cudaStream_t st);
 __global__ void k_bonds64(IkGeom g, IkPoly12 pot, int n, const int* sorted, const int* cell_of,
                           const double* pos, const double* diam, const int* cell_start, IkB64* bonds,
                           int maxb, int* nb, int* status, int* maxnb);
@@ -35,18 +42,18 @@ struct GatherArgs32 {
     int reach[3];          // halo reach (cells) per axis; 0 on non-periodic axes
     float kappa, R2s, margin;
     double R2;             // FP64 R^2 for the boundary re-check
-    // Gauss-Legendre in symmetric form: xi_k > 0 (k < npairs) with weights w_k, centre w0
+    // Gauss-Legendre in symmetric form: nodes +-xi_k (k < npairs) with weights w_k,
+    // centre weight w0; xi2 = xi^2, m2xi = -2 xi
     int npairs;
-    float w0, xi[32], w[32];
-    // particle data (sorted order)
+    float w0, xi2[32], m2xi[32], w[32];
+    // particle data (cell order)
     const IkPRec* prec;
+    const IkB64* pos64;    // raw FP64 positions in cell order
     const int* cell_start;
-    const int* nb;
-    const float4* bonds;
+    const int* boff;       // CSR offsets of the bond records (n + 1)
+    const float4* bonds;   // {kappa r_ij / 2, 2 forceDivR / kappa^2}
     int maxb;
     const float4* kin;
-    const int* sorted;
-    const double* pos;
     // grid
     const float4* gpts;    // bin-ordered {ux,uy,uz, bits(grid index)}
     const double* grid;    // original FP64 grid (g x 3)
@@ -64,7 +71,6 @@ struct GatherArgs32 {
 };
 cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, int blocks, int threads,
                             size_t smem, cudaStream_t st);
-int gather32_regs(int dim, int kind, bool kahan);
 
 // ---- FP64 plain gather (ik_gather64.cu) ------------------------------------
 struct GatherArgs64 {

@@ -153,7 +153,7 @@ def test_gaussian_2d_vs_oracle(ik, oracle, seed):
     gv, gk, _ = run_gpu(ik, 2, f.L, f.pos, f.diam, grid, cg, "fp64", vel=f.vel, mass=f.mass)
     assert_fields(gv, ov, FP64_TOL, what="fp64 virial")
     assert_fields(gk, ok, FP64_TOL, what="fp64 kinetic")
-    for flags in (0, 2):  # Kahan-compensated and plain per-lane sums
+    for flags in (0, 2):  # plain and Kahan-compensated per-lane sums
         gv, gk, _ = run_gpu(ik, 2, f.L, f.pos, f.diam, grid, cg, "fp32", vel=f.vel, mass=f.mass, flags=flags)
         assert_fields(gv, ov, FP32_TOL, FP32_MAX_TOL, what=f"fp32 virial flags={flags}")
         assert_fields(gk, ok, FP32_TOL, FP32_MAX_TOL, what=f"fp32 kinetic flags={flags}")
