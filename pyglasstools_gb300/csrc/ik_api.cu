@@ -100,7 +100,7 @@ struct ik_ctx {
     DevBuf gpts_d, items_d;
     // work buffers
     DevBuf cell_of, rank, cell_count, cell_start, sorted, prec, kin, diam32;
-    DevBuf bonds32, nb32, bonds64, nb64, pos64, bonds_tmp, boff, bsum;
+    DevBuf bonds32, nb32, bonds64, nb64, pos64, bonds_tmp, boff, bsum, bsum_cells, relhi, rello, plo;
     DevBuf status, maxnb, work_counter;
     int maxb = 0, halo_cap = 0;
     // neighbour-query scratch
@@ -307,7 +307,7 @@ int ensure_ready(ik_ctx* c)
 
 // Cell list for a slot into (cell_of, rank, count, start, sorted) buffers.
 int build_cells(ik_ctx* c, Slot& s, const IkGeom& g, DevBuf& cell_of, DevBuf& rank, DevBuf& count,
-                DevBuf& start, DevBuf& sorted)
+                DevBuf& start, DevBuf& sorted, bool tuned = false)
 {
     int n = (int)s.n;
     ENS(cell_of, sizeof(int) * std::max(n, 1));
@@ -315,14 +315,21 @@ int build_cells(ik_ctx* c, Slot& s, const IkGeom& g, DevBuf& cell_of, DevBuf& ra
     ENS(count, sizeof(int) * (g.ncell + 1));
     ENS(start, sizeof(int) * (g.ncell + 1));
     ENS(sorted, sizeof(int) * std::max(n, 1));
+    ENS(c->bsum_cells, sizeof(int) * ((g.ncell + 4095) / 4096 + 1));
     CK(cudaMemsetAsync(count.p, 0, sizeof(int) * (g.ncell + 1), c->stream));
     if (n > 0) {
-        k_bin<<<(n + 255) / 256, 256, 0, c->stream>>>(s.pos.as<double>(), n, g, cell_of.as<int>(),
-                                                      rank.as<int>(), count.as<int>(), c->status.as<int>());
-        CK(cudaGetLastError());
+        if (tuned) {
+            ENS(c->relhi, sizeof(float4) * std::max(n, 1));
+            ENS(c->rello, sizeof(float4) * std::max(n, 1));
+            CK(launch_bin32(s.pos.as<double>(), n, g, cell_of.as<int>(), rank.as<int>(), count.as<int>(),
+                            c->relhi.as<float4>(), c->rello.as<float4>(), c->stream));
+        } else {
+            k_bin<<<(n + 255) / 256, 256, 0, c->stream>>>(s.pos.as<double>(), n, g, cell_of.as<int>(),
+                                                          rank.as<int>(), count.as<int>(), c->status.as<int>());
+            CK(cudaGetLastError());
+        }
     }
-    k_scan<<<1, 1024, 0, c->stream>>>(count.as<int>(), g.ncell, start.as<int>());
-    CK(cudaGetLastError());
+    CK(launch_scan(count.as<int>(), g.ncell, start.as<int>(), c->bsum_cells.as<int>(), c->stream));
     if (n > 0) {
         k_scatter<<<(n + 255) / 256, 256, 0, c->stream>>>(cell_of.as<int>(), rank.as<int>(), start.as<int>(), n,
                                                           sorted.as<int>());
@@ -351,9 +358,10 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
     CK(cudaMemsetAsync(s.counters.p, 0, sizeof(unsigned long long) * 4, c->stream));
     if (!(fields & IK_FIELD_KINETIC)) CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->G, c->stream));
     if (!(fields & IK_FIELD_VIRIAL)) CK(cudaMemsetAsync(s.vir.p, 0, sizeof(double) * NC * c->G, c->stream));
-    int r = build_cells(c, s, g, c->cell_of, c->rank, c->cell_count, c->cell_start, c->sorted);
+    int r = build_cells(c, s, g, c->cell_of, c->rank, c->cell_count, c->cell_start, c->sorted,
+                        prec == IK_PREC_FP32);
     if (r) return r;
-    c->launches += (n > 0 ? 3 : 1) + (g.ncell > 0 ? 1 : 0) + (n > 0 ? 1 : 0) + 1; // cells, sort, bonds|pack, gather
+    c->launches += (n > 0 ? 4 : 2) + (g.ncell > 0 ? 1 : 0) + (n > 0 ? 1 : 0) + 1; // cells, sort, bonds|pack, gather
     ENS(c->prec, sizeof(IkPRec) * std::max(n, 1));
     ENS(c->kin, sizeof(float4) * 2 * std::max(n, 1));
     ENS(c->diam32, sizeof(float) * std::max(n, 1));
@@ -366,10 +374,12 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
     unsigned long long* cnt = s.counters.as<unsigned long long>();
     if (prec == IK_PREC_FP32) {
         ENS(c->pos64, sizeof(IkB64) * std::max(n, 1));
-        CK(launch_pack32(g, n, c->sorted.as<int>(), c->cell_of.as<int>(), s.pos.as<double>(),
-                         s.has_vel ? s.vel.as<double>() : nullptr, s.has_mass ? s.mass.as<double>() : nullptr,
-                         s.diam.as<double>(), c->prec.as<IkPRec>(), c->pos64.as<IkB64>(), c->kin.as<float4>(),
-                         c->diam32.as<float>(), c->stream));
+        ENS(c->plo, sizeof(float4) * std::max(n, 1));
+        CK(launch_pack32(g, n, c->sorted.as<int>(), c->cell_of.as<int>(), c->relhi.as<float4>(),
+                         c->rello.as<float4>(), s.pos.as<double>(), s.has_vel ? s.vel.as<double>() : nullptr,
+                         s.has_mass ? s.mass.as<double>() : nullptr, s.diam.as<double>(), c->prec.as<IkPRec>(),
+                         c->plo.as<float4>(), c->pos64.as<IkB64>(), c->kin.as<float4>(), c->diam32.as<float>(),
+                         c->stream));
         if (timing) CK(cudaEventRecord(c->ev[1], c->stream));
         ENS(c->bonds_tmp, sizeof(float4) * (size_t)c->maxb * std::max(n, 1));
         ENS(c->bonds32, sizeof(float4) * (size_t)c->maxb * std::max(n, 1));
@@ -377,7 +387,8 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         ENS(c->boff, sizeof(int) * (std::max(n, 1) + 1));
         ENS(c->bsum, sizeof(int) * ((std::max(n, 1) + 4095) / 4096 + 1));
         CK(launch_bonds32w(D, g, c->pot, c->cg.kappa, n, c->prec.as<IkPRec>(), c->diam32.as<float>(),
-                           c->cell_start.as<int>(), c->pos64.as<IkB64>(), c->bonds_tmp.as<float4>(), c->maxb,
+                           c->cell_start.as<int>(), c->plo.as<float4>(), c->pos64.as<IkB64>(),
+                           c->bonds_tmp.as<float4>(), c->maxb,
                            c->nb32.as<int>(), c->status.as<int>(), c->maxnb.as<int>(), cnt, c->stream));
         CK(launch_scan(c->nb32.as<int>(), n, c->boff.as<int>(), c->bsum.as<int>(), c->stream));
         CK(launch_bond_compact(n, c->maxb, c->nb32.as<int>(), c->boff.as<int>(), c->bonds_tmp.as<float4>(),
@@ -856,6 +867,7 @@ int ik_get_neighbors(ik_ctx* c, int slot, double radius, int64_t* offs, int32_t*
         }
         g.nc[a] = nc;
         g.cw[a] = g.L[a] / nc;
+        g.invL[a] = 1.0 / g.L[a];
         g.reach_bond[a] = 1;
         g.all_bond[a] = nc < 3 ? 1 : 0;
     }

@@ -11,39 +11,58 @@
 #define FULL 0xffffffffu
 
 // ---------------------------------------------------------------------------
-// Pack the particles in cell order: FP32 position relative to the cell corner
-// (wrapped in FP64), the raw FP64 position, kinetic coefficients m v(x)v, FP32
-// diameter.  One thread per sorted particle.
+// Cell index of every particle (atomic rank inside the cell; the order is fixed by
+// the per-cell sort) and its position relative to the lower corner of its cell, as a
+// double-float pair (hi = FP32 rounding, lo = FP32 rounding of the remainder; hi + lo
+// carries ~48 bits).  One thread per particle, original order.
+__global__ void k_bin32(const double* __restrict__ pos, int n, IkGeom g, int* __restrict__ cell_of,
+                        int* __restrict__ rank, int* __restrict__ cell_count, float4* __restrict__ relhi,
+                        float4* __restrict__ rello)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double r[3] = {0.0, 0.0, 0.0};
+    int cc[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (a >= g.dim || g.nc[a] == 1) continue;
+        double t = (pos[3 * i + a] - g.lo[a]) * g.invL[a];
+        t -= floor(t);
+        int k = (int)(t * g.nc[a]);
+        k = k < 0 ? 0 : (k >= g.nc[a] ? g.nc[a] - 1 : k);
+        cc[a] = k;
+        r[a] = t * g.L[a] - k * g.cw[a];
+    }
+    int c = (cc[2] * g.nc[1] + cc[1]) * g.nc[0] + cc[0];
+    cell_of[i] = c;
+    rank[i] = atomicAdd(&cell_count[c], 1);
+    float hx = (float)r[0], hy = (float)r[1], hz = (float)r[2];
+    relhi[i] = make_float4(hx, hy, hz, 0.f);
+    rello[i] = make_float4((float)(r[0] - hx), (float)(r[1] - hy), (float)(r[2] - hz), 0.f);
+}
+
+// Pack the particles in cell order: the double-float cell-relative position, the raw
+// FP64 position, kinetic coefficients m v(x)v, FP32 diameter.  One thread per sorted
+// particle.
 __global__ void k_pack32(IkGeom g, int n, const int* __restrict__ sorted, const int* __restrict__ cell_of,
+                         const float4* __restrict__ relhi, const float4* __restrict__ rello,
                          const double* __restrict__ pos, const double* __restrict__ vel,
                          const double* __restrict__ mass, const double* __restrict__ diam,
-                         IkPRec* __restrict__ prec, IkB64* __restrict__ pos64, float4* __restrict__ kin,
-                         float* __restrict__ diam32)
+                         IkPRec* __restrict__ prec, float4* __restrict__ plo, IkB64* __restrict__ pos64,
+                         float4* __restrict__ kin, float* __restrict__ diam32)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     int i = sorted[p];
-    int c = cell_of[i];
-    int cx = c % g.nc[0], cy = (c / g.nc[0]) % g.nc[1], cz = c / (g.nc[0] * g.nc[1]);
-    double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
-    pos64[p] = make_ikb64(x, y, z, 0.0);
-    // the fractional box coordinate exactly as k_bin computed it (ik_cell_coord), so
-    // that the offset inside the cell is consistent with the cell index
-    double tx = (x - g.lo[0]) / g.L[0], ty = (y - g.lo[1]) / g.L[1];
-    tx -= floor(tx);
-    ty -= floor(ty);
+    float4 h = relhi[i];
     IkPRec r;
-    r.x = (float)(tx * g.L[0] - cx * g.cw[0]);
-    r.y = (float)(ty * g.L[1] - cy * g.cw[1]);
-    if (g.dim == 3) {
-        double tz = (z - g.lo[2]) / g.L[2];
-        tz -= floor(tz);
-        r.z = (float)(tz * g.L[2] - cz * g.cw[2]);
-    } else {
-        r.z = 0.0f;
-    }
-    r.cell = c;
+    r.x = h.x;
+    r.y = h.y;
+    r.z = h.z;
+    r.cell = cell_of[i];
     prec[p] = r;
+    plo[p] = rello[i];
+    pos64[p] = make_ikb64(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.0);
     double m = mass ? mass[i] : 1.0;
     double vx = vel ? vel[3 * i] : 0.0, vy = vel ? vel[3 * i + 1] : 0.0, vz = vel ? vel[3 * i + 2] : 0.0;
     if (g.dim == 2) {
@@ -55,13 +74,29 @@ __global__ void k_pack32(IkGeom g, int n, const int* __restrict__ sorted, const 
     diam32[p] = (float)diam[i];
 }
 
+// b = o + (pj - pi) for double-float operands (o = ohi + olo, p = hi + lo), rounded
+// once to FP32 at the end: TwoSum for the two leading additions, the small terms
+// added after.  Accurate to ~1 ulp of the FP32 result.
+__device__ __forceinline__ float ik_df_diff(float ohi, float olo, float hj, float lj, float hi_, float li)
+{
+    float s = hj - hi_;
+    float bb = s - hj;
+    float e = (hj - (s - bb)) + (-hi_ - bb);
+    float t = ohi + s;
+    float b2 = t - ohi;
+    float e2 = (ohi - (t - b2)) + (s - b2);
+    return t + ((e + e2) + (olo + (lj - li)));
+}
+
 // ---------------------------------------------------------------------------
 // Force-active bonds of one particle per warp.  The 3^d stencil cells are set up by
 // lanes 0..S-1; their candidates are walked 32 at a time (a lane finds its cell by
 // binary search over the stencil prefix sums).  Each candidate is screened in FP32
-// from the cell-relative positions; survivors are re-measured from the FP64
-// positions (minimum image in FP64), so that r_ij carries only its final FP32
-// rounding -- the r^-14 force amplifies position rounding for overlapping pairs.
+// from the cell-relative positions; survivors are re-measured from the double-float
+// positions, so that r_ij carries only its final FP32 rounding -- the r^-14 force
+// amplifies position rounding for strongly overlapping pairs.  (On axes with fewer
+// than three cells the stencil is not the minimum image; those pairs are re-measured
+// in FP64.)
 // Output record (16 B): {hb_x, hb_y, hb_z, f'} with hb = kappa * r_ij / 2 (scaled half
 // bond, r_ij = r_j - r_i) and f' = 2 forceDivR / kappa^2, so that
 // f' * hb (x) hb = 0.5 * forceDivR * r_ij (x) r_ij.  Written at a fixed stride of
@@ -72,6 +107,7 @@ __global__ void __launch_bounds__(256) k_bonds32w(IkGeom g, IkPoly12 pot, float 
                                                   const IkPRec* __restrict__ prec,
                                                   const float* __restrict__ diam32,
                                                   const int* __restrict__ cell_start,
+                                                  const float4* __restrict__ plo,
                                                   const IkB64* __restrict__ pos64, float4* __restrict__ tmp,
                                                   int maxb, int* __restrict__ nb, int* __restrict__ status,
                                                   int* __restrict__ maxnb,
@@ -93,7 +129,7 @@ __global__ void __launch_bounds__(256) k_bonds32w(IkGeom g, IkPoly12 pot, float 
     }
     const int S = len[0] * len[1] * len[2]; // <= 27
     int sstart = 0, scnt = 0;
-    float sox = 0.f, soy = 0.f, soz = 0.f;
+    float sox = 0.f, soy = 0.f, soz = 0.f, slx = 0.f, sly = 0.f, slz = 0.f;
     if (lane < S) {
         int ix = lane % len[0], iy = (lane / len[0]) % len[1], iz = lane / (len[0] * len[1]);
         int ux = lo[0] + ix, uy = lo[1] + iy, uz = lo[2] + iz;
@@ -101,9 +137,12 @@ __global__ void __launch_bounds__(256) k_bonds32w(IkGeom g, IkPoly12 pot, float 
         int cell = (wz * g.nc[1] + wy) * g.nc[0] + wx;
         sstart = cell_start[cell];
         scnt = cell_start[cell + 1] - sstart;
-        sox = (float)((ux - home[0]) * g.cw[0]);
-        soy = (float)((uy - home[1]) * g.cw[1]);
-        soz = DIM == 3 ? (float)((uz - home[2]) * g.cw[2]) : 0.f;
+        // cell offset as a double-float pair
+        const double dox = (ux - home[0]) * g.cw[0], doy = (uy - home[1]) * g.cw[1];
+        const double doz = DIM == 3 ? (uz - home[2]) * g.cw[2] : 0.0;
+        sox = (float)dox; slx = (float)(dox - sox);
+        soy = (float)doy; sly = (float)(doy - soy);
+        soz = (float)doz; slz = (float)(doz - soz);
     }
     int incl = scnt;
 #pragma unroll
@@ -123,6 +162,7 @@ __global__ void __launch_bounds__(256) k_bonds32w(IkGeom g, IkPoly12 pot, float 
     const float screen = 1.0f + 1e-4f;
     const float di = diam32[p];
     const IkB64 pi = pos64[p];
+    const float4 mlo = plo[p];
     const float hk = 0.5f * kappa, fk = 2.0f / (kappa * kappa);
     int cnt = 0;
     for (int base = 0; base < total; base += 32) {
@@ -137,6 +177,7 @@ __global__ void __launch_bounds__(256) k_bonds32w(IkGeom g, IkPoly12 pot, float 
         }
         const int qs = __shfl_sync(FULL, sstart, s), qe = __shfl_sync(FULL, excl, s);
         const float ox = __shfl_sync(FULL, sox, s), oy = __shfl_sync(FULL, soy, s), oz = __shfl_sync(FULL, soz, s);
+        const float olx = __shfl_sync(FULL, slx, s), oly = __shfl_sync(FULL, sly, s), olz = __shfl_sync(FULL, slz, s);
         bool act = false;
         float4 rec = make_float4(0.f, 0.f, 0.f, 0.f);
         if (v < total) {
@@ -152,16 +193,23 @@ __global__ void __launch_bounds__(256) k_bonds32w(IkGeom g, IkPoly12 pot, float 
                 const float sig = 0.5f * (di + dj) * (1.f - eps * fabsf(di - dj));
                 const float s2 = sig * sig;
                 if (r2 < mr2 * screen && r2 < rc2 * s2 * screen) {
-                    const IkB64 pj = pos64[q];
-                    double dx = pj.x - pi.x, dy = pj.y - pi.y;
-                    dx = fma(-g.L[0], rint(dx * g.invL[0]), dx);
-                    dy = fma(-g.L[1], rint(dy * g.invL[1]), dy);
-                    bx = (float)dx;
-                    by = (float)dy;
-                    if (DIM == 3) {
-                        double dz = pj.z - pi.z;
-                        dz = fma(-g.L[2], rint(dz * g.invL[2]), dz);
-                        bz = (float)dz;
+                    if (!(allx || ally || allz)) {
+                        const float4 lq = plo[q];
+                        bx = ik_df_diff(ox, olx, o.x, lq.x, me.x, mlo.x);
+                        by = ik_df_diff(oy, oly, o.y, lq.y, me.y, mlo.y);
+                        if (DIM == 3) bz = ik_df_diff(oz, olz, o.z, lq.z, me.z, mlo.z);
+                    } else {
+                        const IkB64 pj = pos64[q];
+                        double dx = pj.x - pi.x, dy = pj.y - pi.y;
+                        dx = fma(-g.L[0], rint(dx * g.invL[0]), dx);
+                        dy = fma(-g.L[1], rint(dy * g.invL[1]), dy);
+                        bx = (float)dx;
+                        by = (float)dy;
+                        if (DIM == 3) {
+                            double dz = pj.z - pi.z;
+                            dz = fma(-g.L[2], rint(dz * g.invL[2]), dz);
+                            bz = (float)dz;
+                        }
                     }
                     r2 = bx * bx + by * by + bz * bz;
                     if (r2 < mr2 && r2 < rc2 * s2) {
@@ -283,28 +331,39 @@ cudaError_t launch_scan(const int* in, int n, int* out, int* bsum, cudaStream_t 
     return cudaGetLastError();
 }
 
-cudaError_t launch_pack32(IkGeom g, int n, const int* sorted, const int* cell_of, const double* pos,
-                          const double* vel, const double* mass, const double* diam, IkPRec* prec, IkB64* pos64,
-                          float4* kin, float* diam32, cudaStream_t st)
+cudaError_t launch_bin32(const double* pos, int n, IkGeom g, int* cell_of, int* rank, int* cell_count, float4* relhi,
+                         float4* rello, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
-    k_pack32<<<(n + 255) / 256, 256, 0, st>>>(g, n, sorted, cell_of, pos, vel, mass, diam, prec, pos64, kin, diam32);
+    k_bin32<<<(n + 255) / 256, 256, 0, st>>>(pos, n, g, cell_of, rank, cell_count, relhi, rello);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack32(IkGeom g, int n, const int* sorted, const int* cell_of, const float4* relhi,
+                          const float4* rello, const double* pos, const double* vel, const double* mass,
+                          const double* diam, IkPRec* prec, float4* plo, IkB64* pos64, float4* kin, float* diam32,
+                          cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    k_pack32<<<(n + 255) / 256, 256, 0, st>>>(g, n, sorted, cell_of, relhi, rello, pos, vel, mass, diam, prec, plo,
+                                              pos64, kin, diam32);
     return cudaGetLastError();
 }
 
 cudaError_t launch_bonds32w(int dim, IkGeom g, IkPoly12 pot, float kappa, int n, const IkPRec* prec,
-                            const float* diam32, const int* cell_start, const IkB64* pos64, float4* tmp, int maxb,
-                            int* nb, int* status, int* maxnb, unsigned long long* nbond_total, cudaStream_t st)
+                            const float* diam32, const int* cell_start, const float4* plo, const IkB64* pos64,
+                            float4* tmp, int maxb, int* nb, int* status, int* maxnb,
+                            unsigned long long* nbond_total, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
     const int wpb = 8;
     int blocks = (n + wpb - 1) / wpb;
     if (dim == 2)
-        k_bonds32w<2><<<blocks, 32 * wpb, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, pos64, tmp, maxb, nb,
-                                                   status, maxnb, nbond_total);
+        k_bonds32w<2><<<blocks, 32 * wpb, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, plo, pos64, tmp, maxb,
+                                                   nb, status, maxnb, nbond_total);
     else
-        k_bonds32w<3><<<blocks, 32 * wpb, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, pos64, tmp, maxb, nb,
-                                                   status, maxnb, nbond_total);
+        k_bonds32w<3><<<blocks, 32 * wpb, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, plo, pos64, tmp, maxb,
+                                                   nb, status, maxnb, nbond_total);
     return cudaGetLastError();
 }
 

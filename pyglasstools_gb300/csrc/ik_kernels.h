@@ -12,12 +12,16 @@ __global__ void k_cell_sort_pack(IkGeom g, const int* cell_start, int* sorted, c
                                  const double* vel, const double* mass, const double* diam,
                                  IkPRec* prec, float4* kin, float* diam32, int want_pack);
 // ---- tuned-path preparation (ik_bonds.cu) ---------------------------------
-cudaError_t launch_pack32(IkGeom g, int n, const int* sorted, const int* cell_of, const double* pos,
-                          const double* vel, const double* mass, const double* diam, IkPRec* prec, IkB64* pos64,
-                          float4* kin, float* diam32, cudaStream_t st);
+cudaError_t launch_bin32(const double* pos, int n, IkGeom g, int* cell_of, int* rank, int* cell_count, float4* relhi,
+                         float4* rello, cudaStream_t st);
+cudaError_t launch_pack32(IkGeom g, int n, const int* sorted, const int* cell_of, const float4* relhi,
+                          const float4* rello, const double* pos, const double* vel, const double* mass,
+                          const double* diam, IkPRec* prec, float4* plo, IkB64* pos64, float4* kin, float* diam32,
+                          cudaStream_t st);
 cudaError_t launch_bonds32w(int dim, IkGeom g, IkPoly12 pot, float kappa, int n, const IkPRec* prec,
-                            const float* diam32, const int* cell_start, const IkB64* pos64, float4* tmp, int maxb,
-                            int* nb, int* status, int* maxnb, unsigned long long* nbond_total, cudaStream_t st);
+                            const float* diam32, const int* cell_start, const float4* plo, const IkB64* pos64,
+                            float4* tmp, int maxb, int* nb, int* status, int* maxnb,
+                            unsigned long long* nbond_total, cudaStream_t st);
 cudaError_t launch_bond_compact(int n, int maxb, const int* nb, const int* boff, const float4* tmp, float4* bonds,
                                 cudaStream_t st);
 // exclusive scan of n ints into out[0..n]; bsum needs ceil(n / 4096) ints
