@@ -260,6 +260,7 @@ def ours(args, wl, name):
     ev0.record(stream)
     for _ in range(args.steps):
         step()
+    ctx.wait_all()
     ev1.record(stream)
     ctx.synchronize()
     torch.cuda.synchronize()
@@ -312,6 +313,7 @@ def ours(args, wl, name):
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     step("fp64", nplain)
+    ctx.wait_all()
     e1.record(stream)
     ctx.synchronize()
     plain_value = nplain / (e0.elapsed_time(e1) * 1e-3)

@@ -95,8 +95,12 @@ int ik_set_frame(ik_ctx* ctx, int64_t n, const double* pos, const double* vel,
  * stream; results stay in HBM in the slot's field buffers.  fields: IK_FIELD_* mask.
  * Replaces IrvingKirkwood::compute (IrvingKirkwood.h:74-110). */
 int ik_compute_slot(ik_ctx* ctx, int slot, int precision, int fields);
-/* Wait for the stream; reports device-side status words. */
+/* Wait for all of the context's work; reports device-side status words.  (Slots are
+ * computed on several internal streams so that consecutive frames overlap.) */
 int ik_synchronize(ik_ctx* ctx);
+/* Make the context's main stream (ik_get_stream) wait, on the device, for all work
+ * enqueued so far; no host synchronisation.  For timing with events on that stream. */
+int ik_wait_all(ik_ctx* ctx);
 /* ik_compute_slot(0) + ik_synchronize. */
 int ik_compute(ik_ctx* ctx, int precision, int fields);
 

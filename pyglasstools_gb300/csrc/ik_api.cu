@@ -38,6 +38,15 @@ int fail(int code, const char* fmt, ...)
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+    DevBuf& operator=(DevBuf&& o) noexcept
+    {
+        if (this != &o) { if (p) cudaFree(p); p = o.p; bytes = o.bytes; o.p = nullptr; o.bytes = 0; }
+        return *this;
+    }
     ~DevBuf() { if (p) cudaFree(p); }
     int ensure(size_t need)
     {
@@ -65,7 +74,23 @@ struct Slot {
     DevBuf vir, kin;
     int last_prec = -1, last_fields = 0;
     DevBuf counters; // 4 x u64: bonds, pairs, triples, spare
+    cudaEvent_t done = nullptr; // completion of the slot's last computation (on its lane)
+    bool done_recorded = false;
+    Slot() = default;
+    Slot(Slot&&) = default;
+    Slot& operator=(Slot&&) = default;
 };
+
+// A lane: one stream and one set of per-frame work buffers.  Frames computed on
+// different lanes overlap on the GPU.
+struct Lane {
+    cudaStream_t st = nullptr;
+    cudaEvent_t last = nullptr;
+    DevBuf cell_of, rank, cell_count, cell_start, sorted, prec, kin, diam32;
+    DevBuf bonds32, nb32, bonds64, nb64, pos64, bonds_tmp, boff, bsum, bsum_cells, relhi, rello, plo;
+    DevBuf work_counter;
+};
+constexpr int IK_LANES = 4;
 
 struct PendingOp { int slot, prec, fields; };
 
@@ -98,10 +123,12 @@ struct ik_ctx {
     int bw[3] = {1, 1, 1}, reach[3] = {0, 0, 0};
     int nitems = 0;
     DevBuf gpts_d, items_d;
-    // work buffers
-    DevBuf cell_of, rank, cell_count, cell_start, sorted, prec, kin, diam32;
-    DevBuf bonds32, nb32, bonds64, nb64, pos64, bonds_tmp, boff, bsum, bsum_cells, relhi, rello, plo;
-    DevBuf status, maxnb, work_counter;
+    // per-frame work buffers live in the lanes
+    Lane lanes[IK_LANES];
+    int next_lane = 0;
+    cudaEvent_t fork = nullptr;
+    DevBuf status, maxnb;
+    DevBuf bsum_q; // scan scratch of the neighbour queries (main stream)
     int maxb = 0, halo_cap = 0;
     // neighbour-query scratch
     DevBuf q_cell_of, q_rank, q_count, q_start, q_sorted, q_cnt, q_offs, q_idx, q_flag;
@@ -306,8 +333,9 @@ int ensure_ready(ik_ctx* c)
 }
 
 // Cell list for a slot into (cell_of, rank, count, start, sorted) buffers.
-int build_cells(ik_ctx* c, Slot& s, const IkGeom& g, DevBuf& cell_of, DevBuf& rank, DevBuf& count,
-                DevBuf& start, DevBuf& sorted, bool tuned = false)
+int build_cells(ik_ctx* c, Slot& s, const IkGeom& g, cudaStream_t st, DevBuf& cell_of, DevBuf& rank,
+                DevBuf& count, DevBuf& start, DevBuf& sorted, DevBuf& bsum, DevBuf* relhi = nullptr,
+                DevBuf* rello = nullptr)
 {
     int n = (int)s.n;
     ENS(cell_of, sizeof(int) * std::max(n, 1));
@@ -315,24 +343,24 @@ int build_cells(ik_ctx* c, Slot& s, const IkGeom& g, DevBuf& cell_of, DevBuf& ra
     ENS(count, sizeof(int) * (g.ncell + 1));
     ENS(start, sizeof(int) * (g.ncell + 1));
     ENS(sorted, sizeof(int) * std::max(n, 1));
-    ENS(c->bsum_cells, sizeof(int) * ((g.ncell + 4095) / 4096 + 1));
-    CK(cudaMemsetAsync(count.p, 0, sizeof(int) * (g.ncell + 1), c->stream));
+    ENS(bsum, sizeof(int) * ((g.ncell + 4095) / 4096 + 1));
+    CK(cudaMemsetAsync(count.p, 0, sizeof(int) * (g.ncell + 1), st));
     if (n > 0) {
-        if (tuned) {
-            ENS(c->relhi, sizeof(float4) * std::max(n, 1));
-            ENS(c->rello, sizeof(float4) * std::max(n, 1));
+        if (relhi) {
+            ENS(*relhi, sizeof(float4) * std::max(n, 1));
+            ENS(*rello, sizeof(float4) * std::max(n, 1));
             CK(launch_bin32(s.pos.as<double>(), n, g, cell_of.as<int>(), rank.as<int>(), count.as<int>(),
-                            c->relhi.as<float4>(), c->rello.as<float4>(), c->stream));
+                            relhi->as<float4>(), rello->as<float4>(), st));
         } else {
-            k_bin<<<(n + 255) / 256, 256, 0, c->stream>>>(s.pos.as<double>(), n, g, cell_of.as<int>(),
-                                                          rank.as<int>(), count.as<int>(), c->status.as<int>());
+            k_bin<<<(n + 255) / 256, 256, 0, st>>>(s.pos.as<double>(), n, g, cell_of.as<int>(), rank.as<int>(),
+                                                   count.as<int>(), c->status.as<int>());
             CK(cudaGetLastError());
         }
     }
-    CK(launch_scan(count.as<int>(), g.ncell, start.as<int>(), c->bsum_cells.as<int>(), c->stream));
+    CK(launch_scan(count.as<int>(), g.ncell, start.as<int>(), bsum.as<int>(), st));
     if (n > 0) {
-        k_scatter<<<(n + 255) / 256, 256, 0, c->stream>>>(cell_of.as<int>(), rank.as<int>(), start.as<int>(), n,
-                                                          sorted.as<int>());
+        k_scatter<<<(n + 255) / 256, 256, 0, st>>>(cell_of.as<int>(), rank.as<int>(), start.as<int>(), n,
+                                                   sorted.as<int>());
         CK(cudaGetLastError());
     }
     return IK_OK;
@@ -347,54 +375,60 @@ int slot_ok(ik_ctx* c, int slot)
 int enqueue(ik_ctx* c, int slot, int prec, int fields)
 {
     Slot& s = c->slots[(size_t)slot];
+    Lane& L = c->lanes[c->next_lane];
+    c->next_lane = (c->next_lane + 1) % IK_LANES;
+    // fork from the main stream (uploads), and after the slot's previous computation
+    CK(cudaEventRecord(c->fork, c->stream));
+    CK(cudaStreamWaitEvent(L.st, c->fork, 0));
+    if (s.done_recorded) CK(cudaStreamWaitEvent(L.st, s.done, 0));
     const IkGeom& g = c->geom;
     const int D = c->dim, NC = D == 2 ? 3 : 6;
     const int n = (int)s.n;
     bool timing = (c->flags & IK_FLAG_TIMING) != 0;
-    if (timing) CK(cudaEventRecord(c->ev[0], c->stream));
+    if (timing) CK(cudaEventRecord(c->ev[0], L.st));
     ENS(s.vir, sizeof(double) * NC * c->G);
     ENS(s.kin, sizeof(double) * NC * c->G);
     ENS(s.counters, sizeof(unsigned long long) * 4);
-    CK(cudaMemsetAsync(s.counters.p, 0, sizeof(unsigned long long) * 4, c->stream));
-    if (!(fields & IK_FIELD_KINETIC)) CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->G, c->stream));
-    if (!(fields & IK_FIELD_VIRIAL)) CK(cudaMemsetAsync(s.vir.p, 0, sizeof(double) * NC * c->G, c->stream));
-    int r = build_cells(c, s, g, c->cell_of, c->rank, c->cell_count, c->cell_start, c->sorted,
-                        prec == IK_PREC_FP32);
+    CK(cudaMemsetAsync(s.counters.p, 0, sizeof(unsigned long long) * 4, L.st));
+    if (!(fields & IK_FIELD_KINETIC)) CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->G, L.st));
+    if (!(fields & IK_FIELD_VIRIAL)) CK(cudaMemsetAsync(s.vir.p, 0, sizeof(double) * NC * c->G, L.st));
+    int r = build_cells(c, s, g, L.st, L.cell_of, L.rank, L.cell_count, L.cell_start, L.sorted, L.bsum_cells,
+                        prec == IK_PREC_FP32 ? &L.relhi : nullptr, prec == IK_PREC_FP32 ? &L.rello : nullptr);
     if (r) return r;
     c->launches += (n > 0 ? 4 : 2) + (g.ncell > 0 ? 1 : 0) + (n > 0 ? 1 : 0) + 1; // cells, sort, bonds|pack, gather
-    ENS(c->prec, sizeof(IkPRec) * std::max(n, 1));
-    ENS(c->kin, sizeof(float4) * 2 * std::max(n, 1));
-    ENS(c->diam32, sizeof(float) * std::max(n, 1));
+    ENS(L.prec, sizeof(IkPRec) * std::max(n, 1));
+    ENS(L.kin, sizeof(float4) * 2 * std::max(n, 1));
+    ENS(L.diam32, sizeof(float) * std::max(n, 1));
     if (g.ncell > 0) { // sort ids inside each cell: deterministic order
-        k_cell_sort_pack<<<(g.ncell + 127) / 128, 128, 0, c->stream>>>(
-            g, c->cell_start.as<int>(), c->sorted.as<int>(), nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+        k_cell_sort_pack<<<(g.ncell + 127) / 128, 128, 0, L.st>>>(
+            g, L.cell_start.as<int>(), L.sorted.as<int>(), nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
             nullptr, 0);
         CK(cudaGetLastError());
     }
     unsigned long long* cnt = s.counters.as<unsigned long long>();
     if (prec == IK_PREC_FP32) {
-        ENS(c->pos64, sizeof(IkB64) * std::max(n, 1));
-        ENS(c->plo, sizeof(float4) * std::max(n, 1));
-        CK(launch_pack32(g, n, c->sorted.as<int>(), c->cell_of.as<int>(), c->relhi.as<float4>(),
-                         c->rello.as<float4>(), s.pos.as<double>(), s.has_vel ? s.vel.as<double>() : nullptr,
-                         s.has_mass ? s.mass.as<double>() : nullptr, s.diam.as<double>(), c->prec.as<IkPRec>(),
-                         c->plo.as<float4>(), c->pos64.as<IkB64>(), c->kin.as<float4>(), c->diam32.as<float>(),
-                         c->stream));
-        if (timing) CK(cudaEventRecord(c->ev[1], c->stream));
-        ENS(c->bonds_tmp, sizeof(float4) * (size_t)c->maxb * std::max(n, 1));
-        ENS(c->bonds32, sizeof(float4) * (size_t)c->maxb * std::max(n, 1));
-        ENS(c->nb32, sizeof(int) * (std::max(n, 1) + 1));
-        ENS(c->boff, sizeof(int) * (std::max(n, 1) + 1));
-        ENS(c->bsum, sizeof(int) * ((std::max(n, 1) + 4095) / 4096 + 1));
-        CK(launch_bonds32w(D, g, c->pot, c->cg.kappa, n, c->prec.as<IkPRec>(), c->diam32.as<float>(),
-                           c->cell_start.as<int>(), c->plo.as<float4>(), c->pos64.as<IkB64>(),
-                           c->bonds_tmp.as<float4>(), c->maxb,
-                           c->nb32.as<int>(), c->status.as<int>(), c->maxnb.as<int>(), cnt, c->stream));
-        CK(launch_scan(c->nb32.as<int>(), n, c->boff.as<int>(), c->bsum.as<int>(), c->stream));
-        CK(launch_bond_compact(n, c->maxb, c->nb32.as<int>(), c->boff.as<int>(), c->bonds_tmp.as<float4>(),
-                               c->bonds32.as<float4>(), c->stream));
+        ENS(L.pos64, sizeof(IkB64) * std::max(n, 1));
+        ENS(L.plo, sizeof(float4) * std::max(n, 1));
+        CK(launch_pack32(g, n, L.sorted.as<int>(), L.cell_of.as<int>(), L.relhi.as<float4>(),
+                         L.rello.as<float4>(), s.pos.as<double>(), s.has_vel ? s.vel.as<double>() : nullptr,
+                         s.has_mass ? s.mass.as<double>() : nullptr, s.diam.as<double>(), L.prec.as<IkPRec>(),
+                         L.plo.as<float4>(), L.pos64.as<IkB64>(), L.kin.as<float4>(), L.diam32.as<float>(),
+                         L.st));
+        if (timing) CK(cudaEventRecord(c->ev[1], L.st));
+        ENS(L.bonds_tmp, sizeof(float4) * (size_t)c->maxb * std::max(n, 1));
+        ENS(L.bonds32, sizeof(float4) * (size_t)c->maxb * std::max(n, 1));
+        ENS(L.nb32, sizeof(int) * (std::max(n, 1) + 1));
+        ENS(L.boff, sizeof(int) * (std::max(n, 1) + 1));
+        ENS(L.bsum, sizeof(int) * ((std::max(n, 1) + 4095) / 4096 + 1));
+        CK(launch_bonds32w(D, g, c->pot, c->cg.kappa, n, L.prec.as<IkPRec>(), L.diam32.as<float>(),
+                           L.cell_start.as<int>(), L.plo.as<float4>(), L.pos64.as<IkB64>(),
+                           L.bonds_tmp.as<float4>(), c->maxb,
+                           L.nb32.as<int>(), c->status.as<int>(), c->maxnb.as<int>(), L.st));
+        CK(launch_scan(L.nb32.as<int>(), n, L.boff.as<int>(), L.bsum.as<int>(), L.st));
+        CK(launch_bond_compact(n, c->maxb, L.nb32.as<int>(), L.boff.as<int>(), L.bonds_tmp.as<float4>(),
+                               L.bonds32.as<float4>(), cnt, L.st));
         c->launches += 5;
-        if (timing) CK(cudaEventRecord(c->ev[2], c->stream));
+        if (timing) CK(cudaEventRecord(c->ev[2], L.st));
         GatherArgs32 a{};
         a.g = g;
         for (int k = 0; k < 3; ++k) {
@@ -413,13 +447,13 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
             a.m2xi[k] = -2.0f * c->gl.t[k];
             a.w[k] = c->gl.wt[k];
         }
-        a.prec = c->prec.as<IkPRec>();
-        a.pos64 = c->pos64.as<IkB64>();
-        a.cell_start = c->cell_start.as<int>();
-        a.boff = c->boff.as<int>();
-        a.bonds = c->bonds32.as<float4>();
+        a.prec = L.prec.as<IkPRec>();
+        a.pos64 = L.pos64.as<IkB64>();
+        a.cell_start = L.cell_start.as<int>();
+        a.boff = L.boff.as<int>();
+        a.bonds = L.bonds32.as<float4>();
         a.maxb = c->maxb;
-        a.kin = c->kin.as<float4>();
+        a.kin = L.kin.as<float4>();
         a.gpts = c->gpts_d.as<float4>();
         a.grid = c->grid_d.as<double>();
         a.items = c->items_d.as<int4>();
@@ -433,29 +467,29 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         a.out_kin = s.kin.as<double>();
         a.fields = fields & (s.has_vel ? 3 : 1);
         if ((fields & IK_FIELD_KINETIC) && !s.has_vel)
-            CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->G, c->stream));
-        a.work_counter = c->work_counter.as<int>();
+            CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->G, L.st));
+        a.work_counter = L.work_counter.as<int>();
         a.status = c->status.as<int>();
         a.cnt_pairs = cnt + 1;
         a.cnt_triples = cnt + 2;
-        CK(cudaMemsetAsync(c->work_counter.p, 0, sizeof(int), c->stream));
+        CK(cudaMemsetAsync(L.work_counter.p, 0, sizeof(int), L.st));
         size_t smem = (size_t)IK_WARPS_GATHER * ((size_t)c->halo_cap * 16 + (size_t)a.qcap * 4);
         int blocks = std::min(c->nitems, c->sm_count * 2);
         if (blocks > 0)
             CK(launch_gather32(a, c->cg.kind, (c->flags & IK_FLAG_LANE_KAHAN) != 0, blocks, 32 * IK_WARPS_GATHER,
-                               smem, c->stream));
+                               smem, L.st));
     } else {
-        if (timing) CK(cudaEventRecord(c->ev[1], c->stream));
-        ENS(c->bonds64, sizeof(IkB64) * (size_t)c->maxb * std::max(n, 1));
-        ENS(c->nb64, sizeof(int) * std::max(n, 1));
+        if (timing) CK(cudaEventRecord(c->ev[1], L.st));
+        ENS(L.bonds64, sizeof(IkB64) * (size_t)c->maxb * std::max(n, 1));
+        ENS(L.nb64, sizeof(int) * std::max(n, 1));
         if (n > 0) {
-            k_bonds64<<<(n + 127) / 128, 128, 0, c->stream>>>(
-                g, c->pot, n, c->sorted.as<int>(), c->cell_of.as<int>(), s.pos.as<double>(), s.diam.as<double>(),
-                c->cell_start.as<int>(), c->bonds64.as<IkB64>(), c->maxb, c->nb64.as<int>(), c->status.as<int>(),
+            k_bonds64<<<(n + 127) / 128, 128, 0, L.st>>>(
+                g, c->pot, n, L.sorted.as<int>(), L.cell_of.as<int>(), s.pos.as<double>(), s.diam.as<double>(),
+                L.cell_start.as<int>(), L.bonds64.as<IkB64>(), c->maxb, L.nb64.as<int>(), c->status.as<int>(),
                 c->maxnb.as<int>());
             CK(cudaGetLastError());
         }
-        if (timing) CK(cudaEventRecord(c->ev[2], c->stream));
+        if (timing) CK(cudaEventRecord(c->ev[2], L.st));
         GatherArgs64 a{};
         a.g = g;
         a.cg = c->cg;
@@ -465,13 +499,13 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         }
         a.nq = c->gl.n;
         for (int k = 0; k < c->gl.n; ++k) { a.xs[k] = 0.5 + 0.5 * c->gl.x[k]; a.ws[k] = c->gl.w[k]; }
-        a.sorted = c->sorted.as<int>();
-        a.cell_start = c->cell_start.as<int>();
+        a.sorted = L.sorted.as<int>();
+        a.cell_start = L.cell_start.as<int>();
         a.pos = s.pos.as<double>();
         a.vel = s.has_vel ? s.vel.as<double>() : nullptr;
         a.mass = s.has_mass ? s.mass.as<double>() : nullptr;
-        a.nb = c->nb64.as<int>();
-        a.bonds = c->bonds64.as<IkB64>();
+        a.nb = L.nb64.as<int>();
+        a.bonds = L.bonds64.as<IkB64>();
         a.maxb = c->maxb;
         a.grid = c->grid_d.as<double>();
         a.ngrid = c->G;
@@ -479,12 +513,16 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         a.out_kin = s.kin.as<double>();
         a.fields = fields;
         if ((fields & IK_FIELD_KINETIC) && !s.has_vel)
-            CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->G, c->stream));
-        CK(launch_gather64(a, c->stream));
+            CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->G, L.st));
+        CK(launch_gather64(a, L.st));
     }
-    if (timing) CK(cudaEventRecord(c->ev[3], c->stream));
+    if (timing) CK(cudaEventRecord(c->ev[3], L.st));
     s.last_prec = prec;
     s.last_fields = fields;
+    if (!s.done) CK(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
+    CK(cudaEventRecord(s.done, L.st));
+    s.done_recorded = true;
+    CK(cudaEventRecord(L.last, L.st));
     return IK_OK;
 }
 
@@ -519,13 +557,26 @@ int ik_create(ik_ctx** out, int device)
         return fail(IK_ERR_CUDA, "cudaStreamCreate failed");
     }
     for (auto& ev : c->ev) cudaEventCreate(&ev);
+    cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
+    for (Lane& L : c->lanes) {
+        if (cudaStreamCreateWithFlags(&L.st, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&L.last, cudaEventDisableTiming) != cudaSuccess) {
+            ik_destroy(c);
+            return fail(IK_ERR_CUDA, "stream/event creation failed");
+        }
+        cudaEventRecord(L.last, L.st);
+    }
     c->slots.resize(1);
     int r;
-    if ((r = c->status.ensure(sizeof(int))) || (r = c->maxnb.ensure(sizeof(int))) ||
-        (r = c->work_counter.ensure(sizeof(int)))) {
+    if ((r = c->status.ensure(sizeof(int))) || (r = c->maxnb.ensure(sizeof(int)))) {
         ik_destroy(c);
         return r;
     }
+    for (Lane& L : c->lanes)
+        if ((r = L.work_counter.ensure(sizeof(int)))) {
+            ik_destroy(c);
+            return r;
+        }
     cudaMemset(c->status.p, 0, sizeof(int));
     cudaMemset(c->maxnb.p, 0, sizeof(int));
     *out = c;
@@ -536,8 +587,15 @@ int ik_destroy(ik_ctx* c)
 {
     if (!c) return IK_OK;
     cudaSetDevice(c->device);
+    for (Lane& L : c->lanes) if (L.st) cudaStreamSynchronize(L.st);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (auto& ev : c->ev) if (ev) cudaEventDestroy(ev);
+    if (c->fork) cudaEventDestroy(c->fork);
+    for (Slot& s : c->slots) if (s.done) cudaEventDestroy(s.done);
+    for (Lane& L : c->lanes) {
+        if (L.last) cudaEventDestroy(L.last);
+        if (L.st) cudaStreamDestroy(L.st);
+    }
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return IK_OK;
@@ -692,21 +750,8 @@ int ik_reserve_slots(ik_ctx* c, int nslots)
 {
     if (int r = check_ctx(c)) return r;
     if (nslots < 1 || nslots > 65536) return fail(IK_ERR_ARG, "nslots out of range");
-    CK(cudaStreamSynchronize(c->stream));
-    if ((int)c->slots.size() < nslots) {
-        std::vector<Slot> ns(nslots);
-        // move existing DevBufs
-        for (size_t k = 0; k < c->slots.size(); ++k) {
-            std::swap(ns[k].pos, c->slots[k].pos); std::swap(ns[k].vel, c->slots[k].vel);
-            std::swap(ns[k].mass, c->slots[k].mass); std::swap(ns[k].diam, c->slots[k].diam);
-            std::swap(ns[k].vir, c->slots[k].vir); std::swap(ns[k].kin, c->slots[k].kin);
-            std::swap(ns[k].counters, c->slots[k].counters);
-            ns[k].n = c->slots[k].n; ns[k].has_vel = c->slots[k].has_vel; ns[k].has_mass = c->slots[k].has_mass;
-            ns[k].dmax = c->slots[k].dmax; ns[k].last_prec = c->slots[k].last_prec;
-            ns[k].last_fields = c->slots[k].last_fields;
-        }
-        c->slots.swap(ns);
-    }
+    if (int r = ik_synchronize(c)) return r;
+    if ((int)c->slots.size() < nslots) c->slots.resize((size_t)nslots);
     return IK_OK;
 }
 
@@ -722,6 +767,7 @@ int ik_upload_frame(ik_ctx* c, int slot, int64_t n, const double* pos, const dou
     if (!c->max_rcut_set) // Calculator.h:41-45 freezes max_rcut from the first frame
         for (int64_t i = 0; i < n; ++i) dmax = std::max(dmax, diam[i]);
     Slot& s = c->slots[(size_t)slot];
+    if (s.done_recorded) CK(cudaStreamWaitEvent(c->stream, s.done, 0)); // inputs still in use
     ENS(s.pos, sizeof(double) * 3 * std::max<int64_t>(n, 1));
     ENS(s.diam, sizeof(double) * std::max<int64_t>(n, 1));
     if (n > 0) {
@@ -779,6 +825,7 @@ int ik_synchronize(ik_ctx* c)
 {
     if (int r = check_ctx(c)) return r;
     for (int attempt = 0; attempt < 4; ++attempt) {
+        for (Lane& L : c->lanes) CK(cudaStreamSynchronize(L.st));
         CK(cudaStreamSynchronize(c->stream));
         int st = 0, mx = 0;
         CK(cudaMemcpy(&st, c->status.p, sizeof(int), cudaMemcpyDeviceToHost));
@@ -872,7 +919,10 @@ int ik_get_neighbors(ik_ctx* c, int slot, double radius, int64_t* offs, int32_t*
         g.all_bond[a] = nc < 3 ? 1 : 0;
     }
     g.ncell = g.nc[0] * g.nc[1] * g.nc[2];
-    if (int r = build_cells(c, s, g, c->q_cell_of, c->q_rank, c->q_count, c->q_start, c->q_sorted)) return r;
+    if (s.done_recorded) CK(cudaStreamWaitEvent(c->stream, s.done, 0));
+    if (int r = build_cells(c, s, g, c->stream, c->q_cell_of, c->q_rank, c->q_count, c->q_start, c->q_sorted,
+                            c->bsum_q))
+        return r;
     if (g.ncell > 0)
         k_cell_sort_pack<<<(g.ncell + 127) / 128, 128, 0, c->stream>>>(g, c->q_start.as<int>(), c->q_sorted.as<int>(),
                                                                        nullptr, nullptr, nullptr, nullptr, nullptr,
@@ -994,11 +1044,21 @@ int ik_get_timing(ik_ctx* c, float* ms4)
     if (int r = check_ctx(c)) return r;
     if (!ms4) return fail(IK_ERR_ARG, "null output");
     if (!(c->flags & IK_FLAG_TIMING)) return fail(IK_ERR_STATE, "timing flag not set");
-    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaEventSynchronize(c->ev[3]));
     CK(cudaEventElapsedTime(&ms4[0], c->ev[0], c->ev[1]));
     CK(cudaEventElapsedTime(&ms4[1], c->ev[1], c->ev[2]));
     CK(cudaEventElapsedTime(&ms4[2], c->ev[2], c->ev[3]));
     CK(cudaEventElapsedTime(&ms4[3], c->ev[0], c->ev[3]));
+    return IK_OK;
+}
+
+int ik_wait_all(ik_ctx* c)
+{
+    if (int r = check_ctx(c)) return r;
+    for (Lane& L : c->lanes) {
+        CK(cudaEventRecord(L.last, L.st));
+        CK(cudaStreamWaitEvent(c->stream, L.last, 0));
+    }
     return IK_OK;
 }
 
@@ -1028,6 +1088,7 @@ int ik_download_field_async(ik_ctx* c, int slot, int field, double* host_out, in
     Slot& s = c->slots[(size_t)slot];
     const DevBuf& src = field == IK_FIELD_VIRIAL ? s.vir : s.kin;
     if (!src.p) return fail(IK_ERR_STATE, "slot %d has not been computed", slot);
+    if (s.done_recorded) CK(cudaStreamWaitEvent(c->stream, s.done, 0));
     if (c->G > 0) CK(cudaMemcpyAsync(host_out, src.p, sizeof(double) * NC * c->G, cudaMemcpyDeviceToHost, c->stream));
     return IK_OK;
 }

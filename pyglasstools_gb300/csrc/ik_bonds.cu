@@ -110,8 +110,7 @@ __global__ void __launch_bounds__(256) k_bonds32w(IkGeom g, IkPoly12 pot, float 
                                                   const float4* __restrict__ plo,
                                                   const IkB64* __restrict__ pos64, float4* __restrict__ tmp,
                                                   int maxb, int* __restrict__ nb, int* __restrict__ status,
-                                                  int* __restrict__ maxnb,
-                                                  unsigned long long* __restrict__ nbond_total)
+                                                  int* __restrict__ maxnb)
 {
     const int lane = threadIdx.x & 31;
     const int p = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
@@ -229,17 +228,21 @@ __global__ void __launch_bounds__(256) k_bonds32w(IkGeom g, IkPoly12 pot, float 
     }
     if (lane == 0) {
         nb[p] = cnt < maxb ? cnt : maxb;
-        if (cnt > maxb) atomicOr(status, IK_ST_BOND_OVERFLOW);
-        atomicMax(maxnb, cnt);
-        atomicAdd(nbond_total, (unsigned long long)cnt);
+        if (cnt > maxb) { // rare: grow the capacity and recompute (host side)
+            atomicOr(status, IK_ST_BOND_OVERFLOW);
+            atomicMax(maxnb, cnt);
+        }
     }
 }
 
-// Compact the fixed-stride records into CSR order (boff = exclusive scan of nb).
+// Compact the fixed-stride records into CSR order (boff = exclusive scan of nb); the
+// first thread also stores the number of bonds, boff[n], in the frame's counters.
 __global__ void k_bond_compact(int n, int maxb, const int* __restrict__ nb, const int* __restrict__ boff,
-                               const float4* __restrict__ tmp, float4* __restrict__ bonds)
+                               const float4* __restrict__ tmp, float4* __restrict__ bonds,
+                               unsigned long long* __restrict__ nbond_total)
 {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0) *nbond_total = (unsigned long long)boff[n];
     int p = t / maxb, k = t - p * maxb;
     if (p >= n) return;
     if (k < nb[p]) bonds[boff[p] + k] = tmp[(size_t)p * maxb + k];
@@ -352,26 +355,25 @@ cudaError_t launch_pack32(IkGeom g, int n, const int* sorted, const int* cell_of
 
 cudaError_t launch_bonds32w(int dim, IkGeom g, IkPoly12 pot, float kappa, int n, const IkPRec* prec,
                             const float* diam32, const int* cell_start, const float4* plo, const IkB64* pos64,
-                            float4* tmp, int maxb, int* nb, int* status, int* maxnb,
-                            unsigned long long* nbond_total, cudaStream_t st)
+                            float4* tmp, int maxb, int* nb, int* status, int* maxnb, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
     const int wpb = 8;
     int blocks = (n + wpb - 1) / wpb;
     if (dim == 2)
         k_bonds32w<2><<<blocks, 32 * wpb, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, plo, pos64, tmp, maxb,
-                                                   nb, status, maxnb, nbond_total);
+                                                   nb, status, maxnb);
     else
         k_bonds32w<3><<<blocks, 32 * wpb, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, plo, pos64, tmp, maxb,
-                                                   nb, status, maxnb, nbond_total);
+                                                   nb, status, maxnb);
     return cudaGetLastError();
 }
 
 cudaError_t launch_bond_compact(int n, int maxb, const int* nb, const int* boff, const float4* tmp, float4* bonds,
-                                cudaStream_t st)
+                                unsigned long long* nbond_total, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
     long long t = (long long)n * maxb;
-    k_bond_compact<<<(int)((t + 255) / 256), 256, 0, st>>>(n, maxb, nb, boff, tmp, bonds);
+    k_bond_compact<<<(int)((t + 255) / 256), 256, 0, st>>>(n, maxb, nb, boff, tmp, bonds, nbond_total);
     return cudaGetLastError();
 }

@@ -183,8 +183,10 @@ __global__ void k_bonds64(IkGeom g, IkPoly12 pot, int n, const int* __restrict__
         }
     }
     nb[p] = cnt < maxb ? cnt : maxb;
-    if (cnt > maxb) atomicOr(status, IK_ST_BOND_OVERFLOW);
-    atomicMax(maxnb, cnt);
+    if (cnt > maxb) { // rare: grow the capacity and recompute (host side)
+        atomicOr(status, IK_ST_BOND_OVERFLOW);
+        atomicMax(maxnb, cnt);
+    }
 }
 
 // ---------------------------------------------------------------------------

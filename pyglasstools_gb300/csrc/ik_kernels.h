@@ -20,10 +20,9 @@ cudaError_t launch_pack32(IkGeom g, int n, const int* sorted, const int* cell_of
                           cudaStream_t st);
 cudaError_t launch_bonds32w(int dim, IkGeom g, IkPoly12 pot, float kappa, int n, const IkPRec* prec,
                             const float* diam32, const int* cell_start, const float4* plo, const IkB64* pos64,
-                            float4* tmp, int maxb, int* nb, int* status, int* maxnb,
-                            unsigned long long* nbond_total, cudaStream_t st);
+                            float4* tmp, int maxb, int* nb, int* status, int* maxnb, cudaStream_t st);
 cudaError_t launch_bond_compact(int n, int maxb, const int* nb, const int* boff, const float4* tmp, float4* bonds,
-                                cudaStream_t st);
+                                unsigned long long* nbond_total, cudaStream_t st);
 // exclusive scan of n ints into out[0..n]; bsum needs ceil(n / 4096) ints
 cudaError_t launch_scan(const int* in, int n, int* out, int* bsum, cudaStream_t st);
 __global__ void k_bonds64(IkGeom g, IkPoly12 pot, int n, const int* sorted, const int* cell_of,

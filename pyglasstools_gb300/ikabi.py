@@ -71,6 +71,7 @@ def lib():
             "ik_download_field_async": ([vp, i32, i32, dp, i64], i32),
             "ik_measure_fp32_peak": ([i32, dp], i32),
             "ik_get_launch_count": ([vp, C.POINTER(C.c_int64)], i32),
+            "ik_wait_all": ([vp], i32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -173,6 +174,10 @@ class IKContext:
 
     def synchronize(self):
         check(lib().ik_synchronize(self._h))
+
+    def wait_all(self):
+        """Main stream waits (on the device) for all enqueued work."""
+        check(lib().ik_wait_all(self._h))
 
     def compute(self, precision="fp32", fields=FIELD_VIRIAL | FIELD_KINETIC):
         check(lib().ik_compute(self._h, PREC[precision], fields))
