@@ -332,13 +332,16 @@ def ours(args, wl, name):
 
     # ---- roofline of the gather kernel (per-launch CUDA events around it)
     ctx.set_flags(ikabi.FLAG_TIMING)
-    gms, trip = [], []
+    gms, trip, stages = [], [], []
     for k in range(F):
         ctx.compute_slot(k, "fp32")
         ctx.synchronize()
-        gms.append(ctx.timing()[2])
+        t4 = ctx.timing()
+        stages.append(t4)
+        gms.append(t4[2])
         trip.append(ctx.counters(k)[2])
     ctx.set_flags(0)
+    stage_ms = np.mean(np.array(stages), axis=0)
     g_ms = float(np.mean(gms))
     A = float(np.mean(trip))
     flop = FLOP_PER_TRIPLE[D] * A
@@ -363,6 +366,9 @@ def ours(args, wl, name):
                         "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                         "flop_per_launch": flop, "active_triples_per_launch": A, "launch_ms": g_ms,
                         "peak_source": "measured live: FFMA throughput probe (ik_measure_fp32_peak)"},
+           "stage_ms_per_frame": {"cells": float(stage_ms[0]), "bonds": float(stage_ms[1]),
+                                  "gather": float(stage_ms[2]), "total": float(stage_ms[3]),
+                                  "note": "one frame at a time (no overlap), CUDA events"},
            "plain_fp64": {"value": plain_value, "unit": "frames/s", "frames_timed": nplain},
            "tuned_over_plain": value / plain_value,
            "rel_err_vs_fp64": {"virial": err_v, "kinetic": err_k},
