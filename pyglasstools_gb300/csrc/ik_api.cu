@@ -89,6 +89,7 @@ struct Lane {
     DevBuf cell_of, rank, cell_count, cell_start, sorted, prec, kin, diam32;
     DevBuf bonds32, nb32, bonds64, nb64, pos64, bonds_tmp, boff, bsum, bsum_cells, relhi, rello, plo;
     DevBuf work_counter;
+    DevBuf vir2, kin2; // double-float outputs of the FP32 gather
 };
 constexpr int IK_LANES = 4;
 
@@ -211,6 +212,10 @@ int ensure_geometry(ik_ctx* c)
         g.all_bond[a] = (nc < 3) ? 1 : 0;
     }
     if (c->dim == 2) { g.lo[2] = -0.5 * c->boxsize[2] - c->origin[2]; g.cw[2] = g.L[2]; }
+    for (int a = 0; a < 3; ++a) {
+        g.cwhi[a] = (float)g.cw[a];
+        g.cwlo[a] = (float)(g.cw[a] - (double)g.cwhi[a]);
+    }
     long long ncell = (long long)g.nc[0] * g.nc[1] * g.nc[2];
     if (ncell > (1LL << 30)) return fail(IK_ERR_UNSUPPORTED, "too many cells (%lld)", ncell);
     g.ncell = (int)ncell;
@@ -461,10 +466,10 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         a.halo_cap = c->halo_cap;
         a.qcap = 32 * (c->maxb + 1);
         double norm = c->cg.kind == IK_CG_MOLLIFIER ? c->cg.mollifier_norm : c->cg.norm;
-        a.vir_scale = 0.5 * norm;
-        a.kin_scale = norm;
-        a.out_vir = s.vir.as<double>();
-        a.out_kin = s.kin.as<double>();
+        ENS(L.vir2, sizeof(float2) * NC * (size_t)c->G);
+        ENS(L.kin2, sizeof(float2) * NC * (size_t)c->G);
+        a.out_vir = L.vir2.as<float2>();
+        a.out_kin = L.kin2.as<float2>();
         a.fields = fields & (s.has_vel ? 3 : 1);
         if ((fields & IK_FIELD_KINETIC) && !s.has_vel)
             CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->G, L.st));
@@ -478,6 +483,12 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         if (blocks > 0)
             CK(launch_gather32(a, c->cg.kind, (c->flags & IK_FLAG_LANE_KAHAN) != 0, blocks, 32 * IK_WARPS_GATHER,
                                smem, L.st));
+        // FP64 finish: ((double)hi + (double)lo) * normalisation (0.5 of the GL map for the virial)
+        if (a.fields & 1) CK(launch_pairs_to_f64(L.vir2.as<float2>(), s.vir.as<double>(), (long long)NC * c->G,
+                                                 0.5 * norm, L.st));
+        if (a.fields & 2) CK(launch_pairs_to_f64(L.kin2.as<float2>(), s.kin.as<double>(), (long long)NC * c->G,
+                                                 norm, L.st));
+        c->launches += 2;
     } else {
         if (timing) CK(cudaEventRecord(c->ev[1], L.st));
         ENS(L.bonds64, sizeof(IkB64) * (size_t)c->maxb * std::max(n, 1));

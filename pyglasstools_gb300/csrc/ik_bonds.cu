@@ -136,12 +136,12 @@ __global__ void __launch_bounds__(256) k_bonds32w(IkGeom g, IkPoly12 pot, float 
         int cell = (wz * g.nc[1] + wy) * g.nc[0] + wx;
         sstart = cell_start[cell];
         scnt = cell_start[cell + 1] - sstart;
-        // cell offset as a double-float pair
-        const double dox = (ux - home[0]) * g.cw[0], doy = (uy - home[1]) * g.cw[1];
-        const double doz = DIM == 3 ? (uz - home[2]) * g.cw[2] : 0.0;
-        sox = (float)dox; slx = (float)(dox - sox);
-        soy = (float)doy; sly = (float)(doy - soy);
-        soz = (float)doz; slz = (float)(doz - soz);
+        // cell offset as a double-float pair; the offset is -1, 0 or +1 cell widths
+        // (or 0..nc-1 on an axis scanned whole, handled by the FP64 branch below)
+        const float kx = (float)(ux - home[0]), ky = (float)(uy - home[1]), kz = (float)(uz - home[2]);
+        sox = kx * g.cwhi[0]; slx = kx * g.cwlo[0];
+        soy = ky * g.cwhi[1]; sly = ky * g.cwlo[1];
+        soz = DIM == 3 ? kz * g.cwhi[2] : 0.f; slz = DIM == 3 ? kz * g.cwlo[2] : 0.f;
     }
     int incl = scnt;
 #pragma unroll

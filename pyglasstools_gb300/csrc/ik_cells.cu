@@ -298,9 +298,14 @@ cudaError_t launch_fma_probe(int blocks, int threads, int iters, float* out)
 __global__ void k_validate(const double* __restrict__ pos, const double* __restrict__ diam, int n, int dim,
                            int* __restrict__ status)
 {
+    // integer tests on the IEEE-754 bits (no FP64 instructions): finite = exponent
+    // field not all ones; d > 0 = sign clear and not +0; z == 0 = all bits but the sign clear
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2], d = diam[i];
-    bool ok = isfinite(x) && isfinite(y) && isfinite(z) && isfinite(d) && d > 0.0 && (dim == 3 || z == 0.0);
+    const long long* p = reinterpret_cast<const long long*>(pos) + 3 * (size_t)i;
+    long long x = p[0], y = p[1], z = p[2], d = reinterpret_cast<const long long*>(diam)[i];
+    const long long EXP = 0x7ff0000000000000LL, ABS = 0x7fffffffffffffffLL;
+    bool ok = (x & EXP) != EXP && (y & EXP) != EXP && (z & EXP) != EXP && (d & EXP) != EXP && d > 0 &&
+              (dim == 3 || (z & ABS) == 0);
     if (!ok) atomicOr(status, IK_ST_BAD_INPUT);
 }

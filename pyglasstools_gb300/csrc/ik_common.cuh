@@ -23,6 +23,7 @@ struct IkGeom {
     int all_bond[3];     // 1: stencil covers the whole axis once
     double L[3], lo[3], cw[3];
     double invL[3];      // 1 / L (used for minimum-image rounding only)
+    float cwhi[3], cwlo[3]; // cell width as a double-float pair (FP32 hi + lo)
     int periodic[3];
 };
 

@@ -385,39 +385,48 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                 if (lane < qn) process_slot(queue[lane]);
                 __syncwarp();
 
-                // ---- combine lanes (compensated) and write the group's results (FP64):
-                //      virial first, then kinetic, each a transposing butterfly of VH values
+                // ---- combine lanes (compensated): virial, then kinetic, each a
+                //      transposing butterfly of VH values; results are written as
+                //      unscaled double-float pairs (hi, lo), converted to FP64 later
                 constexpr int VH = ik_pow2_ceil(P * NC);
-                constexpr int PER = VH >= 32 ? VH / 32 : 1;
+                static_assert(VH == 16 || VH == 32, "butterfly width");
+                float vh[VH], vl[VH], kh[VH], kl[VH];
 #pragma unroll
-                for (int kinf = 0; kinf < 2; ++kinf) {
-                    if (kinf ? !want_kin : !(a.fields & 1)) continue; // warp-uniform
-                    float hi[VH], lo[VH];
+                for (int p = 0; p < P; ++p)
 #pragma unroll
-                    for (int p = 0; p < P; ++p)
+                    for (int c = 0; c < NC; ++c) {
+                        vh[p * NC + c] = acc[p][c];
+                        vl[p * NC + c] = KAHAN ? -cmp[p][c] : 0.f;
+                        kh[p * NC + c] = kac[p][c];
+                        kl[p * NC + c] = 0.f;
+                    }
 #pragma unroll
-                        for (int c = 0; c < NC; ++c) {
-                            hi[p * NC + c] = kinf ? kac[p][c] : acc[p][c];
-                            lo[p * NC + c] = (!kinf && KAHAN) ? -cmp[p][c] : 0.f;
-                        }
+                for (int k = P * NC; k < VH; ++k) { vh[k] = vl[k] = kh[k] = kl[k] = 0.f; }
+                ik_warp_reduce_cmp<VH>(vh, vl, lane);
+                ik_warp_reduce_cmp<VH>(kh, kl, lane);
+                // VH == 16: lanes 2k and 2k+1 both hold value k -> the even lane writes
+                // the virial, the odd lane the kinetic value; VH == 32: one value per lane
 #pragma unroll
-                    for (int k = P * NC; k < VH; ++k) { hi[k] = 0.f; lo[k] = 0.f; }
-                    ik_warp_reduce_cmp<VH>(hi, lo, lane);
+                for (int f = 0; f < (VH == 16 ? 1 : 2); ++f) {
+                    const bool kin_here = VH == 16 ? (lane & 1) != 0 : f == 1;
+                    const int idx = ik_red_index<VH>(lane, 0);
+                    const float h = kin_here ? kh[0] : vh[0], l = kin_here ? kl[0] : vl[0];
+                    const bool want = kin_here ? want_kin : (a.fields & 1);
+                    if (idx < P * NC && want) {
+                        const int p = idx / NC, c = idx - p * NC;
+                        int g = -1;
 #pragma unroll
-                    for (int k = 0; k < PER; ++k) {
-                        const int idx = ik_red_index<VH>(lane, k);
-                        // with VH < 32 every value is held by 32/VH lanes: the lowest writes
-                        const bool owner = VH >= 32 || (lane & (32 / VH - 1)) == 0;
-                        if (idx < P * NC && owner) {
-                            const int p = idx / NC, c = idx - p * NC;
-                            int g = -1;
-#pragma unroll
-                            for (int pp = 0; pp < P; ++pp) if (pp == p) g = gi[pp];
-                            if (g >= 0) {
-                                double* out = kinf ? a.out_kin : a.out_vir;
-                                const double v = ((double)hi[k] + (double)lo[k]) * (kinf ? a.kin_scale : a.vir_scale);
-                                const size_t o = (size_t)g * NC + c;
-                                out[o] = first ? v : out[o] + v;
+                        for (int pp = 0; pp < P; ++pp) if (pp == p) g = gi[pp];
+                        if (g >= 0) {
+                            float2* out = kin_here ? a.out_kin : a.out_vir;
+                            const size_t o = (size_t)g * NC + c;
+                            if (first) {
+                                out[o] = make_float2(h, l);
+                            } else { // another chunk of the same item: compensated add
+                                const float2 old = out[o];
+                                float s2, e2;
+                                ik_two_sum(old.x, h, s2, e2);
+                                out[o] = make_float2(s2, e2 + (old.y + l));
                             }
                         }
                     }
@@ -474,4 +483,21 @@ cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, int blo
                                    : launch_np<2, false>(a, kind, blocks, threads, smem, st);
     return kahan ? launch_np<3, true>(a, kind, blocks, threads, smem, st)
                  : launch_np<3, false>(a, kind, blocks, threads, smem, st);
+}
+
+// Double-float pairs -> FP64, scaled: out = ((double)hi + (double)lo) * scale.  One
+// thread per value (fully populated warps: the FP64 pipe is narrow on this GPU).
+__global__ void k_pairs_to_f64(const float2* __restrict__ in, double* __restrict__ out, int count, double scale)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const float2 v = in[k];
+    out[k] = ((double)v.x + (double)v.y) * scale;
+}
+
+cudaError_t launch_pairs_to_f64(const float2* in, double* out, long long count, double scale, cudaStream_t st)
+{
+    if (count <= 0) return cudaSuccess;
+    k_pairs_to_f64<<<(int)((count + 255) / 256), 256, 0, st>>>(in, out, (int)count, scale);
+    return cudaGetLastError();
 }

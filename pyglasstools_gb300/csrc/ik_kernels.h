@@ -63,9 +63,8 @@ struct GatherArgs32 {
     const int4* items;     // {cx0, cy0, cz0, gstart}; items[nitems].w = end
     int nitems;
     int halo_cap, qcap;
-    double vir_scale, kin_scale;
-    double* out_vir;
-    double* out_kin;
+    float2* out_vir;       // unscaled double-float pairs (hi, lo), g x NC
+    float2* out_kin;
     int fields;
     int* work_counter;
     int* status;
@@ -74,6 +73,7 @@ struct GatherArgs32 {
 };
 cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, int blocks, int threads,
                             size_t smem, cudaStream_t st);
+cudaError_t launch_pairs_to_f64(const float2* in, double* out, long long count, double scale, cudaStream_t st);
 
 // ---- FP64 plain gather (ik_gather64.cu) ------------------------------------
 struct GatherArgs64 {
