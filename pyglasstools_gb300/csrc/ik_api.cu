@@ -478,7 +478,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         a.cnt_pairs = cnt + 1;
         a.cnt_triples = cnt + 2;
         CK(cudaMemsetAsync(L.work_counter.p, 0, sizeof(int), L.st));
-        size_t smem = (size_t)IK_WARPS_GATHER * ((size_t)c->halo_cap * 16 + (size_t)a.qcap * 4);
+        size_t smem = (size_t)IK_WARPS_GATHER * ((size_t)c->halo_cap * 20 + (size_t)a.qcap * 4);
         int blocks = std::min(c->nitems, c->sm_count * 2);
         if (blocks > 0)
             CK(launch_gather32(a, c->cg.kind, (c->flags & IK_FLAG_LANE_KAHAN) != 0, blocks, 32 * IK_WARPS_GATHER,

@@ -75,6 +75,43 @@ __device__ __forceinline__ void ik_two_sum(float a, float b, float& s, float& e)
 
 __host__ __device__ constexpr int ik_pow2_ceil(int x) { int p = 1; while (p < x) p <<= 1; return p; }
 
+// Packed FP32 pairs (sm_100+ f32x2 arithmetic): two grid points evaluated per instruction.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float a, float b)
+{
+    f32x2 r;
+    asm("mov.b64 %0, {%1,%2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void up2(f32x2 r, float& a, float& b)
+{
+    asm("mov.b64 {%0,%1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b)
+{
+    f32x2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b)
+{
+    f32x2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b)
+{
+    f32x2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c)
+{
+    f32x2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
 // Compensated transposing butterfly over a warp: on entry each lane holds V values
 // (hi[k], lo[k] = 0); after the call lane l holds, for k < max(V/32, 1), the warp sum
 // of value ik_red_index<V>(l, k) as hi[k] + lo[k] (hi + lo exact to ~2 ulp of the
@@ -139,8 +176,11 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
     extern __shared__ float4 smem[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    float4* stage = smem + (size_t)warp * (a.halo_cap + a.qcap / 4);
-    int* queue = reinterpret_cast<int*>(stage + a.halo_cap);
+    // per warp: staged particles (float4 x,y,z, bits(bond offset << 6 | bond count)),
+    // their cell-order indices, and the slot queue
+    float4* stage = smem + (size_t)warp * (a.halo_cap + a.halo_cap / 4 + a.qcap / 4);
+    int* sq = reinterpret_cast<int*>(stage + a.halo_cap);
+    int* queue = sq + a.halo_cap;
 
     const float R2s = a.R2s, margin = a.margin, kappa = a.kappa;
     const bool want_kin = (a.fields & 2) != 0;
@@ -208,12 +248,14 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                     for (int t = 0; t < ccnt; ++t) {
                         int q = cstart + t;
                         IkPRec r = a.prec[q];
+                        int b0 = a.boff[q], b1 = a.boff[q + 1];
                         float4 s;
                         s.x = fmaf(kappa, r.x, ox);
                         s.y = fmaf(kappa, r.y, oy);
                         s.z = DIM == 3 ? fmaf(kappa, r.z, oz) : 0.f;
-                        s.w = __int_as_float(q);
+                        s.w = __int_as_float((b0 << 6) | (b1 - b0));
                         stage[dst + t] = s;
+                        sq[dst + t] = q;
                     }
                 }
                 nst += __shfl_sync(FULL, incl, k - 1);
@@ -243,12 +285,24 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
 #pragma unroll
                     for (int c = 0; c < NC; ++c) { acc[p][c] = 0.f; cmp[p][c] = 0.f; kac[p][c] = 0.f; }
 
+                // packed grid coordinates of the point pairs (0,1), (2,3)
+                f32x2 g2[P / 2][3];
+#pragma unroll
+                for (int j = 0; j < P / 2; ++j)
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) g2[j][d] = pk2(gu[2 * j][d], gu[2 * j + 1][d]);
+                f32x2 acc2[P / 2][NC];
+#pragma unroll
+                for (int j = 0; j < P / 2; ++j)
+#pragma unroll
+                    for (int c = 0; c < NC; ++c) acc2[j][c] = 0ull;
+
                 // one slot: staged particle s, its bond k, grid mask m
                 auto process_slot = [&](int e) {
                     const int s = e >> 10, m = e & 15;
                     const float4 sp = stage[s];
-                    const int q = __float_as_int(sp.w);
-                    const float4 b = __ldg(a.bonds + a.boff[q] + ((e >> 4) & 63));
+                    const int bo = __float_as_int(sp.w) >> 6;
+                    const float4 b = __ldg(a.bonds + bo + ((e >> 4) & 63));
                     const float hbx = b.x, hby = b.y, hbz = b.z;
                     const float hh = DIM == 3 ? fmaf(hbz, hbz, fmaf(hby, hby, hbx * hbx)) : fmaf(hby, hby, hbx * hbx);
                     const float fx = b.w * hbx, fy = b.w * hby;
@@ -264,52 +318,94 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                         cf[4 % NC] = fx * hbz;
                         cf[5 % NC] = fy * hbz;
                     }
-                    float cq[NP > 0 ? NP : 1];
-                    if constexpr (NP > 0) {
-#pragma unroll
-                        for (int t = 0; t < NP; ++t) cq[t] = a.xi2[t] * hh;
-                    }
                     const float mx0 = sp.x + hbx, my0 = sp.y + hby, mz0 = sp.z + hbz; // bond midpoint
+                    if constexpr (!KAHAN && NP > 0) {
+                        // packed path: two grid points per f32x2 instruction
+                        const f32x2 mid2x = pk2(mx0, mx0), mid2y = pk2(my0, my0), mid2z = pk2(mz0, mz0);
+                        const f32x2 hb2x = pk2(hbx, hbx), hb2y = pk2(hby, hby), hb2z = pk2(hbz, hbz);
+                        f32x2 cq2[NP], cf2[NC];
 #pragma unroll
-                    for (int p = 0; p < P; ++p) {
-                        const float mx = gu[p][0] - mx0, my = gu[p][1] - my0;
-                        float M = mx * mx, mb = mx * hbx;
-                        M = fmaf(my, my, M);
-                        mb = fmaf(my, hby, mb);
-                        if (DIM == 3) {
-                            const float mz = gu[p][2] - mz0;
-                            M = fmaf(mz, mz, M);
-                            mb = fmaf(mz, hbz, mb);
-                        }
-                        // r^2(xi) = M - 2 xi mb + xi^2 hh at the symmetric nodes +-xi
-                        float B = a.w0 * ik_kern<KIND>(M, R2s);
-                        if constexpr (NP > 0) {
+                        for (int t = 0; t < NP; ++t) { const float v = a.xi2[t] * hh; cq2[t] = pk2(v, v); }
+#pragma unroll
+                        for (int c = 0; c < NC; ++c) cf2[c] = pk2(cf[c], cf[c]);
+#pragma unroll
+                        for (int j = 0; j < P / 2; ++j) {
+                            const f32x2 mx = sub2(g2[j][0], mid2x), my = sub2(g2[j][1], mid2y);
+                            f32x2 M = fma2(my, my, mul2(mx, mx));
+                            f32x2 mb = fma2(my, hb2y, mul2(mx, hb2x));
+                            if (DIM == 3) {
+                                const f32x2 mz = sub2(g2[j][2], mid2z);
+                                M = fma2(mz, mz, M);
+                                mb = fma2(mz, hb2z, mb);
+                            }
+                            float Ma, Mb;
+                            up2(M, Ma, Mb);
+                            f32x2 B = mul2(pk2(a.w0, a.w0), pk2(ik_kern<KIND>(Ma, R2s), ik_kern<KIND>(Mb, R2s)));
 #pragma unroll
                             for (int t = 0; t < NP; ++t) {
-                                const float base = M + cq[t];
-                                const float kp = ik_kern<KIND>(fmaf(a.m2xi[t], mb, base), R2s);
-                                const float km = ik_kern<KIND>(fmaf(-a.m2xi[t], mb, base), R2s);
-                                B = fmaf(a.w[t], kp + km, B);
+                                const f32x2 base = add2(M, cq2[t]);
+                                const f32x2 rp = fma2(pk2(a.m2xi[t], a.m2xi[t]), mb, base);
+                                const f32x2 rm = fma2(pk2(-a.m2xi[t], -a.m2xi[t]), mb, base);
+                                float pa, pb, qa, qb;
+                                up2(rp, pa, pb);
+                                up2(rm, qa, qb);
+                                const f32x2 ks = pk2(ik_kern<KIND>(pa, R2s) + ik_kern<KIND>(qa, R2s),
+                                                     ik_kern<KIND>(pb, R2s) + ik_kern<KIND>(qb, R2s));
+                                B = fma2(pk2(a.w[t], a.w[t]), ks, B);
                             }
-                        } else {
-#pragma unroll 1
-                            for (int t = 0; t < npairs; ++t) {
-                                const float base = fmaf(a.xi2[t], hh, M);
-                                const float kp = ik_kern<KIND>(fmaf(a.m2xi[t], mb, base), R2s);
-                                const float km = ik_kern<KIND>(fmaf(-a.m2xi[t], mb, base), R2s);
-                                B = fmaf(a.w[t], kp + km, B);
-                            }
-                        }
-                        B = (m & (1 << p)) ? B : 0.f;
+                            float Ba, Bb;
+                            up2(B, Ba, Bb);
+                            B = pk2((m & (1 << (2 * j))) ? Ba : 0.f, (m & (2 << (2 * j))) ? Bb : 0.f);
 #pragma unroll
-                        for (int c = 0; c < NC; ++c) {
-                            if (KAHAN) {
-                                const float y = fmaf(B, cf[c], -cmp[p][c]);
-                                const float t2 = acc[p][c] + y;
-                                cmp[p][c] = (t2 - acc[p][c]) - y;
-                                acc[p][c] = t2;
+                            for (int c = 0; c < NC; ++c) acc2[j][c] = fma2(B, cf2[c], acc2[j][c]);
+                        }
+                    } else {
+                        float cq[NP > 0 ? NP : 1];
+                        if constexpr (NP > 0) {
+#pragma unroll
+                            for (int t = 0; t < NP; ++t) cq[t] = a.xi2[t] * hh;
+                        }
+#pragma unroll
+                        for (int p = 0; p < P; ++p) {
+                            const float mx = gu[p][0] - mx0, my = gu[p][1] - my0;
+                            float M = mx * mx, mb = mx * hbx;
+                            M = fmaf(my, my, M);
+                            mb = fmaf(my, hby, mb);
+                            if (DIM == 3) {
+                                const float mz = gu[p][2] - mz0;
+                                M = fmaf(mz, mz, M);
+                                mb = fmaf(mz, hbz, mb);
+                            }
+                            // r^2(xi) = M - 2 xi mb + xi^2 hh at the symmetric nodes +-xi
+                            float B = a.w0 * ik_kern<KIND>(M, R2s);
+                            if constexpr (NP > 0) {
+#pragma unroll
+                                for (int t = 0; t < NP; ++t) {
+                                    const float base = M + cq[t];
+                                    const float kp = ik_kern<KIND>(fmaf(a.m2xi[t], mb, base), R2s);
+                                    const float km = ik_kern<KIND>(fmaf(-a.m2xi[t], mb, base), R2s);
+                                    B = fmaf(a.w[t], kp + km, B);
+                                }
                             } else {
-                                acc[p][c] = fmaf(B, cf[c], acc[p][c]);
+#pragma unroll 1
+                                for (int t = 0; t < npairs; ++t) {
+                                    const float base = fmaf(a.xi2[t], hh, M);
+                                    const float kp = ik_kern<KIND>(fmaf(a.m2xi[t], mb, base), R2s);
+                                    const float km = ik_kern<KIND>(fmaf(-a.m2xi[t], mb, base), R2s);
+                                    B = fmaf(a.w[t], kp + km, B);
+                                }
+                            }
+                            B = (m & (1 << p)) ? B : 0.f;
+#pragma unroll
+                            for (int c = 0; c < NC; ++c) {
+                                if (KAHAN) {
+                                    const float y = fmaf(B, cf[c], -cmp[p][c]);
+                                    const float t2 = acc[p][c] + y;
+                                    cmp[p][c] = (t2 - acc[p][c]) - y;
+                                    acc[p][c] = t2;
+                                } else {
+                                    acc[p][c] = fmaf(B, cf[c], acc[p][c]);
+                                }
                             }
                         }
                     }
@@ -322,7 +418,6 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                     int mask = 0, cnt = 0;
                     if (s < nst) {
                         const float4 sp = stage[s];
-                        const int q = __float_as_int(sp.w);
                         float r2v[P];
 #pragma unroll
                         for (int p = 0; p < P; ++p) {
@@ -332,7 +427,7 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                             bool in = r2 < R2s;
                             if (fabsf(r2 - R2s) < margin && gi[p] >= 0) {
                                 // boundary band: decide with the FP64 rule of the reference
-                                const IkB64 pq = a.pos64[q];
+                                const IkB64 pq = a.pos64[sq[s]];
                                 const double* xg = a.grid + 3 * (size_t)gi[p];
                                 const double ddx = ik_minimg(__dsub_rn(xg[0], pq.x), a.g.L[0], a.g.periodic[0]);
                                 const double ddy = ik_minimg(__dsub_rn(xg[1], pq.y), a.g.L[1], a.g.periodic[1]);
@@ -343,9 +438,9 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                             if (in) mask |= 1 << p;
                         }
                         if (mask) {
-                            const int nbq = a.boff[q + 1] - a.boff[q];
-                            cnt = nbq;
+                            cnt = __float_as_int(sp.w) & 63;
                             if (want_kin) {
+                                const int q = sq[s];
                                 float4 k0 = __ldg(a.kin + (DIM == 2 ? q : 2 * q));
                                 float4 k1 = DIM == 3 ? __ldg(a.kin + 2 * q + 1) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
@@ -388,6 +483,12 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                 // ---- combine lanes (compensated): virial, then kinetic, each a
                 //      transposing butterfly of VH values; results are written as
                 //      unscaled double-float pairs (hi, lo), converted to FP64 later
+                if constexpr (!KAHAN && NP > 0) {
+#pragma unroll
+                    for (int j = 0; j < P / 2; ++j)
+#pragma unroll
+                        for (int c = 0; c < NC; ++c) up2(acc2[j][c], acc[2 * j][c], acc[2 * j + 1][c]);
+                }
                 constexpr int VH = ik_pow2_ceil(P * NC);
                 static_assert(VH == 16 || VH == 32, "butterfly width");
                 float vh[VH], vl[VH], kh[VH], kl[VH];
