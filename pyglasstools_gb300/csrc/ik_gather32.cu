@@ -266,18 +266,19 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
 
             // ---- process the item's groups against the staged particles
             for (int gs = it.w; gs < gend; gs += P) {
-                float gu[P][3];
+                // the group's grid points, packed in pairs (0,1), (2,3) for f32x2 arithmetic
+                f32x2 g2[P / 2][3];
                 int gi[P];
 #pragma unroll
-                for (int p = 0; p < P; ++p) {
-                    if (gs + p < gend) {
-                        float4 v = a.gpts[gs + p];
-                        gu[p][0] = v.x; gu[p][1] = v.y; gu[p][2] = v.z;
-                        gi[p] = __float_as_int(v.w);
-                    } else {
-                        gu[p][0] = gu[p][1] = gu[p][2] = 1e18f;
-                        gi[p] = -1;
-                    }
+                for (int j = 0; j < P / 2; ++j) {
+                    float4 v0 = make_float4(1e18f, 1e18f, 1e18f, __int_as_float(-1)), v1 = v0;
+                    if (gs + 2 * j < gend) v0 = a.gpts[gs + 2 * j];
+                    if (gs + 2 * j + 1 < gend) v1 = a.gpts[gs + 2 * j + 1];
+                    g2[j][0] = pk2(v0.x, v1.x);
+                    g2[j][1] = pk2(v0.y, v1.y);
+                    g2[j][2] = pk2(v0.z, v1.z);
+                    gi[2 * j] = __float_as_int(v0.w);
+                    gi[2 * j + 1] = __float_as_int(v1.w);
                 }
                 float acc[P][NC], cmp[P][NC], kac[P][NC];
 #pragma unroll
@@ -285,24 +286,20 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
 #pragma unroll
                     for (int c = 0; c < NC; ++c) { acc[p][c] = 0.f; cmp[p][c] = 0.f; kac[p][c] = 0.f; }
 
-                // packed grid coordinates of the point pairs (0,1), (2,3)
-                f32x2 g2[P / 2][3];
-#pragma unroll
-                for (int j = 0; j < P / 2; ++j)
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) g2[j][d] = pk2(gu[2 * j][d], gu[2 * j + 1][d]);
                 f32x2 acc2[P / 2][NC];
 #pragma unroll
                 for (int j = 0; j < P / 2; ++j)
 #pragma unroll
                     for (int c = 0; c < NC; ++c) acc2[j][c] = 0ull;
 
-                // one slot: staged particle s, its bond k, grid mask m
-                auto process_slot = [&](int e) {
-                    const int s = e >> 10, m = e & 15;
-                    const float4 sp = stage[s];
-                    const int bo = __float_as_int(sp.w) >> 6;
-                    const float4 b = __ldg(a.bonds + bo + ((e >> 4) & 63));
+                // one slot: staged particle s, its bond k, grid mask m.  The loads are
+                // separate so that two batches can be in flight before either computes.
+                auto load_slot = [&](int e, float4& sp, float4& b) {
+                    sp = stage[e >> 10];
+                    b = __ldg(a.bonds + (__float_as_int(sp.w) >> 6) + ((e >> 4) & 63));
+                };
+                auto process_slot = [&](int e, const float4& sp, const float4& b) {
+                    const int m = e & 15;
                     const float hbx = b.x, hby = b.y, hbz = b.z;
                     const float hh = DIM == 3 ? fmaf(hbz, hbz, fmaf(hby, hby, hbx * hbx)) : fmaf(hby, hby, hbx * hbx);
                     const float fx = b.w * hbx, fy = b.w * hby;
@@ -367,12 +364,19 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                         }
 #pragma unroll
                         for (int p = 0; p < P; ++p) {
-                            const float mx = gu[p][0] - mx0, my = gu[p][1] - my0;
+                            float gx, gy, gz, t0, t1, t2;
+                            up2(g2[p >> 1][0], t0, t1);
+                            gx = (p & 1) ? t1 : t0;
+                            up2(g2[p >> 1][1], t0, t1);
+                            gy = (p & 1) ? t1 : t0;
+                            up2(g2[p >> 1][2], t0, t2);
+                            gz = (p & 1) ? t2 : t0;
+                            const float mx = gx - mx0, my = gy - my0;
                             float M = mx * mx, mb = mx * hbx;
                             M = fmaf(my, my, M);
                             mb = fmaf(my, hby, mb);
                             if (DIM == 3) {
-                                const float mz = gu[p][2] - mz0;
+                                const float mz = gz - mz0;
                                 M = fmaf(mz, mz, M);
                                 mb = fmaf(mz, hbz, mb);
                             }
@@ -418,12 +422,26 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                     int mask = 0, cnt = 0;
                     if (s < nst) {
                         const float4 sp = stage[s];
+                        float4 k0 = make_float4(0.f, 0.f, 0.f, 0.f), k1 = k0;
+                        if (want_kin) { // issued before the tests so the latency overlaps them
+                            const int q = sq[s];
+                            k0 = __ldg(a.kin + (DIM == 2 ? q : 2 * q));
+                            if (DIM == 3) k1 = __ldg(a.kin + 2 * q + 1);
+                        }
                         float r2v[P];
+                        {
+                            const f32x2 sx = pk2(sp.x, sp.x), sy = pk2(sp.y, sp.y), sz = pk2(sp.z, sp.z);
+#pragma unroll
+                            for (int j = 0; j < P / 2; ++j) {
+                                const f32x2 dx = sub2(g2[j][0], sx), dy = sub2(g2[j][1], sy);
+                                f32x2 r2 = fma2(dy, dy, mul2(dx, dx));
+                                if (DIM == 3) { const f32x2 dz = sub2(g2[j][2], sz); r2 = fma2(dz, dz, r2); }
+                                up2(r2, r2v[2 * j], r2v[2 * j + 1]);
+                            }
+                        }
 #pragma unroll
                         for (int p = 0; p < P; ++p) {
-                            const float dx = gu[p][0] - sp.x, dy = gu[p][1] - sp.y;
-                            float r2 = fmaf(dy, dy, dx * dx);
-                            if (DIM == 3) { const float dz = gu[p][2] - sp.z; r2 = fmaf(dz, dz, r2); }
+                            const float r2 = r2v[p];
                             bool in = r2 < R2s;
                             if (fabsf(r2 - R2s) < margin && gi[p] >= 0) {
                                 // boundary band: decide with the FP64 rule of the reference
@@ -434,15 +452,11 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                                 const double ddz = ik_minimg(__dsub_rn(xg[2], pq.z), a.g.L[2], a.g.periodic[2]);
                                 in = ik_dot3(ddx, ddy, ddz) < a.R2;
                             }
-                            r2v[p] = r2;
                             if (in) mask |= 1 << p;
                         }
                         if (mask) {
                             cnt = __float_as_int(sp.w) & 63;
                             if (want_kin) {
-                                const int q = sq[s];
-                                float4 k0 = __ldg(a.kin + (DIM == 2 ? q : 2 * q));
-                                float4 k1 = DIM == 3 ? __ldg(a.kin + 2 * q + 1) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
                                 for (int p = 0; p < P; ++p) {
                                     const float kv = (mask & (1 << p)) ? ik_kern_in<KIND>(r2v[p]) : 0.f;
@@ -471,13 +485,30 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                     for (int k = 0; k < cnt; ++k) queue[off + k] = entry | (k << 4);
                     qn += tot;
                     __syncwarp();
-                    while (qn >= 32) {
+                    while (qn >= 64) { // two batches in flight
+                        const int e1 = queue[qn - 32 + lane], e2 = queue[qn - 64 + lane];
+                        qn -= 64;
+                        float4 sp1, b1, sp2, b2;
+                        load_slot(e1, sp1, b1);
+                        load_slot(e2, sp2, b2);
+                        process_slot(e1, sp1, b1);
+                        process_slot(e2, sp2, b2);
+                    }
+                    if (qn >= 32) {
                         qn -= 32;
-                        process_slot(queue[qn + lane]);
+                        const int e1 = queue[qn + lane];
+                        float4 sp1, b1;
+                        load_slot(e1, sp1, b1);
+                        process_slot(e1, sp1, b1);
                     }
                     __syncwarp();
                 }
-                if (lane < qn) process_slot(queue[lane]);
+                if (lane < qn) {
+                    const int e1 = queue[lane];
+                    float4 sp1, b1;
+                    load_slot(e1, sp1, b1);
+                    process_slot(e1, sp1, b1);
+                }
                 __syncwarp();
 
                 // ---- combine lanes (compensated): virial, then kinetic, each a
