@@ -95,6 +95,15 @@ int ik_set_frame(ik_ctx* ctx, int64_t n, const double* pos, const double* vel,
  * stream; results stay in HBM in the slot's field buffers.  fields: IK_FIELD_* mask.
  * Replaces IrvingKirkwood::compute (IrvingKirkwood.h:74-110). */
 int ik_compute_slot(ik_ctx* ctx, int slot, int precision, int fields);
+/* Compute `count` slots as one batch.  The first call with a given slot list runs
+ * the slots with ordinary launches (sizing every buffer) and records the same
+ * sequence as a CUDA graph; later calls with the same slots, precision and fields
+ * replay that graph with a single launch (re-recorded automatically after a frame's
+ * size, the box, the grid or a capacity changes).  Asynchronous like ik_compute_slot.
+ * Replaces the per-frame loop of pyglasstools.analyze (pyglasstools/__init__.py:107-138)
+ * over IrvingKirkwood::compute for resident frames. */
+int ik_compute_batch(ik_ctx* ctx, const int* slots, int count, int precision, int fields);
+
 /* Wait for all of the context's work; reports device-side status words.  (Slots are
  * computed on several internal streams so that consecutive frames overlap.) */
 int ik_synchronize(ik_ctx* ctx);

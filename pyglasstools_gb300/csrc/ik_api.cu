@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <atomic>
 #include <vector>
 
 namespace {
@@ -35,6 +36,9 @@ int fail(int code, const char* fmt, ...)
                         __LINE__);                                                        \
     } while (0)
 
+// bumped by every device allocation: a captured graph holds buffer addresses
+static std::atomic<int64_t> g_alloc_epoch{0};
+
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
@@ -53,6 +57,7 @@ struct DevBuf {
         if (need <= bytes && p) return IK_OK;
         if (p) { cudaFree(p); p = nullptr; bytes = 0; }
         size_t b = std::max<size_t>(need, 256);
+        ++g_alloc_epoch;
         cudaError_t e = cudaMalloc(&p, b);
         if (e != cudaSuccess) {
             p = nullptr;
@@ -135,6 +140,16 @@ struct ik_ctx {
     DevBuf q_cell_of, q_rank, q_count, q_start, q_sorted, q_cnt, q_offs, q_idx, q_flag;
     std::vector<Slot> slots;
     std::vector<PendingOp> pending;
+    // CUDA-graph replay of ik_compute_batch
+    bool capturing = false;
+    int captured_lanes = 0;
+    cudaGraphExec_t batch_exec = nullptr;
+    std::vector<int> batch_slots;
+    int batch_prec = -1, batch_fields = 0, batch_maxb = 0, batch_halo = 0;
+    int64_t batch_geom_version = -1, batch_slot_version = -1;
+    int64_t geom_version = 0, slot_version = 0, config_version = 0;
+    int64_t batch_config_version = -1, batch_alloc_epoch = -1;
+    int64_t batch_launches = 0;
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     int64_t launches = 0;
     float timing[4] = {0, 0, 0, 0};
@@ -324,6 +339,7 @@ int ensure_geometry(ik_ctx* c)
     CK(cudaMemcpy(c->gpts_d.p, gpts.data(), gpts.size() * sizeof(float4), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->items_d.p, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
     c->geom_valid = true;
+    ++c->geom_version;
     return IK_OK;
 }
 
@@ -385,11 +401,11 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
     // fork from the main stream (uploads), and after the slot's previous computation
     CK(cudaEventRecord(c->fork, c->stream));
     CK(cudaStreamWaitEvent(L.st, c->fork, 0));
-    if (s.done_recorded) CK(cudaStreamWaitEvent(L.st, s.done, 0));
+    if (s.done_recorded && !c->capturing) CK(cudaStreamWaitEvent(L.st, s.done, 0));
     const IkGeom& g = c->geom;
     const int D = c->dim, NC = D == 2 ? 3 : 6;
     const int n = (int)s.n;
-    bool timing = (c->flags & IK_FLAG_TIMING) != 0;
+    bool timing = (c->flags & IK_FLAG_TIMING) != 0 && !c->capturing;
     if (timing) CK(cudaEventRecord(c->ev[0], L.st));
     ENS(s.vir, sizeof(double) * NC * c->G);
     ENS(s.kin, sizeof(double) * NC * c->G);
@@ -531,6 +547,10 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
     s.last_prec = prec;
     s.last_fields = fields;
     if (!s.done) CK(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
+    if (c->capturing) { // the lane rejoins the main stream at the end of the capture
+        c->captured_lanes |= 1 << (int)(&L - c->lanes);
+        return IK_OK;
+    }
     CK(cudaEventRecord(s.done, L.st));
     s.done_recorded = true;
     CK(cudaEventRecord(L.last, L.st));
@@ -601,6 +621,7 @@ int ik_destroy(ik_ctx* c)
     for (Lane& L : c->lanes) if (L.st) cudaStreamSynchronize(L.st);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (auto& ev : c->ev) if (ev) cudaEventDestroy(ev);
+    if (c->batch_exec) cudaGraphExecDestroy(c->batch_exec);
     if (c->fork) cudaEventDestroy(c->fork);
     for (Slot& s : c->slots) if (s.done) cudaEventDestroy(s.done);
     for (Lane& L : c->lanes) {
@@ -615,6 +636,7 @@ int ik_destroy(ik_ctx* c)
 int ik_set_box(ik_ctx* c, int dim, const double boxsize[3], const double origin[3])
 {
     if (int r = check_ctx(c)) return r;
+    ++c->config_version; // captured batch graphs hold the old settings
     if (dim != 2 && dim != 3) return fail(IK_ERR_ARG, "dim must be 2 or 3 (got %d)", dim);
     if (!boxsize) return fail(IK_ERR_ARG, "null boxsize");
     double b[3] = {boxsize[0], boxsize[1], boxsize[2]};
@@ -640,6 +662,7 @@ int ik_set_box(ik_ctx* c, int dim, const double boxsize[3], const double origin[
 int ik_set_potential_poly12(ik_ctx* c, double scaled_rcut, const double params[5])
 {
     if (int r = check_ctx(c)) return r;
+    ++c->config_version; // captured batch graphs hold the old settings
     if (!params) return fail(IK_ERR_ARG, "null params");
     if (!(scaled_rcut > 0.0)) return fail(IK_ERR_ARG, "scaled_rcut must be > 0");
     c->pot.rcutsq = scaled_rcut * scaled_rcut;
@@ -656,6 +679,7 @@ int ik_set_potential_poly12(ik_ctx* c, double scaled_rcut, const double params[5
 int ik_set_cgfunc(ik_ctx* c, int kind, int mode, int order, double rcut, double width)
 {
     if (int r = check_ctx(c)) return r;
+    ++c->config_version; // captured batch graphs hold the old settings
     if (kind < 0 || kind > 3) return fail(IK_ERR_ARG, "unknown coarse-graining kind %d", kind);
     if (mode < 0 || mode > 3) return fail(IK_ERR_ARG, "unknown quadrature mode %d", mode);
     if (!(rcut > 0.0) || !std::isfinite(rcut)) return fail(IK_ERR_ARG, "rcut must be > 0");
@@ -716,6 +740,7 @@ int ik_set_cgfunc(ik_ctx* c, int kind, int mode, int order, double rcut, double 
 int ik_set_adaptive(ik_ctx* c, int neval, double relerr, double abserr)
 {
     if (int r = check_ctx(c)) return r;
+    ++c->config_version; // captured batch graphs hold the old settings
     c->cg.neval = neval;
     c->cg.relerr = relerr;
     c->cg.abserr = abserr;
@@ -725,6 +750,7 @@ int ik_set_adaptive(ik_ctx* c, int neval, double relerr, double abserr)
 int ik_set_max_rcut(ik_ctx* c, double max_rcut)
 {
     if (int r = check_ctx(c)) return r;
+    ++c->config_version; // captured batch graphs hold the old settings
     if (!(max_rcut > 0.0) || !std::isfinite(max_rcut)) return fail(IK_ERR_ARG, "max_rcut must be > 0");
     if (!c->max_rcut_set || c->max_rcut != max_rcut) c->geom_valid = false;
     c->max_rcut = max_rcut;
@@ -745,6 +771,7 @@ int ik_get_max_rcut(ik_ctx* c, double* out)
 int ik_set_grid(ik_ctx* c, int64_t g, const double* xyz)
 {
     if (int r = check_ctx(c)) return r;
+    ++c->config_version; // captured batch graphs hold the old settings
     if (g < 0 || (g > 0 && !xyz)) return fail(IK_ERR_ARG, "bad grid arguments");
     if (g > (int64_t)1 << 30) return fail(IK_ERR_UNSUPPORTED, "grid too large");
     for (int64_t i = 0; i < 3 * g; ++i)
@@ -760,6 +787,7 @@ int ik_set_grid(ik_ctx* c, int64_t g, const double* xyz)
 int ik_reserve_slots(ik_ctx* c, int nslots)
 {
     if (int r = check_ctx(c)) return r;
+    ++c->config_version; // captured batch graphs hold the old settings
     if (nslots < 1 || nslots > 65536) return fail(IK_ERR_ARG, "nslots out of range");
     if (int r = ik_synchronize(c)) return r;
     if ((int)c->slots.size() < nslots) c->slots.resize((size_t)nslots);
@@ -779,6 +807,8 @@ int ik_upload_frame(ik_ctx* c, int slot, int64_t n, const double* pos, const dou
         for (int64_t i = 0; i < n; ++i) dmax = std::max(dmax, diam[i]);
     Slot& s = c->slots[(size_t)slot];
     if (s.done_recorded) CK(cudaStreamWaitEvent(c->stream, s.done, 0)); // inputs still in use
+    const void* old_ptrs[4] = {s.pos.p, s.diam.p, s.vel.p, s.mass.p};
+    const bool old_vel = s.has_vel, old_mass = s.has_mass;
     ENS(s.pos, sizeof(double) * 3 * std::max<int64_t>(n, 1));
     ENS(s.diam, sizeof(double) * std::max<int64_t>(n, 1));
     if (n > 0) {
@@ -800,6 +830,9 @@ int ik_upload_frame(ik_ctx* c, int slot, int64_t n, const double* pos, const dou
                                                                   c->dim, c->status.as<int>());
         CK(cudaGetLastError());
     }
+    if (s.n != n || old_ptrs[0] != s.pos.p || old_ptrs[1] != s.diam.p || old_ptrs[2] != s.vel.p ||
+        old_ptrs[3] != s.mass.p || old_vel != s.has_vel || old_mass != s.has_mass)
+        ++c->slot_version; // sizes or buffers changed: captured graphs are stale
     s.n = n;
     s.dmax = dmax;
     if (!c->max_rcut_set && n > 0 && c->pot_set) {
@@ -830,6 +863,85 @@ int ik_compute_slot(ik_ctx* c, int slot, int precision, int fields)
     if (c->halo_cap == 0) c->halo_cap = c->dim == 2 ? 512 : 768;
     c->pending.push_back({slot, precision, fields});
     return enqueue(c, slot, precision, fields);
+}
+
+int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int fields)
+{
+    if (int r = check_ctx(c)) return r;
+    if (count < 1 || !slots) return fail(IK_ERR_ARG, "empty batch");
+    for (int k = 0; k < count; ++k) if (int r = slot_ok(c, slots[k])) return r;
+    if (precision != IK_PREC_FP64 && precision != IK_PREC_FP32) return fail(IK_ERR_ARG, "unknown precision %d", precision);
+    if (fields < 1 || fields > 3) return fail(IK_ERR_ARG, "fields mask must be 1, 2 or 3");
+    if (int r = ensure_ready(c)) return r;
+    if (c->cg.mode != IK_QUAD_FIXEDPOINT)
+        return fail(IK_ERR_UNSUPPORTED, "quadrature mode %d is not available on the GPU path yet", c->cg.mode);
+    if (int r = ensure_geometry(c)) return r;
+    if (c->maxb == 0) c->maxb = c->dim == 2 ? IK_MAXB_2D : IK_MAXB_3D;
+    if (c->halo_cap == 0) c->halo_cap = c->dim == 2 ? 512 : 768;
+    std::vector<int> key(slots, slots + count);
+    const bool reuse = c->batch_exec && key == c->batch_slots && c->batch_prec == precision &&
+                       c->batch_fields == fields && c->batch_maxb == c->maxb && c->batch_halo == c->halo_cap &&
+                       c->batch_geom_version == c->geom_version && c->batch_slot_version == c->slot_version &&
+                       c->batch_config_version == c->config_version && c->batch_alloc_epoch == g_alloc_epoch.load() &&
+                       !(c->flags & IK_FLAG_TIMING);
+    if (!reuse) {
+        // first run of this batch: plain launches (sizes every buffer, checks capacities)
+        for (int k = 0; k < count; ++k) {
+            c->pending.push_back({slots[k], precision, fields});
+            if (int r = enqueue(c, slots[k], precision, fields)) return r;
+        }
+        if (int r = ik_synchronize(c)) return r;
+        if (c->flags & IK_FLAG_TIMING) return IK_OK;
+        // then capture the same sequence as one graph (lanes fork from and join the main stream)
+        if (c->batch_exec) { cudaGraphExecDestroy(c->batch_exec); c->batch_exec = nullptr; }
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+        const int64_t launches_before = c->launches;
+        const int64_t epoch_before = g_alloc_epoch.load();
+        c->capturing = true;
+        c->captured_lanes = 0;
+        int rr = IK_OK;
+        for (int k = 0; k < count && rr == IK_OK; ++k) rr = enqueue(c, slots[k], precision, fields);
+        for (int l = 0; l < IK_LANES && rr == IK_OK; ++l)
+            if (c->captured_lanes & (1 << l)) {
+                if (cudaEventRecord(c->lanes[l].last, c->lanes[l].st) != cudaSuccess ||
+                    cudaStreamWaitEvent(c->stream, c->lanes[l].last, 0) != cudaSuccess)
+                    rr = fail(IK_ERR_CUDA, "joining a lane during capture failed");
+            }
+        c->capturing = false;
+        c->batch_launches = c->launches - launches_before;
+        c->launches = launches_before; // captured, not launched
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+        if (rr != IK_OK) { if (graph) cudaGraphDestroy(graph); return rr; }
+        if (e != cudaSuccess) return fail(IK_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&c->batch_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) { c->batch_exec = nullptr; return fail(IK_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e)); }
+        c->batch_slots = key;
+        c->batch_prec = precision;
+        c->batch_fields = fields;
+        c->batch_maxb = c->maxb;
+        c->batch_halo = c->halo_cap;
+        c->batch_geom_version = c->geom_version;
+        c->batch_slot_version = c->slot_version;
+        c->batch_config_version = c->config_version;
+        // an allocation during the capture (none is expected) leaves the graph unused
+        c->batch_alloc_epoch = g_alloc_epoch.load() == epoch_before ? epoch_before : -2;
+        return IK_OK; // the first call's results come from the plain launches
+    }
+    // replay: after everything already enqueued on the lanes
+    if (int r = ik_wait_all(c)) return r;
+    for (int k = 0; k < count; ++k) c->pending.push_back({slots[k], precision, fields});
+    CK(cudaGraphLaunch(c->batch_exec, c->stream));
+    for (int k = 0; k < count; ++k) {
+        Slot& s = c->slots[(size_t)slots[k]];
+        CK(cudaEventRecord(s.done, c->stream));
+        s.done_recorded = true;
+        s.last_prec = precision;
+        s.last_fields = fields;
+    }
+    c->launches += c->batch_launches;
+    return IK_OK;
 }
 
 int ik_synchronize(ik_ctx* c)
@@ -1046,6 +1158,7 @@ int ik_eval_bond(ik_ctx* c, int64_t m, const double* x, const double* ri, const 
 int ik_set_flags(ik_ctx* c, int flags)
 {
     if (int r = check_ctx(c)) return r;
+    ++c->config_version; // captured batch graphs hold the old settings
     c->flags = flags;
     return IK_OK;
 }

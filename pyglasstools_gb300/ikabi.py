@@ -72,6 +72,7 @@ def lib():
             "ik_measure_fp32_peak": ([i32, dp], i32),
             "ik_get_launch_count": ([vp, C.POINTER(C.c_int64)], i32),
             "ik_wait_all": ([vp], i32),
+            "ik_compute_batch": ([vp, C.POINTER(C.c_int), i32, i32, i32], i32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -171,6 +172,11 @@ class IKContext:
 
     def compute_slot(self, slot, precision="fp32", fields=FIELD_VIRIAL | FIELD_KINETIC):
         check(lib().ik_compute_slot(self._h, slot, PREC[precision], fields))
+
+    def compute_batch(self, slots, precision="fp32", fields=FIELD_VIRIAL | FIELD_KINETIC):
+        """Compute several slots as one batch (replayed as a CUDA graph after the first call)."""
+        arr = (C.c_int * len(slots))(*slots)
+        check(lib().ik_compute_batch(self._h, arr, len(slots), PREC[precision], fields))
 
     def synchronize(self):
         check(lib().ik_synchronize(self._h))

@@ -1,0 +1,140 @@
+"""GPU tests of resident multi-frame work: frames kept in slots, computed one slot at a
+time (ik_compute_slot) or as one batch (ik_compute_batch, replayed as a CUDA graph
+after its first call).  The batch must give bit-identical fields to the per-slot
+path -- the same kernels on the same inputs -- and must follow every change that
+stales a recorded graph: new frame contents, a frame of another size, new
+coarse-graining settings.  One slot is also checked against the FP64 oracle at the
+FP32 tolerance.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2, uniq
+
+pytestmark = pytest.mark.gpu
+
+FP32_TOL = 1e-5
+CG = dict(kind="gaussian", rcut=6.0, order=5, width=2.0)
+
+
+def _frames(n, seeds):
+    from pyglasstools_gb300 import synth
+    return [synth.make_frame(n, dim=2, seed=s) for s in seeds]
+
+
+def _context(ik, L, grid, nslots, cg=CG):
+    c = ik.IKContext()
+    c.set_box(2, [L, L, 1.0])
+    c.set_poly12()
+    c.set_cgfunc(cg["kind"], cg["rcut"], order=cg["order"], width=cg["width"])
+    c.set_grid(grid)
+    c.reserve_slots(nslots)
+    return c
+
+
+def _fields(ik, c, slots):
+    return [(c.get_field(ik.FIELD_VIRIAL, slot=k), c.get_field(ik.FIELD_KINETIC, slot=k)) for k in slots]
+
+
+def _upload(c, frames, slots=None):
+    for k, f in zip(slots or range(len(frames)), frames):
+        c.upload_frame(k, f.pos, f.diam, f.vel, f.mass)
+
+
+def _per_slot(ik, c, slots, prec):
+    for k in slots:
+        c.compute_slot(k, prec)
+    c.synchronize()
+    return _fields(ik, c, slots)
+
+
+def _batch(ik, c, slots, prec):
+    c.compute_batch(slots, prec)
+    c.synchronize()
+    return _fields(ik, c, slots)
+
+
+def _same(a, b):
+    for (va, ka), (vb, kb) in zip(a, b):
+        np.testing.assert_array_equal(va, vb)
+        np.testing.assert_array_equal(ka, kb)
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_batch_replay_matches_per_slot(prec):
+    from pyglasstools_gb300 import ikabi as ik, synth
+    F, n = 6, 3000
+    fr = _frames(n, range(100, 100 + F))
+    L = fr[0].L
+    grid = synth.lattice_grid(L, 40, 2)
+    c = _context(ik, L, grid, F)
+    _upload(c, fr)
+    slots = list(range(F))
+    want = _per_slot(ik, c, slots, prec)
+    l0 = c.launch_count()
+    got = _batch(ik, c, slots, prec)  # first call: plain launches + graph recording
+    _same(got, want)
+    assert c.launch_count() > l0
+    got = _batch(ik, c, slots, prec)  # replay of the recorded graph
+    _same(got, want)
+    # new frame contents of the same size: the replay recomputes them
+    fr2 = _frames(n, range(200, 200 + F))
+    _upload(c, fr2)
+    got = _batch(ik, c, slots, prec)
+    want2 = _per_slot(ik, c, slots, prec)
+    _same(got, want2)
+    assert not np.array_equal(want2[0][0], want[0][0])
+    c.close()
+
+
+def test_batch_follows_size_and_setting_changes(oracle):
+    from pyglasstools_gb300 import ikabi as ik, synth
+    F, n = 4, 2500
+    fr = _frames(n, range(300, 300 + F))
+    L = fr[0].L
+    grid = synth.lattice_grid(L, 32, 2)
+    c = _context(ik, L, grid, F)
+    _upload(c, fr)
+    h = n // 2  # slot 1 starts with half of its frame's particles
+    c.upload_frame(1, fr[1].pos[:h], fr[1].diam[:h], fr[1].vel[:h], fr[1].mass[:h])
+    slots = [3, 1, 2, 0]  # any order of slots
+    _batch(ik, c, slots, "fp32")
+    _batch(ik, c, slots, "fp32")
+    # a frame of another size in one slot (its buffers grow)
+    big = fr[1]
+    c.upload_frame(1, big.pos, big.diam, big.vel, big.mass)
+    got = _batch(ik, c, slots, "fp32")
+    want = _per_slot(ik, c, slots, "fp32")
+    _same(got, want)
+    # new coarse-graining width: the recorded graph holds the old one
+    cg2 = dict(CG, width=1.5)
+    c.set_cgfunc(cg2["kind"], cg2["rcut"], order=cg2["order"], width=cg2["width"])
+    got = _batch(ik, c, slots, "fp32")
+    want = _per_slot(ik, c, slots, "fp32")
+    _same(got, want)
+    # and the batch result of the resized slot against the FP64 oracle
+    box = oracle.make_box(2, [L, L, 1.0])
+    p = oracle.make_poly12(1.0, 0.2, 1.25)
+    cgo = oracle.make_cg(cg2["kind"], rcut=cg2["rcut"], mode="fixedpoint", order=cg2["order"], width=cg2["width"])
+    sub = grid[::7]
+    ov, ok = oracle.compute(box, big.pos, big.diam, p, cgo, sub, vel=big.vel, mass=big.mass,
+                            max_rc=c.get_max_rcut())
+    gv, gk = got[slots.index(1)]
+    assert np.all(rel_l2(uniq(gv[::7]), uniq(ov)) <= FP32_TOL)
+    assert np.all(rel_l2(uniq(gk[::7]), uniq(ok)) <= FP32_TOL)
+    c.close()
+
+
+def test_batch_argument_errors():
+    from pyglasstools_gb300 import ikabi as ik, synth
+    fr = _frames(500, [7])
+    L = fr[0].L
+    c = _context(ik, L, synth.lattice_grid(L, 8, 2), 2)
+    _upload(c, fr)
+    with pytest.raises(ik.IKError):
+        c.compute_batch([0, 5], "fp32")
+    with pytest.raises(ik.IKError):
+        c.compute_batch([], "fp32")
+    c.compute_batch([0], "fp32")
+    c.synchronize()
+    c.close()
