@@ -192,6 +192,43 @@ int ik_get_launch_count(ik_ctx* ctx, int64_t* out);
  * [1] accepted (grid, particle) pairs, [2] active (grid, i, j) triples (FP32 path). */
 int ik_get_counters(ik_ctx* ctx, int slot, int64_t* out3);
 
+/* ---- learned bond-integral surrogate -------------------------------------------
+ * No reference counterpart: a small network (4 -> 64 -> 64 -> 64 -> 1, SiLU) that
+ * stands in for the quadrature of the bond integral (cgfunc/CoarseGrainFunction.h:85-88
+ * fixed point, :124-127 adaptive) of a Gaussian kernel truncated at 3 widths, on the
+ * bonds that cross the kernel's support.  Units of the width w throughout:
+ *   B(d, a, b) = int_0^1 exp(-(d^2 + (a + s (b - a))^2) / 2) [inside r < 3] ds,
+ * d = distance of the grid point from the bond's line, a / b = signed positions of the
+ * inside / outside end along it (b > 0).  Inputs x = (sqrt(1 - (d/3)^2), a/4, b/4,
+ * 2 (w - 1.5)); output y = B exp(d^2/2).  Trained on the GPU in FP32 (own forward,
+ * backward and Adam kernels) on labels from adaptive quadrature; deployed in BF16 on
+ * the tensor cores (tcgen05, FP32 accumulation).  A per-bin table from validation
+ * decides where the network replaces the fixed-point rule (max error <= tol).
+ * Parameters: W1[64][4], b1[64], W2[64][64], b2[64], W3[64][64], b3[64], w4[64], b4. */
+typedef struct ik_mlp ik_mlp;
+int ik_mlp_create(ik_mlp** out, int device);
+int ik_mlp_destroy(ik_mlp* m);
+int ik_mlp_num_params(void);                                       /* 8705 */
+int ik_mlp_init(ik_mlp* m, uint64_t seed);                          /* fan-in uniform weights */
+int ik_mlp_set_params(ik_mlp* m, const float* params, int64_t n);
+int ik_mlp_get_params(ik_mlp* m, float* params, int64_t n);
+/* n seeded samples of the crossing-bond domain: feats n x {d, a, b, w}, labels B (FP64) */
+int ik_mlp_samples(ik_mlp* m, int64_t n, uint64_t seed, float* feats, double* labels);
+/* gradient of the mean squared error of y over a batch (n a power of two) */
+int ik_mlp_grad(ik_mlp* m, int64_t n, const float* feats, const float* targets, float* grad, double* loss);
+/* Adam on nsamples (power of two) generated samples; loss_hist gets the per-step loss */
+int ik_mlp_train(ik_mlp* m, int64_t nsamples, int epochs, int ctas, double lr, uint64_t seed,
+                 double* loss_hist, int64_t hist_len);
+/* B of n feature rows; kernel 0 = tensor cores (BF16), 1 = CUDA cores BF16, 2 = FP32 */
+int ik_mlp_eval(ik_mlp* m, int64_t n, const float* feats, float* out, int kernel);
+/* error of the deployed network on n fresh samples; builds the per-bin use table:
+ * bins of (w, d, a, b) with >= 8 samples and max |B_net - B_label| <= tol */
+int ik_mlp_validate(ik_mlp* m, int64_t n, uint64_t seed, double tol, double* coverage, double* max_err,
+                    double* rms_err, double* bin_err, int64_t nbins);
+/* Attach a validated surrogate to a context; used by ik_set_cgfunc(.., IK_QUAD_MLP, ..)
+ * on the FP32 path.  The caller keeps the surrogate alive while attached. */
+int ik_set_mlp(ik_ctx* ctx, ik_mlp* m);
+
 #ifdef __cplusplus
 }
 #endif

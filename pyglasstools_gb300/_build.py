@@ -14,7 +14,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libik_gb300.so")
-CU_SOURCES = ["ik_api.cu", "ik_cells.cu", "ik_gather32.cu", "ik_gather64.cu", "ik_noalloc.cu", "ik_bonds.cu"]
+CU_SOURCES = ["ik_api.cu", "ik_cells.cu", "ik_gather32.cu", "ik_gather64.cu", "ik_noalloc.cu", "ik_bonds.cu",
+              "ik_mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -140,6 +140,7 @@ struct ik_ctx {
     DevBuf q_cell_of, q_rank, q_count, q_start, q_sorted, q_cnt, q_offs, q_idx, q_flag;
     std::vector<Slot> slots;
     std::vector<PendingOp> pending;
+    ik_mlp* mlp = nullptr; // learned bond-integral surrogate (IK_QUAD_MLP)
     // CUDA-graph replay of ik_compute_batch
     bool capturing = false;
     int captured_lanes = 0;
@@ -561,6 +562,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
 
 // Lets entry points defined in other translation units report through ik_last_error().
 void ik_internal_set_error(const char* msg) { g_err = msg; }
+void ik_gl_rule(int n, double* x, double* w) { gl_rule(n, x, w); }
 
 // ===========================================================================
 extern "C" {
@@ -1152,6 +1154,14 @@ int ik_eval_bond(ik_ctx* c, int64_t m, const double* x, const double* ri, const 
     CK(cudaMemcpyAsync(bond, d + 9 * m, sizeof(double) * m, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(delta, d + 10 * m, sizeof(double) * m, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    return IK_OK;
+}
+
+int ik_set_mlp(ik_ctx* c, ik_mlp* m)
+{
+    if (int r = check_ctx(c)) return r;
+    ++c->config_version; // captured batch graphs hold the old settings
+    c->mlp = m;
     return IK_OK;
 }
 

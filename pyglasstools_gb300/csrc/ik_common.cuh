@@ -13,6 +13,8 @@
 #define IK_ST_HALO_OVERFLOW 2
 #define IK_ST_BAD_INPUT     4
 #define IK_ST_NEIGH_OVERFLOW 8
+#define IK_ST_MMA_TIMEOUT   16  /* a tensor-core completion wait gave up */
+#define IK_ST_MLP_OVERFLOW  32  /* the surrogate record buffer overflowed */
 
 // Box + cell grid.  Cells tile [lo, lo+L) per axis; nc[c] = 1 on non-periodic axes.
 struct IkGeom {

@@ -108,5 +108,15 @@ cudaError_t launch_eval_bond(const IkCG& cg, int dim, const double* xs, const do
 #define IK_FMA_PROBE_CHAINS 8
 cudaError_t launch_fma_probe(int blocks, int threads, int iters, float* out);
 
-// ---- error text shared by the C-ABI translation units (ik_api.cu) ------------
+// ---- learned bond-integral surrogate (ik_mlp.cu) ----------------------------
+struct ik_mlp;
+const unsigned char* ik_mlp_internal_blob(ik_mlp* m);   // deployed BF16 weights (null if none)
+const unsigned char* ik_mlp_internal_table(ik_mlp* m);  // per-bin use table (null if not validated)
+// records {M, mb, hh, B_fixed} + {grid index, bond index} -> fixed-point corrections (2^-32)
+cudaError_t launch_mlp_records(ik_mlp* m, const float4* rec, const int2* rid, const unsigned long long* count,
+                               long long capacity, const float4* bonds, float to_w, float w, int nc,
+                               unsigned long long* corr, int* status, int blocks, cudaStream_t st);
+
+// ---- shared host helpers (ik_api.cu) -----------------------------------------
 void ik_internal_set_error(const char* msg);
+void ik_gl_rule(int n, double* x, double* w);  // n-point Gauss-Legendre on [-1, 1]

@@ -39,6 +39,7 @@ def lib():
             raise ImportError(f"{LIB_PATH} is not built (python -m pyglasstools_gb300._build)")
         L = C.CDLL(LIB_PATH)
         vp, dp, i64, i32 = C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.c_int
+        fp = C.POINTER(C.c_float)
         sig = {
             "ik_last_error": ([], C.c_char_p),
             "ik_version": ([], i32),
@@ -73,6 +74,18 @@ def lib():
             "ik_get_launch_count": ([vp, C.POINTER(C.c_int64)], i32),
             "ik_wait_all": ([vp], i32),
             "ik_compute_batch": ([vp, C.POINTER(C.c_int), i32, i32, i32], i32),
+            "ik_set_mlp": ([vp, vp], i32),
+            "ik_mlp_create": ([C.POINTER(vp), i32], i32),
+            "ik_mlp_destroy": ([vp], i32),
+            "ik_mlp_num_params": ([], i32),
+            "ik_mlp_init": ([vp, C.c_uint64], i32),
+            "ik_mlp_set_params": ([vp, fp, i64], i32),
+            "ik_mlp_get_params": ([vp, fp, i64], i32),
+            "ik_mlp_samples": ([vp, i64, C.c_uint64, fp, dp], i32),
+            "ik_mlp_grad": ([vp, i64, fp, fp, fp, dp], i32),
+            "ik_mlp_train": ([vp, i64, i32, i32, C.c_double, C.c_uint64, dp, i64], i32),
+            "ik_mlp_eval": ([vp, i64, fp, fp, i32], i32),
+            "ik_mlp_validate": ([vp, i64, C.c_uint64, C.c_double, dp, dp, dp, dp, i64], i32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -84,6 +97,10 @@ def lib():
 
 def _dp(a):
     return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _fp(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
 
 
 def _c64(a, shape=None):
@@ -172,6 +189,11 @@ class IKContext:
 
     def compute_slot(self, slot, precision="fp32", fields=FIELD_VIRIAL | FIELD_KINETIC):
         check(lib().ik_compute_slot(self._h, slot, PREC[precision], fields))
+
+    def set_mlp(self, mlp):
+        """Attach a validated surrogate (MLP) used by cgfunc mode "mlp" on the FP32 path."""
+        check(lib().ik_set_mlp(self._h, None if mlp is None else mlp._h))
+        self._mlp = mlp
 
     def compute_batch(self, slots, precision="fp32", fields=FIELD_VIRIAL | FIELD_KINETIC):
         """Compute several slots as one batch (replayed as a CUDA graph after the first call)."""
@@ -265,3 +287,80 @@ def measure_fp32_peak(device=0):
     v = C.c_double()
     check(lib().ik_measure_fp32_peak(device, C.byref(v)))
     return v.value
+
+
+MLP_BINS = 2 * 12 * 24 * 16   # (w, d, a, b) bins of the surrogate's use table
+
+
+class MLP:
+    """Learned bond-integral surrogate (ik_mlp_* in include/ik_gb300.h)."""
+
+    def __init__(self, device=0):
+        self._h = C.c_void_p()
+        check(lib().ik_mlp_create(C.byref(self._h), device))
+        self.nparams = lib().ik_mlp_num_params()
+
+    def close(self):
+        if self._h:
+            lib().ik_mlp_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init(self, seed=0):
+        check(lib().ik_mlp_init(self._h, seed))
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        check(lib().ik_mlp_set_params(self._h, _fp(p), p.size))
+
+    def get_params(self):
+        p = np.empty(self.nparams, dtype=np.float32)
+        check(lib().ik_mlp_get_params(self._h, _fp(p), p.size))
+        return p
+
+    def samples(self, n, seed=0):
+        """n seeded samples {d, a, b, w} (float32) and their labels B (float64)."""
+        f = np.empty((n, 4), dtype=np.float32)
+        lab = np.empty(n, dtype=np.float64)
+        check(lib().ik_mlp_samples(self._h, n, seed, _fp(f), _dp(lab)))
+        return f, lab
+
+    def grad(self, feats, targets):
+        f = np.ascontiguousarray(feats, dtype=np.float32)
+        y = np.ascontiguousarray(targets, dtype=np.float32)
+        g = np.empty(self.nparams, dtype=np.float32)
+        loss = C.c_double()
+        check(lib().ik_mlp_grad(self._h, len(f), _fp(f), _fp(y), _fp(g), C.byref(loss)))
+        return g, loss.value
+
+    def train(self, nsamples=1 << 22, epochs=10, ctas=152, lr=2e-3, seed=1):
+        batch = ctas * 128
+        steps = ((nsamples + batch - 1) // batch) * epochs
+        hist = np.zeros(steps, dtype=np.float64)
+        check(lib().ik_mlp_train(self._h, nsamples, epochs, ctas, lr, seed, _dp(hist), steps))
+        return hist
+
+    def eval(self, feats, kernel=0):
+        """kernel 0: tensor cores (BF16); 1: CUDA cores, BF16 arithmetic; 2: CUDA cores, FP32."""
+        f = np.ascontiguousarray(feats, dtype=np.float32)
+        out = np.empty(len(f), dtype=np.float32)
+        check(lib().ik_mlp_eval(self._h, len(f), _fp(f), _fp(out), kernel))
+        return out
+
+    def validate(self, n=1 << 20, seed=7, tol=1e-6):
+        cov, mx, rms = C.c_double(), C.c_double(), C.c_double()
+        bins = np.zeros(MLP_BINS, dtype=np.float64)
+        check(lib().ik_mlp_validate(self._h, n, seed, tol, C.byref(cov), C.byref(mx), C.byref(rms), _dp(bins),
+                                    MLP_BINS))
+        return {"coverage": cov.value, "max_err": mx.value, "rms_err": rms.value, "bin_max_err": bins}

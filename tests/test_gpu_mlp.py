@@ -1,0 +1,102 @@
+"""GPU tests of the learned bond-integral surrogate (ik_mlp_* in include/ik_gb300.h):
+labels from the GPU's adaptive quadrature against the closed form of the oracle,
+the FP32 training gradient against the oracle's FP64 reverse-mode gradient, the
+tensor-core (tcgen05, BF16) inference against the CUDA-core BF16 and FP32 networks
+and the oracle's BF16 emulation, and training + validation end to end.
+
+Tolerances: labels 1e-12 absolute; gradient relative L2 <= 1e-4 per parameter block
+(FP32 accumulation over the batch); tensor-core vs CUDA-core BF16 outputs within 4e-3
+of the output scale (the same BF16 roundings, FP32 sums in another order).
+"""
+import numpy as np
+import pytest
+
+from oracle import mlp as M
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ik():
+    from pyglasstools_gb300 import ikabi
+    return ikabi
+
+
+def test_labels_match_closed_form_and_domain(ik):
+    with ik.MLP() as m:
+        f, lab = m.samples(4096, seed=11)
+    d, a, b, w = (f[:, k].astype(np.float64) for k in range(4))
+    tc = np.sqrt(9 - d * d)
+    assert np.all((d >= 0) & (d < 3))
+    assert np.all((a > -tc - 1e-5) & (a < tc + 1e-5))   # inside end
+    assert np.all((b >= tc - 1e-5) & (b <= 4 + 1e-5))   # outside end, b > 0
+    assert np.all(b - a <= 2.5 + 1e-5)
+    assert set(np.unique(w)) == {1.0, 2.0}
+    # labels were computed from the FP64 sample before rounding to float32: compare
+    # against the closed form at the float32 features with the matching tolerance
+    want = M.label(d, a, b)
+    assert np.max(np.abs(lab - want)) < 2e-6
+    # and exactly, regenerating the FP64 draw is not possible from float32 features:
+    # the mean error stays at the rounding of the features
+    assert np.mean(np.abs(lab - want)) < 2e-7
+
+
+def test_gradient_matches_oracle(ik):
+    with ik.MLP() as m:
+        m.init(seed=3)
+        p = m.get_params()
+        f, lab = m.samples(512, seed=12)
+        d = f[:, 0].astype(np.float64)
+        y = (lab * np.exp(0.5 * d * d)).astype(np.float32)
+        g, loss = m.grad(f, y)
+    want_loss, want = M.loss_and_grad(p.astype(np.float64), f, y)
+    assert loss == pytest.approx(want_loss, rel=1e-4)
+    for lo, hi in [(M.O_W1, M.O_B1), (M.O_B1, M.O_W2), (M.O_W2, M.O_B2), (M.O_B2, M.O_W3),
+                   (M.O_W3, M.O_B3), (M.O_B3, M.O_W4), (M.O_W4, M.O_B4), (M.O_B4, M.NPAR)]:
+        err = np.linalg.norm(g[lo:hi] - want[lo:hi]) / max(np.linalg.norm(want[lo:hi]), 1e-30)
+        assert err <= 1e-4, (lo, err)
+
+
+def test_tensor_core_inference_matches_cuda_cores(ik):
+    with ik.MLP() as m:
+        m.init(seed=4)
+        p = m.get_params()
+        f, _ = m.samples(1000, seed=13)  # 1000: a ragged last tile
+        tc = m.eval(f, kernel=0)
+        simt16 = m.eval(f, kernel=1)
+        fp32 = m.eval(f, kernel=2)
+    scale = np.max(np.abs(fp32))
+    assert np.all(np.isfinite(tc))
+    assert np.max(np.abs(tc - simt16)) <= 4e-3 * scale
+    assert np.max(np.abs(tc - M.forward_bf16(p, f))) <= 4e-3 * scale
+    d = f[:, 0].astype(np.float64)
+    assert np.max(np.abs(fp32 - M.forward(p, f) * np.exp(-0.5 * d * d))) <= 1e-5 * scale
+    # BF16 against FP32: the quantisation error, not a layout error
+    assert np.max(np.abs(tc - fp32)) <= 0.05 * scale
+
+
+def test_training_fits_and_validation_builds_table(ik):
+    with ik.MLP() as m:
+        hist = m.train(nsamples=1 << 18, epochs=6, ctas=64, lr=3e-3, seed=21)
+        assert np.all(np.isfinite(hist))
+        assert hist[-20:].mean() < hist[:20].mean() / 50
+        v_tight = m.validate(n=1 << 16, seed=77, tol=1e-6)
+        v_loose = m.validate(n=1 << 16, seed=77, tol=3e-2)
+        f, lab = m.samples(2048, seed=78)
+        b = m.eval(f, kernel=0)
+    assert v_tight["rms_err"] < 2e-2 and v_tight["max_err"] < 0.2
+    assert 0.0 <= v_tight["coverage"] <= v_loose["coverage"] <= 1.0
+    assert v_loose["coverage"] > 0.3
+    assert np.sqrt(np.mean((b - lab) ** 2)) < 2e-2
+    seen = v_loose["bin_max_err"][v_loose["bin_max_err"] >= 0]
+    assert len(seen) > 100
+
+
+def test_errors_are_reported(ik):
+    with ik.MLP() as m:
+        with pytest.raises(ik.IKError):
+            m.eval(np.zeros((4, 4), np.float32))          # no parameters yet
+        with pytest.raises(ik.IKError):
+            m.train(nsamples=1000)                         # not a power of two
+        with pytest.raises(ik.IKError):
+            m.set_params(np.zeros(10, np.float32))         # wrong size
