@@ -200,7 +200,9 @@ int ik_get_counters(ik_ctx* ctx, int slot, int64_t* out3);
  *   B(d, a, b) = int_0^1 exp(-(d^2 + (a + s (b - a))^2) / 2) [inside r < 3] ds,
  * d = distance of the grid point from the bond's line, a / b = signed positions of the
  * inside / outside end along it (b > 0).  Inputs x = (sqrt(1 - (d/3)^2), a/4, b/4,
- * 2 (w - 1.5)); output y = B exp(d^2/2).  Trained on the GPU in FP32 (own forward,
+ * 2 (w - 1.5)); output y with B = base (1 + y), base = the midpoint rule on the part of
+ * the bond inside the support (s1 exp(-(d^2 + m^2)/2), s1 = (t_c - a)/(b - a),
+ * m = (a + t_c)/2, t_c = sqrt(9 - d^2)).  Trained on the GPU in FP32 (own forward,
  * backward and Adam kernels) on labels from adaptive quadrature; deployed in BF16 on
  * the tensor cores (tcgen05, FP32 accumulation).  A per-bin table from validation
  * decides where the network replaces the fixed-point rule (max error <= tol).

@@ -11,8 +11,12 @@
 //   B(d, a, b) = int_0^1 K(d^2 + (a + s (b - a))^2) ds
 // with d the distance from the grid point to the bond's line, a and b the signed
 // positions of r_i (inside the support) and r_j (outside) along it, reflected so
-// that b > 0.  The network reads x = (sqrt(1 - (d/3)^2), a/4, b/4, 2 (w - 1.5)) and
-// predicts y = B exp(d^2 / 2) in [0, 1].
+// that b > 0.  The clipped part of the segment is known in closed form: it ends where
+// the line leaves the ball, at t_c = sqrt(9 - d^2), a fraction s1 = (t_c - a)/(b - a)
+// of the bond.  The midpoint rule on it, base = s1 exp(-(d^2 + m^2)/2) with
+// m = (a + t_c)/2, is the first approximation; the network predicts the relative
+// correction y = B / base - 1 from x = (t_c / 3, a/4, b/4, 2 (w - 1.5)), so that
+// B = base (1 + y).
 //
 // Kernels:
 //   k_mlp_samples   seeded samples of the crossing-bond domain and their labels by
@@ -24,8 +28,11 @@
 //   k_mlp_deploy    FP32 parameters -> BF16 operand tiles in the tensor-core layout;
 //   k_mlp_infer_tc  inference on the 5th-generation tensor cores: per 128-row tile,
 //                   tcgen05.mma (kind::f16, BF16 in, FP32 accumulators in TMEM) for the
-//                   three hidden layers, tcgen05.ld epilogues (bias + SiLU + BF16) that
-//                   write the next layer's operand back to shared memory;
+//                   three hidden layers, tcgen05.ld epilogues (bias + SiLU) that write the
+//                   next layer's operand back to shared memory.  Activations travel as
+//                   BF16 hi + lo pairs (K = 128 against the weight tile used twice) and
+//                   the first layer is split three ways (x_hi W_hi + x_lo W_hi + x_hi W_lo),
+//                   so BF16 rounding of the weights is the remaining quantisation;
 //   k_mlp_infer_simt the same BF16 arithmetic on the CUDA cores (cross-check), or FP32.
 #include "ik_kernels.h"
 #include "../../include/ik_gb300.h"
@@ -62,10 +69,20 @@ __host__ __device__ inline void mlp_inputs(float d, float a, float b, float w, f
 {
     const float dd = d * (1.0f / 3.0f);
     const float t = 1.0f - dd * dd;
-    x[0] = t > 0.0f ? sqrtf(t) : 0.0f;
+    x[0] = t > 0.0f ? sqrtf(t) : 0.0f; // t_c / 3
     x[1] = 0.25f * a;
     x[2] = 0.25f * b;
     x[3] = 2.0f * (w - 1.5f);
+}
+
+// midpoint-rule baseline of the clipped segment (see the header comment)
+__host__ __device__ inline float mlp_base(float d, float a, float b)
+{
+    const float tc = sqrtf(fmaxf(9.0f - d * d, 0.0f));
+    const float l = b - a;
+    const float s1 = l > 0.0f ? fminf(fmaxf((tc - a) / l, 0.0f), 1.0f) : 0.0f;
+    const float m = 0.5f * (a + tc);
+    return s1 * expf(-0.5f * (d * d + m * m));
 }
 
 __device__ __forceinline__ float silu_exact(float z) { return z / (1.0f + expf(-z)); }
@@ -172,9 +189,13 @@ __global__ void k_mlp_samples(long long n, unsigned long long seed, MlpGL q, flo
     const double B = mlp_label(q, d, a, b);
     feats[i] = make_float4((float)d, (float)a, (float)b, (float)w);
     labels[i] = B;
-    // target y = B exp(d^2/2), from the FP32 features (what the network sees)
-    const double df = (double)(float)d;
-    targets[i] = (float)(B * exp(0.5 * df * df));
+    // target y = B / base - 1, the baseline from the FP32 features (what the network sees)
+    const double df = (float)d, af = (float)a, bf = (float)b;
+    const double tcf = sqrt(fmax(9.0 - df * df, 0.0));
+    const double s1 = fmin(fmax((tcf - af) / (bf - af), 0.0), 1.0);
+    const double mf = 0.5 * (af + tcf);
+    const double base = s1 * exp(-0.5 * (df * df + mf * mf));
+    targets[i] = base > 1e-30 ? (float)(B / base - 1.0) : 0.0f;
 }
 
 // ---------------------------------------------------------------------------- training
@@ -429,9 +450,11 @@ __host__ __device__ inline int op_off(int r, int k, int K)
 __global__ void k_mlp_deploy(const float* P, unsigned char* blob)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < 64 * 16) { // W1 padded to K = 16
-        const int n = i / 16, k = i % 16;
-        const float v = k < 4 ? P[O_W1 + n * 4 + k] : 0.f;
+    if (i < 64 * 16) { // W1 as [hi | hi | lo | 0] against inputs [x_hi | x_lo | x_hi | 0]
+        const int n = i / 16, k = i % 16, j = k & 3;
+        const float w = P[O_W1 + n * 4 + j];
+        const float hi = bf16r(w);
+        const float v = k < 8 ? hi : (k < 12 ? w - hi : 0.f);
         *reinterpret_cast<__nv_bfloat16*>(blob + DB_W1 + op_off(n, k, 16)) = __float2bfloat16_rn(v);
     }
     if (i < 64 * 64) {
@@ -451,8 +474,9 @@ __global__ void k_mlp_deploy(const float* P, unsigned char* blob)
 
 // ---------------------------------------------------------------------------- SIMT inference
 // mode 0: FP32 weights and activations, exact SiLU (the training network);
-// mode 1: BF16 weights and activations, FP32 accumulation, the deployed SiLU (the
-//         arithmetic of the tensor-core kernel, for cross-checks).
+// mode 1: the arithmetic of the tensor-core kernel (BF16 weights, activations as BF16
+//         hi + lo pairs, first layer split three ways, FP32 accumulation, the deployed
+//         SiLU), for cross-checks.
 __global__ void k_mlp_infer_simt(const float* P, const float4* feats, long long n, int mode, float* out)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -464,11 +488,23 @@ __global__ void k_mlp_infer_simt(const float* P, const float4* feats, long long 
     float x[4];
     mlp_inputs(f.x, f.y, f.z, f.w, x);
     float h[64], g[64];
-    for (int k = 0; k < 4; ++k) x[k] = R(x[k]);
+    // BF16 split of the first layer (x_hi W_hi + x_lo W_hi + x_hi W_lo) and of the
+    // activations (hi + lo), BF16 weights elsewhere
+    auto P2 = [&](float v) { return q ? bf16r(v) + bf16r(v - bf16r(v)) : v; };
     for (int nn = 0; nn < 64; ++nn) {
         float z = 0.f;
-        for (int k = 0; k < 4; ++k) z = fmaf(R(P[O_W1 + nn * 4 + k]), x[k], z);
-        h[nn] = R(S(z + P[O_B1 + nn]));
+        for (int k = 0; k < 4; ++k) {
+            const float w = P[O_W1 + nn * 4 + k];
+            if (q) {
+                const float xh = bf16r(x[k]), xl = bf16r(x[k] - xh), wh = bf16r(w), wl = bf16r(w - wh);
+                z = fmaf(wh, xh, z);
+                z = fmaf(wh, xl, z);
+                z = fmaf(wl, xh, z);
+            } else {
+                z = fmaf(w, x[k], z);
+            }
+        }
+        h[nn] = P2(S(z + P[O_B1 + nn]));
     }
     for (int layer = 0; layer < 2; ++layer) {
         const int ow = layer == 0 ? O_W2 : O_W3, ob = layer == 0 ? O_B2 : O_B3;
@@ -477,12 +513,12 @@ __global__ void k_mlp_infer_simt(const float* P, const float4* feats, long long 
             for (int k = 0; k < 64; ++k) z = fmaf(R(P[ow + nn * 64 + k]), h[k], z);
             g[nn] = z + P[ob + nn];
         }
-        for (int nn = 0; nn < 64; ++nn) h[nn] = R(S(g[nn]));
+        for (int nn = 0; nn < 64; ++nn) h[nn] = layer == 0 ? P2(S(g[nn])) : S(g[nn]);
     }
     float y = 0.f;
     for (int k = 0; k < 64; ++k) y = fmaf(R(P[O_W4 + k]), h[k], y);
     y += P[O_B4];
-    out[i] = y * expf(-0.5f * f.x * f.x);
+    out[i] = mlp_base(f.x, f.y, f.z) * (1.0f + y);
 }
 
 // ---------------------------------------------------------------------------- tcgen05 helpers
@@ -577,8 +613,8 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi)
 // ---------------------------------------------------------------------------- tcgen05 inference
 // Shared memory layout of k_mlp_infer_tc (bytes, 1024-aligned pieces):
 constexpr int TC_A0 = 0;                    // 128 x 16 bf16 input operand   4096
-constexpr int TC_H = TC_A0 + 128 * 16 * 2;  // 128 x 64 bf16 hidden operand  16384
-constexpr int TC_W = TC_H + 128 * 64 * 2;   // deployed blob (W1, W2, W3, floats)
+constexpr int TC_H = TC_A0 + 128 * 16 * 2;  // 128 x 128 bf16 hidden operand [hi | lo]  32768
+constexpr int TC_W = TC_H + 128 * 128 * 2;  // deployed blob (W1, W2, W3, floats)
 constexpr int TC_BAR = TC_W + ((DB_BYTES + 1023) / 1024) * 1024;
 constexpr int TC_SMEM = TC_BAR + 64;
 // At least this much dynamic shared memory per CTA keeps at most 4 CTAs on an SM, so
@@ -686,10 +722,16 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
             }
         }
         {
-            float x[4];
+            // inputs as [x_hi | x_lo | x_hi | 0] against W1 as [hi | hi | lo | 0]
+            float x[4], xl[4];
             mlp_inputs(fd, fa, fb, fw, x);
-            uint4 c0 = make_uint4(pack_bf16x2(x[0], x[1]), pack_bf16x2(x[2], x[3]), 0u, 0u);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) { const float hi = bf16r(x[k]); xl[k] = x[k] - hi; x[k] = hi; }
+            const uint4 c0 = make_uint4(pack_bf16x2(x[0], x[1]), pack_bf16x2(x[2], x[3]),
+                                        pack_bf16x2(xl[0], xl[1]), pack_bf16x2(xl[2], xl[3]));
+            const uint4 c1 = make_uint4(pack_bf16x2(x[0], x[1]), pack_bf16x2(x[2], x[3]), 0u, 0u);
             *reinterpret_cast<uint4*>(sA0 + op_off(t, 0, 16)) = c0;
+            *reinterpret_cast<uint4*>(sA0 + op_off(t, 8, 16)) = c1;
         }
         fence_async_smem();
         fence_before();
@@ -702,11 +744,12 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
                 if (layer == 0) {
                     umma_bf16(tmem, umma_desc(aA0, 128, 256), umma_desc(aW1, 128, 256), ID, 0u);
                 } else {
+                    // [h_hi | h_lo] (K = 128) against [W | W]: the same W tile twice
                     const uint32_t aw = layer == 1 ? aW2 : aW3;
 #pragma unroll
-                    for (int kk = 0; kk < 4; ++kk)
-                        umma_bf16(tmem, umma_desc(aH + kk * 256, 128, 1024), umma_desc(aw + kk * 256, 128, 1024), ID,
-                                  kk > 0 ? 1u : 0u);
+                    for (int kk = 0; kk < 8; ++kk)
+                        umma_bf16(tmem, umma_desc(aH + kk * 256, 128, 2048),
+                                  umma_desc(aw + (kk & 3) * 256, 128, 1024), ID, kk > 0 ? 1u : 0u);
                 }
                 umma_commit(aBar);
             }
@@ -723,15 +766,24 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
                 for (int c16 = 0; c16 < 4; ++c16) {
                     float v[16];
                     tmem_ld16(tl + 16 * c16, v);
+                    float vl[16];
 #pragma unroll
-                    for (int k = 0; k < 16; ++k) v[k] = silu_fast(v[k] + bias[16 * c16 + k]);
+                    for (int k = 0; k < 16; ++k) {
+                        const float a = silu_fast(v[k] + bias[16 * c16 + k]);
+                        v[k] = bf16r(a);
+                        vl[k] = a - v[k];
+                    }
 #pragma unroll
                     for (int h8 = 0; h8 < 2; ++h8) {
                         const int k0 = 16 * c16 + 8 * h8;
-                        uint4 pk = make_uint4(pack_bf16x2(v[8 * h8], v[8 * h8 + 1]), pack_bf16x2(v[8 * h8 + 2], v[8 * h8 + 3]),
-                                              pack_bf16x2(v[8 * h8 + 4], v[8 * h8 + 5]),
-                                              pack_bf16x2(v[8 * h8 + 6], v[8 * h8 + 7]));
-                        *reinterpret_cast<uint4*>(sH + op_off(t, k0, 64)) = pk;
+                        const float* u = v + 8 * h8;
+                        const float* ul = vl + 8 * h8;
+                        const uint4 ph = make_uint4(pack_bf16x2(u[0], u[1]), pack_bf16x2(u[2], u[3]),
+                                                    pack_bf16x2(u[4], u[5]), pack_bf16x2(u[6], u[7]));
+                        const uint4 pl = make_uint4(pack_bf16x2(ul[0], ul[1]), pack_bf16x2(ul[2], ul[3]),
+                                                    pack_bf16x2(ul[4], ul[5]), pack_bf16x2(ul[6], ul[7]));
+                        *reinterpret_cast<uint4*>(sH + op_off(t, k0, 128)) = ph;
+                        *reinterpret_cast<uint4*>(sH + op_off(t, 64 + k0, 128)) = pl;
                     }
                 }
                 fence_async_smem();
@@ -739,18 +791,17 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
                 __syncthreads();
                 if (*abort_flag) break;
             } else {
-                // output layer on the CUDA cores: y = w4 . bf16(silu(z3 + b3)) + b4
+                // output layer on the CUDA cores: y = w4 . silu(z3 + b3) + b4 (w4 in BF16)
                 float y = F[256];
 #pragma unroll
                 for (int c16 = 0; c16 < 4; ++c16) {
                     float v[16];
                     tmem_ld16(tl + 16 * c16, v);
 #pragma unroll
-                    for (int k = 0; k < 16; ++k)
-                        y = fmaf(F[192 + 16 * c16 + k], bf16r(silu_fast(v[k] + bias[16 * c16 + k])), y);
+                    for (int k = 0; k < 16; ++k) y = fmaf(F[192 + 16 * c16 + k], silu_fast(v[k] + bias[16 * c16 + k]), y);
                 }
                 fence_before();
-                const float Bs = y * __expf(-0.5f * fd * fd);
+                const float Bs = mlp_base(fd, fa, fb) * (1.0f + y);
                 if (MODE == 0) {
                     if (valid) out[row] = Bs;
                 } else if (valid) {

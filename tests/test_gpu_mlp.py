@@ -5,7 +5,7 @@ tensor-core (tcgen05, BF16) inference against the CUDA-core BF16 and FP32 networ
 and the oracle's BF16 emulation, and training + validation end to end.
 
 Tolerances: labels 1e-12 absolute; gradient relative L2 <= 1e-4 per parameter block
-(FP32 accumulation over the batch); tensor-core vs CUDA-core BF16 outputs within 4e-3
+(FP32 accumulation over the batch); tensor-core vs CUDA-core BF16 outputs within 1e-4
 of the output scale (the same BF16 roundings, FP32 sums in another order).
 """
 import numpy as np
@@ -46,8 +46,7 @@ def test_gradient_matches_oracle(ik):
         m.init(seed=3)
         p = m.get_params()
         f, lab = m.samples(512, seed=12)
-        d = f[:, 0].astype(np.float64)
-        y = (lab * np.exp(0.5 * d * d)).astype(np.float32)
+        y = M.targets(f, lab).astype(np.float32)
         g, loss = m.grad(f, y)
     want_loss, want = M.loss_and_grad(p.astype(np.float64), f, y)
     assert loss == pytest.approx(want_loss, rel=1e-4)
@@ -67,29 +66,42 @@ def test_tensor_core_inference_matches_cuda_cores(ik):
         fp32 = m.eval(f, kernel=2)
     scale = np.max(np.abs(fp32))
     assert np.all(np.isfinite(tc))
-    assert np.max(np.abs(tc - simt16)) <= 4e-3 * scale
-    assert np.max(np.abs(tc - M.forward_bf16(p, f))) <= 4e-3 * scale
-    d = f[:, 0].astype(np.float64)
-    assert np.max(np.abs(fp32 - M.forward(p, f) * np.exp(-0.5 * d * d))) <= 1e-5 * scale
-    # BF16 against FP32: the quantisation error, not a layout error
-    assert np.max(np.abs(tc - fp32)) <= 0.05 * scale
+    assert np.max(np.abs(tc - simt16)) <= 1e-4 * scale
+    assert np.max(np.abs(tc - M.forward_bf16(p, f))) <= 1e-4 * scale
+    assert np.max(np.abs(fp32 - M.base(f) * (1.0 + M.forward(p, f)))) <= 1e-5 * scale
+    # BF16 weights against FP32: the quantisation error, not a layout error
+    assert np.max(np.abs(tc - fp32)) <= 0.02 * scale
 
 
-def test_training_fits_and_validation_builds_table(ik):
+def _gl_bond(f, n=5):
+    """The fixed-point rule of the reference (n-point Gauss-Legendre on [0, 1]) in units of w."""
+    gx, gw = np.polynomial.legendre.leggauss(n)
+    d, a, b = (f[:, k].astype(np.float64) for k in range(3))
+    s = 0.5 + 0.5 * gx[None, :]
+    t = a[:, None] + s * (b - a)[:, None]
+    r2 = d[:, None] ** 2 + t * t
+    return 0.5 * np.sum(gw[None, :] * np.where(r2 < 9.0, np.exp(-0.5 * r2), 0.0), axis=1)
+
+
+def test_training_fits_and_beats_fixed_point_rule(ik):
     with ik.MLP() as m:
-        hist = m.train(nsamples=1 << 18, epochs=6, ctas=64, lr=3e-3, seed=21)
+        hist = m.train(nsamples=1 << 20, epochs=120, ctas=152, lr=3e-3, seed=21)
         assert np.all(np.isfinite(hist))
-        assert hist[-20:].mean() < hist[:20].mean() / 50
-        v_tight = m.validate(n=1 << 16, seed=77, tol=1e-6)
-        v_loose = m.validate(n=1 << 16, seed=77, tol=3e-2)
-        f, lab = m.samples(2048, seed=78)
-        b = m.eval(f, kernel=0)
-    assert v_tight["rms_err"] < 2e-2 and v_tight["max_err"] < 0.2
+        assert hist[-50:].mean() < hist[:20].mean() / 100
+        v_tight = m.validate(n=1 << 18, seed=77, tol=1e-6)
+        v_loose = m.validate(n=1 << 18, seed=77, tol=2e-3)
+        f, lab = m.samples(1 << 16, seed=78)
+        b_tc = m.eval(f, kernel=0)
+    rms = lambda e: float(np.sqrt(np.mean(e * e)))
+    err_net, err_gl5 = rms(b_tc - lab), rms(_gl_bond(f) - lab)
+    print(f"crossing bonds: rms |B - exact| network (BF16, tensor cores) {err_net:.3e}, GL-5 {err_gl5:.3e}; "
+          f"coverage at 1e-6 {v_tight['coverage']:.3f}, at 2e-3 {v_loose['coverage']:.3f}")
+    # what the network gains over the fixed-point rule on the bonds it stands in for
+    assert err_net < err_gl5 / 4
     assert 0.0 <= v_tight["coverage"] <= v_loose["coverage"] <= 1.0
-    assert v_loose["coverage"] > 0.3
-    assert np.sqrt(np.mean((b - lab) ** 2)) < 2e-2
+    assert v_loose["coverage"] > 0.5
     seen = v_loose["bin_max_err"][v_loose["bin_max_err"] >= 0]
-    assert len(seen) > 100
+    assert len(seen) > 1000
 
 
 def test_errors_are_reported(ik):
