@@ -95,6 +95,7 @@ struct Lane {
     DevBuf bonds32, nb32, bonds64, nb64, pos64, bonds_tmp, boff, bsum, bsum_cells, relhi, rello, plo;
     DevBuf work_counter;
     DevBuf vir2, kin2; // double-float outputs of the FP32 gather
+    DevBuf mlp_rec, mlp_rid, mlp_count, corr; // surrogate records and fixed-point corrections
 };
 constexpr int IK_LANES = 4;
 
@@ -141,6 +142,7 @@ struct ik_ctx {
     std::vector<Slot> slots;
     std::vector<PendingOp> pending;
     ik_mlp* mlp = nullptr; // learned bond-integral surrogate (IK_QUAD_MLP)
+    long long mlp_cap = 0;  // record capacity per lane
     // CUDA-graph replay of ik_compute_batch
     bool capturing = false;
     int captured_lanes = 0;
@@ -388,6 +390,18 @@ int build_cells(ik_ctx* c, Slot& s, const IkGeom& g, cudaStream_t st, DevBuf& ce
     return IK_OK;
 }
 
+int mode_ok(ik_ctx* c, int precision)
+{
+    if (c->cg.mode == IK_QUAD_FIXEDPOINT) return IK_OK;
+    if (c->cg.mode == IK_QUAD_MLP) {
+        if (precision != IK_PREC_FP32) return fail(IK_ERR_UNSUPPORTED, "the learned surrogate runs on the FP32 path");
+        if (!c->mlp || !ik_mlp_internal_blob(c->mlp) || !ik_mlp_internal_table(c->mlp))
+            return fail(IK_ERR_STATE, "quadrature mode mlp needs a trained and validated surrogate (ik_set_mlp)");
+        return IK_OK;
+    }
+    return fail(IK_ERR_UNSUPPORTED, "quadrature mode %d is not available on the GPU path yet", c->cg.mode);
+}
+
 int slot_ok(ik_ctx* c, int slot)
 {
     if (slot < 0 || slot >= (int)c->slots.size()) return fail(IK_ERR_ARG, "slot %d out of range", slot);
@@ -495,16 +509,39 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         a.cnt_pairs = cnt + 1;
         a.cnt_triples = cnt + 2;
         CK(cudaMemsetAsync(L.work_counter.p, 0, sizeof(int), L.st));
+        const bool mlp = c->cg.mode == IK_QUAD_MLP && (a.fields & 1);
+        if (mlp) {
+            if (c->mlp_cap == 0) c->mlp_cap = std::max<long long>(1 << 20, 128LL * c->G);
+            ENS(L.mlp_rec, sizeof(float4) * (size_t)c->mlp_cap);
+            ENS(L.mlp_rid, sizeof(int2) * (size_t)c->mlp_cap);
+            ENS(L.mlp_count, sizeof(unsigned long long));
+            ENS(L.corr, sizeof(unsigned long long) * NC * (size_t)c->G);
+            CK(cudaMemsetAsync(L.mlp_count.p, 0, sizeof(unsigned long long), L.st));
+            CK(cudaMemsetAsync(L.corr.p, 0, sizeof(unsigned long long) * NC * (size_t)c->G, L.st));
+            a.mlp_rec = L.mlp_rec.as<float4>();
+            a.mlp_rid = L.mlp_rid.as<int2>();
+            a.mlp_count = L.mlp_count.as<unsigned long long>();
+            a.mlp_cap = c->mlp_cap;
+        }
         size_t smem = (size_t)IK_WARPS_GATHER * ((size_t)c->halo_cap * 20 + (size_t)a.qcap * 4);
         int blocks = std::min(c->nitems, c->sm_count * 2);
         if (blocks > 0)
-            CK(launch_gather32(a, c->cg.kind, (c->flags & IK_FLAG_LANE_KAHAN) != 0, blocks, 32 * IK_WARPS_GATHER,
-                               smem, L.st));
+            CK(launch_gather32(a, c->cg.kind, (c->flags & IK_FLAG_LANE_KAHAN) != 0 && !mlp, mlp, blocks,
+                               32 * IK_WARPS_GATHER, smem, L.st));
+        if (mlp) { // the surrogate on the tensor cores for the recorded bonds
+            const double to_w = std::sqrt(2.0 / 1.4426950408889634);
+            CK(launch_mlp_records(c->mlp, L.mlp_rec.as<float4>(), L.mlp_rid.as<int2>(),
+                                  L.mlp_count.as<unsigned long long>(), c->mlp_cap, L.bonds32.as<float4>(),
+                                  (float)to_w, (float)c->cg.width, NC, L.corr.as<unsigned long long>(),
+                                  c->status.as<int>(), c->sm_count * 3, L.st));
+            c->launches += 1;
+        }
         // FP64 finish: ((double)hi + (double)lo) * normalisation (0.5 of the GL map for the virial)
-        if (a.fields & 1) CK(launch_pairs_to_f64(L.vir2.as<float2>(), s.vir.as<double>(), (long long)NC * c->G,
-                                                 0.5 * norm, L.st));
-        if (a.fields & 2) CK(launch_pairs_to_f64(L.kin2.as<float2>(), s.kin.as<double>(), (long long)NC * c->G,
-                                                 norm, L.st));
+        if (a.fields & 1)
+            CK(launch_pairs_to_f64(L.vir2.as<float2>(), mlp ? L.corr.as<unsigned long long>() : nullptr,
+                                   s.vir.as<double>(), (long long)NC * c->G, 0.5 * norm, L.st));
+        if (a.fields & 2) CK(launch_pairs_to_f64(L.kin2.as<float2>(), nullptr, s.kin.as<double>(),
+                                                 (long long)NC * c->G, norm, L.st));
         c->launches += 2;
     } else {
         if (timing) CK(cudaEventRecord(c->ev[1], L.st));
@@ -685,7 +722,9 @@ int ik_set_cgfunc(ik_ctx* c, int kind, int mode, int order, double rcut, double 
     if (kind < 0 || kind > 3) return fail(IK_ERR_ARG, "unknown coarse-graining kind %d", kind);
     if (mode < 0 || mode > 3) return fail(IK_ERR_ARG, "unknown quadrature mode %d", mode);
     if (!(rcut > 0.0) || !std::isfinite(rcut)) return fail(IK_ERR_ARG, "rcut must be > 0");
-    if (mode == IK_QUAD_FIXEDPOINT && (order < 1 || order > 64))
+    if (mode == IK_QUAD_MLP && kind != IK_CG_GAUSSIAN)
+        return fail(IK_ERR_UNSUPPORTED, "the learned surrogate covers the Gaussian kernel only");
+    if ((mode == IK_QUAD_FIXEDPOINT || mode == IK_QUAD_MLP) && (order < 1 || order > 64))
         return fail(IK_ERR_ARG, "Gauss-Legendre order must be in [1, 64] (got %d)", order);
     if (kind == IK_CG_GAUSSIAN && !(width > 0.0)) return fail(IK_ERR_ARG, "Gaussian width must be > 0");
     const double PI = 3.14159265358979323846;
@@ -721,7 +760,7 @@ int ik_set_cgfunc(ik_ctx* c, int kind, int mode, int order, double rcut, double 
         cg.kappa = (float)(1.0 / rcut);
         cg.R2s = 1.0f;
     }
-    if (mode == IK_QUAD_FIXEDPOINT) {
+    if (mode == IK_QUAD_FIXEDPOINT || mode == IK_QUAD_MLP) { // the surrogate falls back on GL-n
         IkGL& gl = c->gl;
         gl.n = order;
         gl_rule(order, gl.x, gl.w);
@@ -858,8 +897,7 @@ int ik_compute_slot(ik_ctx* c, int slot, int precision, int fields)
     if (precision != IK_PREC_FP64 && precision != IK_PREC_FP32) return fail(IK_ERR_ARG, "unknown precision %d", precision);
     if (fields < 1 || fields > 3) return fail(IK_ERR_ARG, "fields mask must be 1, 2 or 3");
     if (int r = ensure_ready(c)) return r;
-    if (c->cg.mode != IK_QUAD_FIXEDPOINT)
-        return fail(IK_ERR_UNSUPPORTED, "quadrature mode %d is not available on the GPU path yet", c->cg.mode);
+    if (int r = mode_ok(c, precision)) return r;
     if (int r = ensure_geometry(c)) return r;
     if (c->maxb == 0) c->maxb = c->dim == 2 ? IK_MAXB_2D : IK_MAXB_3D;
     if (c->halo_cap == 0) c->halo_cap = c->dim == 2 ? 512 : 768;
@@ -875,8 +913,7 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
     if (precision != IK_PREC_FP64 && precision != IK_PREC_FP32) return fail(IK_ERR_ARG, "unknown precision %d", precision);
     if (fields < 1 || fields > 3) return fail(IK_ERR_ARG, "fields mask must be 1, 2 or 3");
     if (int r = ensure_ready(c)) return r;
-    if (c->cg.mode != IK_QUAD_FIXEDPOINT)
-        return fail(IK_ERR_UNSUPPORTED, "quadrature mode %d is not available on the GPU path yet", c->cg.mode);
+    if (int r = mode_ok(c, precision)) return r;
     if (int r = ensure_geometry(c)) return r;
     if (c->maxb == 0) c->maxb = c->dim == 2 ? IK_MAXB_2D : IK_MAXB_3D;
     if (c->halo_cap == 0) c->halo_cap = c->dim == 2 ? 512 : 768;
@@ -967,6 +1004,12 @@ int ik_synchronize(ik_ctx* c)
             int nm = std::max(mx, c->maxb + 1);
             if (nm > 63) { c->pending.clear(); return fail(IK_ERR_CAPACITY, "a particle has %d force-active bonds (max 63)", mx); }
             c->maxb = nm;
+            grow = true;
+        }
+        if (st & IK_ST_MMA_TIMEOUT) { c->pending.clear(); return fail(IK_ERR_TIMEOUT, "a tensor-core wait gave up"); }
+        if (st & IK_ST_MLP_OVERFLOW) {
+            if (c->mlp_cap >= (1LL << 31)) { c->pending.clear(); return fail(IK_ERR_CAPACITY, "surrogate record buffer cannot grow"); }
+            c->mlp_cap *= 2;
             grow = true;
         }
         if (st & IK_ST_HALO_OVERFLOW) {
@@ -1137,7 +1180,7 @@ int ik_eval_bond(ik_ctx* c, int64_t m, const double* x, const double* ri, const 
 {
     if (int r = check_ctx(c)) return r;
     if (!c->cg_set) return fail(IK_ERR_STATE, "coarse-graining function not set");
-    if (c->cg.mode != IK_QUAD_FIXEDPOINT)
+    if (c->cg.mode != IK_QUAD_FIXEDPOINT && c->cg.mode != IK_QUAD_MLP) // GL-n (the surrogate's fallback)
         return fail(IK_ERR_UNSUPPORTED, "quadrature mode %d is not available on the GPU path yet", c->cg.mode);
     if (m < 0 || (m > 0 && (!x || !ri || !rij || !bond || !delta))) return fail(IK_ERR_ARG, "bad arguments");
     if (m == 0) return IK_OK;

@@ -167,7 +167,8 @@ __device__ __forceinline__ int ik_red_index(int lane, int k)
 }
 
 // NP: number of symmetric Gauss-Legendre node pairs (compile-time when > 0; 0 = runtime).
-template <int DIM, int KIND, bool KAHAN, int NP>
+// MLPM: surrogate mode (bonds crossing the edge of the support become records).
+template <int DIM, int KIND, bool KAHAN, int NP, bool MLPM>
 __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
 {
     constexpr int NC = DIM == 2 ? 3 : 6;       // unique tensor components
@@ -186,6 +187,41 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
     const bool want_kin = (a.fields & 2) != 0;
     const int npairs = NP > 0 ? NP : a.npairs;
     unsigned long long my_pairs = 0, my_triples = 0;
+    // surrogate records: this warp's current chunk [wfill, wend) of the record buffer
+    long long wfill = 0, wend = 0;
+    auto emit = [&](int cmask, const float4 (&crec)[IK_P], const int (&gidx)[IK_P], int bidx) {
+        const int cnt = __popc(cmask);
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int tot = __shfl_sync(FULL, incl, 31);
+        if (tot == 0) return;
+        if (wfill + tot > wend) {
+            for (long long k = wfill + lane; k < wend; k += 32) a.mlp_rid[k] = make_int2(-1, 0);
+            unsigned long long nb = 0;
+            if (lane == 0) nb = atomicAdd(a.mlp_count, (unsigned long long)IK_MLP_CHUNK);
+            nb = __shfl_sync(FULL, nb, 0);
+            if ((long long)nb + IK_MLP_CHUNK > a.mlp_cap) { // overflow: reported, replayed larger
+                if (lane == 0) atomicOr(a.status, IK_ST_MLP_OVERFLOW);
+                wfill = wend = 0;
+                return;
+            }
+            wfill = (long long)nb;
+            wend = wfill + IK_MLP_CHUNK;
+        }
+        long long o = wfill + incl - cnt;
+#pragma unroll
+        for (int p = 0; p < IK_P; ++p)
+            if (cmask & (1 << p)) {
+                a.mlp_rec[o] = crec[p];
+                a.mlp_rid[o] = make_int2(gidx[p], bidx);
+                ++o;
+            }
+        wfill += tot;
+    };
 
     for (;;) {
         int w = 0;
@@ -316,6 +352,8 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                         cf[5 % NC] = fy * hbz;
                     }
                     const float mx0 = sp.x + hbx, my0 = sp.y + hby, mz0 = sp.z + hbz; // bond midpoint
+                    float4 crec[P];
+                    int cmask = 0;
                     if constexpr (!KAHAN && NP > 0) {
                         // packed path: two grid points per f32x2 instruction
                         const f32x2 mid2x = pk2(mx0, mx0), mid2y = pk2(my0, my0), mid2z = pk2(mz0, mz0);
@@ -352,6 +390,22 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                             }
                             float Ba, Bb;
                             up2(B, Ba, Bb);
+                            if constexpr (MLPM) { // r_j outside the support: a record, not a term
+                                const f32x2 rj2 = fma2(pk2(-2.f, -2.f), mb, add2(M, pk2(hh, hh)));
+                                float ra, rb, mba, mbb;
+                                up2(rj2, ra, rb);
+                                up2(mb, mba, mbb);
+                                if ((m & (1 << (2 * j))) && ra >= R2s) {
+                                    crec[2 * j] = make_float4(Ma, mba, hh, Ba);
+                                    cmask |= 1 << (2 * j);
+                                    Ba = 0.f;
+                                }
+                                if ((m & (2 << (2 * j))) && rb >= R2s) {
+                                    crec[2 * j + 1] = make_float4(Mb, mbb, hh, Bb);
+                                    cmask |= 2 << (2 * j);
+                                    Bb = 0.f;
+                                }
+                            }
                             B = pk2((m & (1 << (2 * j))) ? Ba : 0.f, (m & (2 << (2 * j))) ? Bb : 0.f);
 #pragma unroll
                             for (int c = 0; c < NC; ++c) acc2[j][c] = fma2(B, cf2[c], acc2[j][c]);
@@ -400,6 +454,13 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                                 }
                             }
                             B = (m & (1 << p)) ? B : 0.f;
+                            if constexpr (MLPM) {
+                                if ((m & (1 << p)) && fmaf(-2.f, mb, M + hh) >= R2s) {
+                                    crec[p] = make_float4(M, mb, hh, B);
+                                    cmask |= 1 << p;
+                                    B = 0.f;
+                                }
+                            }
 #pragma unroll
                             for (int c = 0; c < NC; ++c) {
                                 if (KAHAN) {
@@ -414,6 +475,7 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                         }
                     }
                     my_triples += __popc(m);
+                    if constexpr (MLPM) emit(cmask, crec, gi, (__float_as_int(sp.w) >> 6) + ((e >> 4) & 63));
                 };
 
                 int qn = 0;
@@ -503,8 +565,8 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                     }
                     __syncwarp();
                 }
-                if (lane < qn) {
-                    const int e1 = queue[lane];
+                if (MLPM ? qn > 0 : lane < qn) { // surrogate mode: all lanes (emission is warp-wide)
+                    const int e1 = lane < qn ? queue[lane] : (queue[0] & ~15); // mask 0 on idle lanes
                     float4 sp1, b1;
                     load_slot(e1, sp1, b1);
                     process_slot(e1, sp1, b1);
@@ -568,6 +630,8 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
             __syncwarp();
         }
     }
+    if constexpr (MLPM)
+        for (long long k = wfill + lane; k < wend; k += 32) a.mlp_rid[k] = make_int2(-1, 0);
     // counters
     for (int o = 16; o; o >>= 1) {
         my_pairs += __shfl_xor_sync(FULL, my_pairs, o);
@@ -579,10 +643,10 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
     }
 }
 
-template <int DIM, int KIND, bool KAHAN, int NP>
+template <int DIM, int KIND, bool KAHAN, int NP, bool MLPM = false>
 static cudaError_t launch_one(const GatherArgs32& a, int blocks, int threads, size_t smem, cudaStream_t st)
 {
-    auto kfn = k_gather32<DIM, KIND, KAHAN, NP>;
+    auto kfn = k_gather32<DIM, KIND, KAHAN, NP, MLPM>;
     cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kfn<<<blocks, threads, smem, st>>>(a);
@@ -608,9 +672,16 @@ static cudaError_t launch_np(const GatherArgs32& a, int kind, int blocks, int th
     return launch_kind<DIM, KAHAN, 0>(a, kind, blocks, threads, smem, st);
 }
 
-cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, int blocks, int threads,
+cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, bool mlp, int blocks, int threads,
                             size_t smem, cudaStream_t st)
 {
+    if (mlp) { // Gaussian kernel only, plain per-lane sums
+        if (kind != 1 || kahan) return cudaErrorInvalidValue;
+        if (a.g.dim == 2) return a.npairs == 2 ? launch_one<2, 1, false, 2, true>(a, blocks, threads, smem, st)
+                                               : launch_one<2, 1, false, 0, true>(a, blocks, threads, smem, st);
+        return a.npairs == 2 ? launch_one<3, 1, false, 2, true>(a, blocks, threads, smem, st)
+                             : launch_one<3, 1, false, 0, true>(a, blocks, threads, smem, st);
+    }
     if (a.g.dim == 2) return kahan ? launch_np<2, true>(a, kind, blocks, threads, smem, st)
                                    : launch_np<2, false>(a, kind, blocks, threads, smem, st);
     return kahan ? launch_np<3, true>(a, kind, blocks, threads, smem, st)
@@ -619,17 +690,22 @@ cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, int blo
 
 // Double-float pairs -> FP64, scaled: out = ((double)hi + (double)lo) * scale.  One
 // thread per value (fully populated warps: the FP64 pipe is narrow on this GPU).
-__global__ void k_pairs_to_f64(const float2* __restrict__ in, double* __restrict__ out, int count, double scale)
+// With surrogate corrections (fixed point, 2^-32 units) added before scaling.
+__global__ void k_pairs_to_f64(const float2* __restrict__ in, const unsigned long long* __restrict__ corr,
+                               double* __restrict__ out, int count, double scale)
 {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= count) return;
     const float2 v = in[k];
-    out[k] = ((double)v.x + (double)v.y) * scale;
+    double s = (double)v.x + (double)v.y;
+    if (corr) s += (double)(long long)corr[k] * 2.3283064365386963e-10;
+    out[k] = s * scale;
 }
 
-cudaError_t launch_pairs_to_f64(const float2* in, double* out, long long count, double scale, cudaStream_t st)
+cudaError_t launch_pairs_to_f64(const float2* in, const unsigned long long* corr, double* out, long long count,
+                                double scale, cudaStream_t st)
 {
     if (count <= 0) return cudaSuccess;
-    k_pairs_to_f64<<<(int)((count + 255) / 256), 256, 0, st>>>(in, out, (int)count, scale);
+    k_pairs_to_f64<<<(int)((count + 255) / 256), 256, 0, st>>>(in, corr, out, (int)count, scale);
     return cudaGetLastError();
 }

@@ -70,10 +70,19 @@ struct GatherArgs32 {
     int* status;
     unsigned long long* cnt_pairs;
     unsigned long long* cnt_triples;
+    // surrogate mode: bonds crossing the edge of the support go to records instead of
+    // the fixed-point sum ({M, mb, hh, B_fixed} + {grid index, bond index})
+    float4* mlp_rec;
+    int2* mlp_rid;
+    unsigned long long* mlp_count;  // records reserved (chunks of IK_MLP_CHUNK)
+    long long mlp_cap;
 };
-cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, int blocks, int threads,
+#define IK_MLP_CHUNK 2048
+cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, bool mlp, int blocks, int threads,
                             size_t smem, cudaStream_t st);
-cudaError_t launch_pairs_to_f64(const float2* in, double* out, long long count, double scale, cudaStream_t st);
+// out = ((double)hi + (double)lo + corr * 2^-32) * scale   (corr: fixed-point, may be null)
+cudaError_t launch_pairs_to_f64(const float2* in, const unsigned long long* corr, double* out, long long count,
+                                double scale, cudaStream_t st);
 
 // ---- FP64 plain gather (ik_gather64.cu) ------------------------------------
 struct GatherArgs64 {

@@ -112,3 +112,82 @@ def test_errors_are_reported(ik):
             m.train(nsamples=1000)                         # not a power of two
         with pytest.raises(ik.IKError):
             m.set_params(np.zeros(10, np.float32))         # wrong size
+
+
+# --------------------------------------------------------------------------- inside the IK gather
+@pytest.fixture(scope="module")
+def trained(ik):
+    m = ik.MLP()
+    m.train(nsamples=1 << 20, epochs=120, ctas=152, lr=3e-3, seed=21)
+    yield m
+    m.close()
+
+
+def _ik_fields(ik, frame, grid, mode, mlp=None, flags=0):
+    with ik.IKContext() as c:
+        c.set_flags(flags)
+        c.set_box(2, [frame.L, frame.L, 1.0])
+        c.set_poly12()
+        c.set_cgfunc("gaussian", 6.0, mode=mode, order=5, width=2.0)
+        if mlp is not None:
+            c.set_mlp(mlp)
+        c.set_grid(grid)
+        c.set_frame(frame.pos, frame.diam, frame.vel, frame.mass)
+        c.compute("fp32")
+        return c.get_field(ik.FIELD_VIRIAL), c.counters(), c.get_max_rcut()
+
+
+def test_ik_surrogate_mode_gains_over_fixed_point_rule(ik, oracle, trained):
+    """The stress field of the surrogate mode (bonds crossing the edge of the support
+    evaluated by the network on the tensor cores) against the exact bond integral, next
+    to the fixed-point rule's: the gain of the trained network in the IK workload."""
+    from conftest import rel_l2, uniq
+    from pyglasstools_gb300 import synth
+    fr = synth.make_frame(4000, dim=2, seed=41)
+    grid = synth.lattice_grid(fr.L, 48, 2)
+    trained.validate(n=1 << 18, seed=5, tol=1.0)   # every populated bin
+    v_gl, _, max_rc = _ik_fields(ik, fr, grid, "fixedpoint")
+    v_net, cnt, _ = _ik_fields(ik, fr, grid, "mlp", trained)
+    box = oracle.make_box(2, [fr.L, fr.L, 1.0])
+    cg = oracle.make_cg("gaussian", rcut=6.0, mode="exact", order=5, width=2.0)
+    exact, _ = oracle.compute(box, fr.pos, fr.diam, oracle.make_poly12(), cg, grid, max_rc=max_rc)
+    e_gl = rel_l2(uniq(v_gl), uniq(exact))
+    e_net = rel_l2(uniq(v_net), uniq(exact))
+    print(f"field error vs exact bond integral: fixed point GL-5 {e_gl}, surrogate {e_net}")
+    assert np.all(e_net < e_gl / 3)
+    assert np.all(e_net < 1e-4)
+    # deterministic (fixed-point accumulation of the surrogate's terms)
+    v_net2, _, _ = _ik_fields(ik, fr, grid, "mlp", trained)
+    np.testing.assert_array_equal(v_net, v_net2)
+
+
+def test_ik_surrogate_mode_with_empty_table_is_fixed_point(ik, trained):
+    """With no bin validated every recorded bond falls back on its fixed-point value:
+    the field equals the plain FP32 one up to the order of summation."""
+    from conftest import rel_l2, uniq
+    from pyglasstools_gb300 import synth
+    fr = synth.make_frame(3000, dim=2, seed=42)
+    grid = synth.lattice_grid(fr.L, 40, 2)
+    trained.validate(n=1 << 16, seed=6, tol=0.0)
+    v_gl, _, _ = _ik_fields(ik, fr, grid, "fixedpoint")
+    v_fb, _, _ = _ik_fields(ik, fr, grid, "mlp", trained)
+    assert np.all(rel_l2(uniq(v_fb), uniq(v_gl)) <= 1e-7)
+
+
+def test_ik_surrogate_mode_errors(ik, trained):
+    from pyglasstools_gb300 import synth
+    fr = synth.make_frame(500, dim=2, seed=43)
+    grid = synth.lattice_grid(fr.L, 8, 2)
+    with ik.IKContext() as c:
+        c.set_box(2, [fr.L, fr.L, 1.0])
+        c.set_poly12()
+        with pytest.raises(ik.IKError):
+            c.set_cgfunc("octic", 2.0, mode="mlp", order=5)    # Gaussian only
+        c.set_cgfunc("gaussian", 6.0, mode="mlp", order=5, width=2.0)
+        c.set_grid(grid)
+        c.set_frame(fr.pos, fr.diam, fr.vel, fr.mass)
+        with pytest.raises(ik.IKError):
+            c.compute("fp32")                                  # no surrogate attached
+        c.set_mlp(trained)
+        with pytest.raises(ik.IKError):
+            c.compute("fp64")                                  # FP32 path only
