@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--workload", default="ik2d_n64k_g256_gauss", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--frames", type=int, default=0, help="override the frames per step (profiling)")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate leg")
     ap.add_argument("--no-graph", action="store_true",
                     help="enqueue every frame with its own launches instead of one CUDA-graph replay per step")
     ap.add_argument("--profile", action="store_true",
@@ -199,6 +200,76 @@ def reference_arm(args, wl, name):
                                        f"FP64 oracle restating IrvingKirkwood::compute, OpenMP {cores} threads"},
             "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------- surrogate leg
+MLP_TOL = 2e-4
+
+
+def surrogate_leg(args, ctx, wl, F, stream, all_slots, v_plain):
+    """The learned bond-integral surrogate on the same frames: train it on the GPU
+    (2^22 samples), validate it, then time the FP32 path with the network standing in
+    for the quadrature on bonds that cross the edge of the support, and state its error
+    against the exact bond integral (FP64, erf closed form) next to the fixed-point rule's."""
+    import torch
+    from pyglasstools_gb300 import ikabi
+    cg = wl["cg"]
+    mlp = ikabi.MLP(torch.cuda.current_device())
+    t0 = time.perf_counter()
+    hist = mlp.train(nsamples=1 << 22, epochs=250, ctas=152, lr=2e-3, seed=5)
+    train_s = time.perf_counter() - t0
+    v_spec = mlp.validate(n=1 << 20, seed=98, tol=1e-6)
+    v_used = mlp.validate(n=1 << 20, seed=98, tol=MLP_TOL)
+    ctx.set_mlp(mlp)
+    ctx.set_cgfunc(cg["kind"], cg["rcut"], mode="mlp", order=5, width=cg["width"])
+    ctx.compute_batch(all_slots, "fp32")  # first call: plain launches, then the graph is recorded
+    ctx.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    for _ in range(2):
+        ctx.compute_batch(all_slots, "fp32")
+    ctx.synchronize()
+    launches0 = ctx.launch_count()
+    e0.record(stream)
+    for _ in range(args.steps):
+        ctx.compute_batch(all_slots, "fp32")
+    ctx.wait_all()
+    e1.record(stream)
+    ctx.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = ctx.launch_count() - launches0
+    v_net = ctx.get_field(ikabi.FIELD_VIRIAL, slot=0)
+    records = ctx.mlp_records(0)
+    triples = ctx.counters(0)[2]
+    # fixed-point FP32 and exact FP64 of frame 0
+    ctx.set_cgfunc(cg["kind"], cg["rcut"], mode="fixedpoint", order=5, width=cg["width"])
+    ctx.compute_slot(0, "fp32")
+    ctx.synchronize()
+    v_gl = ctx.get_field(ikabi.FIELD_VIRIAL, slot=0)
+    ctx.set_cgfunc(cg["kind"], cg["rcut"], mode="exact", order=5, width=cg["width"])
+    ctx.compute_slot(0, "fp64")
+    ctx.synchronize()
+    v_exact = ctx.get_field(ikabi.FIELD_VIRIAL, slot=0)
+    ctx.set_cgfunc(cg["kind"], cg["rcut"], mode="fixedpoint", order=5, width=cg["width"])
+    ctx.set_mlp(None)
+
+    def rel(a, b):
+        iu = [(0, 0), (1, 1), (0, 1)]
+        return [float(np.linalg.norm(a[:, i, j] - b[:, i, j]) / np.linalg.norm(b[:, i, j])) for i, j in iu]
+
+    out = {"value": F * args.steps / (ms * 1e-3), "unit": "frames/s", "gpu_launches": int(launches),
+           "network": "4-64-64-64-1 SiLU, BF16 operands on tcgen05 (activations as BF16 hi+lo pairs), FP32 accum",
+           "train": {"samples": 1 << 22, "steps": len(hist), "seconds": train_s, "final_loss": float(hist[-1])},
+           "validation": {"rms_err": v_used["rms_err"], "max_err": v_used["max_err"],
+                          "coverage_at_1e-6": v_spec["coverage"], "coverage_at_tol": v_used["coverage"],
+                          "tol": MLP_TOL},
+           "rel_err_vs_exact_integral": {"surrogate_fp32": rel(v_net, v_exact), "fixed_point_gl5_fp32": rel(v_gl, v_exact),
+                                         "plain_fp64_gl5": rel(v_plain, v_exact)},
+           "rel_diff_vs_plain_fp64_gl5": rel(v_net, v_plain),
+           "records_slot0": records, "triples_slot0": triples,
+           "tensor_flop_per_eval": 2 * (4 * 64 * 3 + 128 * 64 * 2)}
+    mlp.close()
+    return out
 
 
 # ---------------------------------------------------------------------------- our arm
@@ -364,6 +435,10 @@ def ours(args, wl, name):
             if len(parts) >= 3 and parts[0] == "k_gather32" and parts[1] == name:
                 traffic = float(parts[2])
 
+    surrogate = None
+    if not args.no_surrogate and wl["cg"]["kind"] == "gaussian" and D == 2:
+        surrogate = surrogate_leg(args, ctx, wl, F, stream, all_slots, v64)
+
     out = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, shapes of the named config)",
@@ -384,6 +459,8 @@ def ours(args, wl, name):
            "tuned_over_plain": value / plain_value,
            "rel_err_vs_fp64": {"virial": err_v, "kinetic": err_k},
            "interactions_per_s": A * value}
+    if surrogate is not None:
+        out["surrogate"] = surrogate
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         G = len(grid)

@@ -191,6 +191,10 @@ int ik_get_launch_count(ik_ctx* ctx, int64_t* out);
 /* Counters of the last computation: [0] force-active directed bonds,
  * [1] accepted (grid, particle) pairs, [2] active (grid, i, j) triples (FP32 path). */
 int ik_get_counters(ik_ctx* ctx, int slot, int64_t* out3);
+/* Bonds the last surrogate-mode computation of `slot` handed to the network (crossing
+ * the edge of the support; each falls back on its fixed-point value outside the
+ * validated bins).  No reference counterpart. */
+int ik_get_mlp_records(ik_ctx* ctx, int slot, int64_t* out);
 
 /* ---- learned bond-integral surrogate -------------------------------------------
  * No reference counterpart: a small network (4 -> 64 -> 64 -> 64 -> 1, SiLU) that

@@ -393,6 +393,10 @@ int build_cells(ik_ctx* c, Slot& s, const IkGeom& g, cudaStream_t st, DevBuf& ce
 int mode_ok(ik_ctx* c, int precision)
 {
     if (c->cg.mode == IK_QUAD_FIXEDPOINT) return IK_OK;
+    if (c->cg.mode == IK_QUAD_EXACT) {
+        if (precision != IK_PREC_FP64) return fail(IK_ERR_UNSUPPORTED, "the exact bond integral runs on the FP64 path");
+        return IK_OK;
+    }
     if (c->cg.mode == IK_QUAD_MLP) {
         if (precision != IK_PREC_FP32) return fail(IK_ERR_UNSUPPORTED, "the learned surrogate runs on the FP32 path");
         if (!c->mlp || !ik_mlp_internal_blob(c->mlp) || !ik_mlp_internal_table(c->mlp))
@@ -522,6 +526,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
             a.mlp_rid = L.mlp_rid.as<int2>();
             a.mlp_count = L.mlp_count.as<unsigned long long>();
             a.mlp_cap = c->mlp_cap;
+            a.cnt_records = cnt + 3;
         }
         size_t smem = (size_t)IK_WARPS_GATHER * ((size_t)c->halo_cap * 20 + (size_t)a.qcap * 4);
         int blocks = std::min(c->nitems, c->sm_count * 2);
@@ -724,7 +729,7 @@ int ik_set_cgfunc(ik_ctx* c, int kind, int mode, int order, double rcut, double 
     if (!(rcut > 0.0) || !std::isfinite(rcut)) return fail(IK_ERR_ARG, "rcut must be > 0");
     if (mode == IK_QUAD_MLP && kind != IK_CG_GAUSSIAN)
         return fail(IK_ERR_UNSUPPORTED, "the learned surrogate covers the Gaussian kernel only");
-    if ((mode == IK_QUAD_FIXEDPOINT || mode == IK_QUAD_MLP) && (order < 1 || order > 64))
+    if ((mode == IK_QUAD_FIXEDPOINT || mode == IK_QUAD_MLP || mode == IK_QUAD_EXACT) && (order < 1 || order > 64))
         return fail(IK_ERR_ARG, "Gauss-Legendre order must be in [1, 64] (got %d)", order);
     if (kind == IK_CG_GAUSSIAN && !(width > 0.0)) return fail(IK_ERR_ARG, "Gaussian width must be > 0");
     const double PI = 3.14159265358979323846;
@@ -760,8 +765,11 @@ int ik_set_cgfunc(ik_ctx* c, int kind, int mode, int order, double rcut, double 
         cg.kappa = (float)(1.0 / rcut);
         cg.R2s = 1.0f;
     }
-    if (mode == IK_QUAD_FIXEDPOINT || mode == IK_QUAD_MLP) { // the surrogate falls back on GL-n
+    if (mode == IK_QUAD_FIXEDPOINT || mode == IK_QUAD_MLP || mode == IK_QUAD_EXACT) {
+        // GL-n: the rule itself, the surrogate's fallback, or (exact mode) the rule on
+        // the clipped interval, at least 5 points (20 for the mollifier)
         IkGL& gl = c->gl;
+        if (mode == IK_QUAD_EXACT) order = std::max(order, kind == IK_CG_MOLLIFIER ? 20 : 5);
         gl.n = order;
         gl_rule(order, gl.x, gl.w);
         gl.npairs = order / 2;
@@ -1180,7 +1188,7 @@ int ik_eval_bond(ik_ctx* c, int64_t m, const double* x, const double* ri, const 
 {
     if (int r = check_ctx(c)) return r;
     if (!c->cg_set) return fail(IK_ERR_STATE, "coarse-graining function not set");
-    if (c->cg.mode != IK_QUAD_FIXEDPOINT && c->cg.mode != IK_QUAD_MLP) // GL-n (the surrogate's fallback)
+    if (c->cg.mode == IK_QUAD_ADAPTIVE) // GL-n, the surrogate's fallback GL-n, or the exact integral
         return fail(IK_ERR_UNSUPPORTED, "quadrature mode %d is not available on the GPU path yet", c->cg.mode);
     if (m < 0 || (m > 0 && (!x || !ri || !rij || !bond || !delta))) return fail(IK_ERR_ARG, "bad arguments");
     if (m == 0) return IK_OK;
@@ -1313,6 +1321,19 @@ int ik_get_counters(ik_ctx* c, int slot, int64_t* out3)
     out3[0] = (int64_t)h[0];
     out3[1] = (int64_t)h[1];
     out3[2] = (int64_t)h[2];
+    return IK_OK;
+}
+
+int ik_get_mlp_records(ik_ctx* c, int slot, int64_t* out)
+{
+    if (int r = check_ctx(c)) return r;
+    if (int r = slot_ok(c, slot)) return r;
+    if (!out) return fail(IK_ERR_ARG, "null output");
+    if (int r = ik_synchronize(c)) return r;
+    Slot& s = c->slots[(size_t)slot];
+    unsigned long long h[4] = {0, 0, 0, 0};
+    if (s.counters.p) CK(cudaMemcpy(h, s.counters.p, sizeof h, cudaMemcpyDeviceToHost));
+    *out = (int64_t)h[3];
     return IK_OK;
 }
 

@@ -13,6 +13,7 @@
 #define IK_ST_HALO_OVERFLOW 2
 #define IK_ST_BAD_INPUT     4
 #define IK_ST_NEIGH_OVERFLOW 8
+#define IK_QUAD_EXACT_DEV 2 /* IK_QUAD_EXACT of the C ABI */
 #define IK_ST_MMA_TIMEOUT   16  /* a tensor-core completion wait gave up */
 #define IK_ST_MLP_OVERFLOW  32  /* the surrogate record buffer overflowed */
 

@@ -189,6 +189,7 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
     unsigned long long my_pairs = 0, my_triples = 0;
     // surrogate records: this warp's current chunk [wfill, wend) of the record buffer
     long long wfill = 0, wend = 0;
+    unsigned long long my_records = 0;
     auto emit = [&](int cmask, const float4 (&crec)[IK_P], const int (&gidx)[IK_P], int bidx) {
         const int cnt = __popc(cmask);
         int incl = cnt;
@@ -221,6 +222,7 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                 ++o;
             }
         wfill += tot;
+        my_records += (unsigned long long)cnt;
     };
 
     for (;;) {
@@ -637,9 +639,12 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
         my_pairs += __shfl_xor_sync(FULL, my_pairs, o);
         my_triples += __shfl_xor_sync(FULL, my_triples, o);
     }
+    if constexpr (MLPM)
+        for (int o = 16; o; o >>= 1) my_records += __shfl_xor_sync(FULL, my_records, o);
     if (lane == 0) {
         atomicAdd(a.cnt_pairs, my_pairs);
         atomicAdd(a.cnt_triples, my_triples);
+        if (MLPM) atomicAdd(a.cnt_records, my_records);
     }
 }
 

@@ -9,9 +9,53 @@
 // 0.5 * forceDivR * r_ij (x) r_ij (ListofCommonObservables.h:57-81).
 #include "ik_kernels.h"
 
+// Exact bond integral (no reference counterpart; the answer the fixed-point rule and
+// the learned surrogate approximate): clip the segment r_i + s r_ij, s in [0, 1], to
+// the open ball |x - r| < R, then
+//   Gaussian: the error-function closed form along the line,
+//   others:   Gauss-Legendre on the clipped interval (exact for the octic's degree-8
+//             polynomial at n >= 5).
+__device__ double ik_bond64_exact(const IkCG& cg, const double* xs, const double* ws, int nq, const double x[3],
+                                  const double ri[3], const double rij[3])
+{
+    const double u0 = x[0] - ri[0], u1 = x[1] - ri[1], u2 = x[2] - ri[2];
+    const double bb = rij[0] * rij[0] + rij[1] * rij[1] + rij[2] * rij[2];
+    const double ub = u0 * rij[0] + u1 * rij[1] + u2 * rij[2];
+    const double uu = u0 * u0 + u1 * u1 + u2 * u2;
+    if (bb == 0.0) return ik_delta64(cg, uu);
+    const double disc = ub * ub - bb * (uu - cg.rcutsq);
+    if (!(disc > 0.0)) return 0.0;
+    const double sq = sqrt(disc);
+    const double qq = ub + (ub >= 0.0 ? sq : -sq); // roots without cancellation
+    const double ra = qq / bb, rb = qq != 0.0 ? (uu - cg.rcutsq) / qq : ra;
+    const double s0 = fmax(fmin(ra, rb), 0.0), s1 = fmin(fmax(ra, rb), 1.0);
+    if (!(s1 > s0)) return 0.0;
+    if (cg.kind == 1) {
+        const double w = cg.width, sstar = ub / bb;
+        const double p0 = u0 - sstar * rij[0], p1 = u1 - sstar * rij[1], p2 = u2 - sstar * rij[2];
+        const double dperp2 = p0 * p0 + p1 * p1 + p2 * p2;
+        const double blen = sqrt(bb), k = blen / (1.4142135623730951 * w);
+        const double ta = (s0 - sstar) * k, tb = (s1 - sstar) * k;
+        double diff;
+        if (ta >= 0.0) diff = erfc(ta) - erfc(tb);
+        else if (tb <= 0.0) diff = erfc(-tb) - erfc(-ta);
+        else diff = erf(tb) - erf(ta);
+        return cg.norm * exp(-dperp2 / (2.0 * w * w)) * 1.2533141373155003 * (w / blen) * diff;
+    }
+    double acc = 0.0;
+    for (int k = 0; k < nq; ++k) {
+        const double s = s0 + (s1 - s0) * xs[k];
+        const double d0 = u0 - s * rij[0], d1 = u1 - s * rij[1], d2 = u2 - s * rij[2];
+        const double r2 = fmin(d0 * d0 + d1 * d1 + d2 * d2, cg.rcutsq * (1.0 - 1e-15)); // inside by construction
+        acc += ws[k] * ik_delta64(cg, r2);
+    }
+    return 0.5 * acc * (s1 - s0);
+}
+
 __device__ __forceinline__ double ik_bond64(const IkCG& cg, const double* xs, const double* ws, int nq,
                                             const double x[3], const double ri[3], const double rij[3])
 {
+    if (cg.mode == IK_QUAD_EXACT_DEV) return ik_bond64_exact(cg, xs, ws, nq, x, ri, rij);
     double acc = 0.0;
     for (int k = 0; k < nq; ++k) {
         double s = xs[k];

@@ -76,6 +76,7 @@ struct GatherArgs32 {
     int2* mlp_rid;
     unsigned long long* mlp_count;  // records reserved (chunks of IK_MLP_CHUNK)
     long long mlp_cap;
+    unsigned long long* cnt_records;
 };
 #define IK_MLP_CHUNK 2048
 cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, bool mlp, int blocks, int threads,

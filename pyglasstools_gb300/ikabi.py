@@ -75,6 +75,7 @@ def lib():
             "ik_wait_all": ([vp], i32),
             "ik_compute_batch": ([vp, C.POINTER(C.c_int), i32, i32, i32], i32),
             "ik_set_mlp": ([vp, vp], i32),
+            "ik_get_mlp_records": ([vp, i32, C.POINTER(C.c_int64)], i32),
             "ik_mlp_create": ([C.POINTER(vp), i32], i32),
             "ik_mlp_destroy": ([vp], i32),
             "ik_mlp_num_params": ([], i32),
@@ -281,6 +282,11 @@ class IKContext:
         c = (C.c_int64 * 3)()
         check(lib().ik_get_counters(self._h, slot, c))
         return list(c)
+
+    def mlp_records(self, slot=0):
+        v = C.c_int64()
+        check(lib().ik_get_mlp_records(self._h, slot, C.byref(v)))
+        return v.value
 
 
 def measure_fp32_peak(device=0):

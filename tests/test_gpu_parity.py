@@ -385,3 +385,19 @@ def test_python_api_end_to_end(tmp_path, golden, monkeypatch):
     # values are printed with 6 significant digits
     np.testing.assert_allclose(vals, gold, rtol=6e-6, atol=1e-300)
     assert open(tmp_path / "restart.log").read() == "Frame 2"
+
+
+@pytest.mark.parametrize("cg", [dict(kind="gaussian", rcut=6.0, mode="exact", order=5, width=2.0),
+                                dict(kind="octic", rcut=2.0, mode="exact", order=5)])
+def test_exact_bond_integral_fp64_vs_oracle(ik, oracle, cg):
+    """Exact mode (segment clipped to the support; erf closed form for the Gaussian,
+    GL-5 on the clipped interval for the octic) on the plain FP64 path."""
+    from pyglasstools_gb300 import synth
+    fr = synth.make_frame(2500, dim=2, seed=61)
+    grid = synth.lattice_grid(fr.L, 40, 2)
+    got_v, got_k, _ = run_gpu(ik, 2, fr.L, fr.pos, fr.diam, grid, cg, "fp64", vel=fr.vel, mass=fr.mass)
+    want_v, want_k = run_oracle(oracle, 2, fr.L, fr.pos, fr.diam, grid, cg, vel=fr.vel, mass=fr.mass)
+    assert_fields(got_v, want_v, FP64_TOL, what="exact virial")
+    assert_fields(got_k, want_k, FP64_TOL, what="exact kinetic")
+    with pytest.raises(ik.IKError):
+        run_gpu(ik, 2, fr.L, fr.pos, fr.diam, grid, cg, "fp32")  # FP64 path only
