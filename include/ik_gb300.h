@@ -144,6 +144,8 @@ int ik_eval_bond(ik_ctx* ctx, int64_t m, const double* x, const double* ri,
 /* FP32 path: Kahan-compensated per-lane sums (the combination of the lane partials
  * of every grid point is always compensated; per-lane sums are plain by default). */
 #define IK_FLAG_LANE_KAHAN 2
+#define IK_FLAG_CSR_BONDS 4 /* FP32 path: compact the bond records to CSR even when the
+                               fixed-stride layout fits (the layout used for n * maxb >= 2^25) */
 int ik_set_flags(ik_ctx* ctx, int flags);
 int ik_get_timing(ik_ctx* ctx, float* ms4);
 

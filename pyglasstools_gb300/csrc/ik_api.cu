@@ -435,39 +435,51 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
     int r = build_cells(c, s, g, L.st, L.cell_of, L.rank, L.cell_count, L.cell_start, L.sorted, L.bsum_cells,
                         prec == IK_PREC_FP32 ? &L.relhi : nullptr, prec == IK_PREC_FP32 ? &L.rello : nullptr);
     if (r) return r;
-    c->launches += (n > 0 ? 4 : 2) + (g.ncell > 0 ? 1 : 0) + (n > 0 ? 1 : 0) + 1; // cells, sort, bonds|pack, gather
+    const int scan_launches = g.ncell <= 65536 ? 1 : 2;
+    c->launches += (n > 0 ? 2 : 0) + scan_launches; // bin, scan, scatter
     ENS(L.prec, sizeof(IkPRec) * std::max(n, 1));
     ENS(L.kin, sizeof(float4) * 2 * std::max(n, 1));
     ENS(L.diam32, sizeof(float) * std::max(n, 1));
-    if (g.ncell > 0) { // sort ids inside each cell: deterministic order
+    if (g.ncell > 0 && prec != IK_PREC_FP32) { // sort ids inside each cell: deterministic order
         k_cell_sort_pack<<<(g.ncell + 127) / 128, 128, 0, L.st>>>(
             g, L.cell_start.as<int>(), L.sorted.as<int>(), nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
             nullptr, 0);
         CK(cudaGetLastError());
+        c->launches += 1;
     }
     unsigned long long* cnt = s.counters.as<unsigned long long>();
     if (prec == IK_PREC_FP32) {
         ENS(L.pos64, sizeof(IkB64) * std::max(n, 1));
         ENS(L.plo, sizeof(float4) * std::max(n, 1));
-        CK(launch_pack32(g, n, L.sorted.as<int>(), L.cell_of.as<int>(), L.relhi.as<float4>(),
-                         L.rello.as<float4>(), s.pos.as<double>(), s.has_vel ? s.vel.as<double>() : nullptr,
-                         s.has_mass ? s.mass.as<double>() : nullptr, s.diam.as<double>(), L.prec.as<IkPRec>(),
-                         L.plo.as<float4>(), L.pos64.as<IkB64>(), L.kin.as<float4>(), L.diam32.as<float>(),
-                         L.st));
+        // per-cell sort + pack in one launch
+        CK(launch_sort_pack32(g, L.cell_start.as<int>(), L.sorted.as<int>(), L.relhi.as<float4>(),
+                              L.rello.as<float4>(), s.pos.as<double>(), s.has_vel ? s.vel.as<double>() : nullptr,
+                              s.has_mass ? s.mass.as<double>() : nullptr, s.diam.as<double>(), L.prec.as<IkPRec>(),
+                              L.plo.as<float4>(), L.pos64.as<IkB64>(), L.kin.as<float4>(), L.diam32.as<float>(),
+                              L.st));
+        c->launches += g.ncell > 0 ? 1 : 0;
         if (timing) CK(cudaEventRecord(c->ev[1], L.st));
+        // bond records at a fixed stride of maxb per particle; compacted to CSR only
+        // when the staged (offset << 6 | count) word would not hold the offsets
+        const bool stride = (size_t)std::max(n, 1) * (size_t)c->maxb < ((size_t)1 << 25) &&
+                            !(c->flags & IK_FLAG_CSR_BONDS);
         ENS(L.bonds_tmp, sizeof(float4) * (size_t)c->maxb * std::max(n, 1));
-        ENS(L.bonds32, sizeof(float4) * (size_t)c->maxb * std::max(n, 1));
         ENS(L.nb32, sizeof(int) * (std::max(n, 1) + 1));
-        ENS(L.boff, sizeof(int) * (std::max(n, 1) + 1));
-        ENS(L.bsum, sizeof(int) * ((std::max(n, 1) + 4095) / 4096 + 1));
-        CK(launch_bonds32w(D, g, c->pot, c->cg.kappa, n, L.prec.as<IkPRec>(), L.diam32.as<float>(),
-                           L.cell_start.as<int>(), L.plo.as<float4>(), L.pos64.as<IkB64>(),
-                           L.bonds_tmp.as<float4>(), c->maxb,
-                           L.nb32.as<int>(), c->status.as<int>(), c->maxnb.as<int>(), L.st));
-        CK(launch_scan(L.nb32.as<int>(), n, L.boff.as<int>(), L.bsum.as<int>(), L.st));
-        CK(launch_bond_compact(n, c->maxb, L.nb32.as<int>(), L.boff.as<int>(), L.bonds_tmp.as<float4>(),
-                               L.bonds32.as<float4>(), cnt, L.st));
-        c->launches += 5;
+        CK(launch_bonds32(D, g, c->pot, c->cg.kappa, n, L.prec.as<IkPRec>(), L.diam32.as<float>(),
+                          L.cell_start.as<int>(), L.plo.as<float4>(), L.pos64.as<IkB64>(),
+                          L.bonds_tmp.as<float4>(), c->maxb, L.nb32.as<int>(), c->status.as<int>(),
+                          c->maxnb.as<int>(), stride ? cnt : nullptr, L.st));
+        c->launches += n > 0 ? 1 : 0;
+        if (!stride) {
+            ENS(L.bonds32, sizeof(float4) * (size_t)c->maxb * std::max(n, 1));
+            ENS(L.boff, sizeof(int) * (std::max(n, 1) + 1));
+            ENS(L.bsum, sizeof(int) * ((std::max(n, 1) + 4095) / 4096 + 1));
+            CK(launch_scan(L.nb32.as<int>(), n, L.boff.as<int>(), L.bsum.as<int>(), L.st));
+            CK(launch_bond_compact(n, c->maxb, L.nb32.as<int>(), L.boff.as<int>(), L.bonds_tmp.as<float4>(),
+                                   L.bonds32.as<float4>(), cnt, L.st));
+            c->launches += (n <= 65536 ? 1 : 2) + (n > 0 ? 1 : 0);
+        }
+        const float4* bonds = stride ? L.bonds_tmp.as<float4>() : L.bonds32.as<float4>();
         if (timing) CK(cudaEventRecord(c->ev[2], L.st));
         GatherArgs32 a{};
         a.g = g;
@@ -490,8 +502,9 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         a.prec = L.prec.as<IkPRec>();
         a.pos64 = L.pos64.as<IkB64>();
         a.cell_start = L.cell_start.as<int>();
-        a.boff = L.boff.as<int>();
-        a.bonds = L.bonds32.as<float4>();
+        a.boff = stride ? nullptr : L.boff.as<int>();
+        a.nb = L.nb32.as<int>();
+        a.bonds = bonds;
         a.maxb = c->maxb;
         a.kin = L.kin.as<float4>();
         a.gpts = c->gpts_d.as<float4>();
@@ -530,24 +543,24 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         }
         size_t smem = (size_t)IK_WARPS_GATHER * ((size_t)c->halo_cap * 20 + (size_t)a.qcap * 4);
         int blocks = std::min(c->nitems, c->sm_count * 2);
-        if (blocks > 0)
+        if (blocks > 0) {
             CK(launch_gather32(a, c->cg.kind, (c->flags & IK_FLAG_LANE_KAHAN) != 0 && !mlp, mlp, blocks,
                                32 * IK_WARPS_GATHER, smem, L.st));
+            c->launches += 1;
+        }
         if (mlp) { // the surrogate on the tensor cores for the recorded bonds
             const double to_w = std::sqrt(2.0 / 1.4426950408889634);
             CK(launch_mlp_records(c->mlp, L.mlp_rec.as<float4>(), L.mlp_rid.as<int2>(),
-                                  L.mlp_count.as<unsigned long long>(), c->mlp_cap, L.bonds32.as<float4>(),
+                                  L.mlp_count.as<unsigned long long>(), c->mlp_cap, bonds,
                                   (float)to_w, (float)c->cg.width, NC, L.corr.as<unsigned long long>(),
                                   c->status.as<int>(), c->sm_count * 3, L.st));
             c->launches += 1;
         }
         // FP64 finish: ((double)hi + (double)lo) * normalisation (0.5 of the GL map for the virial)
-        if (a.fields & 1)
-            CK(launch_pairs_to_f64(L.vir2.as<float2>(), mlp ? L.corr.as<unsigned long long>() : nullptr,
-                                   s.vir.as<double>(), (long long)NC * c->G, 0.5 * norm, L.st));
-        if (a.fields & 2) CK(launch_pairs_to_f64(L.kin2.as<float2>(), nullptr, s.kin.as<double>(),
-                                                 (long long)NC * c->G, norm, L.st));
-        c->launches += 2;
+        CK(launch_pairs_to_f64(L.vir2.as<float2>(), mlp ? L.corr.as<unsigned long long>() : nullptr,
+                               (a.fields & 1) ? s.vir.as<double>() : nullptr, 0.5 * norm, L.kin2.as<float2>(),
+                               (a.fields & 2) ? s.kin.as<double>() : nullptr, norm, (long long)NC * c->G, L.st));
+        c->launches += (c->G > 0 && a.fields) ? 1 : 0;
     } else {
         if (timing) CK(cudaEventRecord(c->ev[1], L.st));
         ENS(L.bonds64, sizeof(IkB64) * (size_t)c->maxb * std::max(n, 1));
@@ -585,6 +598,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         if ((fields & IK_FIELD_KINETIC) && !s.has_vel)
             CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->G, L.st));
         CK(launch_gather64(a, L.st));
+        c->launches += (n > 0 ? 1 : 0) + (c->G > 0 ? 1 : 0);
     }
     if (timing) CK(cudaEventRecord(c->ev[3], L.st));
     s.last_prec = prec;

@@ -89,36 +89,33 @@ __device__ __forceinline__ float ik_df_diff(float ohi, float olo, float hj, floa
 }
 
 // ---------------------------------------------------------------------------
-// Force-active bonds of one particle per warp.  The 3^d stencil cells are set up by
-// lanes 0..S-1; their candidates are walked 32 at a time (a lane finds its cell by
-// binary search over the stencil prefix sums).  Each candidate is screened in FP32
-// from the cell-relative positions; survivors are re-measured from the double-float
-// positions, so that r_ij carries only its final FP32 rounding -- the r^-14 force
-// amplifies position rounding for strongly overlapping pairs.  (On axes with fewer
-// than three cells the stencil is not the minimum image; those pairs are re-measured
-// in FP64.)
+// Force-active bonds, one thread per particle (particles in cell order, so that
+// neighbouring threads walk the same candidate cells and their loads hit in L1).
+// Each candidate of the 3^d stencil is screened in FP32 from the cell-relative
+// positions; survivors are re-measured from the double-float positions, so that r_ij
+// carries only its final FP32 rounding -- the r^-14 force amplifies position rounding
+// for strongly overlapping pairs.  (On axes with fewer than three cells the stencil is
+// not the minimum image; those pairs are re-measured in FP64.)
 // Output record (16 B): {hb_x, hb_y, hb_z, f'} with hb = kappa * r_ij / 2 (scaled half
 // bond, r_ij = r_j - r_i) and f' = 2 forceDivR / kappa^2, so that
 // f' * hb (x) hb = 0.5 * forceDivR * r_ij (x) r_ij.  Written at a fixed stride of
-// `maxb` records per particle in candidate order (stencil cell, then ascending
-// sorted index): deterministic.
+// `maxb` records per particle in candidate order (stencil cell with x fastest, then
+// ascending sorted index): deterministic.
 template <int DIM>
-__global__ void __launch_bounds__(256) k_bonds32w(IkGeom g, IkPoly12 pot, float kappa, int n,
+__global__ void __launch_bounds__(128) k_bonds32t(IkGeom g, IkPoly12 pot, float kappa, int n,
                                                   const IkPRec* __restrict__ prec,
                                                   const float* __restrict__ diam32,
                                                   const int* __restrict__ cell_start,
                                                   const float4* __restrict__ plo,
                                                   const IkB64* __restrict__ pos64, float4* __restrict__ tmp,
                                                   int maxb, int* __restrict__ nb, int* __restrict__ status,
-                                                  int* __restrict__ maxnb)
+                                                  int* __restrict__ maxnb, unsigned long long* nbond_total)
 {
-    const int lane = threadIdx.x & 31;
-    const int p = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-    if (p >= n) return; // warp-uniform
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
     const IkPRec me = prec[p];
     const int c = me.cell;
     const int home[3] = {c % g.nc[0], (c / g.nc[0]) % g.nc[1], c / (g.nc[0] * g.nc[1])};
-    // stencil extent per axis
     int lo[3], len[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -126,31 +123,6 @@ __global__ void __launch_bounds__(256) k_bonds32w(IkGeom g, IkPoly12 pot, float 
         else if (g.all_bond[a]) { lo[a] = 0; len[a] = g.nc[a]; }
         else { lo[a] = home[a] - 1; len[a] = 3; }
     }
-    const int S = len[0] * len[1] * len[2]; // <= 27
-    int sstart = 0, scnt = 0;
-    float sox = 0.f, soy = 0.f, soz = 0.f, slx = 0.f, sly = 0.f, slz = 0.f;
-    if (lane < S) {
-        int ix = lane % len[0], iy = (lane / len[0]) % len[1], iz = lane / (len[0] * len[1]);
-        int ux = lo[0] + ix, uy = lo[1] + iy, uz = lo[2] + iz;
-        int wx = ik_wrap(ux, g.nc[0]), wy = ik_wrap(uy, g.nc[1]), wz = DIM == 3 ? ik_wrap(uz, g.nc[2]) : 0;
-        int cell = (wz * g.nc[1] + wy) * g.nc[0] + wx;
-        sstart = cell_start[cell];
-        scnt = cell_start[cell + 1] - sstart;
-        // cell offset as a double-float pair; the offset is -1, 0 or +1 cell widths
-        // (or 0..nc-1 on an axis scanned whole, handled by the FP64 branch below)
-        const float kx = (float)(ux - home[0]), ky = (float)(uy - home[1]), kz = (float)(uz - home[2]);
-        sox = kx * g.cwhi[0]; slx = kx * g.cwlo[0];
-        soy = ky * g.cwhi[1]; sly = ky * g.cwlo[1];
-        soz = DIM == 3 ? kz * g.cwhi[2] : 0.f; slz = DIM == 3 ? kz * g.cwlo[2] : 0.f;
-    }
-    int incl = scnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        int t = __shfl_up_sync(FULL, incl, o);
-        if (lane >= o) incl += t;
-    }
-    const int excl = incl - scnt;
-    const int total = __shfl_sync(FULL, incl, 31);
     const bool allx = len[0] > 3 || (g.all_bond[0] && g.nc[0] > 1);
     const bool ally = len[1] > 3 || (g.all_bond[1] && g.nc[1] > 1);
     const bool allz = DIM == 3 && (len[2] > 3 || (g.all_bond[2] && g.nc[2] > 1));
@@ -160,45 +132,47 @@ __global__ void __launch_bounds__(256) k_bonds32w(IkGeom g, IkPoly12 pot, float 
                 c2x4 = (float)(4.0 * pot.c2);
     const float screen = 1.0f + 1e-4f;
     const float di = diam32[p];
-    const IkB64 pi = pos64[p];
     const float4 mlo = plo[p];
     const float hk = 0.5f * kappa, fk = 2.0f / (kappa * kappa);
+    float4* out = tmp + (size_t)p * maxb;
     int cnt = 0;
-    for (int base = 0; base < total; base += 32) {
-        const int v = base + lane;
-        // stencil slot of candidate v: largest s with excl_s <= v (binary search)
-        int s = 0;
-#pragma unroll
-        for (int step = 16; step >= 1; step >>= 1) {
-            int t = s + step;
-            int et = __shfl_sync(FULL, excl, t & 31);
-            if (t < S && et <= v) s = t;
-        }
-        const int qs = __shfl_sync(FULL, sstart, s), qe = __shfl_sync(FULL, excl, s);
-        const float ox = __shfl_sync(FULL, sox, s), oy = __shfl_sync(FULL, soy, s), oz = __shfl_sync(FULL, soz, s);
-        const float olx = __shfl_sync(FULL, slx, s), oly = __shfl_sync(FULL, sly, s), olz = __shfl_sync(FULL, slz, s);
-        bool act = false;
-        float4 rec = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (v < total) {
-            const int q = qs + (v - qe);
-            if (q != p) {
-                const IkPRec o = prec[q];
-                float bx = ox + (o.x - me.x), by = oy + (o.y - me.y), bz = DIM == 3 ? oz + (o.z - me.z) : 0.f;
-                if (allx) bx -= L0 * rintf(bx / L0);
-                if (ally) by -= L1 * rintf(by / L1);
-                if (allz) bz -= L2 * rintf(bz / L2);
-                float r2 = bx * bx + by * by + bz * bz;
-                const float dj = diam32[q];
-                const float sig = 0.5f * (di + dj) * (1.f - eps * fabsf(di - dj));
-                const float s2 = sig * sig;
-                if (r2 < mr2 * screen && r2 < rc2 * s2 * screen) {
+    for (int iz = 0; iz < len[2]; ++iz) {
+        const int uz = lo[2] + iz;
+        const int wz = DIM == 3 ? ik_wrap(uz, g.nc[2]) : 0;
+        const float kz = (float)(uz - home[2]);
+        const float oz = DIM == 3 ? kz * g.cwhi[2] : 0.f, olz = DIM == 3 ? kz * g.cwlo[2] : 0.f;
+        for (int iy = 0; iy < len[1]; ++iy) {
+            const int uy = lo[1] + iy;
+            const int wy = ik_wrap(uy, g.nc[1]);
+            const float ky = (float)(uy - home[1]);
+            const float oy = ky * g.cwhi[1], oly = ky * g.cwlo[1];
+            for (int ix = 0; ix < len[0]; ++ix) {
+                const int ux = lo[0] + ix;
+                const int wx = ik_wrap(ux, g.nc[0]);
+                const float kx = (float)(ux - home[0]);
+                const float ox = kx * g.cwhi[0], olx = kx * g.cwlo[0];
+                const int cell = (wz * g.nc[1] + wy) * g.nc[0] + wx;
+                const int qe = cell_start[cell + 1];
+                for (int q = cell_start[cell]; q < qe; ++q) {
+                    if (q == p) continue;
+                    const IkPRec o = prec[q];
+                    float bx = ox + (o.x - me.x), by = oy + (o.y - me.y), bz = DIM == 3 ? oz + (o.z - me.z) : 0.f;
+                    if (allx) bx -= L0 * rintf(bx / L0);
+                    if (ally) by -= L1 * rintf(by / L1);
+                    if (allz) bz -= L2 * rintf(bz / L2);
+                    float r2 = bx * bx + by * by + bz * bz;
+                    if (!(r2 < mr2 * screen)) continue;
+                    const float dj = diam32[q];
+                    const float sig = 0.5f * (di + dj) * (1.f - eps * fabsf(di - dj));
+                    const float s2 = sig * sig;
+                    if (!(r2 < rc2 * s2 * screen)) continue;
                     if (!(allx || ally || allz)) {
                         const float4 lq = plo[q];
                         bx = ik_df_diff(ox, olx, o.x, lq.x, me.x, mlo.x);
                         by = ik_df_diff(oy, oly, o.y, lq.y, me.y, mlo.y);
                         if (DIM == 3) bz = ik_df_diff(oz, olz, o.z, lq.z, me.z, mlo.z);
                     } else {
-                        const IkB64 pj = pos64[q];
+                        const IkB64 pi = pos64[p], pj = pos64[q];
                         double dx = pj.x - pi.x, dy = pj.y - pi.y;
                         dx = fma(-g.L[0], rint(dx * g.invL[0]), dx);
                         dy = fma(-g.L[1], rint(dy * g.invL[1]), dy);
@@ -215,23 +189,22 @@ __global__ void __launch_bounds__(256) k_bonds32w(IkGeom g, IkPoly12 pot, float 
                         const float r2inv = s2 / r2;
                         const float r6 = r2inv * r2inv * r2inv;
                         const float f = (v12 * r2inv * r6 * r6 - c1x2 - c2x4 * (r2 / s2)) / s2;
-                        rec = make_float4(hk * bx, hk * by, hk * bz, fk * f);
-                        act = true;
+                        if (cnt < maxb) out[cnt] = make_float4(hk * bx, hk * by, hk * bz, fk * f);
+                        ++cnt;
                     }
                 }
             }
         }
-        const unsigned bal = __ballot_sync(FULL, act);
-        const int rank = __popc(bal & ((1u << lane) - 1u));
-        if (act && cnt + rank < maxb) tmp[(size_t)p * maxb + cnt + rank] = rec;
-        cnt += __popc(bal);
     }
-    if (lane == 0) {
-        nb[p] = cnt < maxb ? cnt : maxb;
-        if (cnt > maxb) { // rare: grow the capacity and recompute (host side)
-            atomicOr(status, IK_ST_BOND_OVERFLOW);
-            atomicMax(maxnb, cnt);
-        }
+    nb[p] = cnt < maxb ? cnt : maxb;
+    if (cnt > maxb) { // rare: grow the capacity and recompute (host side)
+        atomicOr(status, IK_ST_BOND_OVERFLOW);
+        atomicMax(maxnb, cnt);
+    }
+    if (nbond_total) { // force-active directed bonds of the frame (one atomic per warp)
+        const unsigned act = __activemask();
+        const int tot = __reduce_add_sync(act, cnt);
+        if ((threadIdx.x & 31) == __ffs(act) - 1) atomicAdd(nbond_total, (unsigned long long)tot);
     }
 }
 
@@ -327,6 +300,10 @@ __global__ void __launch_bounds__(1024) k_scan_apply(const int* __restrict__ in,
 
 cudaError_t launch_scan(const int* in, int n, int* out, int* bsum, cudaStream_t st)
 {
+    if (n <= 65536) { // one CTA walks the tiles with a carry: one launch
+        k_scan<<<1, 1024, 0, st>>>(in, n, out);
+        return cudaGetLastError();
+    }
     int blocks = (n + 4095) / 4096;
     if (blocks < 1) blocks = 1;
     k_scan_sums<<<blocks, 1024, 0, st>>>(in, n, bsum);
@@ -342,6 +319,59 @@ cudaError_t launch_bin32(const double* pos, int n, IkGeom g, int* cell_of, int* 
     return cudaGetLastError();
 }
 
+// Sort the ids of each cell (insertion sort: cells hold a handful of particles; fixes
+// the order the atomic ranks left) and pack the cell's particles in that order: the
+// two steps of k_cell_sort_pack + k_pack32 in one launch, one thread per cell.
+__global__ void k_cell_sort_pack32(IkGeom g, const int* __restrict__ cell_start, int* __restrict__ sorted,
+                                   const float4* __restrict__ relhi, const float4* __restrict__ rello,
+                                   const double* __restrict__ pos, const double* __restrict__ vel,
+                                   const double* __restrict__ mass, const double* __restrict__ diam,
+                                   IkPRec* __restrict__ prec, float4* __restrict__ plo, IkB64* __restrict__ pos64,
+                                   float4* __restrict__ kin, float* __restrict__ diam32)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.ncell) return;
+    const int s = cell_start[c], e = cell_start[c + 1];
+    for (int a = s + 1; a < e; ++a) {
+        const int v = sorted[a];
+        int b = a - 1;
+        while (b >= s && sorted[b] > v) { sorted[b + 1] = sorted[b]; --b; }
+        sorted[b + 1] = v;
+    }
+    for (int p = s; p < e; ++p) {
+        const int i = sorted[p];
+        const float4 h = relhi[i];
+        IkPRec r;
+        r.x = h.x;
+        r.y = h.y;
+        r.z = h.z;
+        r.cell = c;
+        prec[p] = r;
+        plo[p] = rello[i];
+        pos64[p] = make_ikb64(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.0);
+        const double m = mass ? mass[i] : 1.0;
+        const double vx = vel ? vel[3 * i] : 0.0, vy = vel ? vel[3 * i + 1] : 0.0, vz = vel ? vel[3 * i + 2] : 0.0;
+        if (g.dim == 2) {
+            kin[p] = make_float4((float)(m * vx * vx), (float)(m * vy * vy), (float)(m * vx * vy), 0.f);
+        } else {
+            kin[2 * p] = make_float4((float)(m * vx * vx), (float)(m * vy * vy), (float)(m * vz * vz),
+                                     (float)(m * vx * vy));
+            kin[2 * p + 1] = make_float4((float)(m * vx * vz), (float)(m * vy * vz), 0.f, 0.f);
+        }
+        diam32[p] = (float)diam[i];
+    }
+}
+
+cudaError_t launch_sort_pack32(IkGeom g, const int* cell_start, int* sorted, const float4* relhi, const float4* rello,
+                               const double* pos, const double* vel, const double* mass, const double* diam,
+                               IkPRec* prec, float4* plo, IkB64* pos64, float4* kin, float* diam32, cudaStream_t st)
+{
+    if (g.ncell <= 0) return cudaSuccess;
+    k_cell_sort_pack32<<<(g.ncell + 127) / 128, 128, 0, st>>>(g, cell_start, sorted, relhi, rello, pos, vel, mass,
+                                                              diam, prec, plo, pos64, kin, diam32);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_pack32(IkGeom g, int n, const int* sorted, const int* cell_of, const float4* relhi,
                           const float4* rello, const double* pos, const double* vel, const double* mass,
                           const double* diam, IkPRec* prec, float4* plo, IkB64* pos64, float4* kin, float* diam32,
@@ -353,19 +383,20 @@ cudaError_t launch_pack32(IkGeom g, int n, const int* sorted, const int* cell_of
     return cudaGetLastError();
 }
 
-cudaError_t launch_bonds32w(int dim, IkGeom g, IkPoly12 pot, float kappa, int n, const IkPRec* prec,
+cudaError_t launch_bonds32(int dim, IkGeom g, IkPoly12 pot, float kappa, int n, const IkPRec* prec,
                             const float* diam32, const int* cell_start, const float4* plo, const IkB64* pos64,
-                            float4* tmp, int maxb, int* nb, int* status, int* maxnb, cudaStream_t st)
+                            float4* tmp, int maxb, int* nb, int* status, int* maxnb,
+                            unsigned long long* nbond_total, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
-    const int wpb = 8;
-    int blocks = (n + wpb - 1) / wpb;
+    const int threads = 128;
+    const int blocks = (n + threads - 1) / threads;
     if (dim == 2)
-        k_bonds32w<2><<<blocks, 32 * wpb, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, plo, pos64, tmp, maxb,
-                                                   nb, status, maxnb);
+        k_bonds32t<2><<<blocks, threads, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, plo, pos64, tmp, maxb,
+                                                  nb, status, maxnb, nbond_total);
     else
-        k_bonds32w<3><<<blocks, 32 * wpb, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, plo, pos64, tmp, maxb,
-                                                   nb, status, maxnb);
+        k_bonds32t<3><<<blocks, threads, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, plo, pos64, tmp, maxb,
+                                                  nb, status, maxnb, nbond_total);
     return cudaGetLastError();
 }
 

@@ -286,12 +286,14 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                     for (int t = 0; t < ccnt; ++t) {
                         int q = cstart + t;
                         IkPRec r = a.prec[q];
-                        int b0 = a.boff[q], b1 = a.boff[q + 1];
+                        int b0, nbq;
+                        if (a.boff) { b0 = a.boff[q]; nbq = a.boff[q + 1] - b0; }
+                        else { b0 = q * a.maxb; nbq = a.nb[q]; }
                         float4 s;
                         s.x = fmaf(kappa, r.x, ox);
                         s.y = fmaf(kappa, r.y, oy);
                         s.z = DIM == 3 ? fmaf(kappa, r.z, oz) : 0.f;
-                        s.w = __int_as_float((b0 << 6) | (b1 - b0));
+                        s.w = __int_as_float((b0 << 6) | nbq);
                         stage[dst + t] = s;
                         sq[dst + t] = q;
                     }
@@ -695,22 +697,29 @@ cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, bool ml
 
 // Double-float pairs -> FP64, scaled: out = ((double)hi + (double)lo) * scale.  One
 // thread per value (fully populated warps: the FP64 pipe is narrow on this GPU).
-// With surrogate corrections (fixed point, 2^-32 units) added before scaling.
-__global__ void k_pairs_to_f64(const float2* __restrict__ in, const unsigned long long* __restrict__ corr,
-                               double* __restrict__ out, int count, double scale)
+// With surrogate corrections (fixed point, 2^-32 units) added to the virial before scaling.
+__global__ void k_pairs_to_f64(const float2* __restrict__ vin, const unsigned long long* __restrict__ corr,
+                               double* __restrict__ vout, double svir, const float2* __restrict__ kin,
+                               double* __restrict__ kout, double skin, int count)
 {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= count) return;
-    const float2 v = in[k];
-    double s = (double)v.x + (double)v.y;
-    if (corr) s += (double)(long long)corr[k] * 2.3283064365386963e-10;
-    out[k] = s * scale;
+    if (vout) {
+        const float2 v = vin[k];
+        double s = (double)v.x + (double)v.y;
+        if (corr) s += (double)(long long)corr[k] * 2.3283064365386963e-10;
+        vout[k] = s * svir;
+    }
+    if (kout) {
+        const float2 v = kin[k];
+        kout[k] = ((double)v.x + (double)v.y) * skin;
+    }
 }
 
-cudaError_t launch_pairs_to_f64(const float2* in, const unsigned long long* corr, double* out, long long count,
-                                double scale, cudaStream_t st)
+cudaError_t launch_pairs_to_f64(const float2* vin, const unsigned long long* corr, double* vout, double svir,
+                                const float2* kin, double* kout, double skin, long long count, cudaStream_t st)
 {
-    if (count <= 0) return cudaSuccess;
-    k_pairs_to_f64<<<(int)((count + 255) / 256), 256, 0, st>>>(in, corr, out, (int)count, scale);
+    if (count <= 0 || (!vout && !kout)) return cudaSuccess;
+    k_pairs_to_f64<<<(int)((count + 255) / 256), 256, 0, st>>>(vin, corr, vout, svir, kin, kout, skin, (int)count);
     return cudaGetLastError();
 }

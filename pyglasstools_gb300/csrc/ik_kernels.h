@@ -18,9 +18,14 @@ cudaError_t launch_pack32(IkGeom g, int n, const int* sorted, const int* cell_of
                           const float4* rello, const double* pos, const double* vel, const double* mass,
                           const double* diam, IkPRec* prec, float4* plo, IkB64* pos64, float4* kin, float* diam32,
                           cudaStream_t st);
-cudaError_t launch_bonds32w(int dim, IkGeom g, IkPoly12 pot, float kappa, int n, const IkPRec* prec,
+cudaError_t launch_sort_pack32(IkGeom g, const int* cell_start, int* sorted, const float4* relhi, const float4* rello,
+                               const double* pos, const double* vel, const double* mass, const double* diam,
+                               IkPRec* prec, float4* plo, IkB64* pos64, float4* kin, float* diam32, cudaStream_t st);
+// nbond_total (may be null): += force-active directed bonds
+cudaError_t launch_bonds32(int dim, IkGeom g, IkPoly12 pot, float kappa, int n, const IkPRec* prec,
                             const float* diam32, const int* cell_start, const float4* plo, const IkB64* pos64,
-                            float4* tmp, int maxb, int* nb, int* status, int* maxnb, cudaStream_t st);
+                            float4* tmp, int maxb, int* nb, int* status, int* maxnb,
+                            unsigned long long* nbond_total, cudaStream_t st);
 cudaError_t launch_bond_compact(int n, int maxb, const int* nb, const int* boff, const float4* tmp, float4* bonds,
                                 unsigned long long* nbond_total, cudaStream_t st);
 // exclusive scan of n ints into out[0..n]; bsum needs ceil(n / 4096) ints
@@ -53,7 +58,9 @@ struct GatherArgs32 {
     const IkPRec* prec;
     const IkB64* pos64;    // raw FP64 positions in cell order
     const int* cell_start;
-    const int* boff;       // CSR offsets of the bond records (n + 1)
+    const int* boff;       // CSR offsets of the bond records (n + 1), or null: records of
+                           // particle q at q * maxb (fixed stride), nb[q] of them
+    const int* nb;
     const float4* bonds;   // {kappa r_ij / 2, 2 forceDivR / kappa^2}
     int maxb;
     const float4* kin;
@@ -81,9 +88,10 @@ struct GatherArgs32 {
 #define IK_MLP_CHUNK 2048
 cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, bool mlp, int blocks, int threads,
                             size_t smem, cudaStream_t st);
-// out = ((double)hi + (double)lo + corr * 2^-32) * scale   (corr: fixed-point, may be null)
-cudaError_t launch_pairs_to_f64(const float2* in, const unsigned long long* corr, double* out, long long count,
-                                double scale, cudaStream_t st);
+// vir = ((double)hi + (double)lo + corr * 2^-32) * svir   (corr: fixed point, may be null),
+// kin = ((double)hi + (double)lo) * skin; a null output is skipped.  One launch.
+cudaError_t launch_pairs_to_f64(const float2* vin, const unsigned long long* corr, double* vout, double svir,
+                                const float2* kin, double* kout, double skin, long long count, cudaStream_t st);
 
 // ---- FP64 plain gather (ik_gather64.cu) ------------------------------------
 struct GatherArgs64 {

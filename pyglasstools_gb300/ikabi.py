@@ -21,7 +21,7 @@ CG = {"octic": 0, "gaussian": 1, "rect": 2, "mollifier": 3}
 QUAD = {"fixedpoint": 0, "adaptive": 1, "exact": 2, "mlp": 3}
 PREC = {"fp64": 0, "fp32": 1}
 FIELD_VIRIAL, FIELD_KINETIC = 1, 2
-FLAG_TIMING, FLAG_LANE_KAHAN = 1, 2
+FLAG_TIMING, FLAG_LANE_KAHAN, FLAG_CSR_BONDS = 1, 2, 4
 
 _lib = None
 

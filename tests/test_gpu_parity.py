@@ -288,6 +288,10 @@ def test_fp32_deterministic_and_order_independent(ik):
     a, _, _ = run_gpu(ik, 2, f.L, f.pos, f.diam, grid, cg, "fp32")
     b, _, _ = run_gpu(ik, 2, f.L, f.pos, f.diam, grid, cg, "fp32")
     assert np.array_equal(a, b)  # no float atomics: bitwise reproducible
+    # bond records compacted to CSR (the layout of very large frames): same records, same sums
+    a_csr, _, cnt_csr = run_gpu(ik, 2, f.L, f.pos, f.diam, grid, cg, "fp32", flags=ik.FLAG_CSR_BONDS)
+    _, _, cnt = run_gpu(ik, 2, f.L, f.pos, f.diam, grid, cg, "fp32")
+    assert np.array_equal(a, a_csr) and cnt == cnt_csr
     perm = np.random.default_rng(0).permutation(len(f.pos))
     c, _, _ = run_gpu(ik, 2, f.L, f.pos[perm], f.diam[perm], grid, cg, "fp64")
     d, _, _ = run_gpu(ik, 2, f.L, f.pos, f.diam, grid, cg, "fp64")
