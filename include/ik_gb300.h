@@ -193,6 +193,16 @@ int ik_get_launch_count(ik_ctx* ctx, int64_t* out);
 /* Counters of the last computation: [0] force-active directed bonds,
  * [1] accepted (grid, particle) pairs, [2] active (grid, i, j) triples (FP32 path). */
 int ik_get_counters(ik_ctx* ctx, int slot, int64_t* out3);
+/* Tuning of the FP32 gather (no reference counterpart).  0 restores the default.
+ *   IK_TUNE_BIN_POINTS     target grid points per work item (bin of cells)
+ *   IK_TUNE_BLOCKS_PER_SM  persistent CTAs launched per SM
+ *   IK_TUNE_HALO_CAP       staged halo particles per warp (grows on overflow) */
+#define IK_TUNE_BIN_POINTS 1
+#define IK_TUNE_BLOCKS_PER_SM 2
+#define IK_TUNE_HALO_CAP 3
+int ik_set_tuning(ik_ctx* ctx, int param, int value);
+int ik_get_tuning(ik_ctx* ctx, int param, int* value);
+
 /* Bonds the last surrogate-mode computation of `slot` handed to the network (crossing
  * the edge of the support; each falls back on its fixed-point value outside the
  * validated bins).  No reference counterpart. */

@@ -142,6 +142,8 @@ struct ik_ctx {
     std::vector<Slot> slots;
     std::vector<PendingOp> pending;
     ik_mlp* mlp = nullptr; // learned bond-integral surrogate (IK_QUAD_MLP)
+    // tuning of the FP32 gather (0 = default)
+    int tune_bin_points = 0, tune_blocks_per_sm = 0;
     long long mlp_cap = 0;  // record capacity per lane
     // CUDA-graph replay of ik_compute_batch
     bool capturing = false;
@@ -242,7 +244,7 @@ int ensure_geometry(ik_ctx* c)
     double cellvol = 1.0, boxvol = 1.0;
     for (int a = 0; a < c->dim; ++a) { cellvol *= g.cw[a]; boxvol *= g.L[a]; }
     double pts_per_cell = c->G > 0 ? (double)c->G * cellvol / boxvol : 1.0;
-    double target = c->dim == 2 ? 20.0 : 24.0;
+    double target = c->tune_bin_points > 0 ? (double)c->tune_bin_points : (c->dim == 2 ? 20.0 : 24.0);
     int bwv = (int)std::lround(std::pow(std::max(target / std::max(pts_per_cell, 1e-9), 1.0), 1.0 / c->dim));
     bwv = std::max(1, std::min(bwv, 8));
     for (int a = 0; a < 3; ++a) {
@@ -542,7 +544,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
             a.cnt_records = cnt + 3;
         }
         size_t smem = (size_t)IK_WARPS_GATHER * ((size_t)c->halo_cap * 20 + (size_t)a.qcap * 4);
-        int blocks = std::min(c->nitems, c->sm_count * 2);
+        int blocks = std::min(c->nitems, c->sm_count * (c->tune_blocks_per_sm > 0 ? c->tune_blocks_per_sm : 2));
         if (blocks > 0) {
             CK(launch_gather32(a, c->cg.kind, (c->flags & IK_FLAG_LANE_KAHAN) != 0 && !mlp, mlp, blocks,
                                32 * IK_WARPS_GATHER, smem, L.st));
@@ -1228,6 +1230,41 @@ int ik_set_mlp(ik_ctx* c, ik_mlp* m)
     ++c->config_version; // captured batch graphs hold the old settings
     c->mlp = m;
     return IK_OK;
+}
+
+int ik_set_tuning(ik_ctx* c, int param, int value)
+{
+    if (int r = check_ctx(c)) return r;
+    ++c->config_version; // captured batch graphs hold the old settings
+    switch (param) {
+    case IK_TUNE_BIN_POINTS:
+        if (value < 0 || value > 4096) return fail(IK_ERR_ARG, "bin points must be in [0, 4096]");
+        c->tune_bin_points = value;
+        c->geom_valid = false;
+        return IK_OK;
+    case IK_TUNE_BLOCKS_PER_SM:
+        if (value < 0 || value > 16) return fail(IK_ERR_ARG, "blocks per SM must be in [0, 16]");
+        c->tune_blocks_per_sm = value;
+        return IK_OK;
+    case IK_TUNE_HALO_CAP:
+        if (value < 0 || value > 8192) return fail(IK_ERR_ARG, "halo capacity must be in [0, 8192]");
+        c->halo_cap = value;
+        return IK_OK;
+    default:
+        return fail(IK_ERR_ARG, "unknown tuning parameter %d", param);
+    }
+}
+
+int ik_get_tuning(ik_ctx* c, int param, int* value)
+{
+    if (int r = check_ctx(c)) return r;
+    if (!value) return fail(IK_ERR_ARG, "null output");
+    switch (param) {
+    case IK_TUNE_BIN_POINTS: *value = c->tune_bin_points; return IK_OK;
+    case IK_TUNE_BLOCKS_PER_SM: *value = c->tune_blocks_per_sm; return IK_OK;
+    case IK_TUNE_HALO_CAP: *value = c->halo_cap; return IK_OK;
+    default: return fail(IK_ERR_ARG, "unknown tuning parameter %d", param);
+    }
 }
 
 int ik_set_flags(ik_ctx* c, int flags)

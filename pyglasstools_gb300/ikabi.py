@@ -22,6 +22,7 @@ QUAD = {"fixedpoint": 0, "adaptive": 1, "exact": 2, "mlp": 3}
 PREC = {"fp64": 0, "fp32": 1}
 FIELD_VIRIAL, FIELD_KINETIC = 1, 2
 FLAG_TIMING, FLAG_LANE_KAHAN, FLAG_CSR_BONDS = 1, 2, 4
+TUNE = {"bin_points": 1, "blocks_per_sm": 2, "halo_cap": 3}
 
 _lib = None
 
@@ -75,6 +76,8 @@ def lib():
             "ik_wait_all": ([vp], i32),
             "ik_compute_batch": ([vp, C.POINTER(C.c_int), i32, i32, i32], i32),
             "ik_set_mlp": ([vp, vp], i32),
+            "ik_set_tuning": ([vp, i32, i32], i32),
+            "ik_get_tuning": ([vp, i32, C.POINTER(C.c_int)], i32),
             "ik_get_mlp_records": ([vp, i32, C.POINTER(C.c_int64)], i32),
             "ik_mlp_create": ([C.POINTER(vp), i32], i32),
             "ik_mlp_destroy": ([vp], i32),
@@ -190,6 +193,14 @@ class IKContext:
 
     def compute_slot(self, slot, precision="fp32", fields=FIELD_VIRIAL | FIELD_KINETIC):
         check(lib().ik_compute_slot(self._h, slot, PREC[precision], fields))
+
+    def set_tuning(self, param, value):
+        check(lib().ik_set_tuning(self._h, TUNE[param], int(value)))
+
+    def get_tuning(self, param):
+        v = C.c_int()
+        check(lib().ik_get_tuning(self._h, TUNE[param], C.byref(v)))
+        return v.value
 
     def set_mlp(self, mlp):
         """Attach a validated surrogate (MLP) used by cgfunc mode "mlp" on the FP32 path."""
