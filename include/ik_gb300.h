@@ -202,6 +202,11 @@ int ik_get_counters(ik_ctx* ctx, int slot, int64_t* out3);
 #define IK_TUNE_HALO_CAP 3
 int ik_set_tuning(ik_ctx* ctx, int param, int value);
 int ik_get_tuning(ik_ctx* ctx, int param, int* value);
+/* Autotuner: times ik_compute_batch over the given slots (`reps` CUDA-graph replays per
+ * candidate, CUDA events on the context's stream) for each candidate bin size x CTAs
+ * per SM, keeps the fastest and reports it.  FP32 path only. */
+int ik_autotune_batch(ik_ctx* ctx, const int* slots, int count, int precision, int fields, int reps,
+                      int* best_bin_points, int* best_blocks_per_sm, float* best_ms);
 
 /* Bonds the last surrogate-mode computation of `slot` handed to the network (crossing
  * the edge of the support; each falls back on its fixed-point value outside the

@@ -1255,6 +1255,52 @@ int ik_set_tuning(ik_ctx* c, int param, int value)
     }
 }
 
+// Time the batch under each candidate (bin points x CTAs per SM), keep the fastest.
+int ik_autotune_batch(ik_ctx* c, const int* slots, int count, int precision, int fields, int reps,
+                      int* best_bin_points, int* best_blocks_per_sm, float* best_ms)
+{
+    if (int r = check_ctx(c)) return r;
+    if (reps < 1 || reps > 1000) return fail(IK_ERR_ARG, "reps must be in [1, 1000]");
+    if (precision != IK_PREC_FP32) return fail(IK_ERR_ARG, "the autotuner tunes the FP32 path");
+    static const int bins_2d[] = {12, 16, 20, 25, 36};
+    static const int bins_3d[] = {16, 24, 48, 96};
+    static const int blocks[] = {1, 2};
+    if (int r = ensure_ready(c)) return r;
+    const int* bins = c->dim == 3 ? bins_3d : bins_2d;
+    const int nbins = c->dim == 3 ? 4 : 5;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); return fail(IK_ERR_CUDA, "event creation failed"); }
+    float best = 1e30f;
+    int bb = 0, bk = 0, rc = IK_OK;
+    for (int i = 0; i < nbins && rc == IK_OK; ++i)
+        for (int k = 0; k < 2 && rc == IK_OK; ++k) {
+            if ((rc = ik_set_tuning(c, IK_TUNE_BIN_POINTS, bins[i])) ||
+                (rc = ik_set_tuning(c, IK_TUNE_BLOCKS_PER_SM, blocks[k])) ||
+                (rc = ik_compute_batch(c, slots, count, precision, fields)) || // plain run + graph recording
+                (rc = ik_compute_batch(c, slots, count, precision, fields)) || (rc = ik_wait_all(c)))
+                break;
+            if (cudaEventRecord(e0, c->stream) != cudaSuccess) { rc = fail(IK_ERR_CUDA, "event record failed"); break; }
+            for (int t = 0; t < reps && rc == IK_OK; ++t) rc = ik_compute_batch(c, slots, count, precision, fields);
+            if (rc || (rc = ik_wait_all(c))) break;
+            float ms = 0.f;
+            if (cudaEventRecord(e1, c->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) { rc = fail(IK_ERR_CUDA, "event timing failed"); break; }
+            if ((rc = ik_synchronize(c))) break;
+            ms /= (float)reps;
+            if (ms < best) { best = ms; bb = bins[i]; bk = blocks[k]; }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (int r = ik_set_tuning(c, IK_TUNE_BIN_POINTS, bb)) return r;
+    if (int r = ik_set_tuning(c, IK_TUNE_BLOCKS_PER_SM, bk)) return r;
+    if (best_bin_points) *best_bin_points = bb;
+    if (best_blocks_per_sm) *best_blocks_per_sm = bk;
+    if (best_ms) *best_ms = best;
+    return IK_OK;
+}
+
 int ik_get_tuning(ik_ctx* c, int param, int* value)
 {
     if (int r = check_ctx(c)) return r;

@@ -78,6 +78,8 @@ def lib():
             "ik_set_mlp": ([vp, vp], i32),
             "ik_set_tuning": ([vp, i32, i32], i32),
             "ik_get_tuning": ([vp, i32, C.POINTER(C.c_int)], i32),
+            "ik_autotune_batch": ([vp, C.POINTER(C.c_int), i32, i32, i32, i32, C.POINTER(C.c_int),
+                                   C.POINTER(C.c_int), C.POINTER(C.c_float)], i32),
             "ik_get_mlp_records": ([vp, i32, C.POINTER(C.c_int64)], i32),
             "ik_mlp_create": ([C.POINTER(vp), i32], i32),
             "ik_mlp_destroy": ([vp], i32),
@@ -201,6 +203,14 @@ class IKContext:
         v = C.c_int()
         check(lib().ik_get_tuning(self._h, TUNE[param], C.byref(v)))
         return v.value
+
+    def autotune_batch(self, slots, precision="fp32", fields=FIELD_VIRIAL | FIELD_KINETIC, reps=3):
+        """Time the batch under each candidate tuning, keep the fastest; returns it."""
+        arr = (C.c_int * len(slots))(*slots)
+        bp, bk, ms = C.c_int(), C.c_int(), C.c_float()
+        check(lib().ik_autotune_batch(self._h, arr, len(slots), PREC[precision], fields, reps, C.byref(bp),
+                                      C.byref(bk), C.byref(ms)))
+        return {"bin_points": bp.value, "blocks_per_sm": bk.value, "ms_per_batch": ms.value}
 
     def set_mlp(self, mlp):
         """Attach a validated surrogate (MLP) used by cgfunc mode "mlp" on the FP32 path."""

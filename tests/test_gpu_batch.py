@@ -138,3 +138,26 @@ def test_batch_argument_errors():
     c.compute_batch([0], "fp32")
     c.synchronize()
     c.close()
+
+
+def test_autotuner_picks_a_candidate_and_keeps_results():
+    """The autotuner times each candidate bin size x CTAs per SM on the batch and keeps
+    the fastest; results under every tuning agree within the FP32 tolerance."""
+    from pyglasstools_gb300 import ikabi as ik, synth
+    F, n = 4, 6000
+    fr = _frames(n, range(500, 500 + F))
+    L = fr[0].L
+    grid = synth.lattice_grid(L, 60, 2)
+    c = _context(ik, L, grid, F)
+    _upload(c, fr)
+    slots = list(range(F))
+    before = _batch(ik, c, slots, "fp32")
+    best = c.autotune_batch(slots, "fp32", reps=2)
+    assert best["bin_points"] in (12, 16, 20, 25, 36) and best["blocks_per_sm"] in (1, 2)
+    assert best["ms_per_batch"] > 0
+    assert c.get_tuning("bin_points") == best["bin_points"]
+    after = _batch(ik, c, slots, "fp32")
+    for (va, ka), (vb, kb) in zip(after, before):
+        assert np.all(rel_l2(uniq(va), uniq(vb)) <= FP32_TOL)
+        assert np.all(rel_l2(uniq(ka), uniq(kb)) <= FP32_TOL)
+    c.close()
