@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--frames", type=int, default=0, help="override the frames per step (profiling)")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate leg")
+    ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch leg")
     ap.add_argument("--no-graph", action="store_true",
                     help="enqueue every frame with its own launches instead of one CUDA-graph replay per step")
     ap.add_argument("--profile", action="store_true",
@@ -272,6 +273,65 @@ def surrogate_leg(args, ctx, wl, F, stream, all_slots, v_plain):
     return out
 
 
+# ---------------------------------------------------------------------------- uneven batch leg
+def uneven_leg(args):
+    """256 seeded 2D frames with N log-uniform on [1000, 128000] (density 1, each frame
+    its own box and a grid of spacing ~1), Gaussian w = 2 cut at 6: the batch replayed
+    as one CUDA graph with the autotuner's bin size and CTAs per SM, against the same
+    frames launched one by one with the default tuning."""
+    import torch
+    from pyglasstools_gb300 import ikabi, synth
+    rng = np.random.default_rng(2024)
+    F = 256
+    Ns = np.exp(rng.uniform(np.log(1000.0), np.log(128000.0), F)).astype(int)
+    c = ikabi.IKContext(torch.cuda.current_device())
+    c.set_poly12()
+    c.set_cgfunc("gaussian", 6.0, order=5, width=2.0)
+    c.reserve_slots(F)
+    c.set_max_rcut(1.25 * 1.62)
+    G_total = 0
+    for k, n in enumerate(Ns):
+        f = synth.make_frame(int(n), dim=2, seed=5000 + k)
+        grid = synth.lattice_grid(f.L, max(int(f.L), 2), 2)
+        G_total += len(grid)
+        c.set_slot_geometry(k, 2, [f.L, f.L, 1.0], grid)
+        c.upload_frame(k, f.pos, f.diam, f.vel, f.mass)
+    c.synchronize()
+    slots = list(range(F))
+    stream = torch.cuda.ExternalStream(c.stream())
+    reps = max(3, min(args.steps, 10))
+
+    def timed(fn):
+        fn()
+        c.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        c.wait_all()
+        e1.record(stream)
+        c.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def per_frame():
+        for k in slots:
+            c.compute_slot(k, "fp32")
+
+    ms_plain = timed(per_frame)
+    best = c.autotune_batch(slots, "fp32", reps=2)
+    l0 = c.launch_count()
+    ms_graph = timed(lambda: c.compute_batch(slots, "fp32"))
+    launches = (c.launch_count() - l0) // (reps + 1)
+    c.close()
+    return {"workload": "256 frames, N log-uniform [1000, 128000], own box and grid (spacing ~1), Gaussian w=2 R=6",
+            "particles": int(Ns.sum()), "grid_points": int(G_total),
+            "per_frame_launches": {"frames_per_s": F / (ms_plain * 1e-3), "ms_per_batch": ms_plain},
+            "graph_autotuned": {"frames_per_s": F / (ms_graph * 1e-3), "ms_per_batch": ms_graph,
+                                "tuning": best, "kernel_launches_per_batch": int(launches)},
+            "speedup": ms_plain / ms_graph}
+
+
 # ---------------------------------------------------------------------------- our arm
 def ours(args, wl, name):
     import torch
@@ -438,6 +498,9 @@ def ours(args, wl, name):
     surrogate = None
     if not args.no_surrogate and wl["cg"]["kind"] == "gaussian" and D == 2:
         surrogate = surrogate_leg(args, ctx, wl, F, stream, all_slots, v64)
+    uneven = None
+    if not args.no_uneven and name == "ik2d_n64k_g256_gauss":
+        uneven = uneven_leg(args)
 
     out = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -461,6 +524,8 @@ def ours(args, wl, name):
            "interactions_per_s": A * value}
     if surrogate is not None:
         out["surrogate"] = surrogate
+    if uneven is not None:
+        out["uneven_batch"] = uneven
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         G = len(grid)

@@ -86,6 +86,12 @@ int ik_set_grid(ik_ctx* ctx, int64_t g, const double* xyz);
  * Slot 0 is the default frame.  The copy is asynchronous on the context stream
  * from pinned host memory and synchronous otherwise. */
 int ik_reserve_slots(ik_ctx* ctx, int nslots);
+/* A box and grid of the slot's own (frames of different sizes in one batch): the
+ * slot's computations use them instead of the context's ik_set_box / ik_set_grid,
+ * and its fields have g grid points.  Same meaning as SimBox::SimBox (SimBox.cc:25-45)
+ * and the ikcalculator grid (irvingkirkwood/__init__.py:44-51), per frame. */
+int ik_set_slot_geometry(ik_ctx* ctx, int slot, int dim, const double boxsize[3], const double origin[3],
+                         int64_t g, const double* xyz);
 int ik_upload_frame(ik_ctx* ctx, int slot, int64_t n, const double* pos, const double* vel,
                     const double* mass, const double* diam);
 int ik_set_frame(ik_ctx* ctx, int64_t n, const double* pos, const double* vel,

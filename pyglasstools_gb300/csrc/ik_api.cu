@@ -71,8 +71,26 @@ struct DevBuf {
 
 #define ENS(buf, n) do { int r_ = (buf).ensure(n); if (r_) return r_; } while (0)
 
+// Box, grid and the binning derived from them.  The context holds one; a slot with a
+// geometry of its own (frames of different boxes in one batch) holds another, swapped
+// in while that slot is processed.
+struct Geo {
+    double boxsize[3] = {0, 0, 0}, origin[3] = {0, 0, 0};
+    bool box_set = false;
+    std::vector<double> grid_h;
+    int64_t G = 0;
+    DevBuf grid_d;
+    IkGeom geom{};
+    bool geom_valid = false;
+    int bw[3] = {1, 1, 1}, reach[3] = {0, 0, 0};
+    int nitems = 0;
+    DevBuf gpts_d, items_d;
+};
+
 struct Slot {
     int64_t n = 0;
+    bool has_geo = false; // own box + grid (ik_set_slot_geometry)
+    Geo geo;
     bool has_vel = false, has_mass = false;
     double dmax = 0.0;
     DevBuf pos, vel, mass, diam;
@@ -110,8 +128,7 @@ struct ik_ctx {
     int flags = 0;
     // configuration
     int dim = 0;
-    double boxsize[3] = {0, 0, 0}, origin[3] = {0, 0, 0};
-    bool box_set = false;
+    Geo geo; // box, grid, binning (swapped with a slot's own while it is processed)
     IkPoly12 pot{};
     bool pot_set = false;
     IkCG cg{};
@@ -120,16 +137,6 @@ struct ik_ctx {
     double cg_width_param = 0.0;
     double max_rcut = 0.0;
     bool max_rcut_set = false;
-    // grid
-    std::vector<double> grid_h;
-    int64_t G = 0;
-    DevBuf grid_d;
-    // geometry + binning cache
-    IkGeom geom{};
-    bool geom_valid = false;
-    int bw[3] = {1, 1, 1}, reach[3] = {0, 0, 0};
-    int nitems = 0;
-    DevBuf gpts_d, items_d;
     // per-frame work buffers live in the lanes
     Lane lanes[IK_LANES];
     int next_lane = 0;
@@ -207,13 +214,13 @@ int nc_of(int dim, int c) { return c < dim ? 1 : 0; }
 // (Re)build the cell geometry and the grid binning for the current box, cut-offs and grid.
 int ensure_geometry(ik_ctx* c)
 {
-    if (c->geom_valid) return IK_OK;
+    if (c->geo.geom_valid) return IK_OK;
     IkGeom g{};
     g.dim = c->dim;
     const double R = c->cg.rcut;
     for (int a = 0; a < 3; ++a) {
-        g.L[a] = c->boxsize[a];
-        g.lo[a] = -0.5 * c->boxsize[a] - c->origin[a];
+        g.L[a] = c->geo.boxsize[a];
+        g.lo[a] = -0.5 * c->geo.boxsize[a] - c->geo.origin[a];
         g.periodic[a] = nc_of(c->dim, a);
         int nc = 1;
         if (g.periodic[a]) {
@@ -231,7 +238,7 @@ int ensure_geometry(ik_ctx* c)
         g.reach_bond[a] = 1;
         g.all_bond[a] = (nc < 3) ? 1 : 0;
     }
-    if (c->dim == 2) { g.lo[2] = -0.5 * c->boxsize[2] - c->origin[2]; g.cw[2] = g.L[2]; }
+    if (c->dim == 2) { g.lo[2] = -0.5 * c->geo.boxsize[2] - c->geo.origin[2]; g.cw[2] = g.L[2]; }
     for (int a = 0; a < 3; ++a) {
         g.cwhi[a] = (float)g.cw[a];
         g.cwlo[a] = (float)(g.cw[a] - (double)g.cwhi[a]);
@@ -243,44 +250,44 @@ int ensure_geometry(ik_ctx* c)
     // halo reach and bin width for the FP32 gather
     double cellvol = 1.0, boxvol = 1.0;
     for (int a = 0; a < c->dim; ++a) { cellvol *= g.cw[a]; boxvol *= g.L[a]; }
-    double pts_per_cell = c->G > 0 ? (double)c->G * cellvol / boxvol : 1.0;
+    double pts_per_cell = c->geo.G > 0 ? (double)c->geo.G * cellvol / boxvol : 1.0;
     double target = c->tune_bin_points > 0 ? (double)c->tune_bin_points : (c->dim == 2 ? 20.0 : 24.0);
     int bwv = (int)std::lround(std::pow(std::max(target / std::max(pts_per_cell, 1e-9), 1.0), 1.0 / c->dim));
     bwv = std::max(1, std::min(bwv, 8));
     for (int a = 0; a < 3; ++a) {
         if (a < c->dim) {
-            c->reach[a] = (int)std::ceil(R / g.cw[a]);
-            if (c->reach[a] < 1) c->reach[a] = 1;
-            c->bw[a] = std::min(bwv, g.nc[a]);
+            c->geo.reach[a] = (int)std::ceil(R / g.cw[a]);
+            if (c->geo.reach[a] < 1) c->geo.reach[a] = 1;
+            c->geo.bw[a] = std::min(bwv, g.nc[a]);
         } else {
-            c->reach[a] = 0;
-            c->bw[a] = 1;
+            c->geo.reach[a] = 0;
+            c->geo.bw[a] = 1;
         }
     }
-    c->geom = g;
+    c->geo.geom = g;
 
     // ---- bin the grid points (host, once per box/grid)
     const int D = c->dim;
     int nb[3] = {1, 1, 1};
-    for (int a = 0; a < D; ++a) nb[a] = (g.nc[a] + c->bw[a] - 1) / c->bw[a];
-    const double spacing = std::pow(boxvol / std::max<int64_t>(c->G, 1), 1.0 / D);
+    for (int a = 0; a < D; ++a) nb[a] = (g.nc[a] + c->geo.bw[a] - 1) / c->geo.bw[a];
+    const double spacing = std::pow(boxvol / std::max<int64_t>(c->geo.G, 1), 1.0 / D);
     struct Key { int64_t bin; uint64_t morton; int64_t idx; double w[3]; int cell0[3]; };
-    std::vector<Key> keys((size_t)c->G);
-    for (int64_t i = 0; i < c->G; ++i) {
+    std::vector<Key> keys((size_t)c->geo.G);
+    for (int64_t i = 0; i < c->geo.G; ++i) {
         Key k{};
         k.idx = i;
         int bcoord[3] = {0, 0, 0};
         uint32_t qv[3] = {0, 0, 0};
         for (int a = 0; a < 3; ++a) {
-            double x = c->grid_h[3 * i + a];
+            double x = c->geo.grid_h[3 * i + a];
             if (a < D) {
                 double t = (x - g.lo[a]) / g.L[a];
                 t -= std::floor(t);
                 double xw = g.lo[a] + t * g.L[a];
                 int cell = (int)(t * g.nc[a]);
                 cell = std::max(0, std::min(cell, g.nc[a] - 1));
-                bcoord[a] = cell / c->bw[a];
-                k.cell0[a] = bcoord[a] * c->bw[a];
+                bcoord[a] = cell / c->geo.bw[a];
+                k.cell0[a] = bcoord[a] * c->geo.bw[a];
                 k.w[a] = xw - (g.lo[a] + k.cell0[a] * g.cw[a]);
                 double qq = std::floor(k.w[a] / spacing);
                 qv[a] = (uint32_t)std::max(0.0, std::min(qq, 1023.0));
@@ -302,8 +309,8 @@ int ensure_geometry(ik_ctx* c)
         return x.idx < y.idx;
     });
     const float kappa = c->cg.kappa;
-    std::vector<float4> gpts((size_t)std::max<int64_t>(c->G, 1));
-    for (int64_t k = 0; k < c->G; ++k) {
+    std::vector<float4> gpts((size_t)std::max<int64_t>(c->geo.G, 1));
+    for (int64_t k = 0; k < c->geo.G; ++k) {
         const Key& kk = keys[(size_t)k];
         float4 v;
         v.x = (float)(kappa * kk.w[0]);
@@ -315,12 +322,12 @@ int ensure_geometry(ik_ctx* c)
     }
     // work items: ranges of groups inside a bin, sized for >= ~4 items per warp slot
     int64_t nbins_used = 0;
-    for (int64_t k = 0; k < c->G; ++k) if (k == 0 || keys[(size_t)k].bin != keys[(size_t)k - 1].bin) ++nbins_used;
+    for (int64_t k = 0; k < c->geo.G; ++k) if (k == 0 || keys[(size_t)k].bin != keys[(size_t)k - 1].bin) ++nbins_used;
     int64_t total_groups = 0;
     {
         int64_t s = 0;
-        for (int64_t k = 1; k <= c->G; ++k)
-            if (k == c->G || keys[(size_t)k].bin != keys[(size_t)k - 1].bin) { total_groups += (k - s + IK_P - 1) / IK_P; s = k; }
+        for (int64_t k = 1; k <= c->geo.G; ++k)
+            if (k == c->geo.G || keys[(size_t)k].bin != keys[(size_t)k - 1].bin) { total_groups += (k - s + IK_P - 1) / IK_P; s = k; }
     }
     int64_t warps = (int64_t)c->sm_count * 16;
     int64_t want_items = std::max<int64_t>(4 * warps, nbins_used);
@@ -328,32 +335,32 @@ int ensure_geometry(ik_ctx* c)
     std::vector<int4> items;
     {
         int64_t s = 0;
-        for (int64_t k = 1; k <= c->G; ++k) {
-            if (k == c->G || keys[(size_t)k].bin != keys[(size_t)k - 1].bin) {
+        for (int64_t k = 1; k <= c->geo.G; ++k) {
+            if (k == c->geo.G || keys[(size_t)k].bin != keys[(size_t)k - 1].bin) {
                 const Key& kk = keys[(size_t)s];
                 for (int64_t t = s; t < k; t += (int64_t)gi_max * IK_P)
                     items.push_back(make_int4(kk.cell0[0], kk.cell0[1], kk.cell0[2], (int)t));
                 s = k;
             }
         }
-        items.push_back(make_int4(0, 0, 0, (int)c->G));
+        items.push_back(make_int4(0, 0, 0, (int)c->geo.G));
     }
-    c->nitems = (int)items.size() - 1;
-    ENS(c->gpts_d, gpts.size() * sizeof(float4));
-    ENS(c->items_d, items.size() * sizeof(int4));
-    CK(cudaMemcpy(c->gpts_d.p, gpts.data(), gpts.size() * sizeof(float4), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(c->items_d.p, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
-    c->geom_valid = true;
+    c->geo.nitems = (int)items.size() - 1;
+    ENS(c->geo.gpts_d, gpts.size() * sizeof(float4));
+    ENS(c->geo.items_d, items.size() * sizeof(int4));
+    CK(cudaMemcpy(c->geo.gpts_d.p, gpts.data(), gpts.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->geo.items_d.p, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    c->geo.geom_valid = true;
     ++c->geom_version;
     return IK_OK;
 }
 
 int ensure_ready(ik_ctx* c)
 {
-    if (!c->box_set) return fail(IK_ERR_STATE, "box not set (ik_set_box)");
+    if (!c->geo.box_set) return fail(IK_ERR_STATE, "box not set (ik_set_box)");
     if (!c->pot_set) return fail(IK_ERR_STATE, "pair potential not set");
     if (!c->cg_set) return fail(IK_ERR_STATE, "coarse-graining function not set");
-    if (c->G <= 0) return fail(IK_ERR_STATE, "grid not set (ik_set_grid)");
+    if (c->geo.G <= 0) return fail(IK_ERR_STATE, "grid not set (ik_set_grid)");
     if (!c->max_rcut_set) return fail(IK_ERR_STATE, "max_rcut unknown: upload a frame or call ik_set_max_rcut");
     return IK_OK;
 }
@@ -423,17 +430,17 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
     CK(cudaEventRecord(c->fork, c->stream));
     CK(cudaStreamWaitEvent(L.st, c->fork, 0));
     if (s.done_recorded && !c->capturing) CK(cudaStreamWaitEvent(L.st, s.done, 0));
-    const IkGeom& g = c->geom;
+    const IkGeom& g = c->geo.geom;
     const int D = c->dim, NC = D == 2 ? 3 : 6;
     const int n = (int)s.n;
     bool timing = (c->flags & IK_FLAG_TIMING) != 0 && !c->capturing;
     if (timing) CK(cudaEventRecord(c->ev[0], L.st));
-    ENS(s.vir, sizeof(double) * NC * c->G);
-    ENS(s.kin, sizeof(double) * NC * c->G);
+    ENS(s.vir, sizeof(double) * NC * c->geo.G);
+    ENS(s.kin, sizeof(double) * NC * c->geo.G);
     ENS(s.counters, sizeof(unsigned long long) * 4);
     CK(cudaMemsetAsync(s.counters.p, 0, sizeof(unsigned long long) * 4, L.st));
-    if (!(fields & IK_FIELD_KINETIC)) CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->G, L.st));
-    if (!(fields & IK_FIELD_VIRIAL)) CK(cudaMemsetAsync(s.vir.p, 0, sizeof(double) * NC * c->G, L.st));
+    if (!(fields & IK_FIELD_KINETIC)) CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->geo.G, L.st));
+    if (!(fields & IK_FIELD_VIRIAL)) CK(cudaMemsetAsync(s.vir.p, 0, sizeof(double) * NC * c->geo.G, L.st));
     int r = build_cells(c, s, g, L.st, L.cell_of, L.rank, L.cell_count, L.cell_start, L.sorted, L.bsum_cells,
                         prec == IK_PREC_FP32 ? &L.relhi : nullptr, prec == IK_PREC_FP32 ? &L.rello : nullptr);
     if (r) return r;
@@ -487,8 +494,8 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         a.g = g;
         for (int k = 0; k < 3; ++k) {
             a.cws[k] = (float)(c->cg.kappa * g.cw[k]);
-            a.bw[k] = c->bw[k];
-            a.reach[k] = c->reach[k];
+            a.bw[k] = c->geo.bw[k];
+            a.reach[k] = c->geo.reach[k];
         }
         a.kappa = c->cg.kappa;
         a.R2s = c->cg.R2s;
@@ -509,20 +516,20 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         a.bonds = bonds;
         a.maxb = c->maxb;
         a.kin = L.kin.as<float4>();
-        a.gpts = c->gpts_d.as<float4>();
-        a.grid = c->grid_d.as<double>();
-        a.items = c->items_d.as<int4>();
-        a.nitems = c->nitems;
+        a.gpts = c->geo.gpts_d.as<float4>();
+        a.grid = c->geo.grid_d.as<double>();
+        a.items = c->geo.items_d.as<int4>();
+        a.nitems = c->geo.nitems;
         a.halo_cap = c->halo_cap;
         a.qcap = 32 * (c->maxb + 1);
         double norm = c->cg.kind == IK_CG_MOLLIFIER ? c->cg.mollifier_norm : c->cg.norm;
-        ENS(L.vir2, sizeof(float2) * NC * (size_t)c->G);
-        ENS(L.kin2, sizeof(float2) * NC * (size_t)c->G);
+        ENS(L.vir2, sizeof(float2) * NC * (size_t)c->geo.G);
+        ENS(L.kin2, sizeof(float2) * NC * (size_t)c->geo.G);
         a.out_vir = L.vir2.as<float2>();
         a.out_kin = L.kin2.as<float2>();
         a.fields = fields & (s.has_vel ? 3 : 1);
         if ((fields & IK_FIELD_KINETIC) && !s.has_vel)
-            CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->G, L.st));
+            CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->geo.G, L.st));
         a.work_counter = L.work_counter.as<int>();
         a.status = c->status.as<int>();
         a.cnt_pairs = cnt + 1;
@@ -530,13 +537,13 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         CK(cudaMemsetAsync(L.work_counter.p, 0, sizeof(int), L.st));
         const bool mlp = c->cg.mode == IK_QUAD_MLP && (a.fields & 1);
         if (mlp) {
-            if (c->mlp_cap == 0) c->mlp_cap = std::max<long long>(1 << 20, 128LL * c->G);
+            if (c->mlp_cap == 0) c->mlp_cap = std::max<long long>(1 << 20, 128LL * c->geo.G);
             ENS(L.mlp_rec, sizeof(float4) * (size_t)c->mlp_cap);
             ENS(L.mlp_rid, sizeof(int2) * (size_t)c->mlp_cap);
             ENS(L.mlp_count, sizeof(unsigned long long));
-            ENS(L.corr, sizeof(unsigned long long) * NC * (size_t)c->G);
+            ENS(L.corr, sizeof(unsigned long long) * NC * (size_t)c->geo.G);
             CK(cudaMemsetAsync(L.mlp_count.p, 0, sizeof(unsigned long long), L.st));
-            CK(cudaMemsetAsync(L.corr.p, 0, sizeof(unsigned long long) * NC * (size_t)c->G, L.st));
+            CK(cudaMemsetAsync(L.corr.p, 0, sizeof(unsigned long long) * NC * (size_t)c->geo.G, L.st));
             a.mlp_rec = L.mlp_rec.as<float4>();
             a.mlp_rid = L.mlp_rid.as<int2>();
             a.mlp_count = L.mlp_count.as<unsigned long long>();
@@ -544,7 +551,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
             a.cnt_records = cnt + 3;
         }
         size_t smem = (size_t)IK_WARPS_GATHER * ((size_t)c->halo_cap * 20 + (size_t)a.qcap * 4);
-        int blocks = std::min(c->nitems, c->sm_count * (c->tune_blocks_per_sm > 0 ? c->tune_blocks_per_sm : 2));
+        int blocks = std::min(c->geo.nitems, c->sm_count * (c->tune_blocks_per_sm > 0 ? c->tune_blocks_per_sm : 2));
         if (blocks > 0) {
             CK(launch_gather32(a, c->cg.kind, (c->flags & IK_FLAG_LANE_KAHAN) != 0 && !mlp, mlp, blocks,
                                32 * IK_WARPS_GATHER, smem, L.st));
@@ -561,8 +568,8 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         // FP64 finish: ((double)hi + (double)lo) * normalisation (0.5 of the GL map for the virial)
         CK(launch_pairs_to_f64(L.vir2.as<float2>(), mlp ? L.corr.as<unsigned long long>() : nullptr,
                                (a.fields & 1) ? s.vir.as<double>() : nullptr, 0.5 * norm, L.kin2.as<float2>(),
-                               (a.fields & 2) ? s.kin.as<double>() : nullptr, norm, (long long)NC * c->G, L.st));
-        c->launches += (c->G > 0 && a.fields) ? 1 : 0;
+                               (a.fields & 2) ? s.kin.as<double>() : nullptr, norm, (long long)NC * c->geo.G, L.st));
+        c->launches += (c->geo.G > 0 && a.fields) ? 1 : 0;
     } else {
         if (timing) CK(cudaEventRecord(c->ev[1], L.st));
         ENS(L.bonds64, sizeof(IkB64) * (size_t)c->maxb * std::max(n, 1));
@@ -579,8 +586,8 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         a.g = g;
         a.cg = c->cg;
         for (int k = 0; k < 3; ++k) {
-            a.reach[k] = c->reach[k];
-            a.all[k] = (k < D && 2 * c->reach[k] + 1 >= g.nc[k]) ? 1 : 0;
+            a.reach[k] = c->geo.reach[k];
+            a.all[k] = (k < D && 2 * c->geo.reach[k] + 1 >= g.nc[k]) ? 1 : 0;
         }
         a.nq = c->gl.n;
         for (int k = 0; k < c->gl.n; ++k) { a.xs[k] = 0.5 + 0.5 * c->gl.x[k]; a.ws[k] = c->gl.w[k]; }
@@ -592,15 +599,15 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         a.nb = L.nb64.as<int>();
         a.bonds = L.bonds64.as<IkB64>();
         a.maxb = c->maxb;
-        a.grid = c->grid_d.as<double>();
-        a.ngrid = c->G;
+        a.grid = c->geo.grid_d.as<double>();
+        a.ngrid = c->geo.G;
         a.out_vir = s.vir.as<double>();
         a.out_kin = s.kin.as<double>();
         a.fields = fields;
         if ((fields & IK_FIELD_KINETIC) && !s.has_vel)
-            CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->G, L.st));
+            CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->geo.G, L.st));
         CK(launch_gather64(a, L.st));
-        c->launches += (n > 0 ? 1 : 0) + (c->G > 0 ? 1 : 0);
+        c->launches += (n > 0 ? 1 : 0) + (c->geo.G > 0 ? 1 : 0);
     }
     if (timing) CK(cudaEventRecord(c->ev[3], L.st));
     s.last_prec = prec;
@@ -614,6 +621,41 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
     s.done_recorded = true;
     CK(cudaEventRecord(L.last, L.st));
     return IK_OK;
+}
+
+// Settings that every binning depends on (cut-offs, kappa, bin size) changed.
+void invalidate_geometry(ik_ctx* c)
+{
+    c->geo.geom_valid = false;
+    for (Slot& s : c->slots) s.geo.geom_valid = false;
+}
+
+// Swaps a slot's own geometry (if any) into the context for the scope.
+struct GeoSwap {
+    ik_ctx* c;
+    Slot* s = nullptr;
+    GeoSwap(ik_ctx* c_, int slot) : c(c_)
+    {
+        if (slot >= 0 && slot < (int)c->slots.size() && c->slots[(size_t)slot].has_geo) {
+            s = &c->slots[(size_t)slot];
+            std::swap(c->geo, s->geo);
+        }
+    }
+    ~GeoSwap() { if (s) std::swap(c->geo, s->geo); }
+    GeoSwap(const GeoSwap&) = delete;
+    GeoSwap& operator=(const GeoSwap&) = delete;
+};
+
+// Checks, geometry and capacities of one slot, then its launches.
+int prepare_enqueue(ik_ctx* c, int slot, int prec, int fields)
+{
+    GeoSwap gs(c, slot);
+    if (int r = ensure_ready(c)) return r;
+    if (int r = mode_ok(c, prec)) return r;
+    if (int r = ensure_geometry(c)) return r;
+    if (c->maxb == 0) c->maxb = c->dim == 2 ? IK_MAXB_2D : IK_MAXB_3D;
+    if (c->halo_cap == 0) c->halo_cap = c->dim == 2 ? 512 : 768;
+    return enqueue(c, slot, prec, fields);
 }
 
 } // namespace
@@ -704,13 +746,13 @@ int ik_set_box(ik_ctx* c, int dim, const double boxsize[3], const double origin[
     if (dim == 2) { b[2] = 1.0; o[2] = 0.0; } // SimBox.cc:34-40
     for (int a = 0; a < dim; ++a)
         if (!(b[a] > 0.0) || !std::isfinite(b[a])) return fail(IK_ERR_ARG, "box edge %d must be > 0 (got %g)", a, b[a]);
-    bool same = c->box_set && c->dim == dim;
-    for (int a = 0; a < 3 && same; ++a) same = (c->boxsize[a] == b[a] && c->origin[a] == o[a]);
+    bool same = c->geo.box_set && c->dim == dim;
+    for (int a = 0; a < 3 && same; ++a) same = (c->geo.boxsize[a] == b[a] && c->geo.origin[a] == o[a]);
     if (!same) {
         c->dim = dim;
-        for (int a = 0; a < 3; ++a) { c->boxsize[a] = b[a]; c->origin[a] = o[a]; }
-        c->geom_valid = false;
-        c->box_set = true;
+        for (int a = 0; a < 3; ++a) { c->geo.boxsize[a] = b[a]; c->geo.origin[a] = o[a]; }
+        c->geo.geom_valid = false;
+        c->geo.box_set = true;
         if (c->cg_set) { // the Gaussian normalisation depends on dim
             int r = ik_set_cgfunc(c, c->cg.kind, c->cg.mode, c->cg.order, c->cg.rcut, c->cg_width_param);
             if (r) return r;
@@ -796,8 +838,8 @@ int ik_set_cgfunc(ik_ctx* c, int kind, int mode, int order, double rcut, double 
             gl.wt[k] = (float)gl.w[order - 1 - k];
         }
     }
-    if (!c->cg_set || old_kind != kind || old_rcut != rcut) c->geom_valid = false;
-    if (kind == IK_CG_GAUSSIAN) c->geom_valid = false; // kappa changes gpts
+    if (!c->cg_set || old_kind != kind || old_rcut != rcut) invalidate_geometry(c);
+    if (kind == IK_CG_GAUSSIAN) invalidate_geometry(c); // kappa changes gpts
     c->cg_set = true;
     return IK_OK;
 }
@@ -817,7 +859,7 @@ int ik_set_max_rcut(ik_ctx* c, double max_rcut)
     if (int r = check_ctx(c)) return r;
     ++c->config_version; // captured batch graphs hold the old settings
     if (!(max_rcut > 0.0) || !std::isfinite(max_rcut)) return fail(IK_ERR_ARG, "max_rcut must be > 0");
-    if (!c->max_rcut_set || c->max_rcut != max_rcut) c->geom_valid = false;
+    if (!c->max_rcut_set || c->max_rcut != max_rcut) invalidate_geometry(c);
     c->max_rcut = max_rcut;
     c->max_rcut_set = true;
     c->pot.max_rcut_sq = max_rcut * max_rcut;
@@ -841,11 +883,47 @@ int ik_set_grid(ik_ctx* c, int64_t g, const double* xyz)
     if (g > (int64_t)1 << 30) return fail(IK_ERR_UNSUPPORTED, "grid too large");
     for (int64_t i = 0; i < 3 * g; ++i)
         if (!std::isfinite(xyz[i])) return fail(IK_ERR_ARG, "grid coordinate %lld is not finite", (long long)i);
-    c->grid_h.assign(xyz, xyz + 3 * g);
-    c->G = g;
-    ENS(c->grid_d, sizeof(double) * 3 * std::max<int64_t>(g, 1));
-    if (g > 0) CK(cudaMemcpy(c->grid_d.p, xyz, sizeof(double) * 3 * g, cudaMemcpyHostToDevice));
-    c->geom_valid = false;
+    c->geo.grid_h.assign(xyz, xyz + 3 * g);
+    c->geo.G = g;
+    ENS(c->geo.grid_d, sizeof(double) * 3 * std::max<int64_t>(g, 1));
+    if (g > 0) CK(cudaMemcpy(c->geo.grid_d.p, xyz, sizeof(double) * 3 * g, cudaMemcpyHostToDevice));
+    c->geo.geom_valid = false;
+    return IK_OK;
+}
+
+int ik_set_slot_geometry(ik_ctx* c, int slot, int dim, const double boxsize[3], const double origin[3], int64_t g,
+                         const double* xyz)
+{
+    if (int r = check_ctx(c)) return r;
+    if (int r = slot_ok(c, slot)) return r;
+    if (dim != 2 && dim != 3) return fail(IK_ERR_ARG, "dim must be 2 or 3 (got %d)", dim);
+    if (c->dim != 0 && c->dim != dim) return fail(IK_ERR_ARG, "dim %d differs from the context's %d", dim, c->dim);
+    if (!boxsize) return fail(IK_ERR_ARG, "null box");
+    for (int a = 0; a < 3; ++a)
+        if (!(boxsize[a] > 0.0) || !std::isfinite(boxsize[a])) return fail(IK_ERR_ARG, "box lengths must be > 0");
+    if (g < 1 || g > ((int64_t)1 << 30) || !xyz) return fail(IK_ERR_ARG, "bad grid arguments");
+    for (int64_t i = 0; i < 3 * g; ++i)
+        if (!std::isfinite(xyz[i])) return fail(IK_ERR_ARG, "grid coordinate %lld is not finite", (long long)i);
+    Slot& s = c->slots[(size_t)slot];
+    if (s.done_recorded) CK(cudaEventSynchronize(s.done)); // the slot's grid may be in use
+    if (c->dim == 0) { // the first geometry fixes the context's dimension
+        c->dim = dim;
+        if (c->cg_set) {
+            int r = ik_set_cgfunc(c, c->cg.kind, c->cg.mode, c->cg.order, c->cg.rcut, c->cg_width_param);
+            if (r) return r;
+        }
+    }
+    Geo& G = s.geo;
+    for (int a = 0; a < 3; ++a) { G.boxsize[a] = boxsize[a]; G.origin[a] = origin ? origin[a] : 0.0; }
+    G.box_set = true;
+    G.grid_h.assign(xyz, xyz + 3 * g);
+    G.G = g;
+    ENS(G.grid_d, sizeof(double) * 3 * g);
+    CK(cudaMemcpy(G.grid_d.p, xyz, sizeof(double) * 3 * g, cudaMemcpyHostToDevice));
+    G.geom_valid = false;
+    s.has_geo = true;
+    ++c->slot_version;
+    ++c->config_version;
     return IK_OK;
 }
 
@@ -866,7 +944,7 @@ int ik_upload_frame(ik_ctx* c, int slot, int64_t n, const double* pos, const dou
     if (int r = slot_ok(c, slot)) return r;
     if (n < 0 || n >= (1 << 25)) return fail(IK_ERR_ARG, "particle count %lld out of range (max 2^25 - 1)", (long long)n);
     if (n > 0 && (!pos || !diam)) return fail(IK_ERR_ARG, "positions and diameters are required");
-    if (!c->box_set) return fail(IK_ERR_STATE, "box not set (ik_set_box)");
+    if (!c->geo.box_set) return fail(IK_ERR_STATE, "box not set (ik_set_box)");
     double dmax = 0.0;
     if (!c->max_rcut_set) // Calculator.h:41-45 freezes max_rcut from the first frame
         for (int64_t i = 0; i < n; ++i) dmax = std::max(dmax, diam[i]);
@@ -920,13 +998,9 @@ int ik_compute_slot(ik_ctx* c, int slot, int precision, int fields)
     if (int r = slot_ok(c, slot)) return r;
     if (precision != IK_PREC_FP64 && precision != IK_PREC_FP32) return fail(IK_ERR_ARG, "unknown precision %d", precision);
     if (fields < 1 || fields > 3) return fail(IK_ERR_ARG, "fields mask must be 1, 2 or 3");
-    if (int r = ensure_ready(c)) return r;
-    if (int r = mode_ok(c, precision)) return r;
-    if (int r = ensure_geometry(c)) return r;
-    if (c->maxb == 0) c->maxb = c->dim == 2 ? IK_MAXB_2D : IK_MAXB_3D;
-    if (c->halo_cap == 0) c->halo_cap = c->dim == 2 ? 512 : 768;
     c->pending.push_back({slot, precision, fields});
-    return enqueue(c, slot, precision, fields);
+    if (int r = prepare_enqueue(c, slot, precision, fields)) { c->pending.pop_back(); return r; }
+    return IK_OK;
 }
 
 int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int fields)
@@ -936,9 +1010,12 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
     for (int k = 0; k < count; ++k) if (int r = slot_ok(c, slots[k])) return r;
     if (precision != IK_PREC_FP64 && precision != IK_PREC_FP32) return fail(IK_ERR_ARG, "unknown precision %d", precision);
     if (fields < 1 || fields > 3) return fail(IK_ERR_ARG, "fields mask must be 1, 2 or 3");
-    if (int r = ensure_ready(c)) return r;
-    if (int r = mode_ok(c, precision)) return r;
-    if (int r = ensure_geometry(c)) return r;
+    for (int k = 0; k < count; ++k) { // every slot ready, its geometry current
+        GeoSwap gs(c, slots[k]);
+        if (int r = ensure_ready(c)) return r;
+        if (int r = mode_ok(c, precision)) return r;
+        if (int r = ensure_geometry(c)) return r;
+    }
     if (c->maxb == 0) c->maxb = c->dim == 2 ? IK_MAXB_2D : IK_MAXB_3D;
     if (c->halo_cap == 0) c->halo_cap = c->dim == 2 ? 512 : 768;
     std::vector<int> key(slots, slots + count);
@@ -951,7 +1028,7 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
         // first run of this batch: plain launches (sizes every buffer, checks capacities)
         for (int k = 0; k < count; ++k) {
             c->pending.push_back({slots[k], precision, fields});
-            if (int r = enqueue(c, slots[k], precision, fields)) return r;
+            if (int r = prepare_enqueue(c, slots[k], precision, fields)) return r;
         }
         if (int r = ik_synchronize(c)) return r;
         if (c->flags & IK_FLAG_TIMING) return IK_OK;
@@ -963,7 +1040,7 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
         c->capturing = true;
         c->captured_lanes = 0;
         int rr = IK_OK;
-        for (int k = 0; k < count && rr == IK_OK; ++k) rr = enqueue(c, slots[k], precision, fields);
+        for (int k = 0; k < count && rr == IK_OK; ++k) rr = prepare_enqueue(c, slots[k], precision, fields);
         for (int l = 0; l < IK_LANES && rr == IK_OK; ++l)
             if (c->captured_lanes & (1 << l)) {
                 if (cudaEventRecord(c->lanes[l].last, c->lanes[l].st) != cudaSuccess ||
@@ -1044,7 +1121,7 @@ int ik_synchronize(ik_ctx* c)
         if (!grow) { c->pending.clear(); return fail(IK_ERR_CUDA, "device status 0x%x", st); }
         std::vector<PendingOp> ops = c->pending;
         for (const PendingOp& op : ops)
-            if (int r = enqueue(c, op.slot, op.prec, op.fields)) { c->pending.clear(); return r; }
+            if (int r = prepare_enqueue(c, op.slot, op.prec, op.fields)) { c->pending.clear(); return r; }
     }
     c->pending.clear();
     return fail(IK_ERR_CAPACITY, "capacity growth did not converge");
@@ -1060,18 +1137,19 @@ int ik_get_field(ik_ctx* c, int slot, int field, double* out, int64_t count)
 {
     if (int r = check_ctx(c)) return r;
     if (int r = slot_ok(c, slot)) return r;
+    GeoSwap gs(c, slot);
     if (field != IK_FIELD_VIRIAL && field != IK_FIELD_KINETIC) return fail(IK_ERR_ARG, "unknown field %d", field);
     if (int r = ik_synchronize(c)) return r;
     Slot& s = c->slots[(size_t)slot];
     if (s.last_prec < 0) return fail(IK_ERR_STATE, "slot %d has not been computed", slot);
     const int D = c->dim, NC = D == 2 ? 3 : 6;
-    if (count != c->G * D * D) return fail(IK_ERR_ARG, "output needs %lld doubles (got %lld)", (long long)(c->G * D * D), (long long)count);
-    std::vector<double> tmp((size_t)(NC * c->G));
+    if (count != c->geo.G * D * D) return fail(IK_ERR_ARG, "output needs %lld doubles (got %lld)", (long long)(c->geo.G * D * D), (long long)count);
+    std::vector<double> tmp((size_t)(NC * c->geo.G));
     const DevBuf& src = field == IK_FIELD_VIRIAL ? s.vir : s.kin;
-    if (c->G > 0) CK(cudaMemcpy(tmp.data(), src.p, sizeof(double) * NC * c->G, cudaMemcpyDeviceToHost));
+    if (c->geo.G > 0) CK(cudaMemcpy(tmp.data(), src.p, sizeof(double) * NC * c->geo.G, cudaMemcpyDeviceToHost));
     static const int map2[3][2] = {{0, 0}, {1, 1}, {0, 1}};
     static const int map3[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
-    for (int64_t g = 0; g < c->G; ++g) {
+    for (int64_t g = 0; g < c->geo.G; ++g) {
         double* o = out + g * D * D;
         for (int k = 0; k < NC; ++k) {
             int a = D == 2 ? map2[k][0] : map3[k][0], b = D == 2 ? map2[k][1] : map3[k][1];
@@ -1088,7 +1166,8 @@ int ik_get_neighbors(ik_ctx* c, int slot, double radius, int64_t* offs, int32_t*
 {
     if (int r = check_ctx(c)) return r;
     if (int r = slot_ok(c, slot)) return r;
-    if (!c->box_set) return fail(IK_ERR_STATE, "box not set");
+    GeoSwap gs(c, slot);
+    if (!c->geo.box_set) return fail(IK_ERR_STATE, "box not set");
     if (!(radius > 0.0)) return fail(IK_ERR_ARG, "radius must be > 0");
     if (!offs || !nnz) return fail(IK_ERR_ARG, "null output");
     Slot& s = c->slots[(size_t)slot];
@@ -1096,8 +1175,8 @@ int ik_get_neighbors(ik_ctx* c, int slot, double radius, int64_t* offs, int32_t*
     IkGeom g{};
     g.dim = c->dim;
     for (int a = 0; a < 3; ++a) {
-        g.L[a] = c->boxsize[a];
-        g.lo[a] = -0.5 * c->boxsize[a] - c->origin[a];
+        g.L[a] = c->geo.boxsize[a];
+        g.lo[a] = -0.5 * c->geo.boxsize[a] - c->geo.origin[a];
         g.periodic[a] = nc_of(c->dim, a);
         int nc = 1;
         if (g.periodic[a]) {
@@ -1146,15 +1225,16 @@ int ik_get_neighbors_point(ik_ctx* c, int slot, const double point[3], double ra
 {
     if (int r = check_ctx(c)) return r;
     if (int r = slot_ok(c, slot)) return r;
-    if (!c->box_set) return fail(IK_ERR_STATE, "box not set");
+    GeoSwap gs(c, slot);
+    if (!c->geo.box_set) return fail(IK_ERR_STATE, "box not set");
     if (!point || !count) return fail(IK_ERR_ARG, "null argument");
     Slot& s = c->slots[(size_t)slot];
     int n = (int)s.n;
     IkGeom g{};
     g.dim = c->dim;
     for (int a = 0; a < 3; ++a) {
-        g.L[a] = c->boxsize[a];
-        g.lo[a] = -0.5 * c->boxsize[a] - c->origin[a];
+        g.L[a] = c->geo.boxsize[a];
+        g.lo[a] = -0.5 * c->geo.boxsize[a] - c->geo.origin[a];
         g.periodic[a] = nc_of(c->dim, a);
     }
     ENS(c->q_flag, std::max(n, 1));
@@ -1240,7 +1320,7 @@ int ik_set_tuning(ik_ctx* c, int param, int value)
     case IK_TUNE_BIN_POINTS:
         if (value < 0 || value > 4096) return fail(IK_ERR_ARG, "bin points must be in [0, 4096]");
         c->tune_bin_points = value;
-        c->geom_valid = false;
+        invalidate_geometry(c);
         return IK_OK;
     case IK_TUNE_BLOCKS_PER_SM:
         if (value < 0 || value > 16) return fail(IK_ERR_ARG, "blocks per SM must be in [0, 16]");
@@ -1265,7 +1345,6 @@ int ik_autotune_batch(ik_ctx* c, const int* slots, int count, int precision, int
     static const int bins_2d[] = {12, 16, 20, 25, 36};
     static const int bins_3d[] = {16, 24, 48, 96};
     static const int blocks[] = {1, 2};
-    if (int r = ensure_ready(c)) return r;
     const int* bins = c->dim == 3 ? bins_3d : bins_2d;
     const int nbins = c->dim == 3 ? 4 : 5;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -1364,14 +1443,15 @@ int ik_download_field_async(ik_ctx* c, int slot, int field, double* host_out, in
 {
     if (int r = check_ctx(c)) return r;
     if (int r = slot_ok(c, slot)) return r;
+    GeoSwap gs(c, slot);
     if (field != IK_FIELD_VIRIAL && field != IK_FIELD_KINETIC) return fail(IK_ERR_ARG, "unknown field %d", field);
     const int NC = c->dim == 2 ? 3 : 6;
-    if (!host_out || count != c->G * NC) return fail(IK_ERR_ARG, "output needs %lld doubles", (long long)(c->G * NC));
+    if (!host_out || count != c->geo.G * NC) return fail(IK_ERR_ARG, "output needs %lld doubles", (long long)(c->geo.G * NC));
     Slot& s = c->slots[(size_t)slot];
     const DevBuf& src = field == IK_FIELD_VIRIAL ? s.vir : s.kin;
     if (!src.p) return fail(IK_ERR_STATE, "slot %d has not been computed", slot);
     if (s.done_recorded) CK(cudaStreamWaitEvent(c->stream, s.done, 0));
-    if (c->G > 0) CK(cudaMemcpyAsync(host_out, src.p, sizeof(double) * NC * c->G, cudaMemcpyDeviceToHost, c->stream));
+    if (c->geo.G > 0) CK(cudaMemcpyAsync(host_out, src.p, sizeof(double) * NC * c->geo.G, cudaMemcpyDeviceToHost, c->stream));
     return IK_OK;
 }
 

@@ -54,6 +54,7 @@ def lib():
             "ik_get_max_rcut": ([vp, dp], i32),
             "ik_set_grid": ([vp, i64, dp], i32),
             "ik_reserve_slots": ([vp, i32], i32),
+            "ik_set_slot_geometry": ([vp, i32, i32, dp, dp, i64, dp], i32),
             "ik_upload_frame": ([vp, i32, i64, dp, dp, dp, dp], i32),
             "ik_set_frame": ([vp, i64, dp, dp, dp, dp], i32),
             "ik_compute_slot": ([vp, i32, i32, i32], i32),
@@ -181,6 +182,17 @@ class IKContext:
     def reserve_slots(self, n):
         check(lib().ik_reserve_slots(self._h, n))
 
+    def set_slot_geometry(self, slot, dim, box, grid, origin=(0.0, 0.0, 0.0)):
+        """Give `slot` a box and grid of its own (uneven batches)."""
+        b = _c64(box)
+        o = _c64(origin)
+        g = _c64(grid, (-1, 3))
+        check(lib().ik_set_slot_geometry(self._h, slot, dim, _dp(b), _dp(o), len(g), _dp(g)))
+        self.slot_G = getattr(self, "slot_G", {})
+        self.slot_G[slot] = len(g)
+        if self.dim is None:
+            self.dim = dim
+
     def upload_frame(self, slot, pos, diam, vel=None, mass=None):
         pos = _c64(pos, (-1, 3))
         diam = _c64(diam)
@@ -234,7 +246,8 @@ class IKContext:
 
     def get_field(self, field=FIELD_VIRIAL, slot=0):
         D = self.dim
-        out = np.zeros((self.G, D, D))
+        G = getattr(self, "slot_G", {}).get(slot, self.G)
+        out = np.zeros((G, D, D))
         check(lib().ik_get_field(self._h, slot, field, _dp(out), out.size))
         # column-major per grid point -> [g, a, b] = T_ab (symmetric)
         return out.transpose(0, 2, 1).copy()
