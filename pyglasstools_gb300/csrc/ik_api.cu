@@ -944,7 +944,8 @@ int ik_upload_frame(ik_ctx* c, int slot, int64_t n, const double* pos, const dou
     if (int r = slot_ok(c, slot)) return r;
     if (n < 0 || n >= (1 << 25)) return fail(IK_ERR_ARG, "particle count %lld out of range (max 2^25 - 1)", (long long)n);
     if (n > 0 && (!pos || !diam)) return fail(IK_ERR_ARG, "positions and diameters are required");
-    if (!c->geo.box_set) return fail(IK_ERR_STATE, "box not set (ik_set_box)");
+    if (!c->geo.box_set && !c->slots[(size_t)slot].has_geo)
+        return fail(IK_ERR_STATE, "box not set (ik_set_box or ik_set_slot_geometry)");
     double dmax = 0.0;
     if (!c->max_rcut_set) // Calculator.h:41-45 freezes max_rcut from the first frame
         for (int64_t i = 0; i < n; ++i) dmax = std::max(dmax, diam[i]);
