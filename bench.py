@@ -135,15 +135,20 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------- dist helpers
-def dist_setup():
+def dist_setup(backend=None):
+    """Replica setup from the torchrun environment: NCCL with one GPU per rank, or gloo
+    (host-side tests).  The path is not sharded: ranks only meet at barriers and the
+    max over ranks of the timed region."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        backend = backend or "nccl"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
     return world, rank, local
 
 
@@ -158,7 +163,8 @@ def max_over_ranks(x, world):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 

@@ -20,7 +20,11 @@
 //   * accumulation: every lane sums its slots of a group in FP32 (optionally with
 //     Kahan compensation); the 32 lane partials are combined with error-free
 //     transformations (TwoSum) in a transposing butterfly -- each shuffle level halves
-//     the values a lane holds -- and the compensated result is written in FP64.
+//     the values a lane holds -- and the compensated result is written as a
+//     double-float pair (hi, lo), converted to FP64 and scaled by k_pairs_to_f64;
+//   * surrogate mode (MLPM): a bond whose far end r_j lies outside the support
+//     becomes a record {M, m.h, |h|^2, B_fixed} + {grid point, bond} for the learned
+//     surrogate (ik_mlp.cu) instead of a term of the sum.
 // Bond records (CSR, 16 B): {hb = kappa r_ij / 2, f' = 2 forceDivR / kappa^2}; the
 // stress coefficient is f' hb (x) hb.
 #include "ik_kernels.h"
