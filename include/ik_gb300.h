@@ -63,7 +63,12 @@ int ik_set_potential_poly12(ik_ctx* ctx, double scaled_rcut, const double params
 
 /* Coarse-graining function.  rcut = support radius R (Gaussian: cut * width);
  * width = Gaussian standard deviation (Mollifier: the radius its normalisation was
- * built with); order = Gauss-Legendre points for IK_QUAD_FIXEDPOINT.
+ * built with); order = Gauss-Legendre points for IK_QUAD_FIXEDPOINT.  Modes on the GPU:
+ * IK_QUAD_FIXEDPOINT (both paths); IK_QUAD_EXACT (FP64 path: the segment clipped to the
+ * support, erf closed form for the Gaussian, GL on the clipped interval otherwise);
+ * IK_QUAD_MLP (FP32 path, Gaussian: the attached surrogate on bonds that cross the edge
+ * of the support, GL-order elsewhere and as its fallback).  IK_QUAD_ADAPTIVE exists in
+ * the oracle only (IK_ERR_UNSUPPORTED here).
  * Replaces FixedPointCGFunc<...>(order, rcut) / AdaptiveCGFunc<...>(neval, relerr,
  * abserr, rcut) (irvingkirkwood/cgfunc/CoarseGrainFunction.h:56-134). */
 int ik_set_cgfunc(ik_ctx* ctx, int kind, int mode, int order, double rcut, double width);

@@ -48,11 +48,15 @@ __device__ __forceinline__ float ik_rcp(float x)
 template <int KIND>
 __device__ __forceinline__ float ik_kern(float q, float R2s)
 {
-    if (KIND == 0) {            // octic: q = r^2/R^2, (1 - q^2)^2 inside
-        float u = fmaxf(fmaf(-q, q, 1.0f), 0.0f);
+    if (KIND == 0) {            // octic: q = r^2/R^2, (1 - q^2)^2 inside (1 - q^2 <= 1: the
+                                // saturation only clips at 0)
+        float u = __saturatef(fmaf(-q, q, 1.0f));
         return u * u;
-    } else if (KIND == 1) {     // gaussian: q = r^2 * log2(e)/(2 w^2)
-        return q < R2s ? ik_ex2(-q) : 0.0f;
+    } else if (KIND == 1) {     // gaussian: q = r^2 * log2(e)/(2 w^2), cut at q = R2s.  The
+                                // cut as a saturated FMA: (R2s - q) * 2^100 is >= 1 for every
+                                // float q < R2s (they differ by >= 1 ulp of R2s) and <= 0 else
+        const float inside = __saturatef(fmaf(-q, 0x1p100f, R2s * 0x1p100f));
+        return ik_ex2(-q) * inside;
     } else if (KIND == 2) {     // rect
         return q < 1.0f ? 1.0f : 0.0f;
     } else {                    // mollifier: exp(-1/(1-q))
@@ -383,7 +387,8 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                             }
                             float Ma, Mb;
                             up2(M, Ma, Mb);
-                            f32x2 B = mul2(pk2(a.w0, a.w0), pk2(ik_kern<KIND>(Ma, R2s), ik_kern<KIND>(Mb, R2s)));
+                            // node values per grid point in scalar form (no packing moves)
+                            float Ba = a.w0 * ik_kern<KIND>(Ma, R2s), Bb = a.w0 * ik_kern<KIND>(Mb, R2s);
 #pragma unroll
                             for (int t = 0; t < NP; ++t) {
                                 const f32x2 base = add2(M, cq2[t]);
@@ -392,12 +397,10 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                                 float pa, pb, qa, qb;
                                 up2(rp, pa, pb);
                                 up2(rm, qa, qb);
-                                const f32x2 ks = pk2(ik_kern<KIND>(pa, R2s) + ik_kern<KIND>(qa, R2s),
-                                                     ik_kern<KIND>(pb, R2s) + ik_kern<KIND>(qb, R2s));
-                                B = fma2(pk2(a.w[t], a.w[t]), ks, B);
+                                Ba = fmaf(a.w[t], ik_kern<KIND>(pa, R2s) + ik_kern<KIND>(qa, R2s), Ba);
+                                Bb = fmaf(a.w[t], ik_kern<KIND>(pb, R2s) + ik_kern<KIND>(qb, R2s), Bb);
                             }
-                            float Ba, Bb;
-                            up2(B, Ba, Bb);
+                            f32x2 B;
                             if constexpr (MLPM) { // r_j outside the support: a record, not a term
                                 const f32x2 rj2 = fma2(pk2(-2.f, -2.f), mb, add2(M, pk2(hh, hh)));
                                 float ra, rb, mba, mbb;
