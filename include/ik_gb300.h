@@ -37,7 +37,8 @@ enum ik_quad_mode { IK_QUAD_FIXEDPOINT = 0, IK_QUAD_ADAPTIVE = 1, IK_QUAD_EXACT 
 enum ik_precision { IK_PREC_FP64 = 0,   /* plain path: FP64 throughout */
                     IK_PREC_FP32 = 1 }; /* tuned path: FP32 pair arithmetic, compensated
                                            accumulation, FP64 min-image/selection/final */
-enum ik_field { IK_FIELD_VIRIAL = 1, IK_FIELD_KINETIC = 2 };
+enum ik_field { IK_FIELD_VIRIAL = 1, IK_FIELD_KINETIC = 2,
+                IK_FIELD_ELASTIC = 4 }; /* ElasticVirialStressField (needs displacements) */
 
 typedef struct ik_ctx ik_ctx;
 
@@ -95,6 +96,13 @@ int ik_reserve_slots(ik_ctx* ctx, int nslots);
  * slot's computations use them instead of the context's ik_set_box / ik_set_grid,
  * and its fields have g grid points.  Same meaning as SimBox::SimBox (SimBox.cc:25-45)
  * and the ikcalculator grid (irvingkirkwood/__init__.py:44-51), per frame. */
+/* Per-particle displacements u (n x 3, the slot's particle order) for the elastic
+ * virial field IK_FIELD_ELASTIC: per neighbour pair within max_rcut,
+ * 0.5 * bond * (f(|r+u_ij|) (r+u_ij)(x)(r+u_ij) - f(|r|) r(x)r), u_ij = u_j - u_i.
+ * Replaces ParticleSystem::setDisplacement (ParticleSystem.cc:60-67) feeding
+ * ElasticVirialStress (ListofCommonObservables.h:86-122) in ElasticVirialStressField
+ * (irvingkirkwood/module-irvingkirkwood.cpp:10-11). */
+int ik_upload_displacement(ik_ctx* ctx, int slot, int64_t n, const double* disp);
 int ik_set_slot_geometry(ik_ctx* ctx, int slot, int dim, const double boxsize[3], const double origin[3],
                          int64_t g, const double* xyz);
 int ik_upload_frame(ik_ctx* ctx, int slot, int64_t n, const double* pos, const double* vel,

@@ -555,6 +555,7 @@ typedef struct {
     const double* diam; const ikor_poly12* pot; const ikor_cg* cg;
     const int64_t* noff; const int32_t* nidx;
     const double* x; double* vir; double* kin; int dim;
+    const double* disp; double* ela; /* elastic virial (ElasticVirialStress), or NULL */
 } g_ctx;
 
 static void g_visit(void* vctx, int64_t i)
@@ -587,13 +588,54 @@ static void g_visit(void* vctx, int64_t i)
         for (int b = 0; b < D; ++b)
             for (int a = 0; a < D; ++a)
                 c->vir[a + D * b] += hb * ((fdr * rij[a]) * rij[b]);
+        if (c->ela) {
+            /* ElasticVirialStress::compute (ListofCommonObservables.h:86-122) through
+             * VirialStress::compute_cg (:72-82): the pair force at the displaced
+             * separation r + u_ij (u_ij = u_j - u_i) minus the force at r, times
+             * 0.5 * bond */
+            const double* ui = &c->disp[3 * i];
+            const double* uj = &c->disp[3 * j];
+            double uij[3] = {uj[0] - ui[0], uj[1] - ui[1], uj[2] - ui[2]};
+            double ur[3] = {uij[0] + rij[0], uij[1] + rij[1], uij[2] + rij[2]};
+            double f1 = ikor_force_divr(c->pot, dot3(ur), c->diam[i], c->diam[j]);
+            for (int b = 0; b < D; ++b)
+                for (int a = 0; a < D; ++a) {
+                    double t = (f1 * ur[a]) * ur[b] - (fdr * rij[a]) * rij[b];
+                    c->ela[a + D * b] += hb * t;
+                }
+        }
     }
 }
+
+static int compute_impl(const ikor_box* box, int64_t n, const double* pos, const double* vel,
+                        const double* mass, const double* diam, const double* disp,
+                        const ikor_poly12* pot, const ikor_cg* cg, double max_rcut, int64_t g0,
+                        int64_t g1, const double* grid, double* virial, double* kinetic,
+                        double* elastic, int nthreads);
 
 int ikor_compute_range(const ikor_box* box, int64_t n, const double* pos, const double* vel,
                        const double* mass, const double* diam, const ikor_poly12* pot,
                        const ikor_cg* cg, double max_rcut, int64_t g0, int64_t g1,
                        const double* grid, double* virial, double* kinetic, int nthreads)
+{
+    return compute_impl(box, n, pos, vel, mass, diam, NULL, pot, cg, max_rcut, g0, g1, grid, virial,
+                        kinetic, NULL, nthreads);
+}
+
+int ikor_compute_elastic(const ikor_box* box, int64_t n, const double* pos, const double* disp,
+                         const double* diam, const ikor_poly12* pot, const ikor_cg* cg,
+                         double max_rcut, int64_t g0, int64_t g1, const double* grid,
+                         double* virial, double* elastic, int nthreads)
+{
+    return compute_impl(box, n, pos, NULL, NULL, diam, disp, pot, cg, max_rcut, g0, g1, grid, virial,
+                        NULL, elastic, nthreads);
+}
+
+static int compute_impl(const ikor_box* box, int64_t n, const double* pos, const double* vel,
+                        const double* mass, const double* diam, const double* disp,
+                        const ikor_poly12* pot, const ikor_cg* cg, double max_rcut, int64_t g0,
+                        int64_t g1, const double* grid, double* virial, double* kinetic,
+                        double* elastic, int nthreads)
 {
     int D = box->dim;
     if (D != 2 && D != 3) return -1;
@@ -614,10 +656,11 @@ int ikor_compute_range(const ikor_box* box, int64_t n, const double* pos, const 
     for (int64_t g = g0; g < g1; ++g) {
         double* vir = &virial[(g - g0) * DD];
         double* kin = kinetic ? &kinetic[(g - g0) * DD] : NULL;
+        double* ela = elastic ? &elastic[(g - g0) * DD] : NULL;
         double kdummy[9];
-        for (int k = 0; k < DD; ++k) { vir[k] = 0.0; if (kin) kin[k] = 0.0; }
+        for (int k = 0; k < DD; ++k) { vir[k] = 0.0; if (kin) kin[k] = 0.0; if (ela) ela[k] = 0.0; }
         g_ctx c = {box, pos, vel, mass, diam, pot, cg, noff, nidx, &grid[3 * g], vir,
-                   kin ? kin : kdummy, D};
+                   kin ? kin : kdummy, D, disp, ela};
         if (!kin) { c.vel = NULL; }
         cell_query(box, &cl, &grid[3 * g], cg->rcut, g_visit, &c);
     }

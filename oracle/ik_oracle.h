@@ -73,6 +73,15 @@ int64_t ikor_neighbors(const ikor_box* box, int64_t n, const double* pos, double
  * vel/mass may be NULL (kinetic field then zero).  grid: g x 3.
  * virial/kinetic: g x dim x dim, column-major per grid point (index a + dim*b).
  * nthreads <= 0: OpenMP default.  Returns 0 or a negative error. */
+/* The same gather with the elastic virial field of ElasticVirialStressField
+ * (ListofCommonObservables.h:86-122 through VirialStress::compute_cg, :72-82): per pair
+ * 0.5 * bond * (f(|r+u|) (r+u)(x)(r+u) - f(|r|) r(x)r), u = disp_j - disp_i, over the
+ * neighbours within max_rcut of the undisplaced frame.  disp: n x 3. */
+int ikor_compute_elastic(const ikor_box* box, int64_t n, const double* pos, const double* disp,
+                         const double* diam, const ikor_poly12* pot, const ikor_cg* cg,
+                         double max_rcut, int64_t g0, int64_t g1, const double* grid,
+                         double* virial, double* elastic, int nthreads);
+
 int ikor_compute(const ikor_box* box, int64_t n, const double* pos, const double* vel,
                  const double* mass, const double* diam, const ikor_poly12* pot,
                  const ikor_cg* cg, double max_rcut, int64_t g, const double* grid,

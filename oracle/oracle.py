@@ -70,6 +70,10 @@ def lib():
                                          C.POINTER(Poly12), C.POINTER(CG), C.c_double,
                                          C.c_int64, C.c_int64, dp, dp, dp, C.c_int]
         L.ikor_compute_range.restype = C.c_int
+        L.ikor_compute_elastic.argtypes = [C.POINTER(Box), C.c_int64, dp, dp, dp, C.POINTER(Poly12),
+                                           C.POINTER(CG), C.c_double, C.c_int64, C.c_int64, dp, dp, dp,
+                                           C.c_int]
+        L.ikor_compute_elastic.restype = C.c_int
         L.ikor_global_virial.argtypes = [C.POINTER(Box), C.c_int64, dp, dp, C.POINTER(Poly12),
                                          C.c_double, dp]
         _LIB = L
@@ -209,6 +213,30 @@ def compute(box, pos, diam, pot, cg, grid, vel=None, mass=None, max_rc=None,
     vir = vir.reshape(g1 - g0, D, D).transpose(0, 2, 1).copy()
     kin = kin.reshape(g1 - g0, D, D).transpose(0, 2, 1).copy()
     return vir, kin
+
+
+def compute_elastic(box, pos, disp, diam, pot, cg, grid, max_rc=None, g0=0, g1=None, nthreads=0):
+    """Virial and elastic virial fields (ElasticVirialStressField) over grid points [g0, g1);
+    disp: per-particle displacements (n x 3).  Returns (virial, elastic), [g, a, b]."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    disp = np.ascontiguousarray(disp, dtype=np.float64)
+    diam = np.ascontiguousarray(diam, dtype=np.float64)
+    grid = np.ascontiguousarray(grid, dtype=np.float64)
+    n = len(pos)
+    if g1 is None:
+        g1 = len(grid)
+    if max_rc is None:
+        max_rc = max_rcut(pot.scaled_rcut, diam)
+    D = box.dim
+    vir = np.zeros((g1 - g0) * D * D)
+    ela = np.zeros((g1 - g0) * D * D)
+    rc = lib().ikor_compute_elastic(C.byref(box), n, _dp(pos), _dp(disp), _dp(diam), C.byref(pot), C.byref(cg),
+                                    max_rc, g0, g1, _dp(grid), _dp(vir), _dp(ela), nthreads)
+    if rc != 0:
+        raise ValueError(f"oracle compute failed ({rc}): box too small for the cut-offs")
+    vir = vir.reshape(g1 - g0, D, D).transpose(0, 2, 1).copy()
+    ela = ela.reshape(g1 - g0, D, D).transpose(0, 2, 1).copy()
+    return vir, ela
 
 
 def global_virial(box, pos, diam, pot, max_rc=None):

@@ -94,7 +94,9 @@ struct Slot {
     bool has_vel = false, has_mass = false;
     double dmax = 0.0;
     DevBuf pos, vel, mass, diam;
-    DevBuf vir, kin;
+    DevBuf disp; // displacements for the elastic virial field (ik_upload_displacement)
+    bool has_disp = false;
+    DevBuf vir, kin, ela;
     int last_prec = -1, last_fields = 0;
     DevBuf counters; // 4 x u64: bonds, pairs, triples, spare
     cudaEvent_t done = nullptr; // completion of the slot's last computation (on its lane)
@@ -114,6 +116,7 @@ struct Lane {
     DevBuf work_counter;
     DevBuf vir2, kin2; // double-float outputs of the FP32 gather
     DevBuf mlp_rec, mlp_rid, mlp_count, corr; // surrogate records and fixed-point corrections
+    DevBuf eb64, ec64, eb32, ec32, enb, ecnt;  // elastic-field bond records, scratch counters
 };
 constexpr int IK_LANES = 4;
 
@@ -144,6 +147,8 @@ struct ik_ctx {
     DevBuf status, maxnb;
     DevBuf bsum_q; // scan scratch of the neighbour queries (main stream)
     int maxb = 0, halo_cap = 0;
+    int maxbe = 0;      // elastic-field records per particle (neighbours within max_rcut)
+    DevBuf maxnbe;
     // neighbour-query scratch
     DevBuf q_cell_of, q_rank, q_count, q_start, q_sorted, q_cnt, q_offs, q_idx, q_flag;
     std::vector<Slot> slots;
@@ -157,7 +162,7 @@ struct ik_ctx {
     int captured_lanes = 0;
     cudaGraphExec_t batch_exec = nullptr;
     std::vector<int> batch_slots;
-    int batch_prec = -1, batch_fields = 0, batch_maxb = 0, batch_halo = 0;
+    int batch_prec = -1, batch_fields = 0, batch_maxb = 0, batch_halo = 0, batch_maxbe = 0;
     int64_t batch_geom_version = -1, batch_slot_version = -1;
     int64_t geom_version = 0, slot_version = 0, config_version = 0;
     int64_t batch_config_version = -1, batch_alloc_epoch = -1;
@@ -296,7 +301,13 @@ int ensure_geometry(ik_ctx* c)
                 k.w[a] = x; // non-periodic axis: absolute (2D z is 0)
             }
         }
-        k.bin = ((int64_t)bcoord[2] * nb[1] + bcoord[1]) * nb[0] + bcoord[0];
+        // bins in Morton order: consecutive work items are spatial neighbours, so the
+        // warps of a CTA (which take consecutive items) share halo particles and bond
+        // records in L1
+        int64_t bm = 0;
+        for (int b = 0; b < 21; ++b)
+            for (int a = 0; a < D; ++a) bm |= (int64_t)((bcoord[a] >> b) & 1) << (b * D + a);
+        k.bin = bm;
         uint64_t m = 0;
         for (int b = 0; b < 10; ++b)
             for (int a = 0; a < D; ++a) m |= (uint64_t)((qv[a] >> b) & 1u) << (b * D + a);
@@ -421,6 +432,36 @@ int slot_ok(ik_ctx* c, int slot)
     return IK_OK;
 }
 
+// Elastic-field bond records of slot s on lane L (k_bonds64e); the cell list is built.
+int elastic_bonds(ik_ctx* c, Slot& s, Lane& L, const IkGeom& g, int n)
+{
+    const int D = c->dim, NC = D == 2 ? 3 : 6, CW = D == 2 ? 1 : 2;
+    if (!s.has_disp) return fail(IK_ERR_STATE, "the elastic field needs displacements (ik_upload_displacement)");
+    if (c->maxbe == 0) c->maxbe = D == 2 ? 32 : 63;
+    if ((size_t)std::max(n, 1) * (size_t)c->maxbe >= ((size_t)1 << 25))
+        return fail(IK_ERR_UNSUPPORTED, "elastic field: n * %d neighbour records exceed 2^25", c->maxbe);
+    const size_t nrec = (size_t)c->maxbe * std::max(n, 1);
+    ENS(s.ela, sizeof(double) * NC * std::max<int64_t>(c->geo.G, 1));
+    ENS(L.eb64, sizeof(IkB64) * nrec);
+    ENS(L.ec64, sizeof(double) * NC * nrec);
+    ENS(L.eb32, sizeof(float4) * nrec);
+    ENS(L.ec32, sizeof(float4) * CW * nrec);
+    ENS(L.enb, sizeof(int) * (std::max(n, 1) + 1));
+    if (n > 0) {
+        k_bonds64e<<<(n + 127) / 128, 128, 0, L.st>>>(g, c->pot, c->cg.kappa, n, L.sorted.as<int>(),
+                                                      L.cell_of.as<int>(), s.pos.as<double>(), s.disp.as<double>(),
+                                                      s.diam.as<double>(), L.cell_start.as<int>(),
+                                                      L.eb64.as<IkB64>(), L.ec64.as<double>(), L.eb32.as<float4>(),
+                                                      L.ec32.as<float4>(), c->maxbe, L.enb.as<int>(),
+                                                      c->status.as<int>(), c->maxnbe.as<int>());
+        CK(cudaGetLastError());
+        c->launches += 1;
+    } else if (c->geo.G > 0) {
+        CK(cudaMemsetAsync(s.ela.p, 0, sizeof(double) * NC * c->geo.G, L.st));
+    }
+    return IK_OK;
+}
+
 int enqueue(ik_ctx* c, int slot, int prec, int fields)
 {
     Slot& s = c->slots[(size_t)slot];
@@ -474,12 +515,15 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
                             !(c->flags & IK_FLAG_CSR_BONDS);
         ENS(L.bonds_tmp, sizeof(float4) * (size_t)c->maxb * std::max(n, 1));
         ENS(L.nb32, sizeof(int) * (std::max(n, 1) + 1));
-        CK(launch_bonds32(D, g, c->pot, c->cg.kappa, n, L.prec.as<IkPRec>(), L.diam32.as<float>(),
-                          L.cell_start.as<int>(), L.plo.as<float4>(), L.pos64.as<IkB64>(),
-                          L.bonds_tmp.as<float4>(), c->maxb, L.nb32.as<int>(), c->status.as<int>(),
-                          c->maxnb.as<int>(), stride ? cnt : nullptr, L.st));
-        c->launches += n > 0 ? 1 : 0;
-        if (!stride) {
+        const bool main_pass = (fields & (IK_FIELD_VIRIAL | IK_FIELD_KINETIC)) != 0;
+        if (main_pass) {
+            CK(launch_bonds32(D, g, c->pot, c->cg.kappa, n, L.prec.as<IkPRec>(), L.diam32.as<float>(),
+                              L.cell_start.as<int>(), L.plo.as<float4>(), L.pos64.as<IkB64>(),
+                              L.bonds_tmp.as<float4>(), c->maxb, L.nb32.as<int>(), c->status.as<int>(),
+                              c->maxnb.as<int>(), stride ? cnt : nullptr, L.st));
+            c->launches += n > 0 ? 1 : 0;
+        }
+        if (!stride && main_pass) {
             ENS(L.bonds32, sizeof(float4) * (size_t)c->maxb * std::max(n, 1));
             ENS(L.boff, sizeof(int) * (std::max(n, 1) + 1));
             ENS(L.bsum, sizeof(int) * ((std::max(n, 1) + 4095) / 4096 + 1));
@@ -552,7 +596,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         }
         size_t smem = (size_t)IK_WARPS_GATHER * ((size_t)c->halo_cap * 20 + (size_t)a.qcap * 4);
         int blocks = std::min(c->geo.nitems, c->sm_count * (c->tune_blocks_per_sm > 0 ? c->tune_blocks_per_sm : 2));
-        if (blocks > 0) {
+        if (blocks > 0 && main_pass) {
             CK(launch_gather32(a, c->cg.kind, (c->flags & IK_FLAG_LANE_KAHAN) != 0 && !mlp, mlp, blocks,
                                32 * IK_WARPS_GATHER, smem, L.st));
             c->launches += 1;
@@ -570,11 +614,39 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
                                (a.fields & 1) ? s.vir.as<double>() : nullptr, 0.5 * norm, L.kin2.as<float2>(),
                                (a.fields & 2) ? s.kin.as<double>() : nullptr, norm, (long long)NC * c->geo.G, L.st));
         c->launches += (c->geo.G > 0 && a.fields) ? 1 : 0;
+        if (fields & IK_FIELD_ELASTIC) { // the elastic virial field: same staging, elastic records
+            if (int r2 = elastic_bonds(c, s, L, g, n)) return r2;
+            GatherArgs32 e = a;
+            e.boff = nullptr;
+            e.nb = L.enb.as<int>();
+            e.bonds = L.eb32.as<float4>();
+            e.bcoef = L.ec32.as<float4>();
+            e.maxb = c->maxbe;
+            e.qcap = 32 * (c->maxbe + 1);
+            e.fields = IK_FIELD_VIRIAL;
+            e.mlp_rec = nullptr;
+            e.mlp_rid = nullptr;
+            e.mlp_count = nullptr;
+            e.cnt_records = nullptr;
+            ENS(L.ecnt, sizeof(unsigned long long) * 2);
+            e.cnt_pairs = L.ecnt.as<unsigned long long>();
+            e.cnt_triples = e.cnt_pairs + 1;
+            CK(cudaMemsetAsync(L.work_counter.p, 0, sizeof(int), L.st));
+            const size_t esmem = (size_t)IK_WARPS_GATHER * ((size_t)c->halo_cap * 20 + (size_t)e.qcap * 4);
+            if (blocks > 0) {
+                CK(launch_gather32(e, c->cg.kind, false, false, blocks, 32 * IK_WARPS_GATHER, esmem, L.st));
+                c->launches += 1;
+            }
+            CK(launch_pairs_to_f64(L.vir2.as<float2>(), nullptr, s.ela.as<double>(), 0.5 * norm, nullptr, nullptr,
+                                   0.0, (long long)NC * c->geo.G, L.st));
+            c->launches += c->geo.G > 0 ? 1 : 0;
+        }
     } else {
         if (timing) CK(cudaEventRecord(c->ev[1], L.st));
         ENS(L.bonds64, sizeof(IkB64) * (size_t)c->maxb * std::max(n, 1));
         ENS(L.nb64, sizeof(int) * std::max(n, 1));
-        if (n > 0) {
+        const bool main_pass = (fields & (IK_FIELD_VIRIAL | IK_FIELD_KINETIC)) != 0;
+        if (n > 0 && main_pass) {
             k_bonds64<<<(n + 127) / 128, 128, 0, L.st>>>(
                 g, c->pot, n, L.sorted.as<int>(), L.cell_of.as<int>(), s.pos.as<double>(), s.diam.as<double>(),
                 L.cell_start.as<int>(), L.bonds64.as<IkB64>(), c->maxb, L.nb64.as<int>(), c->status.as<int>(),
@@ -606,8 +678,23 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         a.fields = fields;
         if ((fields & IK_FIELD_KINETIC) && !s.has_vel)
             CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->geo.G, L.st));
-        CK(launch_gather64(a, L.st));
-        c->launches += (n > 0 ? 1 : 0) + (c->geo.G > 0 ? 1 : 0);
+        if (main_pass) {
+            CK(launch_gather64(a, L.st));
+            c->launches += (n > 0 ? 1 : 0) + (c->geo.G > 0 ? 1 : 0);
+        }
+        if (fields & IK_FIELD_ELASTIC) { // the elastic virial field
+            if (int r2 = elastic_bonds(c, s, L, g, n)) return r2;
+            GatherArgs64 e = a;
+            e.bonds = L.eb64.as<IkB64>();
+            e.nb = L.enb.as<int>();
+            e.ecoef = L.ec64.as<double>();
+            e.maxb = c->maxbe;
+            e.out_vir = s.ela.as<double>();
+            e.out_kin = nullptr;
+            e.fields = IK_FIELD_VIRIAL;
+            CK(launch_gather64(e, L.st));
+            c->launches += c->geo.G > 0 ? 1 : 0;
+        }
     }
     if (timing) CK(cudaEventRecord(c->ev[3], L.st));
     s.last_prec = prec;
@@ -701,7 +788,8 @@ int ik_create(ik_ctx** out, int device)
     }
     c->slots.resize(1);
     int r;
-    if ((r = c->status.ensure(sizeof(int))) || (r = c->maxnb.ensure(sizeof(int)))) {
+    if ((r = c->status.ensure(sizeof(int))) || (r = c->maxnb.ensure(sizeof(int))) ||
+        (r = c->maxnbe.ensure(sizeof(int)))) {
         ik_destroy(c);
         return r;
     }
@@ -712,6 +800,7 @@ int ik_create(ik_ctx** out, int device)
         }
     cudaMemset(c->status.p, 0, sizeof(int));
     cudaMemset(c->maxnb.p, 0, sizeof(int));
+    cudaMemset(c->maxnbe.p, 0, sizeof(int));
     *out = c;
     return IK_OK;
 }
@@ -987,6 +1076,24 @@ int ik_upload_frame(ik_ctx* c, int slot, int64_t n, const double* pos, const dou
     return IK_OK;
 }
 
+int ik_upload_displacement(ik_ctx* c, int slot, int64_t n, const double* disp)
+{
+    if (int r = check_ctx(c)) return r;
+    if (int r = slot_ok(c, slot)) return r;
+    Slot& s = c->slots[(size_t)slot];
+    if (n != s.n) return fail(IK_ERR_ARG, "displacements for %lld particles, the slot holds %lld", (long long)n, (long long)s.n);
+    if (n > 0 && !disp) return fail(IK_ERR_ARG, "null displacements");
+    for (int64_t i = 0; i < 3 * n; ++i)
+        if (!std::isfinite(disp[i])) return fail(IK_ERR_ARG, "displacement %lld is not finite", (long long)(i / 3));
+    if (s.done_recorded) CK(cudaStreamWaitEvent(c->stream, s.done, 0)); // the old ones may be in use
+    const void* old = s.disp.p;
+    ENS(s.disp, sizeof(double) * 3 * std::max<int64_t>(n, 1));
+    if (n > 0) CK(cudaMemcpyAsync(s.disp.p, disp, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c->stream));
+    if (!s.has_disp || old != s.disp.p) ++c->slot_version; // captured graphs hold the old buffer
+    s.has_disp = true;
+    return IK_OK;
+}
+
 int ik_set_frame(ik_ctx* c, int64_t n, const double* pos, const double* vel, const double* mass,
                  const double* diam)
 {
@@ -998,7 +1105,7 @@ int ik_compute_slot(ik_ctx* c, int slot, int precision, int fields)
     if (int r = check_ctx(c)) return r;
     if (int r = slot_ok(c, slot)) return r;
     if (precision != IK_PREC_FP64 && precision != IK_PREC_FP32) return fail(IK_ERR_ARG, "unknown precision %d", precision);
-    if (fields < 1 || fields > 3) return fail(IK_ERR_ARG, "fields mask must be 1, 2 or 3");
+    if (fields < 1 || fields > 7) return fail(IK_ERR_ARG, "fields mask must be in [1, 7]");
     c->pending.push_back({slot, precision, fields});
     if (int r = prepare_enqueue(c, slot, precision, fields)) { c->pending.pop_back(); return r; }
     return IK_OK;
@@ -1010,7 +1117,7 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
     if (count < 1 || !slots) return fail(IK_ERR_ARG, "empty batch");
     for (int k = 0; k < count; ++k) if (int r = slot_ok(c, slots[k])) return r;
     if (precision != IK_PREC_FP64 && precision != IK_PREC_FP32) return fail(IK_ERR_ARG, "unknown precision %d", precision);
-    if (fields < 1 || fields > 3) return fail(IK_ERR_ARG, "fields mask must be 1, 2 or 3");
+    if (fields < 1 || fields > 7) return fail(IK_ERR_ARG, "fields mask must be in [1, 7]");
     for (int k = 0; k < count; ++k) { // every slot ready, its geometry current
         GeoSwap gs(c, slots[k]);
         if (int r = ensure_ready(c)) return r;
@@ -1022,6 +1129,7 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
     std::vector<int> key(slots, slots + count);
     const bool reuse = c->batch_exec && key == c->batch_slots && c->batch_prec == precision &&
                        c->batch_fields == fields && c->batch_maxb == c->maxb && c->batch_halo == c->halo_cap &&
+                       c->batch_maxbe == c->maxbe &&
                        c->batch_geom_version == c->geom_version && c->batch_slot_version == c->slot_version &&
                        c->batch_config_version == c->config_version && c->batch_alloc_epoch == g_alloc_epoch.load() &&
                        !(c->flags & IK_FLAG_TIMING);
@@ -1063,6 +1171,7 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
         c->batch_fields = fields;
         c->batch_maxb = c->maxb;
         c->batch_halo = c->halo_cap;
+        c->batch_maxbe = c->maxbe;
         c->batch_geom_version = c->geom_version;
         c->batch_slot_version = c->slot_version;
         c->batch_config_version = c->config_version;
@@ -1103,9 +1212,16 @@ int ik_synchronize(ik_ctx* c)
         }
         bool grow = false;
         if (st & IK_ST_BOND_OVERFLOW) {
-            int nm = std::max(mx, c->maxb + 1);
-            if (nm > 63) { c->pending.clear(); return fail(IK_ERR_CAPACITY, "a particle has %d force-active bonds (max 63)", mx); }
-            c->maxb = nm;
+            int mxe = 0;
+            CK(cudaMemcpy(&mxe, c->maxnbe.p, sizeof(int), cudaMemcpyDeviceToHost));
+            if (mx > c->maxb) {
+                if (mx > 63) { c->pending.clear(); return fail(IK_ERR_CAPACITY, "a particle has %d force-active bonds (max 63)", mx); }
+                c->maxb = mx;
+            }
+            if (mxe > c->maxbe) {
+                if (mxe > 63) { c->pending.clear(); return fail(IK_ERR_CAPACITY, "a particle has %d neighbours within max_rcut (max 63 for the elastic field)", mxe); }
+                c->maxbe = mxe;
+            }
             grow = true;
         }
         if (st & IK_ST_MMA_TIMEOUT) { c->pending.clear(); return fail(IK_ERR_TIMEOUT, "a tensor-core wait gave up"); }
@@ -1139,14 +1255,15 @@ int ik_get_field(ik_ctx* c, int slot, int field, double* out, int64_t count)
     if (int r = check_ctx(c)) return r;
     if (int r = slot_ok(c, slot)) return r;
     GeoSwap gs(c, slot);
-    if (field != IK_FIELD_VIRIAL && field != IK_FIELD_KINETIC) return fail(IK_ERR_ARG, "unknown field %d", field);
+    if (field != IK_FIELD_VIRIAL && field != IK_FIELD_KINETIC && field != IK_FIELD_ELASTIC)
+        return fail(IK_ERR_ARG, "unknown field %d", field);
     if (int r = ik_synchronize(c)) return r;
     Slot& s = c->slots[(size_t)slot];
     if (s.last_prec < 0) return fail(IK_ERR_STATE, "slot %d has not been computed", slot);
     const int D = c->dim, NC = D == 2 ? 3 : 6;
     if (count != c->geo.G * D * D) return fail(IK_ERR_ARG, "output needs %lld doubles (got %lld)", (long long)(c->geo.G * D * D), (long long)count);
     std::vector<double> tmp((size_t)(NC * c->geo.G));
-    const DevBuf& src = field == IK_FIELD_VIRIAL ? s.vir : s.kin;
+    const DevBuf& src = field == IK_FIELD_VIRIAL ? s.vir : (field == IK_FIELD_KINETIC ? s.kin : s.ela);
     if (c->geo.G > 0) CK(cudaMemcpy(tmp.data(), src.p, sizeof(double) * NC * c->geo.G, cudaMemcpyDeviceToHost));
     static const int map2[3][2] = {{0, 0}, {1, 1}, {0, 1}};
     static const int map3[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
@@ -1445,11 +1562,12 @@ int ik_download_field_async(ik_ctx* c, int slot, int field, double* host_out, in
     if (int r = check_ctx(c)) return r;
     if (int r = slot_ok(c, slot)) return r;
     GeoSwap gs(c, slot);
-    if (field != IK_FIELD_VIRIAL && field != IK_FIELD_KINETIC) return fail(IK_ERR_ARG, "unknown field %d", field);
+    if (field != IK_FIELD_VIRIAL && field != IK_FIELD_KINETIC && field != IK_FIELD_ELASTIC)
+        return fail(IK_ERR_ARG, "unknown field %d", field);
     const int NC = c->dim == 2 ? 3 : 6;
     if (!host_out || count != c->geo.G * NC) return fail(IK_ERR_ARG, "output needs %lld doubles", (long long)(c->geo.G * NC));
     Slot& s = c->slots[(size_t)slot];
-    const DevBuf& src = field == IK_FIELD_VIRIAL ? s.vir : s.kin;
+    const DevBuf& src = field == IK_FIELD_VIRIAL ? s.vir : (field == IK_FIELD_KINETIC ? s.kin : s.ela);
     if (!src.p) return fail(IK_ERR_STATE, "slot %d has not been computed", slot);
     if (s.done_recorded) CK(cudaStreamWaitEvent(c->stream, s.done, 0));
     if (c->geo.G > 0) CK(cudaMemcpyAsync(host_out, src.p, sizeof(double) * NC * c->geo.G, cudaMemcpyDeviceToHost, c->stream));

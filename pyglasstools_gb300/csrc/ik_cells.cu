@@ -190,6 +190,85 @@ __global__ void k_bonds64(IkGeom g, IkPoly12 pot, int n, const int* __restrict__
 }
 
 // ---------------------------------------------------------------------------
+// 5b. Bonds of the elastic virial field (ElasticVirialStress::compute,
+//     ListofCommonObservables.h:86-122, through VirialStress::compute_cg, :72-82):
+//     every neighbour within max_rcut of the undisplaced frame, u_ij = u_j - u_i,
+//     coefficient C = 0.5 (f(|r+u|) (r+u)(x)(r+u) - f(|r|) r(x)r), all in FP64; a
+//     record is kept when either force is non-zero.  Written for both gathers at a
+//     fixed stride of maxb per particle (cell order): FP64 {r_ij} + C (NC doubles),
+//     FP32 {kappa r_ij / 2} + C (float4 x CW).
+__global__ void k_bonds64e(IkGeom g, IkPoly12 pot, float kappa, int n, const int* __restrict__ sorted,
+                           const int* __restrict__ cell_of, const double* __restrict__ pos,
+                           const double* __restrict__ disp, const double* __restrict__ diam,
+                           const int* __restrict__ cell_start, IkB64* __restrict__ b64,
+                           double* __restrict__ c64, float4* __restrict__ b32, float4* __restrict__ c32,
+                           int maxb, int* __restrict__ nb, int* __restrict__ status, int* __restrict__ maxnb)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int NC = g.dim == 2 ? 3 : 6, CW = g.dim == 2 ? 1 : 2;
+    const int i = sorted[p];
+    const int c = cell_of[i];
+    const int cx = c % g.nc[0], cy = (c / g.nc[0]) % g.nc[1], cz = c / (g.nc[0] * g.nc[1]);
+    const double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2], di = diam[i];
+    const double uxi = disp[3 * i], uyi = disp[3 * i + 1], uzi = disp[3 * i + 2];
+    const float hk = 0.5f * kappa;
+    int cnt = 0;
+    StencilAxis az = ik_axis(g, 2, cz), ay = ik_axis(g, 1, cy), ax = ik_axis(g, 0, cx);
+    for (int zz = az.lo; zz <= az.hi; ++zz) {
+        const int wz = g.dim == 3 ? ik_wrap(zz, g.nc[2]) : 0;
+        for (int yy = ay.lo; yy <= ay.hi; ++yy) {
+            const int wy = ik_wrap(yy, g.nc[1]);
+            for (int xx = ax.lo; xx <= ax.hi; ++xx) {
+                const int wx = ik_wrap(xx, g.nc[0]);
+                const int cell = (wz * g.nc[1] + wy) * g.nc[0] + wx;
+                const int e = cell_start[cell + 1];
+                for (int q = cell_start[cell]; q < e; ++q) {
+                    const int j = sorted[q];
+                    if (j == i) continue;
+                    const double dx = ik_minimg(__dsub_rn(pos[3 * j], xi), g.L[0], g.periodic[0]);
+                    const double dy = ik_minimg(__dsub_rn(pos[3 * j + 1], yi), g.L[1], g.periodic[1]);
+                    const double dz = ik_minimg(__dsub_rn(pos[3 * j + 2], zi), g.L[2], g.periodic[2]);
+                    const double rsq = ik_dot3(dx, dy, dz);
+                    if (!(rsq < pot.max_rcut_sq)) continue;
+                    const double sig = ik_sigma64(pot, di, diam[j]);
+                    const double f = ik_active64(pot, rsq, sig) ? ik_force64(pot, rsq, sig) : 0.0;
+                    const double ux = __dadd_rn(__dsub_rn(disp[3 * j], uxi), dx);
+                    const double uy = __dadd_rn(__dsub_rn(disp[3 * j + 1], uyi), dy);
+                    const double uz = __dadd_rn(__dsub_rn(disp[3 * j + 2], uzi), dz);
+                    const double usq = ik_dot3(ux, uy, uz);
+                    const double f1 = ik_active64(pot, usq, sig) ? ik_force64(pot, usq, sig) : 0.0;
+                    if (f == 0.0 && f1 == 0.0) continue;
+                    if (cnt < maxb) {
+                        const double r[3] = {dx, dy, dz}, u[3] = {ux, uy, uz};
+                        const int ia[6] = {0, 1, 2, 0, 0, 1}, ib[6] = {0, 1, 2, 1, 2, 2};
+                        const int ia2[3] = {0, 1, 0}, ib2[3] = {0, 1, 1};
+                        double cc[6];
+                        for (int k = 0; k < NC; ++k) {
+                            const int a_ = g.dim == 2 ? ia2[k] : ia[k], b_ = g.dim == 2 ? ib2[k] : ib[k];
+                            cc[k] = 0.5 * __dsub_rn(__dmul_rn(__dmul_rn(f1, u[a_]), u[b_]),
+                                                    __dmul_rn(__dmul_rn(f, r[a_]), r[b_]));
+                        }
+                        const size_t rec = (size_t)p * maxb + cnt;
+                        b64[rec] = make_ikb64(dx, dy, dz, 0.0);
+                        for (int k = 0; k < NC; ++k) c64[rec * NC + k] = cc[k];
+                        b32[rec] = make_float4(hk * (float)dx, hk * (float)dy, hk * (float)dz, 0.f);
+                        c32[rec * CW] = make_float4((float)cc[0], (float)cc[1], (float)cc[2], NC > 3 ? (float)cc[3] : 0.f);
+                        if (CW == 2) c32[rec * CW + 1] = make_float4((float)cc[4], (float)cc[5], 0.f, 0.f);
+                    }
+                    ++cnt;
+                }
+            }
+        }
+    }
+    nb[p] = cnt < maxb ? cnt : maxb;
+    if (cnt > maxb) {
+        atomicOr(status, IK_ST_BOND_OVERFLOW);
+        atomicMax(maxnb, cnt);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // 6. Candidate neighbour list (FP64, |r_ij|^2 < radius^2, j != i), CSR by
 //    original particle id; count pass, scan, fill pass, per-row sort.
 template <bool FILL>

@@ -176,15 +176,18 @@ __device__ __forceinline__ int ik_red_index(int lane, int k)
 
 // NP: number of symmetric Gauss-Legendre node pairs (compile-time when > 0; 0 = runtime).
 // MLPM: surrogate mode (bonds crossing the edge of the support become records).
-template <int DIM, int KIND, bool KAHAN, int NP, bool MLPM>
+template <int DIM, int KIND, bool KAHAN, int NP, bool MLPM, bool ELA>
 __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
 {
     constexpr int NC = DIM == 2 ? 3 : 6;       // unique tensor components
     constexpr int P = IK_P;
 
     extern __shared__ float4 smem[];
+    __shared__ int s_next; // next item of this CTA's share
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_next = 0;
+    __syncthreads();
     // per warp: staged particles (float4 x,y,z, bits(bond offset << 6 | bond count)),
     // their cell-order indices, and the slot queue
     float4* stage = smem + (size_t)warp * (a.halo_cap + a.halo_cap / 4 + a.qcap / 4);
@@ -234,8 +237,14 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
     };
 
     for (;;) {
+        // work items: first this CTA's contiguous share (spatial neighbours, L1 reuse
+        // across its warps), then a global counter over the remaining tail
         int w = 0;
-        if (lane == 0) w = atomicAdd(a.work_counter, 1);
+        if (lane == 0) {
+            const int per = (int)(((long long)a.nitems * 7 / 8) / gridDim.x);
+            const int k = atomicAdd(&s_next, 1);
+            w = k < per ? (int)blockIdx.x * per + k : per * (int)gridDim.x + atomicAdd(a.work_counter, 1);
+        }
         w = __shfl_sync(FULL, w, 0);
         if (w >= a.nitems) break;
         const int4 it = a.items[w];
@@ -350,18 +359,32 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                     const int m = e & 15;
                     const float hbx = b.x, hby = b.y, hbz = b.z;
                     const float hh = DIM == 3 ? fmaf(hbz, hbz, fmaf(hby, hby, hbx * hbx)) : fmaf(hby, hby, hbx * hbx);
-                    const float fx = b.w * hbx, fy = b.w * hby;
                     float cf[NC];
-                    cf[0] = fx * hbx;
-                    cf[1] = fy * hby;
-                    if (DIM == 2) {
-                        cf[2] = fx * hby;
+                    if constexpr (ELA) { // elastic field: the bond's own coefficient
+                        const int bi = (__float_as_int(sp.w) >> 6) + ((e >> 4) & 63);
+                        const float4 c0 = __ldg(a.bcoef + (size_t)bi * (DIM == 2 ? 1 : 2));
+                        cf[0] = c0.x;
+                        cf[1] = c0.y;
+                        cf[2] = c0.z;
+                        if (DIM == 3) {
+                            const float4 c1 = __ldg(a.bcoef + (size_t)bi * 2 + 1);
+                            cf[3 % NC] = c0.w;
+                            cf[4 % NC] = c1.x;
+                            cf[5 % NC] = c1.y;
+                        }
                     } else {
-                        const float fz = b.w * hbz;
-                        cf[2] = fz * hbz;
-                        cf[3 % NC] = fx * hby;
-                        cf[4 % NC] = fx * hbz;
-                        cf[5 % NC] = fy * hbz;
+                        const float fx = b.w * hbx, fy = b.w * hby;
+                        cf[0] = fx * hbx;
+                        cf[1] = fy * hby;
+                        if (DIM == 2) {
+                            cf[2] = fx * hby;
+                        } else {
+                            const float fz = b.w * hbz;
+                            cf[2] = fz * hbz;
+                            cf[3 % NC] = fx * hby;
+                            cf[4 % NC] = fx * hbz;
+                            cf[5 % NC] = fy * hbz;
+                        }
                     }
                     const float mx0 = sp.x + hbx, my0 = sp.y + hby, mz0 = sp.z + hbz; // bond midpoint
                     float4 crec[P];
@@ -657,10 +680,10 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
     }
 }
 
-template <int DIM, int KIND, bool KAHAN, int NP, bool MLPM = false>
+template <int DIM, int KIND, bool KAHAN, int NP, bool MLPM = false, bool ELA = false>
 static cudaError_t launch_one(const GatherArgs32& a, int blocks, int threads, size_t smem, cudaStream_t st)
 {
-    auto kfn = k_gather32<DIM, KIND, KAHAN, NP, MLPM>;
+    auto kfn = k_gather32<DIM, KIND, KAHAN, NP, MLPM, ELA>;
     cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kfn<<<blocks, threads, smem, st>>>(a);
@@ -686,9 +709,27 @@ static cudaError_t launch_np(const GatherArgs32& a, int kind, int blocks, int th
     return launch_kind<DIM, KAHAN, 0>(a, kind, blocks, threads, smem, st);
 }
 
+template <int DIM, int NP>
+static cudaError_t launch_ela(const GatherArgs32& a, int kind, int blocks, int threads, size_t smem, cudaStream_t st)
+{
+    switch (kind) {
+    case 0: return launch_one<DIM, 0, false, NP, false, true>(a, blocks, threads, smem, st);
+    case 1: return launch_one<DIM, 1, false, NP, false, true>(a, blocks, threads, smem, st);
+    case 2: return launch_one<DIM, 2, false, NP, false, true>(a, blocks, threads, smem, st);
+    default: return launch_one<DIM, 3, false, NP, false, true>(a, blocks, threads, smem, st);
+    }
+}
+
 cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, bool mlp, int blocks, int threads,
                             size_t smem, cudaStream_t st)
 {
+    if (a.bcoef) { // elastic field: plain per-lane sums, no surrogate
+        if (mlp) return cudaErrorInvalidValue;
+        if (a.g.dim == 2) return a.npairs == 2 ? launch_ela<2, 2>(a, kind, blocks, threads, smem, st)
+                                               : launch_ela<2, 0>(a, kind, blocks, threads, smem, st);
+        return a.npairs == 2 ? launch_ela<3, 2>(a, kind, blocks, threads, smem, st)
+                             : launch_ela<3, 0>(a, kind, blocks, threads, smem, st);
+    }
     if (mlp) { // Gaussian kernel only, plain per-lane sums
         if (kind != 1 || kahan) return cudaErrorInvalidValue;
         if (a.g.dim == 2) return a.npairs == 2 ? launch_one<2, 1, false, 2, true>(a, blocks, threads, smem, st)

@@ -125,6 +125,12 @@ __global__ void __launch_bounds__(128) k_gather64(const GatherArgs64 a)
                         IkB64 b = bq[k];
                         double rij[3] = {b.x, b.y, b.z};
                         double bond = ik_bond64(a.cg, a.xs, a.ws, a.nq, x, ri, rij);
+                        if (a.ecoef) { // elastic field: precomputed coefficients (0.5 included)
+                            const double* cc = a.ecoef + ((size_t)q * a.maxb + k) * NC;
+#pragma unroll
+                            for (int cc_i = 0; cc_i < NC; ++cc_i) vir[cc_i] += bond * cc[cc_i];
+                            continue;
+                        }
                         double hb = 0.5 * bond, f = b.w;
                         vir[0] += hb * ((f * rij[0]) * rij[0]);
                         vir[1] += hb * ((f * rij[1]) * rij[1]);

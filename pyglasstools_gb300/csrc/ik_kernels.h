@@ -33,6 +33,10 @@ cudaError_t launch_scan(const int* in, int n, int* out, int* bsum, cudaStream_t 
 __global__ void k_bonds64(IkGeom g, IkPoly12 pot, int n, const int* sorted, const int* cell_of,
                           const double* pos, const double* diam, const int* cell_start, IkB64* bonds,
                           int maxb, int* nb, int* status, int* maxnb);
+__global__ void k_bonds64e(IkGeom g, IkPoly12 pot, float kappa, int n, const int* sorted, const int* cell_of,
+                           const double* pos, const double* disp, const double* diam, const int* cell_start,
+                           IkB64* b64, double* c64, float4* b32, float4* c32, int maxb, int* nb, int* status,
+                           int* maxnb);
 cudaError_t launch_neigh(bool fill, IkGeom g, int n, double r2cut, const int* sorted, const int* cell_of,
                          const double* pos, const int* cell_start, int* count, const int* offs, int* idx,
                          cudaStream_t st);
@@ -62,6 +66,8 @@ struct GatherArgs32 {
                            // particle q at q * maxb (fixed stride), nb[q] of them
     const int* nb;
     const float4* bonds;   // {kappa r_ij / 2, 2 forceDivR / kappa^2}
+    const float4* bcoef;   // elastic field: the bond's stress coefficient (NC floats in
+                           // 1 or 2 float4) instead of f' h (x) h; null otherwise
     int maxb;
     const float4* kin;
     // grid
@@ -87,7 +93,7 @@ struct GatherArgs32 {
 };
 #define IK_MLP_CHUNK 2048
 cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, bool mlp, int blocks, int threads,
-                            size_t smem, cudaStream_t st);
+                            size_t smem, cudaStream_t st);  // a.bcoef != null: elastic coefficients
 // vir = ((double)hi + (double)lo + corr * 2^-32) * svir   (corr: fixed point, may be null),
 // kin = ((double)hi + (double)lo) * skin; a null output is skipped.  One launch.
 cudaError_t launch_pairs_to_f64(const float2* vin, const unsigned long long* corr, double* vout, double svir,
@@ -108,6 +114,7 @@ struct GatherArgs64 {
     const double* mass;
     const int* nb;
     const IkB64* bonds;
+    const double* ecoef;   // elastic field: NC FP64 coefficients per bond record, or null
     int maxb;
     const double* grid;
     int64_t ngrid;

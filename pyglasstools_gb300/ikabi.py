@@ -20,7 +20,7 @@ ERR = {-1: "IK_ERR_ARG", -2: "IK_ERR_CUDA", -3: "IK_ERR_STATE", -4: "IK_ERR_BOX"
 CG = {"octic": 0, "gaussian": 1, "rect": 2, "mollifier": 3}
 QUAD = {"fixedpoint": 0, "adaptive": 1, "exact": 2, "mlp": 3}
 PREC = {"fp64": 0, "fp32": 1}
-FIELD_VIRIAL, FIELD_KINETIC = 1, 2
+FIELD_VIRIAL, FIELD_KINETIC, FIELD_ELASTIC = 1, 2, 4
 FLAG_TIMING, FLAG_LANE_KAHAN, FLAG_CSR_BONDS = 1, 2, 4
 TUNE = {"bin_points": 1, "blocks_per_sm": 2, "halo_cap": 3}
 
@@ -55,6 +55,7 @@ def lib():
             "ik_set_grid": ([vp, i64, dp], i32),
             "ik_reserve_slots": ([vp, i32], i32),
             "ik_set_slot_geometry": ([vp, i32, i32, dp, dp, i64, dp], i32),
+            "ik_upload_displacement": ([vp, i32, i64, dp], i32),
             "ik_upload_frame": ([vp, i32, i64, dp, dp, dp, dp], i32),
             "ik_set_frame": ([vp, i64, dp, dp, dp, dp], i32),
             "ik_compute_slot": ([vp, i32, i32, i32], i32),
@@ -181,6 +182,11 @@ class IKContext:
     # frames ----------------------------------------------------------------
     def reserve_slots(self, n):
         check(lib().ik_reserve_slots(self._h, n))
+
+    def upload_displacement(self, disp, slot=0):
+        """Per-particle displacements (n x 3) for the elastic virial field."""
+        d = _c64(disp, (-1, 3))
+        check(lib().ik_upload_displacement(self._h, slot, len(d), _dp(d)))
 
     def set_slot_geometry(self, slot, dim, box, grid, origin=(0.0, 0.0, 0.0)):
         """Give `slot` a box and grid of its own (uneven batches)."""
