@@ -478,6 +478,8 @@ struct IrvingKirkwood {
                 uploaded = sys->version;
                 uploaded_sys = sys.get();
             }
+            if (fields & IK_FIELD_ELASTIC) // ParticleSystem::setDisplacement (ParticleSystem.cc:60-67)
+                check(ik_upload_displacement(ctx, 0, sys->N, sys->disp.data()));
             check(ik_compute(ctx, precision, fields));
             for (auto& kv : obs)
                 check(ik_get_field(ctx, 0, kv.second->field, kv.second->val.data(), (int64_t)kv.second->val.size()));
@@ -627,5 +629,7 @@ PYBIND11_MODULE(_core, m)
     FIELD(3, IK_FIELD_VIRIAL, "VirialStressField3D");
     FIELD(2, IK_FIELD_KINETIC, "KineticStressField2D");
     FIELD(3, IK_FIELD_KINETIC, "KineticStressField3D");
+    FIELD(2, IK_FIELD_ELASTIC, "ElasticVirialStressField2D");
+    FIELD(3, IK_FIELD_ELASTIC, "ElasticVirialStressField3D");
 #undef FIELD
 }

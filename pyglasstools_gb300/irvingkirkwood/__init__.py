@@ -20,10 +20,14 @@ def initialize_field(names, dim, gridpoints):
     n = len(gridpoints)
     if any("virialstress" in s for s in names):
         if any("elastic" in s for s in names):
-            raise NotImplementedError("elasticvirialstress is not on the GPU path")
-        cls = _irvingkirkwood.VirialStressField2D if dim == 2 else _irvingkirkwood.VirialStressField3D
-        list_obs['virialstress'] = cls("virialstress", "2-TENSOR", False, n)
-        list_obs['virialstress'].addGridpoints(gridpoints)
+            cls = (_irvingkirkwood.ElasticVirialStressField2D if dim == 2
+                   else _irvingkirkwood.ElasticVirialStressField3D)
+            list_obs['elasticvirialstress'] = cls("elasticvirialstress", "2-TENSOR", False, n)
+            list_obs['elasticvirialstress'].addGridpoints(gridpoints)
+        if all("elastic" in s for s in names) is False:
+            cls = _irvingkirkwood.VirialStressField2D if dim == 2 else _irvingkirkwood.VirialStressField3D
+            list_obs['virialstress'] = cls("virialstress", "2-TENSOR", False, n)
+            list_obs['virialstress'].addGridpoints(gridpoints)
     if any("kineticstress" in s for s in names):
         cls = _irvingkirkwood.KineticStressField2D if dim == 2 else _irvingkirkwood.KineticStressField3D
         list_obs['kineticstress'] = cls("kineticstress", "2-TENSOR", True, n)

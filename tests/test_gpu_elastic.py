@@ -82,3 +82,30 @@ def test_zero_displacement_gives_zero_field_and_errors(ik):
         c.set_frame(f.pos, f.diam)
         with pytest.raises(ik.IKError):
             c.upload_displacement(np.zeros((5, 3)))                          # wrong size
+
+
+def test_elastic_field_through_the_pybind_classes(ik, oracle):
+    """ElasticVirialStressField2D with ParticleSystem.setDisplacement and
+    IrvingKirkwood.compute (the reference's module-irvingkirkwood.cpp classes)."""
+    from pyglasstools_gb300 import synth
+    from pyglasstools_gb300._core import _irvingkirkwood as K, _pyglasstools as P, _potential as Pot, _cgfunc as CG
+    f = synth.make_frame(900, dim=2, seed=83)
+    grid = synth.lattice_grid(f.L, 12, 2)
+    u = _disp(f, 2, 0.03, 9)
+    box = P.SimBox(np.array([f.L, f.L, 1.0]), np.zeros(3), 2)
+    sys = P.ParticleSystem(box, len(f.pos), f.diam, f.mass, f.pos, f.vel)
+    sys.setDisplacement(u)
+    rc = 1.25
+    pot = Pot.PairPotentialPoly12(rc, [1.0, 0.2, -28.0 / rc ** 12, 48.0 / rc ** 14, -21.0 / rc ** 16])
+    cg = CG.CGFuncOcticFixedPoint(5, 2.0)
+    calc = K.IrvingKirkwood(sys, pot, cg, P.Communicator())
+    calc.setPrecision("fp64")
+    fld = K.ElasticVirialStressField2D("elasticvirialstress", "2-TENSOR", False, len(grid))
+    fld.addGridpoints(grid)
+    calc.addObservable(fld)
+    calc.compute(grid)
+    got = fld.values()
+    obox = oracle.make_box(2, [f.L, f.L, 1.0])
+    _, want = oracle.compute_elastic(obox, f.pos, u, f.diam, oracle.make_poly12(), oracle.make_cg("octic", rcut=2.0),
+                                     grid, max_rc=calc.max_rcut)
+    assert np.all(rel_l2(uniq(got), uniq(want)) <= 1e-12)
