@@ -615,11 +615,13 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi)
 constexpr int TC_A0 = 0;                    // 128 x 16 bf16 input operand   4096
 constexpr int TC_H = TC_A0 + 128 * 16 * 2;  // 128 x 128 bf16 hidden operand [hi | lo]  32768
 constexpr int TC_W = TC_H + 128 * 128 * 2;  // deployed blob (W1, W2, W3, floats)
-constexpr int TC_BAR = TC_W + ((DB_BYTES + 1023) / 1024) * 1024;
+constexpr int TC_BAR = TC_W + DB_BYTES;  // DB_BYTES is a multiple of 16
 constexpr int TC_SMEM = TC_BAR + 64;
-// At least this much dynamic shared memory per CTA keeps at most 4 CTAs on an SM, so
-// that their TMEM allocations (64 columns each) never wait on one another.
-constexpr int TC_SMEM_LAUNCH = 60 * 1024;
+// 56.4 KB of dynamic shared memory per CTA: at most 4 CTAs on an SM (228 KB), so their
+// TMEM allocations (64 columns each, 256 of 512) never wait on one another.
+constexpr int TC_SMEM_LAUNCH = TC_SMEM;
+static_assert(4 * (TC_SMEM_LAUNCH + 1024) <= 233472 && 5 * (TC_SMEM_LAUNCH + 1024) > 233472,
+              "four CTAs per SM");
 constexpr uint32_t TC_COLS = 64;
 
 // Records of bonds that cross the support, written by the FP32 gather in surrogate
