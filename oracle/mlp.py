@@ -150,7 +150,7 @@ def forward_bf16(p, feats):
     (x_hi W_hi + x_lo W_hi + x_hi W_lo); activations as BF16 hi + lo pairs; FP64
     accumulation; tanh-form SiLU."""
     W1, b1, W2, b2, W3, b3, w4, b4 = split(p)
-    silu = lambda z: z * (0.5 + 0.5 * np.tanh(0.5 * z))
+    silu = lambda z: 0.5 * z + 0.5 * z * np.tanh(0.5 * z)
     x = inputs(feats)
     xh, W1h = bf16(x), bf16(W1)
     xl, W1l = bf16(x - xh), bf16(W1 - W1h)

@@ -450,23 +450,25 @@ __host__ __device__ inline int op_off(int r, int k, int K)
 __global__ void k_mlp_deploy(const float* P, unsigned char* blob)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    // hidden layers prescaled by 1/2 (exact), so that the accumulators hold h = z/2 and
+    // SiLU(z) = h + h tanh(h)
     if (i < 64 * 16) { // W1 as [hi | hi | lo | 0] against inputs [x_hi | x_lo | x_hi | 0]
         const int n = i / 16, k = i % 16, j = k & 3;
-        const float w = P[O_W1 + n * 4 + j];
+        const float w = 0.5f * P[O_W1 + n * 4 + j];
         const float hi = bf16r(w);
         const float v = k < 8 ? hi : (k < 12 ? w - hi : 0.f);
         *reinterpret_cast<__nv_bfloat16*>(blob + DB_W1 + op_off(n, k, 16)) = __float2bfloat16_rn(v);
     }
     if (i < 64 * 64) {
         const int n = i / 64, k = i % 64;
-        *reinterpret_cast<__nv_bfloat16*>(blob + DB_W2 + op_off(n, k, 64)) = __float2bfloat16_rn(P[O_W2 + i]);
-        *reinterpret_cast<__nv_bfloat16*>(blob + DB_W3 + op_off(n, k, 64)) = __float2bfloat16_rn(P[O_W3 + i]);
+        *reinterpret_cast<__nv_bfloat16*>(blob + DB_W2 + op_off(n, k, 64)) = __float2bfloat16_rn(0.5f * P[O_W2 + i]);
+        *reinterpret_cast<__nv_bfloat16*>(blob + DB_W3 + op_off(n, k, 64)) = __float2bfloat16_rn(0.5f * P[O_W3 + i]);
     }
     float* F = reinterpret_cast<float*>(blob + DB_F);
     if (i < 64) {
-        F[i] = P[O_B1 + i];
-        F[64 + i] = P[O_B2 + i];
-        F[128 + i] = P[O_B3 + i];
+        F[i] = 0.5f * P[O_B1 + i];
+        F[64 + i] = 0.5f * P[O_B2 + i];
+        F[128 + i] = 0.5f * P[O_B3 + i];
         F[192 + i] = bf16r(P[O_W4 + i]);
     }
     if (i == 0) F[256] = P[O_B4];
@@ -483,7 +485,11 @@ __global__ void k_mlp_infer_simt(const float* P, const float4* feats, long long 
     if (i >= n) return;
     const bool q = mode == 1;
     auto R = [&](float v) { return q ? bf16r(v) : v; };
-    auto S = [&](float z) { return q ? silu_fast(z) : silu_exact(z); };
+    auto S = [&](float z) { // deployed form: h = z/2 from prescaled weights, h + h tanh(h)
+        if (!q) return silu_exact(z);
+        const float h = 0.5f * z;
+        return fmaf(h, tanh_approx(h), h);
+    };
     const float4 f = feats[i];
     float x[4];
     mlp_inputs(f.x, f.y, f.z, f.w, x);
@@ -723,6 +729,17 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
                 bfix = r.w;
             }
         }
+        // midpoint-rule baseline of the clipped segment (as mlp_base, exp via ex2.approx)
+        float base;
+        {
+            const float tc = sqrtf(fmaxf(9.0f - fd * fd, 0.0f));
+            const float l = fb - fa;
+            const float s1 = l > 0.0f ? fminf(fmaxf((tc - fa) / l, 0.0f), 1.0f) : 0.0f;
+            const float mm = 0.5f * (fa + tc);
+            float ex;
+            asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(ex) : "f"(-0.72134752044448170f * (fd * fd + mm * mm)));
+            base = s1 * ex;
+        }
         {
             // inputs as [x_hi | x_lo | x_hi | 0] against W1 as [hi | hi | lo | 0]
             float x[4], xl[4];
@@ -768,24 +785,24 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
                 for (int c16 = 0; c16 < 4; ++c16) {
                     float v[16];
                     tmem_ld16(tl + 16 * c16, v);
-                    float vl[16];
+                    // h = z/2 (prescaled weights), SiLU = h + h tanh(h); BF16 hi word by a
+                    // packed convert, lo = a - hi
+                    uint32_t ph[8], pl[8];
 #pragma unroll
-                    for (int k = 0; k < 16; ++k) {
-                        const float a = silu_fast(v[k] + bias[16 * c16 + k]);
-                        v[k] = bf16r(a);
-                        vl[k] = a - v[k];
+                    for (int k = 0; k < 16; k += 2) {
+                        const float h0 = v[k] + bias[16 * c16 + k], h1 = v[k + 1] + bias[16 * c16 + k + 1];
+                        const float a0 = fmaf(h0, tanh_approx(h0), h0), a1 = fmaf(h1, tanh_approx(h1), h1);
+                        const uint32_t hp = pack_bf16x2(a0, a1);
+                        ph[k / 2] = hp;
+                        pl[k / 2] = pack_bf16x2(a0 - __uint_as_float(hp << 16), a1 - __uint_as_float(hp & 0xffff0000u));
                     }
 #pragma unroll
                     for (int h8 = 0; h8 < 2; ++h8) {
                         const int k0 = 16 * c16 + 8 * h8;
-                        const float* u = v + 8 * h8;
-                        const float* ul = vl + 8 * h8;
-                        const uint4 ph = make_uint4(pack_bf16x2(u[0], u[1]), pack_bf16x2(u[2], u[3]),
-                                                    pack_bf16x2(u[4], u[5]), pack_bf16x2(u[6], u[7]));
-                        const uint4 pl = make_uint4(pack_bf16x2(ul[0], ul[1]), pack_bf16x2(ul[2], ul[3]),
-                                                    pack_bf16x2(ul[4], ul[5]), pack_bf16x2(ul[6], ul[7]));
-                        *reinterpret_cast<uint4*>(sH + op_off(t, k0, 128)) = ph;
-                        *reinterpret_cast<uint4*>(sH + op_off(t, 64 + k0, 128)) = pl;
+                        *reinterpret_cast<uint4*>(sH + op_off(t, k0, 128)) =
+                            make_uint4(ph[4 * h8], ph[4 * h8 + 1], ph[4 * h8 + 2], ph[4 * h8 + 3]);
+                        *reinterpret_cast<uint4*>(sH + op_off(t, 64 + k0, 128)) =
+                            make_uint4(pl[4 * h8], pl[4 * h8 + 1], pl[4 * h8 + 2], pl[4 * h8 + 3]);
                     }
                 }
                 fence_async_smem();
@@ -800,10 +817,13 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
                     float v[16];
                     tmem_ld16(tl + 16 * c16, v);
 #pragma unroll
-                    for (int k = 0; k < 16; ++k) y = fmaf(F[192 + 16 * c16 + k], silu_fast(v[k] + bias[16 * c16 + k]), y);
+                    for (int k = 0; k < 16; ++k) {
+                        const float h = v[k] + bias[16 * c16 + k];
+                        y = fmaf(F[192 + 16 * c16 + k], fmaf(h, tanh_approx(h), h), y);
+                    }
                 }
                 fence_before();
-                const float Bs = mlp_base(fd, fa, fb) * (1.0f + y);
+                const float Bs = base * (1.0f + y);
                 if (MODE == 0) {
                     if (valid) out[row] = Bs;
                 } else if (valid) {
@@ -812,21 +832,20 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
                     const float Bv = use ? 2.0f * Bs : bfix;
                     const float4 bd = __ldg(R.bonds + bond);
                     const float fx = bd.w * bd.x, fy = bd.w * bd.y;
-                    float cf[6];
-                    cf[0] = fx * bd.x;
-                    cf[1] = fy * bd.y;
+                    auto add = [&](int c, float coef) {
+                        const long long v = __float2ll_rn(Bv * coef * 4294967296.0f);
+                        atomicAdd(R.corr + (size_t)g * R.nc + c, (unsigned long long)v);
+                    };
+                    add(0, fx * bd.x);
+                    add(1, fy * bd.y);
                     if (R.nc == 3) {
-                        cf[2] = fx * bd.y;
+                        add(2, fx * bd.y);
                     } else {
                         const float fz = bd.w * bd.z;
-                        cf[2] = fz * bd.z;
-                        cf[3] = fx * bd.y;
-                        cf[4] = fx * bd.z;
-                        cf[5] = fy * bd.z;
-                    }
-                    for (int c = 0; c < R.nc; ++c) {
-                        const long long v = __float2ll_rn(Bv * cf[c] * 4294967296.0f);
-                        atomicAdd(R.corr + (size_t)g * R.nc + c, (unsigned long long)v);
+                        add(2, fz * bd.z);
+                        add(3, fx * bd.y);
+                        add(4, fx * bd.z);
+                        add(5, fy * bd.z);
                     }
                 }
             }
