@@ -96,6 +96,13 @@ int ik_reserve_slots(ik_ctx* ctx, int nslots);
  * slot's computations use them instead of the context's ik_set_box / ik_set_grid,
  * and its fields have g grid points.  Same meaning as SimBox::SimBox (SimBox.cc:25-45)
  * and the ikcalculator grid (irvingkirkwood/__init__.py:44-51), per frame. */
+/* The same upload from FP32 host arrays, as GSD files store them (particles/position,
+ * velocity, mass, diameter: float32): one staging copy of half the bytes, widened to
+ * FP64 on the GPU (exactly).  Replaces the list conversion of data_gsd.update
+ * (utils.py:85-101) feeding ParticleSystem. */
+int ik_upload_frame_f32(ik_ctx* ctx, int slot, int64_t n, const float* pos, const float* vel, const float* mass,
+                        const float* diam);
+
 /* Per-particle displacements u (n x 3, the slot's particle order) for the elastic
  * virial field IK_FIELD_ELASTIC: per neighbour pair within max_rcut,
  * 0.5 * bond * (f(|r+u_ij|) (r+u_ij)(x)(r+u_ij) - f(|r|) r(x)r), u_ij = u_j - u_i.

@@ -95,6 +95,7 @@ struct Slot {
     double dmax = 0.0;
     DevBuf pos, vel, mass, diam;
     DevBuf disp; // displacements for the elastic virial field (ik_upload_displacement)
+    DevBuf stage32; // FP32 upload staging (ik_upload_frame_f32)
     bool has_disp = false;
     DevBuf vir, kin, ela;
     int last_prec = -1, last_fields = 0;
@@ -1026,8 +1027,9 @@ int ik_reserve_slots(ik_ctx* c, int nslots)
     return IK_OK;
 }
 
-int ik_upload_frame(ik_ctx* c, int slot, int64_t n, const double* pos, const double* vel, const double* mass,
-                    const double* diam)
+// Frame upload from FP64 or FP32 host arrays (FP32: one staging copy, widened on the GPU).
+static int upload_impl(ik_ctx* c, int slot, int64_t n, const void* pos, const void* vel, const void* mass,
+                       const void* diam, bool f32)
 {
     if (int r = check_ctx(c)) return r;
     if (int r = slot_ok(c, slot)) return r;
@@ -1037,26 +1039,35 @@ int ik_upload_frame(ik_ctx* c, int slot, int64_t n, const double* pos, const dou
         return fail(IK_ERR_STATE, "box not set (ik_set_box or ik_set_slot_geometry)");
     double dmax = 0.0;
     if (!c->max_rcut_set) // Calculator.h:41-45 freezes max_rcut from the first frame
-        for (int64_t i = 0; i < n; ++i) dmax = std::max(dmax, diam[i]);
+        for (int64_t i = 0; i < n; ++i)
+            dmax = std::max(dmax, f32 ? (double)((const float*)diam)[i] : ((const double*)diam)[i]);
     Slot& s = c->slots[(size_t)slot];
     if (s.done_recorded) CK(cudaStreamWaitEvent(c->stream, s.done, 0)); // inputs still in use
     const void* old_ptrs[4] = {s.pos.p, s.diam.p, s.vel.p, s.mass.p};
     const bool old_vel = s.has_vel, old_mass = s.has_mass;
     ENS(s.pos, sizeof(double) * 3 * std::max<int64_t>(n, 1));
     ENS(s.diam, sizeof(double) * std::max<int64_t>(n, 1));
-    if (n > 0) {
-        CK(cudaMemcpyAsync(s.pos.p, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c->stream));
-        CK(cudaMemcpyAsync(s.diam.p, diam, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
-    }
     s.has_vel = vel != nullptr;
     s.has_mass = mass != nullptr;
-    if (vel) {
-        ENS(s.vel, sizeof(double) * 3 * std::max<int64_t>(n, 1));
-        if (n > 0) CK(cudaMemcpyAsync(s.vel.p, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c->stream));
-    }
-    if (mass) {
-        ENS(s.mass, sizeof(double) * std::max<int64_t>(n, 1));
-        if (n > 0) CK(cudaMemcpyAsync(s.mass.p, mass, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    if (vel) ENS(s.vel, sizeof(double) * 3 * std::max<int64_t>(n, 1));
+    if (mass) ENS(s.mass, sizeof(double) * std::max<int64_t>(n, 1));
+    if (n > 0 && !f32) {
+        CK(cudaMemcpyAsync(s.pos.p, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(s.diam.p, diam, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+        if (vel) CK(cudaMemcpyAsync(s.vel.p, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c->stream));
+        if (mass) CK(cudaMemcpyAsync(s.mass.p, mass, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    } else if (n > 0) { // staging layout: pos 3n | vel 3n | mass n | diam n floats
+        ENS(s.stage32, sizeof(float) * 8 * n);
+        float* st = s.stage32.as<float>();
+        CK(cudaMemcpyAsync(st, pos, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, c->stream));
+        if (vel) CK(cudaMemcpyAsync(st + 3 * n, vel, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, c->stream));
+        if (mass) CK(cudaMemcpyAsync(st + 6 * n, mass, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(st + 7 * n, diam, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
+        k_widen_frame<<<(int)((n + 255) / 256), 256, 0, c->stream>>>(st, (int)n, s.pos.as<double>(),
+                                                                     vel ? s.vel.as<double>() : nullptr,
+                                                                     mass ? s.mass.as<double>() : nullptr,
+                                                                     s.diam.as<double>());
+        CK(cudaGetLastError());
     }
     if (n > 0) { // device-side validation; reported by ik_synchronize
         k_validate<<<(int)((n + 255) / 256), 256, 0, c->stream>>>(s.pos.as<double>(), s.diam.as<double>(), (int)n,
@@ -1074,6 +1085,18 @@ int ik_upload_frame(ik_ctx* c, int slot, int64_t n, const double* pos, const dou
         ik_set_max_rcut(c, m > dmax ? m : dmax); // Calculator.h:41-45
     }
     return IK_OK;
+}
+
+int ik_upload_frame(ik_ctx* c, int slot, int64_t n, const double* pos, const double* vel, const double* mass,
+                    const double* diam)
+{
+    return upload_impl(c, slot, n, pos, vel, mass, diam, false);
+}
+
+int ik_upload_frame_f32(ik_ctx* c, int slot, int64_t n, const float* pos, const float* vel, const float* mass,
+                        const float* diam)
+{
+    return upload_impl(c, slot, n, pos, vel, mass, diam, true);
 }
 
 int ik_upload_displacement(ik_ctx* c, int slot, int64_t n, const double* disp)

@@ -24,6 +24,21 @@ __global__ void k_bin(const double* __restrict__ pos, int n, IkGeom g, int* __re
     rank[i] = atomicAdd(&cell_count[c], 1);
 }
 
+// 1b. FP32 frame staging (pos 3n | vel 3n | mass n | diam n) widened to the slot's FP64
+//     arrays (exact: every float is a double); vel/mass may be null (not uploaded).
+__global__ void k_widen_frame(const float* __restrict__ st, int n, double* __restrict__ pos,
+                              double* __restrict__ vel, double* __restrict__ mass, double* __restrict__ diam)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int k = 0; k < 3; ++k) {
+        pos[3 * i + k] = (double)st[3 * i + k];
+        if (vel) vel[3 * i + k] = (double)st[3 * (size_t)n + 3 * i + k];
+    }
+    if (mass) mass[i] = (double)st[6 * (size_t)n + i];
+    diam[i] = (double)st[7 * (size_t)n + i];
+}
+
 // 2. exclusive scan of n ints into out[0..n] (single CTA of 1024 threads; tiles of
 //    4096 with a running carry).  Used for cell starts and neighbour offsets.
 __global__ void __launch_bounds__(1024) k_scan(const int* __restrict__ in, int n, int* __restrict__ out)

@@ -7,6 +7,7 @@
 __global__ void k_bin(const double* pos, int n, IkGeom g, int* cell_of, int* rank, int* cell_count,
                       int* status);
 __global__ void k_scan(const int* in, int n, int* out);
+__global__ void k_widen_frame(const float* st, int n, double* pos, double* vel, double* mass, double* diam);
 __global__ void k_scatter(const int* cell_of, const int* rank, const int* cell_start, int n, int* sorted);
 __global__ void k_cell_sort_pack(IkGeom g, const int* cell_start, int* sorted, const double* pos,
                                  const double* vel, const double* mass, const double* diam,

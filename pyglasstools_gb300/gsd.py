@@ -159,3 +159,15 @@ class HOOMDTrajectory:
 
 def open_trajectory(path: str) -> HOOMDTrajectory:
     return HOOMDTrajectory(path)
+
+
+def upload_frames(ctx, traj, frames, slots=None):
+    """Stream GSD frames into resident slots of an engine context (ikabi.IKContext):
+    the float32 chunks go to the GPU as stored (half the bytes of FP64) and are
+    widened there, with no per-particle Python conversion -- the work the reference's
+    data_gsd.update (utils.py:85-101) does with Python lists on every frame."""
+    slots = list(range(len(frames))) if slots is None else list(slots)
+    for f, s in zip(frames, slots):
+        fr = traj[f]
+        ctx.upload_frame_f32(s, fr.position, fr.diameter, fr.velocity, fr.mass)
+    return slots

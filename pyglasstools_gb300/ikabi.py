@@ -56,6 +56,7 @@ def lib():
             "ik_reserve_slots": ([vp, i32], i32),
             "ik_set_slot_geometry": ([vp, i32, i32, dp, dp, i64, dp], i32),
             "ik_upload_displacement": ([vp, i32, i64, dp], i32),
+            "ik_upload_frame_f32": ([vp, i32, i64, fp, fp, fp, fp], i32),
             "ik_upload_frame": ([vp, i32, i64, dp, dp, dp, dp], i32),
             "ik_set_frame": ([vp, i64, dp, dp, dp, dp], i32),
             "ik_compute_slot": ([vp, i32, i32, i32], i32),
@@ -182,6 +183,14 @@ class IKContext:
     # frames ----------------------------------------------------------------
     def reserve_slots(self, n):
         check(lib().ik_reserve_slots(self._h, n))
+
+    def upload_frame_f32(self, slot, pos, diam, vel=None, mass=None):
+        """Upload float32 arrays (e.g. GSD chunks) into a slot; widened to FP64 on the GPU."""
+        f = lambda a, shape=None: None if a is None else np.ascontiguousarray(a, dtype=np.float32).reshape(
+            shape if shape else -1)
+        p, d, v, m = f(pos, (-1, 3)), f(diam), f(vel, (-1, 3)), f(mass)
+        self._keep = (p, d, v, m)  # the copies may be asynchronous (pinned memory)
+        check(lib().ik_upload_frame_f32(self._h, slot, len(p), _fp(p), _fp(v), _fp(m), _fp(d)))
 
     def upload_displacement(self, disp, slot=0):
         """Per-particle displacements (n x 3) for the elastic virial field."""

@@ -198,3 +198,21 @@ def test_uneven_batch_with_per_slot_geometry():
             np.testing.assert_array_equal(got[k][1], want[1])
             np.testing.assert_array_equal(got2[k][0], want[0])
     c.close()
+
+
+def test_float32_upload_equals_float64_upload():
+    """ik_upload_frame_f32 (GSD float32 chunks widened on the GPU) gives the same device
+    data -- and bit-identical fields -- as uploading the same values in FP64."""
+    from pyglasstools_gb300 import ikabi as ik, synth
+    f = synth.make_frame(3000, dim=2, seed=901)
+    p32, d32 = f.pos.astype(np.float32), f.diam.astype(np.float32)
+    v32, m32 = f.vel.astype(np.float32), f.mass.astype(np.float32)
+    grid = synth.lattice_grid(f.L, 40, 2)
+    c = _context(ik, f.L, grid, 2)
+    c.upload_frame(0, p32.astype(np.float64), d32.astype(np.float64), v32.astype(np.float64), m32.astype(np.float64))
+    c.upload_frame_f32(1, p32, d32, v32, m32)
+    for prec in ("fp32", "fp64"):
+        a, b = _per_slot(ik, c, [0, 1], prec)
+        np.testing.assert_array_equal(a[0], b[0])
+        np.testing.assert_array_equal(a[1], b[1])
+    c.close()
