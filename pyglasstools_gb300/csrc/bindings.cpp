@@ -6,6 +6,8 @@
 // potential/PairPotential.h:125-152, irvingkirkwood/cgfunc/CoarseGrainFunction.h:136-167,
 // irvingkirkwood/IrvingKirkwood.h:113-122, irvingkirkwood/CoarseGrainedField.h:342-358.
 #include <pybind11/numpy.h>
+#include <charconv>
+#include <cstdio>
 #include <pybind11/pybind11.h>
 #include <pybind11/stl.h>
 
@@ -353,6 +355,50 @@ struct CGGaussianFixed : CoarseGrainFunction {
     }
 };
 
+// ---------------------------------------------------------------- text output
+// Python's repr() of a float (the "{} ".format(x) of fieldlogger.save_perrank,
+// io.py:112-128): the shortest digits that round-trip, fixed notation for decimal
+// exponents in [-4, 16) with ".0" on integral values, else d.ddde+XX.
+static void py_float_repr(double v, std::string& out)
+{
+    if (std::isnan(v)) { out += "nan"; return; }
+    if (std::isinf(v)) { out += v > 0 ? "inf" : "-inf"; return; }
+    if (v == 0.0) { out += std::signbit(v) ? "-0.0" : "0.0"; return; }
+    char buf[64];
+    auto res = std::to_chars(buf, buf + sizeof buf, v, std::chars_format::scientific);
+    std::string sci(buf, res.ptr);          // [-]d[.ddd]e[+-]XX
+    const bool neg = sci[0] == '-';
+    if (neg) sci.erase(0, 1);
+    const size_t epos = sci.find('e');
+    const int e10 = std::atoi(sci.c_str() + epos + 1);
+    std::string digits;
+    for (size_t k = 0; k < epos; ++k) if (sci[k] != '.') digits += sci[k];
+    while (digits.size() > 1 && digits.back() == '0') digits.pop_back();
+    if (neg) out += '-';
+    if (e10 >= -4 && e10 < 16) {
+        const int point = e10 + 1; // digits before the decimal point
+        if (point <= 0) {
+            out += "0.";
+            out.append((size_t)(-point), '0');
+            out += digits;
+        } else if ((size_t)point >= digits.size()) {
+            out += digits;
+            out.append((size_t)point - digits.size(), '0');
+            out += ".0";
+        } else {
+            out += digits.substr(0, (size_t)point);
+            out += '.';
+            out += digits.substr((size_t)point);
+        }
+    } else {
+        out += digits[0];
+        if (digits.size() > 1) { out += '.'; out += digits.substr(1); }
+        char eb[16];
+        std::snprintf(eb, sizeof eb, "e%c%02d", e10 < 0 ? '-' : '+', e10 < 0 ? -e10 : e10);
+        out += eb;
+    }
+}
+
 // ---------------------------------------------------------------- _irvingkirkwood
 struct CoarseGrainedField {
     std::string name, type;
@@ -622,6 +668,48 @@ PYBIND11_MODULE(_core, m)
         .def_readonly("type", &CoarseGrainedField::type)
         .def_readonly("islocal", &CoarseGrainedField::islocal)
         .def_readonly("dim", &CoarseGrainedField::dim);
+    // Lines of one frame of fieldlogger.save_perrank / save_perrank_polar (io.py:112-144):
+    // per grid point "1 " + the leading columns (repr) + each requested component of
+    // each field (gettostring: default ostream, 6 significant digits) + "\n".
+    im.def("format_field_lines",
+           [](py::array_t<double, py::array::c_style | py::array::forcecast> cols,
+              const std::vector<std::pair<std::shared_ptr<CoarseGrainedField>, int>>& comps,
+              const std::vector<int>& int_cols) {
+               auto c = cols.unchecked<2>();
+               const py::ssize_t G = c.shape(0), K = c.shape(1);
+               for (auto& fc : comps) {
+                   const size_t DD = (size_t)fc.first->dim * fc.first->dim;
+                   if (fc.second < 0 || (size_t)fc.second >= DD || fc.first->val.size() < (size_t)G * DD)
+                       throw std::out_of_range("[ERROR]: grid/component index out of range");
+               }
+               std::string out;
+               out.reserve((size_t)G * (16 * (size_t)K + 14 * comps.size() + 4));
+               char vb[64];
+               {
+                   py::gil_scoped_release nogil;
+                   for (py::ssize_t g = 0; g < G; ++g) {
+                       out += "1 ";
+                       for (py::ssize_t k = 0; k < K; ++k) {
+                           if (std::find(int_cols.begin(), int_cols.end(), (int)k) != int_cols.end()) {
+                               std::snprintf(vb, sizeof vb, "%lld", (long long)c(g, k));
+                               out += vb;
+                           } else {
+                               py_float_repr(c(g, k), out);
+                           }
+                           out += ' ';
+                       }
+                       for (auto& fc : comps) {
+                           const size_t DD = (size_t)fc.first->dim * fc.first->dim;
+                           std::snprintf(vb, sizeof vb, "%g ", fc.first->val[(size_t)g * DD + (size_t)fc.second]);
+                           out += vb;
+                       }
+                       out += '\n';
+                   }
+               }
+               return out;
+           },
+           py::arg("cols"), py::arg("comps"), py::arg("int_cols") = std::vector<int>{});
+    im.def("float_repr", [](double v) { std::string o; py_float_repr(v, o); return o; });
 #define FIELD(D, F, NAME)                                                                    \
     py::class_<FieldT<D, F>, CoarseGrainedField, std::shared_ptr<FieldT<D, F>>>(im, NAME) \
         .def(py::init<std::string, std::string, bool, int>())

@@ -71,3 +71,65 @@ class ikcalculator(object):
     def update(self, frame_num):
         pyglasstools_gb300.update_sysdata(frame_num)
         self.calculator.setSystemData(pyglasstools_gb300.get_sysdata().cppparticledata)
+
+
+def polar_gridpoints(center=(0.0, 0.0, 0.0), spacingtype="normal", rmax=10, rmin=0, dr=0.1, dlnr=0.05):
+    """The radialcalculator grid (irvingkirkwood/__init__.py:83-127): the centre, then
+    rings of radius r (linspace(0, rmax, int(rmax/dr))[1:], or log-spaced) with
+    int(2 pi r / dr) points at theta = linspace(0, 2 pi, .) each.  Returns
+    (gridpoints, gridid, r, theta)."""
+    center = np.asarray(center, dtype=np.float64)
+    if spacingtype == "normal":
+        r = np.linspace(0, rmax, int(rmax / dr))[1:]
+    elif spacingtype == "log":
+        r = np.exp(np.linspace(np.log(rmin), np.log(rmax), int((np.log(rmax) - np.log(rmin)) / dlnr)))
+    else:
+        raise ValueError("spacingtype must be 'normal' or 'log'")
+    gridid, globalr, globaltheta, points = [0.0], [0.0], [0.0], [center]
+    for i in range(len(r)):
+        dtheta = dr / r[i]
+        theta = np.linspace(0, 2 * np.pi, int(2 * np.pi / dtheta))
+        x = r[i] * np.cos(theta)
+        y = r[i] * np.sin(theta)
+        gridid.extend([i + 1.0] * len(theta))
+        globalr.extend([r[i]] * len(theta))
+        globaltheta.extend(theta.tolist())
+        points.extend(np.stack([x, y, np.zeros(len(theta))], axis=1) + center)
+    return (np.asarray(points, dtype=np.float64).reshape(-1, 3), np.asarray(gridid), np.asarray(globalr),
+            np.asarray(globaltheta))
+
+
+class radialcalculator(object):
+    """Fields on a polar grid around ``center`` (irvingkirkwood/__init__.py:80-166); the
+    same IrvingKirkwood computation as ikcalculator, on these grid points."""
+
+    def __init__(self, cgfunc, center=np.array([0, 0, 0]), spacingtype="normal", rmax=10, rmin=0, dr=0.1,
+                 dlnr=0.05, precision="fp32"):
+        self.cgfunc = cgfunc
+        self.manager = _core._pyglasstools.Manager()
+        self.coordmode = "polar"
+        self.center = np.asarray(center, dtype=np.float64)
+        self.gridpoints, self.gridid, self.globalr, self.globaltheta = polar_gridpoints(
+            self.center, spacingtype, rmax, rmin, dr, dlnr)
+        self.gridsize = len(self.gridpoints)
+        sysdata = pyglasstools_gb300.get_sysdata()
+        self.calculator = _irvingkirkwood.IrvingKirkwood(
+            sysdata.cppparticledata, pyglasstools_gb300.get_potential().cpppairpotential,
+            cgfunc._getCGFunc(), comm)
+        self.calculator.setPrecision(precision)
+        solvers_list.append(self)
+
+    def set_center(self, center):
+        self.center = center
+        self.gridpoints[0:] += center
+
+    def add_observables(self, observables):
+        for name in observables:
+            self.calculator.addObservable(observables[name])
+
+    def run(self):
+        self.calculator.compute(self.gridpoints)
+
+    def update(self, frame_num):
+        pyglasstools_gb300.update_sysdata(frame_num)
+        self.calculator.setSystemData(pyglasstools_gb300.get_sysdata().cppparticledata)

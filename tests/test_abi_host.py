@@ -197,3 +197,54 @@ def test_synthetic_generator_recipe():
     assert abs(np.mean(f.vel[:, :2] ** 2) - 0.3) < 0.03
     g = synth.make_frame(2000, dim=2, seed=0)
     assert np.array_equal(f.pos, g.pos)  # seeded, platform independent
+
+
+def test_native_float_repr_matches_python_repr():
+    """The bulk .xyz writer prints grid coordinates exactly like "{} ".format(x)."""
+    from pyglasstools_gb300 import _core
+    K = _core._irvingkirkwood
+    rng = np.random.default_rng(0)
+    vals = np.concatenate([rng.normal(0, 1, 3000) * 10.0 ** rng.integers(-14, 22, 3000),
+                           [0.0, -0.0, 1.0, 2.0, 1e16, 1e15, 9999999999999998.0, 1e-4, 1e-5, 0.30000000000000004,
+                            -2.5e-7, 100.0, 1234567.0, float("inf"), float("-inf")]])
+    for v in vals:
+        assert K.float_repr(float(v)) == repr(float(v)), v
+
+
+def test_bulk_field_lines_match_per_point_formatting():
+    """format_field_lines gives the text of the per-point gettostring loop
+    (io.py:112-128 cartesian, :130-144 polar), here on zero-valued fields."""
+    from pyglasstools_gb300 import _core
+    K = _core._irvingkirkwood
+    g = np.array([[-1.5, 0.25, 0.0], [3.0, 1e-7, 0.0], [2.0 / 3.0, -12.0, 0.0]])
+    vir = K.VirialStressField2D("virialstress", "2-TENSOR", False, len(g))
+    kin = K.KineticStressField2D("kineticstress", "2-TENSOR", True, len(g))
+    comps = [(vir, 0), (vir, 3), (kin, 2)]
+    want = "".join("1 {} {} ".format(p[0], p[1]) + vir.gettostring(0, i) + vir.gettostring(3, i)
+                   + kin.gettostring(2, i) + "\n" for i, p in enumerate(g))
+    assert K.format_field_lines(g[:, :2], comps) == want
+    polar = np.array([[0, 0.0, 0.0], [1, 0.1, 0.5], [2, 0.2, 6.283185307179586]])
+    want_p = "".join("1 {} {} {} ".format(int(p[0]), p[1], p[2]) + vir.gettostring(0, i) + "\n"
+                     for i, p in enumerate(polar))
+    assert K.format_field_lines(polar, [(vir, 0)], [0]) == want_p
+
+
+def test_polar_grid_matches_reference_recipe():
+    """radialcalculator's grid (irvingkirkwood/__init__.py:83-127): origin first, then
+    rings with int(2 pi r / dr) points each."""
+    from pyglasstools_gb300.irvingkirkwood import polar_gridpoints
+    c = np.array([1.0, -2.0, 0.0])
+    pts, gid, r, th = polar_gridpoints(c, "normal", rmax=2.0, dr=0.25)
+    rr = np.linspace(0, 2.0, int(2.0 / 0.25))[1:]
+    assert np.array_equal(pts[0], c) and gid[0] == 0 and r[0] == 0 and th[0] == 0
+    counts = [int(2 * np.pi / (0.25 / x)) for x in rr]
+    assert len(pts) == 1 + sum(counts)
+    k = 1
+    for i, (x, n) in enumerate(zip(rr, counts)):
+        theta = np.linspace(0, 2 * np.pi, n)
+        np.testing.assert_array_equal(th[k:k + n], theta)
+        np.testing.assert_array_equal(gid[k:k + n], i + 1)
+        np.testing.assert_allclose(pts[k:k + n, 0], x * np.cos(theta) + c[0], rtol=0, atol=0)
+        k += n
+    pl, _, rl, _ = polar_gridpoints((0, 0, 0), "log", rmax=4.0, rmin=0.5, dlnr=0.1)
+    assert np.allclose(np.unique(rl[1:]), np.exp(np.linspace(np.log(0.5), np.log(4.0), int(np.log(8.0) / 0.1))))

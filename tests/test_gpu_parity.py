@@ -405,3 +405,50 @@ def test_exact_bond_integral_fp64_vs_oracle(ik, oracle, cg):
     assert_fields(got_k, want_k, FP64_TOL, what="exact kinetic")
     with pytest.raises(ik.IKError):
         run_gpu(ik, 2, fr.L, fr.pos, fr.diam, grid, cg, "fp32")  # FP64 path only
+
+
+def test_radialcalculator_polar_output(tmp_path, golden, monkeypatch, ik):
+    """radialcalculator (irvingkirkwood/__init__.py:80-166) + fieldlogger's polar lines
+    (io.py:130-144) on a fixture frame: '1 id r theta T_00 T_11 T_01', the values those
+    of the same computation on the same grid points through the C ABI."""
+    import pyglasstools_gb300 as pglass
+    import pyglasstools_gb300.io as io
+    import pyglasstools_gb300.irvingkirkwood as ikm
+    import pyglasstools_gb300.irvingkirkwood.cgfunc as cgfunc
+    import pyglasstools_gb300.potential as pot
+    import pyglasstools_gb300.utils as utils
+
+    class Fr:
+        pass
+
+    fx = golden("fixture_frames.npz")
+    fr = Fr()
+    fr.pos = fx["pos180"].astype(np.float64)
+    fr.diam = fx["diam180"].astype(np.float64)
+    fr.L = float(fx["box180"][0])
+    monkeypatch.chdir(tmp_path)
+    pglass.reset()
+    pot.polydisperse12(v0=1.0, eps=0.2, rcut=1.25)
+    mycg = cgfunc.octic(rcut=2.0, mode="fixedpoint", order=5)
+    utils.data_arrays([fr], ndim=2)
+    calc = ikm.radialcalculator(cgfunc=mycg, center=np.array([1.0, -2.0, 0.0]), rmax=5, dr=0.5, precision="fp64")
+    io.fieldlogger(keyword="polar", names=['virialstress_00', 'virialstress_11', 'virialstress_01'], solver=calc)
+    pglass.analyze(frame_list=[0], progress=False)
+    pglass.reset()
+    lines = open(tmp_path / "polar.xyz").read().splitlines()
+    G = calc.gridsize
+    assert lines[0] == f"{G} " and len(lines) == G + 2
+    rows = [ln.split() for ln in lines[2:]]
+    assert [int(r[1]) for r in rows] == [int(v) for v in calc.gridid]
+    np.testing.assert_array_equal(np.array([float(r[2]) for r in rows]), calc.globalr)
+    np.testing.assert_array_equal(np.array([float(r[3]) for r in rows]), calc.globaltheta)
+    vals = np.array([[float(t) for t in r[4:7]] for r in rows])
+    with ik.IKContext() as c:
+        c.set_box(2, [fr.L, fr.L, 1.0])
+        c.set_poly12()
+        c.set_cgfunc("octic", 2.0, order=5)
+        c.set_grid(calc.gridpoints)
+        c.set_frame(fr.pos, fr.diam)
+        c.compute("fp64")
+        v = c.get_field(ik.FIELD_VIRIAL)
+    np.testing.assert_allclose(vals, uniq(v), rtol=6e-6, atol=1e-300)
