@@ -180,8 +180,11 @@ int ik_get_timing(ik_ctx* ctx, float* ms4);
 int ik_get_stream(ik_ctx* ctx, void** stream);
 
 /* Asynchronous download of a slot's field in compact form: g x NC FP64 with
- * NC = 3 (xx, yy, xy) in 2D or 6 (xx, yy, zz, xy, xz, yz) in 3D.  host_out should be
- * pinned for the copy to overlap; it is complete after ik_synchronize. */
+ * NC = 3 (xx, yy, xy) in 2D or 6 (xx, yy, zz, xy, xz, yz) in 3D.  The copy runs on a
+ * download stream of its own after the slot's computation, so that it overlaps the
+ * uploads of other frames and their computations; the slot's next computation waits for
+ * it.  host_out should be pinned for the copy to overlap; it is complete after
+ * ik_synchronize. */
 int ik_download_field_async(ik_ctx* ctx, int slot, int field, double* host_out, int64_t count);
 
 /* Measured FP32 FMA throughput of `device` (TFLOP/s, 2 FLOP per FMA) from a

@@ -102,6 +102,8 @@ struct Slot {
     DevBuf counters; // 4 x u64: bonds, pairs, triples, spare
     cudaEvent_t done = nullptr; // completion of the slot's last computation (on its lane)
     bool done_recorded = false;
+    cudaEvent_t d2h_done = nullptr; // completion of the slot's last field download
+    bool d2h_recorded = false;
     Slot() = default;
     Slot(Slot&&) = default;
     Slot& operator=(Slot&&) = default;
@@ -145,6 +147,8 @@ struct ik_ctx {
     Lane lanes[IK_LANES];
     int next_lane = 0;
     cudaEvent_t fork = nullptr;
+    cudaStream_t d2h = nullptr; // field downloads (ik_download_field_async): full-duplex with uploads
+    cudaEvent_t d2h_last = nullptr;
     DevBuf status, maxnb;
     DevBuf bsum_q; // scan scratch of the neighbour queries (main stream)
     int maxb = 0, halo_cap = 0;
@@ -472,6 +476,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
     CK(cudaEventRecord(c->fork, c->stream));
     CK(cudaStreamWaitEvent(L.st, c->fork, 0));
     if (s.done_recorded && !c->capturing) CK(cudaStreamWaitEvent(L.st, s.done, 0));
+    if (s.d2h_recorded && !c->capturing) CK(cudaStreamWaitEvent(L.st, s.d2h_done, 0)); // outputs being read
     const IkGeom& g = c->geo.geom;
     const int D = c->dim, NC = D == 2 ? 3 : 6;
     const int n = (int)s.n;
@@ -777,8 +782,14 @@ int ik_create(ik_ctx** out, int device)
         delete c;
         return fail(IK_ERR_CUDA, "cudaStreamCreate failed");
     }
+    if (cudaStreamCreateWithFlags(&c->d2h, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return fail(IK_ERR_CUDA, "cudaStreamCreate failed");
+    }
     for (auto& ev : c->ev) cudaEventCreate(&ev);
     cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&c->d2h_last, cudaEventDisableTiming);
     for (Lane& L : c->lanes) {
         if (cudaStreamCreateWithFlags(&L.st, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreateWithFlags(&L.last, cudaEventDisableTiming) != cudaSuccess) {
@@ -812,15 +823,21 @@ int ik_destroy(ik_ctx* c)
     cudaSetDevice(c->device);
     for (Lane& L : c->lanes) if (L.st) cudaStreamSynchronize(L.st);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->d2h) cudaStreamSynchronize(c->d2h);
     for (auto& ev : c->ev) if (ev) cudaEventDestroy(ev);
     if (c->batch_exec) cudaGraphExecDestroy(c->batch_exec);
     if (c->fork) cudaEventDestroy(c->fork);
-    for (Slot& s : c->slots) if (s.done) cudaEventDestroy(s.done);
+    if (c->d2h_last) cudaEventDestroy(c->d2h_last);
+    for (Slot& s : c->slots) {
+        if (s.done) cudaEventDestroy(s.done);
+        if (s.d2h_done) cudaEventDestroy(s.d2h_done);
+    }
     for (Lane& L : c->lanes) {
         if (L.last) cudaEventDestroy(L.last);
         if (L.st) cudaStreamDestroy(L.st);
     }
     if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->d2h) cudaStreamDestroy(c->d2h);
     delete c;
     return IK_OK;
 }
@@ -1202,8 +1219,12 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
         c->batch_alloc_epoch = g_alloc_epoch.load() == epoch_before ? epoch_before : -2;
         return IK_OK; // the first call's results come from the plain launches
     }
-    // replay: after everything already enqueued on the lanes
+    // replay: after everything already enqueued on the lanes and the slots' downloads
     if (int r = ik_wait_all(c)) return r;
+    for (int k = 0; k < count; ++k) {
+        Slot& s = c->slots[(size_t)slots[k]];
+        if (s.d2h_recorded) CK(cudaStreamWaitEvent(c->stream, s.d2h_done, 0));
+    }
     for (int k = 0; k < count; ++k) c->pending.push_back({slots[k], precision, fields});
     CK(cudaGraphLaunch(c->batch_exec, c->stream));
     for (int k = 0; k < count; ++k) {
@@ -1223,6 +1244,7 @@ int ik_synchronize(ik_ctx* c)
     for (int attempt = 0; attempt < 4; ++attempt) {
         for (Lane& L : c->lanes) CK(cudaStreamSynchronize(L.st));
         CK(cudaStreamSynchronize(c->stream));
+        CK(cudaStreamSynchronize(c->d2h));
         int st = 0, mx = 0;
         CK(cudaMemcpy(&st, c->status.p, sizeof(int), cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(&mx, c->maxnb.p, sizeof(int), cudaMemcpyDeviceToHost));
@@ -1561,6 +1583,8 @@ int ik_wait_all(ik_ctx* c)
         CK(cudaEventRecord(L.last, L.st));
         CK(cudaStreamWaitEvent(c->stream, L.last, 0));
     }
+    CK(cudaEventRecord(c->d2h_last, c->d2h));
+    CK(cudaStreamWaitEvent(c->stream, c->d2h_last, 0));
     return IK_OK;
 }
 
@@ -1592,8 +1616,13 @@ int ik_download_field_async(ik_ctx* c, int slot, int field, double* host_out, in
     Slot& s = c->slots[(size_t)slot];
     const DevBuf& src = field == IK_FIELD_VIRIAL ? s.vir : (field == IK_FIELD_KINETIC ? s.kin : s.ela);
     if (!src.p) return fail(IK_ERR_STATE, "slot %d has not been computed", slot);
-    if (s.done_recorded) CK(cudaStreamWaitEvent(c->stream, s.done, 0));
-    if (c->geo.G > 0) CK(cudaMemcpyAsync(host_out, src.p, sizeof(double) * NC * c->geo.G, cudaMemcpyDeviceToHost, c->stream));
+    // on the download stream, after the slot's computation: uploads of other frames
+    // (context stream) and computations (lanes) proceed meanwhile
+    if (s.done_recorded) CK(cudaStreamWaitEvent(c->d2h, s.done, 0));
+    if (c->geo.G > 0) CK(cudaMemcpyAsync(host_out, src.p, sizeof(double) * NC * c->geo.G, cudaMemcpyDeviceToHost, c->d2h));
+    if (!s.d2h_done) CK(cudaEventCreateWithFlags(&s.d2h_done, cudaEventDisableTiming));
+    CK(cudaEventRecord(s.d2h_done, c->d2h));
+    s.d2h_recorded = true;
     return IK_OK;
 }
 

@@ -216,3 +216,29 @@ def test_float32_upload_equals_float64_upload():
         np.testing.assert_array_equal(a[0], b[0])
         np.testing.assert_array_equal(a[1], b[1])
     c.close()
+
+
+def test_async_download_is_not_overwritten_by_the_next_computation():
+    """ik_download_field_async copies on its own stream; the slot's next computation
+    waits for it, so a result being downloaded is never overwritten."""
+    torch = pytest.importorskip("torch")
+    from pyglasstools_gb300 import ikabi as ik, synth
+    fr = _frames(6000, [911, 912])
+    L = fr[0].L
+    grid = synth.lattice_grid(L, 64, 2)
+    c = _context(ik, L, grid, 1)
+    want = []
+    for f in fr:
+        c.upload_frame(0, f.pos, f.diam, f.vel, f.mass)
+        c.compute_slot(0, "fp32")
+        c.synchronize()
+        want.append(uniq(c.get_field(ik.FIELD_VIRIAL)))
+    pinned = [torch.empty((len(grid), 3), dtype=torch.float64, pin_memory=True).numpy() for _ in fr]
+    for k, f in enumerate(fr):  # no synchronisation between the frames
+        c.upload_frame(0, f.pos, f.diam, f.vel, f.mass)
+        c.compute_slot(0, "fp32")
+        c.download_field_async(pinned[k], ik.FIELD_VIRIAL, 0)
+    c.synchronize()
+    for k in range(len(fr)):
+        np.testing.assert_array_equal(pinned[k], want[k])
+    c.close()
