@@ -535,20 +535,24 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                                 up2(r2, r2v[2 * j], r2v[2 * j + 1]);
                             }
                         }
+                        int band = 0;
 #pragma unroll
                         for (int p = 0; p < P; ++p) {
                             const float r2 = r2v[p];
-                            bool in = r2 < R2s;
-                            if (fabsf(r2 - R2s) < margin && gi[p] >= 0) {
-                                // boundary band: decide with the FP64 rule of the reference
-                                const IkB64 pq = a.pos64[sq[s]];
+                            mask |= (r2 < R2s ? 1 : 0) << p;
+                            band |= (fabsf(r2 - R2s) < margin && gi[p] >= 0 ? 1 : 0) << p;
+                        }
+                        if (band) { // rare: inside the thin band around R decide with the FP64 rule
+                            const IkB64 pq = a.pos64[sq[s]];
+#pragma unroll
+                            for (int p = 0; p < P; ++p) {
+                                if (!(band & (1 << p))) continue;
                                 const double* xg = a.grid + 3 * (size_t)gi[p];
                                 const double ddx = ik_minimg(__dsub_rn(xg[0], pq.x), a.g.L[0], a.g.periodic[0]);
                                 const double ddy = ik_minimg(__dsub_rn(xg[1], pq.y), a.g.L[1], a.g.periodic[1]);
                                 const double ddz = ik_minimg(__dsub_rn(xg[2], pq.z), a.g.L[2], a.g.periodic[2]);
-                                in = ik_dot3(ddx, ddy, ddz) < a.R2;
+                                mask = ik_dot3(ddx, ddy, ddz) < a.R2 ? (mask | (1 << p)) : (mask & ~(1 << p));
                             }
-                            if (in) mask |= 1 << p;
                         }
                         if (mask) {
                             cnt = __float_as_int(sp.w) & 63;
