@@ -121,7 +121,7 @@ struct Lane {
     DevBuf mlp_rec, mlp_rid, mlp_count, corr; // surrogate records and fixed-point corrections
     DevBuf eb64, ec64, eb32, ec32, enb, ecnt;  // elastic-field bond records, scratch counters
 };
-constexpr int IK_LANES = 4;
+constexpr int IK_LANES = 8;
 
 struct PendingOp { int slot, prec, fields; };
 
