@@ -57,9 +57,26 @@ int ik_destroy(ik_ctx* ctx);
  * periodic in x, y and (3D only) z.  Replaces SimBox::SimBox (SimBox.cc:25-45). */
 int ik_set_box(ik_ctx* ctx, int dim, const double boxsize[3], const double origin[3]);
 
-/* Pair potential PairPotentialPoly12(scaled_rcut, {v0, eps, c0, c1, c2}).
- * Replaces ShortRangePairPotential<Polydisperse12> (potential/PairPotential.h:83-104,
- * potential/Polydisperse12.h:38-55). */
+/* Pair potentials: the eight ShortRangePairPotential<Model> types the reference exports
+ * (potential/module-potential.cpp:13-34), params in the reference's own order:
+ *   IK_POT_POLY12      PairPotentialPoly12          {v0, eps, c0, c1, c2}      Polydisperse12.h
+ *   IK_POT_LJ          PairPotentialLJ              {eps, vareps}              LennardJones.h:6-88
+ *   IK_POT_FSLJ        PairPotentialForceShiftedLJ  {eps, vareps}              LennardJones.h:91-125
+ *   IK_POT_POLY10      PairPotentialPoly10          {v0, eps, c0, c1, c2, c3}  Polydisperse10.h
+ *   IK_POT_POLY106     PairPotentialPoly106         {v0, eps, c0, c1, c2}      Polydisperse106.h
+ *   IK_POT_POLY18      PairPotentialPoly18          {v0, eps, c0, c1, c2}      Polydisperse18.h
+ *   IK_POT_POLYLJ      PairPotentialPolyLJ          {v0, eps, c0, c1, c2}      PolydisperseLJ.h
+ *   IK_POT_POLYYUKAWA  PairPotentialPolyYukawa      {v0, kappa, eps, c0, c1, c2} PolydisperseYukawa.h
+ * The force (computeForceDivR) is evaluated in FP64 in the reference's expression order
+ * on the FP64 path (bit-identical to the CPU restatement; Yukawa within 2 ulp through
+ * exp) and in FP32 on the FP32 path; the set of force-active bonds is the FP64 one on
+ * both paths.  Replaces ShortRangePairPotential<Model> (potential/PairPotential.h:69-123). */
+enum ik_pot_kind { IK_POT_POLY12 = 0, IK_POT_LJ = 1, IK_POT_FSLJ = 2, IK_POT_POLY10 = 3,
+                   IK_POT_POLY106 = 4, IK_POT_POLY18 = 5, IK_POT_POLYLJ = 6, IK_POT_POLYYUKAWA = 7 };
+int ik_set_potential(ik_ctx* ctx, int kind, double scaled_rcut, const double* params, int nparams);
+/* Number of parameters of a kind (-1: unknown kind). */
+int ik_potential_nparams(int kind);
+/* = ik_set_potential(ctx, IK_POT_POLY12, scaled_rcut, params, 5). */
 int ik_set_potential_poly12(ik_ctx* ctx, double scaled_rcut, const double params[5]);
 
 /* Coarse-graining function.  rcut = support radius R (Gaussian: cut * width);

@@ -1,5 +1,6 @@
 #!/bin/sh
-# Compiles the reference's own Polydisperse12 / Octic / Rect / Mollifier headers
+# Compiles the reference's own pair-potential headers (potential/*.h) and the
+# Octic / Rect / Mollifier headers
 # (header-only, no external dependencies) into oracle/_ref/libref_kernels.so.
 # Only possible where the reference tree exists; outputs go to oracle/_ref only.
 # -ffp-contract=off matches the oracle's evaluation (the reference's own build
@@ -14,9 +15,6 @@ fi
 mkdir -p "$HERE/_ref"
 CG="$REF/pyglasstools/irvingkirkwood/cgfunc"
 ${CXX:-g++} -O2 -fPIC -shared -ffp-contract=off -std=c++14 \
-  -DREF_POLY12_H="\"$REF/pyglasstools/potential/Polydisperse12.h\"" \
-  -DREF_OCTIC_H="\"$CG/CGFuncOctic.h\"" \
-  -DREF_RECT_H="\"$CG/CGFuncRect.h\"" \
-  -DREF_MOLLIFIER_H="\"$CG/CGFuncMollifier.h\"" \
+  -I "$REF/pyglasstools/potential" -I "$CG" \
   -o "$HERE/_ref/libref_kernels.so" "$HERE/ref_kernels.cpp"
 echo "built $HERE/_ref/libref_kernels.so"

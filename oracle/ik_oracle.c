@@ -67,44 +67,102 @@ void ikor_gl_rule(int n, double* x, double* w)
 }
 
 /* ------------------------------------------------------------------------- */
-/* Polydisperse12 (potential/Polydisperse12.h:38-55, :19-35, :57-73) with
- * rsq_cut = scaled_rcut^2 (potential/PairPotential.h:98-104). */
-static double poly12_sigma(const ikor_poly12* p, double di, double dj)
+/* The pair models, each in the evaluation order of its reference expression (C and
+ * C++ both evaluate a*b*c as (a*b)*c; the library is built with -ffp-contract=off):
+ *   Polydisperse12     potential/Polydisperse12.h:19-55
+ *   LennardJones       potential/LennardJones.h:19-57
+ *   ForceShiftedLJ     potential/LennardJones.h:105-124; energy: LennardJones's
+ *   Polydisperse10     potential/Polydisperse10.h:19-53
+ *   Polydisperse106    potential/Polydisperse106.h:19-53
+ *   Polydisperse18     potential/Polydisperse18.h:19-50
+ *   PolydisperseLJ     potential/PolydisperseLJ.h:19-50
+ *   PolydisperseYukawa potential/PolydisperseYukawa.h:19-55
+ * with rsq_cut = scaled_rcut^2 (potential/PairPotential.h:98-113). */
+static double poly12_sigma(const ikor_pot* p, double di, double dj)
 {
     return 0.5 * (di + dj) * (1 - p->eps * fabs(di - dj));
 }
 
-double ikor_force_divr(const ikor_poly12* p, double rsq, double di, double dj)
+double ikor_force_divr(const ikor_pot* p, double rsq, double di, double dj)
 {
     double rcutsq = p->scaled_rcut * p->scaled_rcut;
-    double sigma = poly12_sigma(p, di, dj);
+    double v0 = p->v0, c1 = p->c1, c2 = p->c2, c3 = p->c3, kappa = p->kappa;
+    double sigma = p->kind == IKOR_POT_FSLJ ? 0.5 * (di + dj) : poly12_sigma(p, di, dj);
     double actualrcutsq = rcutsq * sigma * sigma;
-    if (rsq < actualrcutsq) {
-        double r2inv = 1.0 / rsq;
-        r2inv *= sigma * sigma;
-        double _rsq = rsq / (sigma * sigma);
-        double r6inv = r2inv * r2inv * r2inv;
-        return (12.0 * p->v0 * r2inv * r6inv * r6inv - 2.0 * p->c1 - 4.0 * p->c2 * _rsq) / (sigma * sigma);
+    if (!(rsq < actualrcutsq)) return 0.0;
+    if ((p->kind == IKOR_POT_LJ || p->kind == IKOR_POT_FSLJ) && v0 == 0) return 0.0;
+    double r2inv = 1.0 / rsq;
+    r2inv *= sigma * sigma;
+    double _rsq = rsq / (sigma * sigma);
+    double r6inv = r2inv * r2inv * r2inv;
+    double r10inv = r2inv * r2inv * r2inv * r2inv * r2inv;
+    switch (p->kind) {
+    case IKOR_POT_LJ:
+        return (4 * v0 * r2inv * r6inv * (12.0 * r6inv - 6.0)) / (sigma * sigma);
+    case IKOR_POT_FSLJ: {
+        double f = 4 * v0 * r2inv * r6inv * (12.0 * r6inv - 6.0);
+        double c2inv = 1.0 / rcutsq;
+        double c6inv = c2inv * c2inv * c2inv;
+        f -= 4 * v0 * c2inv * c6inv * (12.0 * c6inv - 6.0);
+        return f / (sigma * sigma);
     }
-    return 0.0;
+    case IKOR_POT_POLY10:
+        return (10.0 * v0 * r2inv * r10inv - 2.0 * c1 - 4.0 * c2 * _rsq - 6.0 * c3 * _rsq * _rsq) / (sigma * sigma);
+    case IKOR_POT_POLY106:
+        return (v0 * (10.0 * r10inv * r2inv - 6.0 * r2inv * r2inv * r2inv * r2inv) - 2.0 * c1 - 4.0 * c2 * _rsq) /
+               (sigma * sigma);
+    case IKOR_POT_POLY18:
+        return (18.0 * v0 * r2inv * r6inv * r6inv * r6inv - 2.0 * c1 - 4.0 * c2 * _rsq) / (sigma * sigma);
+    case IKOR_POT_POLYLJ:
+        return (12.0 * v0 * r2inv * r6inv * r6inv - 6.0 * v0 * r2inv * r6inv - 2.0 * c1 - 4.0 * c2 * _rsq) /
+               (sigma * sigma);
+    case IKOR_POT_POLYYUKAWA: {
+        double rinv = sqrt(r2inv), rroot = sqrt(_rsq);
+        return ((exp(-kappa * rroot) * (rinv + kappa) * v0) * r2inv - 2 * c1 - 4 * c2 * _rsq) / (sigma * sigma);
+    }
+    default:
+        return (12.0 * v0 * r2inv * r6inv * r6inv - 2.0 * c1 - 4.0 * c2 * _rsq) / (sigma * sigma);
+    }
 }
 
-double ikor_pair_energy(const ikor_poly12* p, double rsq, double di, double dj)
+double ikor_pair_energy(const ikor_pot* p, double rsq, double di, double dj)
 {
     double rcutsq = p->scaled_rcut * p->scaled_rcut;
+    double v0 = p->v0, c0 = p->c0, c1 = p->c1, c2 = p->c2, c3 = p->c3, kappa = p->kappa;
     double sigma = poly12_sigma(p, di, dj);
     double actualrcutsq = rcutsq * sigma * sigma;
-    if (rsq < actualrcutsq) {
-        double r2inv = 1.0 / rsq;
-        r2inv *= sigma * sigma;
-        double _rsq = rsq / (sigma * sigma);
-        double r6inv = r2inv * r2inv * r2inv;
-        return p->v0 * r6inv * r6inv + p->c0 + p->c1 * _rsq + p->c2 * _rsq * _rsq;
+    if (!(rsq < actualrcutsq)) return 0.0;
+    double r2inv = 1.0 / rsq;
+    r2inv *= sigma * sigma;
+    double _rsq = rsq / (sigma * sigma);
+    double r6inv = r2inv * r2inv * r2inv;
+    double r10inv = r2inv * r2inv * r2inv * r2inv * r2inv;
+    switch (p->kind) {
+    case IKOR_POT_LJ:
+    case IKOR_POT_FSLJ: {
+        double r2invcut = 1.0 / actualrcutsq;
+        r2invcut *= sigma * sigma;
+        double r6invcut = r2invcut * r2invcut * r2invcut;
+        return 4 * v0 * r6inv * (r6inv - 1.0) - 4 * v0 * r6invcut * (r6invcut - 1.0);
     }
-    return 0.0;
+    case IKOR_POT_POLY10:
+        return v0 * r10inv + c0 + c1 * _rsq + c2 * _rsq * _rsq + c3 * _rsq * _rsq * _rsq;
+    case IKOR_POT_POLY106:
+        return v0 * (r10inv - r2inv * r2inv * r2inv) + c0 + c1 * _rsq + c2 * _rsq * _rsq;
+    case IKOR_POT_POLY18:
+        return v0 * r6inv * r6inv * r6inv + c0 + c1 * _rsq + c2 * _rsq * _rsq;
+    case IKOR_POT_POLYLJ:
+        return v0 * r6inv * r6inv - v0 * r6inv + c0 + c1 * _rsq + c2 * _rsq * _rsq;
+    case IKOR_POT_POLYYUKAWA: {
+        double rinv = sqrt(r2inv), rroot = sqrt(_rsq);
+        return v0 * exp(-rroot * kappa) * rinv + c0 + c1 * _rsq + c2 * _rsq * _rsq;
+    }
+    default:
+        return v0 * r6inv * r6inv + c0 + c1 * _rsq + c2 * _rsq * _rsq;
+    }
 }
 
-double ikor_bond_stiffness(const ikor_poly12* p, double rsq, double di, double dj)
+double ikor_bond_stiffness(const ikor_pot* p, double rsq, double di, double dj)
 {
     double rcutsq = p->scaled_rcut * p->scaled_rcut;
     double sigma = poly12_sigma(p, di, dj);
@@ -552,7 +610,7 @@ int64_t ikor_neighbors(const ikor_box* box, int64_t n, const double* pos, double
  * intended KineticStress (ListofCommonObservables.h:131-142, m v(x)v * Delta). */
 typedef struct {
     const ikor_box* box; const double* pos; const double* vel; const double* mass;
-    const double* diam; const ikor_poly12* pot; const ikor_cg* cg;
+    const double* diam; const ikor_pot* pot; const ikor_cg* cg;
     const int64_t* noff; const int32_t* nidx;
     const double* x; double* vir; double* kin; int dim;
     const double* disp; double* ela; /* elastic virial (ElasticVirialStress), or NULL */
@@ -609,12 +667,12 @@ static void g_visit(void* vctx, int64_t i)
 
 static int compute_impl(const ikor_box* box, int64_t n, const double* pos, const double* vel,
                         const double* mass, const double* diam, const double* disp,
-                        const ikor_poly12* pot, const ikor_cg* cg, double max_rcut, int64_t g0,
+                        const ikor_pot* pot, const ikor_cg* cg, double max_rcut, int64_t g0,
                         int64_t g1, const double* grid, double* virial, double* kinetic,
                         double* elastic, int nthreads);
 
 int ikor_compute_range(const ikor_box* box, int64_t n, const double* pos, const double* vel,
-                       const double* mass, const double* diam, const ikor_poly12* pot,
+                       const double* mass, const double* diam, const ikor_pot* pot,
                        const ikor_cg* cg, double max_rcut, int64_t g0, int64_t g1,
                        const double* grid, double* virial, double* kinetic, int nthreads)
 {
@@ -623,7 +681,7 @@ int ikor_compute_range(const ikor_box* box, int64_t n, const double* pos, const 
 }
 
 int ikor_compute_elastic(const ikor_box* box, int64_t n, const double* pos, const double* disp,
-                         const double* diam, const ikor_poly12* pot, const ikor_cg* cg,
+                         const double* diam, const ikor_pot* pot, const ikor_cg* cg,
                          double max_rcut, int64_t g0, int64_t g1, const double* grid,
                          double* virial, double* elastic, int nthreads)
 {
@@ -633,7 +691,7 @@ int ikor_compute_elastic(const ikor_box* box, int64_t n, const double* pos, cons
 
 static int compute_impl(const ikor_box* box, int64_t n, const double* pos, const double* vel,
                         const double* mass, const double* diam, const double* disp,
-                        const ikor_poly12* pot, const ikor_cg* cg, double max_rcut, int64_t g0,
+                        const ikor_pot* pot, const ikor_cg* cg, double max_rcut, int64_t g0,
                         int64_t g1, const double* grid, double* virial, double* kinetic,
                         double* elastic, int nthreads)
 {
@@ -671,7 +729,7 @@ static int compute_impl(const ikor_box* box, int64_t n, const double* pos, const
 }
 
 int ikor_compute(const ikor_box* box, int64_t n, const double* pos, const double* vel,
-                 const double* mass, const double* diam, const ikor_poly12* pot,
+                 const double* mass, const double* diam, const ikor_pot* pot,
                  const ikor_cg* cg, double max_rcut, int64_t g, const double* grid,
                  double* virial, double* kinetic, int nthreads)
 {
@@ -682,7 +740,7 @@ int ikor_compute(const ikor_box* box, int64_t n, const double* pos, const double
 /* ThermoCalculator::compute pair part (thermo/ThermoCalculator.h:68-90):
  * sum over i < j of F (x) r_ij with F = forceDivR * r_ij. */
 void ikor_global_virial(const ikor_box* box, int64_t n, const double* pos, const double* diam,
-                        const ikor_poly12* pot, double max_rcut, double* out)
+                        const ikor_pot* pot, double max_rcut, double* out)
 {
     int D = box->dim;
     for (int k = 0; k < D * D; ++k) out[k] = 0.0;

@@ -30,10 +30,18 @@ typedef struct {
     int periodic[3];    /* 1 = periodic (x, y always; z only in 3D) */
 } ikor_box;
 
+/* The eight pair models of potential/module-potential.cpp:13-34. */
+enum { IKOR_POT_POLY12 = 0, IKOR_POT_LJ = 1, IKOR_POT_FSLJ = 2, IKOR_POT_POLY10 = 3,
+       IKOR_POT_POLY106 = 4, IKOR_POT_POLY18 = 5, IKOR_POT_POLYLJ = 6, IKOR_POT_POLYYUKAWA = 7 };
+
+/* Pair potential in a common layout: v0 = energy scale (LJ: eps), eps = non-additivity
+ * (LJ: vareps), c0..c3 smoothing coefficients (c3: Poly10), kappa (Yukawa). */
 typedef struct {
     double scaled_rcut; /* r~_c: cut-off in units of sigma_ij */
     double v0, eps, c0, c1, c2;
-} ikor_poly12;
+    int kind;           /* IKOR_POT_* */
+    double c3, kappa;
+} ikor_pot;
 
 typedef struct {
     int kind;           /* IKOR_CG_* */
@@ -48,9 +56,10 @@ typedef struct {
 /* Gauss-Legendre nodes/weights on [-1,1] (Newton on the three-term recurrence). */
 void ikor_gl_rule(int n, double* x, double* w);
 
-double ikor_force_divr(const ikor_poly12* p, double rsq, double di, double dj);
-double ikor_pair_energy(const ikor_poly12* p, double rsq, double di, double dj);
-double ikor_bond_stiffness(const ikor_poly12* p, double rsq, double di, double dj);
+/* computeForceDivR / computeEnergy of every model; computeStiffness of Polydisperse12. */
+double ikor_force_divr(const ikor_pot* p, double rsq, double di, double dj);
+double ikor_pair_energy(const ikor_pot* p, double rsq, double di, double dj);
+double ikor_bond_stiffness(const ikor_pot* p, double rsq, double di, double dj);
 
 /* Coarse-graining kernel Delta(dr_sq) for a d-dimensional system. */
 double ikor_delta(const ikor_cg* cg, int dim, double dr_sq);
@@ -78,24 +87,24 @@ int64_t ikor_neighbors(const ikor_box* box, int64_t n, const double* pos, double
  * 0.5 * bond * (f(|r+u|) (r+u)(x)(r+u) - f(|r|) r(x)r), u = disp_j - disp_i, over the
  * neighbours within max_rcut of the undisplaced frame.  disp: n x 3. */
 int ikor_compute_elastic(const ikor_box* box, int64_t n, const double* pos, const double* disp,
-                         const double* diam, const ikor_poly12* pot, const ikor_cg* cg,
+                         const double* diam, const ikor_pot* pot, const ikor_cg* cg,
                          double max_rcut, int64_t g0, int64_t g1, const double* grid,
                          double* virial, double* elastic, int nthreads);
 
 int ikor_compute(const ikor_box* box, int64_t n, const double* pos, const double* vel,
-                 const double* mass, const double* diam, const ikor_poly12* pot,
+                 const double* mass, const double* diam, const ikor_pot* pot,
                  const ikor_cg* cg, double max_rcut, int64_t g, const double* grid,
                  double* virial, double* kinetic, int nthreads);
 
 /* Same loop restricted to grid points [g0, g1) (used for bounded CPU samples). */
 int ikor_compute_range(const ikor_box* box, int64_t n, const double* pos, const double* vel,
-                       const double* mass, const double* diam, const ikor_poly12* pot,
+                       const double* mass, const double* diam, const ikor_pot* pot,
                        const ikor_cg* cg, double max_rcut, int64_t g0, int64_t g1,
                        const double* grid, double* virial, double* kinetic, int nthreads);
 
 /* Global virial sum_{i<j} F_ij (x) r_ij (ThermoCalculator.h:68-90, not divided by volume). */
 void ikor_global_virial(const ikor_box* box, int64_t n, const double* pos, const double* diam,
-                        const ikor_poly12* pot, double max_rcut, double* out /* dim x dim */);
+                        const ikor_pot* pot, double max_rcut, double* out /* dim x dim */);
 
 #ifdef __cplusplus
 }

@@ -29,9 +29,16 @@ class Box(C.Structure):
                 ("periodic", C.c_int * 3)]
 
 
-class Poly12(C.Structure):
+POT_KIND = {"poly12": 0, "lj": 1, "fslj": 2, "poly10": 3, "poly106": 4, "poly18": 5, "polylj": 6,
+            "polyyukawa": 7}
+
+
+class Pot(C.Structure):
+    """ikor_pot: v0 = energy scale (LJ: eps), eps = non-additivity (LJ: vareps)."""
     _fields_ = [("scaled_rcut", C.c_double), ("v0", C.c_double), ("eps", C.c_double),
-                ("c0", C.c_double), ("c1", C.c_double), ("c2", C.c_double)]
+                ("c0", C.c_double), ("c1", C.c_double), ("c2", C.c_double),
+                ("kind", C.c_int), ("c3", C.c_double), ("kappa", C.c_double)]
+
 
 
 class CG(C.Structure):
@@ -55,7 +62,7 @@ def lib():
         L.ikor_gl_rule.argtypes = [C.c_int, dp, dp]
         L.ikor_gk15_rule.argtypes = [dp, dp, dp]
         for f in ("ikor_force_divr", "ikor_pair_energy", "ikor_bond_stiffness"):
-            getattr(L, f).argtypes = [C.POINTER(Poly12), C.c_double, C.c_double, C.c_double]
+            getattr(L, f).argtypes = [C.POINTER(Pot), C.c_double, C.c_double, C.c_double]
             getattr(L, f).restype = C.c_double
         L.ikor_delta.argtypes = [C.POINTER(CG), C.c_int, C.c_double]
         L.ikor_delta.restype = C.c_double
@@ -67,14 +74,14 @@ def lib():
                                      C.POINTER(C.c_int64), C.POINTER(C.c_int32)]
         L.ikor_neighbors.restype = C.c_int64
         L.ikor_compute_range.argtypes = [C.POINTER(Box), C.c_int64, dp, dp, dp, dp,
-                                         C.POINTER(Poly12), C.POINTER(CG), C.c_double,
+                                         C.POINTER(Pot), C.POINTER(CG), C.c_double,
                                          C.c_int64, C.c_int64, dp, dp, dp, C.c_int]
         L.ikor_compute_range.restype = C.c_int
-        L.ikor_compute_elastic.argtypes = [C.POINTER(Box), C.c_int64, dp, dp, dp, C.POINTER(Poly12),
+        L.ikor_compute_elastic.argtypes = [C.POINTER(Box), C.c_int64, dp, dp, dp, C.POINTER(Pot),
                                            C.POINTER(CG), C.c_double, C.c_int64, C.c_int64, dp, dp, dp,
                                            C.c_int]
         L.ikor_compute_elastic.restype = C.c_int
-        L.ikor_global_virial.argtypes = [C.POINTER(Box), C.c_int64, dp, dp, C.POINTER(Poly12),
+        L.ikor_global_virial.argtypes = [C.POINTER(Box), C.c_int64, dp, dp, C.POINTER(Pot),
                                          C.c_double, dp]
         _LIB = L
     return _LIB
@@ -101,14 +108,60 @@ def make_box(dim, L, origin=(0.0, 0.0, 0.0)):
 
 def make_poly12(v0=1.0, eps=0.2, rcut=1.25):
     """pyglasstools.potential.polydisperse12 coefficients (potential/__init__.py:81-86)."""
-    p = Poly12()
+    return make_potential("poly12", rcut, [v0, eps, -28.0 * v0 / rcut ** 12, 48.0 * v0 / rcut ** 14,
+                                           -21.0 * v0 / rcut ** 16])
+
+
+def make_potential(kind, rcut, params):
+    """A pair model from the reference's parameter list (potential/__init__.py:58-146):
+    lj/fslj [eps, vareps]; poly10 [v0, eps, c0, c1, c2, c3]; polyyukawa
+    [v0, kappa, eps, c0, c1, c2]; poly12/poly106/poly18/polylj [v0, eps, c0, c1, c2]."""
+    p = Pot()
+    p.kind = POT_KIND[kind]
     p.scaled_rcut = rcut
-    p.v0 = v0
-    p.eps = eps
-    p.c0 = -28.0 * v0 / rcut ** 12
-    p.c1 = 48.0 * v0 / rcut ** 14
-    p.c2 = -21.0 * v0 / rcut ** 16
+    q = [float(v) for v in params]
+    if kind in ("lj", "fslj"):
+        p.v0, p.eps = q[0], q[1]
+    elif kind == "polyyukawa":
+        p.v0, p.kappa, p.eps, p.c0, p.c1, p.c2 = q[:6]
+    else:
+        p.v0, p.eps, p.c0, p.c1, p.c2 = q[:5]
+        if kind == "poly10":
+            p.c3 = q[5]
     return p
+
+
+def potential_params(kind, **kw):
+    """The parameter list the reference's Python constructor builds for a model
+    (potential/__init__.py:58-146), defaults as there (LJ: eps=1, vareps=0, rcut=2.5)."""
+    import math
+    if kind in ("lj", "fslj"):
+        return kw.get("rcut", 2.5), [kw.get("eps", 1.0), kw.get("vareps", 0.0)]
+    if kind == "poly12":
+        v0, eps, rc = kw.get("v0", 1.0), kw.get("eps", 0.2), kw.get("rcut", 1.25)
+        return rc, [v0, eps, -28.0 * v0 / rc ** 12, 48.0 * v0 / rc ** 14, -21.0 * v0 / rc ** 16]
+    if kind == "poly18":
+        v0, eps, rc = kw.get("v0", 1.0), kw.get("eps", 0.0), kw.get("rcut", 1.25)
+        return rc, [v0, eps, -55.0 * v0 / rc ** 18, 99.0 * v0 / rc ** 20, -45.0 * v0 / rc ** 22]
+    if kind == "polylj":
+        v0, eps, rc = kw.get("v0", 1.0), kw.get("eps", 0.2), kw.get("rcut", 2.5)
+        return rc, [v0, eps, -28.0 * v0 / rc ** 12 + 10.0 / rc ** 6, 48.0 * v0 / rc ** 14 - 15.0 / rc ** 8,
+                    -21.0 * v0 / rc ** 16 + 6.0 / rc ** 10]
+    if kind == "poly10":
+        v0, eps, rc = kw.get("v0", 1.0), kw.get("eps", 0.0416667), kw.get("rcut", 1.48)
+        return rc, [v0, eps, -56.0 * v0 / rc ** 10, 140.0 * v0 / rc ** 12, -120.0 * v0 / rc ** 14,
+                    35.0 * v0 / rc ** 16]
+    if kind == "poly106":
+        v0, eps, rc = kw.get("v0", 1.0), kw.get("eps", 0.1), kw.get("rcut", 3.0)
+        return rc, [v0, eps, (-21 + 10 * rc ** 4) * v0 / rc ** 10, -((5 * (-7 + 3 * rc ** 4) * v0) / rc ** 12),
+                    (3 * (-5 + 2 * rc ** 4) * v0) / rc ** 14]
+    if kind == "polyyukawa":
+        v0, eps, rc, k = kw.get("v0", 10.0), kw.get("eps", 0.0), kw.get("rcut", 4.0), kw.get("kappa", 1.0)
+        e = math.exp(-k * rc)
+        return rc, [v0, k, eps, -((e * (15 + 7 * k * rc + k ** 2 * rc ** 2) * v0) / (8 * rc)),
+                    (e * (5 + 5 * k * rc + k ** 2 * rc ** 2) * v0) / (4 * rc ** 3),
+                    -((e * (3 + 3 * k * rc + k ** 2 * rc ** 2) * v0) / (8 * rc ** 5))]
+    raise KeyError(kind)
 
 
 def make_cg(kind="octic", rcut=2.0, mode="fixedpoint", order=5, width=0.0,
@@ -253,7 +306,7 @@ def global_virial(box, pos, diam, pot, max_rc=None):
 
 # ---- reference kernels compiled from the reference tree (oracle/_ref) --------
 def ref_lib():
-    """The reference's own Polydisperse12/Octic/Rect/Mollifier, or None when
+    """The reference's own pair models and Octic/Rect/Mollifier, or None when
     oracle/_ref was not built (no reference tree on this machine)."""
     path = os.path.join(_HERE, "_ref", "libref_kernels.so")
     if not os.path.exists(path):
@@ -265,6 +318,9 @@ def ref_lib():
     dp = C.POINTER(C.c_double)
     for f in ("ref_poly12_force_divr", "ref_poly12_energy", "ref_poly12_stiffness"):
         getattr(L, f).argtypes = [C.c_double, C.c_double, dp, C.c_double, C.c_double]
+        getattr(L, f).restype = C.c_double
+    for f in ("ref_pot_force_divr", "ref_pot_energy"):
+        getattr(L, f).argtypes = [C.c_int, C.c_double, C.c_double, dp, C.c_int, C.c_double, C.c_double]
         getattr(L, f).restype = C.c_double
     for f in ("ref_octic", "ref_rect", "ref_mollifier"):
         getattr(L, f).argtypes = [C.c_double, C.c_double]

@@ -14,8 +14,9 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libik_gb300.so")
-CU_SOURCES = ["ik_api.cu", "ik_cells.cu", "ik_gather32.cu", "ik_gather64.cu", "ik_noalloc.cu", "ik_bonds.cu",
-              "ik_mlp.cu"]
+# longest first: the build runs them in parallel
+CU_SOURCES = ["ik_gather32.cu", "ik_gather32_aux.cu", "ik_mlp.cu", "ik_api.cu", "ik_cells.cu", "ik_gather64.cu",
+              "ik_noalloc.cu", "ik_bonds.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -59,7 +60,7 @@ def build_cuda(verbose=False):
         o = os.path.join(BUILD, src.replace(".cu", ".o"))
         objs.append(o)
         if _stale(o, [s] + hdrs):
-            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
                          "-Xptxas", "-v", "-c", s, "-o", o])
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         logs = list(ex.map(lambda c: _run(c, verbose), jobs))
@@ -95,7 +96,9 @@ def build_bindings(verbose=False):
     if not _stale(target, [src, LIB] + _headers()):
         return target
     inc = [sysconfig.get_paths()["include"], _pybind_include(), os.path.join(ROOT, "include")]
-    cmd = [os.environ.get("CXX", "g++"), "-O2", "-shared", "-fPIC", "-std=c++17", "-fvisibility=hidden"]
+    # no FMA contraction in host arithmetic (getRcut, max_rcut) on hosts that have FMA
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-shared", "-fPIC", "-std=c++17", "-fvisibility=hidden",
+           "-ffp-contract=off"]
     for i in inc:
         cmd += ["-I", i]
     cmd += [src, "-o", target, "-L" + HERE, "-lik_gb300", "-Wl,-rpath,$ORIGIN"]

@@ -259,26 +259,35 @@ struct PairPotential {
     std::vector<double> getParams() const { return params; }
 };
 
-struct PairPotentialPoly12 : PairPotential {
+// ShortRangePairPotential<Model> for the eight models (potential/PairPotential.h:69-123,
+// potential/module-potential.cpp:13-34); the force and energy are evaluated on the
+// device (ik_eval_pair), getRcut on the host as Model::computeRcut.
+template <int KIND>
+struct ShortRangePairPotential : PairPotential {
     using PairPotential::PairPotential;
-    int model() const override { return 12; }
+    int model() const override { return KIND; }
     void validate() const
     {
-        if (params.size() < 5) throw std::invalid_argument("[ERROR]: Poly12 needs [v0, eps, c0, c1, c2]");
+        const int need = ik_potential_nparams(KIND);
+        if ((int)params.size() < need)
+            throw std::invalid_argument("[ERROR]: this pair potential needs " + std::to_string(need) +
+                                        " parameters, got " + std::to_string(params.size()));
     }
-    double sigma(double di, double dj) const { return 0.5 * (di + dj) * (1 - params[1] * std::fabs(di - dj)); }
+    // computeRcut: rcutsq sigma^2 with the non-additive sigma (the force-shifted LJ
+    // inherits LennardJones::computeRcut, LennardJones.h:77-81)
     double getRcut(py::handle, double di, double dj) override
     {
         validate();
-        double s = sigma(di, dj);
-        return scaled_rcut * scaled_rcut * s * s; // computeRcut (Polydisperse12.h:75-79)
+        const double eps = KIND == IK_POT_POLYYUKAWA ? params[2] : params[1];
+        const double s = 0.5 * (di + dj) * (1 - eps * std::fabs(di - dj));
+        return scaled_rcut * scaled_rcut * s * s;
     }
     std::pair<double, double> eval(py::handle rij, double di, double dj)
     {
         validate();
         Vec3 r = to3(rij);
         ik_ctx* c = util_ctx();
-        check(ik_set_potential_poly12(c, scaled_rcut, params.data()));
+        check(ik_set_potential(c, KIND, scaled_rcut, params.data(), (int)params.size()));
         double f = 0, e = 0;
         check(ik_eval_pair(c, 1, r.data(), &di, &dj, &f, &e));
         return {f, e};
@@ -286,6 +295,7 @@ struct PairPotentialPoly12 : PairPotential {
     double getPairForceDivR(py::handle rij, double di, double dj) override { return eval(rij, di, dj).first; }
     double getPairEnergy(py::handle rij, double di, double dj) override { return eval(rij, di, dj).second; }
 };
+using PairPotentialPoly12 = ShortRangePairPotential<IK_POT_POLY12>;
 
 // ---------------------------------------------------------------- _cgfunc
 struct CoarseGrainFunction {
@@ -494,9 +504,11 @@ struct IrvingKirkwood {
     {
         std::vector<double> grid = to_xyz(gridpoints, (size_t)-1, "gridpoints");
         int64_t G = (int64_t)grid.size() / 3;
-        auto pp = std::dynamic_pointer_cast<PairPotentialPoly12>(pot);
-        if (!pp) throw std::invalid_argument("[ERROR]: only the polydisperse12 potential is on the GPU path");
-        pp->validate();
+        const int kind = pot->model();
+        if (ik_potential_nparams(kind) < 0)
+            throw std::invalid_argument("[ERROR]: the base PairPotential has no force model");
+        if ((int)pot->params.size() < ik_potential_nparams(kind))
+            throw std::invalid_argument("[ERROR]: too few pair-potential parameters");
         const SimBox& b = *sys->simbox;
         double L[3] = {b.boxsize[0], b.boxsize[1], b.boxsize[2]};
         double o[3] = {b.origin[0], b.origin[1], b.origin[2]};
@@ -511,7 +523,7 @@ struct IrvingKirkwood {
         {
             py::gil_scoped_release nogil;
             check(ik_set_box(ctx, b.dim, L, o));
-            check(ik_set_potential_poly12(ctx, pot->scaled_rcut, pot->params.data()));
+            check(ik_set_potential(ctx, kind, pot->scaled_rcut, pot->params.data(), (int)pot->params.size()));
             cg->apply(ctx);
             check(ik_set_max_rcut(ctx, max_rcut));
             if (grid != last_grid) {
@@ -540,6 +552,22 @@ struct IrvingKirkwood {
 };
 
 // ---------------------------------------------------------------- module
+// export_ShortRangePairPotential (potential/PairPotential.h:139-152)
+template <int KIND>
+static void export_short_range(py::module& pm, const char* name)
+{
+    using T = ShortRangePairPotential<KIND>;
+    py::class_<T, PairPotential, std::shared_ptr<T>>(pm, name)
+        .def(py::init<std::vector<double>>())
+        .def(py::init<double, std::vector<double>>())
+        .def("getRcut", &T::getRcut)
+        .def("getPairForceDivR", &T::getPairForceDivR)
+        .def("getPairEnergy", &T::getPairEnergy)
+        .def("getParams", &T::getParams)
+        .def("setParams", &T::setParams)
+        .def_readwrite("scaled_rcut", &T::scaled_rcut);
+}
+
 PYBIND11_MODULE(_core, m)
 {
     m.doc() = "GB300 Irving-Kirkwood engine: pybind11 mirror of pyglasstools' native modules";
@@ -620,9 +648,14 @@ PYBIND11_MODULE(_core, m)
         .def("getParams", &PairPotential::getParams)
         .def("setParams", &PairPotential::setParams)
         .def_readwrite("scaled_rcut", &PairPotential::scaled_rcut);
-    py::class_<PairPotentialPoly12, PairPotential, std::shared_ptr<PairPotentialPoly12>>(pm, "PairPotentialPoly12")
-        .def(py::init<std::vector<double>>())
-        .def(py::init<double, std::vector<double>>());
+    export_short_range<IK_POT_LJ>(pm, "PairPotentialLJ");
+    export_short_range<IK_POT_FSLJ>(pm, "PairPotentialForceShiftedLJ");
+    export_short_range<IK_POT_POLY12>(pm, "PairPotentialPoly12");
+    export_short_range<IK_POT_POLY18>(pm, "PairPotentialPoly18");
+    export_short_range<IK_POT_POLY10>(pm, "PairPotentialPoly10");
+    export_short_range<IK_POT_POLY106>(pm, "PairPotentialPoly106");
+    export_short_range<IK_POT_POLYYUKAWA>(pm, "PairPotentialPolyYukawa");
+    export_short_range<IK_POT_POLYLJ>(pm, "PairPotentialPolyLJ");
 
     py::module cm = m.def_submodule("_cgfunc");
     py::class_<CoarseGrainFunction, std::shared_ptr<CoarseGrainFunction>>(cm, "CoarseGrainFunction")

@@ -135,7 +135,8 @@ struct ik_ctx {
     // configuration
     int dim = 0;
     Geo geo; // box, grid, binning (swapped with a slot's own while it is processed)
-    IkPoly12 pot{};
+    IkPot pot{};
+    double scaled_rcut = 0.0;
     bool pot_set = false;
     IkCG cg{};
     bool cg_set = false;
@@ -571,7 +572,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         a.items = c->geo.items_d.as<int4>();
         a.nitems = c->geo.nitems;
         a.halo_cap = c->halo_cap;
-        a.qcap = 32 * (c->maxb + 1);
+        a.qcap = 32 * (std::min(c->maxb, 63) + 1); // <= 63 bonds per staged entry
         double norm = c->cg.kind == IK_CG_MOLLIFIER ? c->cg.mollifier_norm : c->cg.norm;
         ENS(L.vir2, sizeof(float2) * NC * (size_t)c->geo.G);
         ENS(L.kin2, sizeof(float2) * NC * (size_t)c->geo.G);
@@ -628,7 +629,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
             e.bonds = L.eb32.as<float4>();
             e.bcoef = L.ec32.as<float4>();
             e.maxb = c->maxbe;
-            e.qcap = 32 * (c->maxbe + 1);
+            e.qcap = 32 * (std::min(c->maxbe, 63) + 1);
             e.fields = IK_FIELD_VIRIAL;
             e.mlp_rec = nullptr;
             e.mlp_rid = nullptr;
@@ -868,21 +869,52 @@ int ik_set_box(ik_ctx* c, int dim, const double boxsize[3], const double origin[
     return IK_OK;
 }
 
-int ik_set_potential_poly12(ik_ctx* c, double scaled_rcut, const double params[5])
+// Parameter counts and layouts of the reference's models (potential/__init__.py and the
+// constructors of potential/*.h): LJ [eps, vareps]; Poly10 [v0, eps, c0, c1, c2, c3];
+// PolyYukawa [v0, kappa, eps, c0, c1, c2]; the others [v0, eps, c0, c1, c2].
+int ik_potential_nparams(int kind)
+{
+    switch (kind) {
+    case IK_POT_LJ: case IK_POT_FSLJ: return 2;
+    case IK_POT_POLY10: case IK_POT_POLYYUKAWA: return 6;
+    case IK_POT_POLY12: case IK_POT_POLY106: case IK_POT_POLY18: case IK_POT_POLYLJ: return 5;
+    default: return -1;
+    }
+}
+
+int ik_set_potential(ik_ctx* c, int kind, double scaled_rcut, const double* params, int nparams)
 {
     if (int r = check_ctx(c)) return r;
-    ++c->config_version; // captured batch graphs hold the old settings
+    const int need = ik_potential_nparams(kind);
+    if (need < 0) return fail(IK_ERR_ARG, "unknown pair potential kind %d", kind);
     if (!params) return fail(IK_ERR_ARG, "null params");
-    if (!(scaled_rcut > 0.0)) return fail(IK_ERR_ARG, "scaled_rcut must be > 0");
-    c->pot.rcutsq = scaled_rcut * scaled_rcut;
-    c->pot.v0 = params[0];
-    c->pot.eps = params[1];
-    c->pot.c0 = params[2];
-    c->pot.c1 = params[3];
-    c->pot.c2 = params[4];
-    c->pot.max_rcut_sq = c->max_rcut * c->max_rcut;
+    if (nparams < need) return fail(IK_ERR_ARG, "pair potential kind %d needs %d parameters (got %d)", kind, need, nparams);
+    if (!(scaled_rcut > 0.0) || !std::isfinite(scaled_rcut)) return fail(IK_ERR_ARG, "scaled_rcut must be > 0");
+    ++c->config_version; // captured batch graphs hold the old settings
+    IkPot p{};
+    p.kind = kind;
+    p.rcutsq = scaled_rcut * scaled_rcut;
+    if (need == 2) {
+        p.v0 = params[0];
+        p.eps = params[1];
+    } else if (kind == IK_POT_POLYYUKAWA) {
+        p.v0 = params[0]; p.kappa = params[1]; p.eps = params[2];
+        p.c0 = params[3]; p.c1 = params[4]; p.c2 = params[5];
+    } else {
+        p.v0 = params[0]; p.eps = params[1];
+        p.c0 = params[2]; p.c1 = params[3]; p.c2 = params[4];
+        if (kind == IK_POT_POLY10) p.c3 = params[5];
+    }
+    p.max_rcut_sq = c->max_rcut * c->max_rcut;
+    c->pot = p;
+    c->scaled_rcut = scaled_rcut;
     c->pot_set = true;
     return IK_OK;
+}
+
+int ik_set_potential_poly12(ik_ctx* c, double scaled_rcut, const double params[5])
+{
+    return ik_set_potential(c, IK_POT_POLY12, scaled_rcut, params, 5);
 }
 
 int ik_set_cgfunc(ik_ctx* c, int kind, int mode, int order, double rcut, double width)
@@ -1097,8 +1129,7 @@ static int upload_impl(ik_ctx* c, int slot, int64_t n, const void* pos, const vo
     s.n = n;
     s.dmax = dmax;
     if (!c->max_rcut_set && n > 0 && c->pot_set) {
-        double sr = std::sqrt(c->pot.rcutsq);
-        double m = sr * dmax;
+        double m = c->scaled_rcut * dmax;
         ik_set_max_rcut(c, m > dmax ? m : dmax); // Calculator.h:41-45
     }
     return IK_OK;
@@ -1260,11 +1291,11 @@ int ik_synchronize(ik_ctx* c)
             int mxe = 0;
             CK(cudaMemcpy(&mxe, c->maxnbe.p, sizeof(int), cudaMemcpyDeviceToHost));
             if (mx > c->maxb) {
-                if (mx > 63) { c->pending.clear(); return fail(IK_ERR_CAPACITY, "a particle has %d force-active bonds (max 63)", mx); }
+                if (mx > IK_MAXB_LIMIT) { c->pending.clear(); return fail(IK_ERR_CAPACITY, "a particle has %d force-active bonds (max %d)", mx, IK_MAXB_LIMIT); }
                 c->maxb = mx;
             }
             if (mxe > c->maxbe) {
-                if (mxe > 63) { c->pending.clear(); return fail(IK_ERR_CAPACITY, "a particle has %d neighbours within max_rcut (max 63 for the elastic field)", mxe); }
+                if (mxe > IK_MAXB_LIMIT) { c->pending.clear(); return fail(IK_ERR_CAPACITY, "a particle has %d neighbours within max_rcut (max %d for the elastic field)", mxe, IK_MAXB_LIMIT); }
                 c->maxbe = mxe;
             }
             grow = true;

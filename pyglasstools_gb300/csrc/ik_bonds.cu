@@ -62,7 +62,7 @@ __global__ void k_pack32(IkGeom g, int n, const int* __restrict__ sorted, const 
     r.cell = cell_of[i];
     prec[p] = r;
     plo[p] = rello[i];
-    pos64[p] = make_ikb64(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.0);
+    pos64[p] = make_ikb64(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], diam[i]);
     double m = mass ? mass[i] : 1.0;
     double vx = vel ? vel[3 * i] : 0.0, vy = vel ? vel[3 * i + 1] : 0.0, vz = vel ? vel[3 * i + 2] : 0.0;
     if (g.dim == 2) {
@@ -89,6 +89,90 @@ __device__ __forceinline__ float ik_df_diff(float ohi, float olo, float hj, floa
 }
 
 // ---------------------------------------------------------------------------
+// FP32 force of the eight pair models (the expressions of potential/*.h with FP32
+// constants; r2inv = sigma^2 / r^2, rs = r^2 / sigma^2, s2 = sigma^2).
+struct IkPotF {
+    int kind;
+    float rc2, eps_s, v0, v0x4, c1x2, c2x4, c3x6, kappa, shift;
+};
+__device__ __forceinline__ IkPotF ik_potf(const IkPot& p)
+{
+    IkPotF q;
+    q.kind = p.kind;
+    const bool lj = p.kind == IKP_LJ || p.kind == IKP_FSLJ;
+    q.rc2 = lj && p.v0 == 0.0 ? 0.f : (float)p.rcutsq; // eps = 0: no force (LennardJones.h:48)
+    q.eps_s = p.kind == IKP_FSLJ ? 0.f : (float)p.eps;
+    q.v0 = (float)p.v0;
+    q.v0x4 = (float)(4.0 * p.v0);
+    q.c1x2 = (float)(2.0 * p.c1);
+    q.c2x4 = (float)(4.0 * p.c2);
+    q.c3x6 = (float)(6.0 * p.c3);
+    q.kappa = (float)p.kappa;
+    const double c2inv = 1.0 / p.rcutsq, c6inv = c2inv * c2inv * c2inv;
+    q.shift = (float)(4.0 * p.v0 * c2inv * c6inv * (12.0 * c6inv - 6.0)); // LennardJones.h:117-119
+    return q;
+}
+template <int KIND>
+__device__ __forceinline__ float ik_force32(const IkPotF& q, float r2, float s2)
+{
+    const float r2inv = s2 / r2, rs = r2 / s2;
+    const float r6 = r2inv * r2inv * r2inv;
+    float t;
+    switch (KIND) {
+    case IKP_LJ: t = q.v0x4 * r2inv * r6 * (12.f * r6 - 6.f); break;
+    case IKP_FSLJ: t = q.v0x4 * r2inv * r6 * (12.f * r6 - 6.f) - q.shift; break;
+    case IKP_POLY10: {
+        const float r10 = r6 * r2inv * r2inv;
+        t = 10.f * q.v0 * r2inv * r10 - q.c1x2 - q.c2x4 * rs - q.c3x6 * rs * rs;
+        break;
+    }
+    case IKP_POLY106: {
+        const float r10 = r6 * r2inv * r2inv;
+        t = q.v0 * (10.f * r10 * r2inv - 6.f * r6 * r2inv) - q.c1x2 - q.c2x4 * rs;
+        break;
+    }
+    case IKP_POLY18: t = 18.f * q.v0 * r2inv * r6 * r6 * r6 - q.c1x2 - q.c2x4 * rs; break;
+    case IKP_POLYLJ: t = q.v0 * r2inv * r6 * (12.f * r6 - 6.f) - q.c1x2 - q.c2x4 * rs; break;
+    case IKP_POLYYUKAWA: {
+        const float rinv = sqrtf(r2inv), rroot = sqrtf(rs);
+        t = expf(-q.kappa * rroot) * (rinv + q.kappa) * q.v0 * r2inv - q.c1x2 - q.c2x4 * rs;
+        break;
+    }
+    default: t = 12.f * q.v0 * r2inv * r6 * r6 - q.c1x2 - q.c2x4 * rs; break;
+    }
+    return t / s2;
+}
+
+// The FP64 selection of a bond (k_bonds64's test, bit for bit): within max_rcut and
+// force-active.  The FP32 kernels call it for pairs whose FP32 distance lies within
+// 2e-5 (relative) of a cut-off, so that both paths keep exactly the same bonds.
+__device__ __forceinline__ bool ik_select64_r(const IkPot& pot, double dx, double dy, double dz, double di,
+                                              double dj)
+{
+    const double rsq = ik_dot3(dx, dy, dz);
+    if (!(rsq < pot.max_rcut_sq)) return false;
+    return ik_active64(pot, rsq, ik_sigma64(pot, di, dj));
+}
+// Minimum image by division, as the oracle (boxes with fewer than three cells on an axis).
+__device__ __forceinline__ bool ik_select64(const IkGeom& g, const IkPot& pot, const IkB64& a, const IkB64& b)
+{
+    return ik_select64_r(pot, ik_minimg(__dsub_rn(b.x, a.x), g.L[0], g.periodic[0]),
+                         ik_minimg(__dsub_rn(b.y, a.y), g.L[1], g.periodic[1]),
+                         ik_minimg(__dsub_rn(b.z, a.z), g.L[2], g.periodic[2]), a.w, b.w);
+}
+// With three or more cells per axis a stencil candidate near a cut-off lies within
+// max_rcut <= L/3 of the particle, so the oracle's image count rint(d / L) is exactly
+// minus the stencil's wrap shift s (the image of b used is b + s L): the same
+// d - L k without the divisions.
+__device__ __forceinline__ bool ik_select64_shift(const IkGeom& g, const IkPot& pot, const IkB64& a,
+                                                  const IkB64& b, int sx, int sy, int sz)
+{
+    return ik_select64_r(pot, __dsub_rn(__dsub_rn(b.x, a.x), __dmul_rn(g.L[0], (double)(-sx))),
+                         __dsub_rn(__dsub_rn(b.y, a.y), __dmul_rn(g.L[1], (double)(-sy))),
+                         __dsub_rn(__dsub_rn(b.z, a.z), __dmul_rn(g.L[2], (double)(-sz))), a.w, b.w);
+}
+
+// ---------------------------------------------------------------------------
 // Force-active bonds, one thread per particle (particles in cell order, so that
 // neighbouring threads walk the same candidate cells and their loads hit in L1).
 // Each candidate of the 3^d stencil is screened in FP32 from the cell-relative
@@ -100,9 +184,9 @@ __device__ __forceinline__ float ik_df_diff(float ohi, float olo, float hj, floa
 // bond, r_ij = r_j - r_i) and f' = 2 forceDivR / kappa^2, so that
 // f' * hb (x) hb = 0.5 * forceDivR * r_ij (x) r_ij.  Written at a fixed stride of
 // `maxb` records per particle in candidate order (stencil cell with x fastest, then
-// ascending sorted index): deterministic.
-template <int DIM>
-__global__ void __launch_bounds__(128) k_bonds32t(IkGeom g, IkPoly12 pot, float kappa, int n,
+// ascending sorted index): deterministic.  ALLAX: some axis has fewer than three cells.
+template <int DIM, int KIND, bool ALLAX>
+__global__ void __launch_bounds__(128) k_bonds32t(IkGeom g, IkPot pot, float kappa, int n,
                                                   const IkPRec* __restrict__ prec,
                                                   const float* __restrict__ diam32,
                                                   const int* __restrict__ cell_start,
@@ -123,13 +207,12 @@ __global__ void __launch_bounds__(128) k_bonds32t(IkGeom g, IkPoly12 pot, float 
         else if (g.all_bond[a]) { lo[a] = 0; len[a] = g.nc[a]; }
         else { lo[a] = home[a] - 1; len[a] = 3; }
     }
-    const bool allx = len[0] > 3 || (g.all_bond[0] && g.nc[0] > 1);
-    const bool ally = len[1] > 3 || (g.all_bond[1] && g.nc[1] > 1);
-    const bool allz = DIM == 3 && (len[2] > 3 || (g.all_bond[2] && g.nc[2] > 1));
+    const bool allx = ALLAX && (len[0] > 3 || (g.all_bond[0] && g.nc[0] > 1));
+    const bool ally = ALLAX && (len[1] > 3 || (g.all_bond[1] && g.nc[1] > 1));
+    const bool allz = ALLAX && DIM == 3 && (len[2] > 3 || (g.all_bond[2] && g.nc[2] > 1));
     const float L0 = (float)g.L[0], L1 = (float)g.L[1], L2 = (float)g.L[2];
-    const float rc2 = (float)pot.rcutsq, mr2 = (float)pot.max_rcut_sq;
-    const float eps = (float)pot.eps, v12 = (float)(12.0 * pot.v0), c1x2 = (float)(2.0 * pot.c1),
-                c2x4 = (float)(4.0 * pot.c2);
+    const IkPotF pf = ik_potf(pot);
+    const float rc2 = pf.rc2, mr2 = (float)pot.max_rcut_sq, eps = pf.eps_s;
     const float screen = 1.0f + 1e-4f;
     const float di = diam32[p];
     const float4 mlo = plo[p];
@@ -185,10 +268,15 @@ __global__ void __launch_bounds__(128) k_bonds32t(IkGeom g, IkPoly12 pot, float 
                         }
                     }
                     r2 = bx * bx + by * by + bz * bz;
-                    if (r2 < mr2 && r2 < rc2 * s2) {
-                        const float r2inv = s2 / r2;
-                        const float r6 = r2inv * r2inv * r2inv;
-                        const float f = (v12 * r2inv * r6 * r6 - c1x2 - c2x4 * (r2 / s2)) / s2;
+                    const float rt = rc2 * s2;
+                    bool act = r2 < mr2 && r2 < rt;
+                    if (fabsf(r2 - rt) <= 2e-5f * rt || fabsf(r2 - mr2) <= 2e-5f * mr2) { // at a cut-off: FP64
+                        if (ALLAX) act = ik_select64(g, pot, pos64[p], pos64[q]);
+                        else act = ik_select64_shift(g, pot, pos64[p], pos64[q], (ux > wx) - (ux < wx),
+                                                     (uy > wy) - (uy < wy), DIM == 3 ? (uz > wz) - (uz < wz) : 0);
+                    }
+                    if (act) {
+                        const float f = ik_force32<KIND>(pf, r2, s2);
                         if (cnt < maxb) out[cnt] = make_float4(hk * bx, hk * by, hk * bz, fk * f);
                         ++cnt;
                     }
@@ -348,7 +436,7 @@ __global__ void k_cell_sort_pack32(IkGeom g, const int* __restrict__ cell_start,
         r.cell = c;
         prec[p] = r;
         plo[p] = rello[i];
-        pos64[p] = make_ikb64(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.0);
+        pos64[p] = make_ikb64(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], diam[i]);
         const double m = mass ? mass[i] : 1.0;
         const double vx = vel ? vel[3 * i] : 0.0, vy = vel ? vel[3 * i + 1] : 0.0, vz = vel ? vel[3 * i + 2] : 0.0;
         if (g.dim == 2) {
@@ -383,7 +471,7 @@ cudaError_t launch_pack32(IkGeom g, int n, const int* sorted, const int* cell_of
     return cudaGetLastError();
 }
 
-cudaError_t launch_bonds32(int dim, IkGeom g, IkPoly12 pot, float kappa, int n, const IkPRec* prec,
+cudaError_t launch_bonds32(int dim, IkGeom g, IkPot pot, float kappa, int n, const IkPRec* prec,
                             const float* diam32, const int* cell_start, const float4* plo, const IkB64* pos64,
                             float4* tmp, int maxb, int* nb, int* status, int* maxnb,
                             unsigned long long* nbond_total, cudaStream_t st)
@@ -391,12 +479,28 @@ cudaError_t launch_bonds32(int dim, IkGeom g, IkPoly12 pot, float kappa, int n, 
     if (n <= 0) return cudaSuccess;
     const int threads = 128;
     const int blocks = (n + threads - 1) / threads;
-    if (dim == 2)
-        k_bonds32t<2><<<blocks, threads, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, plo, pos64, tmp, maxb,
-                                                  nb, status, maxnb, nbond_total);
-    else
-        k_bonds32t<3><<<blocks, threads, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, plo, pos64, tmp, maxb,
-                                                  nb, status, maxnb, nbond_total);
+    auto go = [&](auto kernel) {
+        kernel<<<blocks, threads, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, plo, pos64, tmp, maxb, nb,
+                                           status, maxnb, nbond_total);
+    };
+    bool allax = false;
+    for (int a = 0; a < dim; ++a) allax = allax || (g.all_bond[a] && g.nc[a] > 1);
+#define IK_BONDS32_KIND(K)                                                        \
+    case K:                                                                       \
+        if (dim == 2) allax ? go(k_bonds32t<2, K, true>) : go(k_bonds32t<2, K, false>); \
+        else allax ? go(k_bonds32t<3, K, true>) : go(k_bonds32t<3, K, false>);   \
+        break;
+    switch (pot.kind) {
+        IK_BONDS32_KIND(IKP_LJ)
+        IK_BONDS32_KIND(IKP_FSLJ)
+        IK_BONDS32_KIND(IKP_POLY10)
+        IK_BONDS32_KIND(IKP_POLY106)
+        IK_BONDS32_KIND(IKP_POLY18)
+        IK_BONDS32_KIND(IKP_POLYLJ)
+        IK_BONDS32_KIND(IKP_POLYYUKAWA)
+    default: IK_BONDS32_KIND(IKP_POLY12)
+    }
+#undef IK_BONDS32_KIND
     return cudaGetLastError();
 }
 

@@ -158,7 +158,7 @@ __device__ __forceinline__ StencilAxis ik_axis(const IkGeom& g, int c, int home)
 
 // 5b. FP64 force-active bond records (plain path): {rij.x, rij.y, rij.z, forceDivR}
 //     in sorted-particle order, bit-identical selection to the oracle.
-__global__ void k_bonds64(IkGeom g, IkPoly12 pot, int n, const int* __restrict__ sorted,
+__global__ void k_bonds64(IkGeom g, IkPot pot, int n, const int* __restrict__ sorted,
                           const int* __restrict__ cell_of, const double* __restrict__ pos,
                           const double* __restrict__ diam, const int* __restrict__ cell_start,
                           IkB64* __restrict__ bonds, int maxb, int* __restrict__ nb,
@@ -212,7 +212,7 @@ __global__ void k_bonds64(IkGeom g, IkPoly12 pot, int n, const int* __restrict__
 //     record is kept when either force is non-zero.  Written for both gathers at a
 //     fixed stride of maxb per particle (cell order): FP64 {r_ij} + C (NC doubles),
 //     FP32 {kappa r_ij / 2} + C (float4 x CW).
-__global__ void k_bonds64e(IkGeom g, IkPoly12 pot, float kappa, int n, const int* __restrict__ sorted,
+__global__ void k_bonds64e(IkGeom g, IkPot pot, float kappa, int n, const int* __restrict__ sorted,
                            const int* __restrict__ cell_of, const double* __restrict__ pos,
                            const double* __restrict__ disp, const double* __restrict__ diam,
                            const int* __restrict__ cell_start, IkB64* __restrict__ b64,
@@ -353,16 +353,17 @@ __global__ void k_point_query(IkGeom g, int n, const double* __restrict__ pos, d
 }
 
 // 8. scalar evaluations for the Python-facing getPairForceDivR / getBondFunc
-__global__ void k_eval_pair(IkPoly12 pot, int m, const double* __restrict__ rij, const double* __restrict__ di,
+__global__ void k_eval_pair(IkPot pot, int m, const double* __restrict__ rij, const double* __restrict__ di,
                             const double* __restrict__ dj, double* __restrict__ f, double* __restrict__ en)
 {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= m) return;
     double rsq = ik_dot3(rij[3 * k], rij[3 * k + 1], rij[3 * k + 2]);
-    double sig = ik_sigma64(pot, di[k], dj[k]);
-    bool act = ik_active64(pot, rsq, sig);
-    f[k] = act ? ik_force64(pot, rsq, sig) : 0.0;
-    en[k] = act ? ik_energy64(pot, rsq, sig) : 0.0;
+    const double sig = ik_sigma64(pot, di[k], dj[k]);
+    f[k] = ik_active64(pot, rsq, sig) ? ik_force64(pot, rsq, sig) : 0.0;
+    // computeEnergy: its own sigma (force-shifted LJ: the non-additive one) and cut-off
+    const double sie = ik_sigma64(pot, di[k], dj[k], false);
+    en[k] = rsq < __dmul_rn(__dmul_rn(pot.rcutsq, sie), sie) ? ik_energy64(pot, rsq, sie) : 0.0;
 }
 
 // 9. FP32 FMA throughput probe: IK_FMA_PROBE_CHAINS independent FFMA chains per thread.

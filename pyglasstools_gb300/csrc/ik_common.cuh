@@ -7,6 +7,8 @@
 #define IK_MAXB_3D 32
 #define IK_WARPS_GATHER 8
 #define IK_P 4          // grid points per warp group in the FP32 gather
+#define IK_SQ_CONT (1 << 30) // staged-entry flag: further bonds of a particle already staged
+#define IK_MAXB_LIMIT 1023   // force-active bonds (and elastic neighbours) per particle
 
 // device status word bits (ctx->d_status)
 #define IK_ST_BOND_OVERFLOW 1
@@ -30,9 +32,23 @@ struct IkGeom {
     int periodic[3];
 };
 
-struct IkPoly12 {
+// Pair potential (potential/*.h), one struct for the eight models of the reference.
+// kind = IKP_* (the values of ik_pot_kind of the C ABI).  Parameters in a common layout:
+//   v0    energy scale (LennardJones / ForceShiftedLennardJones: eps)
+//   eps   non-additivity of sigma_ij (LennardJones: vareps; ForceShifted: unused)
+//   c0-c3 smoothing polynomial (c3: Polydisperse10 only); kappa (PolydisperseYukawa)
+#define IKP_POLY12 0
+#define IKP_LJ 1
+#define IKP_FSLJ 2
+#define IKP_POLY10 3
+#define IKP_POLY106 4
+#define IKP_POLY18 5
+#define IKP_POLYLJ 6
+#define IKP_POLYYUKAWA 7
+struct IkPot {
+    int kind;
     double rcutsq;       // scaled_rcut^2
-    double v0, eps, c0, c1, c2;
+    double v0, eps, c0, c1, c2, c3, kappa;
     double max_rcut_sq;
 };
 
@@ -85,40 +101,150 @@ __device__ __forceinline__ double ik_dot3(double a, double b, double c)
     return __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c));
 }
 
-// Polydisperse12::computeForceDivR in FP64, evaluation order of the reference
-// (potential/Polydisperse12.h:38-55), explicit rounding.
-__device__ __forceinline__ double ik_sigma64(const IkPoly12& p, double di, double dj)
+// computeForceDivR / computeEnergy of the eight models in FP64, each in the evaluation
+// order of its reference expression (C++ left-to-right), every operation rounded
+// explicitly so that no FMA contraction changes a bit against the CPU oracle.
+//   Polydisperse12   potential/Polydisperse12.h:19-55
+//   LennardJones     potential/LennardJones.h:19-57 (force needs eps != 0)
+//   ForceShiftedLJ   potential/LennardJones.h:105-124 (sigma without vareps; energy of LJ)
+//   Polydisperse10   potential/Polydisperse10.h:19-53
+//   Polydisperse106  potential/Polydisperse106.h:19-53
+//   Polydisperse18   potential/Polydisperse18.h:19-50
+//   PolydisperseLJ   potential/PolydisperseLJ.h:19-50
+//   PolydisperseYukawa potential/PolydisperseYukawa.h:19-55 (exp: CUDA's, <= 2 ulp from libm)
+// sigma_ij: 0.5 (d_i + d_j) (1 - eps |d_i - d_j|); the force-shifted LJ force uses
+// 0.5 (d_i + d_j).  `force` selects the force's sigma (the energy of the force-shifted
+// model is the truncated LJ one, with the non-additive sigma).
+__device__ __forceinline__ double ik_sigma_eps(double eps, double di, double dj)
 {
-    return __dmul_rn(__dmul_rn(0.5, __dadd_rn(di, dj)),
-                     __dsub_rn(1.0, __dmul_rn(p.eps, fabs(__dsub_rn(di, dj)))));
+    return __dmul_rn(__dmul_rn(0.5, __dadd_rn(di, dj)), __dsub_rn(1.0, __dmul_rn(eps, fabs(__dsub_rn(di, dj)))));
 }
-__device__ __forceinline__ bool ik_active64(const IkPoly12& p, double rsq, double sigma)
+__device__ __forceinline__ double ik_sigma64(const IkPot& p, double di, double dj, bool force = true)
+{
+    if (force && p.kind == IKP_FSLJ) return __dmul_rn(0.5, __dadd_rn(di, dj));
+    return ik_sigma_eps(p.eps, di, dj);
+}
+// the force is non-zero only inside the cut-off (and, for the LJ models, for eps != 0)
+__device__ __forceinline__ bool ik_active64(const IkPot& p, double rsq, double sigma)
 {
     double actual = __dmul_rn(__dmul_rn(p.rcutsq, sigma), sigma);
+    if ((p.kind == IKP_LJ || p.kind == IKP_FSLJ) && p.v0 == 0.0) return false;
     return rsq < actual;
 }
-__device__ __forceinline__ double ik_force64(const IkPoly12& p, double rsq, double sigma)
+// 4 v0 r2inv r6inv (12 r6inv - 6), left to right
+__device__ __forceinline__ double ik_lj_fterm(double v0, double r2inv, double r6inv)
 {
-    double s2 = __dmul_rn(sigma, sigma);
-    double r2inv = __dmul_rn(__ddiv_rn(1.0, rsq), s2);
-    double rs = __ddiv_rn(rsq, s2);
-    double r6inv = __dmul_rn(__dmul_rn(r2inv, r2inv), r2inv);
-    double t = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(12.0, p.v0), r2inv), r6inv), r6inv);
-    t = __dsub_rn(t, __dmul_rn(2.0, p.c1));
-    t = __dsub_rn(t, __dmul_rn(__dmul_rn(4.0, p.c2), rs));
-    return __ddiv_rn(t, s2);
+    return __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(4.0, v0), r2inv), r6inv),
+                     __dsub_rn(__dmul_rn(12.0, r6inv), 6.0));
 }
-__device__ __forceinline__ double ik_energy64(const IkPoly12& p, double rsq, double sigma)
+__device__ __forceinline__ double ik_force64(const IkPot& p, double rsq, double sigma)
 {
-    double s2 = __dmul_rn(sigma, sigma);
-    double r2inv = __dmul_rn(__ddiv_rn(1.0, rsq), s2);
-    double rs = __ddiv_rn(rsq, s2);
-    double r6inv = __dmul_rn(__dmul_rn(r2inv, r2inv), r2inv);
-    double t = __dmul_rn(__dmul_rn(p.v0, r6inv), r6inv);
-    t = __dadd_rn(t, p.c0);
+    const double s2 = __dmul_rn(sigma, sigma);
+    const double r2inv = __dmul_rn(__ddiv_rn(1.0, rsq), s2);
+    const double rs = __ddiv_rn(rsq, s2);
+    const double r6inv = __dmul_rn(__dmul_rn(r2inv, r2inv), r2inv);
+    double t;
+    switch (p.kind) {
+    case IKP_LJ:
+        return __ddiv_rn(ik_lj_fterm(p.v0, r2inv, r6inv), s2);
+    case IKP_FSLJ: {
+        t = ik_lj_fterm(p.v0, r2inv, r6inv);
+        const double c2inv = __ddiv_rn(1.0, p.rcutsq);
+        const double c6inv = __dmul_rn(__dmul_rn(c2inv, c2inv), c2inv);
+        return __ddiv_rn(__dsub_rn(t, ik_lj_fterm(p.v0, c2inv, c6inv)), s2);
+    }
+    case IKP_POLY10: {
+        const double r10 = __dmul_rn(__dmul_rn(r6inv, r2inv), r2inv);
+        t = __dmul_rn(__dmul_rn(__dmul_rn(10.0, p.v0), r2inv), r10);
+        t = __dsub_rn(t, __dmul_rn(2.0, p.c1));
+        t = __dsub_rn(t, __dmul_rn(__dmul_rn(4.0, p.c2), rs));
+        t = __dsub_rn(t, __dmul_rn(__dmul_rn(__dmul_rn(6.0, p.c3), rs), rs));
+        return __ddiv_rn(t, s2);
+    }
+    case IKP_POLY106: {
+        const double r10 = __dmul_rn(__dmul_rn(r6inv, r2inv), r2inv);
+        const double a = __dmul_rn(__dmul_rn(10.0, r10), r2inv);
+        const double b = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(6.0, r2inv), r2inv), r2inv), r2inv);
+        t = __dmul_rn(p.v0, __dsub_rn(a, b));
+        t = __dsub_rn(t, __dmul_rn(2.0, p.c1));
+        t = __dsub_rn(t, __dmul_rn(__dmul_rn(4.0, p.c2), rs));
+        return __ddiv_rn(t, s2);
+    }
+    case IKP_POLY18:
+        t = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(18.0, p.v0), r2inv), r6inv), r6inv), r6inv);
+        t = __dsub_rn(t, __dmul_rn(2.0, p.c1));
+        t = __dsub_rn(t, __dmul_rn(__dmul_rn(4.0, p.c2), rs));
+        return __ddiv_rn(t, s2);
+    case IKP_POLYLJ:
+        t = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(12.0, p.v0), r2inv), r6inv), r6inv);
+        t = __dsub_rn(t, __dmul_rn(__dmul_rn(__dmul_rn(6.0, p.v0), r2inv), r6inv));
+        t = __dsub_rn(t, __dmul_rn(2.0, p.c1));
+        t = __dsub_rn(t, __dmul_rn(__dmul_rn(4.0, p.c2), rs));
+        return __ddiv_rn(t, s2);
+    case IKP_POLYYUKAWA: {
+        const double rinv = __dsqrt_rn(r2inv), rroot = __dsqrt_rn(rs);
+        const double e = exp(__dmul_rn(-p.kappa, rroot));
+        t = __dmul_rn(__dmul_rn(__dmul_rn(e, __dadd_rn(rinv, p.kappa)), p.v0), r2inv);
+        t = __dsub_rn(t, __dmul_rn(2.0, p.c1));
+        t = __dsub_rn(t, __dmul_rn(__dmul_rn(4.0, p.c2), rs));
+        return __ddiv_rn(t, s2);
+    }
+    default: // IKP_POLY12
+        t = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(12.0, p.v0), r2inv), r6inv), r6inv);
+        t = __dsub_rn(t, __dmul_rn(2.0, p.c1));
+        t = __dsub_rn(t, __dmul_rn(__dmul_rn(4.0, p.c2), rs));
+        return __ddiv_rn(t, s2);
+    }
+}
+// computeEnergy; call with sigma = ik_sigma64(p, di, dj, false) and the cut-off test
+// rsq < rcutsq sigma^2 (no eps != 0 condition for the LJ energies).
+__device__ __forceinline__ double ik_energy64(const IkPot& p, double rsq, double sigma)
+{
+    const double s2 = __dmul_rn(sigma, sigma);
+    const double r2inv = __dmul_rn(__ddiv_rn(1.0, rsq), s2);
+    const double rs = __ddiv_rn(rsq, s2);
+    const double r6inv = __dmul_rn(__dmul_rn(r2inv, r2inv), r2inv);
+    double t;
+    switch (p.kind) {
+    case IKP_LJ:
+    case IKP_FSLJ: {
+        const double actual = __dmul_rn(__dmul_rn(p.rcutsq, sigma), sigma);
+        const double c2inv = __dmul_rn(__ddiv_rn(1.0, actual), s2);
+        const double c6inv = __dmul_rn(__dmul_rn(c2inv, c2inv), c2inv);
+        const double a = __dmul_rn(__dmul_rn(__dmul_rn(4.0, p.v0), r6inv), __dsub_rn(r6inv, 1.0));
+        const double b = __dmul_rn(__dmul_rn(__dmul_rn(4.0, p.v0), c6inv), __dsub_rn(c6inv, 1.0));
+        return __dsub_rn(a, b);
+    }
+    case IKP_POLY10: {
+        const double r10 = __dmul_rn(__dmul_rn(r6inv, r2inv), r2inv);
+        t = __dadd_rn(__dmul_rn(p.v0, r10), p.c0);
+        t = __dadd_rn(t, __dmul_rn(p.c1, rs));
+        t = __dadd_rn(t, __dmul_rn(__dmul_rn(p.c2, rs), rs));
+        return __dadd_rn(t, __dmul_rn(__dmul_rn(__dmul_rn(p.c3, rs), rs), rs));
+    }
+    case IKP_POLY106: {
+        const double r10 = __dmul_rn(__dmul_rn(r6inv, r2inv), r2inv);
+        t = __dadd_rn(__dmul_rn(p.v0, __dsub_rn(r10, r6inv)), p.c0);
+        break;
+    }
+    case IKP_POLY18:
+        t = __dadd_rn(__dmul_rn(__dmul_rn(__dmul_rn(p.v0, r6inv), r6inv), r6inv), p.c0);
+        break;
+    case IKP_POLYLJ:
+        t = __dsub_rn(__dmul_rn(__dmul_rn(p.v0, r6inv), r6inv), __dmul_rn(p.v0, r6inv));
+        t = __dadd_rn(t, p.c0);
+        break;
+    case IKP_POLYYUKAWA: {
+        const double rinv = __dsqrt_rn(r2inv), rroot = __dsqrt_rn(rs);
+        t = __dadd_rn(__dmul_rn(__dmul_rn(p.v0, exp(__dmul_rn(-rroot, p.kappa))), rinv), p.c0);
+        break;
+    }
+    default: // IKP_POLY12
+        t = __dadd_rn(__dmul_rn(__dmul_rn(p.v0, r6inv), r6inv), p.c0);
+        break;
+    }
     t = __dadd_rn(t, __dmul_rn(p.c1, rs));
-    t = __dadd_rn(t, __dmul_rn(__dmul_rn(p.c2, rs), rs));
-    return t;
+    return __dadd_rn(t, __dmul_rn(__dmul_rn(p.c2, rs), rs));
 }
 
 // Coarse-graining kernels in FP64 (CGFuncOctic.h:16-29, CGFuncRect.h,

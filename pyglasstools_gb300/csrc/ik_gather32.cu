@@ -1,697 +1,13 @@
-// ik_gather32.cu -- the tuned FP32 Irving-Kirkwood gather for sm_103a.
-//
-// Computes, for every grid point x_g,
-//   T(x_g) = sum_{i: |x_g - r_i| < R} sum_{j in bonds(i)} c_ij * int_0^1 Delta(x_g - r_i - s r_ij) ds
-//          + sum_{i: |x_g - r_i| < R} m_i v_i (x) v_i Delta(x_g - r_i)
-// i.e. the loop of IrvingKirkwood::compute (irvingkirkwood/IrvingKirkwood.h:74-110) with
-// VirialStress::compute_cg (ListofCommonObservables.h:72-82) and the intended
-// KineticStress (ListofCommonObservables.h:131-148), c_ij = 0.5 * forceDivR * r_ij (x) r_ij.
-//
-// Organisation (one warp = one worker, persistent, dynamic work queue):
-//   * a work item is a range of grid-point groups inside one spatial bin of bw^dim
-//     cells; the warp stages the bin's halo (particles of the cells within R) into its
-//     private shared memory as scaled, bin-relative FP32 positions;
-//   * a group is IK_P grid points; lanes test 32 staged particles at a time against
-//     the group (FP32, with an FP64 re-check inside a thin band around R so that the
-//     selection equals the FP64 rule), accumulate the kinetic term, and push
-//     (particle, bond, grid mask) slots of accepted particles into a per-warp queue;
-//     every full batch of 32 slots is processed with all lanes busy: per slot, the
-//     bond integral by symmetric Gauss-Legendre for each grid point of the group;
-//   * accumulation: every lane sums its slots of a group in FP32 (optionally with
-//     Kahan compensation); the 32 lane partials are combined with error-free
-//     transformations (TwoSum) in a transposing butterfly -- each shuffle level halves
-//     the values a lane holds -- and the compensated result is written as a
-//     double-float pair (hi, lo), converted to FP64 and scaled by k_pairs_to_f64;
-//   * surrogate mode (MLPM): a bond whose far end r_j lies outside the support
-//     becomes a record {M, m.h, |h|^2, B_fixed} + {grid point, bond} for the learned
-//     surrogate (ik_mlp.cu) instead of a term of the sum.
-// Bond records (CSR, 16 B): {hb = kappa r_ij / 2, f' = 2 forceDivR / kappa^2}; the
-// stress coefficient is f' hb (x) hb.
-#include "ik_kernels.h"
-
-#define FULL 0xffffffffu
-
-__device__ __forceinline__ float ik_ex2(float x)
-{
-    float y;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-__device__ __forceinline__ float ik_rcp(float x)
-{
-    float y;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-
-// Kernel value K(q) in scaled coordinates (normalisation applied on output).
-template <int KIND>
-__device__ __forceinline__ float ik_kern(float q, float R2s)
-{
-    if (KIND == 0) {            // octic: q = r^2/R^2, (1 - q^2)^2 inside (1 - q^2 <= 1: the
-                                // saturation only clips at 0)
-        float u = __saturatef(fmaf(-q, q, 1.0f));
-        return u * u;
-    } else if (KIND == 1) {     // gaussian: q = r^2 * log2(e)/(2 w^2), cut at q = R2s.  The
-                                // cut as a saturated FMA: (R2s - q) * 2^100 is >= 1 for every
-                                // float q < R2s (they differ by >= 1 ulp of R2s) and <= 0 else
-        const float inside = __saturatef(fmaf(-q, 0x1p100f, R2s * 0x1p100f));
-        return ik_ex2(-q) * inside;
-    } else if (KIND == 2) {     // rect
-        return q < 1.0f ? 1.0f : 0.0f;
-    } else {                    // mollifier: exp(-1/(1-q))
-        return q < 1.0f ? ik_ex2(-1.4426950408889634f * ik_rcp(1.0f - q)) : 0.0f;
-    }
-}
-// Kernel value of a particle already selected by the (FP64) support rule.
-template <int KIND>
-__device__ __forceinline__ float ik_kern_in(float q)
-{
-    if (KIND == 1) return ik_ex2(-q);
-    if (KIND == 0) { float u = fmaxf(fmaf(-q, q, 1.0f), 0.0f); return u * u; }
-    if (KIND == 2) return 1.0f;
-    return q < 1.0f ? ik_ex2(-1.4426950408889634f * ik_rcp(1.0f - q)) : 0.0f;
-}
-
-// TwoSum (Knuth): s + e == a + b exactly.
-__device__ __forceinline__ void ik_two_sum(float a, float b, float& s, float& e)
-{
-    s = a + b;
-    float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
-}
-
-__host__ __device__ constexpr int ik_pow2_ceil(int x) { int p = 1; while (p < x) p <<= 1; return p; }
-
-// Packed FP32 pairs (sm_100+ f32x2 arithmetic): two grid points evaluated per instruction.
-typedef unsigned long long f32x2;
-__device__ __forceinline__ f32x2 pk2(float a, float b)
-{
-    f32x2 r;
-    asm("mov.b64 %0, {%1,%2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-__device__ __forceinline__ void up2(f32x2 r, float& a, float& b)
-{
-    asm("mov.b64 {%0,%1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
-}
-__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b)
-{
-    f32x2 d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b)
-{
-    f32x2 d;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b)
-{
-    f32x2 d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c)
-{
-    f32x2 d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
-
-// Compensated transposing butterfly over a warp: on entry each lane holds V values
-// (hi[k], lo[k] = 0); after the call lane l holds, for k < max(V/32, 1), the warp sum
-// of value ik_red_index<V>(l, k) as hi[k] + lo[k] (hi + lo exact to ~2 ulp of the
-// sum, i.e. the accumulation of the 32 partials is compensated).
-template <int V>
-__device__ __forceinline__ void ik_warp_reduce_cmp(float (&hi)[V], float (&lo)[V], int lane)
-{
-#pragma unroll
-    for (int lev = 0; lev < 5; ++lev) {
-        const int o = 16 >> lev;
-        const int cur = (V >> lev) > 1 ? (V >> lev) : 1;
-        if (cur > 1) {
-            const int half = cur >> 1;
-            const bool up = (lane & o) != 0;
-#pragma unroll
-            for (int k = 0; k < V / 2; ++k) {
-                if (k < half) {
-                    float sh = up ? hi[k] : hi[k + half];
-                    float sl = up ? lo[k] : lo[k + half];
-                    float kh = up ? hi[k + half] : hi[k];
-                    float kl = up ? lo[k + half] : lo[k];
-                    float rh = __shfl_xor_sync(FULL, sh, o);
-                    float rl = __shfl_xor_sync(FULL, sl, o);
-                    float s, e;
-                    ik_two_sum(kh, rh, s, e);
-                    hi[k] = s;
-                    lo[k] = e + (kl + rl);
-                }
-            }
-        } else {
-            float rh = __shfl_xor_sync(FULL, hi[0], o);
-            float rl = __shfl_xor_sync(FULL, lo[0], o);
-            float s, e;
-            ik_two_sum(hi[0], rh, s, e);
-            hi[0] = s;
-            lo[0] = e + (lo[0] + rl);
-        }
-    }
-}
-template <int V>
-__device__ __forceinline__ int ik_red_index(int lane, int k)
-{
-    int idx = 0, cur = V;
-#pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) {
-        if (cur > 1) {
-            int half = cur >> 1;
-            if (lane & o) idx += half;
-            cur = half;
-        }
-    }
-    return idx + k;
-}
-
-// NP: number of symmetric Gauss-Legendre node pairs (compile-time when > 0; 0 = runtime).
-// MLPM: surrogate mode (bonds crossing the edge of the support become records).
-template <int DIM, int KIND, bool KAHAN, int NP, bool MLPM, bool ELA>
-__global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
-{
-    constexpr int NC = DIM == 2 ? 3 : 6;       // unique tensor components
-    constexpr int P = IK_P;
-
-    extern __shared__ float4 smem[];
-    __shared__ int s_next; // next item of this CTA's share
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    if (threadIdx.x == 0) s_next = 0;
-    __syncthreads();
-    // per warp: staged particles (float4 x,y,z, bits(bond offset << 6 | bond count)),
-    // their cell-order indices, and the slot queue
-    float4* stage = smem + (size_t)warp * (a.halo_cap + a.halo_cap / 4 + a.qcap / 4);
-    int* sq = reinterpret_cast<int*>(stage + a.halo_cap);
-    int* queue = sq + a.halo_cap;
-
-    const float R2s = a.R2s, margin = a.margin, kappa = a.kappa;
-    const bool want_kin = (a.fields & 2) != 0;
-    const int npairs = NP > 0 ? NP : a.npairs;
-    unsigned long long my_pairs = 0, my_triples = 0;
-    // surrogate records: this warp's current chunk [wfill, wend) of the record buffer
-    long long wfill = 0, wend = 0;
-    unsigned long long my_records = 0;
-    auto emit = [&](int cmask, const float4 (&crec)[IK_P], const int (&gidx)[IK_P], int bidx) {
-        const int cnt = __popc(cmask);
-        int incl = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int t = __shfl_up_sync(FULL, incl, o);
-            if (lane >= o) incl += t;
-        }
-        const int tot = __shfl_sync(FULL, incl, 31);
-        if (tot == 0) return;
-        if (wfill + tot > wend) {
-            for (long long k = wfill + lane; k < wend; k += 32) a.mlp_rid[k] = make_int2(-1, 0);
-            unsigned long long nb = 0;
-            if (lane == 0) nb = atomicAdd(a.mlp_count, (unsigned long long)IK_MLP_CHUNK);
-            nb = __shfl_sync(FULL, nb, 0);
-            if ((long long)nb + IK_MLP_CHUNK > a.mlp_cap) { // overflow: reported, replayed larger
-                if (lane == 0) atomicOr(a.status, IK_ST_MLP_OVERFLOW);
-                wfill = wend = 0;
-                return;
-            }
-            wfill = (long long)nb;
-            wend = wfill + IK_MLP_CHUNK;
-        }
-        long long o = wfill + incl - cnt;
-#pragma unroll
-        for (int p = 0; p < IK_P; ++p)
-            if (cmask & (1 << p)) {
-                a.mlp_rec[o] = crec[p];
-                a.mlp_rid[o] = make_int2(gidx[p], bidx);
-                ++o;
-            }
-        wfill += tot;
-        my_records += (unsigned long long)cnt;
-    };
-
-    for (;;) {
-        // work items: first this CTA's contiguous share (spatial neighbours, L1 reuse
-        // across its warps), then a global counter over the remaining tail
-        int w = 0;
-        if (lane == 0) {
-            const int per = (int)(((long long)a.nitems * 7 / 8) / gridDim.x);
-            const int k = atomicAdd(&s_next, 1);
-            w = k < per ? (int)blockIdx.x * per + k : per * (int)gridDim.x + atomicAdd(a.work_counter, 1);
-        }
-        w = __shfl_sync(FULL, w, 0);
-        if (w >= a.nitems) break;
-        const int4 it = a.items[w];
-        const int gend = a.items[w + 1].w;
-
-        // halo cell box (unwrapped cell coordinates)
-        int h0[3], hn[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            int cc = c == 0 ? it.x : (c == 1 ? it.y : it.z);
-            if (c >= DIM || a.g.nc[c] == 1) { h0[c] = 0; hn[c] = 1; }
-            else { h0[c] = cc - a.reach[c]; hn[c] = a.bw[c] + 2 * a.reach[c]; }
-        }
-        const int nh = hn[0] * hn[1] * hn[2];
-
-        int hc = 0;
-        bool first = true;
-        while (hc < nh) {
-            // ---- stage cells [hc, ...) until the warp's halo buffer is full
-            int nst = 0;
-            for (;;) {
-                int cid = hc + lane;
-                int cstart = 0, ccnt = 0;
-                float ox = 0.f, oy = 0.f, oz = 0.f;
-                if (cid < nh) {
-                    int ix = cid % hn[0], iy = (cid / hn[0]) % hn[1], iz = cid / (hn[0] * hn[1]);
-                    int ux = h0[0] + ix, uy = h0[1] + iy, uz = h0[2] + iz;
-                    int wx = ik_wrap(ux, a.g.nc[0]), wy = ik_wrap(uy, a.g.nc[1]);
-                    int wz = DIM == 3 ? ik_wrap(uz, a.g.nc[2]) : 0;
-                    int cell = (wz * a.g.nc[1] + wy) * a.g.nc[0] + wx;
-                    cstart = a.cell_start[cell];
-                    ccnt = a.cell_start[cell + 1] - cstart;
-                    ox = (ux - it.x) * a.cws[0];
-                    oy = (uy - it.y) * a.cws[1];
-                    oz = DIM == 3 ? (uz - it.z) * a.cws[2] : 0.f;
-                }
-                int incl = ccnt;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    int t = __shfl_up_sync(FULL, incl, o);
-                    if (lane >= o) incl += t;
-                }
-                unsigned fit = __ballot_sync(FULL, cid < nh && nst + incl <= a.halo_cap);
-                int k = __popc(fit & ~(fit + 1u)); // length of the run of ones from bit 0
-                if (k == 0) {
-                    if (nst == 0 && hc < nh) {
-                        // a single cell exceeds the halo buffer: report and skip it
-                        if (lane == 0) atomicOr(a.status, IK_ST_HALO_OVERFLOW);
-                        ++hc;
-                        continue;
-                    }
-                    break;
-                }
-                if (lane < k) {
-                    int dst = nst + incl - ccnt;
-                    for (int t = 0; t < ccnt; ++t) {
-                        int q = cstart + t;
-                        IkPRec r = a.prec[q];
-                        int b0, nbq;
-                        if (a.boff) { b0 = a.boff[q]; nbq = a.boff[q + 1] - b0; }
-                        else { b0 = q * a.maxb; nbq = a.nb[q]; }
-                        float4 s;
-                        s.x = fmaf(kappa, r.x, ox);
-                        s.y = fmaf(kappa, r.y, oy);
-                        s.z = DIM == 3 ? fmaf(kappa, r.z, oz) : 0.f;
-                        s.w = __int_as_float((b0 << 6) | nbq);
-                        stage[dst + t] = s;
-                        sq[dst + t] = q;
-                    }
-                }
-                nst += __shfl_sync(FULL, incl, k - 1);
-                hc += k;
-                if (k < 32 || hc >= nh) break;
-            }
-            __syncwarp();
-
-            // ---- process the item's groups against the staged particles
-            for (int gs = it.w; gs < gend; gs += P) {
-                // the group's grid points, packed in pairs (0,1), (2,3) for f32x2 arithmetic
-                f32x2 g2[P / 2][3];
-                int gi[P];
-#pragma unroll
-                for (int j = 0; j < P / 2; ++j) {
-                    float4 v0 = make_float4(1e18f, 1e18f, 1e18f, __int_as_float(-1)), v1 = v0;
-                    if (gs + 2 * j < gend) v0 = a.gpts[gs + 2 * j];
-                    if (gs + 2 * j + 1 < gend) v1 = a.gpts[gs + 2 * j + 1];
-                    g2[j][0] = pk2(v0.x, v1.x);
-                    g2[j][1] = pk2(v0.y, v1.y);
-                    g2[j][2] = pk2(v0.z, v1.z);
-                    gi[2 * j] = __float_as_int(v0.w);
-                    gi[2 * j + 1] = __float_as_int(v1.w);
-                }
-                float acc[P][NC], cmp[P][NC], kac[P][NC];
-#pragma unroll
-                for (int p = 0; p < P; ++p)
-#pragma unroll
-                    for (int c = 0; c < NC; ++c) { acc[p][c] = 0.f; cmp[p][c] = 0.f; kac[p][c] = 0.f; }
-
-                f32x2 acc2[P / 2][NC];
-#pragma unroll
-                for (int j = 0; j < P / 2; ++j)
-#pragma unroll
-                    for (int c = 0; c < NC; ++c) acc2[j][c] = 0ull;
-
-                // one slot: staged particle s, its bond k, grid mask m.  The loads are
-                // separate so that two batches can be in flight before either computes.
-                auto load_slot = [&](int e, float4& sp, float4& b) {
-                    sp = stage[e >> 10];
-                    b = __ldg(a.bonds + (__float_as_int(sp.w) >> 6) + ((e >> 4) & 63));
-                };
-                auto process_slot = [&](int e, const float4& sp, const float4& b) {
-                    const int m = e & 15;
-                    const float hbx = b.x, hby = b.y, hbz = b.z;
-                    const float hh = DIM == 3 ? fmaf(hbz, hbz, fmaf(hby, hby, hbx * hbx)) : fmaf(hby, hby, hbx * hbx);
-                    float cf[NC];
-                    if constexpr (ELA) { // elastic field: the bond's own coefficient
-                        const int bi = (__float_as_int(sp.w) >> 6) + ((e >> 4) & 63);
-                        const float4 c0 = __ldg(a.bcoef + (size_t)bi * (DIM == 2 ? 1 : 2));
-                        cf[0] = c0.x;
-                        cf[1] = c0.y;
-                        cf[2] = c0.z;
-                        if (DIM == 3) {
-                            const float4 c1 = __ldg(a.bcoef + (size_t)bi * 2 + 1);
-                            cf[3 % NC] = c0.w;
-                            cf[4 % NC] = c1.x;
-                            cf[5 % NC] = c1.y;
-                        }
-                    } else {
-                        const float fx = b.w * hbx, fy = b.w * hby;
-                        cf[0] = fx * hbx;
-                        cf[1] = fy * hby;
-                        if (DIM == 2) {
-                            cf[2] = fx * hby;
-                        } else {
-                            const float fz = b.w * hbz;
-                            cf[2] = fz * hbz;
-                            cf[3 % NC] = fx * hby;
-                            cf[4 % NC] = fx * hbz;
-                            cf[5 % NC] = fy * hbz;
-                        }
-                    }
-                    const float mx0 = sp.x + hbx, my0 = sp.y + hby, mz0 = sp.z + hbz; // bond midpoint
-                    float4 crec[P];
-                    int cmask = 0;
-                    if constexpr (!KAHAN && NP > 0) {
-                        // packed path: two grid points per f32x2 instruction
-                        const f32x2 mid2x = pk2(mx0, mx0), mid2y = pk2(my0, my0), mid2z = pk2(mz0, mz0);
-                        const f32x2 hb2x = pk2(hbx, hbx), hb2y = pk2(hby, hby), hb2z = pk2(hbz, hbz);
-                        f32x2 cq2[NP], cf2[NC];
-#pragma unroll
-                        for (int t = 0; t < NP; ++t) { const float v = a.xi2[t] * hh; cq2[t] = pk2(v, v); }
-#pragma unroll
-                        for (int c = 0; c < NC; ++c) cf2[c] = pk2(cf[c], cf[c]);
-#pragma unroll
-                        for (int j = 0; j < P / 2; ++j) {
-                            const f32x2 mx = sub2(g2[j][0], mid2x), my = sub2(g2[j][1], mid2y);
-                            f32x2 M = fma2(my, my, mul2(mx, mx));
-                            f32x2 mb = fma2(my, hb2y, mul2(mx, hb2x));
-                            if (DIM == 3) {
-                                const f32x2 mz = sub2(g2[j][2], mid2z);
-                                M = fma2(mz, mz, M);
-                                mb = fma2(mz, hb2z, mb);
-                            }
-                            float Ma, Mb;
-                            up2(M, Ma, Mb);
-                            // node values per grid point in scalar form (no packing moves)
-                            float Ba = a.w0 * ik_kern<KIND>(Ma, R2s), Bb = a.w0 * ik_kern<KIND>(Mb, R2s);
-#pragma unroll
-                            for (int t = 0; t < NP; ++t) {
-                                const f32x2 base = add2(M, cq2[t]);
-                                const f32x2 rp = fma2(pk2(a.m2xi[t], a.m2xi[t]), mb, base);
-                                const f32x2 rm = fma2(pk2(-a.m2xi[t], -a.m2xi[t]), mb, base);
-                                float pa, pb, qa, qb;
-                                up2(rp, pa, pb);
-                                up2(rm, qa, qb);
-                                Ba = fmaf(a.w[t], ik_kern<KIND>(pa, R2s) + ik_kern<KIND>(qa, R2s), Ba);
-                                Bb = fmaf(a.w[t], ik_kern<KIND>(pb, R2s) + ik_kern<KIND>(qb, R2s), Bb);
-                            }
-                            f32x2 B;
-                            if constexpr (MLPM) { // r_j outside the support: a record, not a term
-                                const f32x2 rj2 = fma2(pk2(-2.f, -2.f), mb, add2(M, pk2(hh, hh)));
-                                float ra, rb, mba, mbb;
-                                up2(rj2, ra, rb);
-                                up2(mb, mba, mbb);
-                                if ((m & (1 << (2 * j))) && ra >= R2s) {
-                                    crec[2 * j] = make_float4(Ma, mba, hh, Ba);
-                                    cmask |= 1 << (2 * j);
-                                    Ba = 0.f;
-                                }
-                                if ((m & (2 << (2 * j))) && rb >= R2s) {
-                                    crec[2 * j + 1] = make_float4(Mb, mbb, hh, Bb);
-                                    cmask |= 2 << (2 * j);
-                                    Bb = 0.f;
-                                }
-                            }
-                            B = pk2((m & (1 << (2 * j))) ? Ba : 0.f, (m & (2 << (2 * j))) ? Bb : 0.f);
-#pragma unroll
-                            for (int c = 0; c < NC; ++c) acc2[j][c] = fma2(B, cf2[c], acc2[j][c]);
-                        }
-                    } else {
-                        float cq[NP > 0 ? NP : 1];
-                        if constexpr (NP > 0) {
-#pragma unroll
-                            for (int t = 0; t < NP; ++t) cq[t] = a.xi2[t] * hh;
-                        }
-#pragma unroll
-                        for (int p = 0; p < P; ++p) {
-                            float gx, gy, gz, t0, t1, t2;
-                            up2(g2[p >> 1][0], t0, t1);
-                            gx = (p & 1) ? t1 : t0;
-                            up2(g2[p >> 1][1], t0, t1);
-                            gy = (p & 1) ? t1 : t0;
-                            up2(g2[p >> 1][2], t0, t2);
-                            gz = (p & 1) ? t2 : t0;
-                            const float mx = gx - mx0, my = gy - my0;
-                            float M = mx * mx, mb = mx * hbx;
-                            M = fmaf(my, my, M);
-                            mb = fmaf(my, hby, mb);
-                            if (DIM == 3) {
-                                const float mz = gz - mz0;
-                                M = fmaf(mz, mz, M);
-                                mb = fmaf(mz, hbz, mb);
-                            }
-                            // r^2(xi) = M - 2 xi mb + xi^2 hh at the symmetric nodes +-xi
-                            float B = a.w0 * ik_kern<KIND>(M, R2s);
-                            if constexpr (NP > 0) {
-#pragma unroll
-                                for (int t = 0; t < NP; ++t) {
-                                    const float base = M + cq[t];
-                                    const float kp = ik_kern<KIND>(fmaf(a.m2xi[t], mb, base), R2s);
-                                    const float km = ik_kern<KIND>(fmaf(-a.m2xi[t], mb, base), R2s);
-                                    B = fmaf(a.w[t], kp + km, B);
-                                }
-                            } else {
-#pragma unroll 1
-                                for (int t = 0; t < npairs; ++t) {
-                                    const float base = fmaf(a.xi2[t], hh, M);
-                                    const float kp = ik_kern<KIND>(fmaf(a.m2xi[t], mb, base), R2s);
-                                    const float km = ik_kern<KIND>(fmaf(-a.m2xi[t], mb, base), R2s);
-                                    B = fmaf(a.w[t], kp + km, B);
-                                }
-                            }
-                            B = (m & (1 << p)) ? B : 0.f;
-                            if constexpr (MLPM) {
-                                if ((m & (1 << p)) && fmaf(-2.f, mb, M + hh) >= R2s) {
-                                    crec[p] = make_float4(M, mb, hh, B);
-                                    cmask |= 1 << p;
-                                    B = 0.f;
-                                }
-                            }
-#pragma unroll
-                            for (int c = 0; c < NC; ++c) {
-                                if (KAHAN) {
-                                    const float y = fmaf(B, cf[c], -cmp[p][c]);
-                                    const float t2 = acc[p][c] + y;
-                                    cmp[p][c] = (t2 - acc[p][c]) - y;
-                                    acc[p][c] = t2;
-                                } else {
-                                    acc[p][c] = fmaf(B, cf[c], acc[p][c]);
-                                }
-                            }
-                        }
-                    }
-                    my_triples += __popc(m);
-                    if constexpr (MLPM) emit(cmask, crec, gi, (__float_as_int(sp.w) >> 6) + ((e >> 4) & 63));
-                };
-
-                int qn = 0;
-                for (int base = 0; base < nst; base += 32) {
-                    const int s = base + lane;
-                    int mask = 0, cnt = 0;
-                    if (s < nst) {
-                        const float4 sp = stage[s];
-                        float4 k0 = make_float4(0.f, 0.f, 0.f, 0.f), k1 = k0;
-                        if (want_kin) { // issued before the tests so the latency overlaps them
-                            const int q = sq[s];
-                            k0 = __ldg(a.kin + (DIM == 2 ? q : 2 * q));
-                            if (DIM == 3) k1 = __ldg(a.kin + 2 * q + 1);
-                        }
-                        float r2v[P];
-                        {
-                            const f32x2 sx = pk2(sp.x, sp.x), sy = pk2(sp.y, sp.y), sz = pk2(sp.z, sp.z);
-#pragma unroll
-                            for (int j = 0; j < P / 2; ++j) {
-                                const f32x2 dx = sub2(g2[j][0], sx), dy = sub2(g2[j][1], sy);
-                                f32x2 r2 = fma2(dy, dy, mul2(dx, dx));
-                                if (DIM == 3) { const f32x2 dz = sub2(g2[j][2], sz); r2 = fma2(dz, dz, r2); }
-                                up2(r2, r2v[2 * j], r2v[2 * j + 1]);
-                            }
-                        }
-                        int band = 0;
-#pragma unroll
-                        for (int p = 0; p < P; ++p) {
-                            const float r2 = r2v[p];
-                            mask |= (r2 < R2s ? 1 : 0) << p;
-                            band |= (fabsf(r2 - R2s) < margin && gi[p] >= 0 ? 1 : 0) << p;
-                        }
-                        if (band) { // rare: inside the thin band around R decide with the FP64 rule
-                            const IkB64 pq = a.pos64[sq[s]];
-#pragma unroll
-                            for (int p = 0; p < P; ++p) {
-                                if (!(band & (1 << p))) continue;
-                                const double* xg = a.grid + 3 * (size_t)gi[p];
-                                const double ddx = ik_minimg(__dsub_rn(xg[0], pq.x), a.g.L[0], a.g.periodic[0]);
-                                const double ddy = ik_minimg(__dsub_rn(xg[1], pq.y), a.g.L[1], a.g.periodic[1]);
-                                const double ddz = ik_minimg(__dsub_rn(xg[2], pq.z), a.g.L[2], a.g.periodic[2]);
-                                mask = ik_dot3(ddx, ddy, ddz) < a.R2 ? (mask | (1 << p)) : (mask & ~(1 << p));
-                            }
-                        }
-                        if (mask) {
-                            cnt = __float_as_int(sp.w) & 63;
-                            if (want_kin) {
-#pragma unroll
-                                for (int p = 0; p < P; ++p) {
-                                    const float kv = (mask & (1 << p)) ? ik_kern_in<KIND>(r2v[p]) : 0.f;
-                                    kac[p][0] = fmaf(kv, k0.x, kac[p][0]);
-                                    kac[p][1] = fmaf(kv, k0.y, kac[p][1]);
-                                    kac[p][2] = fmaf(kv, k0.z, kac[p][2]);
-                                    if (DIM == 3) {
-                                        kac[p][3 % NC] = fmaf(kv, k0.w, kac[p][3 % NC]);
-                                        kac[p][4 % NC] = fmaf(kv, k1.x, kac[p][4 % NC]);
-                                        kac[p][5 % NC] = fmaf(kv, k1.y, kac[p][5 % NC]);
-                                    }
-                                }
-                            }
-                            my_pairs += __popc(mask);
-                        }
-                    }
-                    int incl = cnt;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        int t = __shfl_up_sync(FULL, incl, o);
-                        if (lane >= o) incl += t;
-                    }
-                    const int tot = __shfl_sync(FULL, incl, 31);
-                    const int off = qn + incl - cnt;
-                    const int entry = (s << 10) | mask;
-                    for (int k = 0; k < cnt; ++k) queue[off + k] = entry | (k << 4);
-                    qn += tot;
-                    __syncwarp();
-                    while (qn >= 64) { // two batches in flight
-                        const int e1 = queue[qn - 32 + lane], e2 = queue[qn - 64 + lane];
-                        qn -= 64;
-                        float4 sp1, b1, sp2, b2;
-                        load_slot(e1, sp1, b1);
-                        load_slot(e2, sp2, b2);
-                        process_slot(e1, sp1, b1);
-                        process_slot(e2, sp2, b2);
-                    }
-                    if (qn >= 32) {
-                        qn -= 32;
-                        const int e1 = queue[qn + lane];
-                        float4 sp1, b1;
-                        load_slot(e1, sp1, b1);
-                        process_slot(e1, sp1, b1);
-                    }
-                    __syncwarp();
-                }
-                if (MLPM ? qn > 0 : lane < qn) { // surrogate mode: all lanes (emission is warp-wide)
-                    const int e1 = lane < qn ? queue[lane] : (queue[0] & ~15); // mask 0 on idle lanes
-                    float4 sp1, b1;
-                    load_slot(e1, sp1, b1);
-                    process_slot(e1, sp1, b1);
-                }
-                __syncwarp();
-
-                // ---- combine lanes (compensated): virial, then kinetic, each a
-                //      transposing butterfly of VH values; results are written as
-                //      unscaled double-float pairs (hi, lo), converted to FP64 later
-                if constexpr (!KAHAN && NP > 0) {
-#pragma unroll
-                    for (int j = 0; j < P / 2; ++j)
-#pragma unroll
-                        for (int c = 0; c < NC; ++c) up2(acc2[j][c], acc[2 * j][c], acc[2 * j + 1][c]);
-                }
-                constexpr int VH = ik_pow2_ceil(P * NC);
-                static_assert(VH == 16 || VH == 32, "butterfly width");
-                float vh[VH], vl[VH], kh[VH], kl[VH];
-#pragma unroll
-                for (int p = 0; p < P; ++p)
-#pragma unroll
-                    for (int c = 0; c < NC; ++c) {
-                        vh[p * NC + c] = acc[p][c];
-                        vl[p * NC + c] = KAHAN ? -cmp[p][c] : 0.f;
-                        kh[p * NC + c] = kac[p][c];
-                        kl[p * NC + c] = 0.f;
-                    }
-#pragma unroll
-                for (int k = P * NC; k < VH; ++k) { vh[k] = vl[k] = kh[k] = kl[k] = 0.f; }
-                ik_warp_reduce_cmp<VH>(vh, vl, lane);
-                ik_warp_reduce_cmp<VH>(kh, kl, lane);
-                // VH == 16: lanes 2k and 2k+1 both hold value k -> the even lane writes
-                // the virial, the odd lane the kinetic value; VH == 32: one value per lane
-#pragma unroll
-                for (int f = 0; f < (VH == 16 ? 1 : 2); ++f) {
-                    const bool kin_here = VH == 16 ? (lane & 1) != 0 : f == 1;
-                    const int idx = ik_red_index<VH>(lane, 0);
-                    const float h = kin_here ? kh[0] : vh[0], l = kin_here ? kl[0] : vl[0];
-                    const bool want = kin_here ? want_kin : (a.fields & 1);
-                    if (idx < P * NC && want) {
-                        const int p = idx / NC, c = idx - p * NC;
-                        int g = -1;
-#pragma unroll
-                        for (int pp = 0; pp < P; ++pp) if (pp == p) g = gi[pp];
-                        if (g >= 0) {
-                            float2* out = kin_here ? a.out_kin : a.out_vir;
-                            const size_t o = (size_t)g * NC + c;
-                            if (first) {
-                                out[o] = make_float2(h, l);
-                            } else { // another chunk of the same item: compensated add
-                                const float2 old = out[o];
-                                float s2, e2;
-                                ik_two_sum(old.x, h, s2, e2);
-                                out[o] = make_float2(s2, e2 + (old.y + l));
-                            }
-                        }
-                    }
-                }
-            }
-            first = false;
-            __syncwarp();
-        }
-    }
-    if constexpr (MLPM)
-        for (long long k = wfill + lane; k < wend; k += 32) a.mlp_rid[k] = make_int2(-1, 0);
-    // counters
-    for (int o = 16; o; o >>= 1) {
-        my_pairs += __shfl_xor_sync(FULL, my_pairs, o);
-        my_triples += __shfl_xor_sync(FULL, my_triples, o);
-    }
-    if constexpr (MLPM)
-        for (int o = 16; o; o >>= 1) my_records += __shfl_xor_sync(FULL, my_records, o);
-    if (lane == 0) {
-        atomicAdd(a.cnt_pairs, my_pairs);
-        atomicAdd(a.cnt_triples, my_triples);
-        if (MLPM) atomicAdd(a.cnt_records, my_records);
-    }
-}
-
-template <int DIM, int KIND, bool KAHAN, int NP, bool MLPM = false, bool ELA = false>
+// ik_gather32.cu -- launchers of the tuned FP32 gather (k_gather32, in
+// ik_gather32_kernel.cuh) for frames with at most 63 bonds per particle, and the FP64
+// conversion of its double-float results.  The elastic-field variants and the
+// variants for more bonds per particle are instantiated in ik_gather32_aux.cu (a
+// second translation unit, compiled in parallel).
+#include "ik_gather32_kernel.cuh"
+template <int DIM, int KIND, bool KAHAN, int NP, bool MLPM = false>
 static cudaError_t launch_one(const GatherArgs32& a, int blocks, int threads, size_t smem, cudaStream_t st)
 {
-    auto kfn = k_gather32<DIM, KIND, KAHAN, NP, MLPM, ELA>;
-    cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    kfn<<<blocks, threads, smem, st>>>(a);
-    return cudaGetLastError();
+    return ik_launch_gather32_kernel<DIM, KIND, KAHAN, NP, MLPM, false, false>(a, blocks, threads, smem, st);
 }
 
 template <int DIM, bool KAHAN, int NP>
@@ -713,27 +29,10 @@ static cudaError_t launch_np(const GatherArgs32& a, int kind, int blocks, int th
     return launch_kind<DIM, KAHAN, 0>(a, kind, blocks, threads, smem, st);
 }
 
-template <int DIM, int NP>
-static cudaError_t launch_ela(const GatherArgs32& a, int kind, int blocks, int threads, size_t smem, cudaStream_t st)
-{
-    switch (kind) {
-    case 0: return launch_one<DIM, 0, false, NP, false, true>(a, blocks, threads, smem, st);
-    case 1: return launch_one<DIM, 1, false, NP, false, true>(a, blocks, threads, smem, st);
-    case 2: return launch_one<DIM, 2, false, NP, false, true>(a, blocks, threads, smem, st);
-    default: return launch_one<DIM, 3, false, NP, false, true>(a, blocks, threads, smem, st);
-    }
-}
-
 cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, bool mlp, int blocks, int threads,
                             size_t smem, cudaStream_t st)
 {
-    if (a.bcoef) { // elastic field: plain per-lane sums, no surrogate
-        if (mlp) return cudaErrorInvalidValue;
-        if (a.g.dim == 2) return a.npairs == 2 ? launch_ela<2, 2>(a, kind, blocks, threads, smem, st)
-                                               : launch_ela<2, 0>(a, kind, blocks, threads, smem, st);
-        return a.npairs == 2 ? launch_ela<3, 2>(a, kind, blocks, threads, smem, st)
-                             : launch_ela<3, 0>(a, kind, blocks, threads, smem, st);
-    }
+    if (a.bcoef || a.maxb > 63) return launch_gather32_aux(a, kind, kahan, mlp, blocks, threads, smem, st);
     if (mlp) { // Gaussian kernel only, plain per-lane sums
         if (kind != 1 || kahan) return cudaErrorInvalidValue;
         if (a.g.dim == 2) return a.npairs == 2 ? launch_one<2, 1, false, 2, true>(a, blocks, threads, smem, st)

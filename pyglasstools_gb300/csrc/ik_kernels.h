@@ -23,7 +23,7 @@ cudaError_t launch_sort_pack32(IkGeom g, const int* cell_start, int* sorted, con
                                const double* pos, const double* vel, const double* mass, const double* diam,
                                IkPRec* prec, float4* plo, IkB64* pos64, float4* kin, float* diam32, cudaStream_t st);
 // nbond_total (may be null): += force-active directed bonds
-cudaError_t launch_bonds32(int dim, IkGeom g, IkPoly12 pot, float kappa, int n, const IkPRec* prec,
+cudaError_t launch_bonds32(int dim, IkGeom g, IkPot pot, float kappa, int n, const IkPRec* prec,
                             const float* diam32, const int* cell_start, const float4* plo, const IkB64* pos64,
                             float4* tmp, int maxb, int* nb, int* status, int* maxnb,
                             unsigned long long* nbond_total, cudaStream_t st);
@@ -31,10 +31,10 @@ cudaError_t launch_bond_compact(int n, int maxb, const int* nb, const int* boff,
                                 unsigned long long* nbond_total, cudaStream_t st);
 // exclusive scan of n ints into out[0..n]; bsum needs ceil(n / 4096) ints
 cudaError_t launch_scan(const int* in, int n, int* out, int* bsum, cudaStream_t st);
-__global__ void k_bonds64(IkGeom g, IkPoly12 pot, int n, const int* sorted, const int* cell_of,
+__global__ void k_bonds64(IkGeom g, IkPot pot, int n, const int* sorted, const int* cell_of,
                           const double* pos, const double* diam, const int* cell_start, IkB64* bonds,
                           int maxb, int* nb, int* status, int* maxnb);
-__global__ void k_bonds64e(IkGeom g, IkPoly12 pot, float kappa, int n, const int* sorted, const int* cell_of,
+__global__ void k_bonds64e(IkGeom g, IkPot pot, float kappa, int n, const int* sorted, const int* cell_of,
                            const double* pos, const double* disp, const double* diam, const int* cell_start,
                            IkB64* b64, double* c64, float4* b32, float4* c32, int maxb, int* nb, int* status,
                            int* maxnb);
@@ -44,7 +44,7 @@ cudaError_t launch_neigh(bool fill, IkGeom g, int n, double r2cut, const int* so
 __global__ void k_point_query(IkGeom g, int n, const double* pos, double px, double py, double pz,
                               double r2cut, unsigned char* flag);
 __global__ void k_validate(const double* pos, const double* diam, int n, int dim, int* status);
-__global__ void k_eval_pair(IkPoly12 pot, int m, const double* rij, const double* di, const double* dj,
+__global__ void k_eval_pair(IkPot pot, int m, const double* rij, const double* di, const double* dj,
                             double* f, double* en);
 
 // ---- FP32 tuned gather (ik_gather32.cu) ------------------------------------
@@ -93,8 +93,12 @@ struct GatherArgs32 {
     unsigned long long* cnt_records;
 };
 #define IK_MLP_CHUNK 2048
+// a.bcoef != null: elastic coefficients.  launch_gather32 passes the elastic field and
+// maxb > 63 on to launch_gather32_aux (variants in the second translation unit).
 cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, bool mlp, int blocks, int threads,
-                            size_t smem, cudaStream_t st);  // a.bcoef != null: elastic coefficients
+                            size_t smem, cudaStream_t st);
+cudaError_t launch_gather32_aux(const GatherArgs32& a, int kind, bool kahan, bool mlp, int blocks, int threads,
+                                size_t smem, cudaStream_t st);
 // vir = ((double)hi + (double)lo + corr * 2^-32) * svir   (corr: fixed point, may be null),
 // kin = ((double)hi + (double)lo) * skin; a null output is skipped.  One launch.
 cudaError_t launch_pairs_to_f64(const float2* vin, const unsigned long long* corr, double* vout, double svir,

@@ -153,7 +153,7 @@ extern "C" int ik_compute_fp64_noalloc(int dim, const double boxsize[3], const d
     }
     geo.ncell = geo.nc[0] * geo.nc[1] * geo.nc[2];
 
-    IkPoly12 pot{};
+    IkPot pot{};
     pot.rcutsq = scaled_rcut * scaled_rcut;
     pot.v0 = params[0]; pot.eps = params[1]; pot.c0 = params[2]; pot.c1 = params[3]; pot.c2 = params[4];
     pot.max_rcut_sq = max_rcut * max_rcut;

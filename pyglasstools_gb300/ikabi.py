@@ -23,6 +23,8 @@ PREC = {"fp64": 0, "fp32": 1}
 FIELD_VIRIAL, FIELD_KINETIC, FIELD_ELASTIC = 1, 2, 4
 FLAG_TIMING, FLAG_LANE_KAHAN, FLAG_CSR_BONDS = 1, 2, 4
 TUNE = {"bin_points": 1, "blocks_per_sm": 2, "halo_cap": 3}
+POT = {"poly12": 0, "lj": 1, "fslj": 2, "poly10": 3, "poly106": 4, "poly18": 5, "polylj": 6,
+       "polyyukawa": 7}
 
 _lib = None
 
@@ -48,6 +50,8 @@ def lib():
             "ik_destroy": ([vp], i32),
             "ik_set_box": ([vp, i32, dp, dp], i32),
             "ik_set_potential_poly12": ([vp, C.c_double, dp], i32),
+            "ik_set_potential": ([vp, i32, C.c_double, dp, i32], i32),
+            "ik_potential_nparams": ([i32], i32),
             "ik_set_cgfunc": ([vp, i32, i32, i32, C.c_double, C.c_double], i32),
             "ik_set_adaptive": ([vp, i32, C.c_double, C.c_double], i32),
             "ik_set_max_rcut": ([vp, C.c_double], i32),
@@ -160,6 +164,12 @@ class IKContext:
     def set_poly12(self, v0=1.0, eps=0.2, rcut=1.25):
         p = np.array([v0, eps, -28.0 * v0 / rcut ** 12, 48.0 * v0 / rcut ** 14, -21.0 * v0 / rcut ** 16])
         check(lib().ik_set_potential_poly12(self._h, rcut, _dp(p)))
+
+    def set_potential(self, kind, rcut, params):
+        """Any of the eight pair models (POT), params in the reference's order."""
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        check(lib().ik_set_potential(self._h, POT[kind] if isinstance(kind, str) else int(kind), rcut,
+                                     _dp(p), len(p)))
 
     def set_cgfunc(self, kind, rcut, mode="fixedpoint", order=5, width=0.0):
         check(lib().ik_set_cgfunc(self._h, CG[kind], QUAD[mode], order, rcut, width))

@@ -13,6 +13,10 @@ Outputs
   ref_kernels.npz      Polydisperse12 force/energy/stiffness and Octic/Rect/Mollifier
                        values produced by the REFERENCE'S OWN headers compiled by
                        oracle/build_ref.sh, on seeded random inputs.
+  ref_potentials.npz   force and energy of all eight pair models (LJ, force-shifted LJ,
+                       Poly10/106/12/18, PolyLJ, PolyYukawa) from the reference's own
+                       headers, on seeded inputs that include overlaps and pairs
+                       within 1e-12 of the cut-off.
   oracle_fixture180.npz  the oracle's virial field (xx, yy, xy per grid point) on frame 180 with the example
                        script's settings (octic R = 2, Gauss-Legendre 5, dx = 0.25).
   oracle_cfg0.npz      the oracle's virial + kinetic fields on a seeded synthetic
@@ -72,6 +76,41 @@ def ref_kernels():
                         stiffness=s, rc=rc, dr=dr, octic=octic, rect=rect, mollifier=moll)
 
 
+# models and constructor keywords of the pinned cases (non-default non-additivity)
+POT_CASES = [("poly12", {}), ("lj", {"eps": 1.0, "vareps": 0.1, "rcut": 2.5}),
+             ("fslj", {"eps": 1.0, "vareps": 0.1, "rcut": 2.5}), ("poly10", {}), ("poly106", {}),
+             ("poly18", {"eps": 0.1}), ("polylj", {}), ("polyyukawa", {"eps": 0.05, "kappa": 1.5})]
+
+
+def ref_potentials():
+    R = O.ref_lib()
+    assert R is not None, "oracle/_ref/libref_kernels.so was not built"
+    rng = np.random.default_rng(4321)
+    out = {}
+    m = 600
+    for kind, kw in POT_CASES:
+        rc, prm = O.potential_params(kind, **kw)
+        di = rng.uniform(0.7, 1.7, m)
+        dj = rng.uniform(0.7, 1.7, m)
+        eps = prm[2] if kind == "polyyukawa" else prm[1]
+        sig = 0.5 * (di + dj) * (1 - eps * np.abs(di - dj))
+        cut = rc * rc * sig * sig
+        u = rng.uniform(0.02, 1.3, m)
+        rsq = u * cut
+        k = m // 10  # pairs at the cut-off: exact, and within a few ulp either side
+        rsq[:k] = cut[:k] * (1.0 + rng.integers(-3, 4, k) * 2.0 ** -52)
+        arr = (C.c_double * len(prm))(*prm)
+        K = O.POT_KIND[kind]
+        out[f"{kind}_rc"] = np.float64(rc)
+        out[f"{kind}_params"] = np.asarray(prm, np.float64)
+        out[f"{kind}_rsq"], out[f"{kind}_di"], out[f"{kind}_dj"] = rsq, di, dj
+        out[f"{kind}_force"] = np.array([R.ref_pot_force_divr(K, a, rc, arr, len(prm), b, c)
+                                         for a, b, c in zip(rsq, di, dj)])
+        out[f"{kind}_energy"] = np.array([R.ref_pot_energy(K, a, rc, arr, len(prm), b, c)
+                                          for a, b, c in zip(rsq, di, dj)])
+    np.savez_compressed(os.path.join(HERE, "ref_potentials.npz"), **out)
+
+
 def oracle_fixture(fr):
     pos = fr["pos180"].astype(np.float64)
     diam = fr["diam180"].astype(np.float64)
@@ -105,6 +144,7 @@ if __name__ == "__main__":
     O.build()
     fr = frames()
     ref_kernels()
+    ref_potentials()
     oracle_fixture(fr)
     oracle_cfg0()
     for fn in sorted(os.listdir(HERE)):

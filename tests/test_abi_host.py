@@ -50,7 +50,9 @@ def test_pybind_modules_import_and_mirror_reference_names():
     from pyglasstools_gb300 import _core
     for mod, names in {
         "_pyglasstools": ["SimBox", "ParticleSystem", "Communicator", "MPILogFile", "Manager"],
-        "_potential": ["PairPotential", "PairPotentialPoly12"],
+        "_potential": ["PairPotential", "PairPotentialLJ", "PairPotentialForceShiftedLJ", "PairPotentialPoly12",
+                       "PairPotentialPoly18", "PairPotentialPoly10", "PairPotentialPoly106",
+                       "PairPotentialPolyYukawa", "PairPotentialPolyLJ"],
         "_cgfunc": ["CoarseGrainFunction", "CGFuncOcticFixedPoint", "CGFuncOcticAdaptive", "CGFuncRectFixedPoint",
                     "CGFuncRectAdaptive", "CGFuncMollifierFixedPoint", "CGFuncMollifierAdaptive",
                     "CGFuncGaussianFixedPoint"],

@@ -43,6 +43,37 @@ def test_force_matches_reference_header_golden(oracle, golden):
     assert np.count_nonzero(f) > 100 and np.count_nonzero(f == 0) > 100  # both branches exercised
 
 
+POT_KINDS = ["poly12", "lj", "fslj", "poly10", "poly106", "poly18", "polylj", "polyyukawa"]
+
+
+@pytest.mark.parametrize("kind", POT_KINDS)
+def test_pair_models_match_reference_headers_golden(oracle, golden, kind):
+    """Force and energy of each of the eight models: bit-identical to the reference's
+    own header (potential/*.h compiled by oracle/build_ref.sh; tests/golden/make_golden.py),
+    including pairs within a few ulp of the cut-off and strongly overlapping pairs."""
+    g = golden("ref_potentials.npz")
+    pot = oracle.make_potential(kind, float(g[f"{kind}_rc"]), g[f"{kind}_params"])
+    rsq, di, dj = g[f"{kind}_rsq"], g[f"{kind}_di"], g[f"{kind}_dj"]
+    f = np.array([oracle.force_divr(pot, a, b, c) for a, b, c in zip(rsq, di, dj)])
+    e = np.array([oracle.pair_energy(pot, a, b, c) for a, b, c in zip(rsq, di, dj)])
+    assert np.array_equal(f, g[f"{kind}_force"])
+    assert np.array_equal(e, g[f"{kind}_energy"])
+    assert np.count_nonzero(f) > 100 and np.count_nonzero(f == 0) > 50
+
+
+def test_pair_model_parameter_lists(oracle):
+    """The constructors' coefficient formulas (potential/__init__.py:58-146) smooth each
+    polynomial model to zero force at the cut-off (sigma = 1)."""
+    for kind in ("poly12", "poly10", "poly106", "poly18", "polylj", "polyyukawa"):
+        rc, prm = oracle.potential_params(kind)
+        prm = list(prm)
+        prm[2 if kind == "polyyukawa" else 1] = 0.0  # eps = 0: sigma = d
+        pot = oracle.make_potential(kind, rc, prm)
+        f = oracle.force_divr(pot, rc * rc * (1 - 1e-9), 1.0, 1.0)
+        f_in = oracle.force_divr(pot, 1.0, 1.0, 1.0)
+        assert abs(f) < 1e-6 * abs(f_in), kind
+
+
 def test_cg_kernels_match_reference_headers_golden(oracle, golden):
     g = golden("ref_kernels.npz")
     rc = float(g["rc"])
@@ -65,6 +96,18 @@ def test_live_reference_build_if_present(oracle):
         rsq, di, dj = rng.uniform(0.05, 5.0), rng.uniform(0.6, 1.8), rng.uniform(0.6, 1.8)
         assert oracle.force_divr(pot, rsq, di, dj) == R.ref_poly12_force_divr(rsq, pot.scaled_rcut, prm, di, dj)
         assert oracle.pair_energy(pot, rsq, di, dj) == R.ref_poly12_energy(rsq, pot.scaled_rcut, prm, di, dj)
+    for kind in POT_KINDS:  # every model, eps != 0 where it has one
+        rc, q = oracle.potential_params(kind)
+        q = list(q)
+        q[2 if kind == "polyyukawa" else 1] = 0.12
+        p = oracle.make_potential(kind, rc, q)
+        arr = (C.c_double * len(q))(*q)
+        K = oracle.POT_KIND[kind]
+        for _ in range(400):
+            di, dj = rng.uniform(0.6, 1.8), rng.uniform(0.6, 1.8)
+            rsq = rng.uniform(0.02, 1.2) * (rc * 0.5 * (di + dj)) ** 2
+            assert oracle.force_divr(p, rsq, di, dj) == R.ref_pot_force_divr(K, rsq, rc, arr, len(q), di, dj), kind
+            assert oracle.pair_energy(p, rsq, di, dj) == R.ref_pot_energy(K, rsq, rc, arr, len(q), di, dj), kind
 
 
 def test_octic_bond_closed_form(oracle):
