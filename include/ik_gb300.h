@@ -233,6 +233,17 @@ int ik_compute_fp64_noalloc(int dim, const double boxsize[3], const double origi
                             const double* d_grid, double* d_virial, double* d_kinetic,
                             void* stream);
 
+/* Global thermodynamic observables of a slot's frame: ThermoCalculator::compute
+ * (thermo/ThermoCalculator.h:68-90) with every observable of thermo/module-thermo.cpp:7-20.
+ * Unique pairs i < j within max_rcut, r_ij = r_i - r_j (the reference's p_j.dx()), and the
+ * particles' kinetic terms, all divided by the box volume (SimBox::vol).  out (FP64, count
+ * >= IK_THERMO_SIZE(dim)): [0] potential energy; then virial, elastic virial (zero unless a
+ * displacement was uploaded) and kinetic stress, dim x dim each at index a + dim*b; then
+ * the Born tensor, dim^4 at index i + dim*(j + dim*(k + dim*l)).  FP64, deterministic,
+ * synchronous.  Replaces ThermoCalculator::compute + the Global* ThermoProperty classes. */
+#define IK_THERMO_SIZE(dim) (1 + 3 * (dim) * (dim) + (dim) * (dim) * (dim) * (dim))
+int ik_compute_thermo(ik_ctx* ctx, int slot, double* out, int64_t count);
+
 /* Number of kernels this context has launched since it was created. */
 int ik_get_launch_count(ik_ctx* ctx, int64_t* out);
 

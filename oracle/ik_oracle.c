@@ -162,19 +162,43 @@ double ikor_pair_energy(const ikor_pot* p, double rsq, double di, double dj)
     }
 }
 
+/* computeStiffness of each model (Polydisperse12.h:57-73, LennardJones.h:60-75 -- the
+ * force-shifted model inherits it --, Polydisperse10.h:56-72, Polydisperse106.h:56-72,
+ * Polydisperse18.h:56-72, PolydisperseLJ.h:56-72, PolydisperseYukawa.h:59-76). */
 double ikor_bond_stiffness(const ikor_pot* p, double rsq, double di, double dj)
 {
     double rcutsq = p->scaled_rcut * p->scaled_rcut;
+    double v0 = p->v0, c1 = p->c1, c2 = p->c2, c3 = p->c3, kappa = p->kappa;
     double sigma = poly12_sigma(p, di, dj);
     double actualrcutsq = rcutsq * sigma * sigma;
-    if (rsq < actualrcutsq) {
-        double r2inv = 1.0 / rsq;
-        r2inv *= sigma * sigma;
-        double _rsq = rsq / (sigma * sigma);
-        double r6inv = r2inv * r2inv * r2inv;
-        return (156.0 * p->v0 * r2inv * r6inv * r6inv + 2.0 * p->c1 + 12.0 * p->c2 * _rsq) / (sigma * sigma);
+    if (!(rsq < actualrcutsq)) return 0.0;
+    if ((p->kind == IKOR_POT_LJ || p->kind == IKOR_POT_FSLJ) && v0 == 0) return 0.0;
+    double r2inv = 1.0 / rsq;
+    r2inv *= sigma * sigma;
+    double _rsq = rsq / (sigma * sigma);
+    double r6inv = r2inv * r2inv * r2inv;
+    switch (p->kind) {
+    case IKOR_POT_LJ:
+    case IKOR_POT_FSLJ:
+        return (4 * v0 * r2inv * r6inv * (13.0 * 12.0 * r6inv - 6.0 * 7.0)) / (sigma * sigma);
+    case IKOR_POT_POLY10:
+        return (110.0 * v0 * r6inv * r6inv + 2.0 * c1 + 12.0 * c2 * _rsq + 30.0 * c3 * _rsq * _rsq) / (sigma * sigma);
+    case IKOR_POT_POLY106:
+        return (v0 * (110.0 * r6inv * r6inv - 42.0 * r2inv * r2inv * r2inv * r2inv) + 2.0 * c1 + 12.0 * c2 * _rsq) /
+               (sigma * sigma);
+    case IKOR_POT_POLY18:
+        return (342.0 * v0 * r2inv * r6inv * r6inv * r6inv + 2.0 * c1 + 12.0 * c2 * _rsq) / (sigma * sigma);
+    case IKOR_POT_POLYLJ:
+        return (156.0 * v0 * r2inv * r6inv * r6inv - 42.0 * v0 * r2inv * r6inv + 2.0 * c1 + 4.0 * c2 * _rsq) /
+               (sigma * sigma);
+    case IKOR_POT_POLYYUKAWA: {
+        double rinv = sqrt(r2inv), rroot = sqrt(_rsq);
+        return (v0 * exp(-kappa * rroot) * (2 * r2inv + 2 * kappa * rinv + kappa * kappa) * rinv + 2 * c1 +
+                12 * c2 * _rsq) / (sigma * sigma);
     }
-    return 0.0;
+    default:
+        return (156.0 * v0 * r2inv * r6inv * r6inv + 2.0 * c1 + 12.0 * c2 * _rsq) / (sigma * sigma);
+    }
 }
 
 /* ------------------------------------------------------------------------- */
@@ -758,6 +782,72 @@ void ikor_global_virial(const ikor_box* box, int64_t n, const double* pos, const
             for (int b = 0; b < D; ++b)
                 for (int a = 0; a < D; ++a) out[a + D * b] += (f * rij[a]) * rij[b];
         }
+    free(noff);
+    free(nidx);
+}
+
+/* ThermoCalculator::compute (thermo/ThermoCalculator.h:68-90) with every global observable
+ * of thermo/module-thermo.cpp:7-20: particles i in id order, neighbours j within max_rcut
+ * with i < j, r_ij = p_j.dx() = r_i - r_j (min image), then everything times 1/vol
+ * (ThermoProperty.h divideByVolume; vol = SimBox::vol, SimBox.cc:15-22).
+ *   PotentialEnergy      sum getPairEnergy                      (ListofCommonObservables.h:10-28)
+ *   VirialStress         (f r_a) r_b                            (:43-70)
+ *   ElasticVirialStress  F1_a (u+r)_b - F_a r_b, u = u_j - u_i  (:86-122)
+ *   KineticStress        (m v_a) v_b per particle               (:125-140)
+ *   BornStiffnessTensor  (s r_i + F_i) r_j n_k n_l, n = r/|r|   (:150-183)
+ * out: [0] energy, [1..] virial, elastic virial, kinetic (D x D each, index a + D b), Born
+ * (D^4, index i + D (j + D (k + D l))).  disp / vel / mass may be NULL (zero / zero / one). */
+void ikor_global_thermo(const ikor_box* box, int64_t n, const double* pos, const double* vel, const double* mass,
+                        const double* diam, const double* disp, const ikor_pot* pot, double max_rcut, double* out)
+{
+    int D = box->dim, D2 = D * D, D4 = D2 * D2;
+    double* pe = out;
+    double* vir = out + 1;
+    double* ela = vir + D2;
+    double* kin = ela + D2;
+    double* born = kin + D2;
+    for (int k = 0; k < 1 + 3 * D2 + D4; ++k) out[k] = 0.0;
+    int64_t* noff = (int64_t*)malloc(sizeof(int64_t) * (size_t)(n + 1));
+    int64_t nnz = ikor_neighbors(box, n, pos, max_rcut, noff, NULL);
+    int32_t* nidx = (int32_t*)malloc(sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1));
+    ikor_neighbors(box, n, pos, max_rcut, noff, nidx);
+    double vol = D == 2 ? box->L[0] * box->L[1] : box->L[0] * box->L[1] * box->L[2];
+    for (int64_t i = 0; i < n; ++i) {
+        double m = mass ? mass[i] : 1.0;
+        if (vel)
+            for (int b = 0; b < D; ++b)
+                for (int a = 0; a < D; ++a) kin[a + D * b] += m * vel[3 * i + a] * vel[3 * i + b];
+        for (int64_t k = noff[i]; k < noff[i + 1]; ++k) {
+            int64_t j = nidx[k];
+            if (!(i < j)) continue;
+            double rij[3];
+            ikor_min_image(box, &pos[3 * j], &pos[3 * i], rij);
+            double rsq = dot3(rij);
+            pe[0] += ikor_pair_energy(pot, rsq, diam[i], diam[j]);
+            double f = ikor_force_divr(pot, rsq, diam[i], diam[j]);
+            double F[3] = {f * rij[0], f * rij[1], f * rij[2]};
+            for (int b = 0; b < D; ++b)
+                for (int a = 0; a < D; ++a) vir[a + D * b] += F[a] * rij[b];
+            if (disp) {
+                double w[3];
+                for (int c = 0; c < 3; ++c) w[c] = (disp[3 * j + c] - disp[3 * i + c]) + rij[c];
+                double f1 = ikor_force_divr(pot, dot3(w), diam[i], diam[j]);
+                double F1[3] = {f1 * w[0], f1 * w[1], f1 * w[2]};
+                for (int b = 0; b < D; ++b)
+                    for (int a = 0; a < D; ++a) ela[a + D * b] += F1[a] * w[b] - F[a] * rij[b];
+            }
+            double st = ikor_bond_stiffness(pot, rsq, diam[i], diam[j]);
+            double nr = sqrt(rsq);
+            double nv[3] = {rij[0] / nr, rij[1] / nr, rij[2] / nr};
+            for (int l = 0; l < D; ++l)
+                for (int kk = 0; kk < D; ++kk)
+                    for (int jj = 0; jj < D; ++jj)
+                        for (int ii = 0; ii < D; ++ii)
+                            born[ii + D * (jj + D * (kk + D * l))] += (st * rij[ii] + F[ii]) * rij[jj] * nv[kk] * nv[l];
+        }
+    }
+    double iv = 1 / vol;
+    for (int k = 0; k < 1 + 3 * D2 + D4; ++k) out[k] = out[k] * iv;
     free(noff);
     free(nidx);
 }

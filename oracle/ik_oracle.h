@@ -105,6 +105,11 @@ int ikor_compute_range(const ikor_box* box, int64_t n, const double* pos, const 
 /* Global virial sum_{i<j} F_ij (x) r_ij (ThermoCalculator.h:68-90, not divided by volume). */
 void ikor_global_virial(const ikor_box* box, int64_t n, const double* pos, const double* diam,
                         const ikor_pot* pot, double max_rcut, double* out /* dim x dim */);
+/* Global thermodynamic observables (ThermoCalculator::compute); out holds
+ * 1 + 3 dim^2 + dim^4 values: energy, virial, elastic virial, kinetic stress, Born tensor,
+ * all divided by the box volume. */
+void ikor_global_thermo(const ikor_box* box, int64_t n, const double* pos, const double* vel, const double* mass,
+                        const double* diam, const double* disp, const ikor_pot* pot, double max_rcut, double* out);
 
 #ifdef __cplusplus
 }

@@ -83,6 +83,8 @@ def lib():
         L.ikor_compute_elastic.restype = C.c_int
         L.ikor_global_virial.argtypes = [C.POINTER(Box), C.c_int64, dp, dp, C.POINTER(Pot),
                                          C.c_double, dp]
+        L.ikor_global_thermo.argtypes = [C.POINTER(Box), C.c_int64, dp, dp, dp, dp, dp, C.POINTER(Pot),
+                                         C.c_double, dp]
         _LIB = L
     return _LIB
 
@@ -304,6 +306,32 @@ def global_virial(box, pos, diam, pot, max_rc=None):
     return out.reshape(D, D).T.copy()
 
 
+def global_thermo(box, pos, diam, pot, vel=None, mass=None, disp=None, max_rc=None):
+    """ThermoCalculator::compute: dict of the global observables divided by the volume:
+    potentialenergy (scalar), virialstress, elasticvirialstress, kineticstress (D x D,
+    [a, b]), borntensor (D x D x D x D, [i, j, k, l])."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    diam = np.ascontiguousarray(diam, dtype=np.float64)
+    if max_rc is None:
+        max_rc = max_rcut(pot.scaled_rcut, diam)
+    D = box.dim
+    out = np.zeros(1 + 3 * D * D + D ** 4)
+    arr = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (vel, mass, disp)]
+    ptr = [None if a is None else _dp(a) for a in arr]
+    lib().ikor_global_thermo(C.byref(box), len(pos), _dp(pos), ptr[0], ptr[1], _dp(diam), ptr[2], C.byref(pot),
+                             max_rc, _dp(out))
+    return unpack_thermo(out, D)
+
+
+def unpack_thermo(out, D):
+    """Split the flat layout [energy | virial | elastic | kinetic | Born] (column-major
+    tensors: index a + D b, i + D (j + D (k + D l)))."""
+    D2 = D * D
+    t = lambda k: out[1 + k * D2:1 + (k + 1) * D2].reshape(D, D).T.copy()
+    return {"potentialenergy": float(out[0]), "virialstress": t(0), "elasticvirialstress": t(1),
+            "kineticstress": t(2), "borntensor": out[1 + 3 * D2:].reshape(D, D, D, D).transpose(3, 2, 1, 0).copy()}
+
+
 # ---- reference kernels compiled from the reference tree (oracle/_ref) --------
 def ref_lib():
     """The reference's own pair models and Octic/Rect/Mollifier, or None when
@@ -319,7 +347,7 @@ def ref_lib():
     for f in ("ref_poly12_force_divr", "ref_poly12_energy", "ref_poly12_stiffness"):
         getattr(L, f).argtypes = [C.c_double, C.c_double, dp, C.c_double, C.c_double]
         getattr(L, f).restype = C.c_double
-    for f in ("ref_pot_force_divr", "ref_pot_energy"):
+    for f in ("ref_pot_force_divr", "ref_pot_energy", "ref_pot_stiffness"):
         getattr(L, f).argtypes = [C.c_int, C.c_double, C.c_double, dp, C.c_int, C.c_double, C.c_double]
         getattr(L, f).restype = C.c_double
     for f in ("ref_octic", "ref_rect", "ref_mollifier"):

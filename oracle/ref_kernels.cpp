@@ -33,6 +33,13 @@ double energy_of(double rsq, double rc, const double* prm, int np, double di, do
     M m(rsq, rc * rc, p);
     return m.computeEnergy(di, dj);
 }
+template <class M>
+double stiffness_of(double rsq, double rc, const double* prm, int np, double di, double dj)
+{
+    std::vector<double> p(prm, prm + np);
+    M m(rsq, rc * rc, p);
+    return m.computeStiffness(di, dj);
+}
 }  // namespace
 
 extern "C" {
@@ -75,6 +82,19 @@ double ref_pot_energy(int kind, double rsq, double rc, const double* prm, int np
     case 6: return energy_of<PolydisperseLJ>(rsq, rc, prm, np, di, dj);
     case 7: return energy_of<PolydisperseYukawa>(rsq, rc, prm, np, di, dj);
     default: return energy_of<Polydisperse12>(rsq, rc, prm, np, di, dj);
+    }
+}
+double ref_pot_stiffness(int kind, double rsq, double rc, const double* prm, int np, double di, double dj)
+{
+    switch (kind) {
+    case 1: return stiffness_of<LennardJones>(rsq, rc, prm, np, di, dj);
+    case 2: return stiffness_of<ForceShiftedLennardJones>(rsq, rc, prm, np, di, dj);
+    case 3: return stiffness_of<Polydisperse10>(rsq, rc, prm, np, di, dj);
+    case 4: return stiffness_of<Polydisperse106>(rsq, rc, prm, np, di, dj);
+    case 5: return stiffness_of<Polydisperse18>(rsq, rc, prm, np, di, dj);
+    case 6: return stiffness_of<PolydisperseLJ>(rsq, rc, prm, np, di, dj);
+    case 7: return stiffness_of<PolydisperseYukawa>(rsq, rc, prm, np, di, dj);
+    default: return stiffness_of<Polydisperse12>(rsq, rc, prm, np, di, dj);
     }
 }
 double ref_octic(double rcut, double dr_sq) { Octic f(rcut); return f.compute(dr_sq); }

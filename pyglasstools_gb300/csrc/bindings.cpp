@@ -11,6 +11,7 @@
 #include <pybind11/pybind11.h>
 #include <pybind11/stl.h>
 
+#include <algorithm>
 #include <array>
 #include <cmath>
 #include <cstdio>
@@ -551,7 +552,110 @@ struct IrvingKirkwood {
     }
 };
 
+// ---------------------------------------------------------------- _thermo
+// Global observables (thermo/ThermoProperty.h, thermo/module-thermo.cpp:7-20): the value
+// tensor of one part of ik_compute_thermo's output, saved as std::to_string(val[index]).
+enum { TH_ENERGY = 0, TH_VIRIAL = 1, TH_ELASTIC = 2, TH_KINETIC = 3, TH_BORN = 4 };
+struct ThermoProperty {
+    std::string name, type;
+    bool islocal = false;
+    int dim = 2, part = TH_ENERGY;
+    std::vector<double> val;
+    ThermoProperty(std::string n, std::string t, bool local, int d, int pt)
+        : name(std::move(n)), type(std::move(t)), islocal(local), dim(d), part(pt)
+    {
+        const size_t D2 = (size_t)d * d;
+        val.assign(pt == TH_ENERGY ? 1 : (pt == TH_BORN ? D2 * D2 : D2), 0.0);
+    }
+    virtual ~ThermoProperty() = default;
+    void save(MPILogFile& f, int index)
+    {
+        if (index < 0 || (size_t)index >= val.size()) throw std::out_of_range("[ERROR]: component index out of range");
+        f.write_shared(std::to_string(val[(size_t)index]));
+    }
+    void clear() { std::fill(val.begin(), val.end(), 0.0); }
+    // the part's slice of ik_compute_thermo's output
+    void take(const std::vector<double>& out)
+    {
+        const size_t D2 = (size_t)dim * dim;
+        const size_t off = part == TH_ENERGY ? 0 : (part == TH_BORN ? 1 + 3 * D2 : 1 + (size_t)(part - 1) * D2);
+        std::copy(out.begin() + (long)off, out.begin() + (long)(off + val.size()), val.begin());
+    }
+};
+
+template <int D, int PART>
+struct GlobalProperty : ThermoProperty {
+    GlobalProperty(std::string n, std::string t, bool local) : ThermoProperty(std::move(n), std::move(t), local, D, PART) {}
+};
+
+// ThermoCalculator (thermo/ThermoCalculator.h:7-90): max_rcut frozen at construction as
+// Calculator does (Calculator.h:41-45); compute() fills every added observable.
+struct ThermoCalculator {
+    std::shared_ptr<ParticleSystem> sys;
+    std::shared_ptr<PairPotential> pot;
+    std::map<std::string, std::shared_ptr<ThermoProperty>> obs;
+    ik_ctx* ctx = nullptr;
+    double max_rcut = 0.0;
+    uint64_t uploaded = (uint64_t)-1;
+    const ParticleSystem* uploaded_sys = nullptr;
+
+    ThermoCalculator(std::shared_ptr<ParticleSystem> s, std::shared_ptr<PairPotential> p)
+        : sys(std::move(s)), pot(std::move(p))
+    {
+        if (!sys || !pot) throw std::invalid_argument("[ERROR]: ThermoCalculator needs sysdata and a potential");
+        double dmax = 0.0;
+        for (double d : sys->diameter) dmax = std::max(dmax, d);
+        max_rcut = std::max(pot->scaled_rcut * dmax, dmax);
+        check(ik_create(&ctx, 0));
+    }
+    ~ThermoCalculator() { if (ctx) ik_destroy(ctx); }
+    void setSystemData(std::shared_ptr<ParticleSystem> s) { sys = std::move(s); }
+    void addObservable(std::shared_ptr<ThermoProperty> o) { obs[o->name] = std::move(o); }
+    void compute()
+    {
+        const int kind = pot->model();
+        if (ik_potential_nparams(kind) < 0) throw std::invalid_argument("[ERROR]: the base PairPotential has no force model");
+        if ((int)pot->params.size() < ik_potential_nparams(kind))
+            throw std::invalid_argument("[ERROR]: too few pair-potential parameters");
+        const SimBox& b = *sys->simbox;
+        std::vector<double> out((size_t)(1 + 3 * b.dim * b.dim + b.dim * b.dim * b.dim * b.dim));
+        {
+            py::gil_scoped_release nogil;
+            double L[3] = {b.boxsize[0], b.boxsize[1], b.boxsize[2]};
+            double o[3] = {b.origin[0], b.origin[1], b.origin[2]};
+            check(ik_set_box(ctx, b.dim, L, o));
+            check(ik_set_potential(ctx, kind, pot->scaled_rcut, pot->params.data(), (int)pot->params.size()));
+            check(ik_set_max_rcut(ctx, max_rcut));
+            if (uploaded != sys->version || uploaded_sys != sys.get()) {
+                check(ik_set_frame(ctx, sys->N, sys->pos.data(), sys->vel.data(), sys->mass.data(),
+                                   sys->diameter.data()));
+                uploaded = sys->version;
+                uploaded_sys = sys.get();
+            }
+            bool ela = false;
+            for (auto& kv : obs) ela = ela || kv.second->part == TH_ELASTIC;
+            if (ela) check(ik_upload_displacement(ctx, 0, sys->N, sys->disp.data()));
+            check(ik_compute_thermo(ctx, 0, out.data(), (int64_t)out.size()));
+        }
+        for (auto& kv : obs) {
+            if (kv.second->dim != b.dim) throw std::invalid_argument("[ERROR]: observable dimension != box dimension");
+            kv.second->take(out);
+        }
+    }
+};
+
 // ---------------------------------------------------------------- module
+// export_ThermoProperty (thermo/ThermoProperty.h:217-225)
+template <int D, int PART>
+static void export_thermo_property(py::module& tm, const char* name)
+{
+    using T = GlobalProperty<D, PART>;
+    py::class_<T, ThermoProperty, std::shared_ptr<T>>(tm, name)
+        .def(py::init<std::string, std::string, bool>())
+        .def("save", &T::save)
+        .def("clear", &T::clear);
+}
+
 // export_ShortRangePairPotential (potential/PairPotential.h:139-152)
 template <int KIND>
 static void export_short_range(py::module& pm, const char* name)
@@ -656,6 +760,30 @@ PYBIND11_MODULE(_core, m)
     export_short_range<IK_POT_POLY106>(pm, "PairPotentialPoly106");
     export_short_range<IK_POT_POLYYUKAWA>(pm, "PairPotentialPolyYukawa");
     export_short_range<IK_POT_POLYLJ>(pm, "PairPotentialPolyLJ");
+
+    py::module tm = m.def_submodule("_thermo");
+    py::class_<ThermoCalculator, std::shared_ptr<ThermoCalculator>>(tm, "ThermoCalculator")
+        .def(py::init<std::shared_ptr<ParticleSystem>, std::shared_ptr<PairPotential>>())
+        .def("compute", &ThermoCalculator::compute)
+        .def("setSystemData", &ThermoCalculator::setSystemData)
+        .def("addObservable", &ThermoCalculator::addObservable)
+        .def_readonly("max_rcut", &ThermoCalculator::max_rcut);
+    py::class_<ThermoProperty, std::shared_ptr<ThermoProperty>>(tm, "ThermoProperty")
+        .def_readonly("name", &ThermoProperty::name)
+        .def_readonly("type", &ThermoProperty::type)
+        .def_readonly("islocal", &ThermoProperty::islocal)
+        .def_readonly("dim", &ThermoProperty::dim)
+        .def_property_readonly("val", [](const ThermoProperty& t) { return t.val; });
+    export_thermo_property<2, TH_ENERGY>(tm, "GlobalPotentialEnergy2D");
+    export_thermo_property<3, TH_ENERGY>(tm, "GlobalPotentialEnergy3D");
+    export_thermo_property<2, TH_VIRIAL>(tm, "GlobalVirialStress2D");
+    export_thermo_property<3, TH_VIRIAL>(tm, "GlobalVirialStress3D");
+    export_thermo_property<2, TH_ELASTIC>(tm, "GlobalElasticVirialStress2D");
+    export_thermo_property<3, TH_ELASTIC>(tm, "GlobalElasticVirialStress3D");
+    export_thermo_property<2, TH_BORN>(tm, "GlobalBornTensor2D");
+    export_thermo_property<3, TH_BORN>(tm, "GlobalBornTensor3D");
+    export_thermo_property<2, TH_KINETIC>(tm, "GlobalKineticStress2D");
+    export_thermo_property<3, TH_KINETIC>(tm, "GlobalKineticStress3D");
 
     py::module cm = m.def_submodule("_cgfunc");
     py::class_<CoarseGrainFunction, std::shared_ptr<CoarseGrainFunction>>(cm, "CoarseGrainFunction")

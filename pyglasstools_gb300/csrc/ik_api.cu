@@ -157,6 +157,7 @@ struct ik_ctx {
     DevBuf maxnbe;
     // neighbour-query scratch
     DevBuf q_cell_of, q_rank, q_count, q_start, q_sorted, q_cnt, q_offs, q_idx, q_flag;
+    DevBuf th_partial, th_out; // global thermodynamic observables (ik_compute_thermo)
     std::vector<Slot> slots;
     std::vector<PendingOp> pending;
     ik_mlp* mlp = nullptr; // learned bond-integral surrogate (IK_QUAD_MLP)
@@ -1355,18 +1356,10 @@ int ik_get_field(ik_ctx* c, int slot, int field, double* out, int64_t count)
     return IK_OK;
 }
 
-int ik_get_neighbors(ik_ctx* c, int slot, double radius, int64_t* offs, int32_t* idx, int64_t idx_capacity,
-                     int64_t* nnz)
+// Cell grid of cut-off `radius` over the current box (ik_get_neighbors, ik_compute_thermo).
+static int query_geometry(ik_ctx* c, double radius, IkGeom& g)
 {
-    if (int r = check_ctx(c)) return r;
-    if (int r = slot_ok(c, slot)) return r;
-    GeoSwap gs(c, slot);
-    if (!c->geo.box_set) return fail(IK_ERR_STATE, "box not set");
-    if (!(radius > 0.0)) return fail(IK_ERR_ARG, "radius must be > 0");
-    if (!offs || !nnz) return fail(IK_ERR_ARG, "null output");
-    Slot& s = c->slots[(size_t)slot];
-    int n = (int)s.n;
-    IkGeom g{};
+    g = IkGeom{};
     g.dim = c->dim;
     for (int a = 0; a < 3; ++a) {
         g.L[a] = c->geo.boxsize[a];
@@ -1384,6 +1377,79 @@ int ik_get_neighbors(ik_ctx* c, int slot, double radius, int64_t* offs, int32_t*
         g.all_bond[a] = nc < 3 ? 1 : 0;
     }
     g.ncell = g.nc[0] * g.nc[1] * g.nc[2];
+    return IK_OK;
+}
+
+int ik_compute_thermo(ik_ctx* c, int slot, double* out, int64_t count)
+{
+    if (int r = check_ctx(c)) return r;
+    if (int r = slot_ok(c, slot)) return r;
+    GeoSwap gs(c, slot);
+    if (!c->geo.box_set) return fail(IK_ERR_STATE, "box not set");
+    if (!c->pot_set) return fail(IK_ERR_STATE, "pair potential not set");
+    if (!c->max_rcut_set) return fail(IK_ERR_STATE, "max_rcut unknown: upload a frame or call ik_set_max_rcut");
+    const int D = c->dim, D2 = D * D;
+    const int64_t need = 1 + 3 * D2 + D2 * D2;
+    if (!out || count < need) return fail(IK_ERR_ARG, "output needs %lld values", (long long)need);
+    Slot& s = c->slots[(size_t)slot];
+    const int n = (int)s.n;
+    IkGeom g;
+    if (int r = query_geometry(c, c->max_rcut, g)) return r;
+    if (s.done_recorded) CK(cudaStreamWaitEvent(c->stream, s.done, 0));
+    if (int r = build_cells(c, s, g, c->stream, c->q_cell_of, c->q_rank, c->q_count, c->q_start, c->q_sorted,
+                            c->bsum_q))
+        return r;
+    if (g.ncell > 0)
+        k_cell_sort_pack<<<(g.ncell + 127) / 128, 128, 0, c->stream>>>(g, c->q_start.as<int>(), c->q_sorted.as<int>(),
+                                                                       nullptr, nullptr, nullptr, nullptr, nullptr,
+                                                                       nullptr, nullptr, 0);
+    const int nq = ik_thermo_nq(D), nblocks = (n + 127) / 128;
+    ENS(c->th_partial, sizeof(double) * (size_t)nq * std::max(nblocks, 1));
+    ENS(c->th_out, sizeof(double) * nq);
+    const double vol = D == 2 ? g.L[0] * g.L[1] : g.L[0] * g.L[1] * g.L[2]; // SimBox.cc:15-22
+    IkPot pot = c->pot;
+    pot.max_rcut_sq = c->max_rcut * c->max_rcut;
+    CK(launch_thermo64(g, pot, n, c->q_sorted.as<int>(), c->q_cell_of.as<int>(), s.pos.as<double>(),
+                       s.has_vel ? s.vel.as<double>() : nullptr, s.has_mass ? s.mass.as<double>() : nullptr,
+                       s.diam.as<double>(), s.has_disp ? s.disp.as<double>() : nullptr, c->q_start.as<int>(),
+                       c->th_partial.as<double>(), nblocks, 1 / vol, c->th_out.as<double>(), c->stream));
+    c->launches += (g.ncell > 0 ? 1 : 0) + (nblocks > 0 ? 1 : 0) + 1;
+    std::vector<double> h((size_t)nq);
+    CK(cudaMemcpyAsync(h.data(), c->th_out.p, sizeof(double) * nq, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    // {energy, virial, elastic, kinetic} as they are; the Born tensor from its symmetric
+    // components (enumerated i <= j <= k <= l as on the device)
+    for (int k = 0; k < 1 + 3 * D2; ++k) out[k] = h[(size_t)k];
+    int sym[3][3][3][3];
+    int u = 1 + 3 * D2;
+    for (int a = 0; a < D; ++a)
+        for (int b = a; b < D; ++b)
+            for (int k = b; k < D; ++k)
+                for (int l = k; l < D; ++l) sym[a][b][k][l] = u++;
+    for (int l = 0; l < D; ++l)
+        for (int k = 0; k < D; ++k)
+            for (int j = 0; j < D; ++j)
+                for (int i = 0; i < D; ++i) {
+                    int t[4] = {i, j, k, l};
+                    std::sort(t, t + 4);
+                    out[1 + 3 * D2 + i + D * (j + D * (k + D * l))] = h[(size_t)sym[t[0]][t[1]][t[2]][t[3]]];
+                }
+    return IK_OK;
+}
+
+int ik_get_neighbors(ik_ctx* c, int slot, double radius, int64_t* offs, int32_t* idx, int64_t idx_capacity,
+                     int64_t* nnz)
+{
+    if (int r = check_ctx(c)) return r;
+    if (int r = slot_ok(c, slot)) return r;
+    GeoSwap gs(c, slot);
+    if (!c->geo.box_set) return fail(IK_ERR_STATE, "box not set");
+    if (!(radius > 0.0)) return fail(IK_ERR_ARG, "radius must be > 0");
+    if (!offs || !nnz) return fail(IK_ERR_ARG, "null output");
+    Slot& s = c->slots[(size_t)slot];
+    int n = (int)s.n;
+    IkGeom g;
+    if (int r = query_geometry(c, radius, g)) return r;
     if (s.done_recorded) CK(cudaStreamWaitEvent(c->stream, s.done, 0));
     if (int r = build_cells(c, s, g, c->stream, c->q_cell_of, c->q_rank, c->q_count, c->q_start, c->q_sorted,
                             c->bsum_q))

@@ -404,3 +404,148 @@ __global__ void k_validate(const double* __restrict__ pos, const double* __restr
               (dim == 3 || (z & ABS) == 0);
     if (!ok) atomicOr(status, IK_ST_BAD_INPUT);
 }
+
+// ---------------------------------------------------------------------------
+// 10. Global thermodynamic observables (ThermoCalculator::compute,
+//     thermo/ThermoCalculator.h:68-90): one thread per particle in cell order; its kinetic
+//     term m v (x) v and, over the stencil, every neighbour j within max_rcut with a
+//     larger id (unique pairs i < j as there), r_ij = r_i - r_j (Aboria's p_j.dx()):
+//       energy, virial F (x) r, elastic virial F1 (x) (u + r) - F (x) r with u = u_j - u_i,
+//       and the Born tensor (s r_i + F_i) r_j n_k n_l = (s + f) r_i r_j r_k r_l / r^2,
+//       kept as its fully symmetric components (i <= j <= k <= l).
+//     FP64 per thread, then a fixed-order block reduction into per-block partials; the
+//     final sums run over the blocks in order (k_thermo_final): deterministic.
+template <int DIM>
+struct ThermoLayout {
+    static constexpr int D2 = DIM * DIM;
+    static constexpr int NB = DIM == 2 ? 5 : 15; // symmetric 4-tensor components
+    static constexpr int NQ = 1 + 3 * D2 + NB;
+};
+
+template <int DIM>
+__global__ void __launch_bounds__(128) k_thermo64(IkGeom g, IkPot pot, int n, const int* __restrict__ sorted,
+                                                  const int* __restrict__ cell_of, const double* __restrict__ pos,
+                                                  const double* __restrict__ vel, const double* __restrict__ mass,
+                                                  const double* __restrict__ diam, const double* __restrict__ disp,
+                                                  const int* __restrict__ cell_start, double* __restrict__ partial)
+{
+    using TL = ThermoLayout<DIM>;
+    constexpr int D2 = TL::D2, NQ = TL::NQ;
+    double acc[NQ];
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) acc[k] = 0.0;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) {
+        const int i = sorted[p];
+        const double m = mass ? mass[i] : 1.0;
+        if (vel) {
+#pragma unroll
+            for (int b = 0; b < DIM; ++b)
+#pragma unroll
+                for (int a = 0; a < DIM; ++a)
+                    acc[1 + 2 * D2 + a + DIM * b] = __dmul_rn(__dmul_rn(m, vel[3 * i + a]), vel[3 * i + b]);
+        }
+        const int c = cell_of[i];
+        const int cx = c % g.nc[0], cy = (c / g.nc[0]) % g.nc[1], cz = c / (g.nc[0] * g.nc[1]);
+        const double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2], di = diam[i];
+        StencilAxis az = ik_axis(g, 2, cz), ay = ik_axis(g, 1, cy), ax = ik_axis(g, 0, cx);
+        for (int zz = az.lo; zz <= az.hi; ++zz) {
+            const int wz = DIM == 3 ? ik_wrap(zz, g.nc[2]) : 0;
+            for (int yy = ay.lo; yy <= ay.hi; ++yy) {
+                const int wy = ik_wrap(yy, g.nc[1]);
+                for (int xx = ax.lo; xx <= ax.hi; ++xx) {
+                    const int wx = ik_wrap(xx, g.nc[0]);
+                    const int cell = (wz * g.nc[1] + wy) * g.nc[0] + wx;
+                    const int e = cell_start[cell + 1];
+                    for (int q = cell_start[cell]; q < e; ++q) {
+                        const int j = sorted[q];
+                        if (j <= i) continue;
+                        double r[3];
+                        r[0] = ik_minimg(__dsub_rn(xi, pos[3 * j]), g.L[0], g.periodic[0]);
+                        r[1] = ik_minimg(__dsub_rn(yi, pos[3 * j + 1]), g.L[1], g.periodic[1]);
+                        r[2] = ik_minimg(__dsub_rn(zi, pos[3 * j + 2]), g.L[2], g.periodic[2]);
+                        const double rsq = ik_dot3(r[0], r[1], r[2]);
+                        if (!(rsq < pot.max_rcut_sq)) continue;
+                        const double dj = diam[j];
+                        const double sie = ik_sigma64(pot, di, dj, false); // energy / stiffness sigma
+                        if (rsq < __dmul_rn(__dmul_rn(pot.rcutsq, sie), sie)) acc[0] += ik_energy64(pot, rsq, sie);
+                        const double sig = ik_sigma64(pot, di, dj);
+                        const double f = ik_active64(pot, rsq, sig) ? ik_force64(pot, rsq, sig) : 0.0;
+#pragma unroll
+                        for (int b = 0; b < DIM; ++b)
+#pragma unroll
+                            for (int a = 0; a < DIM; ++a) acc[1 + a + DIM * b] += __dmul_rn(__dmul_rn(f, r[a]), r[b]);
+                        if (disp) {
+                            double w[3];
+#pragma unroll
+                            for (int k = 0; k < 3; ++k) w[k] = __dadd_rn(__dsub_rn(disp[3 * j + k], disp[3 * i + k]), r[k]);
+                            const double wsq = ik_dot3(w[0], w[1], w[2]);
+                            const double f1 = ik_active64(pot, wsq, sig) ? ik_force64(pot, wsq, sig) : 0.0;
+#pragma unroll
+                            for (int b = 0; b < DIM; ++b)
+#pragma unroll
+                                for (int a = 0; a < DIM; ++a)
+                                    acc[1 + D2 + a + DIM * b] += __dsub_rn(__dmul_rn(__dmul_rn(f1, w[a]), w[b]),
+                                                                           __dmul_rn(__dmul_rn(f, r[a]), r[b]));
+                        }
+                        const double st = ik_active64(pot, rsq, sie) ? ik_stiffness64(pot, rsq, sie) : 0.0;
+                        const double cb = (st + f) / rsq;
+                        int u = 1 + 3 * D2;
+#pragma unroll
+                        for (int a = 0; a < DIM; ++a)
+#pragma unroll
+                            for (int b = a; b < DIM; ++b)
+#pragma unroll
+                                for (int k = b; k < DIM; ++k)
+#pragma unroll
+                                    for (int l = k; l < DIM; ++l) acc[u++] += cb * r[a] * r[b] * r[k] * r[l];
+                    }
+                }
+            }
+        }
+    }
+    // block reduction: warps by shuffles (fixed tree), then the warps in order
+    __shared__ double red[4][NQ];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+        double v = acc[k];
+        for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < NQ) {
+        double v = red[0][threadIdx.x];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v += red[w][threadIdx.x];
+        partial[(size_t)blockIdx.x * NQ + threadIdx.x] = v;
+    }
+}
+
+__global__ void k_thermo_final(const double* __restrict__ partial, int nblocks, int nq, double inv_vol,
+                               double* __restrict__ out)
+{
+    const int k = threadIdx.x;
+    if (k >= nq) return;
+    double v = 0.0;
+    for (int b = 0; b < nblocks; ++b) v += partial[(size_t)b * nq + k];
+    out[k] = v * inv_vol;
+}
+
+int ik_thermo_nq(int dim) { return dim == 2 ? ThermoLayout<2>::NQ : ThermoLayout<3>::NQ; }
+
+cudaError_t launch_thermo64(const IkGeom& g, const IkPot& pot, int n, const int* sorted, const int* cell_of,
+                            const double* pos, const double* vel, const double* mass, const double* diam,
+                            const double* disp, const int* cell_start, double* partial, int nblocks,
+                            double inv_vol, double* out, cudaStream_t st)
+{
+    if (nblocks > 0) {
+        if (g.dim == 2)
+            k_thermo64<2><<<nblocks, 128, 0, st>>>(g, pot, n, sorted, cell_of, pos, vel, mass, diam, disp,
+                                                   cell_start, partial);
+        else
+            k_thermo64<3><<<nblocks, 128, 0, st>>>(g, pot, n, sorted, cell_of, pos, vel, mass, diam, disp,
+                                                   cell_start, partial);
+    }
+    k_thermo_final<<<1, 64, 0, st>>>(partial, nblocks, ik_thermo_nq(g.dim), inv_vol, out);
+    return cudaGetLastError();
+}

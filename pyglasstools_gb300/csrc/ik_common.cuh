@@ -247,6 +247,68 @@ __device__ __forceinline__ double ik_energy64(const IkPot& p, double rsq, double
     return __dadd_rn(t, __dmul_rn(__dmul_rn(p.c2, rs), rs));
 }
 
+// computeStiffness (the bond stiffness, second derivative of the pair energy) of the eight
+// models in FP64, reference expression order: Polydisperse12.h:57-73, LennardJones.h:60-75
+// (also the force-shifted model's: it does not override it), Polydisperse10.h:56-72,
+// Polydisperse106.h:56-72, Polydisperse18.h:56-72, PolydisperseLJ.h:56-72 (its c2 term is
+// 4 c2 r^2 as written there), PolydisperseYukawa.h:59-76.  Call with
+// sigma = ik_sigma64(p, di, dj, false) and ik_active64's test on that sigma.
+__device__ __forceinline__ double ik_stiffness64(const IkPot& p, double rsq, double sigma)
+{
+    const double s2 = __dmul_rn(sigma, sigma);
+    const double r2inv = __dmul_rn(__ddiv_rn(1.0, rsq), s2);
+    const double rs = __ddiv_rn(rsq, s2);
+    const double r6inv = __dmul_rn(__dmul_rn(r2inv, r2inv), r2inv);
+    double t;
+    switch (p.kind) {
+    case IKP_LJ:
+    case IKP_FSLJ:
+        t = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(4.0, p.v0), r2inv), r6inv),
+                      __dsub_rn(__dmul_rn(156.0, r6inv), 42.0));
+        return __ddiv_rn(t, s2);
+    case IKP_POLY10:
+        t = __dmul_rn(__dmul_rn(__dmul_rn(110.0, p.v0), r6inv), r6inv);
+        t = __dadd_rn(t, __dmul_rn(2.0, p.c1));
+        t = __dadd_rn(t, __dmul_rn(__dmul_rn(12.0, p.c2), rs));
+        t = __dadd_rn(t, __dmul_rn(__dmul_rn(__dmul_rn(30.0, p.c3), rs), rs));
+        return __ddiv_rn(t, s2);
+    case IKP_POLY106: {
+        const double a = __dmul_rn(__dmul_rn(110.0, r6inv), r6inv);
+        const double b = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(42.0, r2inv), r2inv), r2inv), r2inv);
+        t = __dmul_rn(p.v0, __dsub_rn(a, b));
+        t = __dadd_rn(t, __dmul_rn(2.0, p.c1));
+        t = __dadd_rn(t, __dmul_rn(__dmul_rn(12.0, p.c2), rs));
+        return __ddiv_rn(t, s2);
+    }
+    case IKP_POLY18:
+        t = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(342.0, p.v0), r2inv), r6inv), r6inv), r6inv);
+        t = __dadd_rn(t, __dmul_rn(2.0, p.c1));
+        t = __dadd_rn(t, __dmul_rn(__dmul_rn(12.0, p.c2), rs));
+        return __ddiv_rn(t, s2);
+    case IKP_POLYLJ:
+        t = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(156.0, p.v0), r2inv), r6inv), r6inv);
+        t = __dsub_rn(t, __dmul_rn(__dmul_rn(__dmul_rn(42.0, p.v0), r2inv), r6inv));
+        t = __dadd_rn(t, __dmul_rn(2.0, p.c1));
+        t = __dadd_rn(t, __dmul_rn(__dmul_rn(4.0, p.c2), rs));
+        return __ddiv_rn(t, s2);
+    case IKP_POLYYUKAWA: {
+        const double rinv = __dsqrt_rn(r2inv), rroot = __dsqrt_rn(rs);
+        const double e = exp(__dmul_rn(-p.kappa, rroot));
+        const double q = __dadd_rn(__dadd_rn(__dmul_rn(2.0, r2inv), __dmul_rn(__dmul_rn(2.0, p.kappa), rinv)),
+                                   __dmul_rn(p.kappa, p.kappa));
+        t = __dmul_rn(__dmul_rn(__dmul_rn(p.v0, e), q), rinv);
+        t = __dadd_rn(t, __dmul_rn(2.0, p.c1));
+        t = __dadd_rn(t, __dmul_rn(__dmul_rn(12.0, p.c2), rs));
+        return __ddiv_rn(t, s2);
+    }
+    default: // IKP_POLY12
+        t = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(156.0, p.v0), r2inv), r6inv), r6inv);
+        t = __dadd_rn(t, __dmul_rn(2.0, p.c1));
+        t = __dadd_rn(t, __dmul_rn(__dmul_rn(12.0, p.c2), rs));
+        return __ddiv_rn(t, s2);
+    }
+}
+
 // Coarse-graining kernels in FP64 (CGFuncOctic.h:16-29, CGFuncRect.h,
 // CGFuncMollifier.h; Gaussian added).  Returns Delta(dr_sq).
 __device__ __forceinline__ double ik_delta64(const IkCG& cg, double dr_sq)

@@ -134,6 +134,15 @@ cudaError_t launch_eval_bond(const IkCG& cg, int dim, const double* xs, const do
                              int m, const double* x, const double* ri, const double* rij, double* bond,
                              double* delta, cudaStream_t st);
 
+// ---- global thermodynamic observables (ik_cells.cu) --------------------------
+// per-block partials (nblocks x ik_thermo_nq(dim)) -> out[ik_thermo_nq(dim)] =
+// {energy, virial D x D, elastic D x D, kinetic D x D, Born symmetric components} / vol
+int ik_thermo_nq(int dim);
+cudaError_t launch_thermo64(const IkGeom& g, const IkPot& pot, int n, const int* sorted, const int* cell_of,
+                            const double* pos, const double* vel, const double* mass, const double* diam,
+                            const double* disp, const int* cell_start, double* partial, int nblocks,
+                            double inv_vol, double* out, cudaStream_t st);
+
 // ---- FP32 FMA throughput probe (ik_cells.cu) --------------------------------
 #define IK_FMA_PROBE_CHAINS 8
 cudaError_t launch_fma_probe(int blocks, int threads, int iters, float* out);

@@ -52,6 +52,7 @@ def lib():
             "ik_set_potential_poly12": ([vp, C.c_double, dp], i32),
             "ik_set_potential": ([vp, i32, C.c_double, dp, i32], i32),
             "ik_potential_nparams": ([i32], i32),
+            "ik_compute_thermo": ([vp, i32, dp, i64], i32),
             "ik_set_cgfunc": ([vp, i32, i32, i32, C.c_double, C.c_double], i32),
             "ik_set_adaptive": ([vp, i32, C.c_double, C.c_double], i32),
             "ik_set_max_rcut": ([vp, C.c_double], i32),
@@ -336,6 +337,18 @@ class IKContext:
         v = C.c_int64()
         check(lib().ik_get_launch_count(self._h, C.byref(v)))
         return v.value
+
+    def compute_thermo(self, slot=0):
+        """Global observables of a slot's frame: dict of potentialenergy (float),
+        virialstress, elasticvirialstress, kineticstress ([a, b]) and borntensor
+        ([i, j, k, l]), each per unit volume."""
+        D = self.dim
+        out = np.zeros(1 + 3 * D * D + D ** 4)
+        check(lib().ik_compute_thermo(self._h, slot, _dp(out), len(out)))
+        D2 = D * D
+        t = lambda k: out[1 + k * D2:1 + (k + 1) * D2].reshape(D, D).T.copy()
+        return {"potentialenergy": float(out[0]), "virialstress": t(0), "elasticvirialstress": t(1),
+                "kineticstress": t(2), "borntensor": out[1 + 3 * D2:].reshape(D, D, D, D).transpose(3, 2, 1, 0).copy()}
 
     def counters(self, slot=0):
         c = (C.c_int64 * 3)()

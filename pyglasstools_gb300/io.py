@@ -1,7 +1,10 @@
-"""Field output (pyglasstools/io.py:82-169): ``fieldlogger(keyword, names, solver)``
+"""Output (pyglasstools/io.py): ``logfile(filename, names, solver)`` for the global
+observables of ``thermo.calculator``, and ``fieldlogger(keyword, names, solver)``
 writes ``<keyword>.xyz`` -- per frame a ``gridsize`` line, a ``#Frame n`` line, then
 one line per grid point ``1 x y [z] T_ab ...`` with the values formatted like a
 default C++ ostream (6 significant digits)."""
+import os
+
 import numpy as np
 
 import pyglasstools_gb300
@@ -10,6 +13,64 @@ from pyglasstools_gb300 import irvingkirkwood
 
 _pyglasstools = _core._pyglasstools
 _irvingkirkwood = _core._irvingkirkwood
+
+
+class logfile(object):
+    R"""Global observables, one line per frame (pyglasstools/io.py:9-80): a header
+    ``Frame name ...`` (unless resuming from a non-empty checkpoint), then per frame
+    ``frame v v ...`` with each value as std::to_string writes it (six decimals).
+    Names: ``potentialenergy``, ``virialstress_ab``, ``elasticvirialstress_ab``,
+    ``kineticstress_ab``, ``borntensor_ijkl``.  (The reference looks elastic names up
+    under 'virialstress', which it never creates for them; here they read the elastic
+    observable.)"""
+
+    def __init__(self, filename, names, solver):
+        self.filename = filename
+        self.__obs_names = names
+        if solver is None:
+            raise ValueError("[ERROR] User must specify solver object!")
+        if names is None:
+            raise ValueError("[ERROR] User must specify list of observables to save!")
+        if filename is None:
+            raise ValueError("[ERROR] User must specify a filename for the logfile!")
+        from pyglasstools_gb300 import thermo
+        self.solver = solver
+        loggers_list.append(self)
+        self.file = _pyglasstools.MPILogFile(comm, self.filename)
+        sysdata = pyglasstools_gb300.get_sysdata()
+        self.global_obs = thermo.initialize_global(self.__obs_names, sysdata.pysimbox.dim)
+        self.solver.add_observables(self.global_obs)
+        ck = sysdata.checkpointfile
+        if rank == 0 and (ck is None or not os.path.exists(ck) or os.path.getsize(ck) == 0):
+            self.file.write_shared("{} ".format("Frame"))
+            for name in self.__obs_names:
+                self.file.write_shared("{} ".format(name))
+            self.file.write_shared("\n")
+            self.file.flush()
+
+    def save(self, frame_num):
+        if rank == 0:
+            Dim = pyglasstools_gb300.get_sysdata().pysimbox.dim
+            self.file.write_shared("{} ".format(frame_num))
+            for name in self.__obs_names:
+                if "potentialenergy" in name:
+                    self.global_obs['potentialenergy'].save(self.file, 0)
+                    self.file.write_shared(" ")
+                if "virialstress" in name:
+                    i, j = int(name[-2]), int(name[-1])
+                    key = 'elasticvirialstress' if "elastic" in name else 'virialstress'
+                    self.global_obs[key].save(self.file, i + Dim * j)
+                    self.file.write_shared(" ")
+                elif "kineticstress" in name:
+                    i, j = int(name[-2]), int(name[-1])
+                    self.global_obs['kineticstress'].save(self.file, i + Dim * j)
+                    self.file.write_shared(" ")
+                elif "borntensor" in name:
+                    i, j, k, l = (int(c) for c in name[-4:])
+                    self.global_obs['borntensor'].save(self.file, l + Dim * (k + Dim * (j + Dim * i)))
+                    self.file.write_shared(" ")
+            self.file.write_shared("\n")
+            self.file.flush()
 
 
 class fieldlogger(object):

@@ -13,7 +13,7 @@ Outputs
   ref_kernels.npz      Polydisperse12 force/energy/stiffness and Octic/Rect/Mollifier
                        values produced by the REFERENCE'S OWN headers compiled by
                        oracle/build_ref.sh, on seeded random inputs.
-  ref_potentials.npz   force and energy of all eight pair models (LJ, force-shifted LJ,
+  ref_potentials.npz   force, energy and stiffness of all eight pair models (LJ, force-shifted LJ,
                        Poly10/106/12/18, PolyLJ, PolyYukawa) from the reference's own
                        headers, on seeded inputs that include overlaps and pairs
                        within 1e-12 of the cut-off.
@@ -108,6 +108,8 @@ def ref_potentials():
                                          for a, b, c in zip(rsq, di, dj)])
         out[f"{kind}_energy"] = np.array([R.ref_pot_energy(K, a, rc, arr, len(prm), b, c)
                                           for a, b, c in zip(rsq, di, dj)])
+        out[f"{kind}_stiffness"] = np.array([R.ref_pot_stiffness(K, a, rc, arr, len(prm), b, c)
+                                             for a, b, c in zip(rsq, di, dj)])
     np.savez_compressed(os.path.join(HERE, "ref_potentials.npz"), **out)
 
 

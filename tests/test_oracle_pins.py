@@ -48,7 +48,7 @@ POT_KINDS = ["poly12", "lj", "fslj", "poly10", "poly106", "poly18", "polylj", "p
 
 @pytest.mark.parametrize("kind", POT_KINDS)
 def test_pair_models_match_reference_headers_golden(oracle, golden, kind):
-    """Force and energy of each of the eight models: bit-identical to the reference's
+    """Force, energy and stiffness of each of the eight models: bit-identical to the reference's
     own header (potential/*.h compiled by oracle/build_ref.sh; tests/golden/make_golden.py),
     including pairs within a few ulp of the cut-off and strongly overlapping pairs."""
     g = golden("ref_potentials.npz")
@@ -56,8 +56,10 @@ def test_pair_models_match_reference_headers_golden(oracle, golden, kind):
     rsq, di, dj = g[f"{kind}_rsq"], g[f"{kind}_di"], g[f"{kind}_dj"]
     f = np.array([oracle.force_divr(pot, a, b, c) for a, b, c in zip(rsq, di, dj)])
     e = np.array([oracle.pair_energy(pot, a, b, c) for a, b, c in zip(rsq, di, dj)])
+    st = np.array([oracle.bond_stiffness(pot, a, b, c) for a, b, c in zip(rsq, di, dj)])
     assert np.array_equal(f, g[f"{kind}_force"])
     assert np.array_equal(e, g[f"{kind}_energy"])
+    assert np.array_equal(st, g[f"{kind}_stiffness"])
     assert np.count_nonzero(f) > 100 and np.count_nonzero(f == 0) > 50
 
 
@@ -108,6 +110,7 @@ def test_live_reference_build_if_present(oracle):
             rsq = rng.uniform(0.02, 1.2) * (rc * 0.5 * (di + dj)) ** 2
             assert oracle.force_divr(p, rsq, di, dj) == R.ref_pot_force_divr(K, rsq, rc, arr, len(q), di, dj), kind
             assert oracle.pair_energy(p, rsq, di, dj) == R.ref_pot_energy(K, rsq, rc, arr, len(q), di, dj), kind
+            assert oracle.bond_stiffness(p, rsq, di, dj) == R.ref_pot_stiffness(K, rsq, rc, arr, len(q), di, dj), kind
 
 
 def test_octic_bond_closed_form(oracle):
