@@ -29,6 +29,7 @@ extern "C" {
 #define IK_ERR_TIMEOUT   -6  /* a bounded device-side wait gave up */
 #define IK_ERR_NOMEM     -7  /* device allocation failed */
 #define IK_ERR_UNSUPPORTED -8
+#define IK_ERR_QUADRATURE -9 /* an adaptive bond integral missed its tolerance (GSL would abort) */
 
 /* ---- enums ------------------------------------------------------------------ */
 enum ik_cg_kind { IK_CG_OCTIC = 0, IK_CG_GAUSSIAN = 1, IK_CG_RECT = 2, IK_CG_MOLLIFIER = 3 };
@@ -85,13 +86,19 @@ int ik_set_potential_poly12(ik_ctx* ctx, double scaled_rcut, const double params
  * IK_QUAD_FIXEDPOINT (both paths); IK_QUAD_EXACT (FP64 path: the segment clipped to the
  * support, erf closed form for the Gaussian, GL on the clipped interval otherwise);
  * IK_QUAD_MLP (FP32 path, Gaussian: the attached surrogate on bonds that cross the edge
- * of the support, GL-order elsewhere and as its fallback).  IK_QUAD_ADAPTIVE exists in
- * the oracle only (IK_ERR_UNSUPPORTED here).
+ * of the support, GL-order elsewhere and as its fallback); IK_QUAD_ADAPTIVE (FP64 path:
+ * QUADPACK's QAG with the GK15 rule per bond integral, as gsl_integration_qag key 1, at
+ * most min(neval, 64) subintervals; a missed tolerance is reported as IK_ERR_QUADRATURE by
+ * ik_synchronize / ik_eval_bond).
  * Replaces FixedPointCGFunc<...>(order, rcut) / AdaptiveCGFunc<...>(neval, relerr,
  * abserr, rcut) (irvingkirkwood/cgfunc/CoarseGrainFunction.h:56-134). */
 int ik_set_cgfunc(ik_ctx* ctx, int kind, int mode, int order, double rcut, double width);
 /* Adaptive-mode tolerances (AdaptiveCGFunc(neval, relerr, abserr, rcut)). */
 int ik_set_adaptive(ik_ctx* ctx, int neval, double relerr, double abserr);
+/* The Gauss-Kronrod 7/15 rule of the adaptive mode on [-1, 1] (host only): x[0] = 0 and
+ * the positive nodes ascending (Kronrod nodes at odd slots, Gauss-7 nodes at even),
+ * Kronrod weights wk, Gauss weights wg of the nodes 0, x[2], x[4], x[6]. */
+int ik_gk15_rule(double x[8], double wk[8], double wg[4]);
 
 /* Neighbour cut-off max_rcut; frozen like Calculator::max_rcut (Calculator.h:41-45).
  * If never set, the first uploaded frame fixes it to max(scaled_rcut*dmax, dmax). */

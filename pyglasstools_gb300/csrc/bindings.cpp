@@ -366,6 +366,18 @@ struct CGGaussianFixed : CoarseGrainFunction {
     }
 };
 
+struct CGGaussianAdaptive : CoarseGrainFunction {
+    CGGaussianAdaptive(int nev, double rel, double abs_, double w, double cut) : CoarseGrainFunction(cut * w)
+    {
+        kind = IK_CG_GAUSSIAN;
+        mode = IK_QUAD_ADAPTIVE;
+        neval = nev;
+        relerr = rel;
+        abserr = abs_;
+        width = w;
+    }
+};
+
 // ---------------------------------------------------------------- text output
 // Python's repr() of a float (the "{} ".format(x) of fieldlogger.save_perrank,
 // io.py:112-128): the shortest digits that round-trip, fixed notation for decimal
@@ -792,7 +804,11 @@ PYBIND11_MODULE(_core, m)
         .def("setRcut", &CoarseGrainFunction::setRcut)
         .def("getDeltaFunc", &CoarseGrainFunction::getDeltaFunc)
         .def("getObjFunc", &CoarseGrainFunction::getObjFunc)
-        .def("getBondFunc", &CoarseGrainFunction::getBondFunc);
+        .def("getBondFunc", &CoarseGrainFunction::getBondFunc)
+        .def_property_readonly("mode", [](const CoarseGrainFunction& f) {
+            return std::string(f.mode == IK_QUAD_ADAPTIVE ? "adaptive" : f.mode == IK_QUAD_EXACT ? "exact"
+                               : f.mode == IK_QUAD_MLP ? "mlp" : "fixedpoint");
+        });
 #define FIXED(T, NAME) py::class_<T, CoarseGrainFunction, std::shared_ptr<T>>(cm, NAME).def(py::init<int, double>())
 #define ADAPT(T, NAME) \
     py::class_<T, CoarseGrainFunction, std::shared_ptr<T>>(cm, NAME).def(py::init<int, double, double, double>())
@@ -806,6 +822,10 @@ PYBIND11_MODULE(_core, m)
 #undef ADAPT
     py::class_<CGGaussianFixed, CoarseGrainFunction, std::shared_ptr<CGGaussianFixed>>(cm, "CGFuncGaussianFixedPoint")
         .def(py::init<int, double, double>(), py::arg("order"), py::arg("width"), py::arg("cut") = 3.0);
+    py::class_<CGGaussianAdaptive, CoarseGrainFunction, std::shared_ptr<CGGaussianAdaptive>>(cm,
+                                                                                           "CGFuncGaussianAdaptive")
+        .def(py::init<int, double, double, double, double>(), py::arg("neval"), py::arg("relerr"),
+             py::arg("abserr"), py::arg("width"), py::arg("cut") = 3.0);
 
     py::module im = m.def_submodule("_irvingkirkwood");
     py::class_<IrvingKirkwood, std::shared_ptr<IrvingKirkwood>>(im, "IrvingKirkwood")

@@ -213,6 +213,93 @@ void gl_rule(int n, double* x, double* w)
     if (n % 2 == 1) x[n / 2] = 0.0;
 }
 
+// Gauss-Kronrod 7/15 rule (the rule of gsl_integration_qag key 1).  The Kronrod nodes
+// are the zeros of the Stieltjes polynomial E_8(x) = x^8 + a6 x^6 + a4 x^4 + a2 x^2 + a0,
+// fixed by orthogonality to x^k (k = 1, 3, 5, 7; the even k vanish by parity) under the
+// weight P_7 on [-1, 1] (Kronrod 1965); they interlace with the Gauss nodes, which locates
+// each for bisection.  The 15 weights make the rule exact on x^(2m), m = 0..7 (degree 22
+// with the odd powers).  Long double throughout; computed once.
+static IkGK make_gk15()
+{
+    typedef long double LD;
+    // P_7(x) = (429 x^7 - 693 x^5 + 315 x^3 - 35 x) / 16: moments M(q) = int P_7 x^q, q odd
+    const LD p7[4] = {-35.0L / 16, 315.0L / 16, -693.0L / 16, 429.0L / 16}; // x^1, x^3, x^5, x^7
+    auto mom = [&](int q) {
+        LD m = 0;
+        for (int t = 0; t < 4; ++t) m += p7[t] * 2.0L / (LD)(q + 2 * t + 1 + 1);
+        return m;
+    };
+    // sum_e c_e M(k + e) = -M(k + 8) over e = 0, 2, 4, 6 (coefficients a0, a2, a4, a6), k odd
+    LD A[4][5];
+    for (int r = 0; r < 4; ++r) {
+        const int k = 2 * r + 1;
+        for (int e = 0; e < 4; ++e) A[r][e] = mom(k + 2 * e);
+        A[r][4] = -mom(k + 8);
+    }
+    for (int col = 0; col < 4; ++col) {
+        int piv = col;
+        for (int r = col + 1; r < 4; ++r)
+            if (fabsl(A[r][col]) > fabsl(A[piv][col])) piv = r;
+        for (int t = 0; t < 5; ++t) std::swap(A[col][t], A[piv][t]);
+        for (int r = 0; r < 4; ++r) {
+            if (r == col) continue;
+            const LD f = A[r][col] / A[col][col];
+            for (int t = col; t < 5; ++t) A[r][t] -= f * A[col][t];
+        }
+    }
+    LD a[4];
+    for (int e = 0; e < 4; ++e) a[e] = A[e][4] / A[e][e];
+    auto E8 = [&](LD x) {
+        const LD y = x * x;
+        return (((y + a[3]) * y + a[2]) * y + a[1]) * y + a[0];
+    };
+    double gx[7], gw[7];
+    gl_rule(7, gx, gw);
+    const LD edges[5] = {0.0L, (LD)gx[4], (LD)gx[5], (LD)gx[6], 1.0L};
+    LD nodes[8];
+    nodes[0] = 0.0L;
+    for (int r = 0; r < 4; ++r) {
+        LD lo = edges[r], hi = edges[r + 1];
+        const bool neg_lo = E8(lo) < 0;
+        for (int it = 0; it < 128; ++it) {
+            const LD mid = 0.5L * (lo + hi);
+            if ((E8(mid) < 0) == neg_lo) lo = mid;
+            else hi = mid;
+        }
+        nodes[2 * r + 1] = 0.5L * (lo + hi);
+        if (r < 3) nodes[2 * r + 2] = (LD)gx[4 + r];
+    }
+    // weights: w0 [m == 0] + 2 sum_i w_i x_i^(2m) = 2 / (2m + 1), m = 0..7
+    LD W[8][9];
+    for (int m = 0; m < 8; ++m) {
+        for (int t = 0; t < 8; ++t) W[m][t] = t == 0 ? (m == 0 ? 1.0L : 0.0L) : 2.0L * powl(nodes[t], 2 * m);
+        W[m][8] = 2.0L / (2 * m + 1);
+    }
+    for (int col = 0; col < 8; ++col) {
+        int piv = col;
+        for (int r = col + 1; r < 8; ++r)
+            if (fabsl(W[r][col]) > fabsl(W[piv][col])) piv = r;
+        for (int t = 0; t < 9; ++t) std::swap(W[col][t], W[piv][t]);
+        for (int r = 0; r < 8; ++r) {
+            if (r == col) continue;
+            const LD f = W[r][col] / W[col][col];
+            for (int t = col; t < 9; ++t) W[r][t] -= f * W[col][t];
+        }
+    }
+    IkGK g;
+    for (int t = 0; t < 8; ++t) {
+        g.x[t] = (double)nodes[t];
+        g.wk[t] = (double)(W[t][8] / W[t][t]);
+    }
+    for (int t = 0; t < 4; ++t) g.wg[t] = gw[3 + t];
+    return g;
+}
+static const IkGK& gk15()
+{
+    static const IkGK g = make_gk15();
+    return g;
+}
+
 int check_ctx(ik_ctx* c)
 {
     if (!c) return fail(IK_ERR_ARG, "null context");
@@ -422,6 +509,11 @@ int mode_ok(ik_ctx* c, int precision)
     if (c->cg.mode == IK_QUAD_FIXEDPOINT) return IK_OK;
     if (c->cg.mode == IK_QUAD_EXACT) {
         if (precision != IK_PREC_FP64) return fail(IK_ERR_UNSUPPORTED, "the exact bond integral runs on the FP64 path");
+        return IK_OK;
+    }
+    if (c->cg.mode == IK_QUAD_ADAPTIVE) {
+        if (precision != IK_PREC_FP64)
+            return fail(IK_ERR_UNSUPPORTED, "the adaptive bond integral runs on the FP64 path");
         return IK_OK;
     }
     if (c->cg.mode == IK_QUAD_MLP) {
@@ -671,6 +763,8 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         }
         a.nq = c->gl.n;
         for (int k = 0; k < c->gl.n; ++k) { a.xs[k] = 0.5 + 0.5 * c->gl.x[k]; a.ws[k] = c->gl.w[k]; }
+        a.gk = gk15();
+        a.status = c->status.as<int>();
         a.sorted = L.sorted.as<int>();
         a.cell_start = L.cell_start.as<int>();
         a.pos = s.pos.as<double>();
@@ -758,6 +852,15 @@ int prepare_enqueue(ik_ctx* c, int slot, int prec, int fields)
 // Lets entry points defined in other translation units report through ik_last_error().
 void ik_internal_set_error(const char* msg) { g_err = msg; }
 void ik_gl_rule(int n, double* x, double* w) { gl_rule(n, x, w); }
+
+int ik_gk15_rule(double x[8], double wk[8], double wg[4])
+{
+    if (!x || !wk || !wg) return fail(IK_ERR_ARG, "null output");
+    const IkGK& g = gk15();
+    for (int k = 0; k < 8; ++k) { x[k] = g.x[k]; wk[k] = g.wk[k]; }
+    for (int k = 0; k < 4; ++k) wg[k] = g.wg[k];
+    return IK_OK;
+}
 
 // ===========================================================================
 extern "C" {
@@ -1302,6 +1405,11 @@ int ik_synchronize(ik_ctx* c)
             grow = true;
         }
         if (st & IK_ST_MMA_TIMEOUT) { c->pending.clear(); return fail(IK_ERR_TIMEOUT, "a tensor-core wait gave up"); }
+        if (st & IK_ST_QUAD_FAIL) {
+            c->pending.clear();
+            return fail(IK_ERR_QUADRATURE, "adaptive bond integral: tolerance not met within %d subintervals",
+                        std::min(std::max(c->cg.neval, 1), IK_QAG_MAXSUB));
+        }
         if (st & IK_ST_MLP_OVERFLOW) {
             if (c->mlp_cap >= (1LL << 31)) { c->pending.clear(); return fail(IK_ERR_CAPACITY, "surrogate record buffer cannot grow"); }
             c->mlp_cap *= 2;
@@ -1544,8 +1652,6 @@ int ik_eval_bond(ik_ctx* c, int64_t m, const double* x, const double* ri, const 
 {
     if (int r = check_ctx(c)) return r;
     if (!c->cg_set) return fail(IK_ERR_STATE, "coarse-graining function not set");
-    if (c->cg.mode == IK_QUAD_ADAPTIVE) // GL-n, the surrogate's fallback GL-n, or the exact integral
-        return fail(IK_ERR_UNSUPPORTED, "quadrature mode %d is not available on the GPU path yet", c->cg.mode);
     if (m < 0 || (m > 0 && (!x || !ri || !rij || !bond || !delta))) return fail(IK_ERR_ARG, "bad arguments");
     if (m == 0) return IK_OK;
     DevBuf b;
@@ -1556,11 +1662,17 @@ int ik_eval_bond(ik_ctx* c, int64_t m, const double* x, const double* ri, const 
     CK(cudaMemcpyAsync(d + 6 * m, rij, sizeof(double) * 3 * m, cudaMemcpyHostToDevice, c->stream));
     double xs[64], ws[64];
     for (int k = 0; k < c->gl.n; ++k) { xs[k] = 0.5 + 0.5 * c->gl.x[k]; ws[k] = c->gl.w[k]; }
-    CK(launch_eval_bond(c->cg, c->dim ? c->dim : 2, xs, ws, c->gl.n, (int)m, d, d + 3 * m, d + 6 * m, d + 9 * m,
-                        d + 10 * m, c->stream));
+    CK(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->stream));
+    CK(launch_eval_bond(c->cg, c->dim ? c->dim : 2, xs, ws, c->gl.n, gk15(), c->status.as<int>(), (int)m, d,
+                        d + 3 * m, d + 6 * m, d + 9 * m, d + 10 * m, c->stream));
     CK(cudaMemcpyAsync(bond, d + 9 * m, sizeof(double) * m, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(delta, d + 10 * m, sizeof(double) * m, cudaMemcpyDeviceToHost, c->stream));
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, c->status.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    if (st & IK_ST_QUAD_FAIL)
+        return fail(IK_ERR_QUADRATURE, "adaptive bond integral: tolerance not met within %d subintervals",
+                    std::min(std::max(c->cg.neval, 1), IK_QAG_MAXSUB));
     return IK_OK;
 }
 

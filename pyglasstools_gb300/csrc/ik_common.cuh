@@ -16,6 +16,9 @@
 #define IK_ST_BAD_INPUT     4
 #define IK_ST_NEIGH_OVERFLOW 8
 #define IK_QUAD_EXACT_DEV 2 /* IK_QUAD_EXACT of the C ABI */
+#define IK_QUAD_ADAPTIVE_DEV 1 /* IK_QUAD_ADAPTIVE of the C ABI */
+#define IK_ST_QUAD_FAIL     64  /* an adaptive bond integral missed its tolerance within its subintervals */
+#define IK_QAG_MAXSUB       64  /* subintervals one adaptive bond integral may hold on the device */
 #define IK_ST_MMA_TIMEOUT   16  /* a tensor-core completion wait gave up */
 #define IK_ST_MLP_OVERFLOW  32  /* the surrogate record buffer overflowed */
 
@@ -68,6 +71,13 @@ struct IkCG {
     // adaptive
     int neval;
     double relerr, abserr;
+};
+
+// Gauss-Kronrod 7/15 rule on [-1, 1]: x[0] = 0, x[1..7] the positive nodes ascending
+// (Kronrod nodes at odd slots, the 7-point Gauss nodes at even slots), Kronrod weights
+// wk[8], Gauss weights wg[4] of the nodes 0, x[2], x[4], x[6].
+struct IkGK {
+    double x[8], wk[8], wg[4];
 };
 
 // GL nodes on [-1,1] (ascending) and weights, FP64 + FP32 copies (max 64 points).

@@ -52,10 +52,96 @@ __device__ double ik_bond64_exact(const IkCG& cg, const double* xs, const double
     return 0.5 * acc * (s1 - s0);
 }
 
+// Integrand of the bond integral: Delta(|x - (r_i + s r_ij)|^2)
+// (CoarseGrainFunction::getObjFunc, cgfunc/CoarseGrainFunction.h:42-48).
+__device__ __forceinline__ double ik_obj64(const IkCG& cg, const double x[3], const double ri[3],
+                                           const double rij[3], double s)
+{
+    const double p0 = ri[0] + s * rij[0], p1 = ri[1] + s * rij[1], p2 = ri[2] + s * rij[2];
+    const double d0 = x[0] - p0, d1 = x[1] - p1, d2 = x[2] - p2;
+    return ik_delta64(cg, d0 * d0 + d1 * d1 + d2 * d2);
+}
+
+// One Gauss-Kronrod 7/15 application on [a, b] with the QUADPACK error estimate
+// (Piessens et al. 1983): |K15 - G7| scaled by (200 |K15 - G7| / asc)^1.5, bounded below
+// by 50 eps times the integral of |f|.
+__device__ double ik_gk15(const IkCG& cg, const IkGK& gk, const double x[3], const double ri[3],
+                          const double rij[3], double a, double b, double* err)
+{
+    const double c = 0.5 * (a + b), h = 0.5 * (b - a);
+    const double fc = ik_obj64(cg, x, ri, rij, c);
+    double rk = fc * gk.wk[0], rg = 0.0, rabs = fabs(rk);
+    double f1[8], f2[8];
+#pragma unroll
+    for (int i = 1; i < 8; ++i) {
+        f1[i] = ik_obj64(cg, x, ri, rij, c - h * gk.x[i]);
+        f2[i] = ik_obj64(cg, x, ri, rij, c + h * gk.x[i]);
+        rk += gk.wk[i] * (f1[i] + f2[i]);
+        rabs += gk.wk[i] * (fabs(f1[i]) + fabs(f2[i]));
+        if (i % 2 == 0) rg += gk.wg[i / 2] * (f1[i] + f2[i]);
+    }
+    rg += gk.wg[0] * fc;
+    const double mean = 0.5 * rk;
+    double rasc = gk.wk[0] * fabs(fc - mean);
+#pragma unroll
+    for (int i = 1; i < 8; ++i) rasc += gk.wk[i] * (fabs(f1[i] - mean) + fabs(f2[i] - mean));
+    double e = fabs((rk - rg) * h);
+    rasc *= fabs(h);
+    rabs *= fabs(h);
+    if (rasc != 0.0 && e != 0.0) e = rasc * fmin(pow(200.0 * e / rasc, 1.5), 1.0);
+    const double eps = 2.220446049250313e-16;
+    if (rabs > 2.2250738585072014e-308 / (50.0 * eps)) e = fmax(e, 50.0 * eps * rabs);
+    *err = e;
+    return rk * h;
+}
+
+// AdaptiveCGFunc::getBondFunc (cgfunc/CoarseGrainFunction.h:124-127): gsl_integration_qag
+// with key 1 (GK15) on [0, 1] to max(abserr, relerr |B|), at most neval subintervals
+// (cgfunc/Quadrature.h:47-49).  Strategy of QUADPACK's QAG: bisect the subinterval with
+// the largest error estimate, sums recomputed in subinterval order.  Subintervals live in
+// the thread's local memory (at most IK_QAG_MAXSUB); a tolerance missed when they run out
+// sets IK_ST_QUAD_FAIL (the reference's GSL error handler would abort there).
+__device__ double ik_bond64_qag(const IkCG& cg, const IkGK& gk, const double x[3], const double ri[3],
+                                const double rij[3], int* status)
+{
+    double ia[IK_QAG_MAXSUB], ib[IK_QAG_MAXSUB], ir[IK_QAG_MAXSUB], ie[IK_QAG_MAXSUB];
+    const int limit = cg.neval < 1 ? 1 : (cg.neval > IK_QAG_MAXSUB ? IK_QAG_MAXSUB : cg.neval);
+    int n = 1;
+    ia[0] = 0.0;
+    ib[0] = 1.0;
+    ir[0] = ik_gk15(cg, gk, x, ri, rij, 0.0, 1.0, &ie[0]);
+    double res = ir[0], err = ie[0];
+    bool done = false;
+    while (n < limit) {
+        if (err <= fmax(cg.abserr, cg.relerr * fabs(res))) { done = true; break; }
+        int worst = 0;
+        for (int k = 1; k < n; ++k)
+            if (ie[k] > ie[worst]) worst = k;
+        const double a1 = ia[worst], b2 = ib[worst], m = 0.5 * (a1 + b2);
+        double e1, e2;
+        const double r1 = ik_gk15(cg, gk, x, ri, rij, a1, m, &e1);
+        const double r2 = ik_gk15(cg, gk, x, ri, rij, m, b2, &e2);
+        ib[worst] = m; ir[worst] = r1; ie[worst] = e1;
+        ia[n] = m; ib[n] = b2; ir[n] = r2; ie[n] = e2;
+        ++n;
+        res = 0.0;
+        err = 0.0;
+        for (int k = 0; k < n; ++k) { res += ir[k]; err += ie[k]; }
+        if (m <= a1 || m >= b2) { done = true; break; } // interval exhausted
+    }
+    if (!done && !(err <= fmax(cg.abserr, cg.relerr * fabs(res)))) atomicOr(status, IK_ST_QUAD_FAIL);
+    return res;
+}
+
+// ADAPT: the instantiation that carries the adaptive mode (its subinterval arrays cost
+// local memory and registers the other modes do not pay).
+template <bool ADAPT>
 __device__ __forceinline__ double ik_bond64(const IkCG& cg, const double* xs, const double* ws, int nq,
-                                            const double x[3], const double ri[3], const double rij[3])
+                                            const IkGK& gk, int* status, const double x[3], const double ri[3],
+                                            const double rij[3])
 {
     if (cg.mode == IK_QUAD_EXACT_DEV) return ik_bond64_exact(cg, xs, ws, nq, x, ri, rij);
+    if (ADAPT && cg.mode == IK_QUAD_ADAPTIVE_DEV) return ik_bond64_qag(cg, gk, x, ri, rij, status);
     double acc = 0.0;
     for (int k = 0; k < nq; ++k) {
         double s = xs[k];
@@ -66,7 +152,7 @@ __device__ __forceinline__ double ik_bond64(const IkCG& cg, const double* xs, co
     return 0.5 * acc;
 }
 
-template <int DIM>
+template <int DIM, bool ADAPT>
 __global__ void __launch_bounds__(128) k_gather64(const GatherArgs64 a)
 {
     constexpr int NC = DIM == 2 ? 3 : 6;
@@ -124,7 +210,7 @@ __global__ void __launch_bounds__(128) k_gather64(const GatherArgs64 a)
                     for (int k = 0; k < nbq; ++k) {
                         IkB64 b = bq[k];
                         double rij[3] = {b.x, b.y, b.z};
-                        double bond = ik_bond64(a.cg, a.xs, a.ws, a.nq, x, ri, rij);
+                        double bond = ik_bond64<ADAPT>(a.cg, a.xs, a.ws, a.nq, a.gk, a.status, x, ri, rij);
                         if (a.ecoef) { // elastic field: precomputed coefficients (0.5 included)
                             const double* cc = a.ecoef + ((size_t)q * a.maxb + k) * NC;
 #pragma unroll
@@ -159,8 +245,9 @@ cudaError_t launch_gather64(const GatherArgs64& a, cudaStream_t st)
     int threads = 128;
     int blocks = (int)((a.ngrid + threads - 1) / threads);
     if (blocks == 0) return cudaSuccess;
-    if (a.g.dim == 2) k_gather64<2><<<blocks, threads, 0, st>>>(a);
-    else k_gather64<3><<<blocks, threads, 0, st>>>(a);
+    const bool adapt = a.cg.mode == IK_QUAD_ADAPTIVE_DEV;
+    if (a.g.dim == 2) adapt ? k_gather64<2, true><<<blocks, threads, 0, st>>>(a) : k_gather64<2, false><<<blocks, threads, 0, st>>>(a);
+    else adapt ? k_gather64<3, true><<<blocks, threads, 0, st>>>(a) : k_gather64<3, false><<<blocks, threads, 0, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -168,6 +255,8 @@ struct EvalBondArgs {
     IkCG cg;
     int nq;
     double xs[64], ws[64];
+    IkGK gk;
+    int* status;
 };
 
 __global__ void k_eval_bond(const EvalBondArgs a, int m, const double* __restrict__ x,
@@ -179,19 +268,21 @@ __global__ void k_eval_bond(const EvalBondArgs a, int m, const double* __restric
     double xx[3] = {x[3 * k], x[3 * k + 1], x[3 * k + 2]};
     double rr[3] = {ri[3 * k], ri[3 * k + 1], ri[3 * k + 2]};
     double bb[3] = {rij[3 * k], rij[3 * k + 1], rij[3 * k + 2]};
-    bond[k] = ik_bond64(a.cg, a.xs, a.ws, a.nq, xx, rr, bb);
+    bond[k] = ik_bond64<true>(a.cg, a.xs, a.ws, a.nq, a.gk, a.status, xx, rr, bb);
     double e0 = xx[0] - rr[0], e1 = xx[1] - rr[1], e2 = xx[2] - rr[2];
     delta[k] = ik_delta64(a.cg, e0 * e0 + e1 * e1 + e2 * e2);
 }
 
-cudaError_t launch_eval_bond(const IkCG& cg, int dim, const double* xs, const double* ws, int nq, int m,
-                             const double* x, const double* ri, const double* rij, double* bond,
-                             double* delta, cudaStream_t st)
+cudaError_t launch_eval_bond(const IkCG& cg, int dim, const double* xs, const double* ws, int nq,
+                             const IkGK& gk, int* status, int m, const double* x, const double* ri,
+                             const double* rij, double* bond, double* delta, cudaStream_t st)
 {
     (void)dim;
     EvalBondArgs a;
     a.cg = cg;
     a.nq = nq;
+    a.gk = gk;
+    a.status = status;
     for (int k = 0; k < nq && k < 64; ++k) { a.xs[k] = xs[k]; a.ws[k] = ws[k]; }
     int threads = 128, blocks = (m + threads - 1) / threads;
     if (blocks == 0) return cudaSuccess;

@@ -112,6 +112,8 @@ struct GatherArgs64 {
     int all[3];
     int nq;
     double xs[64], ws[64];  // GL nodes mapped to [0,1] (s) and their [-1,1] weights
+    IkGK gk;                // adaptive mode: the GK15 rule
+    int* status;            // adaptive mode: IK_ST_QUAD_FAIL on a missed tolerance
     const int* sorted;
     const int* cell_start;
     const double* pos;
@@ -131,8 +133,8 @@ cudaError_t launch_gather64(const GatherArgs64& a, cudaStream_t st);
 
 // ---- scalar bond evaluations (ik_gather64.cu) ------------------------------
 cudaError_t launch_eval_bond(const IkCG& cg, int dim, const double* xs, const double* ws, int nq,
-                             int m, const double* x, const double* ri, const double* rij, double* bond,
-                             double* delta, cudaStream_t st);
+                             const IkGK& gk, int* status, int m, const double* x, const double* ri,
+                             const double* rij, double* bond, double* delta, cudaStream_t st);
 
 // ---- global thermodynamic observables (ik_cells.cu) --------------------------
 // per-block partials (nblocks x ik_thermo_nq(dim)) -> out[ik_thermo_nq(dim)] =

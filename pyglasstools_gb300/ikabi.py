@@ -16,7 +16,8 @@ LIB_PATH = os.path.join(_HERE, "libik_gb300.so")
 
 IK_OK = 0
 ERR = {-1: "IK_ERR_ARG", -2: "IK_ERR_CUDA", -3: "IK_ERR_STATE", -4: "IK_ERR_BOX",
-       -5: "IK_ERR_CAPACITY", -6: "IK_ERR_TIMEOUT", -7: "IK_ERR_NOMEM", -8: "IK_ERR_UNSUPPORTED"}
+       -5: "IK_ERR_CAPACITY", -6: "IK_ERR_TIMEOUT", -7: "IK_ERR_NOMEM", -8: "IK_ERR_UNSUPPORTED",
+       -9: "IK_ERR_QUADRATURE"}
 CG = {"octic": 0, "gaussian": 1, "rect": 2, "mollifier": 3}
 QUAD = {"fixedpoint": 0, "adaptive": 1, "exact": 2, "mlp": 3}
 PREC = {"fp64": 0, "fp32": 1}
@@ -53,6 +54,7 @@ def lib():
             "ik_set_potential": ([vp, i32, C.c_double, dp, i32], i32),
             "ik_potential_nparams": ([i32], i32),
             "ik_compute_thermo": ([vp, i32, dp, i64], i32),
+            "ik_gk15_rule": ([dp, dp, dp], i32),
             "ik_set_cgfunc": ([vp, i32, i32, i32, C.c_double, C.c_double], i32),
             "ik_set_adaptive": ([vp, i32, C.c_double, C.c_double], i32),
             "ik_set_max_rcut": ([vp, C.c_double], i32),
@@ -174,6 +176,10 @@ class IKContext:
 
     def set_cgfunc(self, kind, rcut, mode="fixedpoint", order=5, width=0.0):
         check(lib().ik_set_cgfunc(self._h, CG[kind], QUAD[mode], order, rcut, width))
+
+    def set_adaptive(self, neval, relerr, abserr):
+        """Tolerances of the adaptive bond integral (AdaptiveCGFunc(neval, relerr, abserr, rcut))."""
+        check(lib().ik_set_adaptive(self._h, int(neval), float(relerr), float(abserr)))
 
     def set_max_rcut(self, r):
         check(lib().ik_set_max_rcut(self._h, r))

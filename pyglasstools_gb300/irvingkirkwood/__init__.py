@@ -1,10 +1,11 @@
 R"""Irving-Kirkwood coarse-grained fields (pyglasstools/irvingkirkwood/__init__.py).
 
-``ikcalculator(cgfunc, dx, precision="fp32")`` builds the reference's lattice grid
+``ikcalculator(cgfunc, dx, precision=None)`` builds the reference's lattice grid
 (linspace(-L/2, L/2, int(L/dx)) per axis, endpoints included) and computes the
-registered fields on the GPU.  ``precision="fp64"`` selects the plain FP64 kernels;
-the default "fp32" is the tuned path (FP32 pair arithmetic, compensated
-accumulation, FP64 selection and final sums).
+registered fields on the GPU.  ``precision="fp64"`` selects the plain FP64 kernels,
+"fp32" the tuned path (FP32 pair arithmetic, compensated accumulation, FP64 selection
+and final sums); the default is "fp32", or "fp64" for an adaptive or exact bond
+integral (those run on the FP64 path).
 """
 import numpy as np
 
@@ -46,8 +47,15 @@ def lattice_gridpoints(L, dx, dim=2):
     return np.stack([gx.ravel(), gy.ravel(), gz.ravel()], axis=1)
 
 
+def _default_precision(cgfunc, precision):
+    """FP32 (the tuned path) unless the bond integral is adaptive or exact (FP64 path)."""
+    if precision is not None:
+        return precision
+    return "fp64" if cgfunc._getCGFunc().mode in ("adaptive", "exact") else "fp32"
+
+
 class ikcalculator(object):
-    def __init__(self, cgfunc, dx, precision="fp32"):
+    def __init__(self, cgfunc, dx, precision=None):
         self.cgfunc = cgfunc
         self.manager = _core._pyglasstools.Manager()
         self.coordmode = "cartesian"
@@ -58,7 +66,7 @@ class ikcalculator(object):
         self.calculator = _irvingkirkwood.IrvingKirkwood(
             sysdata.cppparticledata, pyglasstools_gb300.get_potential().cpppairpotential,
             cgfunc._getCGFunc(), comm)
-        self.calculator.setPrecision(precision)
+        self.calculator.setPrecision(_default_precision(cgfunc, precision))
         solvers_list.append(self)
 
     def add_observables(self, observables):
@@ -104,7 +112,7 @@ class radialcalculator(object):
     same IrvingKirkwood computation as ikcalculator, on these grid points."""
 
     def __init__(self, cgfunc, center=np.array([0, 0, 0]), spacingtype="normal", rmax=10, rmin=0, dr=0.1,
-                 dlnr=0.05, precision="fp32"):
+                 dlnr=0.05, precision=None):
         self.cgfunc = cgfunc
         self.manager = _core._pyglasstools.Manager()
         self.coordmode = "polar"
@@ -116,7 +124,7 @@ class radialcalculator(object):
         self.calculator = _irvingkirkwood.IrvingKirkwood(
             sysdata.cppparticledata, pyglasstools_gb300.get_potential().cpppairpotential,
             cgfunc._getCGFunc(), comm)
-        self.calculator.setPrecision(precision)
+        self.calculator.setPrecision(_default_precision(cgfunc, precision))
         solvers_list.append(self)
 
     def set_center(self, center):

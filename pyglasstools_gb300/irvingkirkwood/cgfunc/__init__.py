@@ -70,9 +70,16 @@ class gaussian(basecgfunc):
     R"""(2 pi w^2)^(-dim/2) exp(-r^2/(2 w^2)) for r < cut*w (new)."""
 
     def __init__(self, width=2.0, cut=3.0, mode="fixedpoint", **kwargs):
-        if mode != "fixedpoint":
-            raise NameError("gaussian: only mode='fixedpoint' is available")
-        order = int(kwargs.get("order", 5))
-        self.cgfunc = _cgfunc.CGFuncGaussianFixedPoint(order, float(width), float(cut))
+        if mode == "fixedpoint":
+            order = int(kwargs.get("order", 5))
+            self.cgfunc = _cgfunc.CGFuncGaussianFixedPoint(order, float(width), float(cut))
+        elif mode == "adaptive":
+            for k in ("relerr", "abserr", "maxiter"):
+                if k not in kwargs:
+                    raise TypeError(f"mode='adaptive' needs {k}=")
+            self.cgfunc = _cgfunc.CGFuncGaussianAdaptive(int(kwargs["maxiter"]), float(kwargs["relerr"]),
+                                                         float(kwargs["abserr"]), float(width), float(cut))
+        else:
+            raise NameError("Coarse-graining mode not recognized: 'fixedpoint' and 'adaptive' are available")
         self.width = width
         self.cut = cut

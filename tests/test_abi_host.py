@@ -250,3 +250,24 @@ def test_polar_grid_matches_reference_recipe():
         k += n
     pl, _, rl, _ = polar_gridpoints((0, 0, 0), "log", rmax=4.0, rmin=0.5, dlnr=0.1)
     assert np.allclose(np.unique(rl[1:]), np.exp(np.linspace(np.log(0.5), np.log(4.0), int(np.log(8.0) / 0.1))))
+
+
+def test_product_gk15_rule_exact_and_equal_to_oracle(oracle):
+    """The adaptive mode's GK15 rule (computed by the library on the host): exact to
+    degree 22, Gauss-7 embedded, equal to the oracle's independent construction."""
+    from pyglasstools_gb300 import ikabi
+    import ctypes as C
+    x, wk, wg = np.zeros(8), np.zeros(8), np.zeros(4)
+    dp = C.POINTER(C.c_double)
+    assert ikabi.lib().ik_gk15_rule(x.ctypes.data_as(dp), wk.ctypes.data_as(dp), wg.ctypes.data_as(dp)) == 0
+    xs = np.concatenate([-x[:0:-1], x])
+    ws = np.concatenate([wk[:0:-1], wk])
+    for k in range(23):
+        exact = 2.0 / (k + 1) if k % 2 == 0 else 0.0
+        assert abs(np.sum(ws * xs ** k) - exact) < 1e-14
+    gx, gw = oracle.gl_rule(7)
+    np.testing.assert_allclose(x[[0, 2, 4, 6]], gx[3:], atol=1e-15)
+    np.testing.assert_allclose(wg, gw[3:], atol=1e-15)
+    ox, owk, owg = oracle.gk15_rule()
+    np.testing.assert_allclose(x, ox, rtol=0, atol=2e-16)
+    np.testing.assert_allclose(wk, owk, rtol=0, atol=2e-16)
