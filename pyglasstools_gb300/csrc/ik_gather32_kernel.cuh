@@ -161,6 +161,34 @@ __device__ __forceinline__ void ik_warp_reduce_cmp(float (&hi)[V], float (&lo)[V
         }
     }
 }
+// The same transposing butterfly with plain FP32 adds (index mapping as above).  The
+// per-lane partial sums already carry the rounding of their own accumulation, which a
+// compensated combination of 32 partials does not remove; the plain tree adds the
+// rounding of 5 adds per value to the ~(terms per lane) adds each lane made.
+template <int V>
+__device__ __forceinline__ void ik_warp_reduce_plain(float (&hi)[V], int lane)
+{
+#pragma unroll
+    for (int lev = 0; lev < 5; ++lev) {
+        const int o = 16 >> lev;
+        const int cur = (V >> lev) > 1 ? (V >> lev) : 1;
+        if (cur > 1) {
+            const int half = cur >> 1;
+            const bool up = (lane & o) != 0;
+#pragma unroll
+            for (int k = 0; k < V / 2; ++k) {
+                if (k < half) {
+                    const float sh = up ? hi[k] : hi[k + half];
+                    const float kh = up ? hi[k + half] : hi[k];
+                    hi[k] = kh + __shfl_xor_sync(FULL, sh, o);
+                }
+            }
+        } else {
+            hi[0] += __shfl_xor_sync(FULL, hi[0], o);
+        }
+    }
+}
+
 template <int V>
 __device__ __forceinline__ int ik_red_index(int lane, int k)
 {
@@ -638,9 +666,10 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                 }
                 __syncwarp();
 
-                // ---- combine lanes (compensated): virial, then kinetic, each a
-                //      transposing butterfly of VH values; results are written as
-                //      unscaled double-float pairs (hi, lo), converted to FP64 later
+                // ---- combine lanes: virial, then kinetic, each a transposing butterfly
+                //      of VH values (compensated in the Kahan variant); results are
+                //      written as unscaled double-float pairs (hi, lo), merged across
+                //      chunks of an item with TwoSum, converted to FP64 later
                 if constexpr (!KAHAN && NP > 0) {
 #pragma unroll
                     for (int j = 0; j < P / 2; ++j)
@@ -661,8 +690,13 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                     }
 #pragma unroll
                 for (int k = P * NC; k < VH; ++k) { vh[k] = vl[k] = kh[k] = kl[k] = 0.f; }
-                ik_warp_reduce_cmp<VH>(vh, vl, lane);
-                ik_warp_reduce_cmp<VH>(kh, kl, lane);
+                if constexpr (KAHAN) { // compensated lanes: compensated combination too
+                    ik_warp_reduce_cmp<VH>(vh, vl, lane);
+                    ik_warp_reduce_cmp<VH>(kh, kl, lane);
+                } else {
+                    ik_warp_reduce_plain<VH>(vh, lane);
+                    ik_warp_reduce_plain<VH>(kh, lane);
+                }
                 // VH == 16: lanes 2k and 2k+1 both hold value k -> the even lane writes
                 // the virial, the odd lane the kinetic value; VH == 32: one value per lane
 #pragma unroll
