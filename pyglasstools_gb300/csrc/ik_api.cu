@@ -843,7 +843,7 @@ int prepare_enqueue(ik_ctx* c, int slot, int prec, int fields)
     if (int r = mode_ok(c, prec)) return r;
     if (int r = ensure_geometry(c)) return r;
     if (c->maxb == 0) c->maxb = c->dim == 2 ? IK_MAXB_2D : IK_MAXB_3D;
-    if (c->halo_cap == 0) c->halo_cap = c->dim == 2 ? 512 : 768;
+    if (c->halo_cap == 0) c->halo_cap = c->dim == 2 ? 384 : 768; // staged particles per warp (grows on overflow)
     return enqueue(c, slot, prec, fields);
 }
 
@@ -1300,7 +1300,7 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
         if (int r = ensure_geometry(c)) return r;
     }
     if (c->maxb == 0) c->maxb = c->dim == 2 ? IK_MAXB_2D : IK_MAXB_3D;
-    if (c->halo_cap == 0) c->halo_cap = c->dim == 2 ? 512 : 768;
+    if (c->halo_cap == 0) c->halo_cap = c->dim == 2 ? 384 : 768; // staged particles per warp (grows on overflow)
     std::vector<int> key(slots, slots + count);
     const bool reuse = c->batch_exec && key == c->batch_slots && c->batch_prec == precision &&
                        c->batch_fields == fields && c->batch_maxb == c->maxb && c->batch_halo == c->halo_cap &&
@@ -1416,8 +1416,11 @@ int ik_synchronize(ik_ctx* c)
             grow = true;
         }
         if (st & IK_ST_HALO_OVERFLOW) {
-            if (c->halo_cap >= 8192) { c->pending.clear(); return fail(IK_ERR_CAPACITY, "a cell holds more particles than the halo buffer"); }
-            c->halo_cap *= 2;
+            // the per-warp stage lives in the CTA's dynamic shared memory (227 KB at most)
+            const int qcap = 32 * (std::min(std::max(c->maxb, c->maxbe), 63) + 1);
+            const int limit = (int)((227 * 1024 / IK_WARPS_GATHER - 4 * qcap - 64) / 20) & ~31;
+            if (c->halo_cap >= limit) { c->pending.clear(); return fail(IK_ERR_CAPACITY, "a cell holds more particles than the halo buffer (%d)", c->halo_cap); }
+            c->halo_cap = std::min(2 * c->halo_cap, limit);
             grow = true;
         }
         if (!grow) { c->pending.clear(); return fail(IK_ERR_CUDA, "device status 0x%x", st); }
@@ -1699,7 +1702,7 @@ int ik_set_tuning(ik_ctx* c, int param, int value)
         c->tune_blocks_per_sm = value;
         return IK_OK;
     case IK_TUNE_HALO_CAP:
-        if (value < 0 || value > 8192) return fail(IK_ERR_ARG, "halo capacity must be in [0, 8192]");
+        if (value < 0 || value > 1024) return fail(IK_ERR_ARG, "halo capacity must be in [0, 1024]");
         c->halo_cap = value;
         return IK_OK;
     default:
