@@ -843,7 +843,7 @@ int prepare_enqueue(ik_ctx* c, int slot, int prec, int fields)
     if (int r = mode_ok(c, prec)) return r;
     if (int r = ensure_geometry(c)) return r;
     if (c->maxb == 0) c->maxb = c->dim == 2 ? IK_MAXB_2D : IK_MAXB_3D;
-    if (c->halo_cap == 0) c->halo_cap = c->dim == 2 ? 384 : 768; // staged particles per warp (grows on overflow)
+    if (c->halo_cap == 0) c->halo_cap = 384; // staged particles per warp (grows on overflow)
     return enqueue(c, slot, prec, fields);
 }
 
@@ -1300,7 +1300,7 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
         if (int r = ensure_geometry(c)) return r;
     }
     if (c->maxb == 0) c->maxb = c->dim == 2 ? IK_MAXB_2D : IK_MAXB_3D;
-    if (c->halo_cap == 0) c->halo_cap = c->dim == 2 ? 384 : 768; // staged particles per warp (grows on overflow)
+    if (c->halo_cap == 0) c->halo_cap = 384; // staged particles per warp (grows on overflow)
     std::vector<int> key(slots, slots + count);
     const bool reuse = c->batch_exec && key == c->batch_slots && c->batch_prec == precision &&
                        c->batch_fields == fields && c->batch_maxb == c->maxb && c->batch_halo == c->halo_cap &&
