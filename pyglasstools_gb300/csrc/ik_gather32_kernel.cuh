@@ -579,23 +579,28 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                             k0 = __ldg(a.kin + (DIM == 2 ? q : 2 * q));
                             if (DIM == 3) k1 = __ldg(a.kin + 2 * q + 1);
                         }
+                        // inside: r2 - R2s < 0 (the sign of an exact-zero-free difference);
+                        // band: (r2 - R2s)^2 < margin^2.  Padding points sit at 1e18: never
+                        // inside, never in the band.
                         float r2v[P];
+                        int band = 0;
                         {
                             const f32x2 sx = pk2(sp.x, sp.x), sy = pk2(sp.y, sp.y), sz = pk2(sp.z, sp.z);
+                            const f32x2 R2p = pk2(R2s, R2s), nM2 = pk2(-margin * margin, -margin * margin);
 #pragma unroll
                             for (int j = 0; j < P / 2; ++j) {
                                 const f32x2 dx = sub2(g2[j][0], sx), dy = sub2(g2[j][1], sy);
                                 f32x2 r2 = fma2(dy, dy, mul2(dx, dx));
                                 if (DIM == 3) { const f32x2 dz = sub2(g2[j][2], sz); r2 = fma2(dz, dz, r2); }
                                 up2(r2, r2v[2 * j], r2v[2 * j + 1]);
+                                const f32x2 d = sub2(r2, R2p);
+                                const f32x2 bd = fma2(d, d, nM2);
+                                float d0, d1, b0, b1;
+                                up2(d, d0, d1);
+                                up2(bd, b0, b1);
+                                mask |= (int)((__float_as_uint(d0) >> 31) | ((__float_as_uint(d1) >> 31) << 1)) << (2 * j);
+                                band |= (int)((__float_as_uint(b0) >> 31) | ((__float_as_uint(b1) >> 31) << 1)) << (2 * j);
                             }
-                        }
-                        int band = 0;
-#pragma unroll
-                        for (int p = 0; p < P; ++p) {
-                            const float r2 = r2v[p];
-                            mask |= (r2 < R2s ? 1 : 0) << p;
-                            band |= (fabsf(r2 - R2s) < margin && gi[p] >= 0 ? 1 : 0) << p;
                         }
                         if (band) { // rare: inside the thin band around R decide with the FP64 rule
                             const IkB64 pq = a.pos64[q];
