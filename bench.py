@@ -9,7 +9,9 @@ kinetic stress.  One step = one pass of the tuned FP32 path over the 64 frames.
   value        frames/s with the frames resident in HBM (cycled: 64 x 4 MB of
                inputs > L2), CUDA events on the engine's stream, max over ranks;
   e2e          frames/s through the C ABI with host buffers: pinned host->device
-               upload of every frame and device->host read of both fields each step;
+               upload of every frame and device->host read of both fields each step
+               (ik_compute_batch_io: copies and kernels of a frame on its lane, one
+               graph per step);
   plain_fp64   frames/s of the plain FP64 GPU kernels (same workload), and the
                tuned path's relative L2 error against them;
   roofline     the FP32 gather kernel: algorithmic FLOPs (66 per active (grid, i, j)
@@ -431,12 +433,21 @@ def ours(args, wl, name):
     hvir = [pin((len(grid), NC)) for _ in range(F)]
     hkin = [pin((len(grid), NC)) for _ in range(F)]
 
+    # one graph per step (ik_compute_batch_io): each frame's upload, kernels and field
+    # downloads on its lane, frames overlapping; the first call records it
+    io_frames = [(hpos[k], hdiam[k], hvel[k], hmass[k]) for k in range(F)]
+    io_outs = [(hvir[k], hkin[k], None) for k in range(F)]
+    io_slots = list(range(F))
+
     def e2e_step():
-        for k in range(F):
-            ctx.upload_frame(k, hpos[k], hdiam[k], hvel[k], hmass[k])
-            ctx.compute_slot(k, "fp32")
-            ctx.download_field_async(hvir[k], ikabi.FIELD_VIRIAL, k)
-            ctx.download_field_async(hkin[k], ikabi.FIELD_KINETIC, k)
+        if args.no_graph:
+            for k in range(F):
+                ctx.upload_frame(k, hpos[k], hdiam[k], hvel[k], hmass[k])
+                ctx.compute_slot(k, "fp32")
+                ctx.download_field_async(hvir[k], ikabi.FIELD_VIRIAL, k)
+                ctx.download_field_async(hkin[k], ikabi.FIELD_KINETIC, k)
+        else:
+            ctx.compute_batch_io(io_slots, io_frames, io_outs)
         ctx.synchronize()
 
     e2e_step()

@@ -203,6 +203,22 @@ int ik_get_timing(ik_ctx* ctx, float* ms4);
  * work against it (e.g. CUDA events recorded on this stream). */
 int ik_get_stream(ik_ctx* ctx, void** stream);
 
+/* One batch with host I/O, replayed as one CUDA graph: for each slots[k], frame k is
+ * copied from page-locked host memory (n[k] particles; pos[k] n x 3 and diam[k] required,
+ * vel[k] n x 3 and mass[k] optional -- vel / mass themselves may be null), computed
+ * (`fields`), and every requested field written to page-locked host memory
+ * out[3k + f] (f = 0 virial, 1 kinetic, 2 elastic; g x NC FP64 as in
+ * ik_download_field_async; null = not copied).  The copies and kernels of a frame run on
+ * one engine lane, so the uploads, computations and downloads of different frames
+ * overlap.  The first call (and any call after a change of slots, sizes, pointers or
+ * settings) runs the plain path and records the graph; later calls replay it, reading the
+ * host inputs' current contents.  Outputs are complete after ik_synchronize (which copies
+ * them again if a capacity growth re-ran a frame).  Slots must be distinct.  Elastic
+ * fields use the displacements of ik_upload_displacement. */
+int ik_compute_batch_io(ik_ctx* ctx, const int* slots, int count, int precision, int fields,
+                        const int64_t* n, const double* const* pos, const double* const* vel,
+                        const double* const* mass, const double* const* diam, double* const* out);
+
 /* Asynchronous download of a slot's field in compact form: g x NC FP64 with
  * NC = 3 (xx, yy, xy) in 2D or 6 (xx, yy, zz, xy, xz, yz) in 3D.  The copy runs on a
  * download stream of its own after the slot's computation, so that it overlaps the

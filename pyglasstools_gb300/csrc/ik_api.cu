@@ -123,7 +123,18 @@ struct Lane {
 };
 constexpr int IK_LANES = 8;
 
-struct PendingOp { int slot, prec, fields; };
+// A computation not yet confirmed by ik_synchronize (re-run after a capacity growth),
+// with the host outputs its fields are being downloaded into (re-issued after a re-run).
+struct PendingOp {
+    int slot, prec, fields;
+    double* out[3] = {nullptr, nullptr, nullptr}; // virial, kinetic, elastic
+};
+
+// Host buffers of one frame of ik_compute_batch_io.
+struct IoFrame {
+    const double *pos = nullptr, *vel = nullptr, *mass = nullptr, *diam = nullptr;
+    double* out[3] = {nullptr, nullptr, nullptr};
+};
 
 } // namespace
 
@@ -174,6 +185,11 @@ struct ik_ctx {
     int64_t geom_version = 0, slot_version = 0, config_version = 0;
     int64_t batch_config_version = -1, batch_alloc_epoch = -1;
     int64_t batch_launches = 0;
+    // CUDA-graph replay of ik_compute_batch_io (copies from and to host inside the graph)
+    cudaGraphExec_t io_exec = nullptr;
+    std::vector<int64_t> io_key;
+    int64_t io_launches = 0;
+    const IoFrame* io_cur = nullptr; // frame whose copies enqueue() adds to its lane
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     int64_t launches = 0;
     float timing[4] = {0, 0, 0, 0};
@@ -574,6 +590,17 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
     const IkGeom& g = c->geo.geom;
     const int D = c->dim, NC = D == 2 ? 3 : 6;
     const int n = (int)s.n;
+    if (c->io_cur && n > 0) { // ik_compute_batch_io: this frame's inputs, copied on its lane
+        const IoFrame& io = *c->io_cur;
+        CK(cudaMemcpyAsync(s.pos.p, io.pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, L.st));
+        CK(cudaMemcpyAsync(s.diam.p, io.diam, sizeof(double) * n, cudaMemcpyHostToDevice, L.st));
+        if (io.vel) CK(cudaMemcpyAsync(s.vel.p, io.vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, L.st));
+        if (io.mass) CK(cudaMemcpyAsync(s.mass.p, io.mass, sizeof(double) * n, cudaMemcpyHostToDevice, L.st));
+        k_validate<<<(n + 255) / 256, 256, 0, L.st>>>(s.pos.as<double>(), s.diam.as<double>(), n, c->dim,
+                                                      c->status.as<int>());
+        CK(cudaGetLastError());
+        c->launches += 1;
+    }
     bool timing = (c->flags & IK_FLAG_TIMING) != 0 && !c->capturing;
     if (timing) CK(cudaEventRecord(c->ev[0], L.st));
     ENS(s.vir, sizeof(double) * NC * c->geo.G);
@@ -798,6 +825,13 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
             c->launches += c->geo.G > 0 ? 1 : 0;
         }
     }
+    if (c->io_cur && c->geo.G > 0) { // ik_compute_batch_io: this frame's fields to the host
+        const DevBuf* src[3] = {&s.vir, &s.kin, &s.ela};
+        for (int f = 0; f < 3; ++f)
+            if (c->io_cur->out[f] && (fields & (1 << f)))
+                CK(cudaMemcpyAsync(c->io_cur->out[f], src[f]->p, sizeof(double) * NC * c->geo.G,
+                                   cudaMemcpyDeviceToHost, L.st));
+    }
     if (timing) CK(cudaEventRecord(c->ev[3], L.st));
     s.last_prec = prec;
     s.last_fields = fields;
@@ -931,6 +965,7 @@ int ik_destroy(ik_ctx* c)
     if (c->d2h) cudaStreamSynchronize(c->d2h);
     for (auto& ev : c->ev) if (ev) cudaEventDestroy(ev);
     if (c->batch_exec) cudaGraphExecDestroy(c->batch_exec);
+    if (c->io_exec) cudaGraphExecDestroy(c->io_exec);
     if (c->fork) cudaEventDestroy(c->fork);
     if (c->d2h_last) cudaEventDestroy(c->d2h_last);
     for (Slot& s : c->slots) {
@@ -1318,6 +1353,7 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
         if (c->flags & IK_FLAG_TIMING) return IK_OK;
         // then capture the same sequence as one graph (lanes fork from and join the main stream)
         if (c->batch_exec) { cudaGraphExecDestroy(c->batch_exec); c->batch_exec = nullptr; }
+        if (c->io_exec) { cudaGraphExecDestroy(c->io_exec); c->io_exec = nullptr; } // versions below are ours now
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
         const int64_t launches_before = c->launches;
         const int64_t epoch_before = g_alloc_epoch.load();
@@ -1373,6 +1409,142 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
     return IK_OK;
 }
 
+static bool host_pinned(const void* p)
+{
+    if (!p) return true;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+int ik_compute_batch_io(ik_ctx* c, const int* slots, int count, int precision, int fields, const int64_t* n,
+                        const double* const* pos, const double* const* vel, const double* const* mass,
+                        const double* const* diam, double* const* out)
+{
+    if (int r = check_ctx(c)) return r;
+    if (count < 1 || !slots || !n || !pos || !diam || !out) return fail(IK_ERR_ARG, "empty batch or null array");
+    if (precision != IK_PREC_FP64 && precision != IK_PREC_FP32) return fail(IK_ERR_ARG, "unknown precision %d", precision);
+    if (fields < 1 || fields > 7) return fail(IK_ERR_ARG, "fields mask must be in [1, 7]");
+    std::vector<IoFrame> fr((size_t)count);
+    std::vector<int64_t> key;
+    key.reserve((size_t)count * 9 + 2);
+    key.push_back(precision);
+    key.push_back(fields);
+    for (int k = 0; k < count; ++k) {
+        if (int r = slot_ok(c, slots[k])) return r;
+        for (int j = 0; j < k; ++j)
+            if (slots[j] == slots[k]) return fail(IK_ERR_ARG, "slot %d appears twice in the batch", slots[k]);
+        if (n[k] < 0 || n[k] >= (1 << 25)) return fail(IK_ERR_ARG, "particle count %lld out of range", (long long)n[k]);
+        IoFrame& f = fr[(size_t)k];
+        f.pos = pos[k];
+        f.diam = diam[k];
+        f.vel = vel ? vel[k] : nullptr;
+        f.mass = mass ? mass[k] : nullptr;
+        for (int q = 0; q < 3; ++q) f.out[q] = (fields & (1 << q)) ? out[3 * k + q] : nullptr;
+        if (n[k] > 0 && (!f.pos || !f.diam)) return fail(IK_ERR_ARG, "frame %d: positions and diameters are required", k);
+        const void* ptrs[7] = {f.pos, f.diam, f.vel, f.mass, f.out[0], f.out[1], f.out[2]};
+        key.push_back(slots[k]);
+        key.push_back(n[k]);
+        for (const void* p : ptrs) key.push_back((int64_t)(intptr_t)p);
+    }
+    if (key != c->io_key) // new buffers: page-locked? (checked once per set of buffers)
+        for (int k = 0; k < count; ++k) {
+            const IoFrame& f = fr[(size_t)k];
+            const void* ptrs[7] = {f.pos, f.diam, f.vel, f.mass, f.out[0], f.out[1], f.out[2]};
+            for (const void* p : ptrs)
+                if (!host_pinned(p)) return fail(IK_ERR_ARG, "frame %d: host buffers must be page-locked", k);
+        }
+    const bool reuse = c->io_exec && key == c->io_key && c->batch_maxb == c->maxb && c->batch_halo == c->halo_cap &&
+                       c->batch_maxbe == c->maxbe && c->batch_geom_version == c->geom_version &&
+                       c->batch_slot_version == c->slot_version && c->batch_config_version == c->config_version &&
+                       c->batch_alloc_epoch == g_alloc_epoch.load() && !(c->flags & IK_FLAG_TIMING);
+    if (!reuse) {
+        // plain path: uploads (sizes every buffer), computations, capacity checks, downloads
+        for (int k = 0; k < count; ++k) {
+            const IoFrame& f = fr[(size_t)k];
+            if (int r = ik_upload_frame(c, slots[k], n[k], f.pos, f.vel, f.mass, f.diam)) return r;
+        }
+        for (int k = 0; k < count; ++k) {
+            c->pending.push_back({slots[k], precision, fields});
+            if (int r = prepare_enqueue(c, slots[k], precision, fields)) return r;
+        }
+        if (int r = ik_synchronize(c)) return r;
+        for (int k = 0; k < count; ++k) {
+            int64_t G = 0;
+            { GeoSwap gs(c, slots[k]); G = c->geo.G; }
+            for (int q = 0; q < 3; ++q)
+                if (fr[(size_t)k].out[q])
+                    if (int r = ik_download_field_async(c, slots[k], 1 << q, fr[(size_t)k].out[q], G * (c->dim == 2 ? 3 : 6)))
+                        return r;
+        }
+        if (int r = ik_synchronize(c)) return r;
+        if (c->flags & IK_FLAG_TIMING) return IK_OK;
+        // record: per frame on its lane, host -> device copies, the kernels, device -> host
+        if (c->io_exec) { cudaGraphExecDestroy(c->io_exec); c->io_exec = nullptr; }
+        if (c->batch_exec) { cudaGraphExecDestroy(c->batch_exec); c->batch_exec = nullptr; } // versions below are ours now
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+        const int64_t launches_before = c->launches;
+        const int64_t epoch_before = g_alloc_epoch.load();
+        c->capturing = true;
+        c->captured_lanes = 0;
+        int rr = IK_OK;
+        for (int k = 0; k < count && rr == IK_OK; ++k) {
+            c->io_cur = &fr[(size_t)k];
+            rr = prepare_enqueue(c, slots[k], precision, fields);
+        }
+        c->io_cur = nullptr;
+        for (int l = 0; l < IK_LANES && rr == IK_OK; ++l)
+            if (c->captured_lanes & (1 << l)) {
+                if (cudaEventRecord(c->lanes[l].last, c->lanes[l].st) != cudaSuccess ||
+                    cudaStreamWaitEvent(c->stream, c->lanes[l].last, 0) != cudaSuccess)
+                    rr = fail(IK_ERR_CUDA, "joining a lane during capture failed");
+            }
+        c->capturing = false;
+        c->io_launches = c->launches - launches_before;
+        c->launches = launches_before;
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+        if (rr != IK_OK) { if (graph) cudaGraphDestroy(graph); return rr; }
+        if (e != cudaSuccess) return fail(IK_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&c->io_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) { c->io_exec = nullptr; return fail(IK_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e)); }
+        c->io_key = key;
+        c->batch_maxb = c->maxb;
+        c->batch_halo = c->halo_cap;
+        c->batch_maxbe = c->maxbe;
+        c->batch_geom_version = c->geom_version;
+        c->batch_slot_version = c->slot_version;
+        c->batch_config_version = c->config_version;
+        c->batch_alloc_epoch = g_alloc_epoch.load() == epoch_before ? epoch_before : -2;
+        return IK_OK; // the first call's results come from the plain path
+    }
+    // replay after everything already enqueued and every download of these slots
+    if (int r = ik_wait_all(c)) return r;
+    for (int k = 0; k < count; ++k) {
+        Slot& s = c->slots[(size_t)slots[k]];
+        if (s.d2h_recorded) CK(cudaStreamWaitEvent(c->stream, s.d2h_done, 0));
+    }
+    for (int k = 0; k < count; ++k) {
+        PendingOp op{slots[k], precision, fields};
+        for (int q = 0; q < 3; ++q) op.out[q] = fr[(size_t)k].out[q];
+        c->pending.push_back(op);
+    }
+    CK(cudaGraphLaunch(c->io_exec, c->stream));
+    for (int k = 0; k < count; ++k) {
+        Slot& s = c->slots[(size_t)slots[k]];
+        CK(cudaEventRecord(s.done, c->stream));
+        s.done_recorded = true;
+        s.last_prec = precision;
+        s.last_fields = fields;
+    }
+    c->launches += c->io_launches;
+    return IK_OK;
+}
+
 int ik_synchronize(ik_ctx* c)
 {
     if (int r = check_ctx(c)) return r;
@@ -1425,8 +1597,19 @@ int ik_synchronize(ik_ctx* c)
         }
         if (!grow) { c->pending.clear(); return fail(IK_ERR_CUDA, "device status 0x%x", st); }
         std::vector<PendingOp> ops = c->pending;
-        for (const PendingOp& op : ops)
+        for (const PendingOp& op : ops) {
             if (int r = prepare_enqueue(c, op.slot, op.prec, op.fields)) { c->pending.clear(); return r; }
+            // downloads of the first attempt copied an incomplete result: copy again
+            for (int f = 0; f < 3; ++f)
+                if (op.out[f]) {
+                    int64_t G = 0;
+                    { GeoSwap gs(c, op.slot); G = c->geo.G; }
+                    if (int r = ik_download_field_async(c, op.slot, 1 << f, op.out[f], G * (c->dim == 2 ? 3 : 6))) {
+                        c->pending.clear();
+                        return r;
+                    }
+                }
+        }
     }
     c->pending.clear();
     return fail(IK_ERR_CAPACITY, "capacity growth did not converge");
@@ -1835,6 +2018,9 @@ int ik_download_field_async(ik_ctx* c, int slot, int field, double* host_out, in
     if (!s.d2h_done) CK(cudaEventCreateWithFlags(&s.d2h_done, cudaEventDisableTiming));
     CK(cudaEventRecord(s.d2h_done, c->d2h));
     s.d2h_recorded = true;
+    // a computation of this slot still to be confirmed: re-download if it is re-run
+    for (auto it = c->pending.rbegin(); it != c->pending.rend(); ++it)
+        if (it->slot == slot) { it->out[field == IK_FIELD_VIRIAL ? 0 : (field == IK_FIELD_KINETIC ? 1 : 2)] = host_out; break; }
     return IK_OK;
 }
 

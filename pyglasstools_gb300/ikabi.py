@@ -54,6 +54,8 @@ def lib():
             "ik_set_potential": ([vp, i32, C.c_double, dp, i32], i32),
             "ik_potential_nparams": ([i32], i32),
             "ik_compute_thermo": ([vp, i32, dp, i64], i32),
+            "ik_compute_batch_io": ([vp, C.POINTER(i32), i32, i32, i32, C.POINTER(i64), C.POINTER(dp), C.POINTER(dp),
+                                     C.POINTER(dp), C.POINTER(dp), C.POINTER(dp)], i32),
             "ik_gk15_rule": ([dp, dp, dp], i32),
             "ik_set_cgfunc": ([vp, i32, i32, i32, C.c_double, C.c_double], i32),
             "ik_set_adaptive": ([vp, i32, C.c_double, C.c_double], i32),
@@ -343,6 +345,28 @@ class IKContext:
         v = C.c_int64()
         check(lib().ik_get_launch_count(self._h, C.byref(v)))
         return v.value
+
+    def compute_batch_io(self, slots, frames, outs, precision="fp32", fields=FIELD_VIRIAL | FIELD_KINETIC):
+        """One CUDA-graph batch with host I/O (ik_compute_batch_io).  frames[k] =
+        (pos, diam, vel, mass) page-locked float64 arrays (vel / mass may be None);
+        outs[k] = (virial, kinetic, elastic) page-locked float64 (g, NC) arrays or None.
+        Complete after synchronize()."""
+        # ctypes argument arrays kept while the same arrays come back (the arrays held, so
+        # their ids stay theirs)
+        arrays = tuple(a for f in frames for a in f) + tuple(o for os_ in outs for o in os_)
+        ids = tuple(map(id, arrays))
+        cached = getattr(self, "_io_args", None)
+        if cached is None or cached[0] != ids or cached[2] != list(slots):
+            cnt = len(slots)
+            P = C.POINTER(C.c_double)
+            ptr = lambda a: a.ctypes.data_as(P) if a is not None else None
+            args = ((C.c_int * cnt)(*slots), cnt, (C.c_int64 * cnt)(*[len(f[1]) for f in frames]),
+                    (P * cnt)(*[ptr(f[0]) for f in frames]), (P * cnt)(*[ptr(f[2]) for f in frames]),
+                    (P * cnt)(*[ptr(f[3]) for f in frames]), (P * cnt)(*[ptr(f[1]) for f in frames]),
+                    (P * (3 * cnt))(*[ptr(o) for os_ in outs for o in os_]))
+            self._io_args = cached = (ids, arrays, list(slots), args)
+        sl, cnt, nn, pos, vel, mass, diam, out = cached[3]
+        check(lib().ik_compute_batch_io(self._h, sl, cnt, PREC[precision], fields, nn, pos, vel, mass, diam, out))
 
     def compute_thermo(self, slot=0):
         """Global observables of a slot's frame: dict of potentialenergy (float),
