@@ -65,6 +65,11 @@ __device__ __forceinline__ float ik_kern(float q, float R2s)
         return q < 1.0f ? ik_ex2(-1.4426950408889634f * ik_rcp(1.0f - q)) : 0.0f;
     }
 }
+// Two kernel values, packed.  Gaussian: the two cuts (saturated FMAs) and exponentials
+// are scalar, their product one packed multiply.
+template <int KIND>
+__device__ __forceinline__ unsigned long long ik_kern2(unsigned long long q2, float R2s);
+
 // Kernel value of a particle already selected by the (FP64) support rule.
 template <int KIND>
 __device__ __forceinline__ float ik_kern_in(float q)
@@ -120,6 +125,19 @@ __device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c)
     f32x2 d;
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
     return d;
+}
+
+template <int KIND>
+__device__ __forceinline__ f32x2 ik_kern2(f32x2 q2, float R2s)
+{
+    float qa, qb;
+    up2(q2, qa, qb);
+    if (KIND == 1) {
+        const float ia = __saturatef(fmaf(-qa, 0x1p100f, R2s * 0x1p100f));
+        const float ib = __saturatef(fmaf(-qb, 0x1p100f, R2s * 0x1p100f));
+        return mul2(pk2(ik_ex2(-qa), ik_ex2(-qb)), pk2(ia, ib));
+    }
+    return pk2(ik_kern<KIND>(qa, R2s), ik_kern<KIND>(qb, R2s));
 }
 
 // Compensated transposing butterfly over a warp: on entry each lane holds V values
@@ -463,19 +481,18 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                             }
                             float Ma, Mb;
                             up2(M, Ma, Mb);
-                            // node values per grid point in scalar form (no packing moves)
-                            float Ba = a.w0 * ik_kern<KIND>(Ma, R2s), Bb = a.w0 * ik_kern<KIND>(Mb, R2s);
+                            // node sums of the two grid points packed (the same roundings as
+                            // per point: w0 K(M) + sum_t w_t (K(r+) + K(r-)))
+                            f32x2 B2 = mul2(pk2(a.w0, a.w0), ik_kern2<KIND>(M, R2s));
 #pragma unroll
                             for (int t = 0; t < NP; ++t) {
                                 const f32x2 base = add2(M, cq2[t]);
                                 const f32x2 rp = fma2(pk2(a.m2xi[t], a.m2xi[t]), mb, base);
                                 const f32x2 rm = fma2(pk2(-a.m2xi[t], -a.m2xi[t]), mb, base);
-                                float pa, pb, qa, qb;
-                                up2(rp, pa, pb);
-                                up2(rm, qa, qb);
-                                Ba = fmaf(a.w[t], ik_kern<KIND>(pa, R2s) + ik_kern<KIND>(qa, R2s), Ba);
-                                Bb = fmaf(a.w[t], ik_kern<KIND>(pb, R2s) + ik_kern<KIND>(qb, R2s), Bb);
+                                B2 = fma2(pk2(a.w[t], a.w[t]), add2(ik_kern2<KIND>(rp, R2s), ik_kern2<KIND>(rm, R2s)), B2);
                             }
+                            float Ba, Bb;
+                            up2(B2, Ba, Bb);
                             f32x2 B;
                             if constexpr (MLPM) { // r_j outside the support: a record, not a term
                                 const f32x2 rj2 = fma2(pk2(-2.f, -2.f), mb, add2(M, pk2(hh, hh)));
