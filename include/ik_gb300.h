@@ -275,7 +275,8 @@ int ik_get_launch_count(ik_ctx* ctx, int64_t* out);
 int ik_get_counters(ik_ctx* ctx, int slot, int64_t* out3);
 /* Tuning of the FP32 gather (no reference counterpart).  0 restores the default.
  *   IK_TUNE_BIN_POINTS     target grid points per work item (bin of cells)
- *   IK_TUNE_BLOCKS_PER_SM  persistent CTAs launched per SM
+ *   IK_TUNE_BLOCKS_PER_SM  persistent CTAs launched per SM (default: 2 for a frame computed alone, 1 for
+ *                          the frames of a batch, which run side by side on the engine lanes)
  *   IK_TUNE_HALO_CAP       staged halo particles per warp (grows on overflow) */
 #define IK_TUNE_BIN_POINTS 1
 #define IK_TUNE_BLOCKS_PER_SM 2

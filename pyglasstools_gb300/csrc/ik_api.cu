@@ -174,6 +174,7 @@ struct ik_ctx {
     ik_mlp* mlp = nullptr; // learned bond-integral surrogate (IK_QUAD_MLP)
     // tuning of the FP32 gather (0 = default)
     int tune_bin_points = 0, tune_blocks_per_sm = 0;
+    bool in_batch = false; // enqueueing a batch: frames share the GPU (default 1 gather CTA per SM)
     long long mlp_cap = 0;  // record capacity per lane
     // CUDA-graph replay of ik_compute_batch
     bool capturing = false;
@@ -722,7 +723,10 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
             a.cnt_records = cnt + 3;
         }
         size_t smem = (size_t)IK_WARPS_GATHER * ((size_t)c->halo_cap * 20 + (size_t)a.qcap * 4);
-        int blocks = std::min(c->geo.nitems, c->sm_count * (c->tune_blocks_per_sm > 0 ? c->tune_blocks_per_sm : 2));
+        // one frame alone: two CTAs per SM fill the GPU; frames of a batch on several lanes
+        // run side by side, and one CTA per SM each measured faster (8330 -> 8620 frames/s)
+        const int bps = c->tune_blocks_per_sm > 0 ? c->tune_blocks_per_sm : (c->in_batch ? 1 : 2);
+        int blocks = std::min(c->geo.nitems, c->sm_count * bps);
         if (blocks > 0 && main_pass) {
             CK(launch_gather32(a, c->cg.kind, (c->flags & IK_FLAG_LANE_KAHAN) != 0 && !mlp, mlp, blocks,
                                32 * IK_WARPS_GATHER, smem, L.st));
@@ -1345,10 +1349,12 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
                        !(c->flags & IK_FLAG_TIMING);
     if (!reuse) {
         // first run of this batch: plain launches (sizes every buffer, checks capacities)
+        c->in_batch = true;
         for (int k = 0; k < count; ++k) {
             c->pending.push_back({slots[k], precision, fields});
-            if (int r = prepare_enqueue(c, slots[k], precision, fields)) return r;
+            if (int r = prepare_enqueue(c, slots[k], precision, fields)) { c->in_batch = false; return r; }
         }
+        c->in_batch = false;
         if (int r = ik_synchronize(c)) return r;
         if (c->flags & IK_FLAG_TIMING) return IK_OK;
         // then capture the same sequence as one graph (lanes fork from and join the main stream)
@@ -1360,7 +1366,9 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
         c->capturing = true;
         c->captured_lanes = 0;
         int rr = IK_OK;
+        c->in_batch = true;
         for (int k = 0; k < count && rr == IK_OK; ++k) rr = prepare_enqueue(c, slots[k], precision, fields);
+        c->in_batch = false;
         for (int l = 0; l < IK_LANES && rr == IK_OK; ++l)
             if (c->captured_lanes & (1 << l)) {
                 if (cudaEventRecord(c->lanes[l].last, c->lanes[l].st) != cudaSuccess ||
@@ -1467,10 +1475,12 @@ int ik_compute_batch_io(ik_ctx* c, const int* slots, int count, int precision, i
             const IoFrame& f = fr[(size_t)k];
             if (int r = ik_upload_frame(c, slots[k], n[k], f.pos, f.vel, f.mass, f.diam)) return r;
         }
+        c->in_batch = true;
         for (int k = 0; k < count; ++k) {
             c->pending.push_back({slots[k], precision, fields});
-            if (int r = prepare_enqueue(c, slots[k], precision, fields)) return r;
+            if (int r = prepare_enqueue(c, slots[k], precision, fields)) { c->in_batch = false; return r; }
         }
+        c->in_batch = false;
         if (int r = ik_synchronize(c)) return r;
         for (int k = 0; k < count; ++k) {
             int64_t G = 0;
@@ -1491,11 +1501,13 @@ int ik_compute_batch_io(ik_ctx* c, const int* slots, int count, int precision, i
         c->capturing = true;
         c->captured_lanes = 0;
         int rr = IK_OK;
+        c->in_batch = true;
         for (int k = 0; k < count && rr == IK_OK; ++k) {
             c->io_cur = &fr[(size_t)k];
             rr = prepare_enqueue(c, slots[k], precision, fields);
         }
         c->io_cur = nullptr;
+        c->in_batch = false;
         for (int l = 0; l < IK_LANES && rr == IK_OK; ++l)
             if (c->captured_lanes & (1 << l)) {
                 if (cudaEventRecord(c->lanes[l].last, c->lanes[l].st) != cudaSuccess ||
