@@ -290,3 +290,33 @@ def test_batch_with_host_io_matches_per_slot():
     with pytest.raises(ik.IKError):
         c.compute_batch_io([0], [(fr[0].pos.copy(), fr[0].diam.copy(), None, None)], [(outs[0][0], None, None)])
     c.close()
+
+
+def test_batch_with_host_io_fp64_and_partial_outputs():
+    """The host-I/O batch on the FP64 path, frames without velocities, only the virial
+    downloaded: equal to the per-slot results."""
+    torch = pytest.importorskip("torch")
+    from pyglasstools_gb300 import ikabi as ik, synth
+    F, n = 3, 1500
+    fr = _frames(n, range(800, 800 + F))
+    L = fr[0].L
+    grid = synth.lattice_grid(L, 24, 2)
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    host = [(pin(f.pos), pin(f.diam), None, None) for f in fr]
+    outs = [(pin(np.zeros((len(grid), 3))), None, None) for _ in fr]
+    c = _context(ik, L, grid, F)
+    slots = [2, 0, 1]
+    for rep in range(2):
+        c.compute_batch_io(slots, [host[k] for k in slots], [outs[k] for k in slots], precision="fp64",
+                           fields=ik.FIELD_VIRIAL)
+        c.synchronize()
+    ref = _context(ik, L, grid, F)
+    for k, f in enumerate(fr):
+        ref.upload_frame(k, f.pos, f.diam)
+    for k in range(F):
+        ref.compute_slot(k, "fp64", ik.FIELD_VIRIAL)
+    ref.synchronize()
+    for k in range(F):
+        np.testing.assert_array_equal(outs[k][0], uniq(ref.get_field(ik.FIELD_VIRIAL, slot=k)))
+    ref.close()
+    c.close()

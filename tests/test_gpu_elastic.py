@@ -109,3 +109,31 @@ def test_elastic_field_through_the_pybind_classes(ik, oracle):
     _, want = oracle.compute_elastic(obox, f.pos, u, f.diam, oracle.make_poly12(), oracle.make_cg("octic", rcut=2.0),
                                      grid, max_rc=calc.max_rcut)
     assert np.all(rel_l2(uniq(got), uniq(want)) <= 1e-12)
+
+
+def test_elastic_field_with_polydisperse_yukawa_vs_oracle(ik, oracle):
+    """The elastic field with another pair model (PolydisperseYukawa, rcut 4: ~130
+    neighbours within max_rcut per particle, past the 63 of one staged entry): both paths
+    against the oracle."""
+    from pyglasstools_gb300 import synth
+    f = synth.make_frame(1500, dim=2, seed=83)
+    grid = synth.lattice_grid(f.L, 24, 2)
+    u = _disp(f, 2, 0.02, 7)
+    rc, prm = oracle.potential_params("polyyukawa")
+    box = oracle.make_box(2, [f.L, f.L, 1.0])
+    ocg = oracle.make_cg("octic", rcut=2.0, mode="fixedpoint", order=5)
+    max_rc = oracle.max_rcut(rc, f.diam)
+    _, want_e = oracle.compute_elastic(box, f.pos, u, f.diam, oracle.make_potential("polyyukawa", rc, prm), ocg, grid,
+                                       max_rc=max_rc)
+    for prec, tol in (("fp64", 1e-12), ("fp32", 1e-5)):
+        with ik.IKContext() as c:
+            c.set_box(2, [f.L, f.L, 1.0])
+            c.set_potential("polyyukawa", rc, prm)
+            c.set_cgfunc("octic", 2.0, order=5)
+            c.set_max_rcut(max_rc)
+            c.set_grid(grid)
+            c.set_frame(f.pos, f.diam, f.vel, f.mass)
+            c.upload_displacement(u)
+            c.compute(prec, ik.FIELD_ELASTIC)
+            got = c.get_field(ik.FIELD_ELASTIC)
+        assert np.all(rel_l2(uniq(got), uniq(want_e)) <= tol), prec
