@@ -245,6 +245,10 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
     int* queue = sq + a.halo_cap;
 
     const float R2s = a.R2s, margin = a.margin, kappa = a.kappa;
+    const float cull_r2 = 1.001f * R2s + margin; // staging: within R of the bin's box, FP32 slack
+    // culling the staged halo pays in 3D (a one-cell bin keeps ~3/4 of its 27-cell halo);
+    // 2D bins of several cells keep ~7/8, less than the second pass over them costs
+    const bool cull = DIM == 3 && a.cull;
     const bool want_kin = (a.fields & 2) != 0;
     const int npairs = NP > 0 ? NP : a.npairs;
     unsigned long long my_pairs = 0, my_triples = 0;
@@ -309,6 +313,20 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
             else { h0[c] = cc - a.reach[c]; hn[c] = a.bw[c] + 2 * a.reach[c]; }
         }
         const int nh = hn[0] * hn[1] * hn[2];
+        // the bin's box in scaled bin-relative coordinates, [0, bw cws) per axis (cells past
+        // the box edge only shrink it: conservative)
+        const float bxs = a.bw[0] * a.cws[0], bys = a.bw[1] * a.cws[1], bzs = DIM == 3 ? a.bw[2] * a.cws[2] : 0.f;
+        auto near_bin = [&](const IkPRec& r, float ox, float oy, float oz) {
+            const float sx = fmaf(kappa, r.x, ox), sy = fmaf(kappa, r.y, oy);
+            const float dx = fmaxf(fmaxf(-sx, sx - bxs), 0.f), dy = fmaxf(fmaxf(-sy, sy - bys), 0.f);
+            float d2 = fmaf(dy, dy, dx * dx);
+            if (DIM == 3) {
+                const float sz = fmaf(kappa, r.z, oz);
+                const float dz = fmaxf(fmaxf(-sz, sz - bzs), 0.f);
+                d2 = fmaf(dz, dz, d2);
+            }
+            return d2 < cull_r2;
+        };
 
         int hc = 0;
         bool first = true;
@@ -331,15 +349,22 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                     oy = (uy - it.y) * a.cws[1];
                     oz = DIM == 3 ? (uz - it.z) * a.cws[2] : 0.f;
                 }
-                // staged entries of the cell: one per particle, and one more per further
-                // 63 bonds where a particle has more (the entry word holds 6 count bits)
+                // staged entries of the cell: one per particle (with cull: only those
+                // within R of the bin's box -- the others cannot reach any of its grid
+                // points), and one more per further 63 bonds where a particle has more
+                // (the entry word holds 6 count bits)
                 int cent = ccnt;
-                if (SPLIT && cid < nh) {
+                if ((SPLIT || cull) && cid < nh) {
                     cent = 0;
                     for (int t = 0; t < ccnt; ++t) {
                         const int q = cstart + t;
-                        const int nbq = a.boff ? a.boff[q + 1] - a.boff[q] : a.nb[q];
-                        cent += nbq > 63 ? (nbq + 62) / 63 : 1;
+                        if (cull && !near_bin(a.prec[q], ox, oy, oz)) continue;
+                        if (SPLIT) {
+                            const int nbq = a.boff ? a.boff[q + 1] - a.boff[q] : a.nb[q];
+                            cent += nbq > 63 ? (nbq + 62) / 63 : 1;
+                        } else {
+                            ++cent;
+                        }
                     }
                 }
                 int incl = cent;
@@ -364,6 +389,7 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                     for (int t = 0; t < ccnt; ++t) {
                         int q = cstart + t;
                         IkPRec r = a.prec[q];
+                        if (cull && !near_bin(r, ox, oy, oz)) continue;
                         int b0, nbq;
                         if (a.boff) { b0 = a.boff[q]; nbq = a.boff[q + 1] - b0; }
                         else { b0 = q * a.maxb; nbq = a.nb[q]; }

@@ -53,6 +53,7 @@ struct GatherArgs32 {
     float cws[3];          // kappa * cell width
     int bw[3];             // bin width (cells) per axis
     int reach[3];          // halo reach (cells) per axis; 0 on non-periodic axes
+    int cull;              // stage only particles within R of the bin's box
     float kappa, R2s, margin;
     double R2;             // FP64 R^2 for the boundary re-check
     // Gauss-Legendre in symmetric form: nodes +-xi_k (k < npairs) with weights w_k,
