@@ -700,6 +700,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         a.pos64 = L.pos64.as<IkB64>();
         a.cell_start = L.cell_start.as<int>();
         a.boff = stride ? nullptr : L.boff.as<int>();
+        a.nprec = n;
         a.nb = L.nb32.as<int>();
         a.bonds = bonds;
         a.maxb = c->maxb;
@@ -1605,6 +1606,11 @@ int ik_synchronize(ik_ctx* c)
             grow = true;
         }
         if (st & IK_ST_MMA_TIMEOUT) { c->pending.clear(); return fail(IK_ERR_TIMEOUT, "a tensor-core wait gave up"); }
+        if (st & IK_ST_BOND_RANGE) {
+            c->pending.clear();
+            return fail(IK_ERR_CAPACITY, "a frame has 2^25 or more force-active bond records, more than the FP32 "
+                                         "gather addresses; use the FP64 path or smaller frames");
+        }
         if (st & IK_ST_QUAD_FAIL) {
             c->pending.clear();
             return fail(IK_ERR_QUADRATURE, "adaptive bond integral: tolerance not met within %d subintervals",

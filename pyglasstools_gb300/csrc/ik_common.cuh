@@ -21,6 +21,7 @@
 #define IK_QAG_MAXSUB       64  /* subintervals one adaptive bond integral may hold on the device */
 #define IK_ST_MMA_TIMEOUT   16  /* a tensor-core completion wait gave up */
 #define IK_ST_MLP_OVERFLOW  32  /* the surrogate record buffer overflowed */
+#define IK_ST_BOND_RANGE    128 /* FP32 path: 2^25 or more bond records (staged-entry word) */
 
 // Box + cell grid.  Cells tile [lo, lo+L) per axis; nc[c] = 1 on non-periodic axes.
 struct IkGeom {

@@ -232,6 +232,11 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
     constexpr int NC = DIM == 2 ? 3 : 6;       // unique tensor components
     constexpr int P = IK_P;
 
+    // CSR bond records are addressed by (offset << 6 | count) words: 2^25 records at most
+    if (a.boff && a.boff[a.nprec] >= (1 << 25)) {
+        if (threadIdx.x == 0 && blockIdx.x == 0) atomicOr(a.status, IK_ST_BOND_RANGE);
+        return;
+    }
     extern __shared__ float4 smem[];
     __shared__ int s_next; // next item of this CTA's share
     const int lane = threadIdx.x & 31;

@@ -66,6 +66,7 @@ struct GatherArgs32 {
     const int* cell_start;
     const int* boff;       // CSR offsets of the bond records (n + 1), or null: records of
                            // particle q at q * maxb (fixed stride), nb[q] of them
+    int nprec;             // particles of the frame (boff[nprec] = its bond records)
     const int* nb;
     const float4* bonds;   // {kappa r_ij / 2, 2 forceDivR / kappa^2}
     const float4* bcoef;   // elastic field: the bond's stress coefficient (NC floats in

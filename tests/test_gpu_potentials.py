@@ -182,3 +182,25 @@ def test_python_frontend_with_polydisperse_lj(tmp_path, golden, monkeypatch, ora
     w = uniq(want)
     # values are printed with 6 significant digits
     np.testing.assert_allclose(vals, w, rtol=6e-6, atol=1e-9 * np.max(np.abs(w)))
+
+
+def test_fp32_bond_record_range_is_reported(ik, oracle):
+    """A 3D Lennard-Jones frame with ~4e7 force-active bond records: past what the FP32
+    gather's (offset << 6 | count) staging word addresses.  The gather checks the CSR
+    total before any work and reports IK_ERR_CAPACITY; the FP64 path computes the frame."""
+    from pyglasstools_gb300 import synth
+    fr = synth.make_frame(600000, dim=3, seed=91)
+    grid = synth.lattice_grid(fr.L, 4, 3)
+    rc, prm = 2.5, [1.0, 0.0]
+    with ik.IKContext() as c:
+        c.set_box(3, [fr.L] * 3)
+        c.set_potential("lj", rc, prm)
+        c.set_cgfunc("octic", 2.0, order=5)
+        c.set_grid(grid)
+        c.set_frame(fr.pos, fr.diam)
+        with pytest.raises(ik.IKError) as e:
+            c.compute("fp32", ik.FIELD_VIRIAL)
+        assert "2^25" in str(e.value)
+        c.compute("fp64", ik.FIELD_VIRIAL)
+        v = c.get_field(ik.FIELD_VIRIAL)
+        assert np.all(np.isfinite(v)) and np.max(np.abs(v)) > 0
