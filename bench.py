@@ -63,6 +63,9 @@ def parse():
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch leg")
     ap.add_argument("--no-graph", action="store_true",
                     help="enqueue every frame with its own launches instead of one CUDA-graph replay per step")
+    ap.add_argument("--profile-mlp", action="store_true",
+                    help="with --profile: run the surrogate mode (a small network trained first), "
+                         "so that the tensor-core kernel appears in the launch list")
     ap.add_argument("--profile", action="store_true",
                     help="only warm-up + timed steps (for ncu launch lists); prints a short JSON line")
     return ap.parse_args()
@@ -373,6 +376,13 @@ def ours(args, wl, name):
                 ctx.compute_slot(k, prec)
 
     if args.profile:
+        if args.profile_mlp:  # surrogate mode: a small network, trained and validated first
+            from pyglasstools_gb300 import ikabi
+            mlp = ikabi.MLP(torch.cuda.current_device())
+            mlp.train(nsamples=1 << 18, epochs=20, ctas=152, lr=2e-3, seed=5)
+            mlp.validate(n=1 << 18, seed=98, tol=MLP_TOL)
+            ctx.set_mlp(mlp)
+            ctx.set_cgfunc(wl["cg"]["kind"], wl["cg"]["rcut"], mode="mlp", order=5, width=wl["cg"]["width"])
         for _ in range(args.warmup):
             step()
         ctx.synchronize()
