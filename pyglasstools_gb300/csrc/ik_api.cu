@@ -739,7 +739,8 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
             a.mlp_cap = c->mlp_cap;
             a.cnt_records = cnt + 3;
         }
-        size_t smem = (size_t)IK_WARPS_GATHER * ((size_t)c->halo_cap * 20 + (size_t)a.qcap * 4);
+        const size_t stage_bytes = D == 3 ? 20 : 16; // float4 (+ the index word in 3D) per staged entry
+        size_t smem = (size_t)IK_WARPS_GATHER * ((size_t)c->halo_cap * stage_bytes + (size_t)a.qcap * 4);
         // one frame alone: two CTAs per SM fill the GPU; frames of a batch on several lanes
         // run side by side, and one CTA per SM each measured faster (8330 -> 8620 frames/s)
         const int bps = c->tune_blocks_per_sm > 0 ? c->tune_blocks_per_sm : (c->in_batch ? 1 : 2);
@@ -780,7 +781,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
             e.cnt_pairs = L.ecnt.as<unsigned long long>();
             e.cnt_triples = e.cnt_pairs + 1;
             CK(cudaMemsetAsync(L.work_counter.p, 0, sizeof(int), L.st));
-            const size_t esmem = (size_t)IK_WARPS_GATHER * ((size_t)c->halo_cap * 20 + (size_t)e.qcap * 4);
+            const size_t esmem = (size_t)IK_WARPS_GATHER * ((size_t)c->halo_cap * stage_bytes + (size_t)e.qcap * 4);
             if (blocks > 0) {
                 CK(launch_gather32(e, c->cg.kind, false, false, blocks, 32 * IK_WARPS_GATHER, esmem, L.st));
                 c->launches += 1;
@@ -1920,7 +1921,7 @@ int ik_set_tuning(ik_ctx* c, int param, int value)
         return IK_OK;
     case IK_TUNE_HALO_CAP:
         if (value < 0 || value > 1024) return fail(IK_ERR_ARG, "halo capacity must be in [0, 1024]");
-        c->halo_cap = value;
+        c->halo_cap = (value + 31) & ~31; // whole warps of entries (the per-warp layout needs a multiple of 4)
         return IK_OK;
     default:
         return fail(IK_ERR_ARG, "unknown tuning parameter %d", param);

@@ -244,10 +244,12 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
     if (threadIdx.x == 0) s_next = 0;
     __syncthreads();
     // per warp: staged particles (float4 x,y,z, bits(bond offset << 6 | bond count)),
-    // their cell-order indices, and the slot queue
-    float4* stage = smem + (size_t)warp * (a.halo_cap + a.halo_cap / 4 + a.qcap / 4);
+    // their cell-order indices (3D; 2D keeps them in the unused z word), and the slot
+    // queue.  halo_cap is a multiple of 32.
+    constexpr int SQW = DIM == 3 ? 1 : 0;
+    float4* stage = smem + (size_t)warp * (a.halo_cap + SQW * a.halo_cap / 4 + a.qcap / 4);
     int* sq = reinterpret_cast<int*>(stage + a.halo_cap);
-    int* queue = sq + a.halo_cap;
+    int* queue = sq + SQW * a.halo_cap;
 
     const float R2s = a.R2s, margin = a.margin, kappa = a.kappa;
     const float cull_r2 = 1.001f * R2s + margin; // staging: within R of the bin's box, FP32 slack
@@ -404,14 +406,16 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                         s.z = DIM == 3 ? fmaf(kappa, r.z, oz) : 0.f;
                         if (!SPLIT || nbq <= 63) {
                             s.w = __int_as_float((b0 << 6) | nbq);
+                            if (DIM == 2) s.z = __int_as_float(q);
                             stage[dst] = s;
-                            sq[dst] = q;
+                            if (DIM == 3) sq[dst] = q;
                             ++dst;
                         } else { // continuation entries carry IK_SQ_CONT
                             for (int j = 0; j < nbq; j += 63) {
                                 s.w = __int_as_float(((b0 + j) << 6) | min(nbq - j, 63));
+                                if (DIM == 2) s.z = __int_as_float(j ? (q | IK_SQ_CONT) : q);
                                 stage[dst] = s;
-                                sq[dst] = j ? (q | IK_SQ_CONT) : q;
+                                if (DIM == 3) sq[dst] = j ? (q | IK_SQ_CONT) : q;
                                 ++dst;
                             }
                         }
@@ -619,7 +623,7 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                     int mask = 0, cnt = 0;
                     if (s < nst) {
                         const float4 sp = stage[s];
-                        const int sqv = sq[s];
+                        const int sqv = DIM == 2 ? __float_as_int(sp.z) : sq[s];
                         const int q = SPLIT ? sqv & (IK_SQ_CONT - 1) : sqv;
                         const bool own = !SPLIT || sqv == q; // not a continuation: the kinetic term
                         float4 k0 = make_float4(0.f, 0.f, 0.f, 0.f), k1 = k0;
