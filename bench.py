@@ -193,7 +193,7 @@ def reference_arm(args, wl, name):
     from oracle import oracle as O
     O.build()
     frames, grid = make_frames(dict(wl, frames=1), 0)
-    cores = os.cpu_count() or 1
+    cores = O.threads(os.cpu_count() or 1)  # threads the oracle's loops actually run on
     G = len(grid)
     g1 = max(256, G // 32)  # a bounded slice of frame 0's grid per step
     for _ in range(args.warmup):
@@ -554,7 +554,8 @@ def ours(args, wl, name):
     if uneven is not None:
         out["uneven_batch"] = uneven
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cores = os.cpu_count() or 1
+        from oracle import oracle as O
+        cores = O.threads(os.cpu_count() or 1)  # threads the oracle's loops actually run on
         G = len(grid)
         g1 = max(256, G // 8)
         t = cpu_sample(wl, frames, grid, g1, cores)

@@ -851,3 +851,22 @@ void ikor_global_thermo(const ikor_box* box, int64_t n, const double* pos, const
     free(noff);
     free(nidx);
 }
+
+/* Threads an OpenMP region of the oracle runs on after asking for `requested` (0: the
+ * default); 1 when the library was built without OpenMP. */
+int ikor_threads(int requested)
+{
+#ifdef _OPENMP
+    if (requested > 0) omp_set_num_threads(requested);
+    int n = 1;
+#pragma omp parallel
+    {
+#pragma omp single
+        n = omp_get_num_threads();
+    }
+    return n;
+#else
+    (void)requested;
+    return 1;
+#endif
+}

@@ -105,6 +105,10 @@ int ikor_compute_range(const ikor_box* box, int64_t n, const double* pos, const 
 /* Global virial sum_{i<j} F_ij (x) r_ij (ThermoCalculator.h:68-90, not divided by volume). */
 void ikor_global_virial(const ikor_box* box, int64_t n, const double* pos, const double* diam,
                         const ikor_pot* pot, double max_rcut, double* out /* dim x dim */);
+/* OpenMP threads of the oracle's parallel regions after asking for `requested` (0: the
+ * default); 1 without OpenMP. */
+int ikor_threads(int requested);
+
 /* Global thermodynamic observables (ThermoCalculator::compute); out holds
  * 1 + 3 dim^2 + dim^4 values: energy, virial, elastic virial, kinetic stress, Born tensor,
  * all divided by the box volume. */

@@ -83,6 +83,8 @@ def lib():
         L.ikor_compute_elastic.restype = C.c_int
         L.ikor_global_virial.argtypes = [C.POINTER(Box), C.c_int64, dp, dp, C.POINTER(Pot),
                                          C.c_double, dp]
+        L.ikor_threads.argtypes = [C.c_int]
+        L.ikor_threads.restype = C.c_int
         L.ikor_global_thermo.argtypes = [C.POINTER(Box), C.c_int64, dp, dp, dp, dp, dp, C.POINTER(Pot),
                                          C.c_double, dp]
         _LIB = L
@@ -304,6 +306,11 @@ def global_virial(box, pos, diam, pot, max_rc=None):
     lib().ikor_global_virial(C.byref(box), len(pos), _dp(pos), _dp(diam), C.byref(pot),
                              max_rc, _dp(out))
     return out.reshape(D, D).T.copy()
+
+
+def threads(requested=0):
+    """OpenMP threads the oracle's parallel loops run on (1 without OpenMP)."""
+    return int(lib().ikor_threads(int(requested)))
 
 
 def global_thermo(box, pos, diam, pot, vel=None, mass=None, disp=None, max_rc=None):
