@@ -320,3 +320,40 @@ def test_batch_with_host_io_fp64_and_partial_outputs():
         np.testing.assert_array_equal(outs[k][0], uniq(ref.get_field(ik.FIELD_VIRIAL, slot=k)))
     ref.close()
     c.close()
+
+
+def test_batch_with_host_io_refetches_fields_after_capacity_growth():
+    """A replay whose new frame contents overflow the bond capacity: ik_synchronize re-runs
+    the frame on the plain path with a larger capacity and copies its fields to the host
+    again, so the host outputs equal the per-slot results."""
+    torch = pytest.importorskip("torch")
+    from pyglasstools_gb300 import ikabi as ik, synth
+    F, n = 2, 2000
+    fr = _frames(n, range(900, 900 + F))
+    L = fr[0].L
+    grid = synth.lattice_grid(L, 24, 2)
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    host = [(pin(f.pos), pin(f.diam), pin(f.vel), pin(f.mass)) for f in fr]
+    outs = [(pin(np.zeros((len(grid), 3))), pin(np.zeros((len(grid), 3))), None) for _ in fr]
+    c = _context(ik, L, grid, F)
+    c.set_max_rcut(1.25 * 1.62)
+    slots = list(range(F))
+    for _ in range(2):  # plain + recording, then a replay
+        c.compute_batch_io(slots, host, outs)
+        c.synchronize()
+    # squeeze frame 1 towards the box centre: many more force-active bonds per particle
+    dense = fr[1].pos.copy()
+    dense[:, :2] *= 0.55
+    host[1][0][:] = dense
+    c.compute_batch_io(slots, host, outs)
+    c.synchronize()
+    ref = _context(ik, L, grid, F)
+    ref.set_max_rcut(1.25 * 1.62)
+    ref.upload_frame(0, fr[0].pos, fr[0].diam, fr[0].vel, fr[0].mass)
+    ref.upload_frame(1, dense, fr[1].diam, fr[1].vel, fr[1].mass)
+    want = [(uniq(v), uniq(k)) for v, k in _per_slot(ik, ref, slots, "fp32")]
+    for k in slots:
+        np.testing.assert_array_equal(outs[k][0], want[k][0])
+        np.testing.assert_array_equal(outs[k][1], want[k][1])
+    ref.close()
+    c.close()
