@@ -691,7 +691,7 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                         int t = __shfl_up_sync(FULL, incl, o);
                         if (lane >= o) incl += t;
                     }
-                    const int tot = __shfl_sync(FULL, incl, 31);
+                    const int tot = __reduce_add_sync(FULL, cnt); // beside the scan, not after it
                     const int off = qn + incl - cnt;
                     const int entry = (s << 10) | mask;
                     for (int k = 0; k < cnt; ++k) queue[off + k] = entry | (k << 4);
