@@ -295,3 +295,33 @@ def test_golden_fixture_field_regenerates(oracle, golden):
     v, _ = oracle.compute(box, pos, diam, pot, cg, grid[sel], max_rc=float(gold["max_rcut"]))
     u = np.stack([v[:, 0, 0], v[:, 1, 1], v[:, 0, 1]], axis=1)
     assert np.max(rel_l2(u, gold["virial"][sel])) < 1e-13
+
+
+@pytest.mark.parametrize("kind", ["octic", "mollifier"])
+def test_adaptive_bond_integral_vs_scipy(oracle, kind):
+    """The oracle's QAG-GK15 (the restatement of gsl_integration_qag key 1 that the GPU's
+    adaptive mode is checked against) against scipy's QUADPACK with the support crossings
+    given as break points: within its tolerance where the segment stays inside the support
+    (a smooth integrand); where it crosses the edge, the kernel's kink there (the octic's
+    curvature jumps, the mollifier's derivatives vanish) is invisible to QAG's K15 - G7
+    estimate, as in GSL, and the answer is good to ~1e-7 relative."""
+    from scipy.integrate import quad
+    rng = np.random.default_rng(12)
+    R = 2.0
+    cg = oracle.make_cg(kind, rcut=R, mode="adaptive", width=R, epsabs=1e-13, epsrel=1e-11, limit=200)
+    x = np.zeros(3)
+    smooth = 0
+    for _ in range(150):
+        ri = np.r_[rng.uniform(-1.9, 1.9, 2), 0.0]
+        rij = np.r_[rng.uniform(-1.5, 1.5, 2), 0.0]
+        f = lambda s: oracle.delta(cg, 2, float(np.sum((x - ri - s * rij) ** 2)))
+        u = x - ri
+        bb, ub, uu = rij @ rij, u @ rij, u @ u
+        disc = ub * ub - bb * (uu - R * R)
+        pts = [r for r in ((ub - np.sqrt(disc)) / bb, (ub + np.sqrt(disc)) / bb) if 0 < r < 1] if disc > 0 else []
+        ref = quad(f, 0, 1, points=pts or None, epsabs=1e-15, epsrel=1e-13, limit=200)[0]
+        got = oracle.bond(cg, 2, x, ri, rij)
+        tol = 1e-12 + 1e-6 * abs(ref) if pts else 1e-13 + 1e-10 * abs(ref)
+        assert abs(got - ref) <= tol, (got, ref, pts)
+        smooth += not pts
+    assert smooth > 10
