@@ -68,6 +68,8 @@ def parse():
                          "so that the tensor-core kernel appears in the launch list")
     ap.add_argument("--profile", action="store_true",
                     help="only warm-up + timed steps (for ncu launch lists); prints a short JSON line")
+    ap.add_argument("--profile-precision", default="fp32", choices=["fp32", "fp64"],
+                    help="with --profile: the path the steps run (fp64 = the plain FP64 gather)")
     return ap.parse_args()
 
 
@@ -384,11 +386,11 @@ def ours(args, wl, name):
             ctx.set_mlp(mlp)
             ctx.set_cgfunc(wl["cg"]["kind"], wl["cg"]["rcut"], mode="mlp", order=5, width=wl["cg"]["width"])
         for _ in range(args.warmup):
-            step()
+            step(args.profile_precision)
         ctx.synchronize()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            step()
+            step(args.profile_precision)
         ctx.synchronize()
         dt = time.perf_counter() - t0
         print(json.dumps({"profile": name, "frames": F, "steps": args.steps, "host_s": dt,
