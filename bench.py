@@ -177,9 +177,10 @@ def max_over_ranks(x, world):
 
 
 # ---------------------------------------------------------------------------- CPU baseline
-def cpu_sample(wl, frames, grid, g1, nthreads):
+def cpu_sample(wl, frames, grid, g1, nthreads, k=0):
+    """Seconds the oracle takes for grid points [0, g1) of frame k on nthreads threads."""
     from oracle import oracle as O
-    f = frames[0]
+    f = frames[k]
     box = O.make_box(wl["dim"], [f.L, f.L, f.L if wl["dim"] == 3 else 1.0])
     pot = O.make_poly12()
     cg = O.make_cg(wl["cg"]["kind"], rcut=wl["cg"]["rcut"], mode="fixedpoint", order=5, width=wl["cg"]["width"])
@@ -188,30 +189,58 @@ def cpu_sample(wl, frames, grid, g1, nthreads):
     return time.perf_counter() - t
 
 
+def host_cpu_info():
+    """CPUs this process may run on: the count the OS reports, the affinity mask and the
+    cgroup v2 CPU quota (a quota below the affinity count time-slices the oracle's threads)."""
+    info = {"nproc": os.cpu_count()}
+    try:
+        info["affinity"] = len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        info["affinity"] = None
+    try:
+        with open("/sys/fs/cgroup/cpu.max") as f:
+            quota, period = f.read().split()[:2]
+        info["cgroup_cpus"] = None if quota == "max" else float(quota) / float(period)
+    except (OSError, ValueError):
+        info["cgroup_cpus"] = None
+    return info
+
+
+def single_core_sample(wl, frames, grid):
+    """The oracle on one thread over the whole of frame 0 (about ten seconds on one core):
+    the per-core rate beside the all-threads baseline."""
+    t = cpu_sample(wl, frames, grid, len(grid), 1)
+    return {"value": 1.0 / t, "unit": "frames/s", "cores": 1,
+            "sample": f"frame 0 whole ({len(grid)} grid points), one thread, {t:.2f} s"}
+
+
 def reference_arm(args, wl, name):
+    """The CPU restatement of the reference's path alone: one step = one whole frame
+    (cell list, neighbour lists and every grid point), frames cycled over eight seeds."""
     world, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
     if rank != 0:
         return
     from oracle import oracle as O
     O.build()
-    frames, grid = make_frames(dict(wl, frames=1), 0)
+    nfr = min(wl["frames"], 8)
+    frames, grid = make_frames(dict(wl, frames=nfr), 0)
     cores = O.threads(os.cpu_count() or 1)  # threads the oracle's loops actually run on
     G = len(grid)
-    g1 = max(256, G // 32)  # a bounded slice of frame 0's grid per step
-    for _ in range(args.warmup):
-        cpu_sample(wl, frames, grid, g1, cores)
+    for k in range(args.warmup):
+        cpu_sample(wl, frames, grid, G, cores, k=k % nfr)
     t = 0.0
-    for _ in range(args.steps):
-        t += cpu_sample(wl, frames, grid, g1, cores)
-    frac = g1 / G
-    value = frac * args.steps / t
+    for k in range(args.steps):
+        t += cpu_sample(wl, frames, grid, G, cores, k=k % nfr)
+    value = args.steps / t
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config_of(name, wl, world),
             "cpu_baseline": {"value": value, "unit": "frames/s", "cores": cores, "kind": "port",
-                             "sample": f"grid points [0, {g1}) of frame 0 ({frac:.4f} of a frame) per step, "
-                                       f"FP64 oracle restating IrvingKirkwood::compute, OpenMP {cores} threads"},
+                             "sample": f"one whole frame per step ({G} grid points; frames cycled over {nfr} "
+                                       f"seeds), FP64 oracle restating IrvingKirkwood::compute, "
+                                       f"OpenMP {cores} threads",
+                             "host_cpus": host_cpu_info()},
             "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -559,11 +588,15 @@ def ours(args, wl, name):
         from oracle import oracle as O
         cores = O.threads(os.cpu_count() or 1)  # threads the oracle's loops actually run on
         G = len(grid)
-        g1 = max(256, G // 8)
-        t = cpu_sample(wl, frames, grid, g1, cores)
-        out["cpu_baseline"] = {"value": (g1 / G) / t, "unit": "frames/s", "cores": cores, "kind": "port",
-                               "sample": f"grid points [0, {g1}) of frame 0 ({g1 / G:.4f} of a frame), FP64 oracle "
-                                         f"restating IrvingKirkwood::compute, OpenMP {cores} threads, {t:.2f} s"}
+        t, nf = 0.0, 0  # whole frames until about 10 s of CPU work (at most 8)
+        while nf < min(len(frames), 8) and t < 10.0:
+            t += cpu_sample(wl, frames, grid, G, cores, k=nf)
+            nf += 1
+        out["cpu_baseline"] = {"value": nf / t, "unit": "frames/s", "cores": cores, "kind": "port",
+                               "sample": f"{nf} whole frame(s) of the workload (frames 0..{nf - 1}), FP64 oracle "
+                                         f"restating IrvingKirkwood::compute, OpenMP {cores} threads, {t:.2f} s",
+                               "host_cpus": host_cpu_info(),
+                               "single_core": single_core_sample(wl, frames, grid)}
     ctx.close()
     if rank == 0:
         print(json.dumps(out), flush=True)

@@ -66,6 +66,29 @@ void ikor_gl_rule(int n, double* x, double* w)
     if (n % 2 == 1) x[n / 2] = 0.0; /* exact centre node */
 }
 
+/* Each rule is built once per process and reused (the reference takes its table from
+ * GSL on every call, FixedPointQuadrature.h:35; rebuilding it by Newton iteration in
+ * long double on every bond would dominate the loop, most of all where long double is
+ * software quad precision, as on aarch64).  The first caller builds under a lock; later
+ * callers see the finished table through an acquire load. */
+static double gl_tab_x[65][64], gl_tab_w[65][64];
+static int gl_tab_ready[65];
+
+static void gl_rule_cached(int n, const double** x, const double** w)
+{
+    if (!__atomic_load_n(&gl_tab_ready[n], __ATOMIC_ACQUIRE)) {
+#pragma omp critical(ikor_rules)
+        {
+            if (!__atomic_load_n(&gl_tab_ready[n], __ATOMIC_RELAXED)) {
+                ikor_gl_rule(n, gl_tab_x[n], gl_tab_w[n]);
+                __atomic_store_n(&gl_tab_ready[n], 1, __ATOMIC_RELEASE);
+            }
+        }
+    }
+    *x = gl_tab_x[n];
+    *w = gl_tab_w[n];
+}
+
 /* ------------------------------------------------------------------------- */
 /* The pair models, each in the evaluation order of its reference expression (C and
  * C++ both evaluate a*b*c as (a*b)*c; the library is built with -ffp-contract=off):
@@ -271,9 +294,8 @@ static long double mom7(int m) /* int_{-1}^{1} P_7(x) x^m dx */
     return s;
 }
 
-static void gk15_init(void)
+static void gk15_build(void)
 {
-    if (gk_ready) return;
     /* E_8 = x^8 + a6 x^6 + a4 x^4 + a2 x^2 + a0; conditions k = 1,3,5,7 */
     long double M7 = mom7(7), M9 = mom7(9), M11 = mom7(11), M13 = mom7(13), M15 = mom7(15);
     long double a6 = -M9 / M7;
@@ -320,7 +342,19 @@ static void gk15_init(void)
     }
     for (int i = 0; i < 8; ++i) { gk_x[i] = (double)nodes[i]; gk_wk[i] = (double)(A[i][8] / A[i][i]); }
     gk_wg[0] = gw[3]; gk_wg[1] = gw[4]; gk_wg[2] = gw[5]; gk_wg[3] = gw[6];
-    gk_ready = 1;
+}
+
+/* built once, as the GL tables: the first caller under a lock, the rest after an acquire load */
+static void gk15_init(void)
+{
+    if (__atomic_load_n(&gk_ready, __ATOMIC_ACQUIRE)) return;
+#pragma omp critical(ikor_rules)
+    {
+        if (!__atomic_load_n(&gk_ready, __ATOMIC_RELAXED)) {
+            gk15_build();
+            __atomic_store_n(&gk_ready, 1, __ATOMIC_RELEASE);
+        }
+    }
 }
 
 /* exported for the pin tests */
@@ -436,8 +470,8 @@ static double bond_exact(const ikor_cg* cg, int dim, const double x[3], const do
     double bb = rij[0] * rij[0] + rij[1] * rij[1] + rij[2] * rij[2];
     if (cg->kind == IKOR_CG_RECT) return ikor_delta(cg, dim, 0.0) * (s1 - s0);
     if (cg->kind == IKOR_CG_OCTIC || bb == 0.0) {
-        double gx[5], gw[5];
-        ikor_gl_rule(5, gx, gw);
+        const double *gx, *gw;
+        gl_rule_cached(5, &gx, &gw);
         double c = 0.5 * (s0 + s1), h = 0.5 * (s1 - s0), acc = 0.0;
         if (bb == 0.0) return ikor_delta(cg, dim, u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
         for (int k = 0; k < 5; ++k) {
@@ -474,9 +508,9 @@ double ikor_bond(const ikor_cg* cg, int dim, const double x[3], const double ri[
     if (cg->mode == IKOR_QUAD_ADAPTIVE) return qag15(cg, dim, x, ri, rij, 0.0, 1.0);
     /* fixed point: GL-n on [0,1]  (CoarseGrainFunction.h:85-88, FixedPointQuadrature.h:39-46) */
     int n = cg->order > 0 ? cg->order : 1;
-    double gx[64], gw[64];
     if (n > 64) n = 64;
-    ikor_gl_rule(n, gx, gw);
+    const double *gx, *gw;
+    gl_rule_cached(n, &gx, &gw);
     double acc = 0.0;
     for (int k = 0; k < n; ++k) acc += gw[k] * obj(cg, dim, x, ri, rij, 0.5 + 0.5 * gx[k]);
     return 0.5 * acc;

@@ -34,7 +34,7 @@ def test_reference_arm_json_line():
     assert line["config"]["workload"] == "ik2d_n2k_g64_octic"
     cb = line["cpu_baseline"]
     assert cb["kind"] == "port" and cb["value"] == line["value"] and cb["cores"] >= 1
-    assert "grid points" in cb["sample"]
+    assert "whole frame" in cb["sample"]
     e2e = line["e2e"]
     assert e2e == {"value": line["value"], "unit": "frames/s",
                    "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
