@@ -325,3 +325,83 @@ def test_adaptive_bond_integral_vs_scipy(oracle, kind):
         assert abs(got - ref) <= tol, (got, ref, pts)
         smooth += not pts
     assert smooth > 10
+
+
+def _py_ik_field(pos, vel, mass, diam, L, grid, R=2.0, v0=1.0, eps=0.2, rc=1.25, order=5):
+    """An independent pure-Python restatement of IrvingKirkwood::compute for a handful of
+    particles (irvingkirkwood/IrvingKirkwood.h:74-110): Polydisperse12 force
+    (potential/Polydisperse12.h:38-55, coefficients potential/__init__.py:83-85), octic
+    kernel (cgfunc/CGFuncOctic.h:16-29), GL-n bond integral on [0, 1] with numpy's
+    Gauss-Legendre nodes, periodic min-image in x and y, the selection rule (ordered
+    pairs, first particle inside the support) and the intended kinetic term."""
+    c1, c2 = 48.0 * v0 / rc ** 14, -21.0 * v0 / rc ** 16
+    xi, wi = np.polynomial.legendre.leggauss(order)
+    n = len(pos)
+    max_rc = max(rc * diam.max(), diam.max())
+
+    def mi(d):
+        d = d.copy()
+        d[:2] -= L * np.round(d[:2] / L)
+        return d
+
+    def force_divr(rsq, di, dj):
+        sig = 0.5 * (di + dj) * (1.0 - eps * abs(di - dj))
+        if rsq >= (rc * sig) ** 2:
+            return 0.0
+        s2 = sig * sig / rsq
+        return (12.0 * v0 * s2 * s2 ** 6 - 2.0 * c1 - 4.0 * c2 * rsq / (sig * sig)) / (sig * sig)
+
+    def delta(r2):
+        if r2 >= R * R:
+            return 0.0
+        q2 = r2 / (R * R)
+        return 15.0 / (8.0 * np.pi * R * R) * (1.0 - 2.0 * q2 * q2 + q2 ** 4)
+
+    vir = np.zeros((len(grid), 2, 2))
+    kin = np.zeros((len(grid), 2, 2))
+    for g, x in enumerate(grid):
+        for i in range(n):
+            dx = mi(x - pos[i])
+            if dx @ dx >= R * R:
+                continue
+            ri = x - dx
+            w = delta(dx @ dx)
+            kin[g] += mass[i] * np.outer(vel[i, :2], vel[i, :2]) * w
+            for j in range(n):
+                if j == i:
+                    continue
+                rij = mi(pos[j] - pos[i])
+                if rij @ rij >= max_rc * max_rc:
+                    continue
+                b = 0.0
+                for s_, w_ in zip(0.5 + 0.5 * xi, wi):
+                    e = x - ri - s_ * rij
+                    b += w_ * delta(e @ e)
+                b *= 0.5
+                f = force_divr(rij @ rij, diam[i], diam[j])
+                vir[g] += 0.5 * b * f * np.outer(rij[:2], rij[:2])
+    return vir, kin
+
+
+def test_three_particle_independent_restatement(oracle):
+    """Three particles straddling the periodic x boundary, 2D octic R = 2, GL-5: the
+    oracle's virial and kinetic fields against the pure-Python restatement above."""
+    L = 12.0
+    base = np.array([[5.6, 0.0, 0.0], [6.5, 0.3, 0.0], [5.8, 1.0, 0.0]])
+    pos = base.copy()
+    pos[:, 0] = (pos[:, 0] + L / 2) % L - L / 2  # wrapped into [-L/2, L/2)
+    vel = np.array([[0.3, -0.2, 0.0], [-0.1, 0.4, 0.0], [0.25, 0.15, 0.0]])
+    mass = np.array([1.0, 1.3, 0.8])
+    diam = np.array([1.0, 0.9, 1.1])
+    gx = np.linspace(4.0, 7.5, 8)
+    gx = (gx + L / 2) % L - L / 2
+    gy = np.linspace(-1.5, 2.5, 7)
+    grid = np.array([[a, b, 0.0] for a in gx for b in gy])
+    box = oracle.make_box(2, [L, L, 1.0])
+    pot = oracle.make_poly12()
+    cg = oracle.make_cg("octic", rcut=2.0, mode="fixedpoint", order=5)
+    vir, kin = oracle.compute(box, pos, diam, pot, cg, grid, vel=vel, mass=mass)
+    pv, pk = _py_ik_field(pos, vel, mass, diam, L, grid)
+    assert np.count_nonzero(np.abs(pv).sum(axis=(1, 2))) > 10  # bonds seen by many points
+    assert np.max(np.abs(vir - pv)) <= 1e-12 * np.max(np.abs(pv))
+    assert np.max(np.abs(kin - pk)) <= 1e-12 * np.max(np.abs(pk))
