@@ -327,13 +327,15 @@ def test_adaptive_bond_integral_vs_scipy(oracle, kind):
     assert smooth > 10
 
 
-def _py_ik_field(pos, vel, mass, diam, L, grid, R=2.0, v0=1.0, eps=0.2, rc=1.25, order=5):
+def _py_ik_field(pos, vel, mass, diam, L, grid, R=2.0, v0=1.0, eps=0.2, rc=1.25, order=5, dim=2):
     """An independent pure-Python restatement of IrvingKirkwood::compute for a handful of
     particles (irvingkirkwood/IrvingKirkwood.h:74-110): Polydisperse12 force
     (potential/Polydisperse12.h:38-55, coefficients potential/__init__.py:83-85), octic
     kernel (cgfunc/CGFuncOctic.h:16-29), GL-n bond integral on [0, 1] with numpy's
-    Gauss-Legendre nodes, periodic min-image in x and y, the selection rule (ordered
-    pairs, first particle inside the support) and the intended kinetic term."""
+    Gauss-Legendre nodes, periodic min-image (x and y in 2D, x, y and z in 3D,
+    SimBox.cc:15,37), the selection rule (ordered pairs, first particle inside the
+    support) and the intended kinetic term.  The octic keeps its 2D normalisation in 3D,
+    as the reference's does."""
     c1, c2 = 48.0 * v0 / rc ** 14, -21.0 * v0 / rc ** 16
     xi, wi = np.polynomial.legendre.leggauss(order)
     n = len(pos)
@@ -341,7 +343,7 @@ def _py_ik_field(pos, vel, mass, diam, L, grid, R=2.0, v0=1.0, eps=0.2, rc=1.25,
 
     def mi(d):
         d = d.copy()
-        d[:2] -= L * np.round(d[:2] / L)
+        d[:dim] -= L * np.round(d[:dim] / L)
         return d
 
     def force_divr(rsq, di, dj):
@@ -357,8 +359,8 @@ def _py_ik_field(pos, vel, mass, diam, L, grid, R=2.0, v0=1.0, eps=0.2, rc=1.25,
         q2 = r2 / (R * R)
         return 15.0 / (8.0 * np.pi * R * R) * (1.0 - 2.0 * q2 * q2 + q2 ** 4)
 
-    vir = np.zeros((len(grid), 2, 2))
-    kin = np.zeros((len(grid), 2, 2))
+    vir = np.zeros((len(grid), dim, dim))
+    kin = np.zeros((len(grid), dim, dim))
     for g, x in enumerate(grid):
         for i in range(n):
             dx = mi(x - pos[i])
@@ -366,7 +368,7 @@ def _py_ik_field(pos, vel, mass, diam, L, grid, R=2.0, v0=1.0, eps=0.2, rc=1.25,
                 continue
             ri = x - dx
             w = delta(dx @ dx)
-            kin[g] += mass[i] * np.outer(vel[i, :2], vel[i, :2]) * w
+            kin[g] += mass[i] * np.outer(vel[i, :dim], vel[i, :dim]) * w
             for j in range(n):
                 if j == i:
                     continue
@@ -379,7 +381,7 @@ def _py_ik_field(pos, vel, mass, diam, L, grid, R=2.0, v0=1.0, eps=0.2, rc=1.25,
                     b += w_ * delta(e @ e)
                 b *= 0.5
                 f = force_divr(rij @ rij, diam[i], diam[j])
-                vir[g] += 0.5 * b * f * np.outer(rij[:2], rij[:2])
+                vir[g] += 0.5 * b * f * np.outer(rij[:dim], rij[:dim])
     return vir, kin
 
 
@@ -403,5 +405,27 @@ def test_three_particle_independent_restatement(oracle):
     vir, kin = oracle.compute(box, pos, diam, pot, cg, grid, vel=vel, mass=mass)
     pv, pk = _py_ik_field(pos, vel, mass, diam, L, grid)
     assert np.count_nonzero(np.abs(pv).sum(axis=(1, 2))) > 10  # bonds seen by many points
+    assert np.max(np.abs(vir - pv)) <= 1e-12 * np.max(np.abs(pv))
+    assert np.max(np.abs(kin - pk)) <= 1e-12 * np.max(np.abs(pk))
+
+
+def test_four_particle_3d_independent_restatement(oracle):
+    """3D: four particles around a box corner (wrapped in x, y and z), octic R = 2, GL-5,
+    against the pure-Python restatement."""
+    L = 10.0
+    base = np.array([[4.7, 4.6, 4.8], [5.5, 4.9, 5.1], [4.9, 5.6, 4.6], [5.2, 5.1, 5.7]])
+    pos = (base + L / 2) % L - L / 2
+    rng = np.random.default_rng(7)
+    vel = rng.normal(0.0, 0.4, (4, 3))
+    mass = np.array([1.0, 0.7, 1.2, 0.9])
+    diam = np.array([1.0, 0.85, 1.1, 0.95])
+    ax = (np.linspace(3.5, 6.5, 5) + L / 2) % L - L / 2
+    grid = np.array([[a, b, c] for a in ax for b in ax for c in ax])
+    box = oracle.make_box(3, [L, L, L])
+    pot = oracle.make_poly12()
+    cg = oracle.make_cg("octic", rcut=2.0, mode="fixedpoint", order=5)
+    vir, kin = oracle.compute(box, pos, diam, pot, cg, grid, vel=vel, mass=mass)
+    pv, pk = _py_ik_field(pos, vel, mass, diam, L, grid, dim=3)
+    assert np.count_nonzero(np.abs(pv).sum(axis=(1, 2))) > 20
     assert np.max(np.abs(vir - pv)) <= 1e-12 * np.max(np.abs(pv))
     assert np.max(np.abs(kin - pk)) <= 1e-12 * np.max(np.abs(pk))
