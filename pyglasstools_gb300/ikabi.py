@@ -128,6 +128,42 @@ def _c64(a, shape=None):
     return a if shape is None else a.reshape(shape)
 
 
+def check_io_arrays(slots, frames, outs):
+    """Arguments of IKContext.compute_batch_io, checked before their raw pointers go to the
+    device copies: one (pos, diam, vel, mass) frame and one (virial, kinetic, elastic)
+    output triple per slot; every array C-contiguous float64 (outputs also writeable);
+    pos and vel n x 3, diam and mass n (n = len(diam)); vel, mass and outputs may be None.
+    Raises ValueError."""
+    if not (len(slots) == len(frames) == len(outs)) or len(slots) == 0:
+        raise ValueError("compute_batch_io: one frame and one output triple per slot")
+
+    def ok(a, what, shape, out=False):
+        if a is None:
+            return
+        if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags.c_contiguous:
+            raise ValueError(f"compute_batch_io: {what} must be a C-contiguous float64 array")
+        if out and not a.flags.writeable:
+            raise ValueError(f"compute_batch_io: {what} must be writeable")
+        if shape is not None and a.shape != shape:
+            raise ValueError(f"compute_batch_io: {what} has shape {a.shape}, expected {shape}")
+
+    for k, (f, o) in enumerate(zip(frames, outs)):
+        if len(f) != 4 or len(o) != 3:
+            raise ValueError(f"compute_batch_io: frame {k} needs (pos, diam, vel, mass) and (virial, kinetic, elastic)")
+        pos, diam, vel, mass = f
+        if pos is None or diam is None:
+            raise ValueError(f"compute_batch_io: frame {k} needs positions and diameters")
+        ok(diam, f"frame {k} diam", None)
+        if diam.ndim != 1:
+            raise ValueError(f"compute_batch_io: frame {k} diam must be one-dimensional")
+        n = len(diam)
+        ok(pos, f"frame {k} pos", (n, 3))
+        ok(vel, f"frame {k} vel", (n, 3))
+        ok(mass, f"frame {k} mass", (n,))
+        for q, name in enumerate(("virial", "kinetic", "elastic")):
+            ok(o[q], f"frame {k} {name} output", None, out=True)
+
+
 def check(rc):
     if rc != IK_OK:
         raise IKError(rc, lib().ik_last_error().decode(errors="replace"))
@@ -357,6 +393,7 @@ class IKContext:
         ids = tuple(map(id, arrays))
         cached = getattr(self, "_io_args", None)
         if cached is None or cached[0] != ids or cached[2] != list(slots):
+            check_io_arrays(slots, frames, outs)
             cnt = len(slots)
             P = C.POINTER(C.c_double)
             ptr = lambda a: a.ctypes.data_as(P) if a is not None else None

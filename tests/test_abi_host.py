@@ -271,3 +271,34 @@ def test_product_gk15_rule_exact_and_equal_to_oracle(oracle):
     ox, owk, owg = oracle.gk15_rule()
     np.testing.assert_allclose(x, ox, rtol=0, atol=2e-16)
     np.testing.assert_allclose(wk, owk, rtol=0, atol=2e-16)
+
+
+def test_batch_io_argument_checks():
+    """IKContext.compute_batch_io checks its arrays before their pointers reach the device
+    copies: one frame and one output triple per slot, C-contiguous float64, n x 3 / n."""
+    from pyglasstools_gb300.ikabi import check_io_arrays
+    n, G = 10, 7
+    pos, diam = np.zeros((n, 3)), np.ones(n)
+    vel, mass = np.zeros((n, 3)), np.ones(n)
+    out = (np.zeros((G, 3)), np.zeros((G, 3)), None)
+    check_io_arrays([0], [(pos, diam, vel, mass)], [out])
+    check_io_arrays([0, 1], [(pos, diam, None, None)] * 2, [out, (None, None, None)])
+    bad = [
+        ([0, 1], [(pos, diam, vel, mass)], [out]),                        # count mismatch
+        ([0], [(pos.astype(np.float32), diam, vel, mass)], [out]),        # float32
+        ([0], [(np.zeros((3, n)).T, diam, vel, mass)], [out]),            # not C-contiguous
+        ([0], [(np.zeros((n + 1, 3)), diam, vel, mass)], [out]),          # n mismatch
+        ([0], [(pos, diam, np.zeros((n, 2)), mass)], [out]),              # vel shape
+        ([0], [(pos, diam, vel, np.ones(n - 1))], [out]),                 # mass shape
+        ([0], [(None, diam, vel, mass)], [out]),                          # positions required
+        ([0], [(pos, diam.reshape(n, 1), vel, mass)], [out]),             # diam not 1-D
+        ([0], [(pos, diam, vel, mass)], [(np.zeros((G, 3), np.float32), None, None)]),
+        ([0], [(pos, diam, vel)], [out]),                                 # frame tuple
+        ([], [], []),
+    ]
+    ro = np.zeros((G, 3))
+    ro.flags.writeable = False
+    bad.append(([0], [(pos, diam, vel, mass)], [(ro, None, None)]))     # read-only output
+    for args in bad:
+        with pytest.raises(ValueError):
+            check_io_arrays(*args)
