@@ -374,7 +374,9 @@ class IKContext:
 
     def download_field_async(self, out, field=FIELD_VIRIAL, slot=0):
         """out: C-contiguous float64 (G, NC) host array (pinned for overlap)."""
-        assert out.dtype == np.float64 and out.flags.c_contiguous
+        if not (isinstance(out, np.ndarray) and out.dtype == np.float64 and out.flags.c_contiguous
+                and out.flags.writeable):
+            raise ValueError("download_field_async: out must be a writeable C-contiguous float64 array")
         check(lib().ik_download_field_async(self._h, slot, field, _dp(out), out.size))
 
     def launch_count(self):
