@@ -18,8 +18,9 @@ kinetic stress.  One step = one pass of the tuned FP32 path over the 64 frames.
                triple, the GL-5-equivalent bond integral + 2D stress accumulation)
                per launch / its CUDA-event duration, against the FP32 FMA peak
                measured live on this GPU;
-  cpu_baseline the FP64 oracle (restatement of IrvingKirkwood::compute) on the host
-               cores on a bounded sample of frame 0.
+  cpu_baseline the FP64 oracle (restatement of IrvingKirkwood::compute) on all host
+               cores over whole frames (about 10 s of work), with a single-core rate
+               and the host's CPU count beside it.
 
 ``--impl reference`` times that CPU restatement of the reference's path alone.
 ``--gpus N`` under torchrun runs N independent replicas (the path is not sharded).
