@@ -59,6 +59,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ik2d_n64k_g256_gauss", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--lane-sums", default="kahan", choices=["kahan", "plain"],
+                    help="per-lane sums of the FP32 gather in the headline: Kahan-compensated (default) or plain "
+                         "FP32 (both merged across lanes and chunks with TwoSum); the other is timed beside it")
     ap.add_argument("--frames", type=int, default=0, help="override the frames per step (profiling)")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate leg")
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch leg")
@@ -74,8 +77,23 @@ def parse():
     return ap.parse_args()
 
 
+def synth_module():
+    """The seeded frame generator (pyglasstools_gb300/synth.py, numpy only), loaded by
+    path: importing it through the package would load the package's native extension,
+    which the CPU-only reference arm must not map."""
+    import importlib.util
+    name = "ik_synth_frames"
+    if name in sys.modules:
+        return sys.modules[name]
+    spec = importlib.util.spec_from_file_location(name, os.path.join(ROOT, "pyglasstools_gb300", "synth.py"))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def make_frames(wl, rank):
-    from pyglasstools_gb300 import synth
+    synth = synth_module()
     frames = [synth.make_frame(wl["N"], dim=wl["dim"], seed=10007 * rank + k) for k in range(wl["frames"])]
     grid = synth.lattice_grid(frames[0].L, wl["nmax"], wl["dim"])
     return frames, grid
@@ -178,16 +196,20 @@ def max_over_ranks(x, world):
 
 
 # ---------------------------------------------------------------------------- CPU baseline
-def cpu_sample(wl, frames, grid, g1, nthreads, k=0):
-    """Seconds the oracle takes for grid points [0, g1) of frame k on nthreads threads."""
+def cpu_sample(wl, frames, grid, g1, nthreads, k=0, fields=None):
+    """Seconds the oracle takes for grid points [0, g1) of frame k on nthreads threads
+    (its virial and kinetic fields appended to `fields` when a list is given)."""
     from oracle import oracle as O
     f = frames[k]
     box = O.make_box(wl["dim"], [f.L, f.L, f.L if wl["dim"] == 3 else 1.0])
     pot = O.make_poly12()
     cg = O.make_cg(wl["cg"]["kind"], rcut=wl["cg"]["rcut"], mode="fixedpoint", order=5, width=wl["cg"]["width"])
     t = time.perf_counter()
-    O.compute(box, f.pos, f.diam, pot, cg, grid, vel=f.vel, mass=f.mass, g0=0, g1=g1, nthreads=nthreads)
-    return time.perf_counter() - t
+    out = O.compute(box, f.pos, f.diam, pot, cg, grid, vel=f.vel, mass=f.mass, g0=0, g1=g1, nthreads=nthreads)
+    dt = time.perf_counter() - t
+    if fields is not None:
+        fields.append(out)
+    return dt
 
 
 def host_cpu_info():
@@ -242,8 +264,20 @@ def reference_arm(args, wl, name):
                                        f"seeds), FP64 oracle restating IrvingKirkwood::compute, "
                                        f"OpenMP {cores} threads",
                              "host_cpus": host_cpu_info()},
-            "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "native_libraries_mapped": repo_libraries_mapped()}
     print(json.dumps(line), flush=True)
+
+
+def repo_libraries_mapped():
+    """Shared objects of this repository mapped into the process (from /proc/self/maps;
+    None where that file does not exist): the reference arm maps only the oracle's."""
+    try:
+        with open("/proc/self/maps") as f:
+            paths = {ln.split()[-1] for ln in f if ln.rstrip().endswith(".so") or ".so." in ln}
+    except OSError:
+        return None
+    return sorted(os.path.relpath(p, ROOT) for p in paths if p.startswith(ROOT + os.sep))
 
 
 # ---------------------------------------------------------------------------- surrogate leg
@@ -396,6 +430,9 @@ def ours(args, wl, name):
         ctx.upload_frame(k, f.pos, f.diam, f.vel, f.mass)
         ctx.synchronize()
     stream = torch.cuda.ExternalStream(ctx.stream())
+    # per-lane sums of the FP32 gather: Kahan-compensated in the headline by default
+    lane_flags = ikabi.FLAG_LANE_KAHAN if args.lane_sums == "kahan" else 0
+    ctx.set_flags(lane_flags)
 
     all_slots = list(range(F))
 
@@ -460,6 +497,25 @@ def ours(args, wl, name):
     barrier(world)
     ms_max = max_over_ranks(ms, world)
     value = world * F * args.steps / (ms_max * 1e-3)
+
+    # ---- the other per-lane summation beside the headline (same frames, same graph path)
+    ctx.set_flags(ikabi.FLAG_LANE_KAHAN - lane_flags)
+    for _ in range(3):
+        step()
+    ctx.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ctx.wait_all()
+    e1.record(stream)
+    ctx.synchronize()
+    other_value = F * args.steps / (e0.elapsed_time(e1) * 1e-3)
+    ctx.set_flags(lane_flags)
+    lane_sums = {"headline": args.lane_sums,
+                 "kahan_frames_per_s": value / world if lane_flags else other_value,
+                 "plain_frames_per_s": other_value if lane_flags else value / world}
 
     # ---- end to end through the C ABI with host buffers
     pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
@@ -530,7 +586,7 @@ def ours(args, wl, name):
     err_v, err_k = relerr(v32, v64), relerr(k32, k64)
 
     # ---- roofline of the gather kernel (per-launch CUDA events around it)
-    ctx.set_flags(ikabi.FLAG_TIMING)
+    ctx.set_flags(ikabi.FLAG_TIMING | lane_flags)
     gms, trip, stages = [], [], []
     for k in range(F):
         ctx.compute_slot(k, "fp32")
@@ -539,7 +595,7 @@ def ours(args, wl, name):
         stages.append(t4)
         gms.append(t4[2])
         trip.append(ctx.counters(k)[2])
-    ctx.set_flags(0)
+    ctx.set_flags(lane_flags)
     stage_ms = np.mean(np.array(stages), axis=0)
     g_ms = float(np.mean(gms))
     A = float(np.mean(trip))
@@ -568,7 +624,8 @@ def ours(args, wl, name):
            "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
            "gpu_launches": int(launches),
            "clocks": clocks.summary(t_soak, t_host1),
-           "roofline": {"bound": "fp32", "kernel": "k_gather32", "achieved": achieved, "peak": peak,
+           "roofline": {"bound": "fp32",
+                        "kernel": "k_gather32<KAHAN=%d>" % (1 if lane_flags else 0), "achieved": achieved, "peak": peak,
                         "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                         "flop_per_launch": flop, "active_triples_per_launch": A, "launch_ms": g_ms,
                         "peak_source": "measured live: FFMA throughput probe (ik_measure_fp32_peak)"},
@@ -580,6 +637,7 @@ def ours(args, wl, name):
            "plain_fp64": {"value": plain_value, "unit": "frames/s", "frames_timed": nplain},
            "tuned_over_plain": value / plain_value,
            "rel_err_vs_fp64": {"virial": err_v, "kinetic": err_k},
+           "lane_sums": lane_sums,
            "interactions_per_s": A * value}
     if surrogate is not None:
         out["surrogate"] = surrogate
@@ -590,9 +648,14 @@ def ours(args, wl, name):
         cores = O.threads(os.cpu_count() or 1)  # threads the oracle's loops actually run on
         G = len(grid)
         t, nf = 0.0, 0  # whole frames, the step's frames cycled, until about 10 s of CPU work
+        o0 = []  # the oracle's fields of frame 0: the error of both GPU paths against them
         while nf < 4096 and t < 10.0:
-            t += cpu_sample(wl, frames, grid, G, cores, k=nf % len(frames))
+            t += cpu_sample(wl, frames, grid, G, cores, k=nf % len(frames), fields=o0 if nf == 0 else None)
             nf += 1
+        out["rel_err_vs_oracle_frame0"] = {
+            "tuned_fp32": {"virial": relerr(v32, o0[0][0]), "kinetic": relerr(k32, o0[0][1])},
+            "plain_fp64": {"virial": relerr(v64, o0[0][0]), "kinetic": relerr(k64, o0[0][1])},
+            "note": "relative L2 per stress component over the grid, FP64 CPU oracle (GL-5) of frame 0"}
         out["cpu_baseline"] = {"value": nf / t, "unit": "frames/s", "cores": cores, "kind": "port",
                                "sample": f"{nf} whole frame(s) of the workload (the step's {len(frames)} frames "
                                          f"cycled), FP64 oracle "

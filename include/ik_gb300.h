@@ -233,21 +233,25 @@ int ik_download_field_async(ik_ctx* ctx, int slot, int field, double* host_out, 
 int ik_measure_fp32_peak(int device, double* tflops);
 
 /* No-allocation variant of the plain FP64 computation (ik_compute with IK_PREC_FP64),
- * for callers that cannot call cudaMalloc: code running where the allocator may not
- * be entered (host callbacks, real-time loops), or in processes whose device memory
- * belongs to another framework's pool or a budget fixed at start-up.  No counterpart
- * in the reference.  Allocates nothing: the caller passes DEVICE pointers for inputs
- * (d_pos n x 3, d_diam n, optional d_vel n x 3 and d_mass n, d_grid g x 3) and outputs
- * (d_virial and optional d_kinetic, each g x NC FP64 with NC = 3 in 2D (xx, yy, xy)
- * or 6 in 3D (xx, yy, zz, xy, xz, yz)); all scratch is a static device array of about
- * 4.3 MB that every GPU loading the library holds until exit.  Limits: n <= 4096
- * particles (larger n is rejected with IK_ERR_CAPACITY), at most 32 force-active
- * bonds per particle.  Runs on `stream` (a cudaStream_t; NULL = default stream) and
- * returns after that stream has finished.  The first call on each device sets up
- * the scratch address; make it before any stream capture.  Calls share the scratch
- * array: calls that overlap on the GPU race and must be serialised by the caller.
- * Box, potential and coarse-graining arguments mean what they mean in ik_set_box,
- * ik_set_potential_poly12, ik_set_max_rcut and ik_set_cgfunc (fixed-point mode). */
+ * for callers that cannot call cudaMalloc: processes whose device memory belongs to
+ * another framework's pool, services under a device-memory budget fixed at start-up,
+ * and code that must not enter cudaMalloc because it can wait for other streams' work.
+ * No counterpart in the reference.  Allocates nothing: the caller passes DEVICE
+ * pointers for inputs (d_pos n x 3, d_diam n, optional d_vel n x 3 and d_mass n,
+ * d_grid g x 3) and outputs (d_virial and optional d_kinetic, each g x NC FP64 with
+ * NC = 3 in 2D (xx, yy, xy) or 6 in 3D (xx, yy, zz, xy, xz, yz)); all scratch is a
+ * static device array of about 4.3 MB that every GPU loading the library holds until
+ * exit.  Limits: n <= 4096 particles (larger n is rejected with IK_ERR_CAPACITY), at
+ * most 32 force-active bonds per particle (IK_ERR_CAPACITY after the run).  Runs on
+ * `stream` (a cudaStream_t; NULL = default stream).  The call is synchronous: it makes
+ * CUDA runtime calls and returns after that stream has finished, so it must not be
+ * made from a stream callback or a host function (cudaLaunchHostFunc).  The first
+ * call in each CUDA context (the first call on each device, for the primary context)
+ * sets up the scratch address; make it before any stream capture.  Calls share the
+ * scratch array: calls that overlap on the GPU race and must be serialised by the
+ * caller.  Box, potential and coarse-graining arguments mean what they mean in
+ * ik_set_box, ik_set_potential_poly12, ik_set_max_rcut and ik_set_cgfunc
+ * (fixed-point mode). */
 int ik_compute_fp64_noalloc(int dim, const double boxsize[3], const double origin[3],
                             double scaled_rcut, const double params[5], double max_rcut,
                             int cg_kind, int gl_order, double cg_rcut, double cg_width,
@@ -329,6 +333,15 @@ int ik_mlp_eval(ik_mlp* m, int64_t n, const float* feats, float* out, int kernel
  * bins of (w, d, a, b) with >= 8 samples and max |B_net - B_label| <= tol */
 int ik_mlp_validate(ik_mlp* m, int64_t n, uint64_t seed, double tol, double* coverage, double* max_err,
                     double* rms_err, double* bin_err, int64_t nbins);
+/* Failure-detection test hook (no reference counterpart; the reference's quadrature
+ * failures abort the process through GSL's default handler, cgfunc/Quadrature.h:47-49,
+ * and its exception hook calls MPI_Abort, pyglasstools/__init__.py:26-35).  With
+ * on != 0 the tensor-core inference kernels of this surrogate issue no MMA and wait for
+ * its completion with a poll limit of 64: the wait runs out, the kernel frees its
+ * tensor memory and returns, and the call reports IK_ERR_TIMEOUT (ik_mlp_eval,
+ * ik_mlp_validate; ik_synchronize for an IK computation in surrogate mode), with the
+ * CUDA context left usable.  on = 0 restores normal operation. */
+int ik_mlp_test_stall(ik_mlp* m, int on);
 /* Attach a validated surrogate to a context; used by ik_set_cgfunc(.., IK_QUAD_MLP, ..)
  * on the FP32 path.  The caller keeps the surrogate alive while attached. */
 int ik_set_mlp(ik_ctx* ctx, ik_mlp* m);

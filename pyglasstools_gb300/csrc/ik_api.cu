@@ -12,6 +12,8 @@
 #include <atomic>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 namespace {
 
 thread_local std::string g_err;
@@ -70,6 +72,26 @@ struct DevBuf {
 };
 
 #define ENS(buf, n) do { int r_ = (buf).ensure(n); if (r_) return r_; } while (0)
+
+// NVTX ranges around the host-side phases (upload, cell list, bonds, gather, finish,
+// download): a profiler's timeline shows which phase enqueued which launches.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+// Consecutive phases of one function: next() closes the open range and opens another.
+struct NvtxPhases {
+    bool open = false;
+    void next(const char* name)
+    {
+        if (open) nvtxRangePop();
+        nvtxRangePushA(name);
+        open = true;
+    }
+    ~NvtxPhases() { if (open) nvtxRangePop(); }
+};
 
 // Box, grid and the binning derived from them.  The context holds one; a slot with a
 // geometry of its own (frames of different boxes in one batch) holds another, swapped
@@ -591,7 +613,9 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
     const IkGeom& g = c->geo.geom;
     const int D = c->dim, NC = D == 2 ? 3 : 6;
     const int n = (int)s.n;
+    NvtxPhases nv;
     if (c->io_cur && n > 0) { // ik_compute_batch_io: this frame's inputs, copied on its lane
+        nv.next("ik upload");
         const IoFrame& io = *c->io_cur;
         CK(cudaMemcpyAsync(s.pos.p, io.pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, L.st));
         CK(cudaMemcpyAsync(s.diam.p, io.diam, sizeof(double) * n, cudaMemcpyHostToDevice, L.st));
@@ -610,6 +634,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
     CK(cudaMemsetAsync(s.counters.p, 0, sizeof(unsigned long long) * 4, L.st));
     if (!(fields & IK_FIELD_KINETIC)) CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->geo.G, L.st));
     if (!(fields & IK_FIELD_VIRIAL)) CK(cudaMemsetAsync(s.vir.p, 0, sizeof(double) * NC * c->geo.G, L.st));
+    nv.next("ik cells");
     int r = build_cells(c, s, g, L.st, L.cell_of, L.rank, L.cell_count, L.cell_start, L.sorted, L.bsum_cells,
                         prec == IK_PREC_FP32 ? &L.relhi : nullptr, prec == IK_PREC_FP32 ? &L.rello : nullptr);
     if (r) return r;
@@ -641,6 +666,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         // when the staged (offset << 6 | count) word would not hold the offsets
         const bool stride = (size_t)std::max(n, 1) * (size_t)c->maxb < ((size_t)1 << 25) &&
                             !(c->flags & IK_FLAG_CSR_BONDS);
+        nv.next("ik bonds");
         ENS(L.bonds_tmp, sizeof(float4) * (size_t)c->maxb * std::max(n, 1));
         ENS(L.nb32, sizeof(int) * (std::max(n, 1) + 1));
         const bool main_pass = (fields & (IK_FIELD_VIRIAL | IK_FIELD_KINETIC)) != 0;
@@ -662,6 +688,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         }
         const float4* bonds = stride ? L.bonds_tmp.as<float4>() : L.bonds32.as<float4>();
         if (timing) CK(cudaEventRecord(c->ev[2], L.st));
+        nv.next("ik gather");
         GatherArgs32 a{};
         a.g = g;
         for (int k = 0; k < 3; ++k) {
@@ -759,11 +786,13 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
             c->launches += 1;
         }
         // FP64 finish: ((double)hi + (double)lo) * normalisation (0.5 of the GL map for the virial)
+        nv.next("ik finish");
         CK(launch_pairs_to_f64(L.vir2.as<float2>(), mlp ? L.corr.as<unsigned long long>() : nullptr,
                                (a.fields & 1) ? s.vir.as<double>() : nullptr, 0.5 * norm, L.kin2.as<float2>(),
                                (a.fields & 2) ? s.kin.as<double>() : nullptr, norm, (long long)NC * c->geo.G, L.st));
         c->launches += (c->geo.G > 0 && a.fields) ? 1 : 0;
         if (fields & IK_FIELD_ELASTIC) { // the elastic virial field: same staging, elastic records
+            nv.next("ik elastic");
             if (int r2 = elastic_bonds(c, s, L, g, n)) return r2;
             GatherArgs32 e = a;
             e.boff = nullptr;
@@ -792,6 +821,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         }
     } else {
         if (timing) CK(cudaEventRecord(c->ev[1], L.st));
+        nv.next("ik bonds");
         ENS(L.bonds64, sizeof(IkB64) * (size_t)c->maxb * std::max(n, 1));
         ENS(L.nb64, sizeof(int) * std::max(n, 1));
         const bool main_pass = (fields & (IK_FIELD_VIRIAL | IK_FIELD_KINETIC)) != 0;
@@ -803,6 +833,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
             CK(cudaGetLastError());
         }
         if (timing) CK(cudaEventRecord(c->ev[2], L.st));
+        nv.next("ik gather");
         GatherArgs64 a{};
         a.g = g;
         a.cg = c->cg;
@@ -834,6 +865,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
             c->launches += (n > 0 ? 1 : 0) + (c->geo.G > 0 ? 1 : 0);
         }
         if (fields & IK_FIELD_ELASTIC) { // the elastic virial field
+            nv.next("ik elastic");
             if (int r2 = elastic_bonds(c, s, L, g, n)) return r2;
             GatherArgs64 e = a;
             e.bonds = L.eb64.as<IkB64>();
@@ -848,6 +880,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         }
     }
     if (c->io_cur && c->geo.G > 0) { // ik_compute_batch_io: this frame's fields to the host
+        nv.next("ik download");
         const DevBuf* src[3] = {&s.vir, &s.kin, &s.ela};
         for (int f = 0; f < 3; ++f)
             if (c->io_cur->out[f] && (fields & (1 << f)))
@@ -1241,6 +1274,7 @@ int ik_reserve_slots(ik_ctx* c, int nslots)
 static int upload_impl(ik_ctx* c, int slot, int64_t n, const void* pos, const void* vel, const void* mass,
                        const void* diam, bool f32)
 {
+    NvtxRange nvr("ik upload");
     if (int r = check_ctx(c)) return r;
     if (int r = slot_ok(c, slot)) return r;
     if (n < 0 || n >= (1 << 25)) return fail(IK_ERR_ARG, "particle count %lld out of range (max 2^25 - 1)", (long long)n);
@@ -1345,6 +1379,7 @@ int ik_compute_slot(ik_ctx* c, int slot, int precision, int fields)
 
 int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int fields)
 {
+    NvtxRange nvr("ik compute_batch");
     if (int r = check_ctx(c)) return r;
     if (count < 1 || !slots) return fail(IK_ERR_ARG, "empty batch");
     for (int k = 0; k < count; ++k) if (int r = slot_ok(c, slots[k])) return r;
@@ -1450,6 +1485,7 @@ int ik_compute_batch_io(ik_ctx* c, const int* slots, int count, int precision, i
                         const double* const* pos, const double* const* vel, const double* const* mass,
                         const double* const* diam, double* const* out)
 {
+    NvtxRange nvr("ik compute_batch_io");
     if (int r = check_ctx(c)) return r;
     if (count < 1 || !slots || !n || !pos || !diam || !out) return fail(IK_ERR_ARG, "empty batch or null array");
     if (precision != IK_PREC_FP64 && precision != IK_PREC_FP32) return fail(IK_ERR_ARG, "unknown precision %d", precision);
@@ -1577,6 +1613,7 @@ int ik_compute_batch_io(ik_ctx* c, const int* slots, int count, int precision, i
 
 int ik_synchronize(ik_ctx* c)
 {
+    NvtxRange nvr("ik synchronize");
     if (int r = check_ctx(c)) return r;
     for (int attempt = 0; attempt < 4; ++attempt) {
         for (Lane& L : c->lanes) CK(cudaStreamSynchronize(L.st));
@@ -1658,6 +1695,7 @@ int ik_compute(ik_ctx* c, int precision, int fields)
 
 int ik_get_field(ik_ctx* c, int slot, int field, double* out, int64_t count)
 {
+    NvtxRange nvr("ik download");
     if (int r = check_ctx(c)) return r;
     if (int r = slot_ok(c, slot)) return r;
     GeoSwap gs(c, slot);
@@ -2036,6 +2074,7 @@ int ik_get_stream(ik_ctx* c, void** stream)
 
 int ik_download_field_async(ik_ctx* c, int slot, int field, double* host_out, int64_t count)
 {
+    NvtxRange nvr("ik download");
     if (int r = check_ctx(c)) return r;
     if (int r = slot_ok(c, slot)) return r;
     GeoSwap gs(c, slot);

@@ -583,13 +583,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t a, uint32_t parity)
         : "memory");
     return ok != 0;
 }
-// bounded wait: false if the phase did not complete within the iteration limit
-__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity)
+// bounded wait: false if the phase did not complete within `limit` polls
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, int limit = 1 << 22)
 {
-    for (int it = 0; it < (1 << 22); ++it)
+    for (int it = 0; it < limit; ++it)
         if (mbar_try_wait(a, parity)) return true;
     return false;
 }
+// Failure-detection test hook (ik_mlp_test_stall): no MMA is issued and nothing is
+// committed to the completion barrier, so its wait runs out after this many polls;
+// no asynchronous tensor-core work is in flight when the kernel then gives up.
+constexpr int TC_STALL_POLLS = 64;
 // 32 lanes x 32 bits, 16 consecutive columns: thread l of warp w gets TMEM lane 32 w + l
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
 {
@@ -663,9 +667,10 @@ __device__ __forceinline__ int mlp_record_coords(const float4 r, float to_w, flo
 
 // MODE 0: out[i] = surrogate B of feats[i] (units of w, un-normalised);
 // MODE 1: IK records -> fixed-point stress corrections.
+// stall != 0: the failure-detection test hook (TC_STALL_POLLS).
 template <int MODE>
 __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __restrict__ blob, const float4* feats,
-                                                     long long n, float* out, MlpRecArgs R, int* status)
+                                                     long long n, float* out, MlpRecArgs R, int* status, int stall)
 {
     extern __shared__ __align__(1024) unsigned char tsm[];
     unsigned char* sA0 = tsm + TC_A0;
@@ -758,7 +763,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
         if (*abort_flag) break;
 #pragma unroll 1
         for (int layer = 0; layer < 3; ++layer) {
-            if (t == 0) {
+            if (t == 0 && !stall) {
                 fence_after();
                 if (layer == 0) {
                     umma_bf16(tmem, umma_desc(aA0, 128, 256), umma_desc(aW1, 128, 256), ID, 0u);
@@ -772,7 +777,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
                 }
                 umma_commit(aBar);
             }
-            if (!mbar_wait(aBar, phase)) {
+            if (!mbar_wait(aBar, phase, stall ? TC_STALL_POLLS : 1 << 22)) {
                 atomicOr(status, IK_ST_MMA_TIMEOUT);
                 *abort_flag = 1;
             }
@@ -892,6 +897,7 @@ struct ik_mlp {
     long long steps = 0;
     double last_loss = 0.0;
     MlpGL gl{};
+    int stall = 0; // failure-detection test hook (ik_mlp_test_stall)
 };
 
 static int mfail(int code, const char* fmt, ...)
@@ -956,7 +962,7 @@ static int run_tc(ik_mlp* m, long long n, const float4* f, float* out)
     const int blocks = (int)std::min<long long>(std::max<long long>(tiles, 1), (long long)m->sm_count * 4);
     MlpRecArgs none{};
     k_mlp_infer_tc<0><<<blocks, 128, TC_SMEM_LAUNCH, m->st>>>(m->blob.as<unsigned char>(), f, n, out, none,
-                                                               m->status.as<int>());
+                                                               m->status.as<int>(), m->stall);
     MCK(cudaGetLastError());
     int st = 0;
     MCK(cudaMemcpyAsync(&st, m->status.p, sizeof(int), cudaMemcpyDeviceToHost, m->st));
@@ -996,7 +1002,7 @@ cudaError_t launch_mlp_records(ik_mlp* m, const float4* rec, const int2* rid, co
     R.nc = nc;
     R.corr = corr;
     k_mlp_infer_tc<1><<<blocks, 128, TC_SMEM_LAUNCH, st>>>(m->blob.as<unsigned char>(), nullptr, 0, nullptr, R,
-                                                            status);
+                                                            status, m->stall);
     return cudaGetLastError();
 }
 
@@ -1202,6 +1208,13 @@ int ik_mlp_train(ik_mlp* m, int64_t nsamples, int epochs, int ctas, double lr, u
     m->last_loss = lh.empty() ? 0.0 : lh.back() / (double)batch;
     m->validated = false;
     return deploy(m);
+}
+
+int ik_mlp_test_stall(ik_mlp* m, int on)
+{
+    if (int r = mcheck(m)) return r;
+    m->stall = on ? 1 : 0;
+    return IK_OK;
 }
 
 int ik_mlp_eval(ik_mlp* m, int64_t n, const float* feats, float* out, int kernel)

@@ -1,11 +1,17 @@
 // ik_noalloc.cu -- ik_compute_fp64_noalloc: the plain FP64 Irving-Kirkwood computation
-// for callers that must not allocate device memory.
+// for callers that cannot allocate device memory.
 //
-// Who needs it: code that runs where cudaMalloc is unavailable or forbidden -- inside
-// a host callback or a real-time loop that may not block on the allocator, in a
-// process whose device memory is owned by another framework's pool, or under a
-// memory budget fixed at start-up.  Such callers bring their own input and output
+// Who needs it: a process whose device memory is owned by another framework's pool
+// (a caching allocator that has reserved the device, where a cudaMalloc from this
+// library would fail or fragment it), a service under a device-memory budget fixed at
+// start-up, and code that must not enter cudaMalloc because cudaMalloc may wait for
+// work on other streams of the device.  Such callers bring their own input and output
 // buffers; this entry point brings the rest.
+//
+// The call is synchronous: it makes CUDA runtime calls (cudaMemsetAsync, kernel
+// launches, cudaMemcpyAsync, cudaStreamSynchronize) and returns once the caller's
+// stream has finished.  It must not be called from a stream callback or a host
+// function (cudaLaunchHostFunc), where CUDA calls are not permitted.
 //
 // All scratch (cell list, sorted particle ids, FP64 bond records, status words)
 // lives in one file-scope __device__ array of IK_NOALLOC_SCRATCH_BYTES (about 4.3 MB).
@@ -15,9 +21,10 @@
 // array keeps the previous call's contents; everything that must start at zero is
 // cleared on the caller's stream at the start of each call.
 //
-// The first call on each device looks up the array's device address
-// (cudaGetSymbolAddress, with that device current); make that first call before any
-// stream capture on the device.
+// The array's address belongs to a CUDA context.  The first call in each context (for
+// the usual primary context: the first call on each device) looks it up with
+// cudaGetSymbolAddress, with that context current, and caches it under the context's
+// unique id; make that first call before any stream capture in the context.
 #include "ik_kernels.h"
 #include "../../include/ik_gb300.h"
 
@@ -56,47 +63,53 @@ int na_fail(int code, const char* msg)
     return code;
 }
 
-constexpr int NA_MAX_DEVICES = 64;
-unsigned char* na_ptr[NA_MAX_DEVICES] = {nullptr};
+// Scratch addresses by CUDA context.  A context id (cuCtxGetId) is unique for the
+// life of the process, so a context created after cudaDeviceReset -- even at a reused
+// handle -- gets a set-up of its own.
+constexpr int NA_MAX_CONTEXTS = 64;
+struct NaEntry { unsigned long long ctx_id; unsigned char* ptr; };
+NaEntry na_cache[NA_MAX_CONTEXTS];
+int na_cached = 0;
 std::mutex na_mutex;
+typedef int (*na_ctx_current_fn)(void** ctx);
+typedef int (*na_ctx_id_fn)(void* ctx, unsigned long long* id);
+na_ctx_current_fn na_ctx_current = nullptr;
+na_ctx_id_fn na_ctx_id = nullptr;
 
-// Device address of the scratch array on the current device (set up once per device).
+// Device address of the scratch array in the current context (set up once per context).
 int na_scratch(unsigned char** out)
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return na_fail(IK_ERR_CUDA, "cudaGetDevice failed");
-    if (dev < 0 || dev >= NA_MAX_DEVICES) return na_fail(IK_ERR_UNSUPPORTED, "device index too large");
     std::lock_guard<std::mutex> lk(na_mutex);
-    if (!na_ptr[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, ik_noalloc_scratch);
-        if (e != cudaSuccess || !p) return na_fail(IK_ERR_CUDA, "cudaGetSymbolAddress of the scratch array failed");
-        na_ptr[dev] = static_cast<unsigned char*>(p);
+    if (!na_ctx_current || !na_ctx_id) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+            q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return na_fail(IK_ERR_CUDA, "the driver's context queries (cuCtxGetCurrent, cuCtxGetId) are unavailable");
+        na_ctx_current = reinterpret_cast<na_ctx_current_fn>(f1);
+        na_ctx_id = reinterpret_cast<na_ctx_id_fn>(f2);
     }
-    *out = na_ptr[dev];
+    void* ctx = nullptr;
+    unsigned long long id = 0;
+    if (na_ctx_current(&ctx) != 0) return na_fail(IK_ERR_CUDA, "cuCtxGetCurrent failed");
+    if (!ctx) { // no context on this thread yet: the device's primary context
+        if (cudaSetDevice(dev) != cudaSuccess || na_ctx_current(&ctx) != 0 || !ctx)
+            return na_fail(IK_ERR_CUDA, "no CUDA context could be made current");
+    }
+    if (na_ctx_id(ctx, &id) != 0) return na_fail(IK_ERR_CUDA, "cuCtxGetId failed");
+    for (int k = 0; k < na_cached; ++k)
+        if (na_cache[k].ctx_id == id) { *out = na_cache[k].ptr; return IK_OK; }
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, ik_noalloc_scratch);
+    if (e != cudaSuccess || !p) return na_fail(IK_ERR_CUDA, "cudaGetSymbolAddress of the scratch array failed");
+    if (na_cached == NA_MAX_CONTEXTS) na_cached = 0; // full: start over (set-ups are redone on demand)
+    na_cache[na_cached++] = NaEntry{id, static_cast<unsigned char*>(p)};
+    *out = static_cast<unsigned char*>(p);
     return IK_OK;
-}
-
-void na_gl_rule(int n, double* x, double* w)
-{
-    // Gauss-Legendre nodes/weights on [-1,1]: Newton on the three-term recurrence.
-    for (int k = 0; k < n; ++k) {
-        long double z = cosl(3.14159265358979323846264338327950288L * (k + 0.75L) / (n + 0.5L)), pp = 1.0L;
-        for (int it = 0; it < 100; ++it) {
-            long double p0 = 1.0L, p1 = z;
-            for (int j = 2; j <= n; ++j) { long double p2 = ((2.0L * j - 1.0L) * z * p1 - (j - 1.0L) * p0) / j; p0 = p1; p1 = p2; }
-            pp = n * (z * p1 - p0) / (z * z - 1.0L);
-            long double dz = p1 / pp;
-            z -= dz;
-            if (fabsl(dz) < 1e-19L) break;
-        }
-        long double p0 = 1.0L, p1 = z;
-        for (int j = 2; j <= n; ++j) { long double p2 = ((2.0L * j - 1.0L) * z * p1 - (j - 1.0L) * p0) / j; p0 = p1; p1 = p2; }
-        pp = n * (z * p1 - p0) / (z * z - 1.0L);
-        x[n - 1 - k] = (double)z;
-        w[n - 1 - k] = (double)(2.0L / ((1.0L - z * z) * pp * pp));
-    }
-    if (n % 2 == 1) x[n / 2] = 0.0;
 }
 
 } // namespace
@@ -184,7 +197,7 @@ extern "C" int ik_compute_fp64_noalloc(int dim, const double boxsize[3], const d
         a.all[k] = (k < dim && 2 * a.reach[k] + 1 >= geo.nc[k]) ? 1 : 0;
     }
     double gx[64], gw[64];
-    na_gl_rule(gl_order, gx, gw);
+    ik_gl_rule(gl_order, gx, gw);
     a.nq = gl_order;
     for (int k = 0; k < gl_order; ++k) { a.xs[k] = 0.5 + 0.5 * gx[k]; a.ws[k] = gw[k]; }
 
@@ -239,9 +252,9 @@ extern "C" int ik_compute_fp64_noalloc(int dim, const double boxsize[3], const d
     if (d_kinetic && !d_vel && g > 0)
         NA_CK(cudaMemsetAsync(d_kinetic, 0, sizeof(double) * (dim == 2 ? 3 : 6) * g, st));
     if (g > 0) NA_CK(launch_gather64(a, st));
+    int hs = 0; // the status word, read on the caller's stream (not the legacy default stream)
+    NA_CK(cudaMemcpyAsync(&hs, status, sizeof(int), cudaMemcpyDeviceToHost, st));
     NA_CK(cudaStreamSynchronize(st));
-    int hs = 0;
-    NA_CK(cudaMemcpy(&hs, status, sizeof(int), cudaMemcpyDeviceToHost));
     if (hs & IK_ST_BAD_INPUT)
         return na_fail(IK_ERR_ARG, "invalid frame: a position is not finite, a diameter is not > 0, or a 2D frame has z != 0");
     if (hs & IK_ST_BOND_OVERFLOW) return na_fail(IK_ERR_CAPACITY, "a particle has more than 32 force-active bonds");

@@ -103,6 +103,7 @@ def lib():
             "ik_mlp_grad": ([vp, i64, fp, fp, fp, dp], i32),
             "ik_mlp_train": ([vp, i64, i32, i32, C.c_double, C.c_uint64, dp, i64], i32),
             "ik_mlp_eval": ([vp, i64, fp, fp, i32], i32),
+            "ik_mlp_test_stall": ([vp, i32], i32),
             "ik_mlp_validate": ([vp, i64, C.c_uint64, C.c_double, dp, dp, dp, dp, i64], i32),
         }
         for name, (args, res) in sig.items():
@@ -497,6 +498,11 @@ class MLP:
         hist = np.zeros(steps, dtype=np.float64)
         check(lib().ik_mlp_train(self._h, nsamples, epochs, ctas, lr, seed, _dp(hist), steps))
         return hist
+
+    def test_stall(self, on=True):
+        """Failure-detection test hook: the tensor-core kernels issue no MMA and their
+        bounded completion wait runs out (IK_ERR_TIMEOUT) until turned off again."""
+        check(lib().ik_mlp_test_stall(self._h, 1 if on else 0))
 
     def eval(self, feats, kernel=0):
         """kernel 0: tensor cores (BF16); 1: CUDA cores, BF16 arithmetic; 2: CUDA cores, FP32."""

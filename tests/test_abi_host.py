@@ -169,7 +169,8 @@ def test_gsd_reader_rejects_corrupt_files(tmp_path, golden):
 
 
 def test_reference_fixture_decodes_if_present():
-    path = "/root/reference/example_scripts/polydisperse12.gsd"
+    path = os.path.join(os.environ.get("PYGLASSTOOLS_REF", "/root/reference"), "example_scripts",
+                        "polydisperse12.gsd")
     if not os.path.exists(path):
         pytest.skip("reference fixture not on this machine")
     from pyglasstools_gb300 import gsd

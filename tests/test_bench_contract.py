@@ -38,6 +38,10 @@ def test_reference_arm_json_line():
     e2e = line["e2e"]
     assert e2e == {"value": line["value"], "unit": "frames/s",
                    "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    # the reference arm runs the oracle alone: none of the product's native libraries
+    mapped = line["native_libraries_mapped"]
+    assert mapped is not None and any(p.startswith("oracle") for p in mapped), mapped
+    assert not any(p.startswith("pyglasstools_gb300") for p in mapped), mapped
 
 
 def test_reference_arm_nonzero_rank_is_silent():

@@ -191,3 +191,50 @@ def test_ik_surrogate_mode_errors(ik, trained):
         c.set_mlp(trained)
         with pytest.raises(ik.IKError):
             c.compute("fp64")                                  # FP32 path only
+
+
+def test_bounded_tensor_core_wait_reports_timeout_and_context_survives(ik, trained):
+    """Failure detection without a GPU fault: with the test hook on, the tensor-core
+    kernels issue no MMA, so their completion wait (an mbarrier polled a bounded number
+    of times) runs out; the kernels free their tensor memory and return, and the status
+    comes back as IK_ERR_TIMEOUT -- from a direct evaluation and from an IK computation
+    in surrogate mode.  Afterwards the same context computes correctly again.  (The
+    reference has no such path: GSL's handler or MPI_Abort ends the process,
+    cgfunc/Quadrature.h:47-49, pyglasstools/__init__.py:26-35.)"""
+    from pyglasstools_gb300 import synth
+    f, _ = trained.samples(3000, seed=91)
+    want = trained.eval(f, kernel=0)
+    trained.test_stall(True)
+    try:
+        with pytest.raises(ik.IKError) as ei:
+            trained.eval(f, kernel=0)
+        assert ei.value.code == -6  # IK_ERR_TIMEOUT
+        assert "gave up" in str(ei.value)
+    finally:
+        trained.test_stall(False)
+    np.testing.assert_array_equal(trained.eval(f, kernel=0), want)
+
+    fr = synth.make_frame(3000, dim=2, seed=92)
+    grid = synth.lattice_grid(fr.L, 40, 2)
+    trained.validate(n=1 << 16, seed=93, tol=1.0)
+    with ik.IKContext() as c:
+        c.set_box(2, [fr.L, fr.L, 1.0])
+        c.set_poly12()
+        c.set_cgfunc("gaussian", 6.0, mode="mlp", order=5, width=2.0)
+        c.set_mlp(trained)
+        c.set_grid(grid)
+        c.set_frame(fr.pos, fr.diam, fr.vel, fr.mass)
+        c.compute("fp32")
+        v_ok = c.get_field(ik.FIELD_VIRIAL)
+        trained.test_stall(True)
+        try:
+            with pytest.raises(ik.IKError) as ei:
+                c.compute("fp32")
+            assert ei.value.code == -6
+        finally:
+            trained.test_stall(False)
+        c.compute("fp32")
+        np.testing.assert_array_equal(c.get_field(ik.FIELD_VIRIAL), v_ok)
+        c.set_cgfunc("gaussian", 6.0, mode="fixedpoint", order=5, width=2.0)
+        c.compute("fp64")  # and the plain path on the same context
+        assert np.all(np.isfinite(c.get_field(ik.FIELD_VIRIAL)))
