@@ -14,13 +14,16 @@ positions of the two ends along it.  This module holds
 
 * ``label``: B in closed form (clip the segment to the ball, then the error function
   along the line) -- the exact answer the GPU's adaptive-quadrature labels must match;
-* ``base`` / ``targets``: the midpoint rule on the clipped segment, and the relative
-  correction y = B / base - 1 the network predicts;
+* ``base`` / ``targets``: four-point Gauss-Legendre on the clipped segment, and the
+  scaled relative correction y = (B / base - 1) * YSCALE the network predicts;
 * ``inputs`` / ``forward`` / ``loss_and_grad``: the network 4 -> 64 -> 64 -> 64 -> 1
   with SiLU in FP64 and its exact gradient by reverse-mode differentiation, in the
   parameter layout of the C ABI (W1[64][4], b1, W2[64][64], b2, W3[64][64], b3, w4, b4);
-* ``forward_bf16``: the deployed arithmetic (BF16 weights, activations as BF16 hi + lo
-  pairs, the first layer split three ways, SiLU through tanh), accumulated in FP64.
+* ``forward_bf16``: the deployed arithmetic (BF16 weights and activations, the first
+  layer split three ways, SiLU through tanh), accumulated in FP64.
+
+The mirrored kernels are in pyglasstools_gb300/csrc/ik_mlp.cu (mlp_base, k_mlp_samples,
+k_mlp_infer_simt, k_mlp_infer_tc).
 """
 from __future__ import annotations
 
@@ -38,6 +41,7 @@ O_B3 = O_W3 + H * H
 O_W4 = O_B3 + H
 O_B4 = O_W4 + H
 NPAR = O_B4 + 1
+YSCALE = 1.0e4  # network output = (B / base - 1) * YSCALE
 
 _erf = np.vectorize(math.erf)
 
@@ -124,39 +128,41 @@ def bf16(v):
 
 
 def base(feats):
-    """Midpoint rule on the part of the bond inside the support: s1 exp(-(d^2 + m^2)/2)
-    with t_c = sqrt(9 - d^2), s1 = (t_c - a)/(b - a) clipped to [0, 1], m = (a + t_c)/2."""
+    """Four-point Gauss-Legendre on the part of the bond inside the support:
+    s1/2 sum_k w_k exp(-(d^2 + t_k^2)/2), t_k = a + s1 (b - a)(1 + x_k)/2, with
+    t_c = sqrt(9 - d^2) and s1 = (t_c - a)/(b - a) clipped to [0, 1]."""
     f = np.asarray(feats, dtype=np.float32).astype(np.float64)
     d, a, b = f[:, 0], f[:, 1], f[:, 2]
     tc = np.sqrt(np.maximum(9.0 - d * d, 0.0))
     s1 = np.clip((tc - a) / np.where(b - a > 0, b - a, 1.0), 0.0, 1.0)
-    m = 0.5 * (a + tc)
-    return s1 * np.exp(-0.5 * (d * d + m * m))
+    x, w = np.polynomial.legendre.leggauss(4)
+    h = 0.5 * s1 * (b - a)
+    t = (a + h)[:, None] + h[:, None] * x[None, :]
+    return 0.5 * s1 * np.sum(w[None, :] * np.exp(-0.5 * (d[:, None] ** 2 + t * t)), axis=1)
 
 
 def targets(feats, labels):
-    """Training targets y = B / base - 1."""
+    """Training targets y = (B / base - 1) * YSCALE."""
     bs = base(feats)
-    return np.where(bs > 1e-30, np.asarray(labels) / np.where(bs > 1e-30, bs, 1.0) - 1.0, 0.0)
+    return np.where(bs > 1e-30, (np.asarray(labels) / np.where(bs > 1e-30, bs, 1.0) - 1.0) * YSCALE, 0.0)
 
 
-def _pair(v):
-    hi = bf16(v)
-    return hi + bf16(v - hi)
+def value(feats, y):
+    """B from the network's output y: base (1 + y / YSCALE)."""
+    return base(feats) * (1.0 + np.asarray(y, dtype=np.float64) / YSCALE)
 
 
 def forward_bf16(p, feats):
-    """B of the deployed network: BF16 weights; the first layer split three ways
-    (x_hi W_hi + x_lo W_hi + x_hi W_lo); activations as BF16 hi + lo pairs; FP64
-    accumulation; tanh-form SiLU."""
+    """y of the deployed network: BF16 weights; the first layer split three ways
+    (x_hi W_hi + x_lo W_hi + x_hi W_lo); BF16 activations; FP64 accumulation; tanh-form
+    SiLU."""
     W1, b1, W2, b2, W3, b3, w4, b4 = split(p)
     silu = lambda z: 0.5 * z + 0.5 * z * np.tanh(0.5 * z)
     x = inputs(feats)
     xh, W1h = bf16(x), bf16(W1)
     xl, W1l = bf16(x - xh), bf16(W1 - W1h)
     z1 = xh @ W1h.T + xl @ W1h.T + xh @ W1l.T + b1
-    h = _pair(silu(z1))
-    h = _pair(silu(h @ bf16(W2).T + b2))
+    h = bf16(silu(z1))
+    h = bf16(silu(h @ bf16(W2).T + b2))
     h = silu(h @ bf16(W3).T + b3)
-    y = h @ bf16(w4) + b4
-    return base(feats) * (1.0 + y)
+    return h @ bf16(w4) + b4

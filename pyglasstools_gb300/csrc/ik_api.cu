@@ -547,7 +547,13 @@ int mode_ok(ik_ctx* c, int precision)
 {
     if (c->cg.mode == IK_QUAD_FIXEDPOINT) return IK_OK;
     if (c->cg.mode == IK_QUAD_EXACT) {
-        if (precision != IK_PREC_FP64) return fail(IK_ERR_UNSUPPORTED, "the exact bond integral runs on the FP64 path");
+        if (precision != IK_PREC_FP64 && c->cg.kind != IK_CG_GAUSSIAN)
+            return fail(IK_ERR_UNSUPPORTED, "the exact bond integral runs on the FP32 path for the Gaussian kernel only");
+        return IK_OK;
+    }
+    if (c->cg.mode == IK_QUAD_CLIPPED) {
+        if (precision != IK_PREC_FP32 || c->cg.kind != IK_CG_GAUSSIAN)
+            return fail(IK_ERR_UNSUPPORTED, "the clipped closed form runs on the FP32 path for the Gaussian kernel only");
         return IK_OK;
     }
     if (c->cg.mode == IK_QUAD_ADAPTIVE) {
@@ -773,7 +779,8 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         const int bps = c->tune_blocks_per_sm > 0 ? c->tune_blocks_per_sm : (c->in_batch ? 1 : 2);
         int blocks = std::min(c->geo.nitems, c->sm_count * bps);
         if (blocks > 0 && main_pass) {
-            CK(launch_gather32(a, c->cg.kind, (c->flags & IK_FLAG_LANE_KAHAN) != 0 && !mlp, mlp, blocks,
+            const int qm = mlp ? 1 : (c->cg.mode == IK_QUAD_CLIPPED ? 2 : (c->cg.mode == IK_QUAD_EXACT ? 3 : 0));
+            CK(launch_gather32(a, c->cg.kind, (c->flags & IK_FLAG_LANE_KAHAN) != 0 && qm == 0, qm, blocks,
                                32 * IK_WARPS_GATHER, smem, L.st));
             c->launches += 1;
         }
@@ -812,7 +819,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
             CK(cudaMemsetAsync(L.work_counter.p, 0, sizeof(int), L.st));
             const size_t esmem = (size_t)IK_WARPS_GATHER * ((size_t)c->halo_cap * stage_bytes + (size_t)e.qcap * 4);
             if (blocks > 0) {
-                CK(launch_gather32(e, c->cg.kind, false, false, blocks, 32 * IK_WARPS_GATHER, esmem, L.st));
+                CK(launch_gather32(e, c->cg.kind, false, 0, blocks, 32 * IK_WARPS_GATHER, esmem, L.st));
                 c->launches += 1;
             }
             CK(launch_pairs_to_f64(L.vir2.as<float2>(), nullptr, s.ela.as<double>(), 0.5 * norm, nullptr, nullptr,
@@ -930,6 +937,9 @@ int prepare_enqueue(ik_ctx* c, int slot, int prec, int fields)
     GeoSwap gs(c, slot);
     if (int r = ensure_ready(c)) return r;
     if (int r = mode_ok(c, prec)) return r;
+    if ((fields & IK_FIELD_ELASTIC) && prec == IK_PREC_FP32 &&
+        (c->cg.mode == IK_QUAD_EXACT || c->cg.mode == IK_QUAD_CLIPPED))
+        return fail(IK_ERR_UNSUPPORTED, "the elastic field on the FP32 path uses the fixed-point rule only");
     if (int r = ensure_geometry(c)) return r;
     if (c->maxb == 0) c->maxb = c->dim == 2 ? IK_MAXB_2D : IK_MAXB_3D;
     if (c->halo_cap == 0) c->halo_cap = 384; // staged particles per warp (grows on overflow)
@@ -1116,11 +1126,14 @@ int ik_set_cgfunc(ik_ctx* c, int kind, int mode, int order, double rcut, double 
     if (int r = check_ctx(c)) return r;
     ++c->config_version; // captured batch graphs hold the old settings
     if (kind < 0 || kind > 3) return fail(IK_ERR_ARG, "unknown coarse-graining kind %d", kind);
-    if (mode < 0 || mode > 3) return fail(IK_ERR_ARG, "unknown quadrature mode %d", mode);
+    if (mode < 0 || mode > 4) return fail(IK_ERR_ARG, "unknown quadrature mode %d", mode);
     if (!(rcut > 0.0) || !std::isfinite(rcut)) return fail(IK_ERR_ARG, "rcut must be > 0");
     if (mode == IK_QUAD_MLP && kind != IK_CG_GAUSSIAN)
         return fail(IK_ERR_UNSUPPORTED, "the learned surrogate covers the Gaussian kernel only");
-    if ((mode == IK_QUAD_FIXEDPOINT || mode == IK_QUAD_MLP || mode == IK_QUAD_EXACT) && (order < 1 || order > 64))
+    if (mode == IK_QUAD_CLIPPED && kind != IK_CG_GAUSSIAN)
+        return fail(IK_ERR_UNSUPPORTED, "the clipped closed form covers the Gaussian kernel only");
+    if ((mode == IK_QUAD_FIXEDPOINT || mode == IK_QUAD_MLP || mode == IK_QUAD_EXACT || mode == IK_QUAD_CLIPPED) &&
+        (order < 1 || order > 64))
         return fail(IK_ERR_ARG, "Gauss-Legendre order must be in [1, 64] (got %d)", order);
     if (kind == IK_CG_GAUSSIAN && !(width > 0.0)) return fail(IK_ERR_ARG, "Gaussian width must be > 0");
     const double PI = 3.14159265358979323846;
@@ -1156,9 +1169,10 @@ int ik_set_cgfunc(ik_ctx* c, int kind, int mode, int order, double rcut, double 
         cg.kappa = (float)(1.0 / rcut);
         cg.R2s = 1.0f;
     }
-    if (mode == IK_QUAD_FIXEDPOINT || mode == IK_QUAD_MLP || mode == IK_QUAD_EXACT) {
-        // GL-n: the rule itself, the surrogate's fallback, or (exact mode) the rule on
-        // the clipped interval, at least 5 points (20 for the mollifier)
+    if (mode == IK_QUAD_FIXEDPOINT || mode == IK_QUAD_MLP || mode == IK_QUAD_EXACT || mode == IK_QUAD_CLIPPED) {
+        // GL-n: the rule itself, the surrogate's (or the clipped closed form's) rule for
+        // the bonds inside the support, or (FP64 exact mode) the rule on the clipped
+        // interval, at least 5 points (20 for the mollifier)
         IkGL& gl = c->gl;
         if (mode == IK_QUAD_EXACT) order = std::max(order, kind == IK_CG_MOLLIFIER ? 20 : 5);
         gl.n = order;

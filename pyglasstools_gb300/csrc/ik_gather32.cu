@@ -4,10 +4,10 @@
 // variants for more bonds per particle are instantiated in ik_gather32_aux.cu (a
 // second translation unit, compiled in parallel).
 #include "ik_gather32_kernel.cuh"
-template <int DIM, int KIND, bool KAHAN, int NP, bool MLPM = false>
+template <int DIM, int KIND, bool KAHAN, int NP, int QM = 0>
 static cudaError_t launch_one(const GatherArgs32& a, int blocks, int threads, size_t smem, cudaStream_t st)
 {
-    return ik_launch_gather32_kernel<DIM, KIND, KAHAN, NP, MLPM, false, false>(a, blocks, threads, smem, st);
+    return ik_launch_gather32_kernel<DIM, KIND, KAHAN, NP, QM, false, false>(a, blocks, threads, smem, st);
 }
 
 template <int DIM, bool KAHAN, int NP>
@@ -29,16 +29,17 @@ static cudaError_t launch_np(const GatherArgs32& a, int kind, int blocks, int th
     return launch_kind<DIM, KAHAN, 0>(a, kind, blocks, threads, smem, st);
 }
 
-cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, bool mlp, int blocks, int threads,
+cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, int qm, int blocks, int threads,
                             size_t smem, cudaStream_t st)
 {
-    if (a.bcoef || a.maxb > 63) return launch_gather32_aux(a, kind, kahan, mlp, blocks, threads, smem, st);
-    if (mlp) { // Gaussian kernel only, plain per-lane sums
+    if (a.bcoef || a.maxb > 63) return launch_gather32_aux(a, kind, kahan, qm, blocks, threads, smem, st);
+    if (qm >= 2) return launch_gather32_exact(a, kind, kahan, qm, blocks, threads, smem, st);
+    if (qm == 1) { // Gaussian kernel only, plain per-lane sums
         if (kind != 1 || kahan) return cudaErrorInvalidValue;
-        if (a.g.dim == 2) return a.npairs == 2 ? launch_one<2, 1, false, 2, true>(a, blocks, threads, smem, st)
-                                               : launch_one<2, 1, false, 0, true>(a, blocks, threads, smem, st);
-        return a.npairs == 2 ? launch_one<3, 1, false, 2, true>(a, blocks, threads, smem, st)
-                             : launch_one<3, 1, false, 0, true>(a, blocks, threads, smem, st);
+        if (a.g.dim == 2) return a.npairs == 2 ? launch_one<2, 1, false, 2, 1>(a, blocks, threads, smem, st)
+                                               : launch_one<2, 1, false, 0, 1>(a, blocks, threads, smem, st);
+        return a.npairs == 2 ? launch_one<3, 1, false, 2, 1>(a, blocks, threads, smem, st)
+                             : launch_one<3, 1, false, 0, 1>(a, blocks, threads, smem, st);
     }
     if (a.g.dim == 2) return kahan ? launch_np<2, true>(a, kind, blocks, threads, smem, st)
                                    : launch_np<2, false>(a, kind, blocks, threads, smem, st);

@@ -23,9 +23,12 @@
 //     transformations (TwoSum) in a transposing butterfly -- each shuffle level halves
 //     the values a lane holds -- and the compensated result is written as a
 //     double-float pair (hi, lo), converted to FP64 and scaled by k_pairs_to_f64;
-//   * surrogate mode (MLPM): a bond whose far end r_j lies outside the support
-//     becomes a record {M, m.h, |h|^2, B_fixed} + {grid point, bond} for the learned
-//     surrogate (ik_mlp.cu) instead of a term of the sum.
+//   * quadrature modes (QM): 0 the fixed-point rule; 1 surrogate mode: a bond whose far
+//     end r_j lies outside the support becomes a record {M, m.h, |h|^2, B_fixed} +
+//     {grid point, bond} for the learned surrogate (ik_mlp.cu) instead of a term of the
+//     sum; 2 the same bonds by the closed form of the truncated Gaussian (the segment
+//     clipped to the support, error functions along it), the rule elsewhere; 3 the
+//     closed form for every bond.
 // Bond records (CSR, 16 B): {hb = kappa r_ij / 2, f' = 2 forceDivR / kappa^2}; the
 // stress coefficient is f' hb (x) hb.
 #pragma once
@@ -69,6 +72,33 @@ __device__ __forceinline__ float ik_kern(float q, float R2s)
 // are scalar, their product one packed multiply.
 template <int KIND>
 __device__ __forceinline__ unsigned long long ik_kern2(unsigned long long q2, float R2s);
+
+// The bond integral of the truncated Gaussian in closed form, in the gather's scaled
+// units (kernel 2^-q, q = |scaled r|^2, support q < R2s):
+//   int_{-1}^{1} 2^{-r^2(xi)} [r^2(xi) < R2s] dxi,  r^2(xi) = hh (xi - xi0)^2 + d2,
+// with xi0 = mb / hh the foot of the grid point on the bond's line and d2 its squared
+// distance from the line (from a cross product: no cancellation near the line).  The
+// segment is clipped to the support, |xi - xi0| < sqrt((R2s - d2) / hh), and
+//   = 2^{-d2} sqrt(pi) / (2 sqrt(a)) (erf(sqrt(a) (hi - xi0)) - erf(sqrt(a) (lo - xi0))),
+// a = ln 2 hh; the difference of error functions is taken through erfc when both
+// arguments lie on the same side beyond 0.5 (no cancellation in the tails).
+__device__ __forceinline__ float ik_bond_gauss_exact(float d2, float mb, float hh, float R2s)
+{
+    const float ihh = ik_rcp(hh);
+    const float t2 = (R2s - d2) * ihh;
+    if (!(t2 > 0.f)) return 0.f;
+    const float xi0 = mb * ihh, tc = sqrtf(t2);
+    const float sa = sqrtf(0.69314718055994531f * hh);
+    // z = sqrt(a) (end - xi0) at the clipped ends, from tc directly where the clip holds
+    const float za = xi0 - tc > -1.f ? -sa * tc : sa * (-1.f - xi0);
+    const float zb = xi0 + tc < 1.f ? sa * tc : sa * (1.f - xi0);
+    if (!(zb > za)) return 0.f;
+    float diff;
+    if (za > 0.5f) diff = erfcf(za) - erfcf(zb);
+    else if (zb < -0.5f) diff = erfcf(-zb) - erfcf(-za);
+    else diff = erff(zb) - erff(za);
+    return ik_ex2(-d2) * (0.88622692545275801f * ik_rcp(sa)) * diff;
+}
 
 // Kernel value of a particle already selected by the (FP64) support rule.
 template <int KIND>
@@ -223,14 +253,18 @@ __device__ __forceinline__ int ik_red_index(int lane, int k)
 }
 
 // NP: number of symmetric Gauss-Legendre node pairs (compile-time when > 0; 0 = runtime).
-// MLPM: surrogate mode (bonds crossing the edge of the support become records).
+// QM: quadrature mode -- 0 fixed-point rule; 1 surrogate (bonds crossing the edge of the
+// support become records); 2 closed form on those bonds; 3 closed form on every bond
+// (2 and 3: the Gaussian kernel only).
 // SPLIT: particles with more than 63 bonds are staged as several entries (one per 63
 // bonds; the entry word holds 6 count bits); the other variants need maxb <= 63.
-template <int DIM, int KIND, bool KAHAN, int NP, bool MLPM, bool ELA, bool SPLIT>
+template <int DIM, int KIND, bool KAHAN, int NP, int QM, bool ELA, bool SPLIT>
 __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
 {
     constexpr int NC = DIM == 2 ? 3 : 6;       // unique tensor components
     constexpr int P = IK_P;
+    constexpr bool MLPM = QM == 1;
+    static_assert(QM < 2 || KIND == 1, "closed-form bond integrals: Gaussian kernel only");
 
     // CSR bond records are addressed by (offset << 6 | count) words: 2^25 records at most
     if (a.boff && a.boff[a.nprec] >= (1 << 25)) {
@@ -449,11 +483,17 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
 #pragma unroll
                     for (int c = 0; c < NC; ++c) { acc[p][c] = 0.f; cmp[p][c] = 0.f; kac[p][c] = 0.f; }
 
-                f32x2 acc2[P / 2][NC];
+                // packed sums of the grid-point pairs; in the Kahan variant also their running
+                // compensations, kept negated (cn = -c: y = B cf + cn, t = acc + y,
+                // cn = y - (t - acc), acc = t -- Kahan's summation, two points per instruction)
+                f32x2 acc2[P / 2][NC], cn2[P / 2][KAHAN ? NC : 1];
 #pragma unroll
-                for (int j = 0; j < P / 2; ++j)
+                for (int j = 0; j < P / 2; ++j) {
 #pragma unroll
                     for (int c = 0; c < NC; ++c) acc2[j][c] = 0ull;
+#pragma unroll
+                    for (int c = 0; c < (KAHAN ? NC : 1); ++c) cn2[j][c] = 0ull;
+                }
 
                 // one slot: staged particle s, its bond k, grid mask m.  The loads are
                 // separate so that two batches can be in flight before either computes.
@@ -495,7 +535,7 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                     const float mx0 = sp.x + hbx, my0 = sp.y + hby, mz0 = sp.z + hbz; // bond midpoint
                     float4 crec[P];
                     int cmask = 0;
-                    if constexpr (!KAHAN && NP > 0) {
+                    if constexpr (NP > 0 && QM != 3) {
                         // packed path: two grid points per f32x2 instruction
                         const f32x2 mid2x = pk2(mx0, mx0), mid2y = pk2(my0, my0), mid2z = pk2(mz0, mz0);
                         const f32x2 hb2x = pk2(hbx, hbx), hb2y = pk2(hby, hby), hb2z = pk2(hbz, hbz);
@@ -545,9 +585,41 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                                     Bb = 0.f;
                                 }
                             }
+                            if constexpr (QM == 2) { // r_j outside the support: the closed form
+                                const f32x2 rj2 = fma2(pk2(-2.f, -2.f), mb, add2(M, pk2(hh, hh)));
+                                float ra, rb;
+                                up2(rj2, ra, rb);
+                                const bool ca = (m & (1 << (2 * j))) && ra >= R2s, cb = (m & (2 << (2 * j))) && rb >= R2s;
+                                if (ca || cb) {
+                                    // squared distance from the bond's line: |m x h|^2 / hh
+                                    f32x2 cr = fma2(mx, hb2y, mul2(pk2(-1.f, -1.f), mul2(my, hb2x)));
+                                    f32x2 c2 = mul2(cr, cr);
+                                    if (DIM == 3) {
+                                        const f32x2 mz = sub2(g2[j][2], mid2z);
+                                        const f32x2 cy = fma2(mz, hb2x, mul2(pk2(-1.f, -1.f), mul2(mx, hb2z)));
+                                        const f32x2 cx = fma2(my, hb2z, mul2(pk2(-1.f, -1.f), mul2(mz, hb2y)));
+                                        c2 = fma2(cy, cy, fma2(cx, cx, c2));
+                                    }
+                                    float c2a, c2b, mba, mbb;
+                                    up2(c2, c2a, c2b);
+                                    up2(mb, mba, mbb);
+                                    const float ihh = ik_rcp(hh);
+                                    if (ca) Ba = ik_bond_gauss_exact(c2a * ihh, mba, hh, R2s);
+                                    if (cb) Bb = ik_bond_gauss_exact(c2b * ihh, mbb, hh, R2s);
+                                }
+                            }
                             B = pk2((m & (1 << (2 * j))) ? Ba : 0.f, (m & (2 << (2 * j))) ? Bb : 0.f);
 #pragma unroll
-                            for (int c = 0; c < NC; ++c) acc2[j][c] = fma2(B, cf2[c], acc2[j][c]);
+                            for (int c = 0; c < NC; ++c) {
+                                if constexpr (KAHAN) {
+                                    const f32x2 y = fma2(B, cf2[c], cn2[j][c]);
+                                    const f32x2 t2 = add2(acc2[j][c], y);
+                                    cn2[j][c] = sub2(y, sub2(t2, acc2[j][c]));
+                                    acc2[j][c] = t2;
+                                } else {
+                                    acc2[j][c] = fma2(B, cf2[c], acc2[j][c]);
+                                }
+                            }
                         }
                     } else {
                         float cq[NP > 0 ? NP : 1];
@@ -574,8 +646,21 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                                 mb = fmaf(mz, hbz, mb);
                             }
                             // r^2(xi) = M - 2 xi mb + xi^2 hh at the symmetric nodes +-xi
-                            float B = a.w0 * ik_kern<KIND>(M, R2s);
-                            if constexpr (NP > 0) {
+                            float B = QM == 3 ? 0.f : a.w0 * ik_kern<KIND>(M, R2s);
+                            if constexpr (QM == 3) {
+                                // the closed form; d2 = |m x h|^2 / hh
+                                float c2;
+                                if (DIM == 2) {
+                                    const float cr = fmaf(mx, hby, -my * hbx);
+                                    c2 = cr * cr;
+                                } else {
+                                    const float mz = gz - mz0;
+                                    const float cx = fmaf(my, hbz, -mz * hby), cy = fmaf(mz, hbx, -mx * hbz),
+                                                cz = fmaf(mx, hby, -my * hbx);
+                                    c2 = fmaf(cz, cz, fmaf(cy, cy, cx * cx));
+                                }
+                                B = ik_bond_gauss_exact(c2 * ik_rcp(hh), mb, hh, R2s);
+                            } else if constexpr (NP > 0) {
 #pragma unroll
                                 for (int t = 0; t < NP; ++t) {
                                     const float base = M + cq[t];
@@ -590,6 +675,21 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                                     const float kp = ik_kern<KIND>(fmaf(a.m2xi[t], mb, base), R2s);
                                     const float km = ik_kern<KIND>(fmaf(-a.m2xi[t], mb, base), R2s);
                                     B = fmaf(a.w[t], kp + km, B);
+                                }
+                            }
+                            if constexpr (QM == 2) {
+                                if ((m & (1 << p)) && fmaf(-2.f, mb, M + hh) >= R2s) {
+                                    float c2;
+                                    if (DIM == 2) {
+                                        const float cr = fmaf(mx, hby, -my * hbx);
+                                        c2 = cr * cr;
+                                    } else {
+                                        const float mz = gz - mz0;
+                                        const float cx = fmaf(my, hbz, -mz * hby), cy = fmaf(mz, hbx, -mx * hbz),
+                                                    cz = fmaf(mx, hby, -my * hbx);
+                                        c2 = fmaf(cz, cz, fmaf(cy, cy, cx * cx));
+                                    }
+                                    B = ik_bond_gauss_exact(c2 * ik_rcp(hh), mb, hh, R2s);
                                 }
                             }
                             B = (m & (1 << p)) ? B : 0.f;
@@ -727,11 +827,19 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                 //      of VH values (compensated in the Kahan variant); results are
                 //      written as unscaled double-float pairs (hi, lo), merged across
                 //      chunks of an item with TwoSum, converted to FP64 later
-                if constexpr (!KAHAN && NP > 0) {
+                if constexpr (NP > 0 && QM != 3) {
 #pragma unroll
                     for (int j = 0; j < P / 2; ++j)
 #pragma unroll
-                        for (int c = 0; c < NC; ++c) up2(acc2[j][c], acc[2 * j][c], acc[2 * j + 1][c]);
+                        for (int c = 0; c < NC; ++c) {
+                            up2(acc2[j][c], acc[2 * j][c], acc[2 * j + 1][c]);
+                            if constexpr (KAHAN) {
+                                float n0, n1;
+                                up2(cn2[j][c % (KAHAN ? NC : 1)], n0, n1);
+                                cmp[2 * j][c] = -n0;
+                                cmp[2 * j + 1][c] = -n1;
+                            }
+                        }
                 }
                 constexpr int VH = ik_pow2_ceil(P * NC);
                 static_assert(VH == 16 || VH == 32, "butterfly width");
@@ -802,11 +910,11 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
     }
 }
 
-template <int DIM, int KIND, bool KAHAN, int NP, bool MLPM, bool ELA, bool SPLIT>
+template <int DIM, int KIND, bool KAHAN, int NP, int QM, bool ELA, bool SPLIT>
 static cudaError_t ik_launch_gather32_kernel(const GatherArgs32& a, int blocks, int threads, size_t smem,
                                              cudaStream_t st)
 {
-    auto kfn = k_gather32<DIM, KIND, KAHAN, NP, MLPM, ELA, SPLIT>;
+    auto kfn = k_gather32<DIM, KIND, KAHAN, NP, QM, ELA, SPLIT>;
     cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kfn<<<blocks, threads, smem, st>>>(a);

@@ -96,11 +96,16 @@ struct GatherArgs32 {
 };
 #define IK_MLP_CHUNK 2048
 // a.bcoef != null: elastic coefficients.  launch_gather32 passes the elastic field and
-// maxb > 63 on to launch_gather32_aux (variants in the second translation unit).
-cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, bool mlp, int blocks, int threads,
+// maxb > 63 on to launch_gather32_aux (variants in the second translation unit), and
+// the closed-form modes to launch_gather32_exact (a third).  qm: the quadrature mode --
+// 0 fixed-point rule, 1 surrogate records, 2 closed form on bonds crossing the edge of
+// the support, 3 closed form on every bond (1-3: Gaussian kernel; 1: plain lane sums).
+cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, int qm, int blocks, int threads,
                             size_t smem, cudaStream_t st);
-cudaError_t launch_gather32_aux(const GatherArgs32& a, int kind, bool kahan, bool mlp, int blocks, int threads,
+cudaError_t launch_gather32_aux(const GatherArgs32& a, int kind, bool kahan, int qm, int blocks, int threads,
                                 size_t smem, cudaStream_t st);
+cudaError_t launch_gather32_exact(const GatherArgs32& a, int kind, bool kahan, int qm, int blocks, int threads,
+                                  size_t smem, cudaStream_t st);
 // vir = ((double)hi + (double)lo + corr * 2^-32) * svir   (corr: fixed point, may be null),
 // kin = ((double)hi + (double)lo) * skin; a null output is skipped.  One launch.
 cudaError_t launch_pairs_to_f64(const float2* vin, const unsigned long long* corr, double* vout, double svir,

@@ -13,10 +13,12 @@
 // positions of r_i (inside the support) and r_j (outside) along it, reflected so
 // that b > 0.  The clipped part of the segment is known in closed form: it ends where
 // the line leaves the ball, at t_c = sqrt(9 - d^2), a fraction s1 = (t_c - a)/(b - a)
-// of the bond.  The midpoint rule on it, base = s1 exp(-(d^2 + m^2)/2) with
-// m = (a + t_c)/2, is the first approximation; the network predicts the relative
-// correction y = B / base - 1 from x = (t_c / 3, a/4, b/4, 2 (w - 1.5)), so that
-// B = base (1 + y).
+// of the bond.  Four-point Gauss-Legendre on it is the first approximation (base; its
+// relative error is below 1e-4 on this domain); the network predicts the scaled
+// relative correction y = (B / base - 1) * MLP_YSCALE from x = (t_c / 3, a/4, b/4,
+// 2 (w - 1.5)), so that B = base (1 + y / MLP_YSCALE).  The network's own error is
+// scaled down by the same factor in B, which is what lets BF16 operands meet a 1e-6
+// bound on B.
 //
 // Kernels:
 //   k_mlp_samples   seeded samples of the crossing-bond domain and their labels by
@@ -29,10 +31,8 @@
 //   k_mlp_infer_tc  inference on the 5th-generation tensor cores: per 128-row tile,
 //                   tcgen05.mma (kind::f16, BF16 in, FP32 accumulators in TMEM) for the
 //                   three hidden layers, tcgen05.ld epilogues (bias + SiLU) that write the
-//                   next layer's operand back to shared memory.  Activations travel as
-//                   BF16 hi + lo pairs (K = 128 against the weight tile used twice) and
-//                   the first layer is split three ways (x_hi W_hi + x_lo W_hi + x_hi W_lo),
-//                   so BF16 rounding of the weights is the remaining quantisation;
+//                   next layer's operand (BF16) back to shared memory; the first layer
+//                   is split three ways (x_hi W_hi + x_lo W_hi + x_hi W_lo);
 //   k_mlp_infer_simt the same BF16 arithmetic on the CUDA cores (cross-check), or FP32.
 #include "ik_kernels.h"
 #include "../../include/ik_gb300.h"
@@ -53,6 +53,11 @@ constexpr int O_W1 = 0, O_B1 = O_W1 + H * NIN, O_W2 = O_B1 + H, O_B2 = O_W2 + H 
               O_B3 = O_W3 + H * H, O_W4 = O_B3 + H, O_B4 = O_W4 + H, NPAR = O_B4 + 1;
 constexpr int NPART = NPAR + 1; // + loss
 constexpr double LMAX = 2.5;    // longest bond sampled (units of w)
+constexpr float MLP_YSCALE = 1.0e4f;        // network output = (B / base - 1) * MLP_YSCALE
+constexpr float MLP_YINV = 1.0f / MLP_YSCALE;
+// four-point Gauss-Legendre on [-1, 1]: nodes +-GL4X0, +-GL4X1, weights GL4W0, GL4W1
+constexpr double GL4X0 = 0.33998104358485626480, GL4X1 = 0.86113631159405257522;
+constexpr double GL4W0 = 0.65214515486254614263, GL4W1 = 0.34785484513745385737;
 
 // deployed blob (bytes): BF16 operand tiles in the no-swizzle K-major layout, then FP32
 constexpr int DB_W1 = 0;                   // 64 x 16 bf16 (K padded from 4)  2048 B
@@ -75,14 +80,19 @@ __host__ __device__ inline void mlp_inputs(float d, float a, float b, float w, f
     x[3] = 2.0f * (w - 1.5f);
 }
 
-// midpoint-rule baseline of the clipped segment (see the header comment)
+// Gauss-Legendre-4 baseline on the clipped segment (see the header comment):
+// base = s1 / 2 * sum_k w_k exp(-(d^2 + t_k^2) / 2), t_k = a + s1 l (1 + x_k) / 2
 __host__ __device__ inline float mlp_base(float d, float a, float b)
 {
     const float tc = sqrtf(fmaxf(9.0f - d * d, 0.0f));
     const float l = b - a;
     const float s1 = l > 0.0f ? fminf(fmaxf((tc - a) / l, 0.0f), 1.0f) : 0.0f;
-    const float m = 0.5f * (a + tc);
-    return s1 * expf(-0.5f * (d * d + m * m));
+    const float h = 0.5f * s1 * l, m = a + h, d2 = d * d;
+    const float t0 = m - h * (float)GL4X1, t1 = m - h * (float)GL4X0, t2 = m + h * (float)GL4X0,
+                t3 = m + h * (float)GL4X1;
+    const float sum = (float)GL4W1 * (expf(-0.5f * (d2 + t0 * t0)) + expf(-0.5f * (d2 + t3 * t3))) +
+                      (float)GL4W0 * (expf(-0.5f * (d2 + t1 * t1)) + expf(-0.5f * (d2 + t2 * t2)));
+    return 0.5f * s1 * sum;
 }
 
 __device__ __forceinline__ float silu_exact(float z) { return z / (1.0f + expf(-z)); }
@@ -189,13 +199,17 @@ __global__ void k_mlp_samples(long long n, unsigned long long seed, MlpGL q, flo
     const double B = mlp_label(q, d, a, b);
     feats[i] = make_float4((float)d, (float)a, (float)b, (float)w);
     labels[i] = B;
-    // target y = B / base - 1, the baseline from the FP32 features (what the network sees)
+    // target y = (B / base - 1) * MLP_YSCALE, the baseline from the FP32 features (what
+    // the network sees), in FP64
     const double df = (float)d, af = (float)a, bf = (float)b;
     const double tcf = sqrt(fmax(9.0 - df * df, 0.0));
-    const double s1 = fmin(fmax((tcf - af) / (bf - af), 0.0), 1.0);
-    const double mf = 0.5 * (af + tcf);
-    const double base = s1 * exp(-0.5 * (df * df + mf * mf));
-    targets[i] = base > 1e-30 ? (float)(B / base - 1.0) : 0.0f;
+    const double l = bf - af;
+    const double s1 = l > 0.0 ? fmin(fmax((tcf - af) / l, 0.0), 1.0) : 0.0;
+    const double h = 0.5 * s1 * l, m = af + h, d2 = df * df;
+    auto e = [&](double t) { return exp(-0.5 * (d2 + t * t)); };
+    const double base = 0.5 * s1 * (GL4W1 * (e(m - h * GL4X1) + e(m + h * GL4X1)) +
+                                    GL4W0 * (e(m - h * GL4X0) + e(m + h * GL4X0)));
+    targets[i] = base > 1e-30 ? (float)((B / base - 1.0) * (double)MLP_YSCALE) : 0.0f;
 }
 
 // ---------------------------------------------------------------------------- training
@@ -476,10 +490,10 @@ __global__ void k_mlp_deploy(const float* P, unsigned char* blob)
 
 // ---------------------------------------------------------------------------- SIMT inference
 // mode 0: FP32 weights and activations, exact SiLU (the training network);
-// mode 1: the arithmetic of the tensor-core kernel (BF16 weights, activations as BF16
-//         hi + lo pairs, first layer split three ways, FP32 accumulation, the deployed
-//         SiLU), for cross-checks.
-__global__ void k_mlp_infer_simt(const float* P, const float4* feats, long long n, int mode, float* out)
+// mode 1: the arithmetic of the tensor-core kernel (BF16 weights and activations, first
+//         layer split three ways, FP32 accumulation, the deployed SiLU), for cross-checks.
+// raw: out = the network's output y instead of B.
+__global__ void k_mlp_infer_simt(const float* P, const float4* feats, long long n, int mode, int raw, float* out)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -494,9 +508,9 @@ __global__ void k_mlp_infer_simt(const float* P, const float4* feats, long long 
     float x[4];
     mlp_inputs(f.x, f.y, f.z, f.w, x);
     float h[64], g[64];
-    // BF16 split of the first layer (x_hi W_hi + x_lo W_hi + x_hi W_lo) and of the
-    // activations (hi + lo), BF16 weights elsewhere
-    auto P2 = [&](float v) { return q ? bf16r(v) + bf16r(v - bf16r(v)) : v; };
+    // BF16 split of the first layer (x_hi W_hi + x_lo W_hi + x_hi W_lo); BF16 weights and
+    // activations elsewhere
+    auto P2 = [&](float v) { return q ? bf16r(v) : v; };
     for (int nn = 0; nn < 64; ++nn) {
         float z = 0.f;
         for (int k = 0; k < 4; ++k) {
@@ -524,7 +538,7 @@ __global__ void k_mlp_infer_simt(const float* P, const float4* feats, long long 
     float y = 0.f;
     for (int k = 0; k < 64; ++k) y = fmaf(R(P[O_W4 + k]), h[k], y);
     y += P[O_B4];
-    out[i] = mlp_base(f.x, f.y, f.z) * (1.0f + y);
+    out[i] = raw ? y : mlp_base(f.x, f.y, f.z) * fmaf(y, MLP_YINV, 1.0f);
 }
 
 // ---------------------------------------------------------------------------- tcgen05 helpers
@@ -623,15 +637,15 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi)
 // ---------------------------------------------------------------------------- tcgen05 inference
 // Shared memory layout of k_mlp_infer_tc (bytes, 1024-aligned pieces):
 constexpr int TC_A0 = 0;                    // 128 x 16 bf16 input operand   4096
-constexpr int TC_H = TC_A0 + 128 * 16 * 2;  // 128 x 128 bf16 hidden operand [hi | lo]  32768
-constexpr int TC_W = TC_H + 128 * 128 * 2;  // deployed blob (W1, W2, W3, floats)
+constexpr int TC_H = TC_A0 + 128 * 16 * 2;  // 128 x 64 bf16 hidden operand   16384
+constexpr int TC_W = TC_H + 128 * 64 * 2;   // deployed blob (W1, W2, W3, floats)
 constexpr int TC_BAR = TC_W + DB_BYTES;  // DB_BYTES is a multiple of 16
 constexpr int TC_SMEM = TC_BAR + 64;
-// 56.4 KB of dynamic shared memory per CTA: at most 4 CTAs on an SM (228 KB), so their
-// TMEM allocations (64 columns each, 256 of 512) never wait on one another.
+// About 40 KB of dynamic shared memory per CTA: at most 5 CTAs on an SM (228 KB), so
+// their TMEM allocations (64 columns each, at most 320 of 512) never wait on one another.
 constexpr int TC_SMEM_LAUNCH = TC_SMEM;
-static_assert(4 * (TC_SMEM_LAUNCH + 1024) <= 233472 && 5 * (TC_SMEM_LAUNCH + 1024) > 233472,
-              "four CTAs per SM");
+constexpr int TC_CTAS_PER_SM = 233472 / (TC_SMEM_LAUNCH + 1024);
+static_assert(TC_CTAS_PER_SM >= 4 && TC_CTAS_PER_SM * 64 <= 512, "TMEM columns of the resident CTAs");
 constexpr uint32_t TC_COLS = 64;
 
 // Records of bonds that cross the support, written by the FP32 gather in surrogate
@@ -667,10 +681,12 @@ __device__ __forceinline__ int mlp_record_coords(const float4 r, float to_w, flo
 
 // MODE 0: out[i] = surrogate B of feats[i] (units of w, un-normalised);
 // MODE 1: IK records -> fixed-point stress corrections.
-// stall != 0: the failure-detection test hook (TC_STALL_POLLS).
+// stall != 0: the failure-detection test hook (TC_STALL_POLLS).  MODE 0 with raw != 0:
+// out[i] = the network's output y instead of B.
 template <int MODE>
 __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __restrict__ blob, const float4* feats,
-                                                     long long n, float* out, MlpRecArgs R, int* status, int stall)
+                                                     long long n, float* out, MlpRecArgs R, int* status, int stall,
+                                                     int raw)
 {
     extern __shared__ __align__(1024) unsigned char tsm[];
     unsigned char* sA0 = tsm + TC_A0;
@@ -734,16 +750,21 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
                 bfix = r.w;
             }
         }
-        // midpoint-rule baseline of the clipped segment (as mlp_base, exp via ex2.approx)
+        // Gauss-Legendre-4 baseline on the clipped segment (as mlp_base, exp via ex2.approx)
         float base;
         {
             const float tc = sqrtf(fmaxf(9.0f - fd * fd, 0.0f));
             const float l = fb - fa;
             const float s1 = l > 0.0f ? fminf(fmaxf((tc - fa) / l, 0.0f), 1.0f) : 0.0f;
-            const float mm = 0.5f * (fa + tc);
-            float ex;
-            asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(ex) : "f"(-0.72134752044448170f * (fd * fd + mm * mm)));
-            base = s1 * ex;
+            const float h = 0.5f * s1 * l, mm = fa + h, d2 = fd * fd;
+            auto ex = [&](float tt) {
+                float r;
+                asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(-0.72134752044448170f * fmaf(tt, tt, d2)));
+                return r;
+            };
+            const float sum = (float)GL4W1 * (ex(fmaf(-h, (float)GL4X1, mm)) + ex(fmaf(h, (float)GL4X1, mm))) +
+                              (float)GL4W0 * (ex(fmaf(-h, (float)GL4X0, mm)) + ex(fmaf(h, (float)GL4X0, mm)));
+            base = 0.5f * s1 * sum;
         }
         {
             // inputs as [x_hi | x_lo | x_hi | 0] against W1 as [hi | hi | lo | 0]
@@ -768,12 +789,12 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
                 if (layer == 0) {
                     umma_bf16(tmem, umma_desc(aA0, 128, 256), umma_desc(aW1, 128, 256), ID, 0u);
                 } else {
-                    // [h_hi | h_lo] (K = 128) against [W | W]: the same W tile twice
+                    // h (K = 64) against W: four MMAs of K = 16
                     const uint32_t aw = layer == 1 ? aW2 : aW3;
 #pragma unroll
-                    for (int kk = 0; kk < 8; ++kk)
-                        umma_bf16(tmem, umma_desc(aH + kk * 256, 128, 2048),
-                                  umma_desc(aw + (kk & 3) * 256, 128, 1024), ID, kk > 0 ? 1u : 0u);
+                    for (int kk = 0; kk < 4; ++kk)
+                        umma_bf16(tmem, umma_desc(aH + kk * 256, 128, 1024), umma_desc(aw + kk * 256, 128, 1024), ID,
+                                  kk > 0 ? 1u : 0u);
                 }
                 umma_commit(aBar);
             }
@@ -790,24 +811,19 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
                 for (int c16 = 0; c16 < 4; ++c16) {
                     float v[16];
                     tmem_ld16(tl + 16 * c16, v);
-                    // h = z/2 (prescaled weights), SiLU = h + h tanh(h); BF16 hi word by a
-                    // packed convert, lo = a - hi
-                    uint32_t ph[8], pl[8];
+                    // h = z/2 (prescaled weights), SiLU = h + h tanh(h), packed to BF16 pairs
+                    uint32_t ph[8];
 #pragma unroll
                     for (int k = 0; k < 16; k += 2) {
                         const float h0 = v[k] + bias[16 * c16 + k], h1 = v[k + 1] + bias[16 * c16 + k + 1];
                         const float a0 = fmaf(h0, tanh_approx(h0), h0), a1 = fmaf(h1, tanh_approx(h1), h1);
-                        const uint32_t hp = pack_bf16x2(a0, a1);
-                        ph[k / 2] = hp;
-                        pl[k / 2] = pack_bf16x2(a0 - __uint_as_float(hp << 16), a1 - __uint_as_float(hp & 0xffff0000u));
+                        ph[k / 2] = pack_bf16x2(a0, a1);
                     }
 #pragma unroll
                     for (int h8 = 0; h8 < 2; ++h8) {
                         const int k0 = 16 * c16 + 8 * h8;
-                        *reinterpret_cast<uint4*>(sH + op_off(t, k0, 128)) =
+                        *reinterpret_cast<uint4*>(sH + op_off(t, k0, 64)) =
                             make_uint4(ph[4 * h8], ph[4 * h8 + 1], ph[4 * h8 + 2], ph[4 * h8 + 3]);
-                        *reinterpret_cast<uint4*>(sH + op_off(t, 64 + k0, 128)) =
-                            make_uint4(pl[4 * h8], pl[4 * h8 + 1], pl[4 * h8 + 2], pl[4 * h8 + 3]);
                     }
                 }
                 fence_async_smem();
@@ -828,9 +844,9 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
                     }
                 }
                 fence_before();
-                const float Bs = base * (1.0f + y);
+                const float Bs = base * fmaf(y, MLP_YINV, 1.0f);
                 if (MODE == 0) {
-                    if (valid) out[row] = Bs;
+                    if (valid) out[row] = raw ? y : Bs;
                 } else if (valid) {
                     // the gather's units: B integrates over [-1, 1] (twice the [0, 1] value)
                     const bool use = bin >= 0 && R.table[bin] != 0;
@@ -952,17 +968,17 @@ static int gen_samples(ik_mlp* m, long long n, unsigned long long seed, MBuf& f,
     return IK_OK;
 }
 
-static int run_tc(ik_mlp* m, long long n, const float4* f, float* out)
+static int run_tc(ik_mlp* m, long long n, const float4* f, float* out, int raw = 0)
 {
     if (!m->deployed) if (int r = deploy(m)) return r;
     MENS(m->status, sizeof(int));
     MCK(cudaMemsetAsync(m->status.p, 0, sizeof(int), m->st));
     MCK(cudaFuncSetAttribute(k_mlp_infer_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_LAUNCH));
     const long long tiles = (n + 127) / 128;
-    const int blocks = (int)std::min<long long>(std::max<long long>(tiles, 1), (long long)m->sm_count * 4);
+    const int blocks = (int)std::min<long long>(std::max<long long>(tiles, 1), (long long)m->sm_count * TC_CTAS_PER_SM);
     MlpRecArgs none{};
     k_mlp_infer_tc<0><<<blocks, 128, TC_SMEM_LAUNCH, m->st>>>(m->blob.as<unsigned char>(), f, n, out, none,
-                                                               m->status.as<int>(), m->stall);
+                                                               m->status.as<int>(), m->stall, raw);
     MCK(cudaGetLastError());
     int st = 0;
     MCK(cudaMemcpyAsync(&st, m->status.p, sizeof(int), cudaMemcpyDeviceToHost, m->st));
@@ -1002,7 +1018,7 @@ cudaError_t launch_mlp_records(ik_mlp* m, const float4* rec, const int2* rid, co
     R.nc = nc;
     R.corr = corr;
     k_mlp_infer_tc<1><<<blocks, 128, TC_SMEM_LAUNCH, st>>>(m->blob.as<unsigned char>(), nullptr, 0, nullptr, R,
-                                                            status, m->stall);
+                                                            status, m->stall, 0);
     return cudaGetLastError();
 }
 
@@ -1221,6 +1237,8 @@ int ik_mlp_eval(ik_mlp* m, int64_t n, const float* feats, float* out, int kernel
 {
     if (int r = mcheck(m)) return r;
     if (!m->initialised) return mfail(IK_ERR_STATE, "surrogate has no parameters");
+    const int raw = (kernel & IK_MLP_EVAL_RAW) ? 1 : 0;
+    kernel &= ~IK_MLP_EVAL_RAW;
     if (n < 0 || (n > 0 && (!feats || !out)) || kernel < 0 || kernel > 2)
         return mfail(IK_ERR_ARG, "bad evaluation arguments");
     if (n == 0) return IK_OK;
@@ -1228,10 +1246,11 @@ int ik_mlp_eval(ik_mlp* m, int64_t n, const float* feats, float* out, int kernel
     MENS(m->eout, sizeof(float) * n);
     MCK(cudaMemcpyAsync(m->efeats.p, feats, sizeof(float4) * n, cudaMemcpyHostToDevice, m->st));
     if (kernel == 0) {
-        if (int r = run_tc(m, n, m->efeats.as<float4>(), m->eout.as<float>())) return r;
+        if (int r = run_tc(m, n, m->efeats.as<float4>(), m->eout.as<float>(), raw)) return r;
     } else {
         k_mlp_infer_simt<<<(unsigned)((n + 127) / 128), 128, 0, m->st>>>(m->params.as<float>(), m->efeats.as<float4>(),
-                                                                         n, kernel == 1 ? 1 : 0, m->eout.as<float>());
+                                                                         n, kernel == 1 ? 1 : 0, raw,
+                                                                         m->eout.as<float>());
         MCK(cudaGetLastError());
     }
     MCK(cudaMemcpyAsync(out, m->eout.p, sizeof(float) * n, cudaMemcpyDeviceToHost, m->st));

@@ -19,7 +19,7 @@ ERR = {-1: "IK_ERR_ARG", -2: "IK_ERR_CUDA", -3: "IK_ERR_STATE", -4: "IK_ERR_BOX"
        -5: "IK_ERR_CAPACITY", -6: "IK_ERR_TIMEOUT", -7: "IK_ERR_NOMEM", -8: "IK_ERR_UNSUPPORTED",
        -9: "IK_ERR_QUADRATURE"}
 CG = {"octic": 0, "gaussian": 1, "rect": 2, "mollifier": 3}
-QUAD = {"fixedpoint": 0, "adaptive": 1, "exact": 2, "mlp": 3}
+QUAD = {"fixedpoint": 0, "adaptive": 1, "exact": 2, "mlp": 3, "clipped": 4}
 PREC = {"fp64": 0, "fp32": 1}
 FIELD_VIRIAL, FIELD_KINETIC, FIELD_ELASTIC = 1, 2, 4
 FLAG_TIMING, FLAG_LANE_KAHAN, FLAG_CSR_BONDS = 1, 2, 4
@@ -504,11 +504,12 @@ class MLP:
         bounded completion wait runs out (IK_ERR_TIMEOUT) until turned off again."""
         check(lib().ik_mlp_test_stall(self._h, 1 if on else 0))
 
-    def eval(self, feats, kernel=0):
-        """kernel 0: tensor cores (BF16); 1: CUDA cores, BF16 arithmetic; 2: CUDA cores, FP32."""
+    def eval(self, feats, kernel=0, raw=False):
+        """kernel 0: tensor cores (BF16); 1: CUDA cores, BF16 arithmetic; 2: CUDA cores, FP32.
+        raw: the network's output y = (B / base - 1) * 1e4 instead of B."""
         f = np.ascontiguousarray(feats, dtype=np.float32)
         out = np.empty(len(f), dtype=np.float32)
-        check(lib().ik_mlp_eval(self._h, len(f), _fp(f), _fp(out), kernel))
+        check(lib().ik_mlp_eval(self._h, len(f), _fp(f), _fp(out), kernel | (4 if raw else 0)))
         return out
 
     def validate(self, n=1 << 20, seed=7, tol=1e-6):

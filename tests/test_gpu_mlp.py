@@ -5,8 +5,10 @@ tensor-core (tcgen05, BF16) inference against the CUDA-core BF16 and FP32 networ
 and the oracle's BF16 emulation, and training + validation end to end.
 
 Tolerances: labels 1e-12 absolute; gradient relative L2 <= 1e-4 per parameter block
-(FP32 accumulation over the batch); tensor-core vs CUDA-core BF16 outputs within 1e-4
-of the output scale (the same BF16 roundings, FP32 sums in another order).
+(FP32 accumulation over the batch); tensor-core vs CUDA-core BF16 network outputs within
+1e-4 of the output scale (the same BF16 roundings, FP32 sums in another order).  The
+trained surrogate must meet the 1e-6 bound on B (validation error per bin) over at
+least 90 % of the samples, the fallback tolerance it runs at in the IK workload.
 """
 import numpy as np
 import pytest
@@ -61,16 +63,19 @@ def test_tensor_core_inference_matches_cuda_cores(ik):
         m.init(seed=4)
         p = m.get_params()
         f, _ = m.samples(1000, seed=13)  # 1000: a ragged last tile
-        tc = m.eval(f, kernel=0)
-        simt16 = m.eval(f, kernel=1)
-        fp32 = m.eval(f, kernel=2)
+        tc = m.eval(f, kernel=0, raw=True)
+        simt16 = m.eval(f, kernel=1, raw=True)
+        fp32 = m.eval(f, kernel=2, raw=True)
+        b_tc = m.eval(f, kernel=0)
     scale = np.max(np.abs(fp32))
     assert np.all(np.isfinite(tc))
     assert np.max(np.abs(tc - simt16)) <= 1e-4 * scale
     assert np.max(np.abs(tc - M.forward_bf16(p, f))) <= 1e-4 * scale
-    assert np.max(np.abs(fp32 - M.base(f) * (1.0 + M.forward(p, f)))) <= 1e-5 * scale
+    assert np.max(np.abs(fp32 - M.forward(p, f))) <= 1e-5 * scale
     # BF16 weights against FP32: the quantisation error, not a layout error
     assert np.max(np.abs(tc - fp32)) <= 0.02 * scale
+    # B from y: base (1 + y / 1e4), the base by ex2.approx in the kernel
+    np.testing.assert_allclose(b_tc, M.value(f, tc.astype(np.float64)), rtol=2e-6, atol=1e-12)
 
 
 def _gl_bond(f, n=5):
@@ -93,13 +98,18 @@ def test_training_fits_and_beats_fixed_point_rule(ik):
         f, lab = m.samples(1 << 16, seed=78)
         b_tc = m.eval(f, kernel=0)
     rms = lambda e: float(np.sqrt(np.mean(e * e)))
-    err_net, err_gl5 = rms(b_tc - lab), rms(_gl_bond(f) - lab)
-    print(f"crossing bonds: rms |B - exact| network (BF16, tensor cores) {err_net:.3e}, GL-5 {err_gl5:.3e}; "
+    err_net, err_gl5, err_base = rms(b_tc - lab), rms(_gl_bond(f) - lab), rms(M.base(f) - lab)
+    print(f"crossing bonds: rms |B - exact| network (BF16, tensor cores) {err_net:.3e}, GL-5 {err_gl5:.3e}, "
+          f"its baseline alone {err_base:.3e}; max {np.max(np.abs(b_tc - lab)):.3e}; "
           f"coverage at 1e-6 {v_tight['coverage']:.3f}, at 2e-3 {v_loose['coverage']:.3f}")
-    # what the network gains over the fixed-point rule on the bonds it stands in for
-    assert err_net < err_gl5 / 4
+    # what the network gains over the fixed-point rule on the bonds it stands in for,
+    # and over its own baseline
+    assert err_net < err_gl5 / 100
+    assert err_net < err_base / 2
+    # the fallback tolerance of the IK workload: 1e-6 on B, met over >= 90 % of samples
+    assert v_tight["coverage"] >= 0.9, v_tight["coverage"]
+    assert v_tight["max_err"] < 2e-6
     assert 0.0 <= v_tight["coverage"] <= v_loose["coverage"] <= 1.0
-    assert v_loose["coverage"] > 0.5
     seen = v_loose["bin_max_err"][v_loose["bin_max_err"] >= 0]
     assert len(seen) > 1000
 
@@ -145,7 +155,7 @@ def test_ik_surrogate_mode_gains_over_fixed_point_rule(ik, oracle, trained):
     from pyglasstools_gb300 import synth
     fr = synth.make_frame(4000, dim=2, seed=41)
     grid = synth.lattice_grid(fr.L, 48, 2)
-    trained.validate(n=1 << 18, seed=5, tol=1.0)   # every populated bin
+    trained.validate(n=1 << 18, seed=5, tol=1e-6)   # the bins within the 1e-6 bound
     v_gl, _, max_rc = _ik_fields(ik, fr, grid, "fixedpoint")
     v_net, cnt, _ = _ik_fields(ik, fr, grid, "mlp", trained)
     box = oracle.make_box(2, [fr.L, fr.L, 1.0])
@@ -154,8 +164,8 @@ def test_ik_surrogate_mode_gains_over_fixed_point_rule(ik, oracle, trained):
     e_gl = rel_l2(uniq(v_gl), uniq(exact))
     e_net = rel_l2(uniq(v_net), uniq(exact))
     print(f"field error vs exact bond integral: fixed point GL-5 {e_gl}, surrogate {e_net}")
-    assert np.all(e_net < e_gl / 3)
-    assert np.all(e_net < 1e-4)
+    assert np.all(e_net < e_gl / 30)
+    assert np.all(e_net < 1e-5)
     # deterministic (fixed-point accumulation of the surrogate's terms)
     v_net2, _, _ = _ik_fields(ik, fr, grid, "mlp", trained)
     np.testing.assert_array_equal(v_net, v_net2)

@@ -61,3 +61,27 @@ def test_bf16_rounding():
     assert r[0] == 1.0 and r[1] == 1.0  # tie to even
     assert r[2] == 1.0078125
     assert abs(r[3] + 3.140625) < 1e-7 and r[4] == 0.0
+
+
+def test_baseline_is_gl4_on_the_clipped_segment_and_close():
+    """The surrogate's baseline (four-point Gauss-Legendre on the part of the bond inside
+    the support) is within 1e-4 relative of the exact integral over the sampled domain,
+    which bounds the scaled target y = (B / base - 1) * 1e4 to about one."""
+    rng = np.random.default_rng(9)
+    n = 200000
+    d = rng.uniform(0, 3, n)
+    tc = np.sqrt(9 - d * d)
+    a = rng.uniform(-tc, tc)
+    b = a + rng.uniform(0, 2.5, n)
+    keep = (b >= tc) & (b <= 4)
+    f = np.stack([d, a, b, np.ones(n)], axis=1)[keep].astype(np.float32)
+    lab = M.label(f[:, 0], f[:, 1], f[:, 2])
+    bs = M.base(f)
+    rel = np.abs(bs / lab - 1.0)
+    assert rel.max() < 1e-4
+    y = M.targets(f, lab)
+    assert np.max(np.abs(y)) < 1.0
+    np.testing.assert_allclose(M.value(f, y), lab, rtol=1e-12, atol=0)
+    # the rule itself: four points integrate a cubic on [a, t_c] exactly
+    x, w = np.polynomial.legendre.leggauss(4)
+    assert abs(np.sum(w * x ** 6) - 2.0 / 7.0) < 1e-15 and abs(np.sum(w * x ** 8) - 2.0 / 9.0) > 1e-3
