@@ -73,6 +73,27 @@ __device__ __forceinline__ float ik_kern(float q, float R2s)
 template <int KIND>
 __device__ __forceinline__ unsigned long long ik_kern2(unsigned long long q2, float R2s);
 
+// erfc(x) for x >= 0 by Hastings' rational approximation (Abramowitz & Stegun,
+// Handbook of Mathematical Functions, 7.1.26): erfc(x) = t (a1 + t (a2 + t (a3 +
+// t (a4 + t a5)))) exp(-x^2), t = 1 / (1 + p x), with |error| <= 1.5e-7.
+__device__ __forceinline__ float ik_erfc_hastings(float x)
+{
+    const float t = ik_rcp(fmaf(0.3275911f, x, 1.0f));
+    float q = fmaf(1.061405429f, t, -1.453152027f);
+    q = fmaf(q, t, 1.421413741f);
+    q = fmaf(q, t, -0.284496736f);
+    q = fmaf(q, t, 0.254829592f);
+    return q * t * ik_ex2(-1.4426950408889634f * x * x);
+}
+// erf(zb) - erf(za) from erfc of |za| and |zb|: with s = sign,
+// (s_b - s_a) + s_a erfc|za| - s_b erfc|zb| -- the difference of the two small tails
+// when both lie on one side (no cancellation), branch-free.
+__device__ __forceinline__ float ik_erf_diff(float za, float zb)
+{
+    const float sa = za < 0.f ? -1.f : 1.f, sb = zb < 0.f ? -1.f : 1.f;
+    return fmaf(sa, ik_erfc_hastings(fabsf(za)), fmaf(-sb, ik_erfc_hastings(fabsf(zb)), sb - sa));
+}
+
 // The bond integral of the truncated Gaussian in closed form, in the gather's scaled
 // units (kernel 2^-q, q = |scaled r|^2, support q < R2s):
 //   int_{-1}^{1} 2^{-r^2(xi)} [r^2(xi) < R2s] dxi,  r^2(xi) = hh (xi - xi0)^2 + d2,
@@ -80,8 +101,7 @@ __device__ __forceinline__ unsigned long long ik_kern2(unsigned long long q2, fl
 // distance from the line (from a cross product: no cancellation near the line).  The
 // segment is clipped to the support, |xi - xi0| < sqrt((R2s - d2) / hh), and
 //   = 2^{-d2} sqrt(pi) / (2 sqrt(a)) (erf(sqrt(a) (hi - xi0)) - erf(sqrt(a) (lo - xi0))),
-// a = ln 2 hh; the difference of error functions is taken through erfc when both
-// arguments lie on the same side beyond 0.5 (no cancellation in the tails).
+// a = ln 2 hh, with the error functions of ik_erf_diff.
 __device__ __forceinline__ float ik_bond_gauss_exact(float d2, float mb, float hh, float R2s)
 {
     const float ihh = ik_rcp(hh);
@@ -93,11 +113,7 @@ __device__ __forceinline__ float ik_bond_gauss_exact(float d2, float mb, float h
     const float za = xi0 - tc > -1.f ? -sa * tc : sa * (-1.f - xi0);
     const float zb = xi0 + tc < 1.f ? sa * tc : sa * (1.f - xi0);
     if (!(zb > za)) return 0.f;
-    float diff;
-    if (za > 0.5f) diff = erfcf(za) - erfcf(zb);
-    else if (zb < -0.5f) diff = erfcf(-zb) - erfcf(-za);
-    else diff = erff(zb) - erff(za);
-    return ik_ex2(-d2) * (0.88622692545275801f * ik_rcp(sa)) * diff;
+    return ik_ex2(-d2) * (0.88622692545275801f * ik_rcp(sa)) * ik_erf_diff(za, zb);
 }
 
 // Kernel value of a particle already selected by the (FP64) support rule.
