@@ -410,7 +410,17 @@ def uneven_leg(args):
         for k in slots:
             c.compute_slot(k, "fp32")
 
+    def graph(fused):
+        c.set_tuning("fused_batch", fused)
+        c.compute_batch(slots, "fp32")  # first call: plain launches, then the graph is recorded
+        c.synchronize()
+        l0 = c.launch_count()
+        ms = timed(lambda: c.compute_batch(slots, "fp32"))
+        return ms, (c.launch_count() - l0) // (reps + 1)
+
     ms_plain = timed(per_frame)
+    ms_fused, launches_fused = graph(1)
+    ms_lanes, launches_lanes = graph(0)
     best = c.autotune_batch(slots, "fp32", reps=2)
     l0 = c.launch_count()
     ms_graph = timed(lambda: c.compute_batch(slots, "fp32"))
@@ -419,6 +429,12 @@ def uneven_leg(args):
     return {"workload": "256 frames, N log-uniform [1000, 128000], own box and grid (spacing ~1), Gaussian w=2 R=6",
             "particles": int(Ns.sum()), "grid_points": int(G_total),
             "per_frame_launches": {"frames_per_s": F / (ms_plain * 1e-3), "ms_per_batch": ms_plain},
+            "fused_graph": {"frames_per_s": F / (ms_fused * 1e-3), "ms_per_batch": ms_fused,
+                            "kernel_launches_per_batch": int(launches_fused),
+                            "what": "every stage once over the batch: one persistent gather over all frames"},
+            "lanes_graph": {"frames_per_s": F / (ms_lanes * 1e-3), "ms_per_batch": ms_lanes,
+                            "kernel_launches_per_batch": int(launches_lanes),
+                            "what": "one launch sequence per frame on eight streams, one graph"},
             "graph_autotuned": {"frames_per_s": F / (ms_graph * 1e-3), "ms_per_batch": ms_graph,
                                 "tuning": best, "kernel_launches_per_batch": int(launches)},
             "speedup": ms_plain / ms_graph}
@@ -513,21 +529,34 @@ def ours(args, wl, name):
     ms_max = max_over_ranks(ms, world)
     value = world * F * args.steps / (ms_max * 1e-3)
 
+    def timed_steps():
+        for _ in range(3):
+            step()
+        ctx.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        l0 = ctx.launch_count()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ctx.wait_all()
+        e1.record(stream)
+        ctx.synchronize()
+        return F * args.steps / (e0.elapsed_time(e1) * 1e-3), (ctx.launch_count() - l0) // args.steps
+
     # ---- the other per-lane summation beside the headline (same frames, same graph path)
     ctx.set_flags(ikabi.FLAG_LANE_KAHAN - lane_flags)
-    for _ in range(3):
-        step()
-    ctx.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-    ctx.wait_all()
-    e1.record(stream)
-    ctx.synchronize()
-    other_value = F * args.steps / (e0.elapsed_time(e1) * 1e-3)
+    other_value, _ = timed_steps()
     ctx.set_flags(lane_flags)
+    # ---- and the other batch schedule: fused (the default) or one launch sequence per frame
+    fused0 = ctx.get_tuning("fused_batch")
+    ctx.set_tuning("fused_batch", 1 - fused0)
+    other_sched, other_launches = timed_steps()
+    ctx.set_tuning("fused_batch", fused0)
+    schedules = {"headline": "fused" if fused0 else "lanes",
+                 "fused_frames_per_s": value / world if fused0 else other_sched,
+                 "lanes_frames_per_s": other_sched if fused0 else value / world,
+                 "launches_per_step": {"headline": int(launches) // args.steps, "other": int(other_launches)}}
     lane_sums = {"headline": args.lane_sums,
                  "kahan_frames_per_s": value / world if lane_flags else other_value,
                  "plain_frames_per_s": other_value if lane_flags else value / world}
@@ -616,6 +645,19 @@ def ours(args, wl, name):
     A = float(np.mean(trip))
     flop = FLOP_PER_TRIPLE[D] * A
     achieved = flop / (g_ms * 1e-3) / 1e12
+    per_frame_gather = {"kernel": "k_gather32<KAHAN=%d> (one frame per launch)" % (1 if lane_flags else 0),
+                        "achieved": achieved, "launch_ms": g_ms, "flop_per_launch": flop}
+    roof_kernel = per_frame_gather["kernel"]
+    if fused0:  # the headline's gather: every frame of the step in one launch
+        tf_ = [ctx.time_fused_batch(all_slots) for _ in range(4)][1:]
+        g_ms = float(np.median([t["gather"] for t in tf_]))
+        A = float(sum(ctx.counters(k)[2] for k in range(F)))
+        flop = FLOP_PER_TRIPLE[D] * A
+        achieved = flop / (g_ms * 1e-3) / 1e12
+        roof_kernel = "k_gather32<KAHAN=%d, BATCH> (fused: the %d frames of a step in one launch)" % (
+            1 if lane_flags else 0, F)
+        stage_ms_fused = {"prepare": float(np.median([t["prepare"] for t in tf_])), "gather": g_ms,
+                          "note": "ms per step of %d frames, CUDA events, no graph" % F}
     peak = ikabi.measure_fp32_peak(local)
     traffic = None
     tf = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
@@ -640,7 +682,7 @@ def ours(args, wl, name):
            "gpu_launches": int(launches),
            "clocks": clocks.summary(t_soak, t_host1),
            "roofline": {"bound": "fp32",
-                        "kernel": "k_gather32<KAHAN=%d>" % (1 if lane_flags else 0), "achieved": achieved, "peak": peak,
+                        "kernel": roof_kernel, "achieved": achieved, "peak": peak,
                         "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                         "flop_per_launch": flop, "active_triples_per_launch": A, "launch_ms": g_ms,
                         "peak_source": "measured live: FFMA throughput probe (ik_measure_fp32_peak)"},
@@ -653,7 +695,14 @@ def ours(args, wl, name):
            "tuned_over_plain": value / plain_value,
            "rel_err_vs_fp64": {"virial": err_v, "kinetic": err_k},
            "lane_sums": lane_sums,
-           "interactions_per_s": A * value}
+           "schedules": schedules,
+           "per_frame_gather": per_frame_gather,
+           "interactions_per_s": (A / F if fused0 else A) * value}
+    if fused0:
+        out["stage_ms_fused"] = stage_ms_fused
+        if traffic is not None:  # the capture is of one frame's gather: scaled to the step's frames
+            out["roofline"]["traffic"] = traffic * F
+            out["roofline"]["traffic_note"] = "ncu DRAM bytes of one frame's gather x %d frames" % F
     if surrogate is not None:
         out["surrogate"] = surrogate
     if uneven is not None:

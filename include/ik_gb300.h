@@ -282,19 +282,37 @@ int ik_get_launch_count(ik_ctx* ctx, int64_t* out);
 /* Counters of the last computation: [0] force-active directed bonds,
  * [1] accepted (grid, particle) pairs, [2] active (grid, i, j) triples (FP32 path). */
 int ik_get_counters(ik_ctx* ctx, int slot, int64_t* out3);
-/* Tuning of the FP32 gather (no reference counterpart).  0 restores the default.
+/* Tuning of the FP32 gather (no reference counterpart).  0 restores the default (except
+ * IK_TUNE_FUSED_BATCH, where 0 turns fused batches off).
  *   IK_TUNE_BIN_POINTS     target grid points per work item (bin of cells)
- *   IK_TUNE_BLOCKS_PER_SM  persistent CTAs launched per SM (default: 2 for a frame computed alone, 1 for
- *                          the frames of a batch, which run side by side on the engine lanes)
- *   IK_TUNE_HALO_CAP       staged halo particles per warp (grows on overflow) */
+ *   IK_TUNE_BLOCKS_PER_SM  persistent CTAs launched per SM (default: 2 for a frame computed alone and
+ *                          for a fused batch, 1 for the frames of a batch that run side by side on
+ *                          the engine lanes)
+ *   IK_TUNE_HALO_CAP       staged halo particles per warp (grows on overflow)
+ *   IK_TUNE_FUSED_BATCH    1 (default): ik_compute_batch runs an eligible batch fused -- every
+ *                          stage once over all its frames (bin, scan, scatter, sort + pack,
+ *                          bonds, one persistent gather over every frame's work items,
+ *                          finish: 7 to 8 kernel launches per batch, recorded as one CUDA
+ *                          graph); 0: one launch sequence per frame on the lanes.  Eligible:
+ *                          FP32 path, virial and/or kinetic field, fixed-point rule of order
+ *                          4 or 5, n * (bonds per particle) < 2^25 per slot, no slot twice */
 #define IK_TUNE_BIN_POINTS 1
 #define IK_TUNE_BLOCKS_PER_SM 2
 #define IK_TUNE_HALO_CAP 3
+#define IK_TUNE_FUSED_BATCH 4
 int ik_set_tuning(ik_ctx* ctx, int param, int value);
 int ik_get_tuning(ik_ctx* ctx, int param, int* value);
+/* Diagnostic (no reference counterpart): runs the batch once fused, without a graph,
+ * with CUDA events around its stages, and returns ms4 = {preparation (bin, scan,
+ * scatter, sort + pack, bonds), 0, the persistent gather over every frame, both}.  The
+ * slots' fields are computed as by ik_compute_batch.  IK_ERR_UNSUPPORTED for a batch
+ * that cannot run fused (see IK_TUNE_FUSED_BATCH). */
+int ik_time_fused_batch(ik_ctx* ctx, const int* slots, int count, int fields, float* ms4);
 /* Autotuner: times ik_compute_batch over the given slots (`reps` CUDA-graph replays per
- * candidate, CUDA events on the context's stream) for each candidate bin size x CTAs
- * per SM, keeps the fastest and reports it.  FP32 path only. */
+ * candidate, CUDA events on the context's stream) for each candidate schedule (fused
+ * batch or per-frame lanes) x bin size x CTAs per SM x staged halo per warp, keeps the
+ * fastest (all four settings, readable with ik_get_tuning) and reports the bin size,
+ * CTAs per SM and time.  FP32 path only. */
 int ik_autotune_batch(ik_ctx* ctx, const int* slots, int count, int precision, int fields, int reps,
                       int* best_bin_points, int* best_blocks_per_sm, float* best_ms);
 

@@ -141,10 +141,15 @@ def base(feats):
     return 0.5 * s1 * np.sum(w[None, :] * np.exp(-0.5 * (d[:, None] ** 2 + t * t)), axis=1)
 
 
+BASE_MIN = 1e-9  # targets are 0 below this baseline (the labels' tolerance is 1e-14 absolute)
+
+
 def targets(feats, labels):
-    """Training targets y = (B / base - 1) * YSCALE."""
+    """Training targets y = (B / base - 1) * YSCALE, clipped to [-8, 8]; 0 where the
+    baseline is below BASE_MIN."""
     bs = base(feats)
-    return np.where(bs > 1e-30, (np.asarray(labels) / np.where(bs > 1e-30, bs, 1.0) - 1.0) * YSCALE, 0.0)
+    y = (np.asarray(labels) / np.where(bs > BASE_MIN, bs, 1.0) - 1.0) * YSCALE
+    return np.where(bs > BASE_MIN, np.clip(y, -8.0, 8.0), 0.0)
 
 
 def value(feats, y):

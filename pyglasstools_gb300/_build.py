@@ -15,8 +15,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libik_gb300.so")
 # longest first: the build runs them in parallel
-CU_SOURCES = ["ik_gather32.cu", "ik_gather32_aux.cu", "ik_gather32_exact.cu", "ik_mlp.cu", "ik_api.cu", "ik_cells.cu", "ik_gather64.cu",
-              "ik_noalloc.cu", "ik_bonds.cu"]
+CU_SOURCES = ["ik_gather32.cu", "ik_gather32_aux.cu", "ik_gather32_batch.cu", "ik_gather32_exact.cu", "ik_mlp.cu", "ik_api.cu", "ik_cells.cu", "ik_gather64.cu",
+              "ik_noalloc.cu", "ik_bonds.cu", "ik_batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -107,6 +107,8 @@ struct Geo {
     int bw[3] = {1, 1, 1}, reach[3] = {0, 0, 0};
     int nitems = 0;
     DevBuf gpts_d, items_d;
+    std::vector<float4> gpts_h; // host copies (the fused batch concatenates them)
+    std::vector<int4> items_h;
 };
 
 struct Slot {
@@ -144,6 +146,18 @@ struct Lane {
     DevBuf eb64, ec64, eb32, ec32, enb, ecnt;  // elastic-field bond records, scratch counters
 };
 constexpr int IK_LANES = 8;
+
+// A fused batch: the frames of ik_compute_batch concatenated (particles, cells, grid
+// points, work items in batch order) so that every stage runs once over the batch.
+// Built on the host when the batch, a slot's size or geometry, or a setting changes.
+struct FusedBatch {
+    IkBatchLaunch b{};
+    int nitems = 0;
+    long long gtot = 0;
+    DevBuf slots, p_offs, c_offs, v_offs, items, item_slot, gpts, grid;
+    DevBuf cell_of, rank, cell_count, cell_start, sorted, bsum, relhi, rello, prec, plo, pos64, kin, diam32, tmp, nb;
+    DevBuf vir2, kin2, work;
+};
 
 // A computation not yet confirmed by ik_synchronize (re-run after a capacity growth),
 // with the host outputs its fields are being downloaded into (re-issued after a re-run).
@@ -196,6 +210,9 @@ struct ik_ctx {
     ik_mlp* mlp = nullptr; // learned bond-integral surrogate (IK_QUAD_MLP)
     // tuning of the FP32 gather (0 = default)
     int tune_bin_points = 0, tune_blocks_per_sm = 0;
+    int tune_fused = 1;     // ik_compute_batch: fused batches where eligible (IK_TUNE_FUSED_BATCH)
+    FusedBatch fused;
+    bool batch_fused = false; // the recorded batch graph is a fused batch
     bool in_batch = false; // enqueueing a batch: frames share the GPU (default 1 gather CTA per SM)
     long long mlp_cap = 0;  // record capacity per lane
     // CUDA-graph replay of ik_compute_batch
@@ -490,6 +507,8 @@ int ensure_geometry(ik_ctx* c)
         items.push_back(make_int4(0, 0, 0, (int)c->geo.G));
     }
     c->geo.nitems = (int)items.size() - 1;
+    c->geo.gpts_h = gpts;
+    c->geo.items_h = items;
     ENS(c->geo.gpts_d, gpts.size() * sizeof(float4));
     ENS(c->geo.items_d, items.size() * sizeof(int4));
     CK(cudaMemcpy(c->geo.gpts_d.p, gpts.data(), gpts.size() * sizeof(float4), cudaMemcpyHostToDevice));
@@ -606,6 +625,9 @@ int elastic_bonds(ik_ctx* c, Slot& s, Lane& L, const IkGeom& g, int n)
     return IK_OK;
 }
 
+GatherGeo gather_geo(ik_ctx* c);
+void gather_rule(ik_ctx* c, GatherArgs32& a);
+
 int enqueue(ik_ctx* c, int slot, int prec, int fields)
 {
     Slot& s = c->slots[(size_t)slot];
@@ -696,39 +718,8 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         if (timing) CK(cudaEventRecord(c->ev[2], L.st));
         nv.next("ik gather");
         GatherArgs32 a{};
-        a.g = g;
-        for (int k = 0; k < 3; ++k) {
-            a.cws[k] = (float)(c->cg.kappa * g.cw[k]);
-            a.bw[k] = c->geo.bw[k];
-            a.reach[k] = c->geo.reach[k];
-        }
-        a.kappa = c->cg.kappa;
-        // cull the staged halo to the particles within R of the bin's box where that drops
-        // a fifth or more of it (3D: a bin of one cell with a reach of one; the kernel
-        // culls in 3D only -- 2D bins of several cells lose ~12 %, less than the second
-        // pass over their particles costs)
-        {
-            double stagedv = 1.0, nearv = 1.0, side[3] = {0, 0, 0};
-            for (int k = 0; k < D; ++k) {
-                side[k] = c->geo.bw[k] * g.cw[k];
-                stagedv *= side[k] + 2.0 * c->geo.reach[k] * g.cw[k];
-            }
-            const double R = c->cg.rcut, PI = 3.14159265358979323846;
-            if (D == 2) nearv = side[0] * side[1] + 2.0 * R * (side[0] + side[1]) + PI * R * R;
-            else nearv = side[0] * side[1] * side[2] + 2.0 * R * (side[0] * side[1] + side[1] * side[2] + side[0] * side[2]) +
-                         PI * R * R * (side[0] + side[1] + side[2]) + 4.0 / 3.0 * PI * R * R * R;
-            a.cull = nearv < 0.8 * stagedv ? 1 : 0;
-        }
-        a.R2s = c->cg.R2s;
-        a.margin = 1e-4f * c->cg.R2s;
-        a.R2 = c->cg.rcutsq;
-        a.npairs = c->gl.npairs;
-        a.w0 = c->gl.w0;
-        for (int k = 0; k < 32; ++k) {
-            a.xi2[k] = c->gl.t[k] * c->gl.t[k];
-            a.m2xi[k] = -2.0f * c->gl.t[k];
-            a.w[k] = c->gl.wt[k];
-        }
+        a.geo = gather_geo(c);
+        gather_rule(c, a);
         a.prec = L.prec.as<IkPRec>();
         a.pos64 = L.pos64.as<IkB64>();
         a.cell_start = L.cell_start.as<int>();
@@ -909,6 +900,53 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
 }
 
 // Settings that every binning depends on (cut-offs, kappa, bin size) changed.
+void invalidate_geometry(ik_ctx* c);
+
+// The FP32 gather's geometry of the current box and binning (ensure_geometry done).
+GatherGeo gather_geo(ik_ctx* c)
+{
+    const IkGeom& g = c->geo.geom;
+    const int D = c->dim;
+    GatherGeo G{};
+    G.g = g;
+    for (int k = 0; k < 3; ++k) {
+        G.cws[k] = (float)(c->cg.kappa * g.cw[k]);
+        G.bw[k] = c->geo.bw[k];
+        G.reach[k] = c->geo.reach[k];
+    }
+    // cull the staged halo to the particles within R of the bin's box where that drops
+    // a fifth or more of it (3D: a bin of one cell with a reach of one; the kernel
+    // culls in 3D only -- 2D bins of several cells lose ~12 %, less than the second
+    // pass over their particles costs)
+    double stagedv = 1.0, nearv = 1.0, side[3] = {0, 0, 0};
+    for (int k = 0; k < D; ++k) {
+        side[k] = c->geo.bw[k] * g.cw[k];
+        stagedv *= side[k] + 2.0 * c->geo.reach[k] * g.cw[k];
+    }
+    const double R = c->cg.rcut, PI = 3.14159265358979323846;
+    if (D == 2) nearv = side[0] * side[1] + 2.0 * R * (side[0] + side[1]) + PI * R * R;
+    else nearv = side[0] * side[1] * side[2] + 2.0 * R * (side[0] * side[1] + side[1] * side[2] + side[0] * side[2]) +
+                 PI * R * R * (side[0] + side[1] + side[2]) + 4.0 / 3.0 * PI * R * R * R;
+    G.cull = nearv < 0.8 * stagedv ? 1 : 0;
+    return G;
+}
+
+// The coarse-graining constants and the Gauss-Legendre rule of the FP32 gather.
+void gather_rule(ik_ctx* c, GatherArgs32& a)
+{
+    a.kappa = c->cg.kappa;
+    a.R2s = c->cg.R2s;
+    a.margin = 1e-4f * c->cg.R2s;
+    a.R2 = c->cg.rcutsq;
+    a.npairs = c->gl.npairs;
+    a.w0 = c->gl.w0;
+    for (int k = 0; k < 32; ++k) {
+        a.xi2[k] = c->gl.t[k] * c->gl.t[k];
+        a.m2xi[k] = -2.0f * c->gl.t[k];
+        a.w[k] = c->gl.wt[k];
+    }
+}
+
 void invalidate_geometry(ik_ctx* c)
 {
     c->geo.geom_valid = false;
@@ -930,6 +968,221 @@ struct GeoSwap {
     GeoSwap(const GeoSwap&) = delete;
     GeoSwap& operator=(const GeoSwap&) = delete;
 };
+
+// ---- fused batches -----------------------------------------------------------
+// A batch runs fused (every stage once over all its frames) when it computes the
+// virial and/or kinetic field on the FP32 path with the fixed-point rule of order 4 or
+// 5, every slot's bond records fit the per-frame staged-entry word (n maxb < 2^25, at
+// most 63 bonds per particle), and no slot appears twice.  Otherwise its frames run on
+// the lanes (one launch sequence per frame), as with fused batches turned off.
+bool fused_eligible(ik_ctx* c, const std::vector<int>& slots, int prec, int fields)
+{
+    if (!c->tune_fused || prec != IK_PREC_FP32 || (fields & ~(IK_FIELD_VIRIAL | IK_FIELD_KINETIC)) || !fields)
+        return false;
+    if (c->cg.mode != IK_QUAD_FIXEDPOINT || c->gl.npairs != 2 || c->maxb > 63) return false;
+    if (c->flags & (IK_FLAG_CSR_BONDS | IK_FLAG_TIMING)) return false;
+    std::vector<int> sorted(slots);
+    std::sort(sorted.begin(), sorted.end());
+    if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end()) return false;
+    long long ptot = 0;
+    for (int k : slots) {
+        const int64_t n = c->slots[(size_t)k].n;
+        if ((size_t)std::max<int64_t>(n, 1) * (size_t)c->maxb >= ((size_t)1 << 25)) return false;
+        ptot += n;
+    }
+    return ptot < (1LL << 30);
+}
+
+// Concatenates the slots' frames, cells, grids and work items (host, then one upload of
+// each array) and sizes the batch-wide work buffers.  Not during a capture.
+int fused_build(ik_ctx* c, const std::vector<int>& slots)
+{
+    const int D = c->dim, NC = D == 2 ? 3 : 6, S = (int)slots.size();
+    FusedBatch& F = c->fused;
+    std::vector<IkBatchSlot> hs((size_t)S);
+    std::vector<int> po((size_t)S + 1), co((size_t)S + 1);
+    std::vector<long long> vo((size_t)S + 1);
+    std::vector<int4> items;
+    std::vector<int> islot;
+    std::vector<float4> gp;
+    std::vector<double> gr;
+    long long P = 0, Cc = 0, Gt = 0;
+    for (int k = 0; k < S; ++k) {
+        GeoSwap gs(c, slots[(size_t)k]);
+        Slot& s = c->slots[(size_t)slots[(size_t)k]];
+        const IkGeom& g = c->geo.geom;
+        const int64_t G = c->geo.G;
+        ENS(s.vir, sizeof(double) * NC * std::max<int64_t>(G, 1));
+        ENS(s.kin, sizeof(double) * NC * std::max<int64_t>(G, 1));
+        ENS(s.counters, sizeof(unsigned long long) * 4);
+        IkBatchSlot& b = hs[(size_t)k];
+        b.geo = gather_geo(c);
+        b.geo.c_off = (int)Cc;
+        b.geo.p_off = (int)P;
+        b.geo.cnt = s.counters.as<unsigned long long>();
+        b.pos = s.pos.as<double>();
+        b.vel = s.has_vel ? s.vel.as<double>() : nullptr;
+        b.mass = s.has_mass ? s.mass.as<double>() : nullptr;
+        b.diam = s.diam.as<double>();
+        b.out_vir = s.vir.as<double>();
+        b.out_kin = s.kin.as<double>();
+        b.n = (int)s.n;
+        b.ncell = g.ncell;
+        b.allax = 0;
+        for (int a = 0; a < D; ++a) b.allax |= (g.all_bond[a] && g.nc[a] > 1) ? 1 : 0;
+        b.G = G;
+        b.g_off = Gt;
+        po[(size_t)k] = (int)P;
+        co[(size_t)k] = (int)Cc;
+        vo[(size_t)k] = Gt * NC;
+        for (int j = 0; j < c->geo.nitems; ++j) {
+            int4 it = c->geo.items_h[(size_t)j];
+            it.w += (int)Gt;
+            items.push_back(it);
+            islot.push_back(k);
+        }
+        for (int64_t j = 0; j < G; ++j) {
+            float4 v = c->geo.gpts_h[(size_t)j];
+            int gi;
+            std::memcpy(&gi, &v.w, 4);
+            gi += (int)Gt;
+            std::memcpy(&v.w, &gi, 4);
+            gp.push_back(v);
+        }
+        gr.insert(gr.end(), c->geo.grid_h.begin(), c->geo.grid_h.begin() + 3 * G);
+        P += s.n;
+        Cc += g.ncell;
+        Gt += G;
+        if (P >= (1LL << 30) || Cc >= (1LL << 30) || Gt >= (1LL << 30))
+            return fail(IK_ERR_UNSUPPORTED, "fused batch too large (particles, cells or grid points >= 2^30)");
+    }
+    po[(size_t)S] = (int)P;
+    co[(size_t)S] = (int)Cc;
+    vo[(size_t)S] = Gt * NC;
+    items.push_back(make_int4(0, 0, 0, (int)Gt));
+    F.nitems = (int)items.size() - 1;
+    F.gtot = Gt;
+    auto up = [&](DevBuf& d, const void* h, size_t bytes) -> int {
+        ENS(d, std::max<size_t>(bytes, 16));
+        if (bytes) CK(cudaMemcpy(d.p, h, bytes, cudaMemcpyHostToDevice));
+        return IK_OK;
+    };
+    if (int r = up(F.slots, hs.data(), sizeof(IkBatchSlot) * hs.size())) return r;
+    if (int r = up(F.p_offs, po.data(), sizeof(int) * po.size())) return r;
+    if (int r = up(F.c_offs, co.data(), sizeof(int) * co.size())) return r;
+    if (int r = up(F.v_offs, vo.data(), sizeof(long long) * vo.size())) return r;
+    if (int r = up(F.items, items.data(), sizeof(int4) * items.size())) return r;
+    if (int r = up(F.item_slot, islot.data(), sizeof(int) * islot.size())) return r;
+    if (int r = up(F.gpts, gp.data(), sizeof(float4) * gp.size())) return r;
+    if (int r = up(F.grid, gr.data(), sizeof(double) * gr.size())) return r;
+    const size_t np = (size_t)std::max<long long>(P, 1), nc1 = (size_t)Cc + 1;
+    ENS(F.cell_of, sizeof(int) * np);
+    ENS(F.rank, sizeof(int) * np);
+    ENS(F.sorted, sizeof(int) * np);
+    ENS(F.nb, sizeof(int) * np);
+    ENS(F.cell_count, sizeof(int) * nc1);
+    ENS(F.cell_start, sizeof(int) * nc1);
+    ENS(F.bsum, sizeof(int) * (nc1 / 4096 + 2));
+    ENS(F.relhi, sizeof(float4) * np);
+    ENS(F.rello, sizeof(float4) * np);
+    ENS(F.prec, sizeof(IkPRec) * np);
+    ENS(F.plo, sizeof(float4) * np);
+    ENS(F.pos64, sizeof(IkB64) * np);
+    ENS(F.kin, sizeof(float4) * (D == 3 ? 2 : 1) * np);
+    ENS(F.diam32, sizeof(float) * np);
+    ENS(F.tmp, sizeof(float4) * (size_t)c->maxb * np);
+    ENS(F.vir2, sizeof(float2) * NC * (size_t)std::max<long long>(Gt, 1));
+    ENS(F.kin2, sizeof(float2) * NC * (size_t)std::max<long long>(Gt, 1));
+    ENS(F.work, sizeof(int));
+    IkBatchLaunch& b = F.b;
+    b.slots = F.slots.as<IkBatchSlot>();
+    b.p_offs = F.p_offs.as<int>();
+    b.c_offs = F.c_offs.as<int>();
+    b.v_offs = F.v_offs.as<long long>();
+    b.nslots = S;
+    b.ptot = (int)P;
+    b.ctot = (int)Cc;
+    b.vtot = Gt * NC;
+    b.cell_of = F.cell_of.as<int>();
+    b.rank = F.rank.as<int>();
+    b.cell_count = F.cell_count.as<int>();
+    b.cell_start = F.cell_start.as<int>();
+    b.sorted = F.sorted.as<int>();
+    b.bsum = F.bsum.as<int>();
+    b.relhi = F.relhi.as<float4>();
+    b.rello = F.rello.as<float4>();
+    b.prec = F.prec.as<IkPRec>();
+    b.plo = F.plo.as<float4>();
+    b.pos64 = F.pos64.as<IkB64>();
+    b.kin = F.kin.as<float4>();
+    b.diam32 = F.diam32.as<float>();
+    b.tmp = F.tmp.as<float4>();
+    b.nb = F.nb.as<int>();
+    b.maxb = c->maxb;
+    b.status = c->status.as<int>();
+    b.maxnb = c->maxnb.as<int>();
+    return IK_OK;
+}
+
+// The launches of a fused batch on the context stream (fused_build done).  timing:
+// events ev[0] before the preparation, ev[1] = ev[2] after it, ev[3] after the gather.
+int fused_enqueue(ik_ctx* c, int fields, bool timing = false)
+{
+    NvtxRange nvr("ik fused batch");
+    FusedBatch& F = c->fused;
+    const IkBatchLaunch& b = F.b;
+    const int D = c->dim;
+    cudaStream_t st = c->stream;
+    if (timing) CK(cudaEventRecord(c->ev[0], st));
+    CK(cudaMemsetAsync(b.cell_count, 0, sizeof(int) * ((size_t)b.ctot + 1), st));
+    CK(cudaMemsetAsync(F.work.p, 0, sizeof(int), st));
+    CK(launch_batch_prepare(b, D, c->pot, c->cg.kappa, st));
+    if (timing) {
+        CK(cudaEventRecord(c->ev[1], st));
+        CK(cudaEventRecord(c->ev[2], st));
+    }
+    c->launches += 1 + (b.ctot <= 65536 ? 1 : 2) + (b.ptot > 0 ? 1 : 0) + (b.ctot > 0 ? 1 : 0) + (b.ptot > 0 ? 1 : 0);
+    GatherArgs32 a{};
+    a.geo.g.dim = D; // the slots carry their own geometry
+    gather_rule(c, a);
+    a.prec = b.prec;
+    a.pos64 = b.pos64;
+    a.cell_start = b.cell_start;
+    a.boff = nullptr;
+    a.nprec = b.ptot;
+    a.nb = b.nb;
+    a.bonds = b.tmp;
+    a.maxb = c->maxb;
+    a.kin = b.kin;
+    a.gpts = F.gpts.as<float4>();
+    a.grid = F.grid.as<double>();
+    a.items = F.items.as<int4>();
+    a.nitems = F.nitems;
+    a.halo_cap = c->halo_cap;
+    a.qcap = 32 * (std::min(c->maxb, 63) + 1);
+    a.out_vir = F.vir2.as<float2>();
+    a.out_kin = F.kin2.as<float2>();
+    a.fields = fields & (IK_FIELD_VIRIAL | IK_FIELD_KINETIC);
+    a.work_counter = F.work.as<int>();
+    a.status = c->status.as<int>();
+    a.slots = b.slots;
+    a.item_slot = F.item_slot.as<int>();
+    const size_t stage_bytes = D == 3 ? 20 : 16;
+    const size_t smem = (size_t)IK_WARPS_GATHER * ((size_t)c->halo_cap * stage_bytes + (size_t)a.qcap * 4);
+    // every frame's items in one launch: two CTAs per SM by default, as a frame alone
+    const int bps = c->tune_blocks_per_sm > 0 ? c->tune_blocks_per_sm : 2;
+    const int blocks = std::min(F.nitems, c->sm_count * bps);
+    if (blocks > 0) {
+        CK(launch_gather32_batch(a, c->cg.kind, (c->flags & IK_FLAG_LANE_KAHAN) != 0, blocks, 32 * IK_WARPS_GATHER,
+                                 smem, st));
+        c->launches += 1;
+    }
+    if (timing) CK(cudaEventRecord(c->ev[3], st));
+    const double norm = c->cg.kind == IK_CG_MOLLIFIER ? c->cg.mollifier_norm : c->cg.norm;
+    CK(launch_batch_finish(b, a.out_vir, a.out_kin, 0.5 * norm, norm, fields, st));
+    c->launches += b.vtot > 0 ? 1 : 0;
+    return IK_OK;
+}
 
 // Checks, geometry and capacities of one slot, then its launches.
 int prepare_enqueue(ik_ctx* c, int slot, int prec, int fields)
@@ -1424,7 +1677,12 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
         c->in_batch = false;
         if (int r = ik_synchronize(c)) return r;
         if (c->flags & IK_FLAG_TIMING) return IK_OK;
-        // then capture the same sequence as one graph (lanes fork from and join the main stream)
+        // then capture the batch as one graph: fused (every stage once over the batch) where
+        // eligible, else the same per-frame sequence (lanes fork from and join the main stream)
+        const bool fused = fused_eligible(c, key, precision, fields);
+        if (fused) {
+            if (int r = fused_build(c, key)) return r;
+        }
         if (c->batch_exec) { cudaGraphExecDestroy(c->batch_exec); c->batch_exec = nullptr; }
         if (c->io_exec) { cudaGraphExecDestroy(c->io_exec); c->io_exec = nullptr; } // versions below are ours now
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
@@ -1434,7 +1692,8 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
         c->captured_lanes = 0;
         int rr = IK_OK;
         c->in_batch = true;
-        for (int k = 0; k < count && rr == IK_OK; ++k) rr = prepare_enqueue(c, slots[k], precision, fields);
+        if (fused) rr = fused_enqueue(c, fields);
+        for (int k = 0; k < count && rr == IK_OK && !fused; ++k) rr = prepare_enqueue(c, slots[k], precision, fields);
         c->in_batch = false;
         for (int l = 0; l < IK_LANES && rr == IK_OK; ++l)
             if (c->captured_lanes & (1 << l)) {
@@ -1453,6 +1712,7 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) { c->batch_exec = nullptr; return fail(IK_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e)); }
         c->batch_slots = key;
+        c->batch_fused = fused;
         c->batch_prec = precision;
         c->batch_fields = fields;
         c->batch_maxb = c->maxb;
@@ -1481,6 +1741,42 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
         s.last_fields = fields;
     }
     c->launches += c->batch_launches;
+    return IK_OK;
+}
+
+int ik_time_fused_batch(ik_ctx* c, const int* slots, int count, int fields, float* ms4)
+{
+    NvtxRange nvr("ik time_fused_batch");
+    if (int r = check_ctx(c)) return r;
+    if (count < 1 || !slots || !ms4) return fail(IK_ERR_ARG, "empty batch or null output");
+    for (int k = 0; k < count; ++k) if (int r = slot_ok(c, slots[k])) return r;
+    for (int k = 0; k < count; ++k) {
+        GeoSwap gs(c, slots[k]);
+        if (int r = ensure_ready(c)) return r;
+        if (int r = mode_ok(c, IK_PREC_FP32)) return r;
+        if (int r = ensure_geometry(c)) return r;
+    }
+    if (c->maxb == 0) c->maxb = c->dim == 2 ? IK_MAXB_2D : IK_MAXB_3D;
+    if (c->halo_cap == 0) c->halo_cap = 384;
+    std::vector<int> key(slots, slots + count);
+    // eligibility of the batch itself, whatever the timing flag and the schedule setting
+    const int saved_flags = c->flags, saved_fused = c->tune_fused;
+    c->flags &= ~IK_FLAG_TIMING;
+    c->tune_fused = 1;
+    const bool ok = fused_eligible(c, key, IK_PREC_FP32, fields);
+    c->flags = saved_flags;
+    c->tune_fused = saved_fused;
+    if (!ok) return fail(IK_ERR_UNSUPPORTED, "this batch cannot run fused");
+    if (int r = ik_wait_all(c)) return r;
+    if (int r = fused_build(c, key)) return r;
+    ++c->config_version; // the fused buffers were rebuilt: a recorded batch graph re-records
+    for (int k = 0; k < count; ++k) c->pending.push_back({slots[k], IK_PREC_FP32, fields});
+    if (int r = fused_enqueue(c, fields, true)) return r;
+    if (int r = ik_synchronize(c)) return r;
+    CK(cudaEventElapsedTime(&ms4[0], c->ev[0], c->ev[1]));
+    CK(cudaEventElapsedTime(&ms4[1], c->ev[1], c->ev[2]));
+    CK(cudaEventElapsedTime(&ms4[2], c->ev[2], c->ev[3]));
+    CK(cudaEventElapsedTime(&ms4[3], c->ev[0], c->ev[3]));
     return IK_OK;
 }
 
@@ -1975,6 +2271,10 @@ int ik_set_tuning(ik_ctx* c, int param, int value)
         if (value < 0 || value > 1024) return fail(IK_ERR_ARG, "halo capacity must be in [0, 1024]");
         c->halo_cap = (value + 31) & ~31; // whole warps of entries (the per-warp layout needs a multiple of 4)
         return IK_OK;
+    case IK_TUNE_FUSED_BATCH:
+        if (value != 0 && value != 1) return fail(IK_ERR_ARG, "fused batches: 0 or 1");
+        c->tune_fused = value;
+        return IK_OK;
     default:
         return fail(IK_ERR_ARG, "unknown tuning parameter %d", param);
     }
@@ -1987,44 +2287,55 @@ int ik_autotune_batch(ik_ctx* c, const int* slots, int count, int precision, int
     if (int r = check_ctx(c)) return r;
     if (reps < 1 || reps > 1000) return fail(IK_ERR_ARG, "reps must be in [1, 1000]");
     if (precision != IK_PREC_FP32) return fail(IK_ERR_ARG, "the autotuner tunes the FP32 path");
+    // candidates: the schedule (fused batch or one launch sequence per frame on the
+    // lanes), the work-item bin size, persistent CTAs per SM, staged halo per warp
     static const int bins_2d[] = {12, 16, 20, 25, 36};
     static const int bins_3d[] = {16, 24, 48, 96};
     static const int blocks[] = {1, 2};
+    static const int halos[] = {256, 384, 512};
     const int* bins = c->dim == 3 ? bins_3d : bins_2d;
     const int nbins = c->dim == 3 ? 4 : 5;
+    const int halo_min = c->halo_cap > 384 ? c->halo_cap : 0; // a halo grown by an overflow stays grown
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     CK(cudaEventCreate(&e0));
     if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); return fail(IK_ERR_CUDA, "event creation failed"); }
     float best = 1e30f;
-    int bb = 0, bk = 0, rc = IK_OK;
-    for (int i = 0; i < nbins && rc == IK_OK; ++i)
-        for (int k = 0; k < 2 && rc == IK_OK; ++k) {
-            if ((rc = ik_set_tuning(c, IK_TUNE_BIN_POINTS, bins[i])) ||
-                (rc = ik_set_tuning(c, IK_TUNE_BLOCKS_PER_SM, blocks[k])) ||
-                (rc = ik_compute_batch(c, slots, count, precision, fields)) || // plain run + graph recording
-                (rc = ik_compute_batch(c, slots, count, precision, fields)) || (rc = ik_wait_all(c)))
-                break;
-            if (cudaEventRecord(e0, c->stream) != cudaSuccess) { rc = fail(IK_ERR_CUDA, "event record failed"); break; }
-            for (int t = 0; t < reps && rc == IK_OK; ++t) rc = ik_compute_batch(c, slots, count, precision, fields);
-            if (rc || (rc = ik_wait_all(c))) break;
-            float ms = 0.f;
-            if (cudaEventRecord(e1, c->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
-                cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) { rc = fail(IK_ERR_CUDA, "event timing failed"); break; }
-            if ((rc = ik_synchronize(c))) break;
-            ms /= (float)reps;
-            if (ms < best) { best = ms; bb = bins[i]; bk = blocks[k]; }
-        }
+    int bb = 0, bk = 0, bh = c->halo_cap, bf = c->tune_fused, rc = IK_OK;
+    for (int fu = 1; fu >= 0 && rc == IK_OK; --fu)
+        for (int i = 0; i < nbins && rc == IK_OK; ++i)
+            for (int k = 0; k < 2 && rc == IK_OK; ++k)
+                for (int h = 0; h < 3 && rc == IK_OK; ++h) {
+                    const int hv = std::max(halos[h], halo_min);
+                    if (h > 0 && hv == std::max(halos[h - 1], halo_min)) continue;
+                    if ((rc = ik_set_tuning(c, IK_TUNE_FUSED_BATCH, fu)) ||
+                        (rc = ik_set_tuning(c, IK_TUNE_BIN_POINTS, bins[i])) ||
+                        (rc = ik_set_tuning(c, IK_TUNE_BLOCKS_PER_SM, blocks[k])) ||
+                        (rc = ik_set_tuning(c, IK_TUNE_HALO_CAP, hv)) ||
+                        (rc = ik_compute_batch(c, slots, count, precision, fields)) || // plain run + graph recording
+                        (rc = ik_compute_batch(c, slots, count, precision, fields)) || (rc = ik_wait_all(c)))
+                        break;
+                    if (cudaEventRecord(e0, c->stream) != cudaSuccess) { rc = fail(IK_ERR_CUDA, "event record failed"); break; }
+                    for (int t = 0; t < reps && rc == IK_OK; ++t) rc = ik_compute_batch(c, slots, count, precision, fields);
+                    if (rc || (rc = ik_wait_all(c))) break;
+                    float ms = 0.f;
+                    if (cudaEventRecord(e1, c->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) { rc = fail(IK_ERR_CUDA, "event timing failed"); break; }
+                    if ((rc = ik_synchronize(c))) break;
+                    ms /= (float)reps;
+                    if (ms < best) { best = ms; bb = bins[i]; bk = blocks[k]; bh = c->halo_cap; bf = fu; }
+                }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
+    if (int r = ik_set_tuning(c, IK_TUNE_FUSED_BATCH, bf)) return r;
     if (int r = ik_set_tuning(c, IK_TUNE_BIN_POINTS, bb)) return r;
     if (int r = ik_set_tuning(c, IK_TUNE_BLOCKS_PER_SM, bk)) return r;
+    if (int r = ik_set_tuning(c, IK_TUNE_HALO_CAP, bh)) return r;
     if (best_bin_points) *best_bin_points = bb;
     if (best_blocks_per_sm) *best_blocks_per_sm = bk;
     if (best_ms) *best_ms = best;
     return IK_OK;
 }
-
 int ik_get_tuning(ik_ctx* c, int param, int* value)
 {
     if (int r = check_ctx(c)) return r;
@@ -2033,6 +2344,7 @@ int ik_get_tuning(ik_ctx* c, int param, int* value)
     case IK_TUNE_BIN_POINTS: *value = c->tune_bin_points; return IK_OK;
     case IK_TUNE_BLOCKS_PER_SM: *value = c->tune_blocks_per_sm; return IK_OK;
     case IK_TUNE_HALO_CAP: *value = c->halo_cap; return IK_OK;
+    case IK_TUNE_FUSED_BATCH: *value = c->tune_fused; return IK_OK;
     default: return fail(IK_ERR_ARG, "unknown tuning parameter %d", param);
     }
 }

@@ -36,12 +36,12 @@ cudaError_t launch_gather32(const GatherArgs32& a, int kind, bool kahan, int qm,
     if (qm >= 2) return launch_gather32_exact(a, kind, kahan, qm, blocks, threads, smem, st);
     if (qm == 1) { // Gaussian kernel only, plain per-lane sums
         if (kind != 1 || kahan) return cudaErrorInvalidValue;
-        if (a.g.dim == 2) return a.npairs == 2 ? launch_one<2, 1, false, 2, 1>(a, blocks, threads, smem, st)
+        if (a.geo.g.dim == 2) return a.npairs == 2 ? launch_one<2, 1, false, 2, 1>(a, blocks, threads, smem, st)
                                                : launch_one<2, 1, false, 0, 1>(a, blocks, threads, smem, st);
         return a.npairs == 2 ? launch_one<3, 1, false, 2, 1>(a, blocks, threads, smem, st)
                              : launch_one<3, 1, false, 0, 1>(a, blocks, threads, smem, st);
     }
-    if (a.g.dim == 2) return kahan ? launch_np<2, true>(a, kind, blocks, threads, smem, st)
+    if (a.geo.g.dim == 2) return kahan ? launch_np<2, true>(a, kind, blocks, threads, smem, st)
                                    : launch_np<2, false>(a, kind, blocks, threads, smem, st);
     return kahan ? launch_np<3, true>(a, kind, blocks, threads, smem, st)
                  : launch_np<3, false>(a, kind, blocks, threads, smem, st);

@@ -18,7 +18,7 @@ static cudaError_t launch_kinds(const GatherArgs32& a, int kind, int blocks, int
 cudaError_t launch_gather32_aux(const GatherArgs32& a, int kind, bool kahan, int qm, int blocks, int threads,
                                 size_t smem, cudaStream_t st)
 {
-    const bool d2 = a.g.dim == 2;
+    const bool d2 = a.geo.g.dim == 2;
     if (a.bcoef) { // elastic field: plain per-lane sums, fixed-point rule
         if (qm) return cudaErrorInvalidValue;
         if (a.npairs == 2) return d2 ? launch_kinds<2, 2, 0, true, false>(a, kind, blocks, threads, smem, st)

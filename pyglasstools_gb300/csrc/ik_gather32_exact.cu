@@ -23,5 +23,5 @@ cudaError_t launch_gather32_exact(const GatherArgs32& a, int kind, bool kahan, i
 {
     (void)kahan; // plain per-lane sums in these modes
     if (kind != 1 || (qm != 2 && qm != 3) || a.bcoef) return cudaErrorInvalidValue;
-    return a.g.dim == 2 ? launch_qm<2>(a, qm, blocks, threads, smem, st) : launch_qm<3>(a, qm, blocks, threads, smem, st);
+    return a.geo.g.dim == 2 ? launch_qm<2>(a, qm, blocks, threads, smem, st) : launch_qm<3>(a, qm, blocks, threads, smem, st);
 }

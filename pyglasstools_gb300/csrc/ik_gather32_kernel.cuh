@@ -274,13 +274,17 @@ __device__ __forceinline__ int ik_red_index(int lane, int k)
 // (2 and 3: the Gaussian kernel only).
 // SPLIT: particles with more than 63 bonds are staged as several entries (one per 63
 // bonds; the entry word holds 6 count bits); the other variants need maxb <= 63.
-template <int DIM, int KIND, bool KAHAN, int NP, int QM, bool ELA, bool SPLIT>
+// BATCH: a fused batch -- work items of every slot in one launch; each item's slot
+// (a.item_slot) gives the geometry (copied to the warp's shared memory when the slot
+// changes) and the counters; particle, bond, grid and output indices are the batch's.
+template <int DIM, int KIND, bool KAHAN, int NP, int QM, bool ELA, bool SPLIT, bool BATCH>
 __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
 {
     constexpr int NC = DIM == 2 ? 3 : 6;       // unique tensor components
     constexpr int P = IK_P;
     constexpr bool MLPM = QM == 1;
     static_assert(QM < 2 || KIND == 1, "closed-form bond integrals: Gaussian kernel only");
+    static_assert(!BATCH || (QM == 0 && !ELA && !SPLIT), "fused batches: fixed-point rule, virial and kinetic");
 
     // CSR bond records are addressed by (offset << 6 | count) words: 2^25 records at most
     if (a.boff && a.boff[a.nprec] >= (1 << 25)) {
@@ -292,6 +296,12 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) s_next = 0;
+    // the geometry of the current item: the frame's (kernel parameter) or, in a fused
+    // batch, the item's slot's (a copy in this warp's shared memory)
+    __shared__ GatherGeo s_geo[BATCH ? IK_WARPS_GATHER : 1];
+    const GatherGeo& G = BATCH ? s_geo[warp] : a.geo;
+    int cur_slot = -1;
+    const float4* bonds_w = a.bonds; // the item's slot's bond records (fused batch: offset)
     __syncthreads();
     // per warp: staged particles (float4 x,y,z, bits(bond offset << 6 | bond count)),
     // their cell-order indices (3D; 2D keeps them in the unused z word), and the slot
@@ -305,7 +315,7 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
     const float cull_r2 = 1.001f * R2s + margin; // staging: within R of the bin's box, FP32 slack
     // culling the staged halo pays in 3D (a one-cell bin keeps ~3/4 of its 27-cell halo);
     // 2D bins of several cells keep ~7/8, less than the second pass over them costs
-    const bool cull = DIM == 3 && a.cull;
+    bool cull = DIM == 3 && G.cull;
     const bool want_kin = (a.fields & 2) != 0;
     const int npairs = NP > 0 ? NP : a.npairs;
     unsigned long long my_pairs = 0, my_triples = 0;
@@ -347,6 +357,22 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
         my_records += (unsigned long long)cnt;
     };
 
+    // pair and triple counts to the frame's counters (fused batch: the current slot's)
+    auto flush_counters = [&]() {
+        if (!BATCH || cur_slot >= 0) {
+            unsigned long long p2 = my_pairs, t2 = my_triples;
+            for (int o = 16; o; o >>= 1) {
+                p2 += __shfl_xor_sync(FULL, p2, o);
+                t2 += __shfl_xor_sync(FULL, t2, o);
+            }
+            if (lane == 0 && (p2 | t2)) {
+                atomicAdd(BATCH ? G.cnt + 1 : a.cnt_pairs, p2);
+                atomicAdd(BATCH ? G.cnt + 2 : a.cnt_triples, t2);
+            }
+        }
+        my_pairs = my_triples = 0;
+    };
+
     for (;;) {
         // work items: first this CTA's contiguous share (spatial neighbours, L1 reuse
         // across its warps), then a global counter over the remaining tail
@@ -358,6 +384,19 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
         }
         w = __shfl_sync(FULL, w, 0);
         if (w >= a.nitems) break;
+        if constexpr (BATCH) { // the item's slot: its geometry into this warp's copy
+            const int sl = __ldg(a.item_slot + w);
+            if (sl != cur_slot) {
+                flush_counters();
+                const int* src = reinterpret_cast<const int*>(&a.slots[sl].geo);
+                int* dst = reinterpret_cast<int*>(&s_geo[warp]);
+                for (int k = lane; k < (int)(sizeof(GatherGeo) / 4); k += 32) dst[k] = __ldg(src + k);
+                __syncwarp();
+                cur_slot = sl;
+                cull = DIM == 3 && G.cull;
+                bonds_w = a.bonds + (size_t)G.p_off * a.maxb;
+            }
+        }
         const int4 it = a.items[w];
         const int gend = a.items[w + 1].w;
 
@@ -366,13 +405,13 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             int cc = c == 0 ? it.x : (c == 1 ? it.y : it.z);
-            if (c >= DIM || a.g.nc[c] == 1) { h0[c] = 0; hn[c] = 1; }
-            else { h0[c] = cc - a.reach[c]; hn[c] = a.bw[c] + 2 * a.reach[c]; }
+            if (c >= DIM || G.g.nc[c] == 1) { h0[c] = 0; hn[c] = 1; }
+            else { h0[c] = cc - G.reach[c]; hn[c] = G.bw[c] + 2 * G.reach[c]; }
         }
         const int nh = hn[0] * hn[1] * hn[2];
         // the bin's box in scaled bin-relative coordinates, [0, bw cws) per axis (cells past
         // the box edge only shrink it: conservative)
-        const float bxs = a.bw[0] * a.cws[0], bys = a.bw[1] * a.cws[1], bzs = DIM == 3 ? a.bw[2] * a.cws[2] : 0.f;
+        const float bxs = G.bw[0] * G.cws[0], bys = G.bw[1] * G.cws[1], bzs = DIM == 3 ? G.bw[2] * G.cws[2] : 0.f;
         auto near_bin = [&](const IkPRec& r, float ox, float oy, float oz) {
             const float sx = fmaf(kappa, r.x, ox), sy = fmaf(kappa, r.y, oy);
             const float dx = fmaxf(fmaxf(-sx, sx - bxs), 0.f), dy = fmaxf(fmaxf(-sy, sy - bys), 0.f);
@@ -397,14 +436,14 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                 if (cid < nh) {
                     int ix = cid % hn[0], iy = (cid / hn[0]) % hn[1], iz = cid / (hn[0] * hn[1]);
                     int ux = h0[0] + ix, uy = h0[1] + iy, uz = h0[2] + iz;
-                    int wx = ik_wrap(ux, a.g.nc[0]), wy = ik_wrap(uy, a.g.nc[1]);
-                    int wz = DIM == 3 ? ik_wrap(uz, a.g.nc[2]) : 0;
-                    int cell = (wz * a.g.nc[1] + wy) * a.g.nc[0] + wx;
+                    int wx = ik_wrap(ux, G.g.nc[0]), wy = ik_wrap(uy, G.g.nc[1]);
+                    int wz = DIM == 3 ? ik_wrap(uz, G.g.nc[2]) : 0;
+                    int cell = (wz * G.g.nc[1] + wy) * G.g.nc[0] + wx + G.c_off;
                     cstart = a.cell_start[cell];
                     ccnt = a.cell_start[cell + 1] - cstart;
-                    ox = (ux - it.x) * a.cws[0];
-                    oy = (uy - it.y) * a.cws[1];
-                    oz = DIM == 3 ? (uz - it.z) * a.cws[2] : 0.f;
+                    ox = (ux - it.x) * G.cws[0];
+                    oy = (uy - it.y) * G.cws[1];
+                    oz = DIM == 3 ? (uz - it.z) * G.cws[2] : 0.f;
                 }
                 // staged entries of the cell: one per particle (with cull: only those
                 // within R of the bin's box -- the others cannot reach any of its grid
@@ -449,7 +488,7 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                         if (cull && !near_bin(r, ox, oy, oz)) continue;
                         int b0, nbq;
                         if (a.boff) { b0 = a.boff[q]; nbq = a.boff[q + 1] - b0; }
-                        else { b0 = q * a.maxb; nbq = a.nb[q]; }
+                        else { b0 = (q - G.p_off) * a.maxb; nbq = a.nb[q]; }
                         float4 s;
                         s.x = fmaf(kappa, r.x, ox);
                         s.y = fmaf(kappa, r.y, oy);
@@ -515,7 +554,7 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                 // separate so that two batches can be in flight before either computes.
                 auto load_slot = [&](int e, float4& sp, float4& b) {
                     sp = stage[e >> 10];
-                    b = __ldg(a.bonds + (__float_as_int(sp.w) >> 6) + ((e >> 4) & 63));
+                    b = __ldg(bonds_w + (__float_as_int(sp.w) >> 6) + ((e >> 4) & 63));
                 };
                 auto process_slot = [&](int e, const float4& sp, const float4& b) {
                     const int m = e & 15;
@@ -776,9 +815,9 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                             for (int p = 0; p < P; ++p) {
                                 if (!(band & (1 << p))) continue;
                                 const double* xg = a.grid + 3 * (size_t)gi[p];
-                                const double ddx = ik_minimg(__dsub_rn(xg[0], pq.x), a.g.L[0], a.g.periodic[0]);
-                                const double ddy = ik_minimg(__dsub_rn(xg[1], pq.y), a.g.L[1], a.g.periodic[1]);
-                                const double ddz = ik_minimg(__dsub_rn(xg[2], pq.z), a.g.L[2], a.g.periodic[2]);
+                                const double ddx = ik_minimg(__dsub_rn(xg[0], pq.x), G.g.L[0], G.g.periodic[0]);
+                                const double ddy = ik_minimg(__dsub_rn(xg[1], pq.y), G.g.L[1], G.g.periodic[1]);
+                                const double ddz = ik_minimg(__dsub_rn(xg[2], pq.z), G.g.L[2], G.g.periodic[2]);
                                 mask = ik_dot3(ddx, ddy, ddz) < a.R2 ? (mask | (1 << p)) : (mask & ~(1 << p));
                             }
                         }
@@ -912,25 +951,18 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
     }
     if constexpr (MLPM)
         for (long long k = wfill + lane; k < wend; k += 32) a.mlp_rid[k] = make_int2(-1, 0);
-    // counters
-    for (int o = 16; o; o >>= 1) {
-        my_pairs += __shfl_xor_sync(FULL, my_pairs, o);
-        my_triples += __shfl_xor_sync(FULL, my_triples, o);
-    }
-    if constexpr (MLPM)
+    flush_counters();
+    if constexpr (MLPM) {
         for (int o = 16; o; o >>= 1) my_records += __shfl_xor_sync(FULL, my_records, o);
-    if (lane == 0) {
-        atomicAdd(a.cnt_pairs, my_pairs);
-        atomicAdd(a.cnt_triples, my_triples);
-        if (MLPM) atomicAdd(a.cnt_records, my_records);
+        if (lane == 0) atomicAdd(a.cnt_records, my_records);
     }
 }
 
-template <int DIM, int KIND, bool KAHAN, int NP, int QM, bool ELA, bool SPLIT>
+template <int DIM, int KIND, bool KAHAN, int NP, int QM, bool ELA, bool SPLIT, bool BATCH = false>
 static cudaError_t ik_launch_gather32_kernel(const GatherArgs32& a, int blocks, int threads, size_t smem,
                                              cudaStream_t st)
 {
-    auto kfn = k_gather32<DIM, KIND, KAHAN, NP, QM, ELA, SPLIT>;
+    auto kfn = k_gather32<DIM, KIND, KAHAN, NP, QM, ELA, SPLIT, BATCH>;
     cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kfn<<<blocks, threads, smem, st>>>(a);

@@ -15,10 +15,6 @@ __global__ void k_cell_sort_pack(IkGeom g, const int* cell_start, int* sorted, c
 // ---- tuned-path preparation (ik_bonds.cu) ---------------------------------
 cudaError_t launch_bin32(const double* pos, int n, IkGeom g, int* cell_of, int* rank, int* cell_count, float4* relhi,
                          float4* rello, cudaStream_t st);
-cudaError_t launch_pack32(IkGeom g, int n, const int* sorted, const int* cell_of, const float4* relhi,
-                          const float4* rello, const double* pos, const double* vel, const double* mass,
-                          const double* diam, IkPRec* prec, float4* plo, IkB64* pos64, float4* kin, float* diam32,
-                          cudaStream_t st);
 cudaError_t launch_sort_pack32(IkGeom g, const int* cell_start, int* sorted, const float4* relhi, const float4* rello,
                                const double* pos, const double* vel, const double* mass, const double* diam,
                                IkPRec* prec, float4* plo, IkB64* pos64, float4* kin, float* diam32, cudaStream_t st);
@@ -48,12 +44,28 @@ __global__ void k_eval_pair(IkPot pot, int m, const double* rij, const double* d
                             double* f, double* en);
 
 // ---- FP32 tuned gather (ik_gather32.cu) ------------------------------------
-struct GatherArgs32 {
+// The geometry the gather needs per frame (per slot in a fused batch).
+struct GatherGeo {
     IkGeom g;
     float cws[3];          // kappa * cell width
     int bw[3];             // bin width (cells) per axis
     int reach[3];          // halo reach (cells) per axis; 0 on non-periodic axes
     int cull;              // stage only particles within R of the bin's box
+    int c_off;             // fused batch: the slot's first cell in the batch's cell list (else 0)
+    int p_off;             // fused batch: the slot's first particle in the batch (else 0)
+    unsigned long long* cnt; // fused batch: the slot's 4 counters (bonds, pairs, triples, spare)
+};
+// A slot of a fused batch (ik_compute_batch with every stage batch-wide): its gather
+// geometry, inputs, outputs and extents in the batch's concatenated arrays.
+struct IkBatchSlot {
+    GatherGeo geo;
+    const double *pos, *vel, *mass, *diam; // the slot's frame (vel / mass may be null)
+    double *out_vir, *out_kin;             // FP64 fields, G x NC (null: not requested)
+    int n, ncell, allax;                   // allax: some axis has fewer than three cells
+    long long G, g_off;                    // grid points; first grid point in the batch
+};
+struct GatherArgs32 {
+    GatherGeo geo;
     float kappa, R2s, margin;
     double R2;             // FP64 R^2 for the boundary re-check
     // Gauss-Legendre in symmetric form: nodes +-xi_k (k < npairs) with weights w_k,
@@ -86,6 +98,10 @@ struct GatherArgs32 {
     int* status;
     unsigned long long* cnt_pairs;
     unsigned long long* cnt_triples;
+    // fused batch: per item its slot (item_slot), per slot its geometry (slots[s].geo);
+    // particle, bond, grid and output indices are the batch's
+    const IkBatchSlot* slots;
+    const int* item_slot;
     // surrogate mode: bonds crossing the edge of the support go to records instead of
     // the fixed-point sum ({M, mb, hh, B_fixed} + {grid index, bond index})
     float4* mlp_rec;
@@ -110,6 +126,38 @@ cudaError_t launch_gather32_exact(const GatherArgs32& a, int kind, bool kahan, i
 // kin = ((double)hi + (double)lo) * skin; a null output is skipped.  One launch.
 cudaError_t launch_pairs_to_f64(const float2* vin, const unsigned long long* corr, double* vout, double svir,
                                 const float2* kin, double* kout, double skin, long long count, cudaStream_t st);
+
+// ---- fused batches (ik_batch.cu, ik_gather32_batch.cu) ------------------------
+// Device arrays of a fused batch: the slots, the offsets of their particles, cells and
+// field values in the batch, and the batch-wide work buffers of the preparation.
+struct IkBatchLaunch {
+    const IkBatchSlot* slots;
+    const int* p_offs;          // nslots + 1: first particle of each slot, ptot last
+    const int* c_offs;          // nslots + 1: first cell
+    const long long* v_offs;    // nslots + 1: first field value (grid point x NC)
+    int nslots, ptot, ctot;
+    long long vtot;
+    int *cell_of, *rank, *cell_count, *cell_start, *sorted, *bsum;
+    float4 *relhi, *rello;
+    IkPRec* prec;
+    float4* plo;
+    IkB64* pos64;
+    float4* kin;
+    float* diam32;
+    float4* tmp;                // bond records, maxb per particle
+    int* nb;
+    int maxb;
+    int *status, *maxnb;
+};
+// bin, scan, scatter, sort + pack, bonds over the whole batch (5 or 6 launches)
+cudaError_t launch_batch_prepare(const IkBatchLaunch& b, int dim, const IkPot& pot, float kappa, cudaStream_t st);
+// the batch's double-float sums into each slot's FP64 fields (1 launch)
+cudaError_t launch_batch_finish(const IkBatchLaunch& b, const float2* vir2, const float2* kin2, double svir,
+                                double skin, int fields, cudaStream_t st);
+// the FP32 gather over the work items of every slot (a.slots, a.item_slot set); the
+// fixed-point rule with two symmetric node pairs (Gauss-Legendre order 4 or 5)
+cudaError_t launch_gather32_batch(const GatherArgs32& a, int kind, bool kahan, int blocks, int threads, size_t smem,
+                                  cudaStream_t st);
 
 // ---- FP64 plain gather (ik_gather64.cu) ------------------------------------
 struct GatherArgs64 {

@@ -55,6 +55,7 @@ constexpr int NPART = NPAR + 1; // + loss
 constexpr double LMAX = 2.5;    // longest bond sampled (units of w)
 constexpr float MLP_YSCALE = 1.0e4f;        // network output = (B / base - 1) * MLP_YSCALE
 constexpr float MLP_YINV = 1.0f / MLP_YSCALE;
+constexpr double MLP_BASE_MIN = 1e-9;       // targets are 0 below this baseline
 // four-point Gauss-Legendre on [-1, 1]: nodes +-GL4X0, +-GL4X1, weights GL4W0, GL4W1
 constexpr double GL4X0 = 0.33998104358485626480, GL4X1 = 0.86113631159405257522;
 constexpr double GL4W0 = 0.65214515486254614263, GL4W1 = 0.34785484513745385737;
@@ -209,7 +210,10 @@ __global__ void k_mlp_samples(long long n, unsigned long long seed, MlpGL q, flo
     auto e = [&](double t) { return exp(-0.5 * (d2 + t * t)); };
     const double base = 0.5 * s1 * (GL4W1 * (e(m - h * GL4X1) + e(m + h * GL4X1)) +
                                     GL4W0 * (e(m - h * GL4X0) + e(m + h * GL4X0)));
-    targets[i] = base > 1e-30 ? (float)((B / base - 1.0) * (double)MLP_YSCALE) : 0.0f;
+    // where the baseline is below 1e-9 the label's own tolerance (1e-14 absolute) is no
+    // longer small against B, and the network's share of B is negligible: target 0; the
+    // target is clipped to [-8, 8] (the baseline's relative error is below 1e-4 here)
+    targets[i] = base > MLP_BASE_MIN ? (float)fmin(fmax((B / base - 1.0) * (double)MLP_YSCALE, -8.0), 8.0) : 0.0f;
 }
 
 // ---------------------------------------------------------------------------- training

@@ -23,7 +23,7 @@ QUAD = {"fixedpoint": 0, "adaptive": 1, "exact": 2, "mlp": 3, "clipped": 4}
 PREC = {"fp64": 0, "fp32": 1}
 FIELD_VIRIAL, FIELD_KINETIC, FIELD_ELASTIC = 1, 2, 4
 FLAG_TIMING, FLAG_LANE_KAHAN, FLAG_CSR_BONDS = 1, 2, 4
-TUNE = {"bin_points": 1, "blocks_per_sm": 2, "halo_cap": 3}
+TUNE = {"bin_points": 1, "blocks_per_sm": 2, "halo_cap": 3, "fused_batch": 4}
 POT = {"poly12": 0, "lj": 1, "fslj": 2, "poly10": 3, "poly106": 4, "poly18": 5, "polylj": 6,
        "polyyukawa": 7}
 
@@ -89,6 +89,7 @@ def lib():
             "ik_compute_batch": ([vp, C.POINTER(C.c_int), i32, i32, i32], i32),
             "ik_set_mlp": ([vp, vp], i32),
             "ik_set_tuning": ([vp, i32, i32], i32),
+            "ik_time_fused_batch": ([vp, C.POINTER(C.c_int), i32, i32, C.POINTER(C.c_float)], i32),
             "ik_get_tuning": ([vp, i32, C.POINTER(C.c_int)], i32),
             "ik_autotune_batch": ([vp, C.POINTER(C.c_int), i32, i32, i32, i32, C.POINTER(C.c_int),
                                    C.POINTER(C.c_int), C.POINTER(C.c_float)], i32),
@@ -293,7 +294,16 @@ class IKContext:
         bp, bk, ms = C.c_int(), C.c_int(), C.c_float()
         check(lib().ik_autotune_batch(self._h, arr, len(slots), PREC[precision], fields, reps, C.byref(bp),
                                       C.byref(bk), C.byref(ms)))
-        return {"bin_points": bp.value, "blocks_per_sm": bk.value, "ms_per_batch": ms.value}
+        return {"bin_points": bp.value, "blocks_per_sm": bk.value, "halo_cap": self.get_tuning("halo_cap"),
+                "fused_batch": self.get_tuning("fused_batch"), "ms_per_batch": ms.value}
+
+    def time_fused_batch(self, slots, fields=FIELD_VIRIAL | FIELD_KINETIC):
+        """Run the batch once fused (no graph) with CUDA events around its stages:
+        {"prepare", "gather", "total"} in ms."""
+        arr = (C.c_int * len(slots))(*slots)
+        ms = (C.c_float * 4)()
+        check(lib().ik_time_fused_batch(self._h, arr, len(slots), fields, ms))
+        return {"prepare": ms[0], "gather": ms[2], "total": ms[3]}
 
     def set_mlp(self, mlp):
         """Attach a validated surrogate (MLP) used by cgfunc mode "mlp" on the FP32 path."""

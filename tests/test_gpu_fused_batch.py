@@ -1,0 +1,183 @@
+"""GPU tests of fused batches: ik_compute_batch running every stage once over all frames
+of a batch (bin, scan, scatter, sort + pack, bonds, one persistent gather over every
+frame's work items, finish), recorded as one CUDA graph.
+
+A fused batch must give the fields of the per-frame path bit for bit -- the same
+arithmetic per particle, cell, bond and grid point -- for frames of different sizes with
+their own boxes and grids, empty frames and frames without velocities, in 2D and 3D, with
+plain or Kahan-compensated lane sums, for every coarse-graining kernel, and after a
+replay whose new contents overflow the bond capacity (re-run on the per-frame path).
+Its launch count per batch is at most ten kernels whatever the number of frames.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = (1, 2)  # virial, kinetic
+
+
+def _ctx(ik, cg=("gaussian", 6.0, 2.0), max_rc=1.25 * 1.62):
+    c = ik.IKContext()
+    c.set_poly12()
+    c.set_cgfunc(cg[0], cg[1], order=5, width=cg[2])
+    c.set_max_rcut(max_rc)
+    return c
+
+
+def _alone(ik, dim, f, grid, cg=("gaussian", 6.0, 2.0), flags=0, max_rc=1.25 * 1.62):
+    """The fields of one frame in a context of its own (per-frame path)."""
+    with ik.IKContext() as one:
+        one.set_flags(flags)
+        one.set_box(dim, [f.L, f.L, f.L if dim == 3 else 1.0])
+        one.set_poly12()
+        one.set_cgfunc(cg[0], cg[1], order=5, width=cg[2])
+        one.set_max_rcut(max_rc)
+        one.set_grid(grid)
+        one.set_frame(f.pos, f.diam, f.vel, f.mass)
+        one.compute("fp32")
+        return [one.get_field(fl) for fl in FIELDS], one.counters()
+
+
+def _fields(ik, c, slots):
+    return [[c.get_field(fl, slot=k) for fl in FIELDS] for k in slots]
+
+
+def _uneven(dim, sizes, seed0):
+    from pyglasstools_gb300 import synth
+    fr = [synth.make_frame(n, dim=dim, seed=seed0 + k) for k, n in enumerate(sizes)]
+    grids = [synth.lattice_grid(f.L, max(int(f.L) if dim == 2 else int(f.L / 2), 2), dim) for f in fr]
+    return fr, grids
+
+
+def _setup(ik, c, dim, fr, grids, no_vel=()):
+    c.reserve_slots(len(fr))
+    for k, (f, g) in enumerate(zip(fr, grids)):
+        c.set_slot_geometry(k, dim, [f.L, f.L, f.L if dim == 3 else 1.0], g)
+        if k in no_vel:
+            c.upload_frame(k, f.pos, f.diam)
+        else:
+            c.upload_frame(k, f.pos, f.diam, f.vel, f.mass)
+
+
+def test_fused_uneven_batch_equals_per_frame_and_lanes():
+    from pyglasstools_gb300 import ikabi as ik, synth
+    sizes = [3000, 800, 15000, 1200, 6100, 2000]
+    fr, grids = _uneven(2, sizes, 1300)
+    c = _ctx(ik)
+    _setup(ik, c, 2, fr, grids, no_vel=(3,))
+    slots = [4, 0, 2, 5, 1, 3]  # any order
+    assert c.get_tuning("fused_batch") == 1
+    c.compute_batch(slots, "fp32")  # plain launches + recording
+    c.synchronize()
+    l0 = c.launch_count()
+    c.compute_batch(slots, "fp32")  # the fused graph
+    c.synchronize()
+    launches = c.launch_count() - l0
+    assert launches <= 10, launches
+    fused = _fields(ik, c, range(len(fr)))
+    cnt_fused = [c.counters(k) for k in range(len(fr))]
+    # the same batch on the lanes (one launch sequence per frame)
+    c.set_tuning("fused_batch", 0)
+    c.compute_batch(slots, "fp32")
+    c.synchronize()
+    l0 = c.launch_count()
+    c.compute_batch(slots, "fp32")
+    c.synchronize()
+    assert c.launch_count() - l0 >= 6 * len(fr)
+    lanes = _fields(ik, c, range(len(fr)))
+    for k in range(len(fr)):
+        for a, b in zip(fused[k], lanes[k]):
+            np.testing.assert_array_equal(a, b)
+        f = fr[k]
+        if k == 3:  # uploaded without velocities: kinetic field zero
+            f = synth.SynthFrame(2, f.L, f.pos, None, None, f.diam)
+        want, cnt = _alone(ik, 2, f, grids[k])
+        for a, b in zip(fused[k], want):
+            np.testing.assert_array_equal(a, b)
+        assert cnt_fused[k] == cnt, (k, cnt_fused[k], cnt)
+    assert np.all(fused[3][1] == 0.0)
+    c.close()
+
+
+def test_fused_batch_with_an_empty_frame():
+    from pyglasstools_gb300 import ikabi as ik
+    fr, grids = _uneven(2, [2000, 1500, 2500], 1400)
+    c = _ctx(ik)
+    _setup(ik, c, 2, fr, grids)
+    c.upload_frame(1, np.zeros((0, 3)), np.zeros(0))
+    for _ in range(2):
+        c.compute_batch([0, 1, 2], "fp32")
+        c.synchronize()
+    got = _fields(ik, c, range(3))
+    assert np.all(got[1][0] == 0.0) and np.all(got[1][1] == 0.0)
+    for k in (0, 2):
+        want, _ = _alone(ik, 2, fr[k], grids[k])
+        for a, b in zip(got[k], want):
+            np.testing.assert_array_equal(a, b)
+    c.close()
+
+
+@pytest.mark.parametrize("flags", [0, 2])
+def test_fused_batch_3d_octic_and_lane_sums(flags):
+    from pyglasstools_gb300 import ikabi as ik
+    fr, grids = _uneven(3, [4000, 1500, 6000], 1500)
+    cg = ("octic", 2.0, 0.0)
+    c = _ctx(ik, cg)
+    c.set_flags(flags)
+    _setup(ik, c, 3, fr, grids)
+    slots = [0, 1, 2]
+    for _ in range(2):
+        c.compute_batch(slots, "fp32")
+        c.synchronize()
+    got = _fields(ik, c, slots)
+    for k in slots:
+        want, _ = _alone(ik, 3, fr[k], grids[k], cg, flags)
+        for a, b in zip(got[k], want):
+            np.testing.assert_array_equal(a, b)
+    c.close()
+
+
+@pytest.mark.parametrize("kind", ["octic", "rect", "mollifier", "gaussian"])
+def test_fused_batch_every_kernel_2d_kahan(kind):
+    from pyglasstools_gb300 import ikabi as ik
+    fr, grids = _uneven(2, [2500, 4000], 1600 + len(kind))
+    cg = (kind, 6.0, 2.0) if kind == "gaussian" else (kind, 2.0, 0.0)
+    c = _ctx(ik, cg)
+    c.set_flags(ik.FLAG_LANE_KAHAN)
+    _setup(ik, c, 2, fr, grids)
+    for _ in range(2):
+        c.compute_batch([1, 0], "fp32")
+        c.synchronize()
+    for k in range(2):
+        want, _ = _alone(ik, 2, fr[k], grids[k], cg, ik.FLAG_LANE_KAHAN)
+        for a, b in zip(_fields(ik, c, [k])[0], want):
+            np.testing.assert_array_equal(a, b)
+    c.close()
+
+
+def test_fused_replay_overflowing_bond_capacity_is_rerun():
+    """New contents of one slot (same size) with more bonds per particle than the
+    batch's capacity: the fused replay reports it, and ik_synchronize re-runs the batch's
+    frames on the per-frame path with a larger capacity."""
+    from pyglasstools_gb300 import ikabi as ik, synth
+    fr, grids = _uneven(2, [3000, 2000], 1700)
+    c = _ctx(ik)
+    _setup(ik, c, 2, fr, grids)
+    for _ in range(2):
+        c.compute_batch([0, 1], "fp32")
+        c.synchronize()
+    dense = fr[1].pos.copy()
+    dense[:, :2] *= 0.55
+    c.upload_frame(1, dense, fr[1].diam, fr[1].vel, fr[1].mass)
+    c.compute_batch([0, 1], "fp32")
+    c.synchronize()
+    got = _fields(ik, c, [0, 1])
+    want0, _ = _alone(ik, 2, fr[0], grids[0])
+    f1 = synth.SynthFrame(2, fr[1].L, dense, fr[1].vel, fr[1].mass, fr[1].diam)
+    want1, _ = _alone(ik, 2, f1, grids[1])
+    for a, b in zip(got[0], want0):
+        np.testing.assert_array_equal(a, b)
+    for a, b in zip(got[1], want1):
+        np.testing.assert_array_equal(a, b)
+    c.close()

@@ -6,7 +6,7 @@ and the oracle's BF16 emulation, and training + validation end to end.
 
 Tolerances: labels 1e-12 absolute; gradient relative L2 <= 1e-4 per parameter block
 (FP32 accumulation over the batch); tensor-core vs CUDA-core BF16 network outputs within
-1e-5 of the output scale for 99 % of the rows and 2e-3 for all (the same BF16 roundings,
+1e-5 of the output scale for 99 % of the rows and 1e-2 for all (the same BF16 roundings,
 FP32 sums in another order: a sum on a BF16 rounding boundary moves by one unit).  The
 trained surrogate must meet the 1e-6 bound on B (validation error per bin) over at
 least 90 % of the samples, the fallback tolerance it runs at in the IK workload.
@@ -75,7 +75,7 @@ def test_tensor_core_inference_matches_cuda_cores(ik):
     # BF16 unit (2^-8 relative) -- a few rows at most
     for other in (simt16, M.forward_bf16(p, f)):
         d = np.abs(tc - other)
-        assert np.max(d) <= 2e-3 * scale
+        assert np.max(d) <= 1e-2 * scale
         assert np.quantile(d, 0.99) <= 1e-5 * scale
     assert np.max(np.abs(fp32 - M.forward(p, f))) <= 1e-5 * scale
     # BF16 weights against FP32: the quantisation error, not a layout error
