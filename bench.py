@@ -296,7 +296,7 @@ def surrogate_leg(args, ctx, wl, F, stream, all_slots, v_plain):
     t0 = time.perf_counter()
     hist = mlp.train(nsamples=1 << 22, epochs=250, ctas=152, lr=2e-3, seed=5)
     train_s = time.perf_counter() - t0
-    v_used = mlp.validate(n=1 << 20, seed=98, tol=MLP_TOL)
+    v_used = mlp.validate(n=1 << 22, seed=98, tol=MLP_TOL)
     ctx.set_mlp(mlp)
 
     def timed_mode(mode):
@@ -322,6 +322,7 @@ def surrogate_leg(args, ctx, wl, F, stream, all_slots, v_plain):
 
     fps_net, launches, v_net = timed_mode("mlp")
     records = ctx.mlp_records(0)
+    fallbacks = ctx.mlp_fallbacks(0)
     triples = ctx.counters(0)[2]
     # the closed forms as comparators: on the same crossing bonds, and on every bond
     fps_clip, _, v_clip = timed_mode("clipped")
@@ -359,7 +360,7 @@ def surrogate_leg(args, ctx, wl, F, stream, all_slots, v_plain):
                "exact_closed_form_fp32": {"frames_per_s": fps_exact32, "what": "erf closed form on every bond"},
                "network_over_clipped_closed_form": fps_net / fps_clip},
            "rel_diff_vs_plain_fp64_gl5": rel(v_net, v_plain),
-           "records_slot0": records, "triples_slot0": triples,
+           "records_slot0": records, "fallback_records_slot0": fallbacks, "triples_slot0": triples,
            "tensor_flop_per_eval": 2 * (4 * 64 * 3 + 128 * 64 * 2)}
     mlp.close()
     return out

@@ -372,6 +372,10 @@ int ik_mlp_test_stall(ik_mlp* m, int on);
 /* Attach a validated surrogate to a context; used by ik_set_cgfunc(.., IK_QUAD_MLP, ..)
  * on the FP32 path.  The caller keeps the surrogate alive while attached. */
 int ik_set_mlp(ik_ctx* ctx, ik_mlp* m);
+/* Records of the slot's last computation in surrogate mode that kept their fixed-point
+ * value (their bin was not validated within the tolerance, or lies outside the table);
+ * ik_get_mlp_records gives all records. */
+int ik_get_mlp_fallbacks(ik_ctx* ctx, int slot, int64_t* out);
 
 #ifdef __cplusplus
 }

@@ -141,7 +141,7 @@ def base(feats):
     return 0.5 * s1 * np.sum(w[None, :] * np.exp(-0.5 * (d[:, None] ** 2 + t * t)), axis=1)
 
 
-BASE_MIN = 1e-9  # targets are 0 below this baseline (the labels' tolerance is 1e-14 absolute)
+BASE_MIN = 1e-6  # targets are 0 below this baseline (the labels' tolerance is 1e-14 absolute)
 
 
 def targets(feats, labels):

@@ -123,7 +123,7 @@ struct Slot {
     bool has_disp = false;
     DevBuf vir, kin, ela;
     int last_prec = -1, last_fields = 0;
-    DevBuf counters; // 4 x u64: bonds, pairs, triples, spare
+    DevBuf counters; // 5 x u64: bonds, pairs, triples, surrogate records, surrogate fallbacks
     cudaEvent_t done = nullptr; // completion of the slot's last computation (on its lane)
     bool done_recorded = false;
     cudaEvent_t d2h_done = nullptr; // completion of the slot's last field download
@@ -658,8 +658,8 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
     if (timing) CK(cudaEventRecord(c->ev[0], L.st));
     ENS(s.vir, sizeof(double) * NC * c->geo.G);
     ENS(s.kin, sizeof(double) * NC * c->geo.G);
-    ENS(s.counters, sizeof(unsigned long long) * 4);
-    CK(cudaMemsetAsync(s.counters.p, 0, sizeof(unsigned long long) * 4, L.st));
+    ENS(s.counters, sizeof(unsigned long long) * 5);
+    CK(cudaMemsetAsync(s.counters.p, 0, sizeof(unsigned long long) * 5, L.st));
     if (!(fields & IK_FIELD_KINETIC)) CK(cudaMemsetAsync(s.kin.p, 0, sizeof(double) * NC * c->geo.G, L.st));
     if (!(fields & IK_FIELD_VIRIAL)) CK(cudaMemsetAsync(s.vir.p, 0, sizeof(double) * NC * c->geo.G, L.st));
     nv.next("ik cells");
@@ -780,7 +780,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
             CK(launch_mlp_records(c->mlp, L.mlp_rec.as<float4>(), L.mlp_rid.as<int2>(),
                                   L.mlp_count.as<unsigned long long>(), c->mlp_cap, bonds,
                                   (float)to_w, (float)c->cg.width, NC, L.corr.as<unsigned long long>(),
-                                  c->status.as<int>(), c->sm_count * 4, L.st));
+                                  cnt + 4, c->status.as<int>(), c->sm_count * 4, L.st));
             c->launches += 1;
         }
         // FP64 finish: ((double)hi + (double)lo) * normalisation (0.5 of the GL map for the virial)
@@ -1014,7 +1014,7 @@ int fused_build(ik_ctx* c, const std::vector<int>& slots)
         const int64_t G = c->geo.G;
         ENS(s.vir, sizeof(double) * NC * std::max<int64_t>(G, 1));
         ENS(s.kin, sizeof(double) * NC * std::max<int64_t>(G, 1));
-        ENS(s.counters, sizeof(unsigned long long) * 4);
+        ENS(s.counters, sizeof(unsigned long long) * 5);
         IkBatchSlot& b = hs[(size_t)k];
         b.geo = gather_geo(c);
         b.geo.c_off = (int)Cc;
@@ -1035,8 +1035,14 @@ int fused_build(ik_ctx* c, const std::vector<int>& slots)
         po[(size_t)k] = (int)P;
         co[(size_t)k] = (int)Cc;
         vo[(size_t)k] = Gt * NC;
+        // one work item per bin: the frame's items split a bin so that a frame alone fills
+        // the GPU; a batch has enough bins, and a whole bin stages its halo once
         for (int j = 0; j < c->geo.nitems; ++j) {
             int4 it = c->geo.items_h[(size_t)j];
+            if (j > 0) {
+                const int4& pv = c->geo.items_h[(size_t)j - 1];
+                if (pv.x == it.x && pv.y == it.y && pv.z == it.z) continue;
+            }
             it.w += (int)Gt;
             items.push_back(it);
             islot.push_back(k);
@@ -2480,6 +2486,19 @@ int ik_get_mlp_records(ik_ctx* c, int slot, int64_t* out)
     unsigned long long h[4] = {0, 0, 0, 0};
     if (s.counters.p) CK(cudaMemcpy(h, s.counters.p, sizeof h, cudaMemcpyDeviceToHost));
     *out = (int64_t)h[3];
+    return IK_OK;
+}
+
+int ik_get_mlp_fallbacks(ik_ctx* c, int slot, int64_t* out)
+{
+    if (int r = check_ctx(c)) return r;
+    if (int r = slot_ok(c, slot)) return r;
+    if (!out) return fail(IK_ERR_ARG, "null output");
+    if (int r = ik_synchronize(c)) return r;
+    Slot& s = c->slots[(size_t)slot];
+    unsigned long long h[5] = {0, 0, 0, 0, 0};
+    if (s.counters.p && s.counters.bytes >= sizeof h) CK(cudaMemcpy(h, s.counters.p, sizeof h, cudaMemcpyDeviceToHost));
+    *out = (int64_t)h[4];
     return IK_OK;
 }
 

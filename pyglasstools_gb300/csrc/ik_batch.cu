@@ -55,8 +55,9 @@ __global__ void k_bin32_batch(const IkBatchSlot* __restrict__ S, const int* __re
                               int* __restrict__ cell_count, float4* __restrict__ relhi, float4* __restrict__ rello)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    // the slots' counters (bonds, pairs, triples, spare) start at zero; the later stages add
-    for (int k = i; k < 4 * nslots; k += gridDim.x * blockDim.x) S[k >> 2].geo.cnt[k & 3] = 0ull;
+    // the slots' counters (bonds, pairs, triples, surrogate records and fallbacks) start at
+    // zero; the later stages add
+    for (int k = i; k < 5 * nslots; k += gridDim.x * blockDim.x) S[k / 5].geo.cnt[k % 5] = 0ull;
     if (i >= ptot) return;
     const int s = ik_batch_slot(p_offs, nslots, i);
     const IkBatchSlot& sl = S[s];
@@ -135,7 +136,7 @@ __global__ void k_pairs_to_f64_batch(const IkBatchSlot* __restrict__ S, const lo
 cudaError_t launch_batch_prepare(const IkBatchLaunch& b, int dim, const IkPot& pot, float kappa, cudaStream_t st)
 {
     const int T = 256;
-    const int bin_threads = std::max(b.ptot, 4 * b.nslots);
+    const int bin_threads = std::max(b.ptot, 5 * b.nslots);
     k_bin32_batch<<<(bin_threads + T - 1) / T, T, 0, st>>>(b.slots, b.p_offs, b.nslots, b.ptot, b.cell_of, b.rank,
                                                            b.cell_count, b.relhi, b.rello);
     cudaError_t e = cudaGetLastError();

@@ -376,11 +376,17 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
     for (;;) {
         // work items: first this CTA's contiguous share (spatial neighbours, L1 reuse
         // across its warps), then a global counter over the remaining tail
+        // (fused batch: the global counter alone, so that the whole GPU works through the
+        // frames in order and a frame's particles and bonds are fetched into L2 once)
         int w = 0;
         if (lane == 0) {
-            const int per = (int)(((long long)a.nitems * 7 / 8) / gridDim.x);
-            const int k = atomicAdd(&s_next, 1);
-            w = k < per ? (int)blockIdx.x * per + k : per * (int)gridDim.x + atomicAdd(a.work_counter, 1);
+            if (BATCH) {
+                w = atomicAdd(a.work_counter, 1);
+            } else {
+                const int per = (int)(((long long)a.nitems * 7 / 8) / gridDim.x);
+                const int k = atomicAdd(&s_next, 1);
+                w = k < per ? (int)blockIdx.x * per + k : per * (int)gridDim.x + atomicAdd(a.work_counter, 1);
+            }
         }
         w = __shfl_sync(FULL, w, 0);
         if (w >= a.nitems) break;

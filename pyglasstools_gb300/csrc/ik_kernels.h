@@ -53,7 +53,7 @@ struct GatherGeo {
     int cull;              // stage only particles within R of the bin's box
     int c_off;             // fused batch: the slot's first cell in the batch's cell list (else 0)
     int p_off;             // fused batch: the slot's first particle in the batch (else 0)
-    unsigned long long* cnt; // fused batch: the slot's 4 counters (bonds, pairs, triples, spare)
+    unsigned long long* cnt; // fused batch: the slot's 5 counters (bonds, pairs, triples, records, fallbacks)
 };
 // A slot of a fused batch (ik_compute_batch with every stage batch-wide): its gather
 // geometry, inputs, outputs and extents in the batch's concatenated arrays.
@@ -208,10 +208,12 @@ cudaError_t launch_fma_probe(int blocks, int threads, int iters, float* out);
 struct ik_mlp;
 const unsigned char* ik_mlp_internal_blob(ik_mlp* m);   // deployed BF16 weights (null if none)
 const unsigned char* ik_mlp_internal_table(ik_mlp* m);  // per-bin use table (null if not validated)
-// records {M, mb, hh, B_fixed} + {grid index, bond index} -> fixed-point corrections (2^-32)
+// records {M, mb, hh, B_fixed} + {grid index, bond index} -> fixed-point corrections (2^-32);
+// fallbacks += records that kept their fixed-point value (bin not validated or outside the table)
 cudaError_t launch_mlp_records(ik_mlp* m, const float4* rec, const int2* rid, const unsigned long long* count,
                                long long capacity, const float4* bonds, float to_w, float w, int nc,
-                               unsigned long long* corr, int* status, int blocks, cudaStream_t st);
+                               unsigned long long* corr, unsigned long long* fallbacks, int* status, int blocks,
+                               cudaStream_t st);
 
 // ---- shared host helpers (ik_api.cu) -----------------------------------------
 void ik_internal_set_error(const char* msg);

@@ -55,7 +55,7 @@ constexpr int NPART = NPAR + 1; // + loss
 constexpr double LMAX = 2.5;    // longest bond sampled (units of w)
 constexpr float MLP_YSCALE = 1.0e4f;        // network output = (B / base - 1) * MLP_YSCALE
 constexpr float MLP_YINV = 1.0f / MLP_YSCALE;
-constexpr double MLP_BASE_MIN = 1e-9;       // targets are 0 below this baseline
+constexpr double MLP_BASE_MIN = 1e-6;       // targets are 0 below this baseline
 // four-point Gauss-Legendre on [-1, 1]: nodes +-GL4X0, +-GL4X1, weights GL4W0, GL4W1
 constexpr double GL4X0 = 0.33998104358485626480, GL4X1 = 0.86113631159405257522;
 constexpr double GL4W0 = 0.65214515486254614263, GL4W1 = 0.34785484513745385737;
@@ -210,8 +210,8 @@ __global__ void k_mlp_samples(long long n, unsigned long long seed, MlpGL q, flo
     auto e = [&](double t) { return exp(-0.5 * (d2 + t * t)); };
     const double base = 0.5 * s1 * (GL4W1 * (e(m - h * GL4X1) + e(m + h * GL4X1)) +
                                     GL4W0 * (e(m - h * GL4X0) + e(m + h * GL4X0)));
-    // where the baseline is below 1e-9 the label's own tolerance (1e-14 absolute) is no
-    // longer small against B, and the network's share of B is negligible: target 0; the
+    // where the baseline is below 1e-6 the label's own tolerance (1e-14 absolute) is no
+    // longer small against the network's share of B (below 1e-9 of B there): target 0; the
     // target is clipped to [-8, 8] (the baseline's relative error is below 1e-4 here)
     targets[i] = base > MLP_BASE_MIN ? (float)fmin(fmax((B / base - 1.0) * (double)MLP_YSCALE, -8.0), 8.0) : 0.0f;
 }
@@ -665,6 +665,7 @@ struct MlpRecArgs {
     float w;
     int nc;                           // 3 (2D) or 6 (3D) components
     unsigned long long* corr;         // fixed-point accumulators, G x nc
+    unsigned long long* fallbacks;    // += records that kept their fixed-point value
 };
 
 // Canonical surrogate coordinates of a record; returns the bin (or -1 outside the table).
@@ -849,12 +850,14 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
                 }
                 fence_before();
                 const float Bs = base * fmaf(y, MLP_YINV, 1.0f);
+                bool fell_back = false;
                 if (MODE == 0) {
                     if (valid) out[row] = raw ? y : Bs;
                 } else if (valid) {
                     // the gather's units: B integrates over [-1, 1] (twice the [0, 1] value)
                     const bool use = bin >= 0 && R.table[bin] != 0;
                     const float Bv = use ? 2.0f * Bs : bfix;
+                    fell_back = !use;
                     const float4 bd = __ldg(R.bonds + bond);
                     const float fx = bd.w * bd.x, fy = bd.w * bd.y;
                     auto add = [&](int c, float coef) {
@@ -872,6 +875,10 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
                         add(4, fx * bd.z);
                         add(5, fy * bd.z);
                     }
+                }
+                if (MODE == 1 && R.fallbacks) { // one atomic per warp
+                    const unsigned fb = __ballot_sync(0xffffffffu, fell_back);
+                    if ((t & 31) == 0 && fb) atomicAdd(R.fallbacks, (unsigned long long)__popc(fb));
                 }
             }
         }
@@ -1005,7 +1012,8 @@ const unsigned char* ik_mlp_internal_table(ik_mlp* m) { return m && m->validated
 
 cudaError_t launch_mlp_records(ik_mlp* m, const float4* rec, const int2* rid, const unsigned long long* count,
                                long long capacity, const float4* bonds, float to_w, float w, int nc,
-                               unsigned long long* corr, int* status, int blocks, cudaStream_t st)
+                               unsigned long long* corr, unsigned long long* fallbacks, int* status, int blocks,
+                               cudaStream_t st)
 {
     cudaError_t e = cudaFuncSetAttribute(k_mlp_infer_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          TC_SMEM_LAUNCH);
@@ -1021,6 +1029,7 @@ cudaError_t launch_mlp_records(ik_mlp* m, const float4* rec, const int2* rid, co
     R.w = w;
     R.nc = nc;
     R.corr = corr;
+    R.fallbacks = fallbacks;
     k_mlp_infer_tc<1><<<blocks, 128, TC_SMEM_LAUNCH, st>>>(m->blob.as<unsigned char>(), nullptr, 0, nullptr, R,
                                                             status, m->stall, 0);
     return cudaGetLastError();

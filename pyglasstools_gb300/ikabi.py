@@ -94,6 +94,7 @@ def lib():
             "ik_autotune_batch": ([vp, C.POINTER(C.c_int), i32, i32, i32, i32, C.POINTER(C.c_int),
                                    C.POINTER(C.c_int), C.POINTER(C.c_float)], i32),
             "ik_get_mlp_records": ([vp, i32, C.POINTER(C.c_int64)], i32),
+            "ik_get_mlp_fallbacks": ([vp, i32, C.POINTER(C.c_int64)], i32),
             "ik_mlp_create": ([C.POINTER(vp), i32], i32),
             "ik_mlp_destroy": ([vp], i32),
             "ik_mlp_num_params": ([], i32),
@@ -438,6 +439,12 @@ class IKContext:
     def mlp_records(self, slot=0):
         v = C.c_int64()
         check(lib().ik_get_mlp_records(self._h, slot, C.byref(v)))
+        return v.value
+
+    def mlp_fallbacks(self, slot=0):
+        """Surrogate records of the last computation that kept their fixed-point value."""
+        v = C.c_int64()
+        check(lib().ik_get_mlp_fallbacks(self._h, slot, C.byref(v)))
         return v.value
 
 
