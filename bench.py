@@ -72,6 +72,9 @@ def parse():
                          "so that the tensor-core kernel appears in the launch list")
     ap.add_argument("--profile", action="store_true",
                     help="only warm-up + timed steps (for ncu launch lists); prints a short JSON line")
+    ap.add_argument("--schedule", default="auto", choices=["auto", "fused", "lanes"],
+                    help="batch schedule of the headline: chosen by the autotuner (default), or fixed: fused "
+                         "(every stage once over the step's frames) or lanes (one launch sequence per frame)")
     ap.add_argument("--profile-precision", default="fp32", choices=["fp32", "fp64"],
                     help="with --profile: the path the steps run (fp64 = the plain FP64 gather)")
     return ap.parse_args()
@@ -467,6 +470,11 @@ def ours(args, wl, name):
     ctx.set_flags(lane_flags)
 
     all_slots = list(range(F))
+    tuning = None
+    if args.schedule == "auto":  # the autotuner: schedule, bin size, CTAs per SM, halo per warp
+        tuning = ctx.autotune_batch(all_slots, "fp32", reps=2)
+    else:
+        ctx.set_tuning("fused_batch", 1 if args.schedule == "fused" else 0)
 
     def step(prec="fp32", nfr=F):
         # one CUDA-graph replay per step for the whole batch of resident frames
@@ -697,6 +705,7 @@ def ours(args, wl, name):
            "rel_err_vs_fp64": {"virial": err_v, "kinetic": err_k},
            "lane_sums": lane_sums,
            "schedules": schedules,
+           "tuning": tuning if tuning is not None else {"schedule": args.schedule},
            "per_frame_gather": per_frame_gather,
            "interactions_per_s": (A / F if fused0 else A) * value}
     if fused0:
