@@ -558,10 +558,14 @@ def ours(args, wl, name):
     other_value, _ = timed_steps()
     ctx.set_flags(lane_flags)
     # ---- and the other batch schedule: fused (the default) or one launch sequence per frame
+    # (its CTAs per SM at their default: the tuned value belongs to the headline's schedule)
     fused0 = ctx.get_tuning("fused_batch")
+    bps0 = ctx.get_tuning("blocks_per_sm")
     ctx.set_tuning("fused_batch", 1 - fused0)
+    ctx.set_tuning("blocks_per_sm", 0)
     other_sched, other_launches = timed_steps()
     ctx.set_tuning("fused_batch", fused0)
+    ctx.set_tuning("blocks_per_sm", bps0)
     schedules = {"headline": "fused" if fused0 else "lanes",
                  "fused_frames_per_s": value / world if fused0 else other_sched,
                  "lanes_frames_per_s": other_sched if fused0 else value / world,
@@ -639,6 +643,9 @@ def ours(args, wl, name):
     err_v, err_k = relerr(v32, v64), relerr(k32, k64)
 
     # ---- roofline of the gather kernel (per-launch CUDA events around it)
+    # one frame's gather timed alone (two CTAs per SM, the default for a frame alone; in the
+    # lanes schedule the frames' gathers run side by side, one CTA per SM each)
+    ctx.set_tuning("blocks_per_sm", 0)
     ctx.set_flags(ikabi.FLAG_TIMING | lane_flags)
     gms, trip, stages = [], [], []
     for k in range(F):
@@ -649,24 +656,30 @@ def ours(args, wl, name):
         gms.append(t4[2])
         trip.append(ctx.counters(k)[2])
     ctx.set_flags(lane_flags)
+    ctx.set_tuning("blocks_per_sm", bps0)
     stage_ms = np.mean(np.array(stages), axis=0)
     g_ms = float(np.mean(gms))
     A = float(np.mean(trip))
     flop = FLOP_PER_TRIPLE[D] * A
     achieved = flop / (g_ms * 1e-3) / 1e12
-    per_frame_gather = {"kernel": "k_gather32<KAHAN=%d> (one frame per launch)" % (1 if lane_flags else 0),
+    per_frame_gather = {"kernel": "k_gather32<KAHAN=%d> (one frame per launch, timed alone)" % (1 if lane_flags else 0),
                         "achieved": achieved, "launch_ms": g_ms, "flop_per_launch": flop}
     roof_kernel = per_frame_gather["kernel"]
-    if fused0:  # the headline's gather: every frame of the step in one launch
-        tf_ = [ctx.time_fused_batch(all_slots) for _ in range(4)][1:]
-        g_ms = float(np.median([t["gather"] for t in tf_]))
-        A = float(sum(ctx.counters(k)[2] for k in range(F)))
-        flop = FLOP_PER_TRIPLE[D] * A
-        achieved = flop / (g_ms * 1e-3) / 1e12
-        roof_kernel = "k_gather32<KAHAN=%d, BATCH> (fused: the %d frames of a step in one launch)" % (
-            1 if lane_flags else 0, F)
-        stage_ms_fused = {"prepare": float(np.median([t["prepare"] for t in tf_])), "gather": g_ms,
-                          "note": "ms per step of %d frames, CUDA events, no graph" % F}
+    # the fused gather: every frame of the step in one launch (CTAs per SM at the fused default)
+    ctx.set_tuning("blocks_per_sm", 0)
+    tf_ = [ctx.time_fused_batch(all_slots) for _ in range(4)][1:]
+    ctx.set_tuning("blocks_per_sm", bps0)
+    fg_ms = float(np.median([t["gather"] for t in tf_]))
+    fA = float(sum(ctx.counters(k)[2] for k in range(F)))
+    f_flop = FLOP_PER_TRIPLE[D] * fA
+    fused_gather = {"kernel": "k_gather32<KAHAN=%d, BATCH> (fused: the %d frames of a step in one launch)" % (
+                        1 if lane_flags else 0, F),
+                    "achieved": f_flop / (fg_ms * 1e-3) / 1e12, "launch_ms": fg_ms, "flop_per_launch": f_flop}
+    stage_ms_fused = {"prepare": float(np.median([t["prepare"] for t in tf_])), "gather": fg_ms,
+                      "note": "ms per step of %d frames, CUDA events, no graph" % F}
+    if fused0:  # the headline's gather
+        g_ms, A, flop, achieved = fg_ms, fA, f_flop, fused_gather["achieved"]
+        roof_kernel = fused_gather["kernel"]
     peak = ikabi.measure_fp32_peak(local)
     traffic = None
     tf = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
@@ -707,9 +720,10 @@ def ours(args, wl, name):
            "schedules": schedules,
            "tuning": tuning if tuning is not None else {"schedule": args.schedule},
            "per_frame_gather": per_frame_gather,
+           "fused_gather": fused_gather,
+           "stage_ms_fused": stage_ms_fused,
            "interactions_per_s": (A / F if fused0 else A) * value}
     if fused0:
-        out["stage_ms_fused"] = stage_ms_fused
         if traffic is not None:  # the capture is of one frame's gather: scaled to the step's frames
             out["roofline"]["traffic"] = traffic * F
             out["roofline"]["traffic_note"] = "ncu DRAM bytes of one frame's gather x %d frames" % F

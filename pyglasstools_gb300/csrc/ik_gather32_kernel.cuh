@@ -35,6 +35,7 @@
 #include "ik_kernels.h"
 
 #define FULL 0xffffffffu
+#define IK_BATCH_ROUND 16 // fused batch: consecutive work items a CTA takes per round
 
 __device__ __forceinline__ float ik_ex2(float x)
 {
@@ -376,12 +377,19 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
     for (;;) {
         // work items: first this CTA's contiguous share (spatial neighbours, L1 reuse
         // across its warps), then a global counter over the remaining tail
-        // (fused batch: the global counter alone, so that the whole GPU works through the
-        // frames in order and a frame's particles and bonds are fetched into L2 once)
+        // (fused batch: rounds of IK_BATCH_ROUND consecutive items per CTA, CTA after CTA,
+        // so that the whole GPU works through the frames in order -- a frame's particles
+        // and bonds are fetched into L2 once -- while a CTA's warps share their items'
+        // halos in L1; the last eighth from the global counter)
         int w = 0;
         if (lane == 0) {
             if (BATCH) {
-                w = atomicAdd(a.work_counter, 1);
+                const long long span = (long long)gridDim.x * IK_BATCH_ROUND;
+                const long long nstatic = ((long long)a.nitems * 7 / 8) / span * span;
+                const int k = atomicAdd(&s_next, 1);
+                const long long ws = (long long)(k / IK_BATCH_ROUND) * span +
+                                     (long long)blockIdx.x * IK_BATCH_ROUND + k % IK_BATCH_ROUND;
+                w = ws < nstatic ? (int)ws : (int)nstatic + atomicAdd(a.work_counter, 1);
             } else {
                 const int per = (int)(((long long)a.nitems * 7 / 8) / gridDim.x);
                 const int k = atomicAdd(&s_next, 1);

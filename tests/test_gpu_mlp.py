@@ -82,8 +82,9 @@ def test_tensor_core_inference_matches_cuda_cores(ik):
     assert np.max(np.abs(fp32 - M.forward(p, f))) <= 1e-5 * scale
     # BF16 weights against FP32: the quantisation error, not a layout error
     assert np.max(np.abs(tc - fp32)) <= 0.02 * scale
-    # B from y: base (1 + y / 1e4), the base by ex2.approx in the kernel
-    np.testing.assert_allclose(b_tc, M.value(f, tc.astype(np.float64)), rtol=2e-6, atol=1e-12)
+    # B from y: base (1 + y / 1e4), the base in FP32 with ex2.approx in the kernel (the
+    # clipped fraction (t_c - a) / (b - a) loses bits when a lies near t_c: absolute 1e-8)
+    np.testing.assert_allclose(b_tc, M.value(f, tc.astype(np.float64)), rtol=2e-6, atol=1e-8)
 
 
 def _gl_bond(f, n=5):
