@@ -12,7 +12,7 @@
 //   launch_scan         cell starts over the batch's concatenated cell counts
 //   k_scatter           particle ids to cell order
 //   k_sort_pack32_batch per cell: sorted ids, packed records
-//   k_bonds32t_batch    per cell (one warp): force-active bonds (records at a fixed stride)
+//   k_bonds32t_batch    per particle: force-active bonds (records at a fixed stride)
 //   k_gather32 (BATCH)  per work item of every frame: the stress field
 //   k_pairs_to_f64_batch double-float sums -> each slot's FP64 fields
 // Replaces, for a list of frames, the per-frame loop of IrvingKirkwood::compute over
@@ -85,7 +85,7 @@ __global__ void k_sort_pack32_batch(const IkBatchSlot* __restrict__ S, const int
 
 template <int DIM, int KIND>
 __global__ void __launch_bounds__(128) k_bonds32t_batch(const IkBatchSlot* __restrict__ S,
-                                                        const int* __restrict__ c_offs, int nslots, int ctot,
+                                                        const int* __restrict__ p_offs, int nslots, int ptot,
                                                         IkPot pot, float kappa, const IkPRec* __restrict__ prec,
                                                         const float* __restrict__ diam32,
                                                         const int* __restrict__ cell_start,
@@ -94,19 +94,20 @@ __global__ void __launch_bounds__(128) k_bonds32t_batch(const IkBatchSlot* __res
                                                         int maxb, int* __restrict__ nb, int* __restrict__ status,
                                                         int* __restrict__ maxnb)
 {
-    const int c = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5); // one warp per cell
-    const int lane = threadIdx.x & 31;
-    if (c >= ctot) return; // warp-uniform
-    const int s = ik_batch_slot(c_offs, nslots, c);
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= ptot) return;
+    const int s = ik_batch_slot(p_offs, nslots, p);
     const IkBatchSlot& sl = S[s];
     const int* cs = cell_start + sl.geo.c_off;
-    const int cl = c - sl.geo.c_off;
-    const int tot = sl.allax ? ik_bonds32_cell<DIM, KIND, true>(sl.geo.g, pot, kappa, cl, lane, prec, diam32, cs, plo,
-                                                                 pos64, tmp, maxb, nb, status, maxnb)
-                             : ik_bonds32_cell<DIM, KIND, false>(sl.geo.g, pot, kappa, cl, lane, prec, diam32, cs,
-                                                                  plo, pos64, tmp, maxb, nb, status, maxnb);
-    // force-active directed bonds of the slot: one atomic per cell
-    if (lane == 0 && tot) atomicAdd(&sl.geo.cnt[0], (unsigned long long)tot);
+    const int cnt = sl.allax ? ik_bonds32_particle<DIM, KIND, true>(sl.geo.g, pot, kappa, p, prec, diam32, cs, plo,
+                                                                    pos64, tmp, maxb, nb, status, maxnb)
+                             : ik_bonds32_particle<DIM, KIND, false>(sl.geo.g, pot, kappa, p, prec, diam32, cs, plo,
+                                                                     pos64, tmp, maxb, nb, status, maxnb);
+    // force-active directed bonds per slot: one atomic per slot present in the warp
+    const unsigned act = __activemask();
+    const unsigned grp = __match_any_sync(act, s);
+    const int tot = __reduce_add_sync(grp, cnt);
+    if ((int)(threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&sl.geo.cnt[0], (unsigned long long)tot);
 }
 
 // out = ((double)hi + (double)lo) * scale into the slot's field, as k_pairs_to_f64;
@@ -152,9 +153,9 @@ cudaError_t launch_batch_prepare(const IkBatchLaunch& b, int dim, const IkPot& p
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     if (b.ptot > 0) {
-        const int blocks = (int)(((long long)b.ctot * 32 + 127) / 128); // one warp per cell
+        const int blocks = (b.ptot + 127) / 128;
         auto go = [&](auto kernel) {
-            kernel<<<blocks, 128, 0, st>>>(b.slots, b.c_offs, b.nslots, b.ctot, pot, kappa, b.prec, b.diam32,
+            kernel<<<blocks, 128, 0, st>>>(b.slots, b.p_offs, b.nslots, b.ptot, pot, kappa, b.prec, b.diam32,
                                            b.cell_start, b.plo, b.pos64, b.tmp, b.maxb, b.nb, b.status, b.maxnb);
         };
 #define IK_BONDS32B_KIND(K)                                                   \

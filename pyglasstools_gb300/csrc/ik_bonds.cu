@@ -30,9 +30,9 @@ __global__ void k_bin32(const double* __restrict__ pos, int n, IkGeom g, int* __
 }
 
 // ---------------------------------------------------------------------------
-// Force-active bonds of a frame, one warp per cell (ik_bonds32_cell).
+// Force-active bonds of a frame, one thread per particle (ik_bonds32_particle).
 template <int DIM, int KIND, bool ALLAX>
-__global__ void __launch_bounds__(128) k_bonds32t(IkGeom g, IkPot pot, float kappa,
+__global__ void __launch_bounds__(128) k_bonds32t(IkGeom g, IkPot pot, float kappa, int n,
                                                   const IkPRec* __restrict__ prec,
                                                   const float* __restrict__ diam32,
                                                   const int* __restrict__ cell_start,
@@ -41,12 +41,15 @@ __global__ void __launch_bounds__(128) k_bonds32t(IkGeom g, IkPot pot, float kap
                                                   int maxb, int* __restrict__ nb, int* __restrict__ status,
                                                   int* __restrict__ maxnb, unsigned long long* nbond_total)
 {
-    const int c = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-    const int lane = threadIdx.x & 31;
-    if (c >= g.ncell) return; // warp-uniform
-    const int tot = ik_bonds32_cell<DIM, KIND, ALLAX>(g, pot, kappa, c, lane, prec, diam32, cell_start, plo, pos64,
-                                                      tmp, maxb, nb, status, maxnb);
-    if (nbond_total && lane == 0 && tot) atomicAdd(nbond_total, (unsigned long long)tot);
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int cnt = ik_bonds32_particle<DIM, KIND, ALLAX>(g, pot, kappa, p, prec, diam32, cell_start, plo, pos64,
+                                                          tmp, maxb, nb, status, maxnb);
+    if (nbond_total) { // force-active directed bonds of the frame (one atomic per warp)
+        const unsigned act = __activemask();
+        const int tot = __reduce_add_sync(act, cnt);
+        if ((threadIdx.x & 31) == __ffs(act) - 1) atomicAdd(nbond_total, (unsigned long long)tot);
+    }
 }
 
 // Compact the fixed-stride records into CSR order (boff = exclusive scan of nb); the
@@ -192,10 +195,10 @@ cudaError_t launch_bonds32(int dim, IkGeom g, IkPot pot, float kappa, int n, con
                             unsigned long long* nbond_total, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
-    const int threads = 128; // four cells per CTA, one warp each
-    const int blocks = (int)(((long long)g.ncell * 32 + threads - 1) / threads);
+    const int threads = 128;
+    const int blocks = (n + threads - 1) / threads;
     auto go = [&](auto kernel) {
-        kernel<<<blocks, threads, 0, st>>>(g, pot, kappa, prec, diam32, cell_start, plo, pos64, tmp, maxb, nb,
+        kernel<<<blocks, threads, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, plo, pos64, tmp, maxb, nb,
                                            status, maxnb, nbond_total);
     };
     bool allax = false;

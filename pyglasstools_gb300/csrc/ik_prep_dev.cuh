@@ -1,7 +1,7 @@
 // ik_prep_dev.cuh -- device functions of the FP32 path's per-frame preparation, shared
 // by the per-frame kernels (ik_bonds.cu) and the batch-wide ones (ik_batch.cu): the
 // double-float cell-relative position of a particle, the per-cell sort and pack, the
-// FP32 pair forces and the force-active bonds of the particles of one cell.
+// FP32 pair forces and the force-active bonds of one particle.
 #pragma once
 #include "ik_kernels.h"
 
@@ -183,30 +183,21 @@ __device__ __forceinline__ bool ik_select64_shift(const IkGeom& g, const IkPot& 
 // f' * hb (x) hb = 0.5 * forceDivR * r_ij (x) r_ij.  Written at a fixed stride of
 // `maxb` records per particle in candidate order (stencil cell with x fastest, then
 // ascending sorted index): deterministic.  ALLAX: some axis has fewer than three cells.
-// The force-active bonds of the particles of cell c, one warp: for each cell of the 3^d
-// stencil (x fastest, then y, z) the lanes take the (candidate q, particle p) pairs with p
-// fastest, 32 at a time, so that a particle's bonds come in the order of a loop over the
-// stencil and then over ascending q -- the deterministic order of the records.  Each pair:
-// an FP32 screen from the cell-relative positions; survivors re-measured from the
-// double-float positions (TwoSum), so that r_ij carries only its final FP32 rounding; pairs
-// within 2e-5 of a cut-off re-decided by the FP64 rule; the FP32 force of the model.  (On
-// axes with fewer than three cells the stencil is not the minimum image; those pairs are
-// re-measured in FP64.)  Records {hb = kappa r_ij / 2, f' = 2 forceDivR / kappa^2}, so that
-// f' hb (x) hb = 0.5 forceDivR r_ij (x) r_ij, at a fixed stride of maxb per particle; nb
-// holds the running counts (only this warp writes them), then min(count, maxb).
-// cell_start is the frame's cell list (indices into prec / plo / pos64 / tmp / nb, which
-// may be a batch's).  Returns the cell's force-active bonds (every lane).
+// The bonds of particle p (cell order); cell_start is the frame's cell list (indices
+// into prec / plo / pos64 / tmp / nb, which may be a batch's); returns the number of
+// force-active bonds (those beyond maxb are counted, not stored).
 template <int DIM, int KIND, bool ALLAX>
-__device__ __forceinline__ int ik_bonds32_cell(const IkGeom& g, const IkPot& pot, float kappa, int c, int lane,
-                                               const IkPRec* __restrict__ prec, const float* __restrict__ diam32,
-                                               const int* __restrict__ cell_start, const float4* __restrict__ plo,
-                                               const IkB64* __restrict__ pos64, float4* __restrict__ tmp, int maxb,
-                                               int* __restrict__ nb, int* __restrict__ status,
-                                               int* __restrict__ maxnb)
+__device__ __forceinline__ int ik_bonds32_particle(const IkGeom& g, const IkPot& pot, float kappa, int p,
+                                                   const IkPRec* __restrict__ prec,
+                                                   const float* __restrict__ diam32,
+                                                   const int* __restrict__ cell_start,
+                                                   const float4* __restrict__ plo,
+                                                   const IkB64* __restrict__ pos64, float4* __restrict__ tmp,
+                                                   int maxb, int* __restrict__ nb, int* __restrict__ status,
+                                                   int* __restrict__ maxnb)
 {
-    const unsigned FULLM = 0xffffffffu;
-    const int ps = cell_start[c], np = cell_start[c + 1] - ps;
-    if (np <= 0) return 0;
+    const IkPRec me = prec[p];
+    const int c = me.cell;
     const int home[3] = {c % g.nc[0], (c / g.nc[0]) % g.nc[1], c / (g.nc[0] * g.nc[1])};
     int lo[3], len[3];
 #pragma unroll
@@ -222,95 +213,81 @@ __device__ __forceinline__ int ik_bonds32_cell(const IkGeom& g, const IkPot& pot
     const IkPotF pf = ik_potf(pot);
     const float rc2 = pf.rc2, mr2 = (float)pot.max_rcut_sq, eps = pf.eps_s;
     const float screen = 1.0f + 1e-4f;
+    const float di = diam32[p];
+    const float4 mlo = plo[p];
     const float hk = 0.5f * kappa, fk = 2.0f / (kappa * kappa);
-    for (int k = lane; k < np; k += 32) nb[ps + k] = 0;
-    __syncwarp();
-    const int ns = len[0] * len[1] * len[2];
-    for (int st = 0; st < ns; ++st) { // warp-uniform
-        const int ix = st % len[0], iy = (st / len[0]) % len[1], iz = st / (len[0] * len[1]);
-        const int ux = lo[0] + ix, uy = lo[1] + iy, uz = lo[2] + iz;
-        const int wx = ik_wrap(ux, g.nc[0]), wy = ik_wrap(uy, g.nc[1]), wz = DIM == 3 ? ik_wrap(uz, g.nc[2]) : 0;
-        const float kx = (float)(ux - home[0]), ky = (float)(uy - home[1]), kz = (float)(uz - home[2]);
-        const float ox = kx * g.cwhi[0], olx = kx * g.cwlo[0];
-        const float oy = ky * g.cwhi[1], oly = ky * g.cwlo[1];
+    float4* out = tmp + (size_t)p * maxb;
+    int cnt = 0;
+    for (int iz = 0; iz < len[2]; ++iz) {
+        const int uz = lo[2] + iz;
+        const int wz = DIM == 3 ? ik_wrap(uz, g.nc[2]) : 0;
+        const float kz = (float)(uz - home[2]);
         const float oz = DIM == 3 ? kz * g.cwhi[2] : 0.f, olz = DIM == 3 ? kz * g.cwlo[2] : 0.f;
-        const int cell = (wz * g.nc[1] + wy) * g.nc[0] + wx;
-        const int qs = cell_start[cell], total = (cell_start[cell + 1] - qs) * np;
-        for (int base = 0; base < total; base += 32) {
-            const int idx = base + lane;
-            const bool valid = idx < total;
-            const int qo = valid ? idx / np : 0, po = valid ? idx - qo * np : 0;
-            const int p = ps + po, q = qs + qo;
-            bool act = false;
-            float4 rec = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (valid && q != p) {
-                const IkPRec me = prec[p], o = prec[q];
-                float bx = ox + (o.x - me.x), by = oy + (o.y - me.y), bz = DIM == 3 ? oz + (o.z - me.z) : 0.f;
-                if (allx) bx -= L0 * rintf(bx / L0);
-                if (ally) by -= L1 * rintf(by / L1);
-                if (allz) bz -= L2 * rintf(bz / L2);
-                float r2 = bx * bx + by * by + bz * bz;
-                if (r2 < mr2 * screen) {
-                    const float di = diam32[p], dj = diam32[q];
+        for (int iy = 0; iy < len[1]; ++iy) {
+            const int uy = lo[1] + iy;
+            const int wy = ik_wrap(uy, g.nc[1]);
+            const float ky = (float)(uy - home[1]);
+            const float oy = ky * g.cwhi[1], oly = ky * g.cwlo[1];
+            for (int ix = 0; ix < len[0]; ++ix) {
+                const int ux = lo[0] + ix;
+                const int wx = ik_wrap(ux, g.nc[0]);
+                const float kx = (float)(ux - home[0]);
+                const float ox = kx * g.cwhi[0], olx = kx * g.cwlo[0];
+                const int cell = (wz * g.nc[1] + wy) * g.nc[0] + wx;
+                const int qe = cell_start[cell + 1];
+                for (int q = cell_start[cell]; q < qe; ++q) {
+                    if (q == p) continue;
+                    const IkPRec o = prec[q];
+                    float bx = ox + (o.x - me.x), by = oy + (o.y - me.y), bz = DIM == 3 ? oz + (o.z - me.z) : 0.f;
+                    if (allx) bx -= L0 * rintf(bx / L0);
+                    if (ally) by -= L1 * rintf(by / L1);
+                    if (allz) bz -= L2 * rintf(bz / L2);
+                    float r2 = bx * bx + by * by + bz * bz;
+                    if (!(r2 < mr2 * screen)) continue;
+                    const float dj = diam32[q];
                     const float sig = 0.5f * (di + dj) * (1.f - eps * fabsf(di - dj));
                     const float s2 = sig * sig;
-                    if (r2 < rc2 * s2 * screen) {
-                        if (!(allx || ally || allz)) {
-                            const float4 lq = plo[q], mlo = plo[p];
-                            bx = ik_df_diff(ox, olx, o.x, lq.x, me.x, mlo.x);
-                            by = ik_df_diff(oy, oly, o.y, lq.y, me.y, mlo.y);
-                            if (DIM == 3) bz = ik_df_diff(oz, olz, o.z, lq.z, me.z, mlo.z);
-                        } else {
-                            const IkB64 pi = pos64[p], pj = pos64[q];
-                            double dx = pj.x - pi.x, dy = pj.y - pi.y;
-                            dx = fma(-g.L[0], rint(dx * g.invL[0]), dx);
-                            dy = fma(-g.L[1], rint(dy * g.invL[1]), dy);
-                            bx = (float)dx;
-                            by = (float)dy;
-                            if (DIM == 3) {
-                                double dz = pj.z - pi.z;
-                                dz = fma(-g.L[2], rint(dz * g.invL[2]), dz);
-                                bz = (float)dz;
-                            }
+                    if (!(r2 < rc2 * s2 * screen)) continue;
+                    if (!(allx || ally || allz)) {
+                        const float4 lq = plo[q];
+                        bx = ik_df_diff(ox, olx, o.x, lq.x, me.x, mlo.x);
+                        by = ik_df_diff(oy, oly, o.y, lq.y, me.y, mlo.y);
+                        if (DIM == 3) bz = ik_df_diff(oz, olz, o.z, lq.z, me.z, mlo.z);
+                    } else {
+                        const IkB64 pi = pos64[p], pj = pos64[q];
+                        double dx = pj.x - pi.x, dy = pj.y - pi.y;
+                        dx = fma(-g.L[0], rint(dx * g.invL[0]), dx);
+                        dy = fma(-g.L[1], rint(dy * g.invL[1]), dy);
+                        bx = (float)dx;
+                        by = (float)dy;
+                        if (DIM == 3) {
+                            double dz = pj.z - pi.z;
+                            dz = fma(-g.L[2], rint(dz * g.invL[2]), dz);
+                            bz = (float)dz;
                         }
-                        r2 = bx * bx + by * by + bz * bz;
-                        const float rt = rc2 * s2;
-                        act = r2 < mr2 && r2 < rt;
-                        if (fabsf(r2 - rt) <= 2e-5f * rt || fabsf(r2 - mr2) <= 2e-5f * mr2) { // at a cut-off: FP64
-                            if (ALLAX) act = ik_select64(g, pot, pos64[p], pos64[q]);
-                            else act = ik_select64_shift(g, pot, pos64[p], pos64[q], (ux > wx) - (ux < wx),
-                                                         (uy > wy) - (uy < wy),
-                                                         DIM == 3 ? (uz > wz) - (uz < wz) : 0);
-                        }
-                        if (act) rec = make_float4(hk * bx, hk * by, hk * bz, fk * ik_force32<KIND>(pf, r2, s2));
+                    }
+                    r2 = bx * bx + by * by + bz * bz;
+                    const float rt = rc2 * s2;
+                    bool act = r2 < mr2 && r2 < rt;
+                    if (fabsf(r2 - rt) <= 2e-5f * rt || fabsf(r2 - mr2) <= 2e-5f * mr2) { // at a cut-off: FP64
+                        if (ALLAX) act = ik_select64(g, pot, pos64[p], pos64[q]);
+                        else act = ik_select64_shift(g, pot, pos64[p], pos64[q], (ux > wx) - (ux < wx),
+                                                     (uy > wy) - (uy < wy), DIM == 3 ? (uz > wz) - (uz < wz) : 0);
+                    }
+                    if (act) {
+                        const float f = ik_force32<KIND>(pf, r2, s2);
+                        if (cnt < maxb) out[cnt] = make_float4(hk * bx, hk * by, hk * bz, fk * f);
+                        ++cnt;
                     }
                 }
             }
-            // the bond's place in particle p's list: its running count plus the active
-            // lanes of the same particle below this lane
-            const unsigned actm = __ballot_sync(FULLM, act);
-            const unsigned same = __match_any_sync(FULLM, valid ? po : -1 - lane);
-            const int run = valid ? nb[p] : 0;
-            if (act) {
-                const int k = run + __popc(same & actm & ((1u << lane) - 1u));
-                if (k < maxb) tmp[(size_t)p * maxb + k] = rec;
-            }
-            __syncwarp();
-            if (valid && lane == __ffs(same) - 1) nb[p] = run + __popc(same & actm);
-            __syncwarp();
         }
     }
-    int tot = 0;
-    for (int k = lane; k < np; k += 32) {
-        const int cnt = nb[ps + k];
-        tot += cnt;
-        if (cnt > maxb) { // rare: grow the capacity and recompute (host side)
-            nb[ps + k] = maxb;
-            atomicOr(status, IK_ST_BOND_OVERFLOW);
-            atomicMax(maxnb, cnt);
-        }
+    nb[p] = cnt < maxb ? cnt : maxb;
+    if (cnt > maxb) { // rare: grow the capacity and recompute (host side)
+        atomicOr(status, IK_ST_BOND_OVERFLOW);
+        atomicMax(maxnb, cnt);
     }
-    return __reduce_add_sync(FULLM, tot);
+    return cnt;
 }
-
 
