@@ -683,7 +683,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         ENS(L.pos64, sizeof(IkB64) * std::max(n, 1));
         ENS(L.plo, sizeof(float4) * std::max(n, 1));
         // per-cell sort + pack in one launch
-        CK(launch_sort_pack32(g, L.cell_start.as<int>(), L.sorted.as<int>(), L.relhi.as<float4>(),
+        CK(launch_sort_pack32(g, L.cell_start.as<int>(), L.sorted.as<int>(), L.cell_of.as<int>(), L.relhi.as<float4>(),
                               L.rello.as<float4>(), s.pos.as<double>(), s.has_vel ? s.vel.as<double>() : nullptr,
                               s.has_mass ? s.mass.as<double>() : nullptr, s.diam.as<double>(), L.prec.as<IkPRec>(),
                               L.plo.as<float4>(), L.pos64.as<IkB64>(), L.kin.as<float4>(), L.diam32.as<float>(),

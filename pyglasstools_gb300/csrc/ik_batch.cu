@@ -69,18 +69,29 @@ __global__ void k_bin32_batch(const IkBatchSlot* __restrict__ S, const int* __re
     rello[i] = rl;
 }
 
-__global__ void k_sort_pack32_batch(const IkBatchSlot* __restrict__ S, const int* __restrict__ c_offs, int nslots,
-                                    int ctot, const int* __restrict__ cell_start, int* __restrict__ sorted,
-                                    const float4* __restrict__ relhi, const float4* __restrict__ rello,
-                                    IkPRec* __restrict__ prec, float4* __restrict__ plo, IkB64* __restrict__ pos64,
-                                    float4* __restrict__ kin, float* __restrict__ diam32)
+// As k_cell_sort_pack32 over the batch's cells: a CTA sorts its 128 cells, then packs
+// their particles (cell_of holds batch cell indices; a particle's frame is found by a
+// search of the particle offsets).
+__global__ void __launch_bounds__(128) k_sort_pack32_batch(const IkBatchSlot* __restrict__ S,
+                                                           const int* __restrict__ p_offs, int nslots, int ctot,
+                                                           const int* __restrict__ cell_start,
+                                                           int* __restrict__ sorted, const int* __restrict__ cell_of,
+                                                           const float4* __restrict__ relhi,
+                                                           const float4* __restrict__ rello,
+                                                           IkPRec* __restrict__ prec, float4* __restrict__ plo,
+                                                           IkB64* __restrict__ pos64, float4* __restrict__ kin,
+                                                           float* __restrict__ diam32)
 {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ctot) return;
-    const int s = ik_batch_slot(c_offs, nslots, c);
-    const IkBatchSlot& sl = S[s];
-    ik_sort_pack_cell(sl.geo.g.dim, c - sl.geo.c_off, cell_start[c], cell_start[c + 1], sl.geo.p_off, sorted, relhi,
-                      rello, sl.pos, sl.vel, sl.mass, sl.diam, prec, plo, pos64, kin, diam32);
+    const int c0 = blockIdx.x * blockDim.x, c = c0 + threadIdx.x;
+    if (c < ctot) ik_sort_cell(cell_start[c], cell_start[c + 1], sorted);
+    __syncthreads();
+    const int pe = cell_start[min(c0 + (int)blockDim.x, ctot)];
+    for (int p = cell_start[c0] + threadIdx.x; p < pe; p += blockDim.x) {
+        const int ig = sorted[p];
+        const IkBatchSlot& sl = S[ik_batch_slot(p_offs, nslots, ig)];
+        ik_pack_one(sl.geo.g.dim, cell_of[ig] - sl.geo.c_off, p, ig, sl.geo.p_off, relhi, rello, sl.pos, sl.vel,
+                    sl.mass, sl.diam, prec, plo, pos64, kin, diam32);
+    }
 }
 
 template <int DIM, int KIND>
@@ -147,9 +158,9 @@ cudaError_t launch_batch_prepare(const IkBatchLaunch& b, int dim, const IkPot& p
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     if (b.ctot > 0) {
-        k_sort_pack32_batch<<<(b.ctot + 127) / 128, 128, 0, st>>>(b.slots, b.c_offs, b.nslots, b.ctot, b.cell_start,
-                                                                  b.sorted, b.relhi, b.rello, b.prec, b.plo, b.pos64,
-                                                                  b.kin, b.diam32);
+        k_sort_pack32_batch<<<(b.ctot + 127) / 128, 128, 0, st>>>(b.slots, b.p_offs, b.nslots, b.ctot, b.cell_start,
+                                                                  b.sorted, b.cell_of, b.relhi, b.rello, b.prec, b.plo,
+                                                                  b.pos64, b.kin, b.diam32);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     if (b.ptot > 0) {

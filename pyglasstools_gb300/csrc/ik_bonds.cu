@@ -164,28 +164,40 @@ cudaError_t launch_bin32(const double* pos, int n, IkGeom g, int* cell_of, int* 
 }
 
 // Sort the ids of each cell (insertion sort: cells hold a handful of particles; fixes
-// the order the atomic ranks left) and pack the cell's particles in that order: the
-// two steps of k_cell_sort_pack + k_pack32 in one launch, one thread per cell.
-__global__ void k_cell_sort_pack32(IkGeom g, const int* __restrict__ cell_start, int* __restrict__ sorted,
-                                   const float4* __restrict__ relhi, const float4* __restrict__ rello,
-                                   const double* __restrict__ pos, const double* __restrict__ vel,
-                                   const double* __restrict__ mass, const double* __restrict__ diam,
-                                   IkPRec* __restrict__ prec, float4* __restrict__ plo, IkB64* __restrict__ pos64,
-                                   float4* __restrict__ kin, float* __restrict__ diam32)
+// the order the atomic ranks left), then pack the particles in that order: a CTA sorts
+// its 128 cells, one thread per cell, and then packs the cells' particles (a contiguous
+// range of the cell list), one thread per particle, so that the packing's loads and
+// stores are spread over all the CTA's threads instead of a cell's particles one after
+// the other.
+__global__ void __launch_bounds__(128) k_cell_sort_pack32(IkGeom g, const int* __restrict__ cell_start,
+                                                          int* __restrict__ sorted, const int* __restrict__ cell_of,
+                                                          const float4* __restrict__ relhi,
+                                                          const float4* __restrict__ rello,
+                                                          const double* __restrict__ pos,
+                                                          const double* __restrict__ vel,
+                                                          const double* __restrict__ mass,
+                                                          const double* __restrict__ diam, IkPRec* __restrict__ prec,
+                                                          float4* __restrict__ plo, IkB64* __restrict__ pos64,
+                                                          float4* __restrict__ kin, float* __restrict__ diam32)
 {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.ncell) return;
-    ik_sort_pack_cell(g.dim, c, cell_start[c], cell_start[c + 1], 0, sorted, relhi, rello, pos, vel, mass, diam, prec,
-                      plo, pos64, kin, diam32);
+    const int c0 = blockIdx.x * blockDim.x, c = c0 + threadIdx.x;
+    if (c < g.ncell) ik_sort_cell(cell_start[c], cell_start[c + 1], sorted);
+    __syncthreads();
+    const int pe = cell_start[min(c0 + (int)blockDim.x, g.ncell)];
+    for (int p = cell_start[c0] + threadIdx.x; p < pe; p += blockDim.x) {
+        const int ig = sorted[p];
+        ik_pack_one(g.dim, cell_of[ig], p, ig, 0, relhi, rello, pos, vel, mass, diam, prec, plo, pos64, kin, diam32);
+    }
 }
 
-cudaError_t launch_sort_pack32(IkGeom g, const int* cell_start, int* sorted, const float4* relhi, const float4* rello,
-                               const double* pos, const double* vel, const double* mass, const double* diam,
-                               IkPRec* prec, float4* plo, IkB64* pos64, float4* kin, float* diam32, cudaStream_t st)
+cudaError_t launch_sort_pack32(IkGeom g, const int* cell_start, int* sorted, const int* cell_of, const float4* relhi,
+                               const float4* rello, const double* pos, const double* vel, const double* mass,
+                               const double* diam, IkPRec* prec, float4* plo, IkB64* pos64, float4* kin,
+                               float* diam32, cudaStream_t st)
 {
     if (g.ncell <= 0) return cudaSuccess;
-    k_cell_sort_pack32<<<(g.ncell + 127) / 128, 128, 0, st>>>(g, cell_start, sorted, relhi, rello, pos, vel, mass,
-                                                              diam, prec, plo, pos64, kin, diam32);
+    k_cell_sort_pack32<<<(g.ncell + 127) / 128, 128, 0, st>>>(g, cell_start, sorted, cell_of, relhi, rello, pos, vel,
+                                                              mass, diam, prec, plo, pos64, kin, diam32);
     return cudaGetLastError();
 }
 

@@ -30,17 +30,8 @@ __device__ __forceinline__ int ik_bin32_one(const IkGeom& g, const double* __res
 }
 
 // Sort the ids of one cell (insertion sort: cells hold a handful of particles; fixes the
-// order the atomic ranks left) and pack the cell's particles in that order.  The ids
-// in sorted / relhi / rello / prec / plo / pos64 / kin / diam32 are the cell list's
-// (a batch's: id0 = the frame's first); pos / vel / mass / diam are the frame's own
-// arrays, indexed by id - id0.  cell = the cell's index in the frame (IkPRec::cell).
-__device__ __forceinline__ void ik_sort_pack_cell(int dim, int cell, int s, int e, int id0, int* __restrict__ sorted,
-                                                  const float4* __restrict__ relhi, const float4* __restrict__ rello,
-                                                  const double* __restrict__ pos, const double* __restrict__ vel,
-                                                  const double* __restrict__ mass, const double* __restrict__ diam,
-                                                  IkPRec* __restrict__ prec, float4* __restrict__ plo,
-                                                  IkB64* __restrict__ pos64, float4* __restrict__ kin,
-                                                  float* __restrict__ diam32)
+// order the atomic ranks left).
+__device__ __forceinline__ void ik_sort_cell(int s, int e, int* __restrict__ sorted)
 {
     for (int a = s + 1; a < e; ++a) {
         const int v = sorted[a];
@@ -48,28 +39,41 @@ __device__ __forceinline__ void ik_sort_pack_cell(int dim, int cell, int s, int 
         while (b >= s && sorted[b] > v) { sorted[b + 1] = sorted[b]; --b; }
         sorted[b + 1] = v;
     }
-    for (int p = s; p < e; ++p) {
-        const int ig = sorted[p], i = ig - id0;
-        const float4 h = relhi[ig];
-        IkPRec r;
-        r.x = h.x;
-        r.y = h.y;
-        r.z = h.z;
-        r.cell = cell;
-        prec[p] = r;
-        plo[p] = rello[ig];
-        pos64[p] = make_ikb64(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], diam[i]);
-        const double m = mass ? mass[i] : 1.0;
-        const double vx = vel ? vel[3 * i] : 0.0, vy = vel ? vel[3 * i + 1] : 0.0, vz = vel ? vel[3 * i + 2] : 0.0;
-        if (dim == 2) {
-            kin[p] = make_float4((float)(m * vx * vx), (float)(m * vy * vy), (float)(m * vx * vy), 0.f);
-        } else {
-            kin[2 * p] = make_float4((float)(m * vx * vx), (float)(m * vy * vy), (float)(m * vz * vz),
-                                     (float)(m * vx * vy));
-            kin[2 * p + 1] = make_float4((float)(m * vx * vz), (float)(m * vy * vz), 0.f, 0.f);
-        }
-        diam32[p] = (float)diam[i];
+}
+
+// Pack the particle at cell-list position p (id ig = sorted[p]): its records in
+// prec / plo / pos64 / kin / diam32, indexed by p.  relhi / rello are indexed by ig (the
+// cell list's ids; a batch's: id0 = the frame's first); pos / vel / mass / diam are the
+// frame's own arrays, indexed by ig - id0.  cell = the cell's index in the frame
+// (IkPRec::cell).
+__device__ __forceinline__ void ik_pack_one(int dim, int cell, int p, int ig, int id0,
+                                            const float4* __restrict__ relhi, const float4* __restrict__ rello,
+                                            const double* __restrict__ pos, const double* __restrict__ vel,
+                                            const double* __restrict__ mass, const double* __restrict__ diam,
+                                            IkPRec* __restrict__ prec, float4* __restrict__ plo,
+                                            IkB64* __restrict__ pos64, float4* __restrict__ kin,
+                                            float* __restrict__ diam32)
+{
+    const int i = ig - id0;
+    const float4 h = relhi[ig];
+    IkPRec r;
+    r.x = h.x;
+    r.y = h.y;
+    r.z = h.z;
+    r.cell = cell;
+    prec[p] = r;
+    plo[p] = rello[ig];
+    pos64[p] = make_ikb64(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], diam[i]);
+    const double m = mass ? mass[i] : 1.0;
+    const double vx = vel ? vel[3 * i] : 0.0, vy = vel ? vel[3 * i + 1] : 0.0, vz = vel ? vel[3 * i + 2] : 0.0;
+    if (dim == 2) {
+        kin[p] = make_float4((float)(m * vx * vx), (float)(m * vy * vy), (float)(m * vx * vy), 0.f);
+    } else {
+        kin[2 * p] = make_float4((float)(m * vx * vx), (float)(m * vy * vy), (float)(m * vz * vz),
+                                 (float)(m * vx * vy));
+        kin[2 * p + 1] = make_float4((float)(m * vx * vz), (float)(m * vy * vz), 0.f, 0.f);
     }
+    diam32[p] = (float)diam[i];
 }
 
 // b = o + (pj - pi) for double-float operands (o = ohi + olo, p = hi + lo), rounded
@@ -183,6 +187,12 @@ __device__ __forceinline__ bool ik_select64_shift(const IkGeom& g, const IkPot& 
 // f' * hb (x) hb = 0.5 * forceDivR * r_ij (x) r_ij.  Written at a fixed stride of
 // `maxb` records per particle in candidate order (stencil cell with x fastest, then
 // ascending sorted index): deterministic.  ALLAX: some axis has fewer than three cells.
+// Without ALLAX a stencil row's three cells (x = hx - 1, hx, hx + 1) are distinct and,
+// unless the row wraps in x, consecutive in the cell list: the row's candidates are one
+// contiguous index range (two at the box's x edges), walked in the same order as cell
+// by cell, with the x offset of a candidate's cell read from the range's inner cell
+// boundaries.  One loop per row instead of one per cell: fewer loop set-ups, no integer
+// division for the wrap, and less divergence between the lanes' ragged cell counts.
 // The bonds of particle p (cell order); cell_start is the frame's cell list (indices
 // into prec / plo / pos64 / tmp / nb, which may be a batch's); returns the number of
 // force-active bonds (those beyond maxb are counted, not stored).
@@ -218,66 +228,112 @@ __device__ __forceinline__ int ik_bonds32_particle(const IkGeom& g, const IkPot&
     const float hk = 0.5f * kappa, fk = 2.0f / (kappa * kappa);
     float4* out = tmp + (size_t)p * maxb;
     int cnt = 0;
-    for (int iz = 0; iz < len[2]; ++iz) {
-        const int uz = lo[2] + iz;
-        const int wz = DIM == 3 ? ik_wrap(uz, g.nc[2]) : 0;
-        const float kz = (float)(uz - home[2]);
-        const float oz = DIM == 3 ? kz * g.cwhi[2] : 0.f, olz = DIM == 3 ? kz * g.cwlo[2] : 0.f;
-        for (int iy = 0; iy < len[1]; ++iy) {
-            const int uy = lo[1] + iy;
-            const int wy = ik_wrap(uy, g.nc[1]);
-            const float ky = (float)(uy - home[1]);
-            const float oy = ky * g.cwhi[1], oly = ky * g.cwlo[1];
-            for (int ix = 0; ix < len[0]; ++ix) {
-                const int ux = lo[0] + ix;
-                const int wx = ik_wrap(ux, g.nc[0]);
-                const float kx = (float)(ux - home[0]);
-                const float ox = kx * g.cwhi[0], olx = kx * g.cwlo[0];
-                const int cell = (wz * g.nc[1] + wy) * g.nc[0] + wx;
-                const int qe = cell_start[cell + 1];
-                for (int q = cell_start[cell]; q < qe; ++q) {
-                    if (q == p) continue;
-                    const IkPRec o = prec[q];
-                    float bx = ox + (o.x - me.x), by = oy + (o.y - me.y), bz = DIM == 3 ? oz + (o.z - me.z) : 0.f;
-                    if (allx) bx -= L0 * rintf(bx / L0);
-                    if (ally) by -= L1 * rintf(by / L1);
-                    if (allz) bz -= L2 * rintf(bz / L2);
-                    float r2 = bx * bx + by * by + bz * bz;
-                    if (!(r2 < mr2 * screen)) continue;
-                    const float dj = diam32[q];
-                    const float sig = 0.5f * (di + dj) * (1.f - eps * fabsf(di - dj));
-                    const float s2 = sig * sig;
-                    if (!(r2 < rc2 * s2 * screen)) continue;
-                    if (!(allx || ally || allz)) {
-                        const float4 lq = plo[q];
-                        bx = ik_df_diff(ox, olx, o.x, lq.x, me.x, mlo.x);
-                        by = ik_df_diff(oy, oly, o.y, lq.y, me.y, mlo.y);
-                        if (DIM == 3) bz = ik_df_diff(oz, olz, o.z, lq.z, me.z, mlo.z);
-                    } else {
-                        const IkB64 pi = pos64[p], pj = pos64[q];
-                        double dx = pj.x - pi.x, dy = pj.y - pi.y;
-                        dx = fma(-g.L[0], rint(dx * g.invL[0]), dx);
-                        dy = fma(-g.L[1], rint(dy * g.invL[1]), dy);
-                        bx = (float)dx;
-                        by = (float)dy;
-                        if (DIM == 3) {
-                            double dz = pj.z - pi.z;
-                            dz = fma(-g.L[2], rint(dz * g.invL[2]), dz);
-                            bz = (float)dz;
-                        }
-                    }
-                    r2 = bx * bx + by * by + bz * bz;
-                    const float rt = rc2 * s2;
-                    bool act = r2 < mr2 && r2 < rt;
-                    if (fabsf(r2 - rt) <= 2e-5f * rt || fabsf(r2 - mr2) <= 2e-5f * mr2) { // at a cut-off: FP64
-                        if (ALLAX) act = ik_select64(g, pot, pos64[p], pos64[q]);
-                        else act = ik_select64_shift(g, pot, pos64[p], pos64[q], (ux > wx) - (ux < wx),
-                                                     (uy > wy) - (uy < wy), DIM == 3 ? (uz > wz) - (uz < wz) : 0);
-                    }
-                    if (act) {
-                        const float f = ik_force32<KIND>(pf, r2, s2);
-                        if (cnt < maxb) out[cnt] = make_float4(hk * bx, hk * by, hk * bz, fk * f);
-                        ++cnt;
+    // one candidate q: cell offset (ox, oy, oz) + (olx, oly, olz) as double-float pairs,
+    // (sx, sy, sz) the stencil's wrap shifts (used by the FP64 re-decision)
+    auto visit = [&](int q, float ox, float olx, float oy, float oly, float oz, float olz, int sx, int sy, int sz) {
+        const IkPRec o = prec[q];
+        float bx = ox + (o.x - me.x), by = oy + (o.y - me.y), bz = DIM == 3 ? oz + (o.z - me.z) : 0.f;
+        if (allx) bx -= L0 * rintf(bx / L0);
+        if (ally) by -= L1 * rintf(by / L1);
+        if (allz) bz -= L2 * rintf(bz / L2);
+        float r2 = bx * bx + by * by + bz * bz;
+        if (!(r2 < mr2 * screen)) return;
+        const float dj = diam32[q];
+        const float sig = 0.5f * (di + dj) * (1.f - eps * fabsf(di - dj));
+        const float s2 = sig * sig;
+        if (!(r2 < rc2 * s2 * screen)) return;
+        if (!(allx || ally || allz)) {
+            const float4 lq = plo[q];
+            bx = ik_df_diff(ox, olx, o.x, lq.x, me.x, mlo.x);
+            by = ik_df_diff(oy, oly, o.y, lq.y, me.y, mlo.y);
+            if (DIM == 3) bz = ik_df_diff(oz, olz, o.z, lq.z, me.z, mlo.z);
+        } else {
+            const IkB64 pi = pos64[p], pj = pos64[q];
+            double dx = pj.x - pi.x, dy = pj.y - pi.y;
+            dx = fma(-g.L[0], rint(dx * g.invL[0]), dx);
+            dy = fma(-g.L[1], rint(dy * g.invL[1]), dy);
+            bx = (float)dx;
+            by = (float)dy;
+            if (DIM == 3) {
+                double dz = pj.z - pi.z;
+                dz = fma(-g.L[2], rint(dz * g.invL[2]), dz);
+                bz = (float)dz;
+            }
+        }
+        r2 = bx * bx + by * by + bz * bz;
+        const float rt = rc2 * s2;
+        bool act = r2 < mr2 && r2 < rt;
+        if (fabsf(r2 - rt) <= 2e-5f * rt || fabsf(r2 - mr2) <= 2e-5f * mr2) { // at a cut-off: FP64
+            if (ALLAX) act = ik_select64(g, pot, pos64[p], pos64[q]);
+            else act = ik_select64_shift(g, pot, pos64[p], pos64[q], sx, sy, sz);
+        }
+        if (act) {
+            const float f = ik_force32<KIND>(pf, r2, s2);
+            if (cnt < maxb) out[cnt] = make_float4(hk * bx, hk * by, hk * bz, fk * f);
+            ++cnt;
+        }
+    };
+    if constexpr (ALLAX) {
+        for (int iz = 0; iz < len[2]; ++iz) {
+            const int uz = lo[2] + iz;
+            const int wz = DIM == 3 ? ik_wrap(uz, g.nc[2]) : 0;
+            const float kz = (float)(uz - home[2]);
+            const float oz = DIM == 3 ? kz * g.cwhi[2] : 0.f, olz = DIM == 3 ? kz * g.cwlo[2] : 0.f;
+            for (int iy = 0; iy < len[1]; ++iy) {
+                const int uy = lo[1] + iy;
+                const int wy = ik_wrap(uy, g.nc[1]);
+                const float ky = (float)(uy - home[1]);
+                const float oy = ky * g.cwhi[1], oly = ky * g.cwlo[1];
+                for (int ix = 0; ix < len[0]; ++ix) {
+                    const int ux = lo[0] + ix;
+                    const int wx = ik_wrap(ux, g.nc[0]);
+                    const float kx = (float)(ux - home[0]);
+                    const float ox = kx * g.cwhi[0], olx = kx * g.cwlo[0];
+                    const int cell = (wz * g.nc[1] + wy) * g.nc[0] + wx;
+                    const int qe = cell_start[cell + 1];
+                    for (int q = cell_start[cell]; q < qe; ++q)
+                        if (q != p) visit(q, ox, olx, oy, oly, oz, olz, 0, 0, 0);
+                }
+            }
+        }
+    } else {
+        // every axis has one cell (len 1) or at least three (len 3, distinct cells)
+        const int nx = g.nc[0], hx = home[0];
+        // the row's cells in stencil order as one or two runs of consecutive x:
+        // run 0 = [xa0, xb0] starting at x offset ka0, run 1 = [xa1, xb1] (empty: xb1 < xa1)
+        int xa0, xb0, ka0, xa1, xb1, ka1;
+        if (len[0] == 1) { xa0 = 0; xb0 = 0; ka0 = 0; xa1 = 1; xb1 = 0; ka1 = 0; }
+        else if (hx == 0) { xa0 = nx - 1; xb0 = nx - 1; ka0 = -1; xa1 = 0; xb1 = 1; ka1 = 0; }
+        else if (hx == nx - 1) { xa0 = nx - 2; xb0 = nx - 1; ka0 = -1; xa1 = 0; xb1 = 0; ka1 = 1; }
+        else { xa0 = hx - 1; xb0 = hx + 1; ka0 = -1; xa1 = 1; xb1 = 0; ka1 = 0; }
+        for (int iz = 0; iz < len[2]; ++iz) {
+            const int uz = lo[2] + iz;
+            const int wz = DIM == 3 ? (uz < 0 ? uz + g.nc[2] : (uz >= g.nc[2] ? uz - g.nc[2] : uz)) : 0;
+            const float kz = (float)(uz - home[2]);
+            const float oz = DIM == 3 ? kz * g.cwhi[2] : 0.f, olz = DIM == 3 ? kz * g.cwlo[2] : 0.f;
+            const int sz = DIM == 3 ? (uz > wz) - (uz < wz) : 0;
+            for (int iy = 0; iy < len[1]; ++iy) {
+                const int uy = lo[1] + iy;
+                const int wy = uy < 0 ? uy + g.nc[1] : (uy >= g.nc[1] ? uy - g.nc[1] : uy);
+                const float ky = (float)(uy - home[1]);
+                const float oy = ky * g.cwhi[1], oly = ky * g.cwlo[1];
+                const int sy = (uy > wy) - (uy < wy);
+                const int* rs = cell_start + (wz * g.nc[1] + wy) * nx;
+#pragma unroll
+                for (int run = 0; run < 2; ++run) {
+                    const int xa = run ? xa1 : xa0, xb = run ? xb1 : xb0, ka = run ? ka1 : ka0;
+                    if (xb < xa) continue;
+                    const int qa = rs[xa], qe = rs[xb + 1];
+                    // inner cell boundaries of the run (past its end where it has fewer cells)
+                    const int b1 = xb >= xa + 1 ? rs[xa + 1] : qe, b2 = xb >= xa + 2 ? rs[xa + 2] : qe;
+                    const float kaf = (float)ka;
+                    for (int q = qa; q < qe; ++q) {
+                        if (q == p) continue;
+                        // the candidate cell's x offset (-1, 0 or 1: exactly the float the
+                        // cell-by-cell walk converts)
+                        const float kxf = kaf + (q >= b1 ? 1.f : 0.f) + (q >= b2 ? 1.f : 0.f);
+                        const int ux = hx + (int)kxf;
+                        visit(q, kxf * g.cwhi[0], kxf * g.cwlo[0], oy, oly, oz, olz, (ux >= nx) - (ux < 0), sy, sz);
                     }
                 }
             }
