@@ -683,7 +683,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         ENS(L.pos64, sizeof(IkB64) * std::max(n, 1));
         ENS(L.plo, sizeof(float4) * std::max(n, 1));
         // per-cell sort + pack in one launch
-        CK(launch_sort_pack32(g, L.cell_start.as<int>(), L.sorted.as<int>(), L.cell_of.as<int>(), L.relhi.as<float4>(),
+        CK(launch_sort_pack32(g, L.cell_start.as<int>(), L.sorted.as<int>(), L.relhi.as<float4>(),
                               L.rello.as<float4>(), s.pos.as<double>(), s.has_vel ? s.vel.as<double>() : nullptr,
                               s.has_mass ? s.mass.as<double>() : nullptr, s.diam.as<double>(), L.prec.as<IkPRec>(),
                               L.plo.as<float4>(), L.pos64.as<IkB64>(), L.kin.as<float4>(), L.diam32.as<float>(),
@@ -749,6 +749,12 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         a.cnt_triples = cnt + 2;
         CK(cudaMemsetAsync(L.work_counter.p, 0, sizeof(int), L.st));
         const bool mlp = c->cg.mode == IK_QUAD_MLP && (a.fields & 1);
+        // without surrogate corrections to add the gather writes the FP64 fields itself
+        a.direct64 = mlp ? 0 : 1;
+        a.out64_vir = (a.fields & 1) ? s.vir.as<double>() : nullptr;
+        a.out64_kin = (a.fields & 2) ? s.kin.as<double>() : nullptr;
+        a.s64_vir = 0.5 * norm;
+        a.s64_kin = norm;
         if (mlp) {
             if (c->mlp_cap == 0) c->mlp_cap = std::max<long long>(1 << 20, 128LL * c->geo.G);
             ENS(L.mlp_rec, sizeof(float4) * (size_t)c->mlp_cap);
@@ -783,12 +789,16 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
                                   cnt + 4, c->status.as<int>(), c->sm_count * 4, L.st));
             c->launches += 1;
         }
-        // FP64 finish: ((double)hi + (double)lo) * normalisation (0.5 of the GL map for the virial)
-        nv.next("ik finish");
-        CK(launch_pairs_to_f64(L.vir2.as<float2>(), mlp ? L.corr.as<unsigned long long>() : nullptr,
-                               (a.fields & 1) ? s.vir.as<double>() : nullptr, 0.5 * norm, L.kin2.as<float2>(),
-                               (a.fields & 2) ? s.kin.as<double>() : nullptr, norm, (long long)NC * c->geo.G, L.st));
-        c->launches += (c->geo.G > 0 && a.fields) ? 1 : 0;
+        // FP64 finish: ((double)hi + (double)lo) * normalisation (0.5 of the GL map for the
+        // virial), with the surrogate's corrections (otherwise done by the gather)
+        if (!a.direct64) {
+            nv.next("ik finish");
+            CK(launch_pairs_to_f64(L.vir2.as<float2>(), mlp ? L.corr.as<unsigned long long>() : nullptr,
+                                   (a.fields & 1) ? s.vir.as<double>() : nullptr, 0.5 * norm, L.kin2.as<float2>(),
+                                   (a.fields & 2) ? s.kin.as<double>() : nullptr, norm, (long long)NC * c->geo.G,
+                                   L.st));
+            c->launches += (c->geo.G > 0 && a.fields) ? 1 : 0;
+        }
         if (fields & IK_FIELD_ELASTIC) { // the elastic virial field: same staging, elastic records
             nv.next("ik elastic");
             if (int r2 = elastic_bonds(c, s, L, g, n)) return r2;
@@ -800,6 +810,10 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
             e.maxb = c->maxbe;
             e.qcap = 32 * (std::min(c->maxbe, 63) + 1);
             e.fields = IK_FIELD_VIRIAL;
+            e.direct64 = 1; // the gather writes the FP64 elastic field itself
+            e.out64_vir = s.ela.as<double>();
+            e.out64_kin = nullptr;
+            e.s64_vir = 0.5 * norm;
             e.mlp_rec = nullptr;
             e.mlp_rid = nullptr;
             e.mlp_count = nullptr;
@@ -813,9 +827,6 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
                 CK(launch_gather32(e, c->cg.kind, false, 0, blocks, 32 * IK_WARPS_GATHER, esmem, L.st));
                 c->launches += 1;
             }
-            CK(launch_pairs_to_f64(L.vir2.as<float2>(), nullptr, s.ela.as<double>(), 0.5 * norm, nullptr, nullptr,
-                                   0.0, (long long)NC * c->geo.G, L.st));
-            c->launches += c->geo.G > 0 ? 1 : 0;
         }
     } else {
         if (timing) CK(cudaEventRecord(c->ev[1], L.st));
@@ -1169,6 +1180,12 @@ int fused_enqueue(ik_ctx* c, int fields, bool timing = false)
     a.out_vir = F.vir2.as<float2>();
     a.out_kin = F.kin2.as<float2>();
     a.fields = fields & (IK_FIELD_VIRIAL | IK_FIELD_KINETIC);
+    const double norm = c->cg.kind == IK_CG_MOLLIFIER ? c->cg.mollifier_norm : c->cg.norm;
+    // both fields: the gather writes each slot's FP64 fields itself; one field: the
+    // finish also writes the other as zeros
+    a.direct64 = a.fields == (IK_FIELD_VIRIAL | IK_FIELD_KINETIC) ? 1 : 0;
+    a.s64_vir = 0.5 * norm;
+    a.s64_kin = norm;
     a.work_counter = F.work.as<int>();
     a.status = c->status.as<int>();
     a.slots = b.slots;
@@ -1184,9 +1201,10 @@ int fused_enqueue(ik_ctx* c, int fields, bool timing = false)
         c->launches += 1;
     }
     if (timing) CK(cudaEventRecord(c->ev[3], st));
-    const double norm = c->cg.kind == IK_CG_MOLLIFIER ? c->cg.mollifier_norm : c->cg.norm;
-    CK(launch_batch_finish(b, a.out_vir, a.out_kin, 0.5 * norm, norm, fields, st));
-    c->launches += b.vtot > 0 ? 1 : 0;
+    if (!a.direct64) {
+        CK(launch_batch_finish(b, a.out_vir, a.out_kin, 0.5 * norm, norm, fields, st));
+        c->launches += b.vtot > 0 ? 1 : 0;
+    }
     return IK_OK;
 }
 

@@ -97,7 +97,8 @@ __global__ void __launch_bounds__(128) k_sort_pack32_batch(const IkBatchSlot* __
 template <int DIM, int KIND>
 __global__ void __launch_bounds__(128) k_bonds32t_batch(const IkBatchSlot* __restrict__ S,
                                                         const int* __restrict__ p_offs, int nslots, int ptot,
-                                                        IkPot pot, float kappa, const IkPRec* __restrict__ prec,
+                                                        IkPot pot, IkPotF pf, float kappa,
+                                                        const IkPRec* __restrict__ prec,
                                                         const float* __restrict__ diam32,
                                                         const int* __restrict__ cell_start,
                                                         const float4* __restrict__ plo,
@@ -110,10 +111,10 @@ __global__ void __launch_bounds__(128) k_bonds32t_batch(const IkBatchSlot* __res
     const int s = ik_batch_slot(p_offs, nslots, p);
     const IkBatchSlot& sl = S[s];
     const int* cs = cell_start + sl.geo.c_off;
-    const int cnt = sl.allax ? ik_bonds32_particle<DIM, KIND, true>(sl.geo.g, pot, kappa, p, prec, diam32, cs, plo,
-                                                                    pos64, tmp, maxb, nb, status, maxnb)
-                             : ik_bonds32_particle<DIM, KIND, false>(sl.geo.g, pot, kappa, p, prec, diam32, cs, plo,
-                                                                     pos64, tmp, maxb, nb, status, maxnb);
+    const int cnt = sl.allax ? ik_bonds32_particle<DIM, KIND, true>(sl.geo.g, pot, pf, kappa, p, prec, diam32, cs,
+                                                                    plo, pos64, tmp, maxb, nb, status, maxnb)
+                             : ik_bonds32_particle<DIM, KIND, false>(sl.geo.g, pot, pf, kappa, p, prec, diam32, cs,
+                                                                     plo, pos64, tmp, maxb, nb, status, maxnb);
     // force-active directed bonds per slot: one atomic per slot present in the warp
     const unsigned act = __activemask();
     const unsigned grp = __match_any_sync(act, s);
@@ -165,8 +166,9 @@ cudaError_t launch_batch_prepare(const IkBatchLaunch& b, int dim, const IkPot& p
     }
     if (b.ptot > 0) {
         const int blocks = (b.ptot + 127) / 128;
+        const IkPotF pf = ik_potf(pot);
         auto go = [&](auto kernel) {
-            kernel<<<blocks, 128, 0, st>>>(b.slots, b.p_offs, b.nslots, b.ptot, pot, kappa, b.prec, b.diam32,
+            kernel<<<blocks, 128, 0, st>>>(b.slots, b.p_offs, b.nslots, b.ptot, pot, pf, kappa, b.prec, b.diam32,
                                            b.cell_start, b.plo, b.pos64, b.tmp, b.maxb, b.nb, b.status, b.maxnb);
         };
 #define IK_BONDS32B_KIND(K)                                                   \

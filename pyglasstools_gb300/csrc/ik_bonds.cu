@@ -32,7 +32,7 @@ __global__ void k_bin32(const double* __restrict__ pos, int n, IkGeom g, int* __
 // ---------------------------------------------------------------------------
 // Force-active bonds of a frame, one thread per particle (ik_bonds32_particle).
 template <int DIM, int KIND, bool ALLAX>
-__global__ void __launch_bounds__(128) k_bonds32t(IkGeom g, IkPot pot, float kappa, int n,
+__global__ void __launch_bounds__(128) k_bonds32t(IkGeom g, IkPot pot, IkPotF pf, float kappa, int n,
                                                   const IkPRec* __restrict__ prec,
                                                   const float* __restrict__ diam32,
                                                   const int* __restrict__ cell_start,
@@ -43,8 +43,8 @@ __global__ void __launch_bounds__(128) k_bonds32t(IkGeom g, IkPot pot, float kap
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
-    const int cnt = ik_bonds32_particle<DIM, KIND, ALLAX>(g, pot, kappa, p, prec, diam32, cell_start, plo, pos64,
-                                                          tmp, maxb, nb, status, maxnb);
+    const int cnt = ik_bonds32_particle<DIM, KIND, ALLAX>(g, pot, pf, kappa, p, prec, diam32, cell_start, plo,
+                                                          pos64, tmp, maxb, nb, status, maxnb);
     if (nbond_total) { // force-active directed bonds of the frame (one atomic per warp)
         const unsigned act = __activemask();
         const int tot = __reduce_add_sync(act, cnt);
@@ -164,14 +164,12 @@ cudaError_t launch_bin32(const double* pos, int n, IkGeom g, int* cell_of, int* 
 }
 
 // Sort the ids of each cell (insertion sort: cells hold a handful of particles; fixes
-// the order the atomic ranks left), then pack the particles in that order: a CTA sorts
-// its 128 cells, one thread per cell, and then packs the cells' particles (a contiguous
-// range of the cell list), one thread per particle, so that the packing's loads and
-// stores are spread over all the CTA's threads instead of a cell's particles one after
-// the other.
+// the order the atomic ranks left) and pack the cell's particles in that order, one
+// thread per cell.  (A frame alone has too few cells for the batch kernel's split into
+// a sort per cell and a pack per particle to pay: its barrier lengthens the chain of
+// dependent loads.)
 __global__ void __launch_bounds__(128) k_cell_sort_pack32(IkGeom g, const int* __restrict__ cell_start,
-                                                          int* __restrict__ sorted, const int* __restrict__ cell_of,
-                                                          const float4* __restrict__ relhi,
+                                                          int* __restrict__ sorted, const float4* __restrict__ relhi,
                                                           const float4* __restrict__ rello,
                                                           const double* __restrict__ pos,
                                                           const double* __restrict__ vel,
@@ -180,24 +178,21 @@ __global__ void __launch_bounds__(128) k_cell_sort_pack32(IkGeom g, const int* _
                                                           float4* __restrict__ plo, IkB64* __restrict__ pos64,
                                                           float4* __restrict__ kin, float* __restrict__ diam32)
 {
-    const int c0 = blockIdx.x * blockDim.x, c = c0 + threadIdx.x;
-    if (c < g.ncell) ik_sort_cell(cell_start[c], cell_start[c + 1], sorted);
-    __syncthreads();
-    const int pe = cell_start[min(c0 + (int)blockDim.x, g.ncell)];
-    for (int p = cell_start[c0] + threadIdx.x; p < pe; p += blockDim.x) {
-        const int ig = sorted[p];
-        ik_pack_one(g.dim, cell_of[ig], p, ig, 0, relhi, rello, pos, vel, mass, diam, prec, plo, pos64, kin, diam32);
-    }
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.ncell) return;
+    const int s = cell_start[c], e = cell_start[c + 1];
+    ik_sort_cell(s, e, sorted);
+    for (int p = s; p < e; ++p)
+        ik_pack_one(g.dim, c, p, sorted[p], 0, relhi, rello, pos, vel, mass, diam, prec, plo, pos64, kin, diam32);
 }
 
-cudaError_t launch_sort_pack32(IkGeom g, const int* cell_start, int* sorted, const int* cell_of, const float4* relhi,
-                               const float4* rello, const double* pos, const double* vel, const double* mass,
-                               const double* diam, IkPRec* prec, float4* plo, IkB64* pos64, float4* kin,
-                               float* diam32, cudaStream_t st)
+cudaError_t launch_sort_pack32(IkGeom g, const int* cell_start, int* sorted, const float4* relhi, const float4* rello,
+                               const double* pos, const double* vel, const double* mass, const double* diam,
+                               IkPRec* prec, float4* plo, IkB64* pos64, float4* kin, float* diam32, cudaStream_t st)
 {
     if (g.ncell <= 0) return cudaSuccess;
-    k_cell_sort_pack32<<<(g.ncell + 127) / 128, 128, 0, st>>>(g, cell_start, sorted, cell_of, relhi, rello, pos, vel,
-                                                              mass, diam, prec, plo, pos64, kin, diam32);
+    k_cell_sort_pack32<<<(g.ncell + 127) / 128, 128, 0, st>>>(g, cell_start, sorted, relhi, rello, pos, vel, mass,
+                                                              diam, prec, plo, pos64, kin, diam32);
     return cudaGetLastError();
 }
 
@@ -209,8 +204,9 @@ cudaError_t launch_bonds32(int dim, IkGeom g, IkPot pot, float kappa, int n, con
     if (n <= 0) return cudaSuccess;
     const int threads = 128;
     const int blocks = (n + threads - 1) / threads;
+    const IkPotF pf = ik_potf(pot);
     auto go = [&](auto kernel) {
-        kernel<<<blocks, threads, 0, st>>>(g, pot, kappa, n, prec, diam32, cell_start, plo, pos64, tmp, maxb, nb,
+        kernel<<<blocks, threads, 0, st>>>(g, pot, pf, kappa, n, prec, diam32, cell_start, plo, pos64, tmp, maxb, nb,
                                            status, maxnb, nbond_total);
     };
     bool allax = false;

@@ -529,6 +529,7 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                 if (k < 32 || hc >= nh) break;
             }
             __syncwarp();
+            const bool last = hc >= nh; // this chunk holds the item's last halo cells
 
             // ---- process the item's groups against the staged particles
             for (int gs = it.w; gs < gend; gs += P) {
@@ -947,13 +948,27 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                         if (g >= 0) {
                             float2* out = kin_here ? a.out_kin : a.out_vir;
                             const size_t o = (size_t)g * NC + c;
-                            if (first) {
-                                out[o] = make_float2(h, l);
-                            } else { // another chunk of the same item: compensated add
+                            float fh = h, fl = l;
+                            if (!first) { // another chunk of the same item: compensated add
                                 const float2 old = out[o];
                                 float s2, e2;
                                 ik_two_sum(old.x, h, s2, e2);
-                                out[o] = make_float2(s2, e2 + (old.y + l));
+                                fh = s2;
+                                fl = e2 + (old.y + l);
+                            }
+                            if (a.direct64 && last) { // the value is final: FP64 into the field
+                                double* o64;
+                                size_t oo = o;
+                                if constexpr (BATCH) {
+                                    const IkBatchSlot& sl = a.slots[cur_slot];
+                                    o64 = kin_here ? sl.out_kin : sl.out_vir;
+                                    oo = (size_t)(g - sl.g_off) * NC + c;
+                                } else {
+                                    o64 = kin_here ? a.out64_kin : a.out64_vir;
+                                }
+                                o64[oo] = ((double)fh + (double)fl) * (kin_here ? a.s64_kin : a.s64_vir);
+                            } else {
+                                out[o] = make_float2(fh, fl);
                             }
                         }
                     }

@@ -15,11 +15,9 @@ __global__ void k_cell_sort_pack(IkGeom g, const int* cell_start, int* sorted, c
 // ---- tuned-path preparation (ik_bonds.cu) ---------------------------------
 cudaError_t launch_bin32(const double* pos, int n, IkGeom g, int* cell_of, int* rank, int* cell_count, float4* relhi,
                          float4* rello, cudaStream_t st);
-// cell_of: each particle's cell (k_bin32's output)
-cudaError_t launch_sort_pack32(IkGeom g, const int* cell_start, int* sorted, const int* cell_of, const float4* relhi,
-                               const float4* rello, const double* pos, const double* vel, const double* mass,
-                               const double* diam, IkPRec* prec, float4* plo, IkB64* pos64, float4* kin,
-                               float* diam32, cudaStream_t st);
+cudaError_t launch_sort_pack32(IkGeom g, const int* cell_start, int* sorted, const float4* relhi, const float4* rello,
+                               const double* pos, const double* vel, const double* mass, const double* diam,
+                               IkPRec* prec, float4* plo, IkB64* pos64, float4* kin, float* diam32, cudaStream_t st);
 // nbond_total (may be null): += force-active directed bonds
 cudaError_t launch_bonds32(int dim, IkGeom g, IkPot pot, float kappa, int n, const IkPRec* prec,
                             const float* diam32, const int* cell_start, const float4* plo, const IkB64* pos64,
@@ -95,6 +93,14 @@ struct GatherArgs32 {
     int halo_cap, qcap;
     float2* out_vir;       // unscaled double-float pairs (hi, lo), g x NC
     float2* out_kin;
+    // direct64: the item's last chunk writes each field value as FP64,
+    // ((double)hi + (double)lo) * scale, into out64_vir / out64_kin (a fused batch: into
+    // its slot's fields) instead of a pair for a separate finish; out_vir / out_kin then
+    // only carry the partial sums between the chunks of an item
+    int direct64;
+    double* out64_vir;
+    double* out64_kin;
+    double s64_vir, s64_kin;
     int fields;
     int* work_counter;
     int* status;

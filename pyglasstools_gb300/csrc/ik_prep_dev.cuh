@@ -93,14 +93,18 @@ __device__ __forceinline__ float ik_df_diff(float ohi, float olo, float hj, floa
 // ---------------------------------------------------------------------------
 // FP32 force of the eight pair models (the expressions of potential/*.h with FP32
 // constants; r2inv = sigma^2 / r^2, rs = r^2 / sigma^2, s2 = sigma^2).
+// Built on the host once per launch (its FP64 set-up, a division among it, would cost
+// every thread of a bond build ~40 operations on GB300's narrow FP64 pipe).
 struct IkPotF {
     int kind;
     float rc2, eps_s, v0, v0x4, c1x2, c2x4, c3x6, kappa, shift;
+    float mr2; // max_rcut^2
 };
-__device__ __forceinline__ IkPotF ik_potf(const IkPot& p)
+__host__ __device__ inline IkPotF ik_potf(const IkPot& p)
 {
     IkPotF q;
     q.kind = p.kind;
+    q.mr2 = (float)p.max_rcut_sq;
     const bool lj = p.kind == IKP_LJ || p.kind == IKP_FSLJ;
     q.rc2 = lj && p.v0 == 0.0 ? 0.f : (float)p.rcutsq; // eps = 0: no force (LennardJones.h:48)
     q.eps_s = p.kind == IKP_FSLJ ? 0.f : (float)p.eps;
@@ -194,10 +198,11 @@ __device__ __forceinline__ bool ik_select64_shift(const IkGeom& g, const IkPot& 
 // boundaries.  One loop per row instead of one per cell: fewer loop set-ups, no integer
 // division for the wrap, and less divergence between the lanes' ragged cell counts.
 // The bonds of particle p (cell order); cell_start is the frame's cell list (indices
-// into prec / plo / pos64 / tmp / nb, which may be a batch's); returns the number of
-// force-active bonds (those beyond maxb are counted, not stored).
+// into prec / plo / pos64 / tmp / nb, which may be a batch's); pf = ik_potf(pot); returns
+// the number of force-active bonds (those beyond maxb are counted, not stored).
 template <int DIM, int KIND, bool ALLAX>
-__device__ __forceinline__ int ik_bonds32_particle(const IkGeom& g, const IkPot& pot, float kappa, int p,
+__device__ __forceinline__ int ik_bonds32_particle(const IkGeom& g, const IkPot& pot, const IkPotF& pf, float kappa,
+                                                   int p,
                                                    const IkPRec* __restrict__ prec,
                                                    const float* __restrict__ diam32,
                                                    const int* __restrict__ cell_start,
@@ -220,8 +225,7 @@ __device__ __forceinline__ int ik_bonds32_particle(const IkGeom& g, const IkPot&
     const bool ally = ALLAX && (len[1] > 3 || (g.all_bond[1] && g.nc[1] > 1));
     const bool allz = ALLAX && DIM == 3 && (len[2] > 3 || (g.all_bond[2] && g.nc[2] > 1));
     const float L0 = (float)g.L[0], L1 = (float)g.L[1], L2 = (float)g.L[2];
-    const IkPotF pf = ik_potf(pot);
-    const float rc2 = pf.rc2, mr2 = (float)pot.max_rcut_sq, eps = pf.eps_s;
+    const float rc2 = pf.rc2, mr2 = pf.mr2, eps = pf.eps_s;
     const float screen = 1.0f + 1e-4f;
     const float di = diam32[p];
     const float4 mlo = plo[p];
