@@ -682,12 +682,15 @@ def ours(args, wl, name):
         roof_kernel = fused_gather["kernel"]
     peak = ikabi.measure_fp32_peak(local)
     traffic = None
+    traffic_batch_frame = None  # the fused gather's capture: DRAM bytes per frame
     tf = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
     if os.path.exists(tf):
         for ln in open(tf):
             parts = ln.split()
             if len(parts) >= 3 and parts[0] == "k_gather32" and parts[1] == name:
                 traffic = float(parts[2])
+            if len(parts) >= 4 and parts[0] == "k_gather32_batch" and parts[1] == name:
+                traffic_batch_frame = float(parts[2]) / float(parts[3])
 
     surrogate = None
     if not args.no_surrogate and wl["cg"]["kind"] == "gaussian" and D == 2:
@@ -724,7 +727,11 @@ def ours(args, wl, name):
            "stage_ms_fused": stage_ms_fused,
            "interactions_per_s": (A / F if fused0 else A) * value}
     if fused0:
-        if traffic is not None:  # the capture is of one frame's gather: scaled to the step's frames
+        if traffic_batch_frame is not None:  # a smaller fused capture, scaled to the step's frames
+            out["roofline"]["traffic"] = traffic_batch_frame * F
+            out["roofline"]["traffic_note"] = ("ncu DRAM bytes of a fused gather over fewer frames, per frame "
+                                               "x %d frames (the traffic grows in proportion to the frames)" % F)
+        elif traffic is not None:  # the capture is of one frame's gather: scaled to the step's frames
             out["roofline"]["traffic"] = traffic * F
             out["roofline"]["traffic_note"] = "ncu DRAM bytes of one frame's gather x %d frames" % F
     if surrogate is not None:
