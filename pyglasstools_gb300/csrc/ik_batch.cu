@@ -106,15 +106,21 @@ __global__ void __launch_bounds__(128) k_bonds32t_batch(const IkBatchSlot* __res
                                                         int maxb, int* __restrict__ nb, int* __restrict__ status,
                                                         int* __restrict__ maxnb)
 {
+    __shared__ int s_qidx[IK_BOND_QUEUE * 128];
+    __shared__ unsigned char s_qcode[IK_BOND_QUEUE * 128];
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= ptot) return;
     const int s = ik_batch_slot(p_offs, nslots, p);
     const IkBatchSlot& sl = S[s];
     const int* cs = cell_start + sl.geo.c_off;
+    int* qi = s_qidx + threadIdx.x;
+    unsigned char* qc = s_qcode + threadIdx.x;
     const int cnt = sl.allax ? ik_bonds32_particle<DIM, KIND, true>(sl.geo.g, pot, pf, kappa, p, prec, diam32, cs,
-                                                                    plo, pos64, tmp, maxb, nb, status, maxnb)
+                                                                    plo, pos64, tmp, maxb, nb, status, maxnb, qi, qc,
+                                                                    128)
                              : ik_bonds32_particle<DIM, KIND, false>(sl.geo.g, pot, pf, kappa, p, prec, diam32, cs,
-                                                                     plo, pos64, tmp, maxb, nb, status, maxnb);
+                                                                     plo, pos64, tmp, maxb, nb, status, maxnb, qi, qc,
+                                                                     128);
     // force-active directed bonds per slot: one atomic per slot present in the warp
     const unsigned act = __activemask();
     const unsigned grp = __match_any_sync(act, s);

@@ -41,10 +41,13 @@ __global__ void __launch_bounds__(128) k_bonds32t(IkGeom g, IkPot pot, IkPotF pf
                                                   int maxb, int* __restrict__ nb, int* __restrict__ status,
                                                   int* __restrict__ maxnb, unsigned long long* nbond_total)
 {
+    __shared__ int s_qidx[IK_BOND_QUEUE * 128];
+    __shared__ unsigned char s_qcode[IK_BOND_QUEUE * 128];
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     const int cnt = ik_bonds32_particle<DIM, KIND, ALLAX>(g, pot, pf, kappa, p, prec, diam32, cell_start, plo,
-                                                          pos64, tmp, maxb, nb, status, maxnb);
+                                                          pos64, tmp, maxb, nb, status, maxnb, s_qidx + threadIdx.x,
+                                                          s_qcode + threadIdx.x, 128);
     if (nbond_total) { // force-active directed bonds of the frame (one atomic per warp)
         const unsigned act = __activemask();
         const int tot = __reduce_add_sync(act, cnt);

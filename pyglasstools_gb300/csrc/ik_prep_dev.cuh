@@ -199,7 +199,10 @@ __device__ __forceinline__ bool ik_select64_shift(const IkGeom& g, const IkPot& 
 // division for the wrap, and less divergence between the lanes' ragged cell counts.
 // The bonds of particle p (cell order); cell_start is the frame's cell list (indices
 // into prec / plo / pos64 / tmp / nb, which may be a batch's); pf = ik_potf(pot); returns
-// the number of force-active bonds (those beyond maxb are counted, not stored).
+// the number of force-active bonds (those beyond maxb are counted, not stored).  qidx /
+// qcode: this thread's survivor queue in shared memory, IK_BOND_QUEUE entries at stride
+// qstride (unused with ALLAX).
+#define IK_BOND_QUEUE 16
 template <int DIM, int KIND, bool ALLAX>
 __device__ __forceinline__ int ik_bonds32_particle(const IkGeom& g, const IkPot& pot, const IkPotF& pf, float kappa,
                                                    int p,
@@ -209,7 +212,8 @@ __device__ __forceinline__ int ik_bonds32_particle(const IkGeom& g, const IkPot&
                                                    const float4* __restrict__ plo,
                                                    const IkB64* __restrict__ pos64, float4* __restrict__ tmp,
                                                    int maxb, int* __restrict__ nb, int* __restrict__ status,
-                                                   int* __restrict__ maxnb)
+                                                   int* __restrict__ maxnb, int* __restrict__ qidx,
+                                                   unsigned char* __restrict__ qcode, int qstride)
 {
     const IkPRec me = prec[p];
     const int c = me.cell;
@@ -226,26 +230,36 @@ __device__ __forceinline__ int ik_bonds32_particle(const IkGeom& g, const IkPot&
     const bool allz = ALLAX && DIM == 3 && (len[2] > 3 || (g.all_bond[2] && g.nc[2] > 1));
     const float L0 = (float)g.L[0], L1 = (float)g.L[1], L2 = (float)g.L[2];
     const float rc2 = pf.rc2, mr2 = pf.mr2, eps = pf.eps_s;
-    const float screen = 1.0f + 1e-4f;
+    const float screen_f = 1.0f + 1e-4f;
     const float di = diam32[p];
     const float4 mlo = plo[p];
     const float hk = 0.5f * kappa, fk = 2.0f / (kappa * kappa);
     float4* out = tmp + (size_t)p * maxb;
     int cnt = 0;
-    // one candidate q: cell offset (ox, oy, oz) + (olx, oly, olz) as double-float pairs,
-    // (sx, sy, sz) the stencil's wrap shifts (used by the FP64 re-decision)
-    auto visit = [&](int q, float ox, float olx, float oy, float oly, float oz, float olz, int sx, int sy, int sz) {
+    // one candidate q, cell offset (ox, oy, oz) + (olx, oly, olz) as double-float pairs:
+    // screen = the two FP32 tests (within max_rcut, within the pair's cut-off, both with a
+    // 1e-4 margin); measure = the rest for a candidate that passed (re-measure, the exact
+    // decision, the force, the record).  (sx, sy, sz): the stencil's wrap shifts, used by
+    // the FP64 re-decision.
+    auto screen = [&](int q, float ox, float oy, float oz) {
         const IkPRec o = prec[q];
         float bx = ox + (o.x - me.x), by = oy + (o.y - me.y), bz = DIM == 3 ? oz + (o.z - me.z) : 0.f;
         if (allx) bx -= L0 * rintf(bx / L0);
         if (ally) by -= L1 * rintf(by / L1);
         if (allz) bz -= L2 * rintf(bz / L2);
-        float r2 = bx * bx + by * by + bz * bz;
-        if (!(r2 < mr2 * screen)) return;
+        const float r2 = bx * bx + by * by + bz * bz;
+        if (!(r2 < mr2 * screen_f)) return false;
         const float dj = diam32[q];
         const float sig = 0.5f * (di + dj) * (1.f - eps * fabsf(di - dj));
         const float s2 = sig * sig;
-        if (!(r2 < rc2 * s2 * screen)) return;
+        return r2 < rc2 * s2 * screen_f;
+    };
+    auto measure = [&](int q, float ox, float olx, float oy, float oly, float oz, float olz, int sx, int sy, int sz) {
+        const IkPRec o = prec[q];
+        const float dj = diam32[q];
+        const float sig = 0.5f * (di + dj) * (1.f - eps * fabsf(di - dj));
+        const float s2 = sig * sig;
+        float bx, by, bz = 0.f;
         if (!(allx || ally || allz)) {
             const float4 lq = plo[q];
             bx = ik_df_diff(ox, olx, o.x, lq.x, me.x, mlo.x);
@@ -264,7 +278,7 @@ __device__ __forceinline__ int ik_bonds32_particle(const IkGeom& g, const IkPot&
                 bz = (float)dz;
             }
         }
-        r2 = bx * bx + by * by + bz * bz;
+        const float r2 = bx * bx + by * by + bz * bz;
         const float rt = rc2 * s2;
         bool act = r2 < mr2 && r2 < rt;
         if (fabsf(r2 - rt) <= 2e-5f * rt || fabsf(r2 - mr2) <= 2e-5f * mr2) { // at a cut-off: FP64
@@ -296,13 +310,33 @@ __device__ __forceinline__ int ik_bonds32_particle(const IkGeom& g, const IkPot&
                     const int cell = (wz * g.nc[1] + wy) * g.nc[0] + wx;
                     const int qe = cell_start[cell + 1];
                     for (int q = cell_start[cell]; q < qe; ++q)
-                        if (q != p) visit(q, ox, olx, oy, oly, oz, olz, 0, 0, 0);
+                        if (q != p && screen(q, ox, oy, oz)) measure(q, ox, olx, oy, oly, oz, olz, 0, 0, 0);
                 }
             }
         }
     } else {
-        // every axis has one cell (len 1) or at least three (len 3, distinct cells)
+        // every axis has one cell (len 1) or at least three (len 3, distinct cells).
+        // Two passes so that the costly part runs with the lanes busy: the screen of every
+        // candidate first, its survivors (≈ 6 of ≈ 37 in the headline workload) queued in
+        // this thread's column of shared memory as (index, cell offset code), then the
+        // measurement of the queued ones in candidate order (the records' order is the
+        // same as measuring each one where it is found).
         const int nx = g.nc[0], hx = home[0];
+        const int ny = g.nc[1], hy = home[1], nz = g.nc[2], hz = home[2];
+        int ns = 0;
+        auto drain = [&]() {
+            for (int t = 0; t < ns; ++t) {
+                const int q = qidx[t * qstride];
+                const int code = qcode[t * qstride];
+                const int kx = code % 3 - 1, ky = code / 3 % 3 - 1, kz = code / 9 - 1;
+                const float kxf = (float)kx, kyf = (float)ky, kzf = (float)kz;
+                const int ux = hx + kx, uy = hy + ky, uz = hz + kz;
+                measure(q, kxf * g.cwhi[0], kxf * g.cwlo[0], kyf * g.cwhi[1], kyf * g.cwlo[1],
+                        DIM == 3 ? kzf * g.cwhi[2] : 0.f, DIM == 3 ? kzf * g.cwlo[2] : 0.f, (ux >= nx) - (ux < 0),
+                        (uy >= ny) - (uy < 0), DIM == 3 ? (uz >= nz) - (uz < 0) : 0);
+            }
+            ns = 0;
+        };
         // the row's cells in stencil order as one or two runs of consecutive x:
         // run 0 = [xa0, xb0] starting at x offset ka0, run 1 = [xa1, xb1] (empty: xb1 < xa1)
         int xa0, xb0, ka0, xa1, xb1, ka1;
@@ -312,17 +346,16 @@ __device__ __forceinline__ int ik_bonds32_particle(const IkGeom& g, const IkPot&
         else { xa0 = hx - 1; xb0 = hx + 1; ka0 = -1; xa1 = 1; xb1 = 0; ka1 = 0; }
         for (int iz = 0; iz < len[2]; ++iz) {
             const int uz = lo[2] + iz;
-            const int wz = DIM == 3 ? (uz < 0 ? uz + g.nc[2] : (uz >= g.nc[2] ? uz - g.nc[2] : uz)) : 0;
-            const float kz = (float)(uz - home[2]);
-            const float oz = DIM == 3 ? kz * g.cwhi[2] : 0.f, olz = DIM == 3 ? kz * g.cwlo[2] : 0.f;
-            const int sz = DIM == 3 ? (uz > wz) - (uz < wz) : 0;
+            const int wz = DIM == 3 ? (uz < 0 ? uz + nz : (uz >= nz ? uz - nz : uz)) : 0;
+            const float kz = (float)(uz - hz);
+            const float oz = DIM == 3 ? kz * g.cwhi[2] : 0.f;
             for (int iy = 0; iy < len[1]; ++iy) {
                 const int uy = lo[1] + iy;
-                const int wy = uy < 0 ? uy + g.nc[1] : (uy >= g.nc[1] ? uy - g.nc[1] : uy);
-                const float ky = (float)(uy - home[1]);
-                const float oy = ky * g.cwhi[1], oly = ky * g.cwlo[1];
-                const int sy = (uy > wy) - (uy < wy);
-                const int* rs = cell_start + (wz * g.nc[1] + wy) * nx;
+                const int wy = uy < 0 ? uy + ny : (uy >= ny ? uy - ny : uy);
+                const float ky = (float)(uy - hy);
+                const float oy = ky * g.cwhi[1];
+                const int row_code = 3 * (uy - hy + 1) + 9 * (uz - hz + 1) + 1; // + kx
+                const int* rs = cell_start + (wz * ny + wy) * nx;
 #pragma unroll
                 for (int run = 0; run < 2; ++run) {
                     const int xa = run ? xa1 : xa0, xb = run ? xb1 : xb0, ka = run ? ka1 : ka0;
@@ -336,12 +369,16 @@ __device__ __forceinline__ int ik_bonds32_particle(const IkGeom& g, const IkPot&
                         // the candidate cell's x offset (-1, 0 or 1: exactly the float the
                         // cell-by-cell walk converts)
                         const float kxf = kaf + (q >= b1 ? 1.f : 0.f) + (q >= b2 ? 1.f : 0.f);
-                        const int ux = hx + (int)kxf;
-                        visit(q, kxf * g.cwhi[0], kxf * g.cwlo[0], oy, oly, oz, olz, (ux >= nx) - (ux < 0), sy, sz);
+                        if (screen(q, kxf * g.cwhi[0], oy, oz)) {
+                            qidx[ns * qstride] = q;
+                            qcode[ns * qstride] = (unsigned char)(row_code + (int)kxf);
+                            if (++ns == IK_BOND_QUEUE) drain();
+                        }
                     }
                 }
             }
         }
+        drain();
     }
     nb[p] = cnt < maxb ? cnt : maxb;
     if (cnt > maxb) { // rare: grow the capacity and recompute (host side)
