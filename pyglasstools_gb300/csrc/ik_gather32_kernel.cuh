@@ -19,10 +19,11 @@
 //     every full batch of 32 slots is processed with all lanes busy: per slot, the
 //     bond integral by symmetric Gauss-Legendre for each grid point of the group;
 //   * accumulation: every lane sums its slots of a group in FP32 (optionally with
-//     Kahan compensation); the 32 lane partials are combined with error-free
-//     transformations (TwoSum) in a transposing butterfly -- each shuffle level halves
-//     the values a lane holds -- and the compensated result is written as a
-//     double-float pair (hi, lo), converted to FP64 and scaled by k_pairs_to_f64;
+//     Kahan compensation); the 32 lane partials of the virial are combined with
+//     error-free transformations (TwoSum) in a transposing butterfly -- each shuffle
+//     level halves the values a lane holds -- those of the kinetic term (a few kernel
+//     values per lane) with plain adds, and the result is kept as a double-float pair
+//     (hi, lo) between the chunks of an item and written as FP64 on its last chunk;
 //   * quadrature modes (QM): 0 the fixed-point rule; 1 surrogate mode: a bond whose far
 //     end r_j lies outside the support becomes a record {M, m.h, |h|^2, B_fixed} +
 //     {grid point, bond} for the learned surrogate (ik_mlp.cu) instead of a term of the
@@ -802,27 +803,31 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                             if (DIM == 3) k1 = __ldg(a.kin + 2 * q + 1);
                         }
                         // inside: r2 - R2s < 0 (the sign of an exact-zero-free difference);
-                        // band: (r2 - R2s)^2 < margin^2.  Padding points sit at 1e18: never
-                        // inside, never in the band.
-                        float r2v[P];
+                        // band: |r2 - R2s| < margin, looked at only when the closest of the
+                        // group's differences is that small.  Padding points sit at 1e18:
+                        // never inside, never in the band.
+                        float r2v[P], dv[P];
                         int band = 0;
                         {
                             const f32x2 sx = pk2(sp.x, sp.x), sy = pk2(sp.y, sp.y), sz = pk2(sp.z, sp.z);
-                            const f32x2 R2p = pk2(R2s, R2s), nM2 = pk2(-margin * margin, -margin * margin);
+                            const f32x2 R2p = pk2(R2s, R2s);
 #pragma unroll
                             for (int j = 0; j < P / 2; ++j) {
                                 const f32x2 dx = sub2(g2[j][0], sx), dy = sub2(g2[j][1], sy);
                                 f32x2 r2 = fma2(dy, dy, mul2(dx, dx));
                                 if (DIM == 3) { const f32x2 dz = sub2(g2[j][2], sz); r2 = fma2(dz, dz, r2); }
                                 up2(r2, r2v[2 * j], r2v[2 * j + 1]);
-                                const f32x2 d = sub2(r2, R2p);
-                                const f32x2 bd = fma2(d, d, nM2);
-                                float d0, d1, b0, b1;
-                                up2(d, d0, d1);
-                                up2(bd, b0, b1);
-                                mask |= (int)((__float_as_uint(d0) >> 31) | ((__float_as_uint(d1) >> 31) << 1)) << (2 * j);
-                                band |= (int)((__float_as_uint(b0) >> 31) | ((__float_as_uint(b1) >> 31) << 1)) << (2 * j);
+                                up2(sub2(r2, R2p), dv[2 * j], dv[2 * j + 1]);
+                                mask |= (int)((__float_as_uint(dv[2 * j]) >> 31) | ((__float_as_uint(dv[2 * j + 1]) >> 31) << 1))
+                                        << (2 * j);
                             }
+                        }
+                        float dmin = fabsf(dv[0]);
+#pragma unroll
+                        for (int p = 1; p < P; ++p) dmin = fminf(dmin, fabsf(dv[p]));
+                        if (dmin < margin) {
+#pragma unroll
+                            for (int p = 0; p < P; ++p) band |= fabsf(dv[p]) < margin ? (1 << p) : 0;
                         }
                         if (band) { // rare: inside the thin band around R decide with the FP64 rule
                             const IkB64 pq = a.pos64[q];
@@ -925,9 +930,11 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                     }
 #pragma unroll
                 for (int k = P * NC; k < VH; ++k) { vh[k] = vl[k] = kh[k] = kl[k] = 0.f; }
-                if constexpr (KAHAN) { // compensated lanes: compensated combination too
+                if constexpr (KAHAN) { // compensated lanes: compensated combination of the virial
                     ik_warp_reduce_cmp<VH>(vh, vl, lane);
-                    ik_warp_reduce_cmp<VH>(kh, kl, lane);
+                    // the kinetic partials are plain per-lane sums of ~4 terms (one
+                    // kernel value per particle): their combination stays plain
+                    ik_warp_reduce_plain<VH>(kh, lane);
                 } else {
                     ik_warp_reduce_plain<VH>(vh, lane);
                     ik_warp_reduce_plain<VH>(kh, lane);
