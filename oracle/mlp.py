@@ -159,15 +159,17 @@ def value(feats, y):
 
 def forward_bf16(p, feats):
     """y of the deployed network: BF16 weights; the first layer split three ways
-    (x_hi W_hi + x_lo W_hi + x_hi W_lo); BF16 activations; FP64 accumulation; tanh-form
+    (x_hi W_hi + x_lo W_hi + x_hi W_lo); hidden-layer biases as the BF16 pair
+    hi + lo that the tensor cores add; BF16 activations; FP64 accumulation; tanh-form
     SiLU."""
     W1, b1, W2, b2, W3, b3, w4, b4 = split(p)
     silu = lambda z: 0.5 * z + 0.5 * z * np.tanh(0.5 * z)
+    bpair = lambda b: bf16(b) + bf16(b - bf16(b))
     x = inputs(feats)
     xh, W1h = bf16(x), bf16(W1)
     xl, W1l = bf16(x - xh), bf16(W1 - W1h)
-    z1 = xh @ W1h.T + xl @ W1h.T + xh @ W1l.T + b1
+    z1 = xh @ W1h.T + xl @ W1h.T + xh @ W1l.T + bpair(b1)
     h = bf16(silu(z1))
-    h = bf16(silu(h @ bf16(W2).T + b2))
-    h = silu(h @ bf16(W3).T + b3)
+    h = bf16(silu(h @ bf16(W2).T + bpair(b2)))
+    h = silu(h @ bf16(W3).T + bpair(b3))
     return h @ bf16(w4) + b4

@@ -60,11 +60,17 @@ constexpr double MLP_BASE_MIN = 1e-6;       // targets are 0 below this baseline
 constexpr double GL4X0 = 0.33998104358485626480, GL4X1 = 0.86113631159405257522;
 constexpr double GL4W0 = 0.65214515486254614263, GL4W1 = 0.34785484513745385737;
 
-// deployed blob (bytes): BF16 operand tiles in the no-swizzle K-major layout, then FP32
+// deployed blob (bytes): BF16 operand tiles in the no-swizzle K-major layout, then FP32.
+// The hidden layers' biases ride on the tensor cores: the input operand carries 1.0 in
+// its columns 12 and 13, and each bias enters as a BF16 pair (hi, lo) in columns 12 and 13
+// of a B operand -- of W1 itself for the first layer, of a 64 x 16 bias tile (zero
+// elsewhere) multiplied by the same input operand for the other two.
 constexpr int DB_W1 = 0;                   // 64 x 16 bf16 (K padded from 4)  2048 B
 constexpr int DB_W2 = DB_W1 + 64 * 16 * 2; // 64 x 64 bf16                     8192 B
 constexpr int DB_W3 = DB_W2 + 64 * 64 * 2; // 64 x 64 bf16                     8192 B
-constexpr int DB_F = DB_W3 + 64 * 64 * 2;  // floats: b1, b2, b3 (64 each), w4 (64, bf16-rounded), b4
+constexpr int DB_B2 = DB_W3 + 64 * 64 * 2; // 64 x 16 bf16 bias tile of layer 2  2048 B
+constexpr int DB_B3 = DB_B2 + 64 * 16 * 2; // 64 x 16 bf16 bias tile of layer 3  2048 B
+constexpr int DB_F = DB_B3 + 64 * 16 * 2;  // floats: b1, b2, b3 (64 each), w4 (64, bf16-rounded), b4
 constexpr int DB_NF = 4 * 64 + 1;
 constexpr int DB_BYTES = (DB_F + DB_NF * 4 + 15) / 16 * 16;
 
@@ -465,17 +471,29 @@ __host__ __device__ inline int op_off(int r, int k, int K)
     return (r >> 3) * (K / 8) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
 }
 
+// A bias as the BF16 pair (hi, lo) that the tensor cores add (hi + lo = b to ~2^-17).
+__device__ __forceinline__ float bias_hi(float b) { return bf16r(b); }
+__device__ __forceinline__ float bias_lo(float b) { return bf16r(b - bf16r(b)); }
+
 __global__ void k_mlp_deploy(const float* P, unsigned char* blob)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     // hidden layers prescaled by 1/2 (exact), so that the accumulators hold h = z/2 and
     // SiLU(z) = h + h tanh(h)
-    if (i < 64 * 16) { // W1 as [hi | hi | lo | 0] against inputs [x_hi | x_lo | x_hi | 0]
+    if (i < 64 * 16) { // W1 as [hi | hi | lo | b1 hi, b1 lo, 0, 0] against inputs
+                       // [x_hi | x_lo | x_hi | 1, 1, 0, 0]
         const int n = i / 16, k = i % 16, j = k & 3;
         const float w = 0.5f * P[O_W1 + n * 4 + j];
         const float hi = bf16r(w);
-        const float v = k < 8 ? hi : (k < 12 ? w - hi : 0.f);
+        const float b1 = 0.5f * P[O_B1 + n];
+        const float v = k < 8 ? hi : (k < 12 ? w - hi : (k == 12 ? bias_hi(b1) : (k == 13 ? bias_lo(b1) : 0.f)));
         *reinterpret_cast<__nv_bfloat16*>(blob + DB_W1 + op_off(n, k, 16)) = __float2bfloat16_rn(v);
+        // bias tiles of layers 2 and 3: (hi, lo) in columns 12 and 13, zero elsewhere
+        const float b2 = 0.5f * P[O_B2 + n], b3 = 0.5f * P[O_B3 + n];
+        const float v2 = k == 12 ? bias_hi(b2) : (k == 13 ? bias_lo(b2) : 0.f);
+        const float v3 = k == 12 ? bias_hi(b3) : (k == 13 ? bias_lo(b3) : 0.f);
+        *reinterpret_cast<__nv_bfloat16*>(blob + DB_B2 + op_off(n, k, 16)) = __float2bfloat16_rn(v2);
+        *reinterpret_cast<__nv_bfloat16*>(blob + DB_B3 + op_off(n, k, 16)) = __float2bfloat16_rn(v3);
     }
     if (i < 64 * 64) {
         const int n = i / 64, k = i % 64;
@@ -515,6 +533,8 @@ __global__ void k_mlp_infer_simt(const float* P, const float4* feats, long long 
     // BF16 split of the first layer (x_hi W_hi + x_lo W_hi + x_hi W_lo); BF16 weights and
     // activations elsewhere
     auto P2 = [&](float v) { return q ? bf16r(v) : v; };
+    // hidden-layer biases as the tensor cores add them: hi + lo of the prescaled bias b/2
+    auto Bq = [&](float b) { return q ? 2.0f * (bias_hi(0.5f * b) + bias_lo(0.5f * b)) : b; };
     for (int nn = 0; nn < 64; ++nn) {
         float z = 0.f;
         for (int k = 0; k < 4; ++k) {
@@ -528,14 +548,14 @@ __global__ void k_mlp_infer_simt(const float* P, const float4* feats, long long 
                 z = fmaf(w, x[k], z);
             }
         }
-        h[nn] = P2(S(z + P[O_B1 + nn]));
+        h[nn] = P2(S(z + Bq(P[O_B1 + nn])));
     }
     for (int layer = 0; layer < 2; ++layer) {
         const int ow = layer == 0 ? O_W2 : O_W3, ob = layer == 0 ? O_B2 : O_B3;
         for (int nn = 0; nn < 64; ++nn) {
             float z = 0.f;
             for (int k = 0; k < 64; ++k) z = fmaf(R(P[ow + nn * 64 + k]), h[k], z);
-            g[nn] = z + P[ob + nn];
+            g[nn] = z + Bq(P[ob + nn]);
         }
         for (int nn = 0; nn < 64; ++nn) h[nn] = layer == 0 ? P2(S(g[nn])) : S(g[nn]);
     }
@@ -632,6 +652,24 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
 #pragma unroll
     for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
 }
+// packed FP32 pairs (f32x2 arithmetic): two columns of a row per instruction
+typedef unsigned long long mlp_f2;
+__device__ __forceinline__ mlp_f2 mlp_pk2(float a, float b)
+{
+    mlp_f2 r;
+    asm("mov.b64 %0, {%1,%2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void mlp_up2(mlp_f2 r, float& a, float& b)
+{
+    asm("mov.b64 {%0,%1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ mlp_f2 mlp_fma2(mlp_f2 a, mlp_f2 b, mlp_f2 c)
+{
+    mlp_f2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
 __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi)
 {
     __nv_bfloat162 p = __floats2bfloat162_rn(lo, hi);
@@ -724,7 +762,8 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
     const uint32_t tl = tmem + ((uint32_t)(32 * warp) << 16); // this warp's TMEM lanes
     const float* F = reinterpret_cast<const float*>(sW + (DB_F));
     const uint32_t aA0 = smem_u32(sA0), aH = smem_u32(sH), aW1 = smem_u32(sW + DB_W1),
-                   aW2 = smem_u32(sW + DB_W2), aW3 = smem_u32(sW + DB_W3), aBar = smem_u32(bar);
+                   aW2 = smem_u32(sW + DB_W2), aW3 = smem_u32(sW + DB_W3), aB2 = smem_u32(sW + DB_B2),
+                   aB3 = smem_u32(sW + DB_B3), aBar = smem_u32(bar);
     constexpr uint32_t ID = idesc_bf16(128, 64);
     uint32_t phase = 0;
 
@@ -772,14 +811,15 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
             base = 0.5f * s1 * sum;
         }
         {
-            // inputs as [x_hi | x_lo | x_hi | 0] against W1 as [hi | hi | lo | 0]
+            // inputs as [x_hi | x_lo | x_hi | 1, 1, 0, 0] against W1 as [hi | hi | lo | b1 hi,
+            // b1 lo, 0, 0]; the ones also multiply the bias tiles of layers 2 and 3
             float x[4], xl[4];
             mlp_inputs(fd, fa, fb, fw, x);
 #pragma unroll
             for (int k = 0; k < 4; ++k) { const float hi = bf16r(x[k]); xl[k] = x[k] - hi; x[k] = hi; }
             const uint4 c0 = make_uint4(pack_bf16x2(x[0], x[1]), pack_bf16x2(x[2], x[3]),
                                         pack_bf16x2(xl[0], xl[1]), pack_bf16x2(xl[2], xl[3]));
-            const uint4 c1 = make_uint4(pack_bf16x2(x[0], x[1]), pack_bf16x2(x[2], x[3]), 0u, 0u);
+            const uint4 c1 = make_uint4(pack_bf16x2(x[0], x[1]), pack_bf16x2(x[2], x[3]), pack_bf16x2(1.0f, 1.0f), 0u);
             *reinterpret_cast<uint4*>(sA0 + op_off(t, 0, 16)) = c0;
             *reinterpret_cast<uint4*>(sA0 + op_off(t, 8, 16)) = c1;
         }
@@ -794,12 +834,14 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
                 if (layer == 0) {
                     umma_bf16(tmem, umma_desc(aA0, 128, 256), umma_desc(aW1, 128, 256), ID, 0u);
                 } else {
-                    // h (K = 64) against W: four MMAs of K = 16
-                    const uint32_t aw = layer == 1 ? aW2 : aW3;
+                    // h (K = 64) against W: four MMAs of K = 16; then the bias: the input
+                    // operand's ones against the layer's bias tile
+                    const uint32_t aw = layer == 1 ? aW2 : aW3, ab = layer == 1 ? aB2 : aB3;
 #pragma unroll
                     for (int kk = 0; kk < 4; ++kk)
                         umma_bf16(tmem, umma_desc(aH + kk * 256, 128, 1024), umma_desc(aw + kk * 256, 128, 1024), ID,
                                   kk > 0 ? 1u : 0u);
+                    umma_bf16(tmem, umma_desc(aA0, 128, 256), umma_desc(ab, 128, 256), ID, 1u);
                 }
                 umma_commit(aBar);
             }
@@ -809,19 +851,20 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
             }
             phase ^= 1u;
             fence_after();
-            const float* bias = F + 64 * layer;
             if (layer < 2) {
-                // bias + SiLU -> BF16 operand of the next layer (own row)
+                // SiLU -> BF16 operand of the next layer (own row); the accumulators hold
+                // h = z/2 with the bias (prescaled weights), SiLU = h + h tanh(h), two
+                // columns per packed FP32 instruction
 #pragma unroll
                 for (int c16 = 0; c16 < 4; ++c16) {
                     float v[16];
                     tmem_ld16(tl + 16 * c16, v);
-                    // h = z/2 (prescaled weights), SiLU = h + h tanh(h), packed to BF16 pairs
                     uint32_t ph[8];
 #pragma unroll
                     for (int k = 0; k < 16; k += 2) {
-                        const float h0 = v[k] + bias[16 * c16 + k], h1 = v[k + 1] + bias[16 * c16 + k + 1];
-                        const float a0 = fmaf(h0, tanh_approx(h0), h0), a1 = fmaf(h1, tanh_approx(h1), h1);
+                        const mlp_f2 h2 = mlp_pk2(v[k], v[k + 1]);
+                        float a0, a1;
+                        mlp_up2(mlp_fma2(h2, mlp_pk2(tanh_approx(v[k]), tanh_approx(v[k + 1])), h2), a0, a1);
                         ph[k / 2] = pack_bf16x2(a0, a1);
                     }
 #pragma unroll
@@ -836,18 +879,26 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
                 __syncthreads();
                 if (*abort_flag) break;
             } else {
-                // output layer on the CUDA cores: y = w4 . silu(z3 + b3) + b4 (w4 in BF16)
-                float y = F[256];
+                // output layer on the CUDA cores: y = w4 . silu(z3 + b3) + b4 (w4 in BF16,
+                // SiLU in FP32), column pairs in packed FP32
+                mlp_f2 y2 = mlp_pk2(0.f, 0.f);
 #pragma unroll
                 for (int c16 = 0; c16 < 4; ++c16) {
                     float v[16];
                     tmem_ld16(tl + 16 * c16, v);
 #pragma unroll
-                    for (int k = 0; k < 16; ++k) {
-                        const float h = v[k] + bias[16 * c16 + k];
-                        y = fmaf(F[192 + 16 * c16 + k], fmaf(h, tanh_approx(h), h), y);
+                    for (int k = 0; k < 16; k += 4) {
+                        const float4 w4 = *reinterpret_cast<const float4*>(F + 192 + 16 * c16 + k);
+                        const mlp_f2 h2 = mlp_pk2(v[k], v[k + 1]), g2 = mlp_pk2(v[k + 2], v[k + 3]);
+                        const mlp_f2 s2 = mlp_fma2(h2, mlp_pk2(tanh_approx(v[k]), tanh_approx(v[k + 1])), h2);
+                        const mlp_f2 t2 = mlp_fma2(g2, mlp_pk2(tanh_approx(v[k + 2]), tanh_approx(v[k + 3])), g2);
+                        y2 = mlp_fma2(s2, mlp_pk2(w4.x, w4.y), y2);
+                        y2 = mlp_fma2(t2, mlp_pk2(w4.z, w4.w), y2);
                     }
                 }
+                float ya, yb;
+                mlp_up2(y2, ya, yb);
+                const float y = F[256] + (ya + yb);
                 fence_before();
                 const float Bs = base * fmaf(y, MLP_YINV, 1.0f);
                 bool fell_back = false;
