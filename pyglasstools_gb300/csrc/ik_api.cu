@@ -786,7 +786,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
             CK(launch_mlp_records(c->mlp, L.mlp_rec.as<float4>(), L.mlp_rid.as<int2>(),
                                   L.mlp_count.as<unsigned long long>(), c->mlp_cap, bonds,
                                   (float)to_w, (float)c->cg.width, NC, L.corr.as<unsigned long long>(),
-                                  cnt + 4, c->status.as<int>(), c->sm_count * 4, L.st));
+                                  cnt + 4, c->status.as<int>(), c->sm_count * mlp_tc_ctas_per_sm(), L.st));
             c->launches += 1;
         }
         // FP64 finish: ((double)hi + (double)lo) * normalisation (0.5 of the GL map for the

@@ -222,6 +222,7 @@ cudaError_t launch_mlp_records(ik_mlp* m, const float4* rec, const int2* rid, co
                                long long capacity, const float4* bonds, float to_w, float w, int nc,
                                unsigned long long* corr, unsigned long long* fallbacks, int* status, int blocks,
                                cudaStream_t st);
+int mlp_tc_ctas_per_sm(); // resident CTAs per SM of the tensor-core kernel (its grid: SMs x this)
 
 // ---- shared host helpers (ik_api.cu) -----------------------------------------
 void ik_internal_set_error(const char* msg);

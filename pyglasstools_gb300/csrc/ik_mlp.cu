@@ -670,6 +670,31 @@ __device__ __forceinline__ mlp_f2 mlp_fma2(mlp_f2 a, mlp_f2 b, mlp_f2 c)
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
     return d;
 }
+// 32 lanes x 32 bits, 32 consecutive columns (one wait for twice the columns of tmem_ld16)
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                   "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]),
+                   "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]),
+                   "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
+                 :
+                 : "memory");
+#pragma unroll
+    for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
+}
 __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi)
 {
     __nv_bfloat162 p = __floats2bfloat162_rn(lo, hi);
@@ -683,11 +708,13 @@ constexpr int TC_H = TC_A0 + 128 * 16 * 2;  // 128 x 64 bf16 hidden operand   16
 constexpr int TC_W = TC_H + 128 * 64 * 2;   // deployed blob (W1, W2, W3, floats)
 constexpr int TC_BAR = TC_W + DB_BYTES;  // DB_BYTES is a multiple of 16
 constexpr int TC_SMEM = TC_BAR + 64;
-// About 40 KB of dynamic shared memory per CTA: at most 5 CTAs on an SM (228 KB), so
+// About 44 KB of dynamic shared memory per CTA: at most 5 CTAs on an SM (228 KB), so
 // their TMEM allocations (64 columns each, at most 320 of 512) never wait on one another.
 constexpr int TC_SMEM_LAUNCH = TC_SMEM;
 constexpr int TC_CTAS_PER_SM = 233472 / (TC_SMEM_LAUNCH + 1024);
 static_assert(TC_CTAS_PER_SM >= 4 && TC_CTAS_PER_SM * 64 <= 512, "TMEM columns of the resident CTAs");
+// CTAs of k_mlp_infer_tc resident per SM (shared memory bound): the records launch's grid
+int mlp_tc_ctas_per_sm() { return TC_CTAS_PER_SM; }
 constexpr uint32_t TC_COLS = 64;
 
 // Records of bonds that cross the support, written by the FP32 gather in surrogate
@@ -773,25 +800,44 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
         if (total > R.capacity) total = R.capacity;
     }
     const long long ntiles = (total + 127) / 128;
+    // a row's inputs are loaded one tile ahead, so that their latency hides under the
+    // previous tile's MMAs and epilogues
+    float4 next_f = make_float4(0.f, 0.f, 0.f, 0.f);
+    int2 next_id = make_int2(-1, 0);
+    auto fetch = [&](long long tl_) {
+        const long long r_ = tl_ * 128 + t;
+        next_id = make_int2(-1, 0);
+        if (tl_ < ntiles && r_ < total) {
+            if (MODE == 0) {
+                next_f = feats[r_];
+            } else {
+                next_f = R.rec[r_];
+                next_id = R.rid[r_];
+            }
+        }
+    };
+    fetch(blockIdx.x);
     for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const long long row = tile * 128 + t;
+        const float4 cur_f = next_f;
+        const int2 cur_id = next_id;
+        fetch(tile + gridDim.x);
         bool valid = row < total;
         float fd = 0.f, fa = 0.f, fb = 0.f, fw = R.w, bfix = 0.f;
-        int g = -1, bond = 0, bin = -1;
+        int g = -1, bin = -1;
+        float4 bd = make_float4(0.f, 0.f, 0.f, 0.f); // MODE 1: the bond's record, for the coefficient
+        bool use = false;                           // MODE 1: the bin uses the network
         if (MODE == 0) {
-            if (valid) {
-                const float4 f = feats[row];
-                fd = f.x; fa = f.y; fb = f.z; fw = f.w;
-            }
+            if (valid) { fd = cur_f.x; fa = cur_f.y; fb = cur_f.z; fw = cur_f.w; }
         } else if (valid) {
-            const float4 r = R.rec[row];
-            const int2 id = R.rid[row];
-            g = id.x;
-            bond = id.y;
+            g = cur_id.x;
             valid = g >= 0;
             if (valid) {
-                bin = mlp_record_coords(r, R.to_w, R.w, fd, fa, fb);
-                bfix = r.w;
+                bin = mlp_record_coords(cur_f, R.to_w, R.w, fd, fa, fb);
+                bfix = cur_f.w;
+                // issued now, used after the MMAs
+                bd = __ldg(R.bonds + cur_id.y);
+                use = bin >= 0 && __ldg(R.table + bin) != 0;
             }
         }
         // Gauss-Legendre-4 baseline on the clipped segment (as mlp_base, exp via ex2.approx)
@@ -856,20 +902,20 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
                 // h = z/2 with the bias (prescaled weights), SiLU = h + h tanh(h), two
                 // columns per packed FP32 instruction
 #pragma unroll
-                for (int c16 = 0; c16 < 4; ++c16) {
-                    float v[16];
-                    tmem_ld16(tl + 16 * c16, v);
-                    uint32_t ph[8];
+                for (int c32 = 0; c32 < 2; ++c32) {
+                    float v[32];
+                    tmem_ld32(tl + 32 * c32, v);
+                    uint32_t ph[16];
 #pragma unroll
-                    for (int k = 0; k < 16; k += 2) {
+                    for (int k = 0; k < 32; k += 2) {
                         const mlp_f2 h2 = mlp_pk2(v[k], v[k + 1]);
                         float a0, a1;
                         mlp_up2(mlp_fma2(h2, mlp_pk2(tanh_approx(v[k]), tanh_approx(v[k + 1])), h2), a0, a1);
                         ph[k / 2] = pack_bf16x2(a0, a1);
                     }
 #pragma unroll
-                    for (int h8 = 0; h8 < 2; ++h8) {
-                        const int k0 = 16 * c16 + 8 * h8;
+                    for (int h8 = 0; h8 < 4; ++h8) {
+                        const int k0 = 32 * c32 + 8 * h8;
                         *reinterpret_cast<uint4*>(sH + op_off(t, k0, 64)) =
                             make_uint4(ph[4 * h8], ph[4 * h8 + 1], ph[4 * h8 + 2], ph[4 * h8 + 3]);
                     }
@@ -883,12 +929,12 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
                 // SiLU in FP32), column pairs in packed FP32
                 mlp_f2 y2 = mlp_pk2(0.f, 0.f);
 #pragma unroll
-                for (int c16 = 0; c16 < 4; ++c16) {
-                    float v[16];
-                    tmem_ld16(tl + 16 * c16, v);
+                for (int c32 = 0; c32 < 2; ++c32) {
+                    float v[32];
+                    tmem_ld32(tl + 32 * c32, v);
 #pragma unroll
-                    for (int k = 0; k < 16; k += 4) {
-                        const float4 w4 = *reinterpret_cast<const float4*>(F + 192 + 16 * c16 + k);
+                    for (int k = 0; k < 32; k += 4) {
+                        const float4 w4 = *reinterpret_cast<const float4*>(F + 192 + 32 * c32 + k);
                         const mlp_f2 h2 = mlp_pk2(v[k], v[k + 1]), g2 = mlp_pk2(v[k + 2], v[k + 3]);
                         const mlp_f2 s2 = mlp_fma2(h2, mlp_pk2(tanh_approx(v[k]), tanh_approx(v[k + 1])), h2);
                         const mlp_f2 t2 = mlp_fma2(g2, mlp_pk2(tanh_approx(v[k + 2]), tanh_approx(v[k + 3])), g2);
@@ -906,10 +952,8 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
                     if (valid) out[row] = raw ? y : Bs;
                 } else if (valid) {
                     // the gather's units: B integrates over [-1, 1] (twice the [0, 1] value)
-                    const bool use = bin >= 0 && R.table[bin] != 0;
                     const float Bv = use ? 2.0f * Bs : bfix;
                     fell_back = !use;
-                    const float4 bd = __ldg(R.bonds + bond);
                     const float fx = bd.w * bd.x, fy = bd.w * bd.y;
                     auto add = [&](int c, float coef) {
                         const long long v = __float2ll_rn(Bv * coef * 4294967296.0f);
