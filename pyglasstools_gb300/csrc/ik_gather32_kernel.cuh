@@ -12,7 +12,7 @@
 //   * a work item is a range of grid-point groups inside one spatial bin of bw^dim
 //     cells; the warp stages the bin's halo (particles of the cells within R) into its
 //     private shared memory as scaled, bin-relative FP32 positions;
-//   * a group is IK_P grid points; lanes test 32 staged particles at a time against
+//   * a group is IK_P grid points (2 in the 3D Kahan variants); lanes test 32 staged particles at a time against
 //     the group (FP32, with an FP64 re-check inside a thin band around R so that the
 //     selection equals the FP64 rule), accumulate the kinetic term, and push
 //     (particle, bond, grid mask) slots of accepted particles into a per-warp queue;
@@ -283,7 +283,10 @@ template <int DIM, int KIND, bool KAHAN, int NP, int QM, bool ELA, bool SPLIT, b
 __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
 {
     constexpr int NC = DIM == 2 ? 3 : 6;       // unique tensor components
-    constexpr int P = IK_P;
+    // grid points per group: IK_P, but 2 for the 3D Kahan variants, whose per-lane sums and
+    // compensations of 4 points x 6 components spill (the fused 3D Kahan gather ran 516 ->
+    // 445 us per frame with 2; the plain 3D variants stay at IK_P, where 2 is slower)
+    constexpr int P = (DIM == 3 && KAHAN) ? 2 : IK_P;
     constexpr bool MLPM = QM == 1;
     static_assert(QM < 2 || KIND == 1, "closed-form bond integrals: Gaussian kernel only");
     static_assert(!BATCH || (QM == 0 && !ELA && !SPLIT), "fused batches: fixed-point rule, virial and kinetic");
@@ -324,7 +327,7 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
     // surrogate records: this warp's current chunk [wfill, wend) of the record buffer
     long long wfill = 0, wend = 0;
     unsigned long long my_records = 0;
-    auto emit = [&](int cmask, const float4 (&crec)[IK_P], const int (&gidx)[IK_P], int bidx) {
+    auto emit = [&](int cmask, const float4 (&crec)[P], const int (&gidx)[P], int bidx) {
         const int cnt = __popc(cmask);
         int incl = cnt;
 #pragma unroll
@@ -349,7 +352,7 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
         }
         long long o = wfill + incl - cnt;
 #pragma unroll
-        for (int p = 0; p < IK_P; ++p)
+        for (int p = 0; p < P; ++p)
             if (cmask & (1 << p)) {
                 a.mlp_rec[o] = crec[p];
                 a.mlp_rid[o] = make_int2(gidx[p], bidx);
