@@ -670,31 +670,6 @@ __device__ __forceinline__ mlp_f2 mlp_fma2(mlp_f2 a, mlp_f2 b, mlp_f2 c)
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
     return d;
 }
-// 32 lanes x 32 bits, 32 consecutive columns (one wait for twice the columns of tmem_ld16)
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
-{
-    uint32_t r[32];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr)
-        : "memory");
-    asm volatile("tcgen05.wait::ld.sync.aligned;"
-                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
-                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
-                   "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]),
-                   "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]),
-                   "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
-                 :
-                 : "memory");
-#pragma unroll
-    for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
-}
 __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi)
 {
     __nv_bfloat162 p = __floats2bfloat162_rn(lo, hi);
@@ -702,20 +677,29 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi)
 }
 
 // ---------------------------------------------------------------------------- tcgen05 inference
+// A CTA holds TC_WG warpgroups; each works through its own 128-row tiles (its own input
+// and hidden operands, TMEM columns and completion barrier), and all of them share the
+// deployed weights in shared memory -- more tiles in flight per SM than one tile per CTA.
+#ifndef IK_TC_WG
+#define IK_TC_WG 4
+#endif
+constexpr int TC_WG = IK_TC_WG;
+constexpr int TC_THREADS = 128 * TC_WG;
 // Shared memory layout of k_mlp_infer_tc (bytes, 1024-aligned pieces):
-constexpr int TC_A0 = 0;                    // 128 x 16 bf16 input operand   4096
-constexpr int TC_H = TC_A0 + 128 * 16 * 2;  // 128 x 64 bf16 hidden operand   16384
-constexpr int TC_W = TC_H + 128 * 64 * 2;   // deployed blob (W1, W2, W3, floats)
-constexpr int TC_BAR = TC_W + DB_BYTES;  // DB_BYTES is a multiple of 16
-constexpr int TC_SMEM = TC_BAR + 64;
-// About 44 KB of dynamic shared memory per CTA: at most 5 CTAs on an SM (228 KB), so
-// their TMEM allocations (64 columns each, at most 320 of 512) never wait on one another.
+constexpr int TC_A0 = 0;                              // per warpgroup: 128 x 16 bf16 input operand   4096
+constexpr int TC_H = TC_A0 + TC_WG * 128 * 16 * 2;    // per warpgroup: 128 x 64 bf16 hidden operand  16384
+constexpr int TC_W = TC_H + TC_WG * 128 * 64 * 2;     // deployed blob (W1, W2, W3, bias tiles, floats)
+constexpr int TC_BAR = TC_W + DB_BYTES;  // DB_BYTES is a multiple of 16: one barrier per warpgroup,
+constexpr int TC_SMEM = TC_BAR + 64;     // the TMEM address and the abort flag
+// The CTAs that fit an SM by shared memory (228 KB) hold 64 TMEM columns per warpgroup,
+// at most 512 in all, so their allocations never wait on one another.
 constexpr int TC_SMEM_LAUNCH = TC_SMEM;
 constexpr int TC_CTAS_PER_SM = 233472 / (TC_SMEM_LAUNCH + 1024);
-static_assert(TC_CTAS_PER_SM >= 4 && TC_CTAS_PER_SM * 64 <= 512, "TMEM columns of the resident CTAs");
+static_assert(TC_CTAS_PER_SM >= 1 && TC_CTAS_PER_SM * 64 * TC_WG <= 512, "TMEM columns of the resident CTAs");
+static_assert(8 * TC_WG + 8 <= 64, "barrier area");
 // CTAs of k_mlp_infer_tc resident per SM (shared memory bound): the records launch's grid
 int mlp_tc_ctas_per_sm() { return TC_CTAS_PER_SM; }
-constexpr uint32_t TC_COLS = 64;
+constexpr uint32_t TC_COLS = 64 * TC_WG;
 
 // Records of bonds that cross the support, written by the FP32 gather in surrogate
 // mode: {M, mb, hh, B_fixed} in the gather's scaled units + {grid index, bond index}.
@@ -754,25 +738,29 @@ __device__ __forceinline__ int mlp_record_coords(const float4 r, float to_w, flo
 // stall != 0: the failure-detection test hook (TC_STALL_POLLS).  MODE 0 with raw != 0:
 // out[i] = the network's output y instead of B.
 template <int MODE>
-__global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __restrict__ blob, const float4* feats,
+__global__ void __launch_bounds__(TC_THREADS, TC_CTAS_PER_SM) k_mlp_infer_tc(const unsigned char* __restrict__ blob, const float4* feats,
                                                      long long n, float* out, MlpRecArgs R, int* status, int stall,
                                                      int raw)
 {
     extern __shared__ __align__(1024) unsigned char tsm[];
-    unsigned char* sA0 = tsm + TC_A0;
-    unsigned char* sH = tsm + TC_H;
+    // t: this thread's row of its warpgroup's tile; warp: the warp within the CTA
+    const int tid = threadIdx.x, wg = tid >> 7, t = tid & 127, warp = tid >> 5;
+    unsigned char* sA0 = tsm + TC_A0 + wg * (128 * 16 * 2);
+    unsigned char* sH = tsm + TC_H + wg * (128 * 64 * 2);
     unsigned char* sW = tsm + TC_W;
-    unsigned long long* bar = reinterpret_cast<unsigned long long*>(tsm + TC_BAR);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(tsm + TC_BAR + 8);
-    int* abort_flag = reinterpret_cast<int*>(tsm + TC_BAR + 16);
-    const int t = threadIdx.x, warp = t >> 5;
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(tsm + TC_BAR) + wg;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(tsm + TC_BAR + 8 * TC_WG);
+    int* abort_flag = reinterpret_cast<int*>(tsm + TC_BAR + 8 * TC_WG + 4);
+    // the warpgroup's own barrier (named barrier wg + 1; 0 is __syncthreads)
+    auto wg_sync = [&]() { asm volatile("bar.sync %0, 128;" ::"r"(wg + 1) : "memory"); };
 
-    // stage the deployed weights; zero the input operand (columns 4..15 stay zero)
-    for (int k = t; k < DB_BYTES / 16; k += 128)
+    // stage the deployed weights; zero the input operands (columns 4..15 stay zero)
+    for (int k = tid; k < DB_BYTES / 16; k += TC_THREADS)
         reinterpret_cast<uint4*>(sW)[k] = reinterpret_cast<const uint4*>(blob)[k];
-    for (int k = t; k < 128 * 16 * 2 / 16; k += 128) reinterpret_cast<uint4*>(sA0)[k] = make_uint4(0, 0, 0, 0);
-    if (t == 0) {
-        mbar_init(smem_u32(bar), 1);
+    for (int k = tid; k < TC_WG * 128 * 16 * 2 / 16; k += TC_THREADS)
+        reinterpret_cast<uint4*>(tsm + TC_A0)[k] = make_uint4(0, 0, 0, 0);
+    if (tid == 0) {
+        for (int w = 0; w < TC_WG; ++w) mbar_init(smem_u32(reinterpret_cast<unsigned long long*>(tsm + TC_BAR) + w), 1);
         *abort_flag = 0;
     }
     if (warp == 0) {
@@ -785,8 +773,9 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
     fence_before();
     __syncthreads();
     fence_after();
-    const uint32_t tmem = *tslot;
-    const uint32_t tl = tmem + ((uint32_t)(32 * warp) << 16); // this warp's TMEM lanes
+    const uint32_t tmem_base = *tslot;
+    const uint32_t tmem = tmem_base + 64u * (uint32_t)wg;        // the warpgroup's columns
+    const uint32_t tl = tmem + ((uint32_t)(32 * (warp & 3)) << 16); // this warp's TMEM lanes
     const float* F = reinterpret_cast<const float*>(sW + (DB_F));
     const uint32_t aA0 = smem_u32(sA0), aH = smem_u32(sH), aW1 = smem_u32(sW + DB_W1),
                    aW2 = smem_u32(sW + DB_W2), aW3 = smem_u32(sW + DB_W3), aB2 = smem_u32(sW + DB_B2),
@@ -816,12 +805,13 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
             }
         }
     };
-    fetch(blockIdx.x);
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const long long tile0 = (long long)blockIdx.x * TC_WG + wg, tstep = (long long)gridDim.x * TC_WG;
+    fetch(tile0);
+    for (long long tile = tile0; tile < ntiles; tile += tstep) {
         const long long row = tile * 128 + t;
         const float4 cur_f = next_f;
         const int2 cur_id = next_id;
-        fetch(tile + gridDim.x);
+        fetch(tile + tstep);
         bool valid = row < total;
         float fd = 0.f, fa = 0.f, fb = 0.f, fw = R.w, bfix = 0.f;
         int g = -1, bin = -1;
@@ -871,7 +861,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
         }
         fence_async_smem();
         fence_before();
-        __syncthreads();
+        wg_sync();
         if (*abort_flag) break;
 #pragma unroll 1
         for (int layer = 0; layer < 3; ++layer) {
@@ -902,39 +892,39 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
                 // h = z/2 with the bias (prescaled weights), SiLU = h + h tanh(h), two
                 // columns per packed FP32 instruction
 #pragma unroll
-                for (int c32 = 0; c32 < 2; ++c32) {
-                    float v[32];
-                    tmem_ld32(tl + 32 * c32, v);
-                    uint32_t ph[16];
+                for (int c16 = 0; c16 < 4; ++c16) {
+                    float v[16];
+                    tmem_ld16(tl + 16 * c16, v);
+                    uint32_t ph[8];
 #pragma unroll
-                    for (int k = 0; k < 32; k += 2) {
+                    for (int k = 0; k < 16; k += 2) {
                         const mlp_f2 h2 = mlp_pk2(v[k], v[k + 1]);
                         float a0, a1;
                         mlp_up2(mlp_fma2(h2, mlp_pk2(tanh_approx(v[k]), tanh_approx(v[k + 1])), h2), a0, a1);
                         ph[k / 2] = pack_bf16x2(a0, a1);
                     }
 #pragma unroll
-                    for (int h8 = 0; h8 < 4; ++h8) {
-                        const int k0 = 32 * c32 + 8 * h8;
+                    for (int h8 = 0; h8 < 2; ++h8) {
+                        const int k0 = 16 * c16 + 8 * h8;
                         *reinterpret_cast<uint4*>(sH + op_off(t, k0, 64)) =
                             make_uint4(ph[4 * h8], ph[4 * h8 + 1], ph[4 * h8 + 2], ph[4 * h8 + 3]);
                     }
                 }
                 fence_async_smem();
                 fence_before();
-                __syncthreads();
+                wg_sync();
                 if (*abort_flag) break;
             } else {
                 // output layer on the CUDA cores: y = w4 . silu(z3 + b3) + b4 (w4 in BF16,
                 // SiLU in FP32), column pairs in packed FP32
                 mlp_f2 y2 = mlp_pk2(0.f, 0.f);
 #pragma unroll
-                for (int c32 = 0; c32 < 2; ++c32) {
-                    float v[32];
-                    tmem_ld32(tl + 32 * c32, v);
+                for (int c16 = 0; c16 < 4; ++c16) {
+                    float v[16];
+                    tmem_ld16(tl + 16 * c16, v);
 #pragma unroll
-                    for (int k = 0; k < 32; k += 4) {
-                        const float4 w4 = *reinterpret_cast<const float4*>(F + 192 + 32 * c32 + k);
+                    for (int k = 0; k < 16; k += 4) {
+                        const float4 w4 = *reinterpret_cast<const float4*>(F + 192 + 16 * c16 + k);
                         const mlp_f2 h2 = mlp_pk2(v[k], v[k + 1]), g2 = mlp_pk2(v[k + 2], v[k + 3]);
                         const mlp_f2 s2 = mlp_fma2(h2, mlp_pk2(tanh_approx(v[k]), tanh_approx(v[k + 1])), h2);
                         const mlp_f2 t2 = mlp_fma2(g2, mlp_pk2(tanh_approx(v[k + 2]), tanh_approx(v[k + 3])), g2);
@@ -983,7 +973,8 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const unsigned char* __res
     __syncthreads();
     if (warp == 0) {
         fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_COLS) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TC_COLS)
+                     : "memory");
     }
 }
 
@@ -1081,9 +1072,10 @@ static int run_tc(ik_mlp* m, long long n, const float4* f, float* out, int raw =
     MCK(cudaMemsetAsync(m->status.p, 0, sizeof(int), m->st));
     MCK(cudaFuncSetAttribute(k_mlp_infer_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_LAUNCH));
     const long long tiles = (n + 127) / 128;
-    const int blocks = (int)std::min<long long>(std::max<long long>(tiles, 1), (long long)m->sm_count * TC_CTAS_PER_SM);
+    const int blocks = (int)std::min<long long>(std::max<long long>((tiles + TC_WG - 1) / TC_WG, 1),
+                                                (long long)m->sm_count * TC_CTAS_PER_SM);
     MlpRecArgs none{};
-    k_mlp_infer_tc<0><<<blocks, 128, TC_SMEM_LAUNCH, m->st>>>(m->blob.as<unsigned char>(), f, n, out, none,
+    k_mlp_infer_tc<0><<<blocks, TC_THREADS, TC_SMEM_LAUNCH, m->st>>>(m->blob.as<unsigned char>(), f, n, out, none,
                                                                m->status.as<int>(), m->stall, raw);
     MCK(cudaGetLastError());
     int st = 0;
@@ -1125,7 +1117,7 @@ cudaError_t launch_mlp_records(ik_mlp* m, const float4* rec, const int2* rid, co
     R.nc = nc;
     R.corr = corr;
     R.fallbacks = fallbacks;
-    k_mlp_infer_tc<1><<<blocks, 128, TC_SMEM_LAUNCH, st>>>(m->blob.as<unsigned char>(), nullptr, 0, nullptr, R,
+    k_mlp_infer_tc<1><<<blocks, TC_THREADS, TC_SMEM_LAUNCH, st>>>(m->blob.as<unsigned char>(), nullptr, 0, nullptr, R,
                                                             status, m->stall, 0);
     return cudaGetLastError();
 }
