@@ -875,7 +875,9 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                     for (int k = 0; k < cnt; ++k) queue[off + k] = entry | (k << 4);
                     qn += tot;
                     __syncwarp();
-                    while (qn >= 64) { // two batches in flight
+                    // two batches in flight; in surrogate mode one at a time: the records of a
+                    // second slot in flight spilled 68 bytes (its gather 192.8 -> 165.8 us per frame)
+                    while (!MLPM && qn >= 64) {
                         const int e1 = queue[qn - 32 + lane], e2 = queue[qn - 64 + lane];
                         qn -= 64;
                         float4 sp1, b1, sp2, b2;
@@ -884,7 +886,7 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                         process_slot(e1, sp1, b1);
                         process_slot(e2, sp2, b2);
                     }
-                    if (qn >= 32) {
+                    while (qn >= 32) { // at most one pass outside surrogate mode (qn < 64 here)
                         qn -= 32;
                         const int e1 = queue[qn + lane];
                         float4 sp1, b1;
