@@ -172,9 +172,18 @@ def test_ik_surrogate_mode_gains_over_fixed_point_rule(ik, oracle, trained):
     exact, _ = oracle.compute(box, fr.pos, fr.diam, oracle.make_poly12(), cg, grid, max_rc=max_rc)
     e_gl = rel_l2(uniq(v_gl), uniq(exact))
     e_net = rel_l2(uniq(v_net), uniq(exact))
-    print(f"field error vs exact bond integral: fixed point GL-5 {e_gl}, surrogate {e_net}")
-    assert np.all(e_net < e_gl / 30)
+    # the comparator: the closed form of the same integral (erf differences, FP32) on the
+    # same crossing bonds.  The network stands in for the quadrature where a kernel has no
+    # closed form; for the Gaussian the closed form is the more accurate route, and the
+    # network stays within a small factor of it
+    v_clip, _, _ = _ik_fields(ik, fr, grid, "clipped")
+    e_clip = rel_l2(uniq(v_clip), uniq(exact))
+    print(f"field error vs exact bond integral: fixed point GL-5 {e_gl}, surrogate {e_net}, "
+          f"closed form on the same bonds {e_clip}")
+    assert np.all(e_net < e_gl / 30)     # what the network gains over the fixed-point rule
     assert np.all(e_net < 1e-5)
+    assert e_clip.max() < e_net.max()    # what it loses against the closed form ...
+    assert e_net.max() < 20 * e_clip.max()  # ... and by how much at most
     # deterministic (fixed-point accumulation of the surrogate's terms)
     v_net2, _, _ = _ik_fields(ik, fr, grid, "mlp", trained)
     np.testing.assert_array_equal(v_net, v_net2)
