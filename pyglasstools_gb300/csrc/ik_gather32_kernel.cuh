@@ -323,7 +323,7 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
     bool cull = DIM == 3 && G.cull;
     const bool want_kin = (a.fields & 2) != 0;
     const int npairs = NP > 0 ? NP : a.npairs;
-    unsigned long long my_pairs = 0, my_triples = 0;
+    unsigned my_pairs = 0, my_triples = 0; // per lane, flushed to the 64-bit counters
     // surrogate records: this warp's current chunk [wfill, wend) of the record buffer
     long long wfill = 0, wend = 0;
     unsigned long long my_records = 0;
@@ -837,7 +837,7 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
 #pragma unroll
                             for (int p = 0; p < P; ++p) {
                                 if (!(band & (1 << p))) continue;
-                                const double* xg = a.grid + 3 * (size_t)gi[p];
+                                const double* xg = a.grid + 3 * (size_t)(MLPM ? gi[p] : __float_as_int(__ldg(&a.gpts[gs + p].w)));
                                 const double ddx = ik_minimg(__dsub_rn(xg[0], pq.x), G.g.L[0], G.g.periodic[0]);
                                 const double ddy = ik_minimg(__dsub_rn(xg[1], pq.y), G.g.L[1], G.g.periodic[1]);
                                 const double ddz = ik_minimg(__dsub_rn(xg[2], pq.z), G.g.L[2], G.g.periodic[2]);
@@ -956,7 +956,11 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                         const int p = idx / NC, c = idx - p * NC;
                         int g = -1;
 #pragma unroll
-                        for (int pp = 0; pp < P; ++pp) if (pp == p) g = gi[pp];
+                        if constexpr (MLPM) {
+                            for (int pp = 0; pp < P; ++pp) if (pp == p) g = gi[pp];
+                        } else { // reloaded: fewer live registers through the group
+                            g = gs + p < gend ? __float_as_int(__ldg(&a.gpts[gs + p].w)) : -1;
+                        }
                         if (g >= 0) {
                             float2* out = kin_here ? a.out_kin : a.out_vir;
                             const size_t o = (size_t)g * NC + c;
