@@ -94,8 +94,10 @@ __global__ void __launch_bounds__(128) k_sort_pack32_batch(const IkBatchSlot* __
     }
 }
 
+// Eight CTAs per SM (64 registers, a few bytes of spill): the bond build waits on its loads,
+// and more resident warps hide that better (fused preparation 21.2 -> 19.4 us per frame).
 template <int DIM, int KIND>
-__global__ void __launch_bounds__(128) k_bonds32t_batch(const IkBatchSlot* __restrict__ S,
+__global__ void __launch_bounds__(128, 8) k_bonds32t_batch(const IkBatchSlot* __restrict__ S,
                                                         const int* __restrict__ p_offs, int nslots, int ptot,
                                                         IkPot pot, IkPotF pf, float kappa,
                                                         const IkPRec* __restrict__ prec,
