@@ -87,6 +87,25 @@ def test_tensor_core_inference_matches_cuda_cores(ik):
     np.testing.assert_allclose(b_tc, M.value(f, tc.astype(np.float64)), rtol=2e-6, atol=5e-8)
 
 
+@pytest.mark.parametrize("n", [1, 37, 129, 513, 4097])
+def test_tensor_core_inference_tile_counts(ik, n):
+    """Row counts that leave warpgroups of a CTA without a tile (1 and 37 rows: one tile for
+    four warpgroups), split tiles across warpgroups and CTAs, and end in ragged tiles: the
+    tensor-core rows equal the CUDA-core BF16 network's to the tolerance above."""
+    with ik.MLP() as m:
+        m.init(seed=9)
+        p = m.get_params()
+        f, _ = m.samples(n, seed=17)
+        tc = m.eval(f, kernel=0, raw=True)
+        simt16 = m.eval(f, kernel=1, raw=True)
+    scale = max(np.max(np.abs(M.forward(p, f))), 1e-6)
+    assert np.all(np.isfinite(tc))
+    d = np.abs(tc - simt16)
+    assert np.max(d) <= 1e-2 * scale
+    if n >= 16:  # a single row can sit on a BF16 rounding boundary
+        assert np.median(d) <= 1e-5 * scale
+
+
 def _gl_bond(f, n=5):
     """The fixed-point rule of the reference (n-point Gauss-Legendre on [0, 1]) in units of w."""
     gx, gw = np.polynomial.legendre.leggauss(n)
