@@ -30,9 +30,10 @@
 //   k_mlp_deploy    FP32 parameters -> BF16 operand tiles in the tensor-core layout;
 //   k_mlp_infer_tc  inference on the 5th-generation tensor cores: per 128-row tile,
 //                   tcgen05.mma (kind::f16, BF16 in, FP32 accumulators in TMEM) for the
-//                   three hidden layers, tcgen05.ld epilogues (bias + SiLU) that write the
-//                   next layer's operand (BF16) back to shared memory; the first layer
-//                   is split three ways (x_hi W_hi + x_lo W_hi + x_hi W_lo);
+//                   three hidden layers with their biases, tcgen05.ld epilogues (SiLU)
+//                   that write the next layer's operand (BF16) back to shared memory; the
+//                   first layer is split three ways (x_hi W_hi + x_lo W_hi + x_hi W_lo);
+//                   four warpgroups per CTA, each through its own tiles, share the weights;
 //   k_mlp_infer_simt the same BF16 arithmetic on the CUDA cores (cross-check), or FP32.
 #include "ik_kernels.h"
 #include "../../include/ik_gb300.h"
