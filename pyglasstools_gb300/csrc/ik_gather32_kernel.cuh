@@ -19,7 +19,8 @@
 //     every full batch of 32 slots is processed with all lanes busy: per slot, the
 //     bond integral by symmetric Gauss-Legendre for each grid point of the group;
 //   * accumulation: every lane sums its slots of a group in FP32 (optionally with
-//     Kahan compensation); the 32 lane partials of the virial are combined with
+//     Kahan compensation, one update per pair of slots in flight: their two products
+//     summed first); the 32 lane partials of the virial are combined with
 //     error-free transformations (TwoSum) in a transposing butterfly -- each shuffle
 //     level halves the values a lane holds -- those of the kinetic term (a few kernel
 //     values per lane) with plain adds, and the result is kept as a double-float pair
@@ -575,7 +576,13 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                     sp = stage[e >> 10];
                     b = __ldg(bonds_w + (__float_as_int(sp.w) >> 6) + ((e >> 4) & 63));
                 };
-                auto process_slot = [&](int e, const float4& sp, const float4& b) {
+                // Kahan lane sums: the two slots in flight are added to the compensated sums
+                // as one term (their products summed first: one Kahan update per pair)
+                constexpr bool PAIRK = KAHAN && NP > 0 && QM == 0 && !ELA;
+                f32x2 pB[PAIRK ? P / 2 : 1], pcf[PAIRK ? NC : 1];
+                // mode 0: accumulate; 1: keep B and the coefficients for the next call;
+                // 2: accumulate together with the kept ones
+                auto process_slot = [&](int e, const float4& sp, const float4& b, int mode = 0) {
                     const int m = e & 15;
                     const float hbx = b.x, hby = b.y, hbz = b.z;
                     const float hh = DIM == 3 ? fmaf(hbz, hbz, fmaf(hby, hby, hbx * hbx)) : fmaf(hby, hby, hbx * hbx);
@@ -618,6 +625,10 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                         for (int t = 0; t < NP; ++t) { const float v = a.xi2[t] * hh; cq2[t] = pk2(v, v); }
 #pragma unroll
                         for (int c = 0; c < NC; ++c) cf2[c] = pk2(cf[c], cf[c]);
+                        if (PAIRK && mode == 1) {
+#pragma unroll
+                            for (int c = 0; c < NC; ++c) pcf[c % (PAIRK ? NC : 1)] = cf2[c];
+                        }
 #pragma unroll
                         for (int j = 0; j < P / 2; ++j) {
                             const f32x2 mx = sub2(g2[j][0], mid2x), my = sub2(g2[j][1], mid2y);
@@ -683,10 +694,13 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                                 }
                             }
                             B = pk2((m & (1 << (2 * j))) ? Ba : 0.f, (m & (2 << (2 * j))) ? Bb : 0.f);
+                            if (PAIRK && mode == 1) { pB[j % (PAIRK ? P / 2 : 1)] = B; continue; }
 #pragma unroll
                             for (int c = 0; c < NC; ++c) {
                                 if constexpr (KAHAN) {
-                                    const f32x2 y = fma2(B, cf2[c], cn2[j][c]);
+                                    const f32x2 y = (PAIRK && mode == 2)
+                                                        ? fma2(B, cf2[c], fma2(pB[j % (PAIRK ? P / 2 : 1)], pcf[c % (PAIRK ? NC : 1)], cn2[j][c]))
+                                                        : fma2(B, cf2[c], cn2[j][c]);
                                     const f32x2 t2 = add2(acc2[j][c], y);
                                     cn2[j][c] = sub2(y, sub2(t2, acc2[j][c]));
                                     acc2[j][c] = t2;
@@ -883,8 +897,8 @@ __global__ void __launch_bounds__(256, 2) k_gather32(const GatherArgs32 a)
                         float4 sp1, b1, sp2, b2;
                         load_slot(e1, sp1, b1);
                         load_slot(e2, sp2, b2);
-                        process_slot(e1, sp1, b1);
-                        process_slot(e2, sp2, b2);
+                        process_slot(e1, sp1, b1, PAIRK ? 1 : 0);
+                        process_slot(e2, sp2, b2, PAIRK ? 2 : 0);
                     }
                     while (qn >= 32) { // at most one pass outside surrogate mode (qn < 64 here)
                         qn -= 32;
