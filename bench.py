@@ -75,6 +75,9 @@ def parse():
     ap.add_argument("--schedule", default="auto", choices=["auto", "fused", "lanes"],
                     help="batch schedule of the headline: chosen by the autotuner (default), or fixed: fused "
                          "(every stage once over the step's frames) or lanes (one launch sequence per frame)")
+    ap.add_argument("--io-batches", type=int, default=-1,
+                    help="schedule of the end-to-end step's copies: 0 per frame on the lanes, n fused sub-batches "
+                         "(default: chosen by the host-I/O autotuner)")
     ap.add_argument("--profile-precision", default="fp32", choices=["fp32", "fp64"],
                     help="with --profile: the path the steps run (fp64 = the plain FP64 gather)")
     return ap.parse_args()
@@ -374,7 +377,9 @@ def uneven_leg(args):
     """256 seeded 2D frames with N log-uniform on [1000, 128000] (density 1, each frame
     its own box and a grid of spacing ~1), Gaussian w = 2 cut at 6: the batch replayed
     as one CUDA graph with the autotuner's bin size and CTAs per SM, against the same
-    frames launched one by one with the default tuning."""
+    frames launched one by one with the default tuning; and end to end from page-locked
+    host frames to host fields, with the host-I/O autotuner's schedule of the copies and
+    with the lanes."""
     import torch
     from pyglasstools_gb300 import ikabi, synth
     rng = np.random.default_rng(2024)
@@ -386,12 +391,16 @@ def uneven_leg(args):
     c.reserve_slots(F)
     c.set_max_rcut(1.25 * 1.62)
     G_total = 0
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    host, outs = [], []  # page-locked host frames and fields of the end-to-end batch
     for k, n in enumerate(Ns):
         f = synth.make_frame(int(n), dim=2, seed=5000 + k)
         grid = synth.lattice_grid(f.L, max(int(f.L), 2), 2)
         G_total += len(grid)
         c.set_slot_geometry(k, 2, [f.L, f.L, 1.0], grid)
         c.upload_frame(k, f.pos, f.diam, f.vel, f.mass)
+        host.append((pin(f.pos), pin(f.diam), pin(f.vel), pin(f.mass)))
+        outs.append((pin(np.zeros((len(grid), 3))), pin(np.zeros((len(grid), 3))), None))
     c.synchronize()
     slots = list(range(F))
     stream = torch.cuda.ExternalStream(c.stream())
@@ -431,6 +440,24 @@ def uneven_leg(args):
     l0 = c.launch_count()
     ms_graph = timed(lambda: c.compute_batch(slots, "fp32"))
     launches = (c.launch_count() - l0) // (reps + 1)
+    # end to end (host frames in, host fields out), the copies' schedule autotuned, and the
+    # lanes beside it: wall time per batch, synchronised
+    io_best = c.autotune_batch_io(slots, host, outs, reps=2)
+
+    def e2e():
+        for _ in range(3):
+            c.compute_batch_io(slots, host, outs)
+            c.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            c.compute_batch_io(slots, host, outs)
+            c.synchronize()
+        return (time.perf_counter() - t0) / reps * 1e3
+
+    ms_e2e = e2e()
+    c.set_tuning("io_batches", 0)
+    c.set_tuning("blocks_per_sm", 0)
+    ms_e2e_lanes = e2e()
     c.close()
     return {"workload": "256 frames, N log-uniform [1000, 128000], own box and grid (spacing ~1), Gaussian w=2 R=6",
             "particles": int(Ns.sum()), "grid_points": int(G_total),
@@ -443,6 +470,11 @@ def uneven_leg(args):
                             "what": "one launch sequence per frame on eight streams, one graph"},
             "graph_autotuned": {"frames_per_s": F / (ms_graph * 1e-3), "ms_per_batch": ms_graph,
                                 "tuning": best, "kernel_launches_per_batch": int(launches)},
+            "e2e_autotuned": {"frames_per_s": F / (ms_e2e * 1e-3), "ms_per_batch": ms_e2e, "tuning": io_best,
+                              "h2d_bytes_per_batch": int(Ns.sum()) * 64, "d2h_bytes_per_batch": int(G_total) * 48,
+                              "what": "host frames in, host fields out, one graph per batch (ik_compute_batch_io)"},
+            "e2e_lanes": {"frames_per_s": F / (ms_e2e_lanes * 1e-3), "ms_per_batch": ms_e2e_lanes,
+                          "what": "the same with each frame's copies and kernels on one of eight lanes"},
             "speedup": ms_plain / ms_graph}
 
 
@@ -607,14 +639,48 @@ def ours(args, wl, name):
             ctx.compute_batch_io(io_slots, io_frames, io_outs)
         ctx.synchronize()
 
-    e2e_step()
-    barrier(world)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_step()
-    t1 = time.perf_counter()
-    e2e_s = max_over_ranks(t1 - t0, world)
-    e2e_value = world * F * args.steps / e2e_s
+    def e2e_run():
+        for _ in range(1 + args.warmup):  # the first call runs the plain path and records the graph
+            e2e_step()
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        t1 = time.perf_counter()
+        return world * F * args.steps / max_over_ranks(t1 - t0, world)
+
+    # the schedule of the copies: per frame on the lanes, or fused sub-batches whose copies
+    # overlap the other sub-batches' computation -- chosen by the host-I/O autotuner (or
+    # --io-batches); the other kind is timed beside it
+    io_tuning = None
+    if args.no_graph:
+        pass
+    elif args.io_batches >= 0:
+        ctx.set_tuning("io_batches", args.io_batches)
+    else:
+        io_tuning = ctx.autotune_batch_io(io_slots, io_frames, io_outs, reps=2)
+    nsub = ctx.get_tuning("io_batches") if not args.no_graph else 0
+    e2e_value = e2e_run()
+    e2e_other, other_desc = None, None
+    if not args.no_graph and ctx.get_tuning("fused_batch"):
+        bps0 = ctx.get_tuning("blocks_per_sm")
+        if nsub:
+            ctx.set_tuning("io_batches", 0)
+            ctx.set_tuning("blocks_per_sm", 0)
+            other_desc = "lanes"
+        else:
+            ctx.set_tuning("io_batches", 8)
+            other_desc = "8 fused sub-batches"
+        e2e_other = e2e_run()
+        ctx.set_tuning("io_batches", nsub)
+        ctx.set_tuning("blocks_per_sm", bps0)
+
+    def io_desc(nb):
+        if nb:
+            return ("%d fused sub-batches of ~%d frames, copies overlapping the other sub-batches' computation"
+                    % (min(nb, F), -(-F // min(nb, F))))
+        return "lanes: each frame's copies and kernels on one of eight streams"
+    e2e_schedule = io_desc(nsub)
     h2d = F * wl["N"] * (3 + 3 + 1 + 1) * 8
     d2h = F * len(grid) * NC * 2 * 8
     clocks.stop()
@@ -705,7 +771,9 @@ def ours(args, wl, name):
            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, shapes of the named config)",
            "config": config_of(name, wl, world),
-           "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+           "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                   "schedule": e2e_schedule, "tuning": io_tuning,
+                   "other_schedule": {"schedule": other_desc, "frames_per_s": e2e_other}},
            "gpu_launches": int(launches),
            "clocks": clocks.summary(t_soak, t_host1),
            "roofline": {"bound": "fp32",

@@ -215,7 +215,11 @@ int ik_get_stream(ik_ctx* ctx, void** stream);
  * out[3k + f] (f = 0 virial, 1 kinetic, 2 elastic; g x NC FP64 as in
  * ik_download_field_async; null = not copied).  The copies and kernels of a frame run on
  * one engine lane, so the uploads, computations and downloads of different frames
- * overlap.  The first call (and any call after a change of slots, sizes, pointers or
+ * overlap; or, with IK_TUNE_IO_BATCHES = n >= 1 and a batch that can run fused (see
+ * IK_TUNE_FUSED_BATCH), the batch runs as n fused sub-batches: one stream uploads the
+ * frames in order, each sub-batch is computed once its frames are on the device, and its
+ * fields are downloaded as soon as it is done, so that the copies of the other
+ * sub-batches overlap its computation.  The first call (and any call after a change of slots, sizes, pointers or
  * settings) runs the plain path and records the graph; later calls replay it, reading the
  * host inputs' current contents.  Outputs are complete after ik_synchronize (which copies
  * them again if a capacity growth re-ran a frame).  Slots must be distinct.  Elastic
@@ -223,6 +227,19 @@ int ik_get_stream(ik_ctx* ctx, void** stream);
 int ik_compute_batch_io(ik_ctx* ctx, const int* slots, int count, int precision, int fields,
                         const int64_t* n, const double* const* pos, const double* const* vel,
                         const double* const* mass, const double* const* diam, double* const* out);
+
+/* Autotuner of ik_compute_batch_io (no reference counterpart; arguments as there): times
+ * `reps` CUDA-graph replays of the batch, host copies included (CUDA events on the
+ * context's stream), for each schedule of its copies -- per frame on the lanes at the
+ * current CTAs per SM and at the lanes' default, and, for a batch that can run fused, 2, 4,
+ * 8, 16 and 32 fused sub-batches (at most one per frame) -- and keeps the fastest
+ * (IK_TUNE_IO_BATCHES, IK_TUNE_BLOCKS_PER_SM).  Tune the resident batch first
+ * (ik_autotune_batch): the sub-batches run with its settings.  The host outputs hold the
+ * batch's fields afterwards. */
+int ik_autotune_batch_io(ik_ctx* ctx, const int* slots, int count, int precision, int fields,
+                         const int64_t* n, const double* const* pos, const double* const* vel,
+                         const double* const* mass, const double* const* diam, double* const* out,
+                         int reps, int* best_io_batches, float* best_ms);
 
 /* Asynchronous download of a slot's field in compact form: g x NC FP64 with
  * NC = 3 (xx, yy, xy) in 2D or 6 (xx, yy, zz, xy, xz, yz) in 3D.  The copy runs on a
@@ -295,11 +312,17 @@ int ik_get_counters(ik_ctx* ctx, int slot, int64_t* out3);
  *                          finish: 7 to 8 kernel launches per batch, recorded as one CUDA
  *                          graph); 0: one launch sequence per frame on the lanes.  Eligible:
  *                          FP32 path, virial and/or kinetic field, fixed-point rule of order
- *                          4 or 5, n * (bonds per particle) < 2^25 per slot, no slot twice */
+ *                          4 or 5, n * (bonds per particle) < 2^25 per slot, no slot twice
+ *   IK_TUNE_IO_BATCHES     ik_compute_batch_io: 0 (default): each frame's copies and kernels on
+ *                          one engine lane; n >= 1, for a batch that can run fused (fused
+ *                          batches on): n fused sub-batches -- contiguous runs of frames with
+ *                          about equal particle counts, never more than the frames -- whose
+ *                          host copies overlap the other sub-batches' computation */
 #define IK_TUNE_BIN_POINTS 1
 #define IK_TUNE_BLOCKS_PER_SM 2
 #define IK_TUNE_HALO_CAP 3
 #define IK_TUNE_FUSED_BATCH 4
+#define IK_TUNE_IO_BATCHES 5
 int ik_set_tuning(ik_ctx* ctx, int param, int value);
 int ik_get_tuning(ik_ctx* ctx, int param, int* value);
 /* Diagnostic (no reference counterpart): runs the batch once fused, without a graph,

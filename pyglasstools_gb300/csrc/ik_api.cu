@@ -230,6 +230,12 @@ struct ik_ctx {
     std::vector<int64_t> io_key;
     int64_t io_launches = 0;
     const IoFrame* io_cur = nullptr; // frame whose copies enqueue() adds to its lane
+    // a fused ik_compute_batch_io: sub-batches of frames, each a fused batch, whose copies
+    // overlap the other sub-batches' computation (IK_TUNE_IO_BATCHES: their number)
+    std::vector<FusedBatch> fused_io;
+    std::vector<cudaEvent_t> io_ev; // per sub-batch: uploads done, computation done
+    int tune_io_batches = 0;
+    bool io_fused = false;
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     int64_t launches = 0;
     float timing[4] = {0, 0, 0, 0};
@@ -1005,11 +1011,10 @@ bool fused_eligible(ik_ctx* c, const std::vector<int>& slots, int prec, int fiel
 }
 
 // Concatenates the slots' frames, cells, grids and work items (host, then one upload of
-// each array) and sizes the batch-wide work buffers.  Not during a capture.
-int fused_build(ik_ctx* c, const std::vector<int>& slots)
+// each array) into F and sizes its batch-wide work buffers.  Not during a capture.
+int fused_build(ik_ctx* c, const std::vector<int>& slots, FusedBatch& F)
 {
     const int D = c->dim, NC = D == 2 ? 3 : 6, S = (int)slots.size();
-    FusedBatch& F = c->fused;
     std::vector<IkBatchSlot> hs((size_t)S);
     std::vector<int> po((size_t)S + 1), co((size_t)S + 1);
     std::vector<long long> vo((size_t)S + 1);
@@ -1141,15 +1146,13 @@ int fused_build(ik_ctx* c, const std::vector<int>& slots)
     return IK_OK;
 }
 
-// The launches of a fused batch on the context stream (fused_build done).  timing:
-// events ev[0] before the preparation, ev[1] = ev[2] after it, ev[3] after the gather.
-int fused_enqueue(ik_ctx* c, int fields, bool timing = false)
+// The launches of the fused batch F on stream st (fused_build done).  timing: events
+// ev[0] before the preparation, ev[1] = ev[2] after it, ev[3] after the gather.
+int fused_enqueue(ik_ctx* c, FusedBatch& F, int fields, cudaStream_t st, bool timing = false)
 {
     NvtxRange nvr("ik fused batch");
-    FusedBatch& F = c->fused;
     const IkBatchLaunch& b = F.b;
     const int D = c->dim;
-    cudaStream_t st = c->stream;
     if (timing) CK(cudaEventRecord(c->ev[0], st));
     CK(cudaMemsetAsync(b.cell_count, 0, sizeof(int) * ((size_t)b.ctot + 1), st));
     CK(cudaMemsetAsync(F.work.p, 0, sizeof(int), st));
@@ -1221,6 +1224,95 @@ int prepare_enqueue(ik_ctx* c, int slot, int prec, int fields)
     if (c->maxb == 0) c->maxb = c->dim == 2 ? IK_MAXB_2D : IK_MAXB_3D;
     if (c->halo_cap == 0) c->halo_cap = 384; // staged particles per warp (grows on overflow)
     return enqueue(c, slot, prec, fields);
+}
+
+// The sub-batches of a fused ik_compute_batch_io: contiguous runs of the batch's frames with
+// about equal particle counts, IK_TUNE_IO_BATCHES of them, never more than the frames.
+// Returns the runs' boundaries (first 0, last count).
+std::vector<int> io_split(ik_ctx* c, const int* slots, int count)
+{
+    long long ptot = 0;
+    for (int k = 0; k < count; ++k) ptot += c->slots[(size_t)slots[k]].n;
+    const int nsub = std::max(1, std::min(c->tune_io_batches, count));
+    std::vector<int> cut{0};
+    long long acc = 0;
+    for (int k = 0; k + 1 < count && (int)cut.size() < nsub; ++k) {
+        acc += c->slots[(size_t)slots[k]].n;
+        const long long b = (long long)cut.size(); // the boundary this frame may close
+        if (acc * nsub >= ptot * b) cut.push_back(k + 1);
+    }
+    cut.push_back(count);
+    return cut;
+}
+
+// At least n completion events for the sub-batches of a fused ik_compute_batch_io (created
+// before a capture).
+int io_events(ik_ctx* c, int n)
+{
+    while ((int)c->io_ev.size() < n) {
+        cudaEvent_t e = nullptr;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        c->io_ev.push_back(e);
+    }
+    return IK_OK;
+}
+
+// The launches and copies of a fused ik_compute_batch_io, to be captured (fused_build of
+// every sub-batch and io_events done).  Lane 0 uploads the frames in batch order (copies
+// only: a kernel there would wait for the SMs that a persistent gather holds, and the next
+// uploads behind it); lanes 1 and 2 take the sub-batches in turn, each the validation of its
+// frames and a fused batch, started once its frames are on the device (the preparation of
+// one overlaps the end of the previous gather); lane 3 downloads a sub-batch's fields as
+// soon as it is computed.  The copies of the other sub-batches overlap every computation
+// but the first upload and the last download.
+int fused_io_enqueue(ik_ctx* c, const int* slots, const std::vector<IoFrame>& fr, const std::vector<int>& cut,
+                     int fields)
+{
+    const int NC = c->dim == 2 ? 3 : 6, nsub = (int)cut.size() - 1;
+    cudaStream_t up = c->lanes[0].st, dn = c->lanes[3].st;
+    CK(cudaEventRecord(c->fork, c->stream));
+    for (int l = 0; l < 4; ++l) CK(cudaStreamWaitEvent(c->lanes[l].st, c->fork, 0));
+    c->captured_lanes |= 0xF;
+    for (int b = 0; b < nsub; ++b) {
+        NvtxRange nvr("ik upload");
+        for (int k = cut[(size_t)b]; k < cut[(size_t)b + 1]; ++k) {
+            Slot& s = c->slots[(size_t)slots[k]];
+            const IoFrame& io = fr[(size_t)k];
+            const int n = (int)s.n;
+            if (n == 0) continue;
+            CK(cudaMemcpyAsync(s.pos.p, io.pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, up));
+            CK(cudaMemcpyAsync(s.diam.p, io.diam, sizeof(double) * n, cudaMemcpyHostToDevice, up));
+            if (io.vel) CK(cudaMemcpyAsync(s.vel.p, io.vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, up));
+            if (io.mass) CK(cudaMemcpyAsync(s.mass.p, io.mass, sizeof(double) * n, cudaMemcpyHostToDevice, up));
+        }
+        CK(cudaEventRecord(c->io_ev[(size_t)(2 * b)], up));
+        cudaStream_t cs = c->lanes[1 + (b & 1)].st;
+        CK(cudaStreamWaitEvent(cs, c->io_ev[(size_t)(2 * b)], 0));
+        for (int k = cut[(size_t)b]; k < cut[(size_t)b + 1]; ++k) {
+            Slot& s = c->slots[(size_t)slots[k]];
+            const int n = (int)s.n;
+            if (n == 0) continue;
+            k_validate<<<(n + 255) / 256, 256, 0, cs>>>(s.pos.as<double>(), s.diam.as<double>(), n, c->dim,
+                                                        c->status.as<int>());
+            CK(cudaGetLastError());
+            c->launches += 1;
+        }
+        if (int r = fused_enqueue(c, c->fused_io[(size_t)b], fields, cs)) return r;
+        CK(cudaEventRecord(c->io_ev[(size_t)(2 * b + 1)], cs));
+        CK(cudaStreamWaitEvent(dn, c->io_ev[(size_t)(2 * b + 1)], 0));
+        for (int k = cut[(size_t)b]; k < cut[(size_t)b + 1]; ++k) {
+            Slot& s = c->slots[(size_t)slots[k]];
+            int64_t G = 0;
+            { GeoSwap gs(c, slots[k]); G = c->geo.G; }
+            if (G == 0) continue;
+            const DevBuf* src[2] = {&s.vir, &s.kin};
+            for (int f = 0; f < 2; ++f)
+                if (fr[(size_t)k].out[f] && (fields & (1 << f)))
+                    CK(cudaMemcpyAsync(fr[(size_t)k].out[f], src[f]->p, sizeof(double) * NC * G,
+                                       cudaMemcpyDeviceToHost, dn));
+        }
+    }
+    return IK_OK;
 }
 
 } // namespace
@@ -1309,6 +1401,7 @@ int ik_destroy(ik_ctx* c)
     if (c->batch_exec) cudaGraphExecDestroy(c->batch_exec);
     if (c->io_exec) cudaGraphExecDestroy(c->io_exec);
     if (c->fork) cudaEventDestroy(c->fork);
+    for (cudaEvent_t e : c->io_ev) cudaEventDestroy(e);
     if (c->d2h_last) cudaEventDestroy(c->d2h_last);
     for (Slot& s : c->slots) {
         if (s.done) cudaEventDestroy(s.done);
@@ -1705,7 +1798,7 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
         // eligible, else the same per-frame sequence (lanes fork from and join the main stream)
         const bool fused = fused_eligible(c, key, precision, fields);
         if (fused) {
-            if (int r = fused_build(c, key)) return r;
+            if (int r = fused_build(c, key, c->fused)) return r;
         }
         if (c->batch_exec) { cudaGraphExecDestroy(c->batch_exec); c->batch_exec = nullptr; }
         if (c->io_exec) { cudaGraphExecDestroy(c->io_exec); c->io_exec = nullptr; } // versions below are ours now
@@ -1716,7 +1809,7 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
         c->captured_lanes = 0;
         int rr = IK_OK;
         c->in_batch = true;
-        if (fused) rr = fused_enqueue(c, fields);
+        if (fused) rr = fused_enqueue(c, c->fused, fields, c->stream);
         for (int k = 0; k < count && rr == IK_OK && !fused; ++k) rr = prepare_enqueue(c, slots[k], precision, fields);
         c->in_batch = false;
         for (int l = 0; l < IK_LANES && rr == IK_OK; ++l)
@@ -1792,10 +1885,10 @@ int ik_time_fused_batch(ik_ctx* c, const int* slots, int count, int fields, floa
     c->tune_fused = saved_fused;
     if (!ok) return fail(IK_ERR_UNSUPPORTED, "this batch cannot run fused");
     if (int r = ik_wait_all(c)) return r;
-    if (int r = fused_build(c, key)) return r;
+    if (int r = fused_build(c, key, c->fused)) return r;
     ++c->config_version; // the fused buffers were rebuilt: a recorded batch graph re-records
     for (int k = 0; k < count; ++k) c->pending.push_back({slots[k], IK_PREC_FP32, fields});
-    if (int r = fused_enqueue(c, fields, true)) return r;
+    if (int r = fused_enqueue(c, c->fused, fields, c->stream, true)) return r;
     if (int r = ik_synchronize(c)) return r;
     CK(cudaEventElapsedTime(&ms4[0], c->ev[0], c->ev[1]));
     CK(cudaEventElapsedTime(&ms4[1], c->ev[1], c->ev[2]));
@@ -1880,7 +1973,22 @@ int ik_compute_batch_io(ik_ctx* c, const int* slots, int count, int precision, i
         }
         if (int r = ik_synchronize(c)) return r;
         if (c->flags & IK_FLAG_TIMING) return IK_OK;
-        // record: per frame on its lane, host -> device copies, the kernels, device -> host
+        // record: an eligible batch as fused sub-batches whose copies overlap each other's
+        // computation, else per frame on its lane, host -> device copies, the kernels,
+        // device -> host
+        const bool fused =
+            c->tune_io_batches > 0 && fused_eligible(c, std::vector<int>(slots, slots + count), precision, fields);
+        std::vector<int> cut;
+        if (fused) {
+            cut = io_split(c, slots, count);
+            const int nsub = (int)cut.size() - 1;
+            if ((int)c->fused_io.size() < nsub) c->fused_io.resize((size_t)nsub);
+            for (int b = 0; b < nsub; ++b)
+                if (int r = fused_build(c, std::vector<int>(slots + cut[(size_t)b], slots + cut[(size_t)b + 1]),
+                                        c->fused_io[(size_t)b]))
+                    return r;
+            if (int r = io_events(c, 2 * nsub)) return r;
+        }
         if (c->io_exec) { cudaGraphExecDestroy(c->io_exec); c->io_exec = nullptr; }
         if (c->batch_exec) { cudaGraphExecDestroy(c->batch_exec); c->batch_exec = nullptr; } // versions below are ours now
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
@@ -1890,7 +1998,8 @@ int ik_compute_batch_io(ik_ctx* c, const int* slots, int count, int precision, i
         c->captured_lanes = 0;
         int rr = IK_OK;
         c->in_batch = true;
-        for (int k = 0; k < count && rr == IK_OK; ++k) {
+        if (fused) rr = fused_io_enqueue(c, slots, fr, cut, fields);
+        for (int k = 0; k < count && rr == IK_OK && !fused; ++k) {
             c->io_cur = &fr[(size_t)k];
             rr = prepare_enqueue(c, slots[k], precision, fields);
         }
@@ -1913,6 +2022,7 @@ int ik_compute_batch_io(ik_ctx* c, const int* slots, int count, int precision, i
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) { c->io_exec = nullptr; return fail(IK_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e)); }
         c->io_key = key;
+        c->io_fused = fused;
         c->batch_maxb = c->maxb;
         c->batch_halo = c->halo_cap;
         c->batch_maxbe = c->maxbe;
@@ -2299,9 +2409,62 @@ int ik_set_tuning(ik_ctx* c, int param, int value)
         if (value != 0 && value != 1) return fail(IK_ERR_ARG, "fused batches: 0 or 1");
         c->tune_fused = value;
         return IK_OK;
+    case IK_TUNE_IO_BATCHES:
+        if (value < 0 || value > 64) return fail(IK_ERR_ARG, "sub-batches must be in [0, 64]");
+        c->tune_io_batches = value;
+        return IK_OK;
     default:
         return fail(IK_ERR_ARG, "unknown tuning parameter %d", param);
     }
+}
+
+// Time the host-I/O batch under each schedule of its copies, keep the fastest.
+int ik_autotune_batch_io(ik_ctx* c, const int* slots, int count, int precision, int fields, const int64_t* n,
+                         const double* const* pos, const double* const* vel, const double* const* mass,
+                         const double* const* diam, double* const* out, int reps, int* best_io_batches,
+                         float* best_ms)
+{
+    NvtxRange nvr("ik autotune_batch_io");
+    if (int r = check_ctx(c)) return r;
+    if (reps < 1 || reps > 1000) return fail(IK_ERR_ARG, "reps must be in [1, 1000]");
+    // candidates: per frame on the lanes (0, at the batch's CTAs per SM and at the lanes'
+    // default), fused sub-batches (when the batch can run fused)
+    static const int subs[] = {0, 0, 2, 4, 8, 16, 32};
+    const int io0 = c->tune_io_batches, bps0 = c->tune_blocks_per_sm;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); return fail(IK_ERR_CUDA, "event creation failed"); }
+    float best = 1e30f;
+    int bi = io0, bk = bps0, rc = IK_OK;
+    for (int i = 0; i < (int)(sizeof(subs) / sizeof(subs[0])) && rc == IK_OK; ++i) {
+        const int nb = subs[i], bps = i == 1 ? 0 : bps0;
+        if ((i == 1 && bps0 == 0) || (nb > 0 && (!c->tune_fused || (nb > count && subs[i - 1] >= count)))) continue;
+        if ((rc = ik_set_tuning(c, IK_TUNE_IO_BATCHES, std::min(nb, count))) ||
+            (rc = ik_set_tuning(c, IK_TUNE_BLOCKS_PER_SM, bps)) ||
+            (rc = ik_compute_batch_io(c, slots, count, precision, fields, n, pos, vel, mass, diam, out)) ||
+            (rc = ik_compute_batch_io(c, slots, count, precision, fields, n, pos, vel, mass, diam, out)) ||
+            (rc = ik_synchronize(c)))
+            break;
+        if (nb > 0 && !c->io_fused) break; // the batch cannot run fused: the lanes ran
+        if (cudaEventRecord(e0, c->stream) != cudaSuccess) { rc = fail(IK_ERR_CUDA, "event record failed"); break; }
+        for (int t = 0; t < reps && rc == IK_OK; ++t)
+            rc = ik_compute_batch_io(c, slots, count, precision, fields, n, pos, vel, mass, diam, out);
+        if (rc) break;
+        float ms = 0.f;
+        if (cudaEventRecord(e1, c->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) { rc = fail(IK_ERR_CUDA, "event timing failed"); break; }
+        if ((rc = ik_synchronize(c))) break;
+        ms /= (float)reps;
+        if (ms < best) { best = ms; bi = std::min(nb, count); bk = bps; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (int r = ik_set_tuning(c, IK_TUNE_IO_BATCHES, bi)) return r;
+    if (int r = ik_set_tuning(c, IK_TUNE_BLOCKS_PER_SM, bk)) return r;
+    if (best_io_batches) *best_io_batches = bi;
+    if (best_ms) *best_ms = best;
+    return IK_OK;
 }
 
 // Time the batch under each candidate (bin points x CTAs per SM), keep the fastest.
@@ -2369,6 +2532,7 @@ int ik_get_tuning(ik_ctx* c, int param, int* value)
     case IK_TUNE_BLOCKS_PER_SM: *value = c->tune_blocks_per_sm; return IK_OK;
     case IK_TUNE_HALO_CAP: *value = c->halo_cap; return IK_OK;
     case IK_TUNE_FUSED_BATCH: *value = c->tune_fused; return IK_OK;
+    case IK_TUNE_IO_BATCHES: *value = c->tune_io_batches; return IK_OK;
     default: return fail(IK_ERR_ARG, "unknown tuning parameter %d", param);
     }
 }

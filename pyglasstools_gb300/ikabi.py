@@ -23,7 +23,7 @@ QUAD = {"fixedpoint": 0, "adaptive": 1, "exact": 2, "mlp": 3, "clipped": 4}
 PREC = {"fp64": 0, "fp32": 1}
 FIELD_VIRIAL, FIELD_KINETIC, FIELD_ELASTIC = 1, 2, 4
 FLAG_TIMING, FLAG_LANE_KAHAN, FLAG_CSR_BONDS = 1, 2, 4
-TUNE = {"bin_points": 1, "blocks_per_sm": 2, "halo_cap": 3, "fused_batch": 4}
+TUNE = {"bin_points": 1, "blocks_per_sm": 2, "halo_cap": 3, "fused_batch": 4, "io_batches": 5}
 POT = {"poly12": 0, "lj": 1, "fslj": 2, "poly10": 3, "poly106": 4, "poly18": 5, "polylj": 6,
        "polyyukawa": 7}
 
@@ -56,6 +56,9 @@ def lib():
             "ik_compute_thermo": ([vp, i32, dp, i64], i32),
             "ik_compute_batch_io": ([vp, C.POINTER(i32), i32, i32, i32, C.POINTER(i64), C.POINTER(dp), C.POINTER(dp),
                                      C.POINTER(dp), C.POINTER(dp), C.POINTER(dp)], i32),
+            "ik_autotune_batch_io": ([vp, C.POINTER(i32), i32, i32, i32, C.POINTER(i64), C.POINTER(dp),
+                                      C.POINTER(dp), C.POINTER(dp), C.POINTER(dp), C.POINTER(dp), i32,
+                                      C.POINTER(i32), C.POINTER(C.c_float)], i32),
             "ik_gk15_rule": ([dp, dp, dp], i32),
             "ik_set_cgfunc": ([vp, i32, i32, i32, C.c_double, C.c_double], i32),
             "ik_set_adaptive": ([vp, i32, C.c_double, C.c_double], i32),
@@ -401,8 +404,12 @@ class IKContext:
         (pos, diam, vel, mass) page-locked float64 arrays (vel / mass may be None);
         outs[k] = (virial, kinetic, elastic) page-locked float64 (g, NC) arrays or None.
         Complete after synchronize()."""
-        # ctypes argument arrays kept while the same arrays come back (the arrays held, so
-        # their ids stay theirs)
+        sl, cnt, nn, pos, vel, mass, diam, out = self._io_call_args(slots, frames, outs)
+        check(lib().ik_compute_batch_io(self._h, sl, cnt, PREC[precision], fields, nn, pos, vel, mass, diam, out))
+
+    def _io_call_args(self, slots, frames, outs):
+        """The ctypes arguments of a host-I/O batch, kept while the same arrays come back
+        (the arrays held, so their ids stay theirs)."""
         arrays = tuple(a for f in frames for a in f) + tuple(o for os_ in outs for o in os_)
         ids = tuple(map(id, arrays))
         cached = getattr(self, "_io_args", None)
@@ -416,8 +423,17 @@ class IKContext:
                     (P * cnt)(*[ptr(f[3]) for f in frames]), (P * cnt)(*[ptr(f[1]) for f in frames]),
                     (P * (3 * cnt))(*[ptr(o) for os_ in outs for o in os_]))
             self._io_args = cached = (ids, arrays, list(slots), args)
-        sl, cnt, nn, pos, vel, mass, diam, out = cached[3]
-        check(lib().ik_compute_batch_io(self._h, sl, cnt, PREC[precision], fields, nn, pos, vel, mass, diam, out))
+        return cached[3]
+
+    def autotune_batch_io(self, slots, frames, outs, precision="fp32", fields=FIELD_VIRIAL | FIELD_KINETIC, reps=3):
+        """Time compute_batch_io (arguments as there) under each schedule of its copies --
+        per frame on the lanes, or fused sub-batches -- keep the fastest; returns
+        {"io_batches", "blocks_per_sm", "ms_per_batch"} (io_batches 0: the lanes)."""
+        sl, cnt, nn, pos, vel, mass, diam, out = self._io_call_args(slots, frames, outs)
+        nb, ms = C.c_int(), C.c_float()
+        check(lib().ik_autotune_batch_io(self._h, sl, cnt, PREC[precision], fields, nn, pos, vel, mass, diam, out,
+                                         reps, C.byref(nb), C.byref(ms)))
+        return {"io_batches": nb.value, "blocks_per_sm": self.get_tuning("blocks_per_sm"), "ms_per_batch": ms.value}
 
     def compute_thermo(self, slot=0):
         """Global observables of a slot's frame: dict of potentialenergy (float),

@@ -181,3 +181,89 @@ def test_fused_replay_overflowing_bond_capacity_is_rerun():
     for a, b in zip(got[1], want1):
         np.testing.assert_array_equal(a, b)
     c.close()
+
+
+@pytest.mark.parametrize("io_batches", [1, 3, 6])
+def test_fused_host_io_sub_batches_equal_per_frame(io_batches):
+    """ik_compute_batch_io of an eligible batch runs as fused sub-batches whose host copies
+    overlap the other sub-batches' computation.  Uneven frames with their own boxes and
+    grids, one without velocities: the host fields equal the per-frame path bit for bit on
+    the first call (plain path), on replays and after new contents, and a replay launches
+    one validation per frame and at most eight kernels per sub-batch."""
+    torch = pytest.importorskip("torch")
+    from conftest import uniq
+    from pyglasstools_gb300 import ikabi as ik, synth
+    sizes = [3000, 800, 15000, 1200, 6100, 2000]
+    fr, grids = _uneven(2, sizes, 1600)
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    host = [(pin(f.pos), pin(f.diam), None if k == 3 else pin(f.vel), None if k == 3 else pin(f.mass))
+            for k, f in enumerate(fr)]
+    outs = [(pin(np.zeros((len(g), 3))), pin(np.zeros((len(g), 3))), None) for g in grids]
+    c = _ctx(ik)
+    _setup(ik, c, 2, fr, grids, no_vel=(3,))
+    c.set_tuning("io_batches", io_batches)
+    assert c.get_tuning("io_batches") == io_batches
+    slots = list(range(len(fr)))
+
+    def want_for(frames):
+        res = []
+        for k, f in enumerate(frames):
+            if k == 3:
+                f = synth.SynthFrame(2, f.L, f.pos, None, None, f.diam)
+            w, _ = _alone(ik, 2, f, grids[k])
+            res.append([uniq(x) for x in w])
+        return res
+
+    def check(want):
+        for k in slots:
+            np.testing.assert_array_equal(outs[k][0], want[k][0])
+            np.testing.assert_array_equal(outs[k][1], want[k][1])
+
+    want = want_for(fr)
+    for rep in range(3):  # plain path + recording, then replays
+        l0 = c.launch_count()
+        c.compute_batch_io(slots, host, outs)
+        c.synchronize()
+        if rep == 2:
+            assert c.launch_count() - l0 <= len(fr) + 8 * io_batches
+        check(want)
+    fr2, _ = _uneven(2, sizes, 1700)  # same sizes and boxes, new contents
+    for k, f in enumerate(fr2):
+        host[k][0][:] = f.pos
+        host[k][1][:] = f.diam
+        if k != 3:
+            host[k][2][:] = f.vel
+            host[k][3][:] = f.mass
+    c.compute_batch_io(slots, host, outs)
+    c.synchronize()
+    check(want_for(fr2))
+    c.close()
+
+
+def test_host_io_autotuner_keeps_a_candidate_and_the_fields():
+    """ik_autotune_batch_io times the lanes and the fused sub-batches of a host-I/O batch,
+    keeps one of them, and the host fields it leaves -- and those of the tuned replay --
+    equal the per-frame path bit for bit."""
+    torch = pytest.importorskip("torch")
+    from conftest import uniq
+    from pyglasstools_gb300 import ikabi as ik
+    sizes = [2500, 900, 7000, 1800]
+    fr, grids = _uneven(2, sizes, 1800)
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    host = [(pin(f.pos), pin(f.diam), pin(f.vel), pin(f.mass)) for f in fr]
+    outs = [(pin(np.zeros((len(g), 3))), pin(np.zeros((len(g), 3))), None) for g in grids]
+    c = _ctx(ik)
+    _setup(ik, c, 2, fr, grids)
+    slots = list(range(len(fr)))
+    best = c.autotune_batch_io(slots, host, outs, reps=1)
+    assert best["io_batches"] in (0, 2, 4) and best["ms_per_batch"] > 0
+    assert c.get_tuning("io_batches") == best["io_batches"]
+    want = [[uniq(x) for x in _alone(ik, 2, f, g)[0]] for f, g in zip(fr, grids)]
+    for rep in range(2):
+        if rep:
+            c.compute_batch_io(slots, host, outs)
+        c.synchronize()
+        for k in slots:
+            np.testing.assert_array_equal(outs[k][0], want[k][0])
+            np.testing.assert_array_equal(outs[k][1], want[k][1])
+    c.close()
