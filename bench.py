@@ -444,15 +444,18 @@ def uneven_leg(args):
     # lanes beside it: wall time per batch, synchronised
     io_best = c.autotune_batch_io(slots, host, outs, reps=2)
 
-    def e2e():
+    def e2e():  # ms per batch: the median of three timed runs (the host link's rate varies run to run)
         for _ in range(3):
             c.compute_batch_io(slots, host, outs)
             c.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            c.compute_batch_io(slots, host, outs)
-            c.synchronize()
-        return (time.perf_counter() - t0) / reps * 1e3
+        runs = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                c.compute_batch_io(slots, host, outs)
+                c.synchronize()
+            runs.append((time.perf_counter() - t0) / reps * 1e3)
+        return float(np.median(runs))
 
     ms_e2e = e2e()
     c.set_tuning("io_batches", 0)
