@@ -663,6 +663,7 @@ def ours(args, wl, name):
     else:
         io_tuning = ctx.autotune_batch_io(io_slots, io_frames, io_outs, reps=2)
     nsub = ctx.get_tuning("io_batches") if not args.no_graph else 0
+    io_mapped = ctx.get_tuning("io_mapped") if nsub else 0
     e2e_value = e2e_run()
     e2e_other, other_desc = None, None
     if not args.no_graph and ctx.get_tuning("fused_batch"):
@@ -673,17 +674,22 @@ def ours(args, wl, name):
             other_desc = "lanes"
         else:
             ctx.set_tuning("io_batches", 8)
+            ctx.set_tuning("io_mapped", 0)
             other_desc = "8 fused sub-batches"
         e2e_other = e2e_run()
         ctx.set_tuning("io_batches", nsub)
+        ctx.set_tuning("io_mapped", io_mapped)
         ctx.set_tuning("blocks_per_sm", bps0)
 
-    def io_desc(nb):
+    def io_desc(nb, mapped):
+        if nb and mapped:
+            return ("%d fused sub-batches of ~%d frames, each sub-batch's copies one kernel over the host arrays' "
+                    "device view" % (min(nb, F), -(-F // min(nb, F))))
         if nb:
             return ("%d fused sub-batches of ~%d frames, copies overlapping the other sub-batches' computation"
                     % (min(nb, F), -(-F // min(nb, F))))
         return "lanes: each frame's copies and kernels on one of eight streams"
-    e2e_schedule = io_desc(nsub)
+    e2e_schedule = io_desc(nsub, io_mapped)
     h2d = F * wl["N"] * (3 + 3 + 1 + 1) * 8
     d2h = F * len(grid) * NC * 2 * 8
     clocks.stop()

@@ -232,8 +232,9 @@ int ik_compute_batch_io(ik_ctx* ctx, const int* slots, int count, int precision,
  * `reps` CUDA-graph replays of the batch, host copies included (CUDA events on the
  * context's stream), for each schedule of its copies -- per frame on the lanes at the
  * current CTAs per SM and at the lanes' default, and, for a batch that can run fused, 2, 4,
- * 8, 16 and 32 fused sub-batches (at most one per frame) -- and keeps the fastest
- * (IK_TUNE_IO_BATCHES, IK_TUNE_BLOCKS_PER_SM).  Tune the resident batch first
+ * 8, 16 and 32 fused sub-batches with their copies on the copy engines and 1, 2 and 4 with
+ * host-mapped copies (at most one sub-batch per frame) -- and keeps the fastest
+ * (IK_TUNE_IO_BATCHES, IK_TUNE_IO_MAPPED, IK_TUNE_BLOCKS_PER_SM).  Tune the resident batch first
  * (ik_autotune_batch): the sub-batches run with its settings.  The host outputs hold the
  * batch's fields afterwards. */
 int ik_autotune_batch_io(ik_ctx* ctx, const int* slots, int count, int precision, int fields,
@@ -317,12 +318,19 @@ int ik_get_counters(ik_ctx* ctx, int slot, int64_t* out3);
  *                          one engine lane; n >= 1, for a batch that can run fused (fused
  *                          batches on): n fused sub-batches -- contiguous runs of frames with
  *                          about equal particle counts, never more than the frames -- whose
- *                          host copies overlap the other sub-batches' computation */
+ *                          host copies overlap the other sub-batches' computation
+ *   IK_TUNE_IO_MAPPED      with IK_TUNE_IO_BATCHES >= 1: 0 (default): the copies on the copy
+ *                          engines, one per array; 1: each sub-batch's uploads (with the
+ *                          frames' validation) and downloads as one kernel each, reading and
+ *                          writing the device's view of the page-locked host arrays, on the
+ *                          sub-batch's stream -- no per-array copy cost, for batches of
+ *                          many small frames (arrays without a device view: copy engines) */
 #define IK_TUNE_BIN_POINTS 1
 #define IK_TUNE_BLOCKS_PER_SM 2
 #define IK_TUNE_HALO_CAP 3
 #define IK_TUNE_FUSED_BATCH 4
 #define IK_TUNE_IO_BATCHES 5
+#define IK_TUNE_IO_MAPPED 6
 int ik_set_tuning(ik_ctx* ctx, int param, int value);
 int ik_get_tuning(ik_ctx* ctx, int param, int* value);
 /* Diagnostic (no reference counterpart): runs the batch once fused, without a graph,

@@ -4,6 +4,7 @@
 #include "../../include/ik_gb300.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -157,6 +158,11 @@ struct FusedBatch {
     DevBuf slots, p_offs, c_offs, v_offs, items, item_slot, gpts, grid;
     DevBuf cell_of, rank, cell_count, cell_start, sorted, bsum, relhi, rello, prec, plo, pos64, kin, diam32, tmp, nb;
     DevBuf vir2, kin2, work;
+    // host-mapped copies of a fused ik_compute_batch_io (IK_TUNE_IO_MAPPED): the frames'
+    // uploads and the fields' downloads, one launch_io_copy each
+    DevBuf io_up, io_dn;
+    int n_up = 0, n_dn = 0;
+    long long w_up = 0, w_dn = 0;
 };
 
 // A computation not yet confirmed by ik_synchronize (re-run after a capacity growth),
@@ -234,8 +240,8 @@ struct ik_ctx {
     // overlap the other sub-batches' computation (IK_TUNE_IO_BATCHES: their number)
     std::vector<FusedBatch> fused_io;
     std::vector<cudaEvent_t> io_ev; // per sub-batch: uploads done, computation done
-    int tune_io_batches = 0;
-    bool io_fused = false;
+    int tune_io_batches = 0, tune_io_mapped = 0;
+    bool io_fused = false, io_mapped = false;
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     int64_t launches = 0;
     float timing[4] = {0, 0, 0, 0};
@@ -1257,6 +1263,78 @@ int io_events(ik_ctx* c, int n)
     return IK_OK;
 }
 
+// The device's view of a page-locked host array (null when it has none).
+const void* host_mapped(const void* p)
+{
+    if (!p) return nullptr;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// The descriptor tables of host-mapped copies (IK_TUNE_IO_MAPPED) for the sub-batches of a
+// fused ik_compute_batch_io (fused_build of each done): per frame its positions (checked),
+// diameters (checked), velocities and masses into the slot's buffers; per frame each
+// requested field out of the slot's buffer.  Returns false (nothing built) when an array
+// has no device view, so that the copies stay on the copy engines.
+bool io_build_mapped(ik_ctx* c, const int* slots, const std::vector<IoFrame>& fr, const std::vector<int>& cut,
+                     int fields, int* err)
+{
+    *err = IK_OK;
+    const int NC = c->dim == 2 ? 3 : 6, nsub = (int)cut.size() - 1;
+    std::vector<std::vector<IkIoCopy>> ups((size_t)nsub), dns((size_t)nsub);
+    for (int b = 0; b < nsub; ++b)
+        for (int k = cut[(size_t)b]; k < cut[(size_t)b + 1]; ++k) {
+            Slot& s = c->slots[(size_t)slots[k]];
+            const IoFrame& io = fr[(size_t)k];
+            const long long n = s.n;
+            // one copy: host array -> device buffer (up) or device buffer -> host array
+            auto add = [&](bool up, const void* src, void* dst, long long words, int check) {
+                if (words <= 0) return true;
+                const void* ms = up ? host_mapped(src) : src;
+                const void* md = up ? dst : host_mapped(dst);
+                if (!ms || !md) return false;
+                IkIoCopy d{};
+                d.src = static_cast<const long long*>(ms);
+                d.dst = static_cast<long long*>(const_cast<void*>(md));
+                d.words = words;
+                d.check = check;
+                d.dim = c->dim;
+                (up ? ups : dns)[(size_t)b].push_back(d);
+                return true;
+            };
+            if (!add(true, io.pos, s.pos.p, 3 * n, 1) || !add(true, io.diam, s.diam.p, n, 2) ||
+                (io.vel && !add(true, io.vel, s.vel.p, 3 * n, 0)) || (io.mass && !add(true, io.mass, s.mass.p, n, 0)))
+                return false;
+            int64_t G = 0;
+            { GeoSwap gs(c, slots[k]); G = c->geo.G; }
+            const DevBuf* src[2] = {&s.vir, &s.kin};
+            for (int f = 0; f < 2; ++f)
+                if (io.out[f] && (fields & (1 << f)) && !add(false, src[f]->p, io.out[f], (long long)NC * G, 0))
+                    return false;
+        }
+    for (int b = 0; b < nsub; ++b) {
+        FusedBatch& F = c->fused_io[(size_t)b];
+        for (int dir = 0; dir < 2; ++dir) {
+            std::vector<IkIoCopy>& v = dir ? dns[(size_t)b] : ups[(size_t)b];
+            long long off = 0;
+            for (IkIoCopy& d : v) { d.off = off; off += d.words; }
+            DevBuf& buf = dir ? F.io_dn : F.io_up;
+            if ((*err = buf.ensure(std::max<size_t>(v.size(), 1) * sizeof(IkIoCopy)))) return false;
+            if (!v.empty() && cudaMemcpy(buf.p, v.data(), v.size() * sizeof(IkIoCopy), cudaMemcpyHostToDevice) != cudaSuccess) {
+                *err = fail(IK_ERR_CUDA, "descriptor upload failed");
+                return false;
+            }
+            (dir ? F.n_dn : F.n_up) = (int)v.size();
+            (dir ? F.w_dn : F.w_up) = off;
+        }
+    }
+    return true;
+}
+
 // The launches and copies of a fused ik_compute_batch_io, to be captured (fused_build of
 // every sub-batch and io_events done).  Lane 0 uploads the frames in batch order (copies
 // only: a kernel there would wait for the SMs that a persistent gather holds, and the next
@@ -1266,13 +1344,27 @@ int io_events(ik_ctx* c, int n)
 // soon as it is computed.  The copies of the other sub-batches overlap every computation
 // but the first upload and the last download.
 int fused_io_enqueue(ik_ctx* c, const int* slots, const std::vector<IoFrame>& fr, const std::vector<int>& cut,
-                     int fields)
+                     int fields, bool mapped)
 {
     const int NC = c->dim == 2 ? 3 : 6, nsub = (int)cut.size() - 1;
     cudaStream_t up = c->lanes[0].st, dn = c->lanes[3].st;
     CK(cudaEventRecord(c->fork, c->stream));
     for (int l = 0; l < 4; ++l) CK(cudaStreamWaitEvent(c->lanes[l].st, c->fork, 0));
     c->captured_lanes |= 0xF;
+    if (mapped) {
+        // host-mapped copies (io_build_mapped done): a sub-batch's uploads with their
+        // validation, its fused batch and its downloads, on lanes 1 and 2 in turn
+        for (int b = 0; b < nsub; ++b) {
+            FusedBatch& F = c->fused_io[(size_t)b];
+            cudaStream_t cs = c->lanes[1 + (b & 1)].st;
+            CK(launch_io_copy(F.io_up.as<IkIoCopy>(), F.n_up, F.w_up, c->status.as<int>(), c->sm_count, cs));
+            c->launches += F.w_up > 0 ? 1 : 0;
+            if (int r = fused_enqueue(c, F, fields, cs)) return r;
+            CK(launch_io_copy(F.io_dn.as<IkIoCopy>(), F.n_dn, F.w_dn, c->status.as<int>(), c->sm_count, cs));
+            c->launches += F.w_dn > 0 ? 1 : 0;
+        }
+        return IK_OK;
+    }
     for (int b = 0; b < nsub; ++b) {
         NvtxRange nvr("ik upload");
         for (int k = cut[(size_t)b]; k < cut[(size_t)b + 1]; ++k) {
@@ -1979,6 +2071,7 @@ int ik_compute_batch_io(ik_ctx* c, const int* slots, int count, int precision, i
         const bool fused =
             c->tune_io_batches > 0 && fused_eligible(c, std::vector<int>(slots, slots + count), precision, fields);
         std::vector<int> cut;
+        bool mapped = false;
         if (fused) {
             cut = io_split(c, slots, count);
             const int nsub = (int)cut.size() - 1;
@@ -1988,6 +2081,9 @@ int ik_compute_batch_io(ik_ctx* c, const int* slots, int count, int precision, i
                                         c->fused_io[(size_t)b]))
                     return r;
             if (int r = io_events(c, 2 * nsub)) return r;
+            int err = IK_OK;
+            mapped = c->tune_io_mapped && io_build_mapped(c, slots, fr, cut, fields, &err);
+            if (err) return err;
         }
         if (c->io_exec) { cudaGraphExecDestroy(c->io_exec); c->io_exec = nullptr; }
         if (c->batch_exec) { cudaGraphExecDestroy(c->batch_exec); c->batch_exec = nullptr; } // versions below are ours now
@@ -1998,7 +2094,7 @@ int ik_compute_batch_io(ik_ctx* c, const int* slots, int count, int precision, i
         c->captured_lanes = 0;
         int rr = IK_OK;
         c->in_batch = true;
-        if (fused) rr = fused_io_enqueue(c, slots, fr, cut, fields);
+        if (fused) rr = fused_io_enqueue(c, slots, fr, cut, fields, mapped);
         for (int k = 0; k < count && rr == IK_OK && !fused; ++k) {
             c->io_cur = &fr[(size_t)k];
             rr = prepare_enqueue(c, slots[k], precision, fields);
@@ -2023,6 +2119,7 @@ int ik_compute_batch_io(ik_ctx* c, const int* slots, int count, int precision, i
         if (e != cudaSuccess) { c->io_exec = nullptr; return fail(IK_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e)); }
         c->io_key = key;
         c->io_fused = fused;
+        c->io_mapped = mapped;
         c->batch_maxb = c->maxb;
         c->batch_halo = c->halo_cap;
         c->batch_maxbe = c->maxbe;
@@ -2413,6 +2510,10 @@ int ik_set_tuning(ik_ctx* c, int param, int value)
         if (value < 0 || value > 64) return fail(IK_ERR_ARG, "sub-batches must be in [0, 64]");
         c->tune_io_batches = value;
         return IK_OK;
+    case IK_TUNE_IO_MAPPED:
+        if (value != 0 && value != 1) return fail(IK_ERR_ARG, "host-mapped copies: 0 or 1");
+        c->tune_io_mapped = value;
+        return IK_OK;
     default:
         return fail(IK_ERR_ARG, "unknown tuning parameter %d", param);
     }
@@ -2427,25 +2528,36 @@ int ik_autotune_batch_io(ik_ctx* c, const int* slots, int count, int precision, 
     NvtxRange nvr("ik autotune_batch_io");
     if (int r = check_ctx(c)) return r;
     if (reps < 1 || reps > 1000) return fail(IK_ERR_ARG, "reps must be in [1, 1000]");
-    // candidates: per frame on the lanes (0, at the batch's CTAs per SM and at the lanes'
-    // default), fused sub-batches (when the batch can run fused)
-    static const int subs[] = {0, 0, 2, 4, 8, 16, 32};
-    const int io0 = c->tune_io_batches, bps0 = c->tune_blocks_per_sm;
+    // candidates: per frame on the lanes (at the batch's CTAs per SM and at the lanes'
+    // default), fused sub-batches with their copies on the copy engines, and fused
+    // sub-batches with host-mapped copies (both when the batch can run fused)
+    struct Cand { int nb, mapped, lanes_default; };
+    static const Cand cands[] = {{0, 0, 0}, {0, 0, 1}, {2, 0, 0}, {4, 0, 0}, {8, 0, 0}, {16, 0, 0}, {32, 0, 0},
+                                 {1, 1, 0}, {2, 1, 0}, {4, 1, 0}};
+    const int io0 = c->tune_io_batches, map0 = c->tune_io_mapped, bps0 = c->tune_blocks_per_sm;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     CK(cudaEventCreate(&e0));
     if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); return fail(IK_ERR_CUDA, "event creation failed"); }
     float best = 1e30f;
-    int bi = io0, bk = bps0, rc = IK_OK;
-    for (int i = 0; i < (int)(sizeof(subs) / sizeof(subs[0])) && rc == IK_OK; ++i) {
-        const int nb = subs[i], bps = i == 1 ? 0 : bps0;
-        if ((i == 1 && bps0 == 0) || (nb > 0 && (!c->tune_fused || (nb > count && subs[i - 1] >= count)))) continue;
-        if ((rc = ik_set_tuning(c, IK_TUNE_IO_BATCHES, std::min(nb, count))) ||
+    int bi = io0, bm = map0, bk = bps0, rc = IK_OK;
+    bool fused_ok = c->tune_fused != 0, mapped_ok = true;
+    std::vector<std::array<int, 3>> tried;
+    for (const Cand& cd : cands) {
+        if (rc != IK_OK) break;
+        const int nb = std::min(cd.nb, count), bps = cd.lanes_default ? 0 : bps0;
+        if (cd.lanes_default && bps0 == 0) continue;
+        if (nb > 0 && (!fused_ok || (cd.mapped && !mapped_ok))) continue;
+        const std::array<int, 3> key{nb, cd.mapped, bps};
+        if (std::find(tried.begin(), tried.end(), key) != tried.end()) continue;
+        tried.push_back(key);
+        if ((rc = ik_set_tuning(c, IK_TUNE_IO_BATCHES, nb)) || (rc = ik_set_tuning(c, IK_TUNE_IO_MAPPED, cd.mapped)) ||
             (rc = ik_set_tuning(c, IK_TUNE_BLOCKS_PER_SM, bps)) ||
             (rc = ik_compute_batch_io(c, slots, count, precision, fields, n, pos, vel, mass, diam, out)) ||
             (rc = ik_compute_batch_io(c, slots, count, precision, fields, n, pos, vel, mass, diam, out)) ||
             (rc = ik_synchronize(c)))
             break;
-        if (nb > 0 && !c->io_fused) break; // the batch cannot run fused: the lanes ran
+        if (nb > 0 && !c->io_fused) { fused_ok = false; continue; } // the batch cannot run fused
+        if (cd.mapped && !c->io_mapped) { mapped_ok = false; continue; } // an array has no device view
         if (cudaEventRecord(e0, c->stream) != cudaSuccess) { rc = fail(IK_ERR_CUDA, "event record failed"); break; }
         for (int t = 0; t < reps && rc == IK_OK; ++t)
             rc = ik_compute_batch_io(c, slots, count, precision, fields, n, pos, vel, mass, diam, out);
@@ -2455,12 +2567,13 @@ int ik_autotune_batch_io(ik_ctx* c, const int* slots, int count, int precision, 
             cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) { rc = fail(IK_ERR_CUDA, "event timing failed"); break; }
         if ((rc = ik_synchronize(c))) break;
         ms /= (float)reps;
-        if (ms < best) { best = ms; bi = std::min(nb, count); bk = bps; }
+        if (ms < best) { best = ms; bi = nb; bm = cd.mapped; bk = bps; }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
     if (int r = ik_set_tuning(c, IK_TUNE_IO_BATCHES, bi)) return r;
+    if (int r = ik_set_tuning(c, IK_TUNE_IO_MAPPED, bm)) return r;
     if (int r = ik_set_tuning(c, IK_TUNE_BLOCKS_PER_SM, bk)) return r;
     if (best_io_batches) *best_io_batches = bi;
     if (best_ms) *best_ms = best;
@@ -2533,6 +2646,7 @@ int ik_get_tuning(ik_ctx* c, int param, int* value)
     case IK_TUNE_HALO_CAP: *value = c->halo_cap; return IK_OK;
     case IK_TUNE_FUSED_BATCH: *value = c->tune_fused; return IK_OK;
     case IK_TUNE_IO_BATCHES: *value = c->tune_io_batches; return IK_OK;
+    case IK_TUNE_IO_MAPPED: *value = c->tune_io_mapped; return IK_OK;
     default: return fail(IK_ERR_ARG, "unknown tuning parameter %d", param);
     }
 }

@@ -6,6 +6,7 @@
 // ParticleSystem::init_neighbour_search (ParticleSystem.cc:13).
 #include "ik_common.cuh"
 #include "ik_kernels.h"
+#include <algorithm>
 
 // ---------------------------------------------------------------------------
 // 1. cell id + rank within the cell (atomic, order fixed later by k_cell_sort)
@@ -403,6 +404,42 @@ __global__ void k_validate(const double* __restrict__ pos, const double* __restr
     bool ok = (x & EXP) != EXP && (y & EXP) != EXP && (z & EXP) != EXP && (d & EXP) != EXP && d > 0 &&
               (dim == 3 || (z & ABS) == 0);
     if (!ok) atomicOr(status, IK_ST_BAD_INPUT);
+}
+
+// Host copies of a batch as one kernel (the copies of many small frames without a copy
+// node each): thread w copies word w of the concatenation, its copy found by a binary
+// search of the offsets, and applies the copy's checks (the tests of k_validate on the
+// IEEE-754 bits).
+__global__ void k_io_copy(const IkIoCopy* __restrict__ d, int n, long long total, int* __restrict__ status)
+{
+    const long long EXP = 0x7ff0000000000000LL, ABS = 0x7fffffffffffffffLL;
+    bool ok = true;
+    for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < total;
+         w += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(&d[mid].off) <= w) lo = mid;
+            else hi = mid - 1;
+        }
+        const long long k = w - __ldg(&d[lo].off);
+        const long long v = d[lo].src[k];
+        d[lo].dst[k] = v;
+        const int check = __ldg(&d[lo].check);
+        if (check == 1) ok = ok && (v & EXP) != EXP && (__ldg(&d[lo].dim) == 3 || k % 3 != 2 || (v & ABS) == 0);
+        else if (check == 2) ok = ok && (v & EXP) != EXP && v > 0;
+    }
+    if (!ok) atomicOr(status, IK_ST_BAD_INPUT);
+}
+
+cudaError_t launch_io_copy(const IkIoCopy* d, int n, long long total, int* status, int sm_count, cudaStream_t st)
+{
+    if (n <= 0 || total <= 0) return cudaSuccess;
+    const int T = 256;
+    const long long want = (total + T - 1) / T;
+    const int blocks = (int)std::min<long long>(want, (long long)sm_count * 8);
+    k_io_copy<<<blocks, T, 0, st>>>(d, n, total, status);
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------

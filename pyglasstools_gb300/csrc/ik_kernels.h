@@ -40,6 +40,20 @@ cudaError_t launch_neigh(bool fill, IkGeom g, int n, double r2cut, const int* so
 __global__ void k_point_query(IkGeom g, int n, const double* pos, double px, double py, double pz,
                               double r2cut, unsigned char* flag);
 __global__ void k_validate(const double* pos, const double* diam, int n, int dim, int* status);
+// One copy of a host-mapped batch copy (launch_io_copy): `words` 8-byte words from src to
+// dst, the copy's first word at `off` in the launch's concatenation; check: 0 none,
+// 1 positions (n x 3: finite, z == 0 in 2D), 2 diameters (finite, > 0) -- k_validate's
+// tests, made while copying.
+struct IkIoCopy {
+    const long long* src;
+    long long* dst;
+    long long words, off;
+    int check, dim;
+};
+// Every copy of `d` (n descriptors, `total` words, none empty, contiguous offsets) in one
+// kernel whose threads read and write through the device's view of page-locked host
+// memory; failed checks set IK_ST_BAD_INPUT in status.
+cudaError_t launch_io_copy(const IkIoCopy* d, int n, long long total, int* status, int sm_count, cudaStream_t st);
 __global__ void k_eval_pair(IkPot pot, int m, const double* rij, const double* di, const double* dj,
                             double* f, double* en);
 

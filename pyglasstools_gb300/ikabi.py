@@ -23,7 +23,7 @@ QUAD = {"fixedpoint": 0, "adaptive": 1, "exact": 2, "mlp": 3, "clipped": 4}
 PREC = {"fp64": 0, "fp32": 1}
 FIELD_VIRIAL, FIELD_KINETIC, FIELD_ELASTIC = 1, 2, 4
 FLAG_TIMING, FLAG_LANE_KAHAN, FLAG_CSR_BONDS = 1, 2, 4
-TUNE = {"bin_points": 1, "blocks_per_sm": 2, "halo_cap": 3, "fused_batch": 4, "io_batches": 5}
+TUNE = {"bin_points": 1, "blocks_per_sm": 2, "halo_cap": 3, "fused_batch": 4, "io_batches": 5, "io_mapped": 6}
 POT = {"poly12": 0, "lj": 1, "fslj": 2, "poly10": 3, "poly106": 4, "poly18": 5, "polylj": 6,
        "polyyukawa": 7}
 
@@ -428,12 +428,13 @@ class IKContext:
     def autotune_batch_io(self, slots, frames, outs, precision="fp32", fields=FIELD_VIRIAL | FIELD_KINETIC, reps=3):
         """Time compute_batch_io (arguments as there) under each schedule of its copies --
         per frame on the lanes, or fused sub-batches -- keep the fastest; returns
-        {"io_batches", "blocks_per_sm", "ms_per_batch"} (io_batches 0: the lanes)."""
+        {"io_batches", "io_mapped", "blocks_per_sm", "ms_per_batch"} (io_batches 0: the lanes)."""
         sl, cnt, nn, pos, vel, mass, diam, out = self._io_call_args(slots, frames, outs)
         nb, ms = C.c_int(), C.c_float()
         check(lib().ik_autotune_batch_io(self._h, sl, cnt, PREC[precision], fields, nn, pos, vel, mass, diam, out,
                                          reps, C.byref(nb), C.byref(ms)))
-        return {"io_batches": nb.value, "blocks_per_sm": self.get_tuning("blocks_per_sm"), "ms_per_batch": ms.value}
+        return {"io_batches": nb.value, "io_mapped": self.get_tuning("io_mapped"),
+                "blocks_per_sm": self.get_tuning("blocks_per_sm"), "ms_per_batch": ms.value}
 
     def compute_thermo(self, slot=0):
         """Global observables of a slot's frame: dict of potentialenergy (float),

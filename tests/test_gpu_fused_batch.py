@@ -183,13 +183,15 @@ def test_fused_replay_overflowing_bond_capacity_is_rerun():
     c.close()
 
 
-@pytest.mark.parametrize("io_batches", [1, 3, 6])
-def test_fused_host_io_sub_batches_equal_per_frame(io_batches):
+@pytest.mark.parametrize("io_batches,mapped", [(1, 0), (3, 0), (6, 0), (1, 1), (3, 1)])
+def test_fused_host_io_sub_batches_equal_per_frame(io_batches, mapped):
     """ik_compute_batch_io of an eligible batch runs as fused sub-batches whose host copies
-    overlap the other sub-batches' computation.  Uneven frames with their own boxes and
-    grids, one without velocities: the host fields equal the per-frame path bit for bit on
-    the first call (plain path), on replays and after new contents, and a replay launches
-    one validation per frame and at most eight kernels per sub-batch."""
+    overlap the other sub-batches' computation (copy engines), or with each sub-batch's
+    copies as one kernel over the host arrays' device view (host-mapped).  Uneven frames
+    with their own boxes and grids, one without velocities: the host fields equal the
+    per-frame path bit for bit on the first call (plain path), on replays and after new
+    contents, and a replay launches at most one validation per frame and eight kernels per
+    sub-batch."""
     torch = pytest.importorskip("torch")
     from conftest import uniq
     from pyglasstools_gb300 import ikabi as ik, synth
@@ -202,7 +204,8 @@ def test_fused_host_io_sub_batches_equal_per_frame(io_batches):
     c = _ctx(ik)
     _setup(ik, c, 2, fr, grids, no_vel=(3,))
     c.set_tuning("io_batches", io_batches)
-    assert c.get_tuning("io_batches") == io_batches
+    c.set_tuning("io_mapped", mapped)
+    assert c.get_tuning("io_batches") == io_batches and c.get_tuning("io_mapped") == mapped
     slots = list(range(len(fr)))
 
     def want_for(frames):
@@ -256,7 +259,8 @@ def test_host_io_autotuner_keeps_a_candidate_and_the_fields():
     _setup(ik, c, 2, fr, grids)
     slots = list(range(len(fr)))
     best = c.autotune_batch_io(slots, host, outs, reps=1)
-    assert best["io_batches"] in (0, 2, 4) and best["ms_per_batch"] > 0
+    assert best["io_batches"] in (0, 1, 2, 4) and best["io_mapped"] in (0, 1) and best["ms_per_batch"] > 0
+    assert best["io_batches"] > 0 or best["io_mapped"] == 0
     assert c.get_tuning("io_batches") == best["io_batches"]
     want = [[uniq(x) for x in _alone(ik, 2, f, g)[0]] for f, g in zip(fr, grids)]
     for rep in range(2):
@@ -266,4 +270,43 @@ def test_host_io_autotuner_keeps_a_candidate_and_the_fields():
         for k in slots:
             np.testing.assert_array_equal(outs[k][0], want[k][0])
             np.testing.assert_array_equal(outs[k][1], want[k][1])
+    c.close()
+
+
+def test_host_mapped_copies_validate_the_frames():
+    """Host-mapped copies check each frame as they copy it: a replay whose new contents
+    hold a non-finite position, or a 2D position with z != 0, is reported as IK_ERR_ARG by
+    synchronize; the context stays usable, and a replay of valid contents gives the
+    per-frame fields."""
+    torch = pytest.importorskip("torch")
+    from conftest import uniq
+    from pyglasstools_gb300 import ikabi as ik
+    fr, grids = _uneven(2, [1500, 2600], 1900)
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    host = [(pin(f.pos), pin(f.diam), pin(f.vel), pin(f.mass)) for f in fr]
+    outs = [(pin(np.zeros((len(g), 3))), pin(np.zeros((len(g), 3))), None) for g in grids]
+    c = _ctx(ik)
+    _setup(ik, c, 2, fr, grids)
+    c.set_tuning("io_batches", 1)
+    c.set_tuning("io_mapped", 1)
+    slots = [0, 1]
+    for _ in range(2):  # plain path + recording, then a replay
+        c.compute_batch_io(slots, host, outs)
+        c.synchronize()
+    for k, bad in ((7, np.nan), (11, 0.25)):
+        keep = host[1][0][k].copy()
+        if np.isnan(bad):
+            host[1][0][k, 0] = bad
+        else:
+            host[1][0][k, 2] = bad  # z of a 2D frame
+        c.compute_batch_io(slots, host, outs)
+        with pytest.raises(ik.IKError, match="IK_ERR_ARG"):
+            c.synchronize()
+        host[1][0][k] = keep
+    c.compute_batch_io(slots, host, outs)
+    c.synchronize()
+    for k in slots:
+        want = [uniq(x) for x in _alone(ik, 2, fr[k], grids[k])[0]]
+        np.testing.assert_array_equal(outs[k][0], want[0])
+        np.testing.assert_array_equal(outs[k][1], want[1])
     c.close()
