@@ -221,7 +221,10 @@ int ik_get_stream(ik_ctx* ctx, void** stream);
  * fields are downloaded as soon as it is done, so that the copies of the other
  * sub-batches overlap its computation.  The first call (and any call after a change of slots, sizes, pointers or
  * settings) runs the plain path and records the graph; later calls replay it, reading the
- * host inputs' current contents.  Outputs are complete after ik_synchronize (which copies
+ * host inputs' current contents.  The graph holds the host arrays' addresses (page-locked
+ * status is checked when they change): an array freed and replaced by another at the same
+ * address must be page-locked too, as the replay copies from and to it (host-mapped
+ * copies: through the device's view of it).  Outputs are complete after ik_synchronize (which copies
  * them again if a capacity growth re-ran a frame).  Slots must be distinct.  Elastic
  * fields use the displacements of ik_upload_displacement. */
 int ik_compute_batch_io(ik_ctx* ctx, const int* slots, int count, int precision, int fields,
