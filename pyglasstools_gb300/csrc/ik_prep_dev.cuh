@@ -241,19 +241,18 @@ __device__ __forceinline__ int ik_bonds32_particle(const IkGeom& g, const IkPot&
     // 1e-4 margin); measure = the rest for a candidate that passed (re-measure, the exact
     // decision, the force, the record).  (sx, sy, sz): the stencil's wrap shifts, used by
     // the FP64 re-decision.
-    auto screen_rec = [&](const IkPRec& o, int q, float ox, float oy, float oz) { // o = prec[q]
+    auto screen_rec = [&](const IkPRec& o, float dj, float ox, float oy, float oz) { // o = prec[q], dj = diam32[q]
         float bx = ox + (o.x - me.x), by = oy + (o.y - me.y), bz = DIM == 3 ? oz + (o.z - me.z) : 0.f;
         if (allx) bx -= L0 * rintf(bx / L0);
         if (ally) by -= L1 * rintf(by / L1);
         if (allz) bz -= L2 * rintf(bz / L2);
         const float r2 = bx * bx + by * by + bz * bz;
         if (!(r2 < mr2 * screen_f)) return false;
-        const float dj = diam32[q];
         const float sig = 0.5f * (di + dj) * (1.f - eps * fabsf(di - dj));
         const float s2 = sig * sig;
         return r2 < rc2 * s2 * screen_f;
     };
-    auto screen = [&](int q, float ox, float oy, float oz) { return screen_rec(prec[q], q, ox, oy, oz); };
+    auto screen = [&](int q, float ox, float oy, float oz) { return screen_rec(prec[q], diam32[q], ox, oy, oz); };
     auto measure = [&](int q, float ox, float olx, float oy, float oly, float oz, float olz, int sx, int sy, int sz) {
         const IkPRec o = prec[q];
         const float dj = diam32[q];
@@ -364,18 +363,20 @@ __device__ __forceinline__ int ik_bonds32_particle(const IkGeom& g, const IkPot&
                     // inner cell boundaries of the run (past its end where it has fewer cells)
                     const int b1 = xb >= xa + 1 ? rs[xa + 1] : qe, b2 = xb >= xa + 2 ? rs[xa + 2] : qe;
                     const float kaf = (float)ka;
-                    // the next candidate's record is loaded before the current one is
-                    // screened, so that its latency overlaps the test (fused preparation
-                    // 19.6 -> 18.8 us per frame)
+                    // the next candidate's record and diameter are loaded before the
+                    // current one is screened, so that their latency overlaps the test
+                    // (fused preparation 19.6 -> 18.4 us per frame)
                     IkPRec nxt = qa < qe ? prec[qa] : me;
+                    float ndj = qa < qe ? diam32[qa] : di;
                     for (int q = qa; q < qe; ++q) {
                         const IkPRec cur = nxt;
-                        if (q + 1 < qe) nxt = prec[q + 1];
+                        const float cdj = ndj;
+                        if (q + 1 < qe) { nxt = prec[q + 1]; ndj = diam32[q + 1]; }
                         if (q == p) continue;
                         // the candidate cell's x offset (-1, 0 or 1: exactly the float the
                         // cell-by-cell walk converts)
                         const float kxf = kaf + (q >= b1 ? 1.f : 0.f) + (q >= b2 ? 1.f : 0.f);
-                        if (screen_rec(cur, q, kxf * g.cwhi[0], oy, oz)) {
+                        if (screen_rec(cur, cdj, kxf * g.cwhi[0], oy, oz)) {
                             qidx[ns * qstride] = q;
                             qcode[ns * qstride] = (unsigned char)(row_code + (int)kxf);
                             if (++ns == IK_BOND_QUEUE) drain();
