@@ -1338,10 +1338,10 @@ bool io_build_mapped(ik_ctx* c, const int* slots, const std::vector<IoFrame>& fr
 // The launches and copies of a fused ik_compute_batch_io, to be captured (fused_build of
 // every sub-batch and io_events done).  Lane 0 uploads the frames in batch order (copies
 // only: a kernel there would wait for the SMs that a persistent gather holds, and the next
-// uploads behind it); lanes 1 and 2 take the sub-batches in turn, each the validation of its
-// frames and a fused batch, started once its frames are on the device (the preparation of
-// one overlaps the end of the previous gather); lane 3 downloads a sub-batch's fields as
-// soon as it is computed.  The copies of the other sub-batches overlap every computation
+// uploads behind it); lanes 1 and 2 take the sub-batches in turn, each a fused batch
+// (whose binning and packing validate the frames) started once its frames are on the
+// device (the preparation of one overlaps the end of the previous gather); lane 3
+// downloads a sub-batch's fields as soon as it is computed.  The copies of the other sub-batches overlap every computation
 // but the first upload and the last download.
 int fused_io_enqueue(ik_ctx* c, const int* slots, const std::vector<IoFrame>& fr, const std::vector<int>& cut,
                      int fields, bool mapped)
@@ -1380,15 +1380,6 @@ int fused_io_enqueue(ik_ctx* c, const int* slots, const std::vector<IoFrame>& fr
         CK(cudaEventRecord(c->io_ev[(size_t)(2 * b)], up));
         cudaStream_t cs = c->lanes[1 + (b & 1)].st;
         CK(cudaStreamWaitEvent(cs, c->io_ev[(size_t)(2 * b)], 0));
-        for (int k = cut[(size_t)b]; k < cut[(size_t)b + 1]; ++k) {
-            Slot& s = c->slots[(size_t)slots[k]];
-            const int n = (int)s.n;
-            if (n == 0) continue;
-            k_validate<<<(n + 255) / 256, 256, 0, cs>>>(s.pos.as<double>(), s.diam.as<double>(), n, c->dim,
-                                                        c->status.as<int>());
-            CK(cudaGetLastError());
-            c->launches += 1;
-        }
         if (int r = fused_enqueue(c, c->fused_io[(size_t)b], fields, cs)) return r;
         CK(cudaEventRecord(c->io_ev[(size_t)(2 * b + 1)], cs));
         CK(cudaStreamWaitEvent(dn, c->io_ev[(size_t)(2 * b + 1)], 0));

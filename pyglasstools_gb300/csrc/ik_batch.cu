@@ -8,10 +8,11 @@
 //
 // Launch sequence of a fused batch (all on one stream, recorded once as a CUDA graph):
 //   k_bin32_batch       cell of every particle, its rank in the cell, double-float
-//                       cell-relative position; zeroes the slots' counters
+//                       cell-relative position; zeroes the slots' counters; checks the
+//                       positions (finite, z == 0 in 2D)
 //   launch_scan         cell starts over the batch's concatenated cell counts
 //   k_scatter           particle ids to cell order
-//   k_sort_pack32_batch per cell: sorted ids, packed records
+//   k_sort_pack32_batch per cell: sorted ids, packed records; checks the diameters
 //   k_bonds32t_batch    per particle: force-active bonds (records at a fixed stride)
 //   k_gather32 (BATCH)  per work item of every frame: the stress field
 //   k_pairs_to_f64_batch double-float sums -> each slot's FP64 fields
@@ -50,9 +51,26 @@ __device__ __forceinline__ int ik_batch_slot64(const long long* __restrict__ off
     return lo;
 }
 
+// The tests of k_validate on the IEEE-754 bits: finite, and for a 2D position z == 0
+// (positions), finite and > 0 (diameters).
+__device__ __forceinline__ bool ik_pos_ok(const double* p, int dim)
+{
+    const long long EXP = 0x7ff0000000000000LL, ABS = 0x7fffffffffffffffLL;
+    const long long x = __double_as_longlong(p[0]), y = __double_as_longlong(p[1]), z = __double_as_longlong(p[2]);
+    return (x & EXP) != EXP && (y & EXP) != EXP && (z & EXP) != EXP && (dim == 3 || (z & ABS) == 0);
+}
+__device__ __forceinline__ bool ik_diam_ok(double d)
+{
+    const long long v = __double_as_longlong(d);
+    return (v & 0x7ff0000000000000LL) != 0x7ff0000000000000LL && v > 0;
+}
+
+// Also checks every position (as k_validate does at an upload): a batch whose frames were
+// copied in by its own graph is validated here, without a launch per frame.
 __global__ void k_bin32_batch(const IkBatchSlot* __restrict__ S, const int* __restrict__ p_offs, int nslots,
                               int ptot, int* __restrict__ cell_of, int* __restrict__ rank,
-                              int* __restrict__ cell_count, float4* __restrict__ relhi, float4* __restrict__ rello)
+                              int* __restrict__ cell_count, float4* __restrict__ relhi, float4* __restrict__ rello,
+                              int* __restrict__ status)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     // the slots' counters (bonds, pairs, triples, surrogate records and fallbacks) start at
@@ -62,7 +80,9 @@ __global__ void k_bin32_batch(const IkBatchSlot* __restrict__ S, const int* __re
     const int s = ik_batch_slot(p_offs, nslots, i);
     const IkBatchSlot& sl = S[s];
     float4 rh, rl;
-    const int c = sl.geo.c_off + ik_bin32_one(sl.geo.g, sl.pos + 3 * (size_t)(i - sl.geo.p_off), rh, rl);
+    const double* pi = sl.pos + 3 * (size_t)(i - sl.geo.p_off);
+    if (!ik_pos_ok(pi, sl.geo.g.dim)) atomicOr(status, IK_ST_BAD_INPUT);
+    const int c = sl.geo.c_off + ik_bin32_one(sl.geo.g, pi, rh, rl);
     cell_of[i] = c;
     rank[i] = atomicAdd(&cell_count[c], 1);
     relhi[i] = rh;
@@ -71,7 +91,7 @@ __global__ void k_bin32_batch(const IkBatchSlot* __restrict__ S, const int* __re
 
 // As k_cell_sort_pack32 over the batch's cells: a CTA sorts its 128 cells, then packs
 // their particles (cell_of holds batch cell indices; a particle's frame is found by a
-// search of the particle offsets).
+// search of the particle offsets), checking every diameter as k_validate does.
 __global__ void __launch_bounds__(128) k_sort_pack32_batch(const IkBatchSlot* __restrict__ S,
                                                            const int* __restrict__ p_offs, int nslots, int ctot,
                                                            const int* __restrict__ cell_start,
@@ -80,7 +100,7 @@ __global__ void __launch_bounds__(128) k_sort_pack32_batch(const IkBatchSlot* __
                                                            const float4* __restrict__ rello,
                                                            IkPRec* __restrict__ prec, float4* __restrict__ plo,
                                                            IkB64* __restrict__ pos64, float4* __restrict__ kin,
-                                                           float* __restrict__ diam32)
+                                                           float* __restrict__ diam32, int* __restrict__ status)
 {
     const int c0 = blockIdx.x * blockDim.x, c = c0 + threadIdx.x;
     if (c < ctot) ik_sort_cell(cell_start[c], cell_start[c + 1], sorted);
@@ -89,6 +109,7 @@ __global__ void __launch_bounds__(128) k_sort_pack32_batch(const IkBatchSlot* __
     for (int p = cell_start[c0] + threadIdx.x; p < pe; p += blockDim.x) {
         const int ig = sorted[p];
         const IkBatchSlot& sl = S[ik_batch_slot(p_offs, nslots, ig)];
+        if (!ik_diam_ok(sl.diam[ig - sl.geo.p_off])) atomicOr(status, IK_ST_BAD_INPUT);
         ik_pack_one(sl.geo.g.dim, cell_of[ig] - sl.geo.c_off, p, ig, sl.geo.p_off, relhi, rello, sl.pos, sl.vel,
                     sl.mass, sl.diam, prec, plo, pos64, kin, diam32);
     }
@@ -158,7 +179,7 @@ cudaError_t launch_batch_prepare(const IkBatchLaunch& b, int dim, const IkPot& p
     const int T = 256;
     const int bin_threads = std::max(b.ptot, 5 * b.nslots);
     k_bin32_batch<<<(bin_threads + T - 1) / T, T, 0, st>>>(b.slots, b.p_offs, b.nslots, b.ptot, b.cell_of, b.rank,
-                                                           b.cell_count, b.relhi, b.rello);
+                                                           b.cell_count, b.relhi, b.rello, b.status);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if ((e = launch_scan(b.cell_count, b.ctot, b.cell_start, b.bsum, st)) != cudaSuccess) return e;
@@ -169,7 +190,7 @@ cudaError_t launch_batch_prepare(const IkBatchLaunch& b, int dim, const IkPot& p
     if (b.ctot > 0) {
         k_sort_pack32_batch<<<(b.ctot + 127) / 128, 128, 0, st>>>(b.slots, b.p_offs, b.nslots, b.ctot, b.cell_start,
                                                                   b.sorted, b.cell_of, b.relhi, b.rello, b.prec, b.plo,
-                                                                  b.pos64, b.kin, b.diam32);
+                                                                  b.pos64, b.kin, b.diam32, b.status);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     if (b.ptot > 0) {

@@ -273,11 +273,12 @@ def test_host_io_autotuner_keeps_a_candidate_and_the_fields():
     c.close()
 
 
-def test_host_mapped_copies_validate_the_frames():
-    """Host-mapped copies check each frame as they copy it: a replay whose new contents
-    hold a non-finite position, or a 2D position with z != 0, is reported as IK_ERR_ARG by
-    synchronize; the context stays usable, and a replay of valid contents gives the
-    per-frame fields."""
+@pytest.mark.parametrize("mapped", [0, 1])
+def test_host_io_sub_batches_validate_the_frames(mapped):
+    """Fused host-I/O sub-batches check each frame (the fused binning and packing; host-mapped
+    copies also as they copy): a replay whose new contents hold a non-finite position, or a
+    2D position with z != 0, is reported as IK_ERR_ARG by synchronize; the context stays
+    usable, and a replay of valid contents gives the per-frame fields."""
     torch = pytest.importorskip("torch")
     from conftest import uniq
     from pyglasstools_gb300 import ikabi as ik
@@ -288,7 +289,7 @@ def test_host_mapped_copies_validate_the_frames():
     c = _ctx(ik)
     _setup(ik, c, 2, fr, grids)
     c.set_tuning("io_batches", 1)
-    c.set_tuning("io_mapped", 1)
+    c.set_tuning("io_mapped", mapped)
     slots = [0, 1]
     for _ in range(2):  # plain path + recording, then a replay
         c.compute_batch_io(slots, host, outs)
