@@ -558,7 +558,7 @@ int build_cells(ik_ctx* c, Slot& s, const IkGeom& g, cudaStream_t st, DevBuf& ce
             ENS(*relhi, sizeof(float4) * std::max(n, 1));
             ENS(*rello, sizeof(float4) * std::max(n, 1));
             CK(launch_bin32(s.pos.as<double>(), n, g, cell_of.as<int>(), rank.as<int>(), count.as<int>(),
-                            relhi->as<float4>(), rello->as<float4>(), st));
+                            relhi->as<float4>(), rello->as<float4>(), c->status.as<int>(), st));
         } else {
             k_bin<<<(n + 255) / 256, 256, 0, st>>>(s.pos.as<double>(), n, g, cell_of.as<int>(), rank.as<int>(),
                                                    count.as<int>(), c->status.as<int>());
@@ -661,10 +661,12 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
         CK(cudaMemcpyAsync(s.diam.p, io.diam, sizeof(double) * n, cudaMemcpyHostToDevice, L.st));
         if (io.vel) CK(cudaMemcpyAsync(s.vel.p, io.vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, L.st));
         if (io.mass) CK(cudaMemcpyAsync(s.mass.p, io.mass, sizeof(double) * n, cudaMemcpyHostToDevice, L.st));
-        k_validate<<<(n + 255) / 256, 256, 0, L.st>>>(s.pos.as<double>(), s.diam.as<double>(), n, c->dim,
-                                                      c->status.as<int>());
-        CK(cudaGetLastError());
-        c->launches += 1;
+        if (prec != IK_PREC_FP32) { // the FP32 path's binning and packing make these tests themselves
+            k_validate<<<(n + 255) / 256, 256, 0, L.st>>>(s.pos.as<double>(), s.diam.as<double>(), n, c->dim,
+                                                          c->status.as<int>());
+            CK(cudaGetLastError());
+            c->launches += 1;
+        }
     }
     bool timing = (c->flags & IK_FLAG_TIMING) != 0 && !c->capturing;
     if (timing) CK(cudaEventRecord(c->ev[0], L.st));
@@ -699,7 +701,7 @@ int enqueue(ik_ctx* c, int slot, int prec, int fields)
                               L.rello.as<float4>(), s.pos.as<double>(), s.has_vel ? s.vel.as<double>() : nullptr,
                               s.has_mass ? s.mass.as<double>() : nullptr, s.diam.as<double>(), L.prec.as<IkPRec>(),
                               L.plo.as<float4>(), L.pos64.as<IkB64>(), L.kin.as<float4>(), L.diam32.as<float>(),
-                              L.st));
+                              c->status.as<int>(), L.st));
         c->launches += g.ncell > 0 ? 1 : 0;
         if (timing) CK(cudaEventRecord(c->ev[1], L.st));
         // bond records at a fixed stride of maxb per particle; compacted to CSR only
@@ -1868,7 +1870,10 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
                        c->batch_config_version == c->config_version && c->batch_alloc_epoch == g_alloc_epoch.load() &&
                        !(c->flags & IK_FLAG_TIMING);
     if (!reuse) {
-        // first run of this batch: plain launches (sizes every buffer, checks capacities)
+        // first run of this batch: plain launches (sizes every buffer, checks capacities);
+        // frames take the lanes from lane 0 here and in the capture, so that the capture
+        // finds every buffer it uses sized (an allocation there leaves the graph unused)
+        c->next_lane = 0;
         c->in_batch = true;
         for (int k = 0; k < count; ++k) {
             c->pending.push_back({slots[k], precision, fields});
@@ -1891,6 +1896,7 @@ int ik_compute_batch(ik_ctx* c, const int* slots, int count, int precision, int 
         c->capturing = true;
         c->captured_lanes = 0;
         int rr = IK_OK;
+        c->next_lane = 0;
         c->in_batch = true;
         if (fused) rr = fused_enqueue(c, c->fused, fields, c->stream);
         for (int k = 0; k < count && rr == IK_OK && !fused; ++k) rr = prepare_enqueue(c, slots[k], precision, fields);
@@ -2039,6 +2045,7 @@ int ik_compute_batch_io(ik_ctx* c, const int* slots, int count, int precision, i
             const IoFrame& f = fr[(size_t)k];
             if (int r = ik_upload_frame(c, slots[k], n[k], f.pos, f.vel, f.mass, f.diam)) return r;
         }
+        c->next_lane = 0; // the same lanes here and in the capture (see ik_compute_batch)
         c->in_batch = true;
         for (int k = 0; k < count; ++k) {
             c->pending.push_back({slots[k], precision, fields});
@@ -2084,6 +2091,7 @@ int ik_compute_batch_io(ik_ctx* c, const int* slots, int count, int precision, i
         c->capturing = true;
         c->captured_lanes = 0;
         int rr = IK_OK;
+        c->next_lane = 0;
         c->in_batch = true;
         if (fused) rr = fused_io_enqueue(c, slots, fr, cut, fields, mapped);
         for (int k = 0; k < count && rr == IK_OK && !fused; ++k) {

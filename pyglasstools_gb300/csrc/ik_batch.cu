@@ -51,20 +51,6 @@ __device__ __forceinline__ int ik_batch_slot64(const long long* __restrict__ off
     return lo;
 }
 
-// The tests of k_validate on the IEEE-754 bits: finite, and for a 2D position z == 0
-// (positions), finite and > 0 (diameters).
-__device__ __forceinline__ bool ik_pos_ok(const double* p, int dim)
-{
-    const long long EXP = 0x7ff0000000000000LL, ABS = 0x7fffffffffffffffLL;
-    const long long x = __double_as_longlong(p[0]), y = __double_as_longlong(p[1]), z = __double_as_longlong(p[2]);
-    return (x & EXP) != EXP && (y & EXP) != EXP && (z & EXP) != EXP && (dim == 3 || (z & ABS) == 0);
-}
-__device__ __forceinline__ bool ik_diam_ok(double d)
-{
-    const long long v = __double_as_longlong(d);
-    return (v & 0x7ff0000000000000LL) != 0x7ff0000000000000LL && v > 0;
-}
-
 // Also checks every position (as k_validate does at an upload): a batch whose frames were
 // copied in by its own graph is validated here, without a launch per frame.
 __global__ void k_bin32_batch(const IkBatchSlot* __restrict__ S, const int* __restrict__ p_offs, int nslots,

@@ -17,11 +17,12 @@
 // carries ~48 bits).  One thread per particle, original order.
 __global__ void k_bin32(const double* __restrict__ pos, int n, IkGeom g, int* __restrict__ cell_of,
                         int* __restrict__ rank, int* __restrict__ cell_count, float4* __restrict__ relhi,
-                        float4* __restrict__ rello)
+                        float4* __restrict__ rello, int* __restrict__ status)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 rh, rl;
+    if (!ik_pos_ok(pos + 3 * (size_t)i, g.dim)) atomicOr(status, IK_ST_BAD_INPUT); // k_validate's test
     const int c = ik_bin32_one(g, pos + 3 * (size_t)i, rh, rl);
     cell_of[i] = c;
     rank[i] = atomicAdd(&cell_count[c], 1);
@@ -159,10 +160,10 @@ cudaError_t launch_scan(const int* in, int n, int* out, int* bsum, cudaStream_t 
 }
 
 cudaError_t launch_bin32(const double* pos, int n, IkGeom g, int* cell_of, int* rank, int* cell_count, float4* relhi,
-                         float4* rello, cudaStream_t st)
+                         float4* rello, int* status, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
-    k_bin32<<<(n + 255) / 256, 256, 0, st>>>(pos, n, g, cell_of, rank, cell_count, relhi, rello);
+    k_bin32<<<(n + 255) / 256, 256, 0, st>>>(pos, n, g, cell_of, rank, cell_count, relhi, rello, status);
     return cudaGetLastError();
 }
 
@@ -179,23 +180,28 @@ __global__ void __launch_bounds__(128) k_cell_sort_pack32(IkGeom g, const int* _
                                                           const double* __restrict__ mass,
                                                           const double* __restrict__ diam, IkPRec* __restrict__ prec,
                                                           float4* __restrict__ plo, IkB64* __restrict__ pos64,
-                                                          float4* __restrict__ kin, float* __restrict__ diam32)
+                                                          float4* __restrict__ kin, float* __restrict__ diam32,
+                                                          int* __restrict__ status)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.ncell) return;
     const int s = cell_start[c], e = cell_start[c + 1];
     ik_sort_cell(s, e, sorted);
-    for (int p = s; p < e; ++p)
-        ik_pack_one(g.dim, c, p, sorted[p], 0, relhi, rello, pos, vel, mass, diam, prec, plo, pos64, kin, diam32);
+    for (int p = s; p < e; ++p) {
+        const int ig = sorted[p];
+        if (!ik_diam_ok(diam[ig])) atomicOr(status, IK_ST_BAD_INPUT); // k_validate's test
+        ik_pack_one(g.dim, c, p, ig, 0, relhi, rello, pos, vel, mass, diam, prec, plo, pos64, kin, diam32);
+    }
 }
 
 cudaError_t launch_sort_pack32(IkGeom g, const int* cell_start, int* sorted, const float4* relhi, const float4* rello,
                                const double* pos, const double* vel, const double* mass, const double* diam,
-                               IkPRec* prec, float4* plo, IkB64* pos64, float4* kin, float* diam32, cudaStream_t st)
+                               IkPRec* prec, float4* plo, IkB64* pos64, float4* kin, float* diam32, int* status,
+                               cudaStream_t st)
 {
     if (g.ncell <= 0) return cudaSuccess;
     k_cell_sort_pack32<<<(g.ncell + 127) / 128, 128, 0, st>>>(g, cell_start, sorted, relhi, rello, pos, vel, mass,
-                                                              diam, prec, plo, pos64, kin, diam32);
+                                                              diam, prec, plo, pos64, kin, diam32, status);
     return cudaGetLastError();
 }
 

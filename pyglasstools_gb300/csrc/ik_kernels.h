@@ -13,11 +13,14 @@ __global__ void k_cell_sort_pack(IkGeom g, const int* cell_start, int* sorted, c
                                  const double* vel, const double* mass, const double* diam,
                                  IkPRec* prec, float4* kin, float* diam32, int want_pack);
 // ---- tuned-path preparation (ik_bonds.cu) ---------------------------------
+// both also make k_validate's tests (positions in the binning, diameters in the packing),
+// reported as IK_ST_BAD_INPUT in status
 cudaError_t launch_bin32(const double* pos, int n, IkGeom g, int* cell_of, int* rank, int* cell_count, float4* relhi,
-                         float4* rello, cudaStream_t st);
+                         float4* rello, int* status, cudaStream_t st);
 cudaError_t launch_sort_pack32(IkGeom g, const int* cell_start, int* sorted, const float4* relhi, const float4* rello,
                                const double* pos, const double* vel, const double* mass, const double* diam,
-                               IkPRec* prec, float4* plo, IkB64* pos64, float4* kin, float* diam32, cudaStream_t st);
+                               IkPRec* prec, float4* plo, IkB64* pos64, float4* kin, float* diam32, int* status,
+                               cudaStream_t st);
 // nbond_total (may be null): += force-active directed bonds
 cudaError_t launch_bonds32(int dim, IkGeom g, IkPot pot, float kappa, int n, const IkPRec* prec,
                             const float* diam32, const int* cell_start, const float4* plo, const IkB64* pos64,

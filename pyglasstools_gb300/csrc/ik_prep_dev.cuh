@@ -29,6 +29,20 @@ __device__ __forceinline__ int ik_bin32_one(const IkGeom& g, const double* __res
     return (cc[2] * g.nc[1] + cc[1]) * g.nc[0] + cc[0];
 }
 
+// The tests of k_validate on the IEEE-754 bits: finite, and for a 2D position z == 0
+// (positions), finite and > 0 (diameters).
+__device__ __forceinline__ bool ik_pos_ok(const double* p, int dim)
+{
+    const long long EXP = 0x7ff0000000000000LL, ABS = 0x7fffffffffffffffLL;
+    const long long x = __double_as_longlong(p[0]), y = __double_as_longlong(p[1]), z = __double_as_longlong(p[2]);
+    return (x & EXP) != EXP && (y & EXP) != EXP && (z & EXP) != EXP && (dim == 3 || (z & ABS) == 0);
+}
+__device__ __forceinline__ bool ik_diam_ok(double d)
+{
+    const long long v = __double_as_longlong(d);
+    return (v & 0x7ff0000000000000LL) != 0x7ff0000000000000LL && v > 0;
+}
+
 // Sort the ids of one cell (insertion sort: cells hold a handful of particles; fixes the
 // order the atomic ranks left).
 __device__ __forceinline__ void ik_sort_cell(int s, int e, int* __restrict__ sorted)

@@ -273,12 +273,14 @@ def test_host_io_autotuner_keeps_a_candidate_and_the_fields():
     c.close()
 
 
-@pytest.mark.parametrize("mapped", [0, 1])
-def test_host_io_sub_batches_validate_the_frames(mapped):
-    """Fused host-I/O sub-batches check each frame (the fused binning and packing; host-mapped
-    copies also as they copy): a replay whose new contents hold a non-finite position, or a
-    2D position with z != 0, is reported as IK_ERR_ARG by synchronize; the context stays
-    usable, and a replay of valid contents gives the per-frame fields."""
+@pytest.mark.parametrize("io_batches,mapped", [(0, 0), (1, 0), (1, 1)])
+def test_host_io_sub_batches_validate_the_frames(io_batches, mapped):
+    """Host-I/O batches check each frame without a launch of their own -- the binning checks
+    the positions and the packing the diameters (lanes: per frame; fused sub-batches: over
+    the batch), host-mapped copies also as they copy: a replay whose new contents hold a
+    non-finite position, or a 2D position with z != 0, is reported as IK_ERR_ARG by
+    synchronize; the context stays usable, and a replay of valid contents gives the
+    per-frame fields."""
     torch = pytest.importorskip("torch")
     from conftest import uniq
     from pyglasstools_gb300 import ikabi as ik
@@ -288,7 +290,7 @@ def test_host_io_sub_batches_validate_the_frames(mapped):
     outs = [(pin(np.zeros((len(g), 3))), pin(np.zeros((len(g), 3))), None) for g in grids]
     c = _ctx(ik)
     _setup(ik, c, 2, fr, grids)
-    c.set_tuning("io_batches", 1)
+    c.set_tuning("io_batches", io_batches)
     c.set_tuning("io_mapped", mapped)
     slots = [0, 1]
     for _ in range(2):  # plain path + recording, then a replay
