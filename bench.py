@@ -442,7 +442,7 @@ def uneven_leg(args):
     launches = (c.launch_count() - l0) // (reps + 1)
     # end to end (host frames in, host fields out), the copies' schedule autotuned, and the
     # lanes beside it: wall time per batch, synchronised
-    io_best = c.autotune_batch_io(slots, host, outs, reps=2)
+    io_best = c.autotune_batch_io(slots, host, outs, reps=3)
 
     def e2e():  # ms per batch: the median of three timed runs (the host link's rate varies run to run)
         for _ in range(3):
@@ -661,7 +661,7 @@ def ours(args, wl, name):
     elif args.io_batches >= 0:
         ctx.set_tuning("io_batches", args.io_batches)
     else:
-        io_tuning = ctx.autotune_batch_io(io_slots, io_frames, io_outs, reps=2)
+        io_tuning = ctx.autotune_batch_io(io_slots, io_frames, io_outs, reps=4)
     nsub = ctx.get_tuning("io_batches") if not args.no_graph else 0
     io_mapped = ctx.get_tuning("io_mapped") if nsub else 0
     e2e_value = e2e_run()
